@@ -1,0 +1,219 @@
+"""ORACLE — test infrastructure only.
+
+ctypes front end of ``mc_oracle.cpp``: a CPU restatement of minicore's clustering hot path
+(``include/minicore/dist/applicator.h:1632-1915``, ``optim/kmeans.h:49-215``,
+``clustering/solve.h:98-285``, ``clustering/centroid.h:81-178,649-779``,
+``coreset/coreset.h:340-699``).  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg may import this package, and only as the checker; the
+product package ``minicore_gb300`` never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_LIB = os.path.join(_BUILD, "liboracle.so")
+_SRC = os.path.join(_HERE, "mc_oracle.cpp")
+
+L1, L2, SQRL2, JSM, JSD, MKL, HELLINGER = 0, 1, 2, 3, 4, 5, 6
+BFL, FL, LFKF, VX, LBK = 0, 1, 2, 3, 4
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (-ffp-contract=off keeps float arithmetic unfused)."""
+    os.makedirs(_BUILD, exist_ok=True)
+    if not force and os.path.exists(_LIB) and os.path.getmtime(_LIB) >= os.path.getmtime(_SRC):
+        return _LIB
+    tmp = _LIB + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           "-o", tmp, _SRC]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _LIB)
+    return _LIB
+
+
+class _Matrix(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("pad", ctypes.c_int32), ("n", ctypes.c_uint64),
+                ("d", ctypes.c_uint64), ("vals", ctypes.c_void_p), ("idx", ctypes.c_void_p),
+                ("indptr", ctypes.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        P, U64, D, I = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_int
+        U32 = ctypes.c_uint32
+        sig = {
+            "orc_uniform": (D, [U64, U64]),
+            "orc_uniforms": (None, [U64, U64, U64, P]),
+            "orc_det_sum": (D, [P, U64]),
+            "orc_det_draw": (U64, [P, U64, D]),
+            "orc_msr_dense": (D, [I, P, P, U64, D, D, D, D]),
+            "orc_msr_sparse": (D, [I, P, P, U64, P, P, U64, U64, D, D, D, D]),
+            "orc_assign": (I, [P, P, U32, I, D, P, P]),
+            "orc_kmeanspp": (I, [P, U32, I, D, P, P, P, P, P]),
+            "orc_hcluster": (I, [P, P, U32, I, D, P, D, U64, U64, P, P, P, P, P, P]),
+            "orc_sensitivity": (I, [U64, U64, U64, P, I, P, P, I, D, P]),
+            "orc_alias_build": (I, [U64, P, P, P]),
+            "orc_alias_draw": (U64, [U64, P, P, U64, U64]),
+            "orc_coreset_sample": (None, [U64, P, P, P, P, I, U64, U64, U64, I, P, P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(_lib, name)
+            f.restype = res
+            f.argtypes = args
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Matrix:
+    """Dense f32 (n x d) or CSR (f32 values, u32 indices, u64 indptr) view kept alive."""
+
+    def __init__(self, X):
+        import scipy.sparse as sp
+        if sp.issparse(X):
+            X = sp.csr_matrix(X)
+            X.sort_indices()
+            self.vals = np.ascontiguousarray(X.data, dtype=np.float32)
+            self.idx = np.ascontiguousarray(X.indices, dtype=np.uint32)
+            self.indptr = np.ascontiguousarray(X.indptr, dtype=np.uint64)
+            self.n, self.d = X.shape
+            self.kind = 1
+        else:
+            self.vals = np.ascontiguousarray(X, dtype=np.float32)
+            self.idx = self.indptr = None
+            self.n, self.d = self.vals.shape
+            self.kind = 0
+        self.s = _Matrix(self.kind, 0, self.n, self.d, self.vals.ctypes.data,
+                         None if self.idx is None else self.idx.ctypes.data,
+                         None if self.indptr is None else self.indptr.ctypes.data)
+
+    def ref(self):
+        return ctypes.byref(self.s)
+
+
+def uniforms(seed: int, m: int, offset: int = 0) -> np.ndarray:
+    out = np.empty(m, dtype=np.float64)
+    lib().orc_uniforms(seed, offset, m, _p(out))
+    return out
+
+
+def det_sum(v) -> float:
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    return lib().orc_det_sum(_p(v), v.size)
+
+
+def det_draw(v, u: float) -> int:
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    return int(lib().orc_det_draw(_p(v), v.size, u))
+
+
+def msr_dense(msr, row, center, prior, prior_sum=None, rowsum=None, ctrsum=None):
+    row = np.ascontiguousarray(row, dtype=np.float32)
+    center = np.ascontiguousarray(center, dtype=np.float32)
+    d = row.size
+    prior_sum = prior * d if prior_sum is None else prior_sum
+    rowsum = float(row.astype(np.float64).sum()) if rowsum is None else rowsum
+    ctrsum = float(center.astype(np.float64).sum()) if ctrsum is None else ctrsum
+    return lib().orc_msr_dense(msr, _p(row), _p(center), d, prior, prior_sum, rowsum, ctrsum)
+
+
+def msr_sparse(msr, row, center, prior, prior_sum=None):
+    """row/center: dense 1-D arrays converted to sparse (nonzero entries)."""
+    row = np.asarray(row, dtype=np.float32)
+    center = np.asarray(center, dtype=np.float32)
+    d = row.size
+    ri = np.nonzero(row)[0].astype(np.uint32)
+    ci = np.nonzero(center)[0].astype(np.uint32)
+    rv = np.ascontiguousarray(row[ri])
+    cv = np.ascontiguousarray(center[ci])
+    prior_sum = prior * d if prior_sum is None else prior_sum
+    return lib().orc_msr_sparse(msr, _p(rv), _p(ri), ri.size, _p(cv), _p(ci), ci.size, d, prior,
+                                prior_sum, float(row.astype(np.float64).sum()),
+                                float(center.astype(np.float64).sum()))
+
+
+def assign(X, centers, msr, prior):
+    M = Matrix(X)
+    C = np.ascontiguousarray(centers, dtype=np.float32)
+    asn = np.empty(M.n, dtype=np.uint32)
+    costs = np.empty(M.n, dtype=np.float64)
+    lib().orc_assign(M.ref(), _p(C), C.shape[0], msr, prior, _p(asn), _p(costs))
+    return asn, costs
+
+
+def kmeanspp(X, k, msr, prior, uniforms_, weights=None):
+    M = Matrix(X)
+    u = np.ascontiguousarray(uniforms_, dtype=np.float64)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    kk = min(k, M.n)
+    ids = np.empty(kk, dtype=np.uint32)
+    asn = np.empty(M.n, dtype=np.uint32)
+    costs = np.empty(M.n, dtype=np.float64)
+    rc = lib().orc_kmeanspp(M.ref(), k, msr, prior, _p(w), _p(u), _p(ids), _p(asn), _p(costs))
+    if rc:
+        raise ValueError("orc_kmeanspp failed")
+    return ids, asn, costs
+
+
+def hcluster(X, centers, msr, prior, weights=None, eps=1e-10, maxiter=100, seed=1):
+    M = Matrix(X)
+    C = np.ascontiguousarray(centers, dtype=np.float32)
+    k = C.shape[0]
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    cout = np.empty_like(C)
+    asn = np.empty(M.n, dtype=np.uint32)
+    costs = np.empty(M.n, dtype=np.float64)
+    ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+    rc = lib().orc_hcluster(M.ref(), _p(C), k, msr, prior, _p(w), eps, maxiter, seed, _p(cout), _p(asn),
+                            _p(costs), ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it))
+    if rc == 2:
+        raise RuntimeError("Unexpected nan in ctr")
+    return dict(initcost=ic.value, finalcost=fc.value, numiter=it.value, centers=cout, asn=asn,
+                costs=costs)
+
+
+def sensitivity(costs, asn, ncenters, method, weights=None, k=None, alpha_est=0.0):
+    costs = np.ascontiguousarray(costs)
+    f64 = 1 if costs.dtype == np.float64 else 0
+    if not f64:
+        costs = costs.astype(np.float32)
+    asn = np.ascontiguousarray(asn, dtype=np.uint32)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    probs = np.empty(costs.size, dtype=np.float32)
+    rc = lib().orc_sensitivity(costs.size, ncenters, ncenters if k is None else k, _p(costs), f64, _p(asn),
+                               _p(w), method, alpha_est, _p(probs))
+    if rc:
+        raise ValueError("orc_sensitivity failed")
+    return probs
+
+
+def alias_build(probs):
+    probs = np.ascontiguousarray(probs, dtype=np.float32)
+    pt = np.empty(probs.size, dtype=np.float64)
+    at = np.empty(probs.size, dtype=np.uint32)
+    if lib().orc_alias_build(probs.size, _p(probs), _p(pt), _p(at)):
+        raise ValueError("alias build failed")
+    return pt, at
+
+
+def coreset_sample(probs, prob_tab, alias_tab, m, seed, unique=False, weights=None, method=0, b=0):
+    probs = np.ascontiguousarray(probs, dtype=np.float32)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    wo = np.empty(m, dtype=np.float32)
+    io = np.empty(m, dtype=np.uint64)
+    lib().orc_coreset_sample(probs.size, _p(probs), _p(prob_tab), _p(alias_tab), _p(w), method, b, m, seed,
+                             int(bool(unique)), _p(wo), _p(io))
+    return wo, io

@@ -1,0 +1,811 @@
+// ORACLE — test infrastructure only.
+//
+// A plain C++17 (+OpenMP) restatement of the CPU algorithm of dnbaker/minicore for the
+// clustering hot path: cmp::msr_with_prior, coresets::kmeanspp, assign_points_hard,
+// set_centroids_full_mean / set_center, perform_hard_clustering, and the CoresetSampler
+// sensitivity + sampling code.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline leg may load this library, and only as the checker.  The product path
+// (minicore_gb300) never calls it.
+//
+// Parity anchors (reference files, paths within the minicore project):
+//   include/minicore/dist/applicator.h:1632-1915   msr_with_prior (prior setup, dense + sparse)
+//   include/minicore/util/merge.h:26-65             for_each_by_case (sharednz)
+//   include/minicore/optim/kmeans.h:49-215          kmeanspp
+//   include/minicore/clustering/solve.h:98-285      perform_hard_clustering / assign_points_hard
+//   include/minicore/clustering/centroid.h:81-178,649-779  set_center / set_centroids_full_mean
+//   include/minicore/coreset/coreset.h:340-699      make_probs_* / sample
+//
+// Where the reference delegates to libraries that are absent from the reference tree
+// (libkl reducers, libsimdsampling reservoir sampling, alias_sampler, wy RNG), this file
+// fixes one explicit definition and the CUDA path implements the same definition:
+//   * element reductions: sequential over columns, float arithmetic, fmaf where noted;
+//   * every random draw consumes a caller-supplied uniform in [0,1) (splitmix64 stream);
+//   * D^2 draws are an FP64 inverse CDF in a fixed blocked summation order (det_*);
+//   * centroid sums use a fixed chunked order (compensated FP32 within a chunk of rows,
+//     FP64 across chunks; FP64 fma when weighted);
+//   * the alias table is Vose's method in FP64 over the float probabilities.
+// Compile with -ffp-contract=off so that no multiply-add is fused behind our back.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <map>
+#include <numeric>
+#include <vector>
+
+namespace {
+
+enum Msr { L1 = 0, L2 = 1, SQRL2 = 2, JSM = 3, JSD = 4, MKL = 5, HELLINGER = 6 };
+
+constexpr double kSqrt1_2 = 0.70710678118654752440;
+
+// ---------------------------------------------------------------------------------------
+// splitmix64 uniform stream: U(seed, i) in [0, 1)
+// ---------------------------------------------------------------------------------------
+inline double uniform_at(uint64_t seed, uint64_t i) {
+    uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return double(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------------------------------
+// Canonical deterministic FP64 sums (mirrors the CUDA det_sum kernels exactly).
+// A chunk is 8192 elements; 256 "threads" each sum 32 strided elements sequentially;
+// each warp of 32 partials is reduced by an xor butterfly (lane 0's value); the 8 warp
+// totals are summed sequentially; chunk totals are summed sequentially.
+// ---------------------------------------------------------------------------------------
+constexpr uint64_t kChunk = 8192, kThreads = 256, kPer = 32;
+
+template <class Get>
+double thread_partial(const Get &get, uint64_t n, uint64_t base, uint64_t t) {
+    double acc = 0.0;
+    for (uint64_t m = 0; m < kPer; ++m) {
+        uint64_t i = base + t + kThreads * m;
+        if (i < n) acc = acc + get(i);
+    }
+    return acc;
+}
+
+inline double warp_butterfly(double *v) {  // v[32], returns lane 0 result of xor butterfly
+    double cur[32], nxt[32];
+    for (int l = 0; l < 32; ++l) cur[l] = v[l];
+    for (int off = 16; off >= 1; off >>= 1) {
+        for (int l = 0; l < 32; ++l) nxt[l] = cur[l] + cur[l ^ off];
+        std::memcpy(cur, nxt, sizeof(cur));
+    }
+    return cur[0];
+}
+
+template <class Get>
+double chunk_total(const Get &get, uint64_t n, uint64_t g, double *partials_out = nullptr) {
+    const uint64_t base = g * kChunk;
+    double p[kThreads];
+    for (uint64_t t = 0; t < kThreads; ++t) p[t] = thread_partial(get, n, base, t);
+    if (partials_out) std::memcpy(partials_out, p, sizeof(p));
+    double wsum[8];
+    for (int w = 0; w < 8; ++w) wsum[w] = warp_butterfly(p + 32 * w);
+    double tot = wsum[0];
+    for (int w = 1; w < 8; ++w) tot = tot + wsum[w];
+    return tot;
+}
+
+template <class Get>
+double det_sum(const Get &get, uint64_t n, std::vector<double> *chunk_totals = nullptr) {
+    const uint64_t G = (n + kChunk - 1) / kChunk;
+    std::vector<double> T(G);
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < int64_t(G); ++g) T[g] = chunk_total(get, n, uint64_t(g));
+    double s = 0.0;
+    for (uint64_t g = 0; g < G; ++g) s = s + T[g];
+    if (chunk_totals) *chunk_totals = std::move(T);
+    return s;
+}
+
+// Inverse-CDF draw over non-negative weights v[0..n) with uniform u.  Returns n when the
+// total weight is not positive.
+template <class Get>
+uint64_t det_draw(const Get &get, uint64_t n, double u) {
+    std::vector<double> T;
+    const double S = det_sum(get, n, &T);
+    if (!(S > 0.0)) return n;
+    const uint64_t G = T.size();
+    const double t = u * S;
+    double C = 0.0;
+    int64_t gs = -1;
+    for (uint64_t g = 0; g < G; ++g) {
+        if (C + T[g] > t) { gs = int64_t(g); break; }
+        C = C + T[g];
+    }
+    bool clamp = false;
+    if (gs < 0) {  // rounding pushed t past the running total: take the last positive chunk
+        for (int64_t g = int64_t(G) - 1; g >= 0; --g) if (T[g] > 0.0) { gs = g; break; }
+        clamp = true;
+    }
+    const uint64_t base = uint64_t(gs) * kChunk;
+    double P[kThreads];
+    chunk_total(get, n, uint64_t(gs), P);
+    const double r = t - C;
+    int64_t tau = -1;
+    double Q = 0.0;
+    if (!clamp) {
+        for (uint64_t th = 0; th < kThreads; ++th) {
+            if (Q + P[th] > r) { tau = int64_t(th); break; }
+            Q = Q + P[th];
+        }
+    }
+    auto last_pos_in_thread = [&](uint64_t th) -> uint64_t {
+        uint64_t best = n;
+        for (uint64_t m = 0; m < kPer; ++m) {
+            uint64_t i = base + th + kThreads * m;
+            if (i < n && get(i) > 0.0) best = i;
+        }
+        return best;
+    };
+    if (tau < 0) {
+        for (int64_t th = int64_t(kThreads) - 1; th >= 0; --th)
+            if (P[th] > 0.0) return last_pos_in_thread(uint64_t(th));
+        return n;
+    }
+    const double r2 = r - Q;
+    double R = 0.0;
+    for (uint64_t m = 0; m < kPer; ++m) {
+        uint64_t i = base + uint64_t(tau) + kThreads * m;
+        double val = i < n ? get(i) : 0.0;
+        if (R + val > r2) return i;
+        R = R + val;
+    }
+    return last_pos_in_thread(uint64_t(tau));
+}
+
+// ---------------------------------------------------------------------------------------
+// msr_with_prior restatement (applicator.h:1632-1915).  FT = float.
+// Role names: `row` is the reference's 2nd argument (`ctr`, the data row on every hot call
+// site) and `cen` is its 3rd argument (`mr`, the center).  "lh" = center, "rh" = row.
+// ---------------------------------------------------------------------------------------
+struct PairScalars {
+    float pv, lhsum, rhsum, lhrsi, rhrsi, lhinc, rhinc;
+};
+
+inline PairScalars pair_scalars(double prior, double prior_sum_arg, double rowsum, double ctrsum,
+                                uint64_t nd) {
+    PairScalars s;
+    float lhsum = float(ctrsum + prior_sum_arg);
+    float rhsum = float(rowsum + prior_sum_arg);
+    const float smallest_pv = 7.0069e-42f * (lhsum + rhsum);
+    const float pv = std::max(float(prior), smallest_pv);
+    const float psum = pv * float(nd);
+    lhsum = float(ctrsum + double(psum));
+    rhsum = float(rowsum + double(psum));
+    const float lhrsi = 1.f / lhsum, rhrsi = 1.f / rhsum;
+    float lhinc = (pv != 0.f && lhsum != 0.f) ? pv * lhrsi : 0.f;
+    float rhinc = (pv != 0.f && rhsum != 0.f) ? pv * rhrsi : 0.f;
+    if (std::isnan(lhinc)) lhinc = 0.f;
+    if (std::isnan(rhinc)) rhinc = 0.f;
+    s.pv = pv; s.lhsum = lhsum; s.rhsum = rhsum; s.lhrsi = lhrsi; s.rhrsi = rhrsi;
+    s.lhinc = lhinc; s.rhinc = rhinc;
+    return s;
+}
+
+inline double post_divergence(double ret) {  // applicator.h:1754-1760
+    ret = std::max(ret, 0.);
+    if (ret == double(std::numeric_limits<float>::infinity())) ret = double(std::numeric_limits<float>::max());
+    else if (ret == -double(std::numeric_limits<float>::infinity())) ret = 0.;
+    return ret;
+}
+
+// element terms shared by the dense and sparse paths (libkl reducer definitions)
+struct Reducer {
+    int msr;
+    PairScalars s;
+    float acc = 0.f;
+    inline void add(float c, float x) {
+        switch (msr) {
+            case SQRL2: { float d = c - x; acc = std::fma(d, d, acc); break; }
+            case L1: { float a = c + s.pv, b = x + s.pv; acc = acc + std::fabs(a - b); break; }
+            case HELLINGER: {
+                float a = std::sqrt(c * s.lhrsi + s.lhinc), b = std::sqrt(x * s.rhrsi + s.rhinc);
+                float d = a - b; acc = std::fma(d, d, acc); break;
+            }
+            case MKL: {
+                float a = c * s.lhrsi + s.lhinc, b = x * s.rhrsi + s.rhinc;
+                acc = std::fma(a, std::log(a) - std::log(b), acc); break;
+            }
+            case JSD: {
+                float a = c * s.lhrsi + s.lhinc, b = x * s.rhrsi + s.rhinc;
+                float m = a + b;
+                float t = (a * std::log(a) + b * std::log(b)) - m * std::log(m * 0.5f);
+                acc = acc + t; break;
+            }
+            default: break;
+        }
+    }
+};
+
+double msr_dense(int msr, const float *row, const float *cen, uint64_t d, double prior,
+                 double prior_sum, double rowsum, double ctrsum) {
+    Reducer r{msr, pair_scalars(prior, prior_sum, rowsum, ctrsum, d)};
+    for (uint64_t j = 0; j < d; ++j) r.add(cen[j], row[j]);
+    switch (msr) {
+        case SQRL2: return double(r.acc);
+        case L1: return double(r.acc * 0.5f) * 2.;
+        case HELLINGER: return double(std::sqrt(r.acc)) * kSqrt1_2;
+        case MKL: return post_divergence(double(r.acc));
+        case JSD: return post_divergence(double(r.acc * 0.5f));
+        default: return -1.;
+    }
+}
+
+// sparse/sparse path: merge the union of the two index sets; sharednz = d - |union|
+double msr_sparse(int msr, const float *rv, const uint32_t *ri, uint64_t rnz, const float *cv,
+                  const uint32_t *ci, uint64_t cnz, uint64_t d, double prior, double prior_sum,
+                  double rowsum, double ctrsum) {
+    const PairScalars s = pair_scalars(prior, prior_sum, rowsum, ctrsum, d);
+    Reducer r{msr, s};
+    uint64_t a = 0, b = 0, nunion = 0;
+    // MKL/JSD merge the scaled vectors (wr = mr * lhrsi, wc = ctr * rhrsi) and the reducer
+    // adds the increments; the metric measures merge raw values.  The reducer applies the
+    // scaling itself, so both orderings reduce to the same element terms.
+    while (a < cnz || b < rnz) {
+        float c, x;
+        if (a < cnz && b < rnz && ci[a] == ri[b]) { c = cv[a++]; x = rv[b++]; }
+        else if (b >= rnz || (a < cnz && ci[a] < ri[b])) { c = cv[a++]; x = 0.f; }
+        else { c = 0.f; x = rv[b++]; }
+        ++nunion;
+        r.add(c, x);
+    }
+    const uint64_t sharednz = d - nunion;
+    switch (msr) {
+        case SQRL2: {
+            double ret = r.acc;
+            if (ret < 0.) ret = 0.;
+            else if (std::isnan(ret)) ret = -1.;
+            return ret;
+        }
+        case L1: return double(r.acc * 0.5f) * 2.;
+        case HELLINGER: {
+            double ret = double(r.acc) +
+                         std::pow(std::sqrt(double(s.lhinc)) - std::sqrt(double(s.rhinc)), 2.) * double(sharednz);
+            return std::sqrt(ret) * kSqrt1_2;
+        }
+        case MKL: {
+            const float rhl = s.rhinc != 0.f ? std::log(s.rhinc) : 0.f;
+            const float lhl = s.lhinc != 0.f ? std::log(s.lhinc) : 0.f;
+            const float zc = float(sharednz) * s.lhinc * (lhl - rhl);
+            return post_divergence(double(r.acc + zc));
+        }
+        case JSD: {
+            const float rhl = s.rhinc != 0.f ? std::log(s.rhinc) : 0.f;
+            const float lhl = s.lhinc != 0.f ? std::log(s.lhinc) : 0.f;
+            const float rhincl = s.rhinc != 0.f ? rhl * s.rhinc : 0.f;
+            const float lhincl = s.lhinc != 0.f ? lhl * s.lhinc : 0.f;
+            const float shl = std::log((s.lhinc + s.rhinc) * 0.5f);
+            const float shincl = (s.rhinc + s.lhinc > 0.f) ? (s.lhinc + s.rhinc) * shl : 0.f;
+            const float zc = ((lhincl + rhincl - shincl) * float(sharednz)) * 0.5f;
+            return post_divergence(double(r.acc * 0.5f + zc));
+        }
+        default: return -1.;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Matrix views
+// ---------------------------------------------------------------------------------------
+struct Mat {
+    int kind;  // 0 dense row-major f32, 1 CSR f32/u32/u64
+    uint64_t n, d;
+    const float *vals;
+    const uint32_t *idx;
+    const uint64_t *indptr;
+};
+
+struct SparseVec { std::vector<uint32_t> i; std::vector<float> v; };
+
+inline double row_sum(const Mat &m, uint64_t r) {  // Blaze rowwise sum into double
+    double s = 0.;
+    if (m.kind == 0) { for (uint64_t j = 0; j < m.d; ++j) s += m.vals[r * m.d + j]; }
+    else for (uint64_t p = m.indptr[r]; p < m.indptr[r + 1]; ++p) s += m.vals[p];
+    return s;
+}
+
+inline double vec_sum(const float *v, uint64_t d) { double s = 0.; for (uint64_t j = 0; j < d; ++j) s += v[j]; return s; }
+
+SparseVec to_sparse(const float *dense, uint64_t d) {
+    SparseVec s;
+    for (uint64_t j = 0; j < d; ++j) if (dense[j] != 0.f) { s.i.push_back(uint32_t(j)); s.v.push_back(dense[j]); }
+    return s;
+}
+
+// distance between data row r and a center (dense center for dense data, sparse for CSR)
+struct CenterSet {
+    uint64_t k, d;
+    std::vector<float> dense;     // k*d
+    std::vector<SparseVec> sp;    // CSR data only
+    std::vector<double> sums;
+    void set_from_dense(const float *C, uint64_t k_, uint64_t d_, bool sparse) {
+        k = k_; d = d_;
+        dense.assign(C, C + k * d);
+        sums.resize(k);
+        sp.clear();
+        for (uint64_t c = 0; c < k; ++c) {
+            sums[c] = vec_sum(&dense[c * d], d);
+            if (sparse) sp.push_back(to_sparse(&dense[c * d], d));
+        }
+    }
+    void set_row(uint64_t c, const std::vector<float> &v, bool sparse) {
+        std::copy(v.begin(), v.end(), dense.begin() + c * d);
+        sums[c] = vec_sum(v.data(), d);
+        if (sparse) sp[c] = to_sparse(v.data(), d);
+    }
+};
+
+inline double dist_row_center(const Mat &m, uint64_t r, const CenterSet &C, uint64_t c, int msr,
+                              double prior, double psum, double rsum) {
+    if (m.kind == 0)
+        return msr_dense(msr, m.vals + r * m.d, &C.dense[c * m.d], m.d, prior, psum, rsum, C.sums[c]);
+    const uint64_t b = m.indptr[r], e = m.indptr[r + 1];
+    const SparseVec &s = C.sp[c];
+    return msr_sparse(msr, m.vals + b, m.idx + b, e - b, s.v.data(), s.i.data(), s.i.size(), m.d, prior, psum,
+                      rsum, C.sums[c]);
+}
+
+inline double dist_row_row(const Mat &m, uint64_t r, uint64_t cr, int msr, double prior, double psum,
+                           double rsum, double csum) {
+    if (m.kind == 0)
+        return msr_dense(msr, m.vals + r * m.d, m.vals + cr * m.d, m.d, prior, psum, rsum, csum);
+    const uint64_t b = m.indptr[r], e = m.indptr[r + 1], cb = m.indptr[cr], ce = m.indptr[cr + 1];
+    return msr_sparse(msr, m.vals + b, m.idx + b, e - b, m.vals + cb, m.idx + cb, ce - cb, m.d, prior, psum, rsum,
+                      csum);
+}
+
+std::vector<float> dense_row(const Mat &m, uint64_t r) {
+    std::vector<float> v(m.d, 0.f);
+    if (m.kind == 0) std::copy(m.vals + r * m.d, m.vals + (r + 1) * m.d, v.begin());
+    else for (uint64_t p = m.indptr[r]; p < m.indptr[r + 1]; ++p) v[m.idx[p]] = m.vals[p];
+    return v;
+}
+
+// assign_points_hard (solve.h:234-285): strict < keeps the lowest index on ties
+// Costs are kept in double (the dense bindings store double costs, pycluster_dense.cpp:24);
+// the CSR bindings store float costs (pycluster.h:160), so CSR values are rounded to float.
+void assign_all(const Mat &m, const CenterSet &C, int msr, double prior, double psum, const std::vector<double> &rs,
+                uint32_t *asn, double *costs) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < int64_t(m.n); ++i) {
+        double best = dist_row_center(m, uint64_t(i), C, 0, msr, prior, psum, rs[i]);
+        uint32_t bi = 0;
+        for (uint64_t j = 1; j < C.k; ++j) {
+            double v = dist_row_center(m, uint64_t(i), C, j, msr, prior, psum, rs[i]);
+            if (v < best) { best = v; bi = uint32_t(j); }
+        }
+        asn[i] = bi;
+        costs[i] = m.kind == 1 ? double(float(best)) : best;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Centroid accumulation in the canonical chunked order.
+// Unweighted: per chunk of `ch` rows (rows of a cluster in ascending order), per column a
+// compensated float sum (Knuth TwoSum, separate error accumulator); chunk value =
+// double(s) + double(e); chunk values summed in FP64 in chunk order.  Weighted: per chunk
+// FP64 fma(w, x, acc) and FP64 weight sum; then across chunks in FP64.
+// ---------------------------------------------------------------------------------------
+inline void two_sum_add(float &s, float &e, float x) {
+    const float t = s + x;
+    const float bp = t - s;
+    const float err = (s - (t - bp)) + (x - bp);
+    s = t;
+    e = e + err;
+}
+
+uint64_t centroid_chunk_rows(const Mat &m) { return m.kind == 0 ? 256 : 4096; }
+
+void mean_of_rows(const Mat &m, const std::vector<uint64_t> &rows, const double *w, float *out) {
+    const uint64_t d = m.d, ch = centroid_chunk_rows(m);
+    std::vector<double> S(d, 0.0), part(d);
+    std::vector<float> ps(d), pe(d);
+    double W = 0.0;
+    bool first = true;
+    for (uint64_t q0 = 0; q0 < rows.size(); q0 += ch) {
+        const uint64_t q1 = std::min<uint64_t>(rows.size(), q0 + ch);
+        if (w) {
+            std::fill(part.begin(), part.end(), 0.0);
+            double wq = 0.0;
+            for (uint64_t q = q0; q < q1; ++q) {
+                const uint64_t r = rows[q];
+                const double wr = w[r];
+                wq = wq + wr;
+                if (m.kind == 0) { for (uint64_t j = 0; j < d; ++j) part[j] = std::fma(wr, double(m.vals[r * d + j]), part[j]); }
+                else for (uint64_t p = m.indptr[r]; p < m.indptr[r + 1]; ++p) part[m.idx[p]] = std::fma(wr, double(m.vals[p]), part[m.idx[p]]);
+            }
+            W = first ? wq : W + wq;
+        } else {
+            std::fill(ps.begin(), ps.end(), 0.f);
+            std::fill(pe.begin(), pe.end(), 0.f);
+            for (uint64_t q = q0; q < q1; ++q) {
+                const uint64_t r = rows[q];
+                if (m.kind == 0) { for (uint64_t j = 0; j < d; ++j) two_sum_add(ps[j], pe[j], m.vals[r * d + j]); }
+                else for (uint64_t p = m.indptr[r]; p < m.indptr[r + 1]; ++p) two_sum_add(ps[m.idx[p]], pe[m.idx[p]], m.vals[p]);
+            }
+            for (uint64_t j = 0; j < d; ++j) part[j] = double(ps[j]) + double(pe[j]);
+        }
+        if (first) { S = part; first = false; }
+        else for (uint64_t j = 0; j < d; ++j) S[j] = S[j] + part[j];
+    }
+    const double denom = w ? W : double(rows.size());
+    for (uint64_t j = 0; j < d; ++j) out[j] = float(S[j] / denom);
+}
+
+// total cost (solve.h:120-123) in FP64 canonical order, returned as FT=float
+float compute_cost(const double *costs, const double *w, uint64_t n) {
+    double s = w ? det_sum([&](uint64_t i) { return costs[i] * w[i]; }, n)
+                 : det_sum([&](uint64_t i) { return costs[i]; }, n);
+    return float(s);
+}
+
+// set_centroids_full_mean (centroid.h:649-779).  Returns 1 if any center was restarted,
+// 0 otherwise, -1 on a NaN center.
+int set_centroids_full_mean(const Mat &m, int msr, double prior, std::vector<uint32_t> &asn, std::vector<double> &costs,
+                            CenterSet &C, const double *w, const std::vector<double> &rs, uint64_t seed,
+                            uint64_t &restart_counter) {
+    const uint64_t n = m.n, k = C.k;
+    const bool sparse = m.kind == 1;
+    std::vector<std::vector<uint64_t>> assigned(k);
+    for (uint64_t i = 0; i < n; ++i) assigned[asn[i]].push_back(i);
+    std::vector<uint32_t> empty;
+    for (uint32_t i = 0; i < k; ++i) if (assigned[i].empty()) empty.push_back(i);
+    int restarted = 0;
+    if (!empty.empty()) {
+        restarted = 1;
+        // the reference passes prior[0] * prior.size() as the prior sum here (centroid.h:700)
+        const double psum_restart = double(float(prior)) * 1.0;
+        for (auto &a : assigned) a.clear();
+        std::vector<uint64_t> rsel;
+        for (uint32_t id : empty) {
+            const double u = uniform_at(seed, restart_counter++);
+            uint64_t r = det_draw([&](uint64_t i) { return costs[i]; }, n, u);
+            if (r >= n) r = 0;
+            rsel.push_back(r);
+            C.set_row(id, dense_row(m, r), sparse);
+        }
+        std::vector<uint32_t> best(n);
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t i = 0; i < int64_t(n); ++i) {
+            double c0 = dist_row_center(m, uint64_t(i), C, 0, msr, prior, psum_restart, rs[i]);
+            uint32_t bi = 0;
+            for (uint64_t j = 0; j < k; ++j) {
+                double c = dist_row_center(m, uint64_t(i), C, j, msr, prior, psum_restart, rs[i]);
+                if (c < c0) { c0 = c; bi = uint32_t(j); }
+            }
+            costs[i] = m.kind == 1 ? double(float(c0)) : c0;
+            best[i] = bi;
+        }
+        for (uint64_t i = 0; i < n; ++i) { asn[i] = best[i]; assigned[best[i]].push_back(i); }
+        for (size_t e = 0; e < empty.size(); ++e) {
+            const uint64_t pid = rsel[e];
+            const uint32_t cid = empty[e];
+            if (asn[pid] != cid) {  // the row also stays in its previous list (centroid.h:743-751)
+                asn[pid] = cid;
+                costs[pid] = 0.;
+                assigned[cid].push_back(pid);
+            }
+        }
+    }
+    for (auto &a : assigned) std::sort(a.begin(), a.end());
+    std::vector<float> out(m.d);
+    for (uint32_t i = 0; i < k; ++i) {
+        const auto &rows = assigned[i];
+        if (rows.empty()) continue;
+        if (rows.size() == 1) { C.set_row(i, dense_row(m, rows[0]), sparse); continue; }
+        mean_of_rows(m, rows, w, out.data());
+        for (float v : out) if (std::isnan(v)) return -1;
+        C.set_row(i, out, sparse);
+    }
+    return restarted;
+}
+
+}  // namespace
+
+// =======================================================================================
+// C interface (test infrastructure)
+// =======================================================================================
+extern "C" {
+
+struct orc_matrix {
+    int32_t kind;
+    int32_t pad;
+    uint64_t n, d;
+    const float *vals;
+    const uint32_t *idx;
+    const uint64_t *indptr;
+};
+
+static Mat to_mat(const orc_matrix *m) { return Mat{m->kind, m->n, m->d, m->vals, m->idx, m->indptr}; }
+
+double orc_uniform(uint64_t seed, uint64_t i) { return uniform_at(seed, i); }
+void orc_uniforms(uint64_t seed, uint64_t offset, uint64_t m, double *out) {
+    for (uint64_t i = 0; i < m; ++i) out[i] = uniform_at(seed, offset + i);
+}
+
+double orc_det_sum(const double *v, uint64_t n) { return det_sum([&](uint64_t i) { return v[i]; }, n); }
+uint64_t orc_det_draw(const double *v, uint64_t n, double u) { return det_draw([&](uint64_t i) { return v[i]; }, n, u); }
+
+double orc_msr_dense(int msr, const float *row, const float *cen, uint64_t d, double prior, double prior_sum,
+                     double rowsum, double ctrsum) {
+    return msr_dense(msr, row, cen, d, prior, prior_sum, rowsum, ctrsum);
+}
+double orc_msr_sparse(int msr, const float *rv, const uint32_t *ri, uint64_t rnz, const float *cv,
+                      const uint32_t *ci, uint64_t cnz, uint64_t d, double prior, double prior_sum, double rowsum,
+                      double ctrsum) {
+    return msr_sparse(msr, rv, ri, rnz, cv, ci, cnz, d, prior, prior_sum, rowsum, ctrsum);
+}
+
+// one hard assignment pass; centers dense k x d (sparse copies are made for CSR data)
+int orc_assign(const orc_matrix *mm, const float *centers, uint32_t k, int msr, double prior, uint32_t *asn,
+               double *costs) {
+    const Mat m = to_mat(mm);
+    CenterSet C;
+    C.set_from_dense(centers, k, m.d, m.kind == 1);
+    std::vector<double> rs(m.n);
+    for (uint64_t i = 0; i < m.n; ++i) rs[i] = row_sum(m, i);
+    const double psum = double(float(prior * double(m.d)));
+    assign_all(m, C, msr, prior, psum, rs, asn, costs);
+    return 0;
+}
+
+// coresets::kmeanspp (kmeans.h:49-215) with n_local_trials == 1 and no ls++.
+// uniforms[0] picks the first center (floor(u * n)); uniforms[c] drives round c.
+int orc_kmeanspp(const orc_matrix *mm, uint32_t k, int msr, double prior, const double *w, const double *uniforms,
+                 uint32_t *centers, uint32_t *asn, double *costs) {
+    const Mat m = to_mat(mm);
+    const uint64_t n = m.n;
+    if (n == 0 || k == 0) return 1;
+    if (k > n) k = uint32_t(n);
+    std::vector<double> rs(n);
+    for (uint64_t i = 0; i < n; ++i) rs[i] = row_sum(m, i);
+    const double psum = prior * double(m.d);
+    std::vector<double> dist(n);
+    uint64_t fc = uint64_t(uniforms[0] * double(n));
+    if (fc >= n) fc = n - 1;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < int64_t(n); ++i)
+        dist[i] = (uint64_t(i) == fc) ? 0. : dist_row_row(m, uint64_t(i), fc, msr, prior, psum, rs[i], rs[fc]);
+    std::fill(asn, asn + n, 0u);
+    centers[0] = uint32_t(fc);
+    for (uint32_t ci = 1; ci < k; ++ci) {
+        const double u = uniforms[ci];
+        uint64_t newc = w ? det_draw([&](uint64_t i) { return w[i] * dist[i]; }, n, u)
+                          : det_draw([&](uint64_t i) { return dist[i]; }, n, u);
+        if (newc >= n || dist[newc] == 0.) {  // argmax fallback (kmeans.h:179-186): first maximum
+            uint64_t am = 0;
+            for (uint64_t i = 1; i < n; ++i) if (dist[i] > dist[am]) am = i;
+            newc = am;
+        }
+        asn[newc] = ci;
+        centers[ci] = uint32_t(newc);
+        const double cs = rs[newc];
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t i = 0; i < int64_t(n); ++i) {
+            if (uint64_t(i) == newc) continue;
+            if (dist[i] <= 0.) continue;
+            const double dv = dist_row_row(m, uint64_t(i), newc, msr, prior, psum, rs[i], cs);
+            if (dv < dist[i]) { asn[i] = ci; dist[i] = dv; }
+        }
+        dist[newc] = 0.;
+    }
+    std::copy(dist.begin(), dist.end(), costs);
+    return 0;
+}
+
+// perform_hard_clustering (solve.h:98-175) from explicit dense centers.
+// Returns 0 on success, 2 if a NaN center appeared.
+int orc_hcluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int msr, double prior, const double *w,
+                 double eps, uint64_t maxiter, uint64_t seed, float *centers_out, uint32_t *asn_out, double *costs_out,
+                 double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
+    const Mat m = to_mat(mm);
+    const uint64_t n = m.n;
+    const bool sparse = m.kind == 1;
+    std::vector<double> rs(n);
+    for (uint64_t i = 0; i < n; ++i) rs[i] = row_sum(m, i);
+    const double psum = double(float(prior * double(m.d)));
+    CenterSet centers, cpy;
+    centers.set_from_dense(centers_in, k, m.d, sparse);
+    std::vector<uint32_t> asn(n);
+    std::vector<double> costs(n);
+    uint64_t restart_counter = 0;
+    assign_all(m, centers, msr, prior, psum, rs, asn.data(), costs.data());
+    const float initcost = compute_cost(costs.data(), w, n);
+    float cost = initcost;
+    uint64_t iternum = 0;
+    int rc = 0;
+    if (cost == 0.f) {
+        *initcost_out = 0.; *finalcost_out = 0.; *numiter_out = 0;
+    } else {
+        cpy = centers;
+        for (;;) {
+            int res = set_centroids_full_mean(m, msr, prior, asn, costs, cpy, w, rs, seed, restart_counter);
+            if (res < 0) { rc = 2; break; }
+            assign_all(m, cpy, msr, prior, psum, rs, asn.data(), costs.data());
+            const float newcost = compute_cost(costs.data(), w, n);
+            if (newcost > cost && !res) {
+                assign_all(m, centers, msr, prior, psum, rs, asn.data(), costs.data());
+                break;
+            }
+            centers = cpy;
+            ++iternum;
+            const float oldcost = cost;
+            cost = newcost;
+            if (double(oldcost - newcost) < eps * std::max(double(newcost), double(oldcost)) || iternum > maxiter) break;
+        }
+        *initcost_out = initcost; *finalcost_out = cost; *numiter_out = iternum;
+    }
+    std::copy(centers.dense.begin(), centers.dense.end(), centers_out);
+    std::copy(asn.begin(), asn.end(), asn_out);
+    std::copy(costs.begin(), costs.end(), costs_out);
+    return rc;
+}
+
+// CoresetSampler (coreset.h:340-578).  The sampler keeps point weights as float
+// (CoresetSampler<float,uint32_t>::weights_, coreset.h:234,290), so `w` is float here.
+// Per-cluster sums (weight, cost, count) are FP64 over the cluster's points in ascending
+// index order, in chunks of 256 points (sequential within a chunk, chunk partials summed
+// in order).  Per-point sensitivity arithmetic is FP64; probabilities are stored as float.
+// methods: 0 BFL, 1 FL, 2 LFKF, 3 VX, 4 LBK.  costs_f64 != 0 -> costs is double*.
+// ---------------------------------------------------------------------------------------
+static std::vector<double> cluster_sums(uint64_t n, uint64_t nc, const uint32_t *asn,
+                                        const std::function<double(uint64_t)> &val) {
+    std::vector<std::vector<uint64_t>> lists(nc);
+    for (uint64_t i = 0; i < n; ++i) lists[asn[i]].push_back(i);
+    std::vector<double> out(nc, 0.0);
+    for (uint64_t c = 0; c < nc; ++c) {
+        const auto &L = lists[c];
+        double S = 0.0;
+        bool first = true;
+        for (uint64_t q0 = 0; q0 < L.size(); q0 += 256) {
+            double p = 0.0;
+            for (uint64_t q = q0; q < std::min<uint64_t>(L.size(), q0 + 256); ++q) p = p + val(L[q]);
+            S = first ? p : S + p;
+            first = false;
+        }
+        out[c] = S;
+    }
+    return out;
+}
+
+int orc_sensitivity(uint64_t n, uint64_t ncenters, uint64_t k, const void *costs, int costs_f64, const uint32_t *asn,
+                    const float *w, int method, double alpha_est, float *probs) {
+    auto cost = [&](uint64_t i) -> double {
+        return costs_f64 ? ((const double *)costs)[i] : double(((const float *)costs)[i]);
+    };
+    auto wt = [&](uint64_t i) -> double { return w ? double(w[i]) : 1.0; };
+    for (uint64_t i = 0; i < n; ++i) if (asn[i] >= ncenters) return 1;
+    const std::vector<double> cnt = cluster_sums(n, ncenters, asn, [&](uint64_t) { return 1.0; });
+    const std::vector<double> wsum = cluster_sums(n, ncenters, asn, wt);
+    std::vector<double> s(n);
+    switch (method) {
+        case 0: {  // BFL (coreset.h:534-578)
+            const double total_cost = det_sum([&](uint64_t i) { return wt(i) * cost(i); }, n);
+            for (uint64_t i = 0; i < n; ++i) {
+                const double fraccost = wt(i) * cost(i) / total_cost;
+                const double fracw = wt(i) / (wsum[asn[i]] * cnt[asn[i]]);
+                s[i] = 0.5 * (fraccost + fracw);
+            }
+            break;
+        }
+        case 1: {  // FL (coreset.h:456-486): not normalised
+            const double total_cost = det_sum([&](uint64_t i) { return wt(i) * cost(i); }, n);
+            const double inv = 1.0 / total_cost;
+            for (uint64_t i = 0; i < n; ++i) {
+                if (w) probs[i] = float(wt(i) * cost(i) * inv);
+                else probs[i] = float(std::ceil(double(n) * inv * cost(i)) + 1.0);
+            }
+            return 0;
+        }
+        case 2: {  // LFKF (coreset.h:340-381): squared costs, per-point (the reference sizes
+                   // its per-point buffer by ncenters; the per-point intent is used here)
+            const std::vector<double> csum = cluster_sums(n, ncenters, asn, [&](uint64_t i) { return wt(i) * cost(i) * cost(i); });
+            const double tc2 = det_sum([&](uint64_t i) { return wt(i) * cost(i) * cost(i); }, n);
+            for (uint64_t i = 0; i < n; ++i) {
+                const uint32_t a = asn[i];
+                s[i] = alpha_est * wt(i) * (cost(i) * cost(i) + csum[a] / wsum[a]) + 2.0 * tc2 / wsum[a];
+            }
+            break;
+        }
+        case 3: {  // VX (coreset.h:423-455)
+            const double total_cost = det_sum([&](uint64_t i) { return wt(i) * cost(i); }, n);
+            for (uint64_t i = 0; i < n; ++i) s[i] = wt(i) * cost(i) / total_cost + 1.0 / cnt[asn[i]];
+            break;
+        }
+        case 4: {  // LBK (coreset.h:487-533)
+            const std::vector<double> csum = cluster_sums(n, ncenters, asn, [&](uint64_t i) { return wt(i) * cost(i); });
+            const double total_cost = det_sum([&](uint64_t i) { return wt(i) * cost(i); }, n);
+            const double alpha = 16.0 * std::log(double(k)) + 32.0, alpha2 = 2.0 * alpha;
+            double W = 0.0;
+            for (uint64_t c = 0; c < ncenters; ++c) W = W + wsum[c];
+            const double avg = total_cost / W;
+            const double tcinv = alpha / avg;
+            std::vector<double> adj(ncenters);
+            for (uint64_t c = 0; c < ncenters; ++c) adj[c] = alpha2 * csum[c] / (wsum[c] * avg) + 4.0 * W / wsum[c];
+            for (uint64_t i = 0; i < n; ++i) s[i] = tcinv * cost(i) + adj[asn[i]];
+            break;
+        }
+        default: return 1;
+    }
+    const double tot = det_sum([&](uint64_t i) { return s[i]; }, n);
+    const double inv = 1.0 / tot;
+    for (uint64_t i = 0; i < n; ++i) probs[i] = float(s[i] * inv);
+    return 0;
+}
+
+// Vose alias table in FP64 over float weights: scaled q_i = p_i * n / sum(p) (sum in the
+// canonical det order).  Light (q < 1) and heavy (q >= 1) items are FIFO worklists in index
+// order; each light item takes the current heavy item as alias; a heavy item whose
+// residual drops below 1 moves to the back of the light list.
+int orc_alias_build(uint64_t n, const float *probs, double *prob_tab, uint32_t *alias_tab) {
+    if (n == 0) return 1;
+    const double S = det_sum([&](uint64_t i) { return double(probs[i]); }, n);
+    if (!(S > 0.0)) return 1;
+    const double scale = double(n) / S;
+    std::vector<double> q(n);
+    std::vector<uint32_t> light, heavy;
+    for (uint64_t i = 0; i < n; ++i) {
+        q[i] = double(probs[i]) * scale;
+        if (q[i] < 1.0) light.push_back(uint32_t(i)); else heavy.push_back(uint32_t(i));
+    }
+    size_t li = 0, hi = 0;
+    while (li < light.size() && hi < heavy.size()) {
+        const uint32_t l = light[li++];
+        const uint32_t g = heavy[hi];
+        prob_tab[l] = q[l];
+        alias_tab[l] = g;
+        q[g] = (q[g] + q[l]) - 1.0;
+        if (q[g] < 1.0) { light.push_back(g); ++hi; }
+    }
+    while (hi < heavy.size()) { const uint32_t g = heavy[hi++]; prob_tab[g] = 1.0; alias_tab[g] = g; }
+    while (li < light.size()) { const uint32_t l = light[li++]; prob_tab[l] = 1.0; alias_tab[l] = l; }
+    return 0;
+}
+
+uint64_t orc_alias_draw(uint64_t np, const double *prob_tab, const uint32_t *alias_tab, uint64_t seed, uint64_t s) {
+    const double u1 = uniform_at(seed, 2 * s), u2 = uniform_at(seed, 2 * s + 1);
+    uint64_t i = uint64_t(u1 * double(np));
+    if (i >= np) i = np - 1;
+    return (u2 < prob_tab[i]) ? i : alias_tab[i];
+}
+
+// CoresetSampler::sample (coreset.h:625-699).  Draw s uses U(seed, 2s) for the bucket and
+// U(seed, 2s+1) for the coin.  With unique, draws continue until sampled_directly distinct
+// indices were seen; the entries are sorted by index and weighted by their count, in the
+// reference's float arithmetic (coreset.h:669).  FL samples m - b points directly and
+// leaves the remaining b entries zero (no bicriteria points are set through the binding).
+// Writes m entries.
+void orc_coreset_sample(uint64_t np, const float *probs, const double *prob_tab, const uint32_t *alias_tab,
+                        const float *w, int method, uint64_t b, uint64_t m, uint64_t seed, int unique,
+                        float *weights_out, uint64_t *idx_out) {
+    const uint64_t sampled_directly = (method == 1) ? (m > b ? m - b : 0) : m;
+    auto wt = [&](uint64_t i) -> float { return w ? w[i] : 1.f; };
+    for (uint64_t i = 0; i < m; ++i) { weights_out[i] = 0.f; idx_out[i] = 0; }
+    if (!unique) {
+        for (uint64_t s = 0; s < sampled_directly; ++s) {
+            const uint64_t ind = orc_alias_draw(np, prob_tab, alias_tab, seed, s);
+            idx_out[s] = ind;
+            weights_out[s] = float(double(wt(ind)) / (double(m) * double(probs[ind])));
+        }
+        return;
+    }
+    std::map<uint64_t, uint32_t> ctr;
+    for (uint64_t s = 0; ctr.size() < sampled_directly; ++s) ++ctr[orc_alias_draw(np, prob_tab, alias_tab, seed, s)];
+    uint64_t o = 0;
+    for (const auto &kv : ctr) {
+        idx_out[o] = kv.first;
+        weights_out[o] = float(kv.second) * (wt(kv.first) / (float(m) * probs[kv.first]));
+        ++o;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,217 @@
+"""The oracle against the reference's own known-answer tests and invariants.
+
+Anchors: src/tests/testmsr.cpp (self-distance ~0 for every measure and prior in
+{0, 1, 50, 1e-2}; positivity of msr(cv1, cv4); the MKL value for prior 1),
+src/tests/testmsrcsr.cpp (sparse and dense representations agree within 1e-5 on the large
+count-vector pair), src/tests/test_centroid.cpp (exact weighted means), and
+src/tests/coreset_test.cpp (sampled indices in range).
+"""
+import os
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "msr_fixtures.npz")
+MEASURES = [0, 2, 4, 5, 6]  # L1, SQRL2, JSD, MKL, HELLINGER
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLD)
+
+
+@pytest.mark.parametrize("msr", MEASURES)
+@pytest.mark.parametrize("prior", [0.0, 1.0, 50.0, 1e-2])
+def test_self_distance_zero_and_positive(orc, gold, msr, prior):
+    cv1, cv4 = gold["cv1"], gold["cv4"]
+    for f in (orc.msr_dense, orc.msr_sparse):
+        v = f(msr, cv1, cv1, prior)
+        assert abs(v) <= 5e-4  # testmsr.cpp:50-55
+        assert not np.isnan(v)
+        assert f(msr, cv1, cv4, prior) > 0  # testmsr.cpp:62-66
+
+
+def test_mkl_known_answer(orc, gold):
+    # testmsr.cpp:67 calls msr_with_prior(MKL, cv1, cv4, prior=1, psum=12, ...).
+    # The reference's own sparse correction terms (applicator.h:1849) fix the direction as
+    # KL(center~ || row~) with the 3rd argument (cv4) as the center: 0.5377195590904397.
+    # The value printed by that test, 0.539179777847523, is the other direction.
+    cv1, cv4 = gold["cv1"], gold["cv4"]
+    v = orc.msr_dense(5, cv1, cv4, 1.0, 12.0)
+    assert v == pytest.approx(0.5377195590904397, rel=2e-6)
+    assert orc.msr_sparse(5, cv1, cv4, 1.0, 12.0) == pytest.approx(0.5377195590904397, rel=2e-6)
+    a = (cv4.astype(np.float64) + 1) / (cv4.sum() + 12)
+    b = (cv1.astype(np.float64) + 1) / (cv1.sum() + 12)
+    assert float((b * np.log(b / a)).sum()) == pytest.approx(0.539179777847523, rel=1e-12)
+
+
+def test_large_sparse_pair_dense_vs_sparse(orc, gold):
+    d = int(gold["big_dim"])
+    lhs = np.zeros(d, np.float32)
+    rhs = np.zeros(d, np.float32)
+    lhs[gold["lhs_idx"]] = gold["lhs_val"]
+    rhs[gold["rhs_idx"]] = gold["rhs_val"]
+    prior = 1e-5  # testmsr.cpp:72-73
+    for msr in (5,):
+        v_dense = orc.msr_dense(msr, lhs, rhs, prior, prior * d)
+        v_sparse = orc.msr_sparse(msr, lhs, rhs, prior, prior * d)
+        assert v_dense > 0 and v_sparse > 0
+        assert abs(v_dense - v_sparse) <= 1e-5 * max(1.0, abs(v_dense))  # testmsrcsr.cpp:94-95
+    for msr in MEASURES:
+        a = orc.msr_dense(msr, lhs, rhs, 1.0)
+        b = orc.msr_sparse(msr, lhs, rhs, 1.0)
+        assert abs(a - b) <= 1e-5 * max(1.0, abs(a))
+
+
+def _np_measure(msr, row, cen, prior):
+    """FP64 textbook form of each measure (applicator.h:1672-1760)."""
+    row = row.astype(np.float64)
+    cen = cen.astype(np.float64)
+    d = row.size
+    pv = prior
+    a = (cen + pv) / (cen.sum() + pv * d)
+    b = (row + pv) / (row.sum() + pv * d)
+    if msr == 2:
+        return ((cen - row) ** 2).sum()
+    if msr == 0:
+        return np.abs(cen - row).sum()
+    if msr == 6:
+        return np.sqrt(((np.sqrt(a) - np.sqrt(b)) ** 2).sum()) * np.sqrt(0.5)
+    if msr == 5:
+        return (a * np.log(a / b)).sum()
+    if msr == 4:
+        m = a + b
+        return 0.5 * (a * np.log(a) + b * np.log(b) - m * np.log(m / 2)).sum()
+
+
+@pytest.mark.parametrize("msr", MEASURES)
+def test_measures_match_fp64_formulas(orc, msr):
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        d = int(rng.integers(3, 300))
+        row = rng.poisson(2.0, d).astype(np.float32)
+        cen = rng.gamma(2.0, 1.0, d).astype(np.float32)
+        for prior in (0.5, 1.0):
+            ref = _np_measure(msr, row, cen, prior)
+            assert orc.msr_dense(msr, row, cen, prior) == pytest.approx(ref, rel=2e-5, abs=1e-6)
+            assert orc.msr_sparse(msr, row, cen, prior) == pytest.approx(ref, rel=2e-5, abs=1e-6)
+
+
+def test_centroid_known_answers(orc):
+    # test_centroid.cpp:48-60: identity-diagonal rows (value 10 on the diagonal) -> mean 1;
+    # 10x10 CSR diagonal of ones -> 0.1 everywhere.
+    dm = np.eye(10, dtype=np.float32) * 10
+    out = orc.hcluster(dm, dm[:1], 2, 0.0, maxiter=0)  # one center: the mean of all rows
+    # after one update the single center is the column mean
+    Xs = sp.csr_matrix(np.eye(10, dtype=np.float32))
+    res = orc.hcluster(Xs, np.eye(10, dtype=np.float32)[:1], 2, 0.0, maxiter=0)
+    assert np.allclose(res["centers"][0], 0.1, atol=1e-7)
+    # fcsm2 case (test_centroid.cpp:94-112): rows i have columns 0,2,4,6,8 with values
+    # 2(5i+j+1); the mean of column 2j is 47 + 2j.
+    data = 2.0 * (np.arange(50) + 1.0)
+    idx = np.tile(np.arange(0, 10, 2), 10)
+    indptr = np.arange(0, 51, 5)
+    F = sp.csr_matrix((data.astype(np.float32), idx, indptr), shape=(10, 10))
+    res = orc.hcluster(F, F.toarray()[:1], 2, 0.0, maxiter=0)
+    c = res["centers"][0]
+    for j in range(5):
+        assert int(c[2 * j]) == 47 + 2 * j
+
+
+def test_det_sum_and_draw(orc):
+    rng = np.random.default_rng(1)
+    v = rng.random(100_003)
+    assert orc.det_sum(v) == pytest.approx(v.sum(), rel=1e-13)
+    # canonical visiting order: chunks of 8192 in order; within a chunk, thread-major over
+    # 256 threads, each thread visiting its 32 strided elements (t, t+256, ...)
+    n = v.size
+    order = []
+    for base in range(0, n, 8192):
+        for t in range(256):
+            order.extend(i for i in range(base + t, min(n, base + 8192), 256))
+    order = np.array(order)
+    pos = np.empty(n, dtype=np.int64)
+    pos[order] = np.arange(n)
+    c = np.cumsum(v[order])
+    for u in rng.random(200):
+        i = orc.det_draw(v, u)
+        t = u * c[-1]
+        # the drawn element's cumulative interval contains the target (up to rounding)
+        p = pos[i]
+        lo = c[p - 1] if p else 0.0
+        assert lo - 1e-9 * c[-1] <= t <= c[p] + 1e-9 * c[-1]
+    z = np.zeros(10)
+    assert orc.det_draw(z, 0.5) == 10
+    w = np.zeros(20000)
+    w[12345] = 3.0
+    assert orc.det_draw(w, 0.999) == 12345
+
+
+def test_uniform_stream_properties(orc):
+    u = orc.uniforms(42, 100000)
+    assert u.min() >= 0 and u.max() < 1
+    assert abs(u.mean() - 0.5) < 0.01
+    assert np.array_equal(orc.uniforms(42, 10, offset=5), u[5:15])
+
+
+def test_kmeanspp_basic(orc):
+    rng = np.random.default_rng(0)
+    centers = rng.uniform(-10, 10, (5, 8))
+    X = (centers[rng.integers(0, 5, 2000)] + rng.normal(size=(2000, 8))).astype(np.float32)
+    u = orc.uniforms(7, 5)
+    ids, asn, costs = orc.kmeanspp(X, 5, 2, 0.0, u)
+    assert len(set(ids.tolist())) == 5
+    assert costs[ids].max() == 0
+    d2 = ((X[:, None, :].astype(np.float64) - X[ids][None].astype(np.float64)) ** 2).sum(-1)
+    assert np.allclose(costs, d2.min(1), rtol=1e-5, atol=1e-4)
+    # D^2 seeding on well-separated blobs hits every blob in most runs
+    true = ((X[:, None] - centers[None]) ** 2).sum(-1).argmin(1)
+    hits = sum(len(set(true[orc.kmeanspp(X, 5, 2, 0.0, orc.uniforms(s, 5))[0]].tolist())) == 5
+               for s in range(20))
+    assert hits >= 15
+
+
+def test_hcluster_converges_monotone(orc):
+    rng = np.random.default_rng(3)
+    mu = rng.uniform(-10, 10, (25, 50))
+    X = (mu[np.repeat(np.arange(25), 40)] + rng.normal(size=(1000, 50))).astype(np.float32)
+    u = orc.uniforms(11, 25)
+    ids, _, _ = orc.kmeanspp(X, 25, 2, 0.0, u)
+    res = orc.hcluster(X, X[ids], 2, 0.0, maxiter=19)
+    assert res["finalcost"] <= res["initcost"]
+    d2 = ((X[:, None, :].astype(np.float64) - res["centers"][None].astype(np.float64)) ** 2).sum(-1)
+    assert np.array_equal(res["asn"], d2.argmin(1))
+
+
+@pytest.mark.parametrize("method", [0, 1, 2, 3, 4])
+def test_sensitivity_and_sampling(orc, method):
+    rng = np.random.default_rng(method)
+    n, nc = 10000, 20
+    asn = rng.integers(0, nc, n).astype(np.uint32)
+    costs = (rng.integers(0, 3, n) + 0.1).astype(np.float32)
+    w = (1.0 / (rng.integers(0, 5, n) + 1)).astype(np.float32)
+    for weights in (None, w):
+        p = orc.sensitivity(costs, asn, nc, method, weights=weights)
+        assert np.all(p > 0)
+        if method != 1:
+            assert p.astype(np.float64).sum() == pytest.approx(1.0, rel=1e-5)
+        pt, at = orc.alias_build(p)
+        for m in (20, 200, 2000):
+            wo, io = orc.coreset_sample(p, pt, at, m, seed=9, weights=weights, method=method, b=nc)
+            assert io.max() < n  # coreset_test.cpp:30
+            wo2, io2 = orc.coreset_sample(p, pt, at, m, seed=9, unique=True, weights=weights, method=method, b=nc)
+            direct = m - nc if method == 1 else m
+            assert np.all(np.diff(io2[:direct].astype(np.int64)) > 0)
+
+
+def test_alias_table_is_exact_distribution(orc):
+    rng = np.random.default_rng(2)
+    p = rng.random(1000).astype(np.float32) ** 3
+    pt, at = orc.alias_build(p)
+    n = p.size
+    mass = pt / n
+    mass_alias = np.zeros(n)
+    np.add.at(mass_alias, at, (1 - pt) / n)
+    q = p.astype(np.float64) / p.astype(np.float64).sum()
+    assert np.allclose(mass + mass_alias, q, atol=1e-12)
