@@ -1,0 +1,306 @@
+#!/usr/bin/env python3
+"""Benchmark: Lloyd iterations/s on the dense 4M x 128, k=1024 Gaussian-mixture workload.
+
+A step is one Lloyd iteration (centroid update + hard assignment) over all rows.
+
+* value: device-resident rows/centers (torch tensors handed to the C ABI), K steps timed
+  with CUDA events on the library's stream, barrier + synchronize on both sides.  The rows
+  (2 GiB f32 + 1 GiB bf16 copy) exceed the 129 MB L2, so no flush is needed between steps.
+* e2e: the reference-facing call (mc_hcluster through minicore_gb300.hcluster) with host
+  buffers in pinned memory: each step uploads the rows, runs kmeans++-seeded centers
+  through 10 Lloyd updates and reads back centers / assignments / costs.
+* roofline: the assignment kernel (the dominant launch), timed alone with CUDA events.
+* cpu_baseline / --impl reference: the oracle (C++/OpenMP restatement of the reference's
+  CPU path) on a row sample, scaled to the full row count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, D, K, COMPONENTS = 4_000_000, 128, 1024, 1024
+E2E_ITERS = 10
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "tf32", "fp32"])
+    ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def make_data(n, seed=0):
+    """1024 component means ~N(0, 4I), points ~N(mean, I) (seeded, generated on the GPU)."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    mu = torch.randn(COMPONENTS, D, generator=g, device="cuda") * 2.0
+    lab = torch.randint(0, COMPONENTS, (n,), generator=g, device="cuda")
+    X = torch.randn(n, D, generator=g, device="cuda")
+    X.add_(mu[lab])
+    return X.contiguous()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        s = [x for x in self.samples if len(x) >= 8]
+        if not s:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(x[0]) for x in s if x[0].replace(".", "").isdigit()]
+        mx = [float(x[1]) for x in s if x[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for x in s for i in range(4) if x[4 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(s)}
+
+
+def cpu_baseline(X_sample, C, threads):
+    """One Lloyd iteration (assignment + centroid update) of the oracle on a row sample."""
+    import oracle
+    oracle.build()
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    t0 = time.perf_counter()
+    oracle.hcluster(X_sample, C, 2, 0.0, eps=0.0, maxiter=0, seed=1)  # assign, update, assign
+    t = time.perf_counter() - t0
+    # two assignment passes + one centroid update; a Lloyd iteration is one of each
+    per_iter = t / 2.0
+    return per_iter
+
+
+def reference_arm(args):
+    """--impl reference: the oracle's CPU Lloyd iteration, all host threads, on a sample."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    rng = np.random.default_rng(0)
+    S = 20_000
+    mu = rng.normal(size=(COMPONENTS, D)) * 2.0
+    Xs = (mu[rng.integers(0, COMPONENTS, S)] + rng.normal(size=(S, D))).astype(np.float32)
+    C = Xs[rng.choice(S, K, replace=False)]
+    for _ in range(args.warmup):
+        pass
+    times = []
+    for _ in range(max(args.steps, 1)):
+        times.append(cpu_baseline(Xs, C, threads))
+    per_iter_full = float(np.mean(times)) * (args.n / S)
+    v = 1.0 / per_iter_full
+    line = {"metric": "Lloyd iters/s 4M x128 k=1024", "value": v, "unit": "iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter_full * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"dense {args.n}x{D} gaussian mixture, SQRL2, k={K}, Lloyd iteration",
+                       "sample_rows": S},
+            "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
+                             "sample": f"{S} rows x k={K} (one assignment + centroid update), scaled by {args.n}/{S}"},
+            "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    import minicore_gb300 as mc
+    ctx = mc.Context(local)
+    # a dedicated (non-default) stream: the library launches on it and the CUDA events
+    # that time the steps are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    n = args.n
+    X = make_data(n, seed=rank)
+    # kmeans++ centers (untimed setup), ids on the host
+    seeds = mc.uniforms(1234, K)
+    ids = np.empty(K, np.uint32)
+    asn0 = torch.empty(n, dtype=torch.int32, device="cuda")
+    costs0 = torch.empty(n, dtype=torch.float64, device="cuda")
+    from minicore_gb300 import _lib
+    M = mc._MatrixArg(X)
+    u = torch.from_numpy(seeds).cuda()
+    idst = torch.empty(K, dtype=torch.int32, device="cuda")
+    _lib.check(_lib.load().mc_kmeanspp(ctx.handle, M.ref, K, 2, 0.0, None, mc._p(u), mc._p(idst), mc._p(asn0),
+                                       mc._p(costs0)))
+    torch.cuda.synchronize()
+    ids = idst.cpu().numpy().astype(np.int64)
+    C0 = X[torch.from_numpy(ids).cuda()].contiguous()
+    del asn0, costs0
+
+    job = mc.Job(X, C0, msr=2, precision=args.precision, seed=7, ctx=ctx)
+    job.assign()
+    for _ in range(args.warmup):
+        job.lloyd_step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = Clocks()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    lib = _lib.load()
+    l0 = lib.mc_kernel_launches()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        job.lloyd_step()
+    ev1.record(stream)
+    launches = int(lib.mc_kernel_launches() - l0)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * 1000.0 / ms_per_step  # independent replicas: iterations completed per second
+    recheck = job.recheck_count()
+
+    # dominant kernel: the assignment pass, timed alone
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    job.assign()
+    torch.cuda.synchronize()
+    a0.record(stream)
+    for _ in range(reps):
+        job.assign()
+    a1.record(stream)
+    torch.cuda.synchronize()
+    assign_ms = a0.elapsed_time(a1) / reps
+    pk, pk_kind = peaks()
+    flops = 2.0 * n * K * D
+    achieved = flops / (assign_ms * 1e-3) / 1e12
+    peak = pk.get("bf16_tflops", 1935.7)
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "peak_source": pk_kind,
+                "kernel": f"assignment pass ({args.precision})", "kernel_ms": assign_ms,
+                "algorithmic": "2*n*k*d FLOP per pass"}
+
+    # FP32 plain kernel for the same iteration (the comparison named by the metric)
+    fp32 = None
+    if args.precision != "fp32":
+        j32 = mc.Job(X, C0, msr=2, precision="fp32", seed=7, ctx=ctx)
+        j32.assign()
+        j32.lloyd_step()
+        torch.cuda.synchronize()
+        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        b0.record(stream)
+        for _ in range(2):
+            j32.lloyd_step()
+        b1.record(stream)
+        torch.cuda.synchronize()
+        fp32 = 1000.0 / (b0.elapsed_time(b1) / 2)
+        j32.close()
+
+    # e2e: hcluster from pinned host buffers, 10 Lloyd updates per step
+    e2e = None
+    if not args.no_e2e:
+        Xh = torch.empty((n, D), dtype=torch.float32, pin_memory=True)
+        Xh.copy_(X)
+        Ch = C0.cpu().numpy()
+        Xn = Xh.numpy()
+        mc.hcluster(Xn, Ch, msr=2, eps=0.0, maxiter=1, precision=args.precision, ctx=ctx)  # warm
+        torch.cuda.synchronize()
+        e_steps = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        iters = 0
+        for _ in range(e_steps):
+            r = mc.hcluster(Xn, Ch, msr=2, eps=0.0, maxiter=E2E_ITERS - 1, precision=args.precision, ctx=ctx)
+            iters += int(r["numiter"])
+        t = time.perf_counter() - t0
+        e2e = {"value": iters / t, "unit": "iters/s", "h2d_bytes_per_step": int(n * D * 4 + K * D * 4),
+               "d2h_bytes_per_step": int(K * D * 4 + n * 4 + n * 8),
+               "call": "minicore_gb300.hcluster(host pinned rows, maxiter=9, eps=0)"}
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        threads = os.cpu_count() or 1
+        S = 20_000
+        Xs = X[:S].cpu().numpy()
+        Cs = C0.cpu().numpy()
+        per = cpu_baseline(Xs, Cs, threads)
+        cpu = {"value": 1.0 / (per * n / S), "unit": "iters/s", "cores": threads, "kind": "port",
+               "sample": f"{S} rows x k={K}: one assignment + centroid update of the oracle, scaled by {n}/{S}"}
+
+    if rank == 0:
+        line = {"metric": "Lloyd iters/s 4M x128 k=1024", "value": value, "unit": "iters/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": args.precision, "data": "synthetic",
+                "config": {"workload": f"dense {n}x{D} gaussian mixture ({COMPONENTS} comps), SQRL2, k={K}, "
+                                       f"kmeans++ centers, Lloyd iteration",
+                           "precision": args.precision, "parallelism": f"replicas{world}",
+                           "l2": "inputs (2 GiB f32) larger than L2; no flush"},
+                "fp32_gpu_iters_per_s": fp32,
+                "speedup_vs_fp32_gpu": (value / world / fp32) if fp32 else None,
+                "recheck_rows_last_pass": recheck,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * minicore_gb300 — C ABI of the GB300-native clustering hot path.
+ *
+ * Every entry point here replaces one call the reference makes on its hot path
+ * (dnbaker/minicore, paths within that project):
+ *
+ *   mc_kmeanspp          coresets::kmeanspp            include/minicore/optim/kmeans.h:49-215
+ *                        driven by py_kmeanspp_noso(_dense) python/smw.h:179-412
+ *   mc_assign            assign_points_hard            include/minicore/clustering/solve.h:234-285
+ *                        (per-pair cmp::msr_with_prior include/minicore/dist/applicator.h:1632-1915)
+ *   mc_set_centroids     set_centroids_full_mean       include/minicore/clustering/centroid.h:649-779
+ *                        + set_center                  centroid.h:81-112 (CSR), 137-178 (dense)
+ *   mc_hcluster          perform_hard_clustering       include/minicore/clustering/solve.h:98-175
+ *                        driven by cpp_pycluster_from_centers python/pycluster.h:10-63
+ *   mc_sampler_*         CoresetSampler::make_sampler  include/minicore/coreset/coreset.h:386-422
+ *                        make_probs_{bfl,fl,vx,lbk}, make_gmm_sampler coreset.h:340-578,
+ *                        sample                        coreset.h:625-699
+ *   mc_job_* / mc_server_*  resident-state jobs and the continuous-batching server (no
+ *                        reference counterpart: the reference runs one call at a time).
+ *
+ * Conventions
+ *  - Every pointer argument may point to host memory or to device memory of the
+ *    context's GPU; the library detects which (cudaPointerGetAttributes) and copies as
+ *    needed.  Outputs are written in place.
+ *  - Calls return an mc_status; mc_last_error() returns a thread-local message for the
+ *    last failing call on the calling thread.
+ *  - Measures use the reference's numbering (include/minicore/dist/distance.h:24-64).
+ *  - Randomness: every draw consumes a uniform in [0,1).  Where an entry point takes a
+ *    seed, draw i uses U(seed, i) of the splitmix64 stream that mc_uniforms() produces.
+ */
+#ifndef MINICORE_GB300_H_
+#define MINICORE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mc_status {
+    MC_OK = 0,
+    MC_EINVAL = 1,       /* invalid argument (reference: std::invalid_argument)        */
+    MC_ENOMEM = 2,       /* device allocation failed / admission refused                */
+    MC_ETIMEOUT = 3,     /* a bounded device wait gave up                                */
+    MC_ECUDA = 4,        /* CUDA runtime error                                           */
+    MC_ENAN = 5,         /* NaN center (reference: runtime_error "Unexpected nan in ctr") */
+    MC_EUNSUPPORTED = 6, /* measure / option outside the implemented hot path            */
+    MC_EBUSY = 7         /* result not ready yet (mc_server_poll)                        */
+} mc_status;
+
+typedef enum mc_measure {
+    MC_L1 = 0,
+    MC_SQRL2 = 2,
+    MC_JSD = 4,
+    MC_MKL = 5,
+    MC_HELLINGER = 6
+} mc_measure;
+
+typedef enum mc_precision {
+    MC_FP32 = 0, /* exact FP32 CUDA-core distances                                   */
+    MC_TF32 = 1, /* SQRL2 dense: tcgen05 TF32 GEMM + FP32 re-check of near ties      */
+    MC_BF16 = 2  /* SQRL2 dense: tcgen05 BF16 GEMM + FP32 re-check of near ties      */
+} mc_precision;
+
+typedef enum mc_sensitivity {
+    MC_BFL = 0, MC_FL = 1, MC_LFKF = 2, MC_VX = 3, MC_LBK = 4
+} mc_sensitivity;
+
+typedef enum mc_matrix_kind { MC_DENSE_F32 = 0, MC_CSR_F32 = 1 } mc_matrix_kind;
+
+/* Dense row-major float32 matrix, or CSR with float32 values, uint32 column indices
+ * (ascending within each row) and uint64 row offsets: the zero-copy view the reference's
+ * PyCSparseMatrix keeps (python/pycsparse.h:33-70). */
+typedef struct mc_matrix {
+    int32_t kind;              /* mc_matrix_kind                                */
+    int32_t reserved;
+    uint64_t nrows, ncols;
+    const float *values;       /* dense: nrows*ncols; CSR: nnz                  */
+    const uint32_t *indices;   /* CSR only                                      */
+    const uint64_t *indptr;    /* CSR only, nrows+1 entries                     */
+    uint64_t nnz;              /* CSR only                                      */
+} mc_matrix;
+
+typedef struct mc_context mc_context;
+typedef struct mc_sampler mc_sampler;
+typedef struct mc_job mc_job;
+typedef struct mc_server mc_server;
+
+const char *mc_version(void);
+const char *mc_last_error(void);
+/* Number of CUDA kernels this library has launched in this process (diagnostics). */
+uint64_t mc_kernel_launches(void);
+
+int mc_context_create(int device, mc_context **out);
+int mc_context_destroy(mc_context *ctx);
+/* Launch on this stream (a cudaStream_t) instead of the context's own stream. */
+int mc_context_set_stream(mc_context *ctx, void *cuda_stream);
+int mc_context_synchronize(mc_context *ctx);
+
+/* U(seed, offset + i), i < m, into host memory. */
+int mc_uniforms(uint64_t seed, uint64_t offset, uint64_t m, double *out);
+
+/* D^2 / k-means++ seeding (kmeans.h:49-215, n_local_trials == 1, no ls++).
+ * uniforms: k values; uniforms[0] picks the first center (floor(u*n)), uniforms[c] drives
+ * round c.  weights: optional (double, n).  Outputs: center_ids[k], asn[n] (center
+ * ordinal), costs[n] (distance to the nearest chosen center). */
+int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior,
+                const double *weights, const double *uniforms,
+                uint32_t *center_ids, uint32_t *asn, double *costs);
+
+/* One hard assignment pass (solve.h:234-285): asn[i] = argmin_j msr(row i, center j),
+ * lowest index on ties; costs[i] = that distance.  centers: dense k x ncols float32. */
+int mc_assign(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_t k, int msr,
+              double prior, int precision, uint32_t *asn, double *costs);
+
+/* Lloyd / Bregman EM from explicit centers (solve.h:98-175): eps, maxiter and the
+ * revert-on-increase rule as in the reference; empty clusters restart by D^2 draws
+ * U(seed, r).  weights: optional (double, n). */
+int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
+                double prior, const double *weights, double eps, uint64_t maxiter, uint64_t seed,
+                int precision, float *centers_out, uint32_t *asn, double *costs,
+                double *initcost, double *finalcost, uint64_t *numiter);
+
+/* Coreset sampler (coreset.h:386-422).  costs: float32 or float64 (costs_f64 != 0);
+ * weights: optional float32 (the reference stores them as float). k: the k of LBK's
+ * alpha (pass ncenters for the reference default). */
+int mc_sampler_create(mc_context *ctx, uint64_t np, uint64_t ncenters, uint64_t k,
+                      const void *costs, int costs_f64, const uint32_t *asn, const float *weights,
+                      int method, double alpha_est, mc_sampler **out);
+int mc_sampler_destroy(mc_sampler *s);
+int mc_sampler_probs(mc_sampler *s, float *probs);
+int mc_sampler_alias(mc_sampler *s, double *prob_table, uint32_t *alias_table);
+/* m draws (coreset.h:625-699); draw t uses U(seed, 2t) and U(seed, 2t+1).  Writes m
+ * weights and indices (unused FL slots stay zero, as in the reference). */
+int mc_sampler_sample(mc_sampler *s, uint64_t m, uint64_t seed, int unique, float *weights,
+                      uint64_t *indices);
+
+/* Resident jobs: the matrix, centers, assignments and costs stay on the device. */
+int mc_job_create(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_t k, int msr,
+                  double prior, const double *weights, int precision, uint64_t seed, mc_job **out);
+int mc_job_destroy(mc_job *job);
+int mc_job_assign(mc_job *job);                       /* assignment pass with current centers */
+int mc_job_lloyd_step(mc_job *job, int *restarted);   /* centroid update + assignment */
+int mc_job_cost(mc_job *job, double *cost);           /* FP64 objective of current asn/costs */
+int mc_job_run(mc_job *job, double eps, uint64_t maxiter, double *initcost, double *finalcost,
+               uint64_t *numiter);                    /* the perform_hard_clustering loop */
+int mc_job_read(mc_job *job, float *centers, uint32_t *asn, double *costs);
+/* rows whose BF16/TF32 margin fell below the bound in the last pass (0 for FP32) */
+int mc_job_recheck_count(mc_job *job, uint64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MINICORE_GB300_H_ */

@@ -1,0 +1,479 @@
+"""minicore_gb300 — GB300-native clustering hot path with minicore's Python entry points.
+
+Drop-in functions (same names, argument meanings and defaults as the reference's
+``minicore`` package, ``minicore/__init__.py:23-163`` and the pybind11 module
+``pyminicore``):
+
+* ``kmeanspp(matrix, k, *, msr=2, prior=0., seed=0, ntimes=1, lspp=0, expskips=0,
+  n_local_trials=1, weights=None)`` -> ``(center_ids u32[k], asn u8/u16/u32[n], costs)``
+  (``python/pydense.cpp:34-77``, ``python/smw.h:179-412``);
+* ``hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxiter=1000,
+  ...)`` -> ``{initcost, finalcost, numiter, centers, costs, asn}``
+  (``python/pycluster_dense.cpp:69-112``, ``python/pycluster.h:10-205``);
+* ``CoresetSampler`` with ``make_sampler / get_probs / sample`` (``python/pycs.cpp:3-58``);
+* ``CSparseMatrix`` (``python/pycsparse.cpp:15-89``) and ``cluster`` (``minicore/__init__.py:235-261``).
+
+All computation runs in the CUDA library ``libminicore_gb300.so`` through its C ABI
+(``include/minicore_gb300.h``).  There is no CPU fallback.
+
+Differences from the reference, by design:
+* randomness: the reference's wy/aesctr RNG streams and libsimdsampling are not part of
+  its tree; every draw here consumes U(seed, i) of a splitmix64 stream (``uniforms``);
+* float64 inputs are computed in float32 (the reference computes them in float64);
+* ``precision="bf16"|"tf32"`` selects the tensor-core SQRL2 assignment for dense data.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _lib
+from ._lib import McMatrix, check
+
+__all__ = ["kmeanspp", "hcluster", "cluster", "CoresetSampler", "CSparseMatrix", "Context", "Job",
+           "uniforms", "library_path", "L1", "SQRL2", "JSD", "MKL", "HELLINGER",
+           "BFL", "FL", "LFKF", "VX", "LBK"]
+
+L1, SQRL2, JSD, MKL, HELLINGER = 0, 2, 4, 5, 6
+BFL, FL, LFKF, VX, LBK = 0, 1, 2, 3, 4
+_MEASURE_NAMES = {"L1": 0, "SQRL2": 2, "JSD": 4, "MKL": 5, "HELLINGER": 6}
+_PREC = {"fp32": _lib.MC_FP32, "tf32": _lib.MC_TF32, "bf16": _lib.MC_BF16}
+
+library_path = _lib.library_path
+
+
+def _msr(m) -> int:
+    if isinstance(m, str):
+        key = m.upper()
+        if key not in _MEASURE_NAMES:
+            raise NotImplementedError(f"measure {m!r} is outside the implemented hot path")
+        return _MEASURE_NAMES[key]
+    return int(m)
+
+
+def _p(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _seed(seed) -> int:
+    seed = int(seed)
+    if seed == 0:  # the reference draws a random seed for 0 (python/smw.h:188)
+        seed = int.from_bytes(os.urandom(8), "little") or 1
+    return seed & 0xFFFFFFFFFFFFFFFF
+
+
+def uniforms(seed: int, m: int, offset: int = 0) -> np.ndarray:
+    """U(seed, offset + i), i < m: the splitmix64 stream every draw of this library uses."""
+    out = np.empty(m, dtype=np.float64)
+    check(_lib.load().mc_uniforms(seed, offset, m, _p(out)))
+    return out
+
+
+# ------------------------------------------------------------------------------------
+# context
+# ------------------------------------------------------------------------------------
+class Context:
+    """One CUDA device + stream.  Thread-compatible; one per thread for concurrency."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.mc_context_create(device, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self._lib.mc_context_set_stream(self.handle, ctypes.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self):
+        check(self._lib.mc_context_synchronize(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.mc_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_tls = threading.local()
+
+
+def default_context() -> Context:
+    ctx = getattr(_tls, "ctx", None)
+    if ctx is None:
+        ctx = Context(0)
+        _tls.ctx = ctx
+    return ctx
+
+
+# ------------------------------------------------------------------------------------
+# matrices
+# ------------------------------------------------------------------------------------
+class CSparseMatrix:
+    """Zero-copy view of CSR arrays (python/pycsparse.h:33-70).  Values are used as float32,
+    column indices as uint32 and row offsets as uint64; other dtypes are converted once."""
+
+    def __init__(self, sparray=None, *, data=None, indices=None, indptr=None, shape=None):
+        if sparray is not None:
+            if isinstance(sparray, tuple) and len(sparray) == 2 and isinstance(sparray[0], tuple):
+                (data, indices, indptr), shape = sparray
+            else:
+                data, indices, indptr = sparray.data, sparray.indices, sparray.indptr
+                shape = sparray.shape
+        self.data = data if (hasattr(data, "data_ptr") or (isinstance(data, np.ndarray) and data.dtype == np.float32
+                                                             and data.flags.c_contiguous)) \
+            else np.ascontiguousarray(data, dtype=np.float32)
+        self.indices = indices if (hasattr(indices, "data_ptr") or (isinstance(indices, np.ndarray)
+                                   and indices.dtype == np.uint32 and indices.flags.c_contiguous)) \
+            else np.ascontiguousarray(indices, dtype=np.uint32)
+        self.indptr = indptr if (hasattr(indptr, "data_ptr") or (isinstance(indptr, np.ndarray)
+                                 and indptr.dtype == np.uint64 and indptr.flags.c_contiguous)) \
+            else np.ascontiguousarray(indptr, dtype=np.uint64)
+        self.shape = (int(shape[0]), int(shape[1]))
+
+    @staticmethod
+    def from_items(data, indices, indptr, shape):
+        return CSparseMatrix(data=data, indices=indices, indptr=indptr, shape=shape)
+
+    def rows(self):
+        return self.shape[0]
+
+    def columns(self):
+        return self.shape[1]
+
+    def nnz(self):
+        return int(self.data.shape[0]) if hasattr(self.data, "shape") else len(self.data)
+
+    def __str__(self):
+        return f"CSparseMatrix, {self.shape[0]}x{self.shape[1]}, {self.nnz()}"
+
+
+def _is_sparse(x) -> bool:
+    try:
+        import scipy.sparse as sp
+        if sp.issparse(x):
+            return True
+    except ImportError:  # pragma: no cover
+        pass
+    return isinstance(x, CSparseMatrix)
+
+
+class _MatrixArg:
+    """Keeps the arrays behind an mc_matrix alive for the duration of a call."""
+
+    def __init__(self, X):
+        if _is_sparse(X):
+            if not isinstance(X, CSparseMatrix):
+                import scipy.sparse as sp
+                X = sp.csr_matrix(X)
+                if not X.has_sorted_indices:
+                    X = X.sorted_indices()
+                X = CSparseMatrix(X)
+            self.keep = X
+            self.kind = _lib.MC_CSR_F32
+            self.n, self.d = X.shape
+            self.m = McMatrix(_lib.MC_CSR_F32, 0, self.n, self.d, _p(X.data), _p(X.indices), _p(X.indptr),
+                              X.nnz())
+        else:
+            if hasattr(X, "data_ptr"):  # torch tensor (device-resident input)
+                if X.dtype.__str__() != "torch.float32" or not X.is_contiguous() or X.dim() != 2:
+                    raise ValueError("device matrices must be contiguous 2-D float32 tensors")
+                self.keep = X
+                self.n, self.d = X.shape
+            else:
+                A = np.ascontiguousarray(X, dtype=np.float32)
+                if A.ndim != 2:
+                    raise ValueError("Wrong number of dimensions")
+                self.keep = A
+                self.n, self.d = A.shape
+            self.kind = _lib.MC_DENSE_F32
+            self.m = McMatrix(_lib.MC_DENSE_F32, 0, self.n, self.d, _p(self.keep), None, None, 0)
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.m)
+
+
+def _row_dense(M: _MatrixArg, r: int) -> np.ndarray:
+    X = M.keep
+    if M.kind == _lib.MC_DENSE_F32:
+        return np.asarray(X[r], dtype=np.float32) if not hasattr(X, "data_ptr") else X[r].cpu().numpy()
+    out = np.zeros(M.d, dtype=np.float32)
+    ip = np.asarray(X.indptr)
+    b, e = int(ip[r]), int(ip[r + 1])
+    out[np.asarray(X.indices)[b:e].astype(np.int64)] = np.asarray(X.data)[b:e]
+    return out
+
+
+def _centers_array(M: _MatrixArg, centers) -> np.ndarray:
+    """Center specification as in obj2dvec (python/pyhelpers.h:123-218): 1-D integer array or
+    sequence of row ids, a 2-D array, or a sequence of 1-D arrays."""
+    if isinstance(centers, np.ndarray) and centers.ndim == 2:
+        C = np.ascontiguousarray(centers, dtype=np.float32)
+    elif isinstance(centers, np.ndarray) and centers.ndim == 1 and np.issubdtype(centers.dtype, np.integer):
+        C = np.stack([_row_dense(M, int(r)) for r in centers])
+    elif isinstance(centers, (list, tuple)) and len(centers) and isinstance(centers[0], np.ndarray):
+        C = np.stack([np.asarray(c, dtype=np.float32).ravel() for c in centers])
+    elif isinstance(centers, (list, tuple)):
+        C = np.stack([_row_dense(M, int(r)) for r in centers])
+    else:
+        raise ValueError("Invalid: expected numpy array or list of numpy arrays or list of center ids")
+    if C.ndim != 2 or C.shape[1] != M.d:
+        raise ValueError("centers must have as many columns as the matrix")
+    return np.ascontiguousarray(C, dtype=np.float32)
+
+
+# ------------------------------------------------------------------------------------
+# kmeans++
+# ------------------------------------------------------------------------------------
+def _asn_dtype(k: int):
+    # python/smw.h:329-341 (dense) and 211-220 (CSR)
+    if k <= 256:
+        return np.uint8
+    if k <= 63356:
+        return np.uint16
+    return np.uint32
+
+
+def kmeanspp(matrix, k, *, msr=2, prior=0., seed=0, ntimes=1, lspp=0, expskips=0, n_local_trials=1,
+             weights=None, ctx: Context | None = None):
+    """D^2 seeding (include/minicore/optim/kmeans.h:49-215).  Returns (center ids,
+    assignments, costs); costs are float32 for dense input and float64 for CSR input, as in
+    the reference bindings.  ``lspp`` rounds and ``n_local_trials > 1`` are not implemented."""
+    if lspp:
+        raise NotImplementedError("localsearch++ rounds are outside the implemented hot path")
+    if n_local_trials and int(n_local_trials) > 1:
+        raise NotImplementedError("n_local_trials > 1 is outside the implemented hot path")
+    ctx = ctx or default_context()
+    M = _MatrixArg(matrix)
+    k = int(k)
+    if k <= 0:
+        raise ValueError("k must be positive")
+    if prior < 0:
+        prior = 1.0 / M.d  # python/smw.h:184-187
+    seed = _seed(seed)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    kk = min(k, M.n)
+    # dense: ntimes - 1 extra runs, best total cost kept (python/pydense.cpp:41, smw.h:385-393).
+    # CSR: the reference compares the extra runs against the first run's own cost
+    # (python/smw.h:250), so the first run is always returned.
+    runs = max(int(ntimes), 1) if M.kind == _lib.MC_DENSE_F32 else 1
+    best = None
+    for t in range(runs):
+        u = uniforms(seed, k, offset=t * k)
+        ids = np.empty(kk, dtype=np.uint32)
+        asn = np.empty(M.n, dtype=np.uint32)
+        costs = np.empty(M.n, dtype=np.float64)
+        check(_lib.load().mc_kmeanspp(ctx.handle, M.ref, k, _msr(msr), float(prior), _p(w), _p(u), _p(ids),
+                                      _p(asn), _p(costs)))
+        c = costs.sum()
+        if best is None or c < best[0]:
+            best = (c, ids, asn, costs)
+    _, ids, asn, costs = best
+    asn = asn.astype(_asn_dtype(k))
+    if M.kind == _lib.MC_DENSE_F32:
+        costs = costs.astype(np.float32)
+    return ids, asn, costs
+
+
+# ------------------------------------------------------------------------------------
+# hcluster
+# ------------------------------------------------------------------------------------
+def _centers_to_csr(C: np.ndarray):
+    """centers2pylist (python/pyhelpers.h:67-112): ((data f32, idx u32, indptr u64), shape)."""
+    nz = C != 0
+    indptr = np.zeros(C.shape[0] + 1, dtype=np.uint64)
+    indptr[1:] = np.cumsum(nz.sum(1))
+    rows, cols = np.nonzero(nz)
+    return ((C[rows, cols].astype(np.float32), cols.astype(np.uint32), indptr),
+            np.array(C.shape, dtype=np.uint64))
+
+
+def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxiter=1000, mbsize=-1,
+             ncheckins=-1, with_rep=False, cs=False, seed=0, reseed_count=5, precision="fp32",
+             ctx: Context | None = None):
+    """Hard Lloyd/Bregman EM from explicit centers (clustering/solve.h:98-175)."""
+    if mbsize is not None and int(mbsize) > 0:
+        raise NotImplementedError("minibatch clustering is outside the implemented hot path")
+    ctx = ctx or default_context()
+    M = _MatrixArg(matrix)
+    C = _centers_array(M, centers)
+    k = C.shape[0]
+    if prior < 0:
+        prior = 1.0 / M.d
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    cout = np.empty_like(C)
+    asn = np.empty(M.n, dtype=np.uint32)
+    costs = np.empty(M.n, dtype=np.float64)
+    ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+    check(_lib.load().mc_hcluster(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(eps),
+                                  int(maxiter), _seed(seed), _PREC[precision], _p(cout), _p(asn), _p(costs),
+                                  ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
+    centers_out = cout if M.kind == _lib.MC_DENSE_F32 else _centers_to_csr(cout)
+    return {"initcost": ic.value, "finalcost": fc.value, "numiter": it.value, "centers": centers_out,
+            "costs": costs.astype(np.float32), "asn": asn}
+
+
+def cluster_from_centers(*args, **kwargs):
+    return hcluster(*args, **kwargs)
+
+
+def cluster(data, *, msr, k, prior=0., seed=0, nmkc=0, ntimes=1, lspp=0, use_exponential_skips=False,
+            n_local_trials=1, weights=None, mbsize=-1, clustereps=1e-4, temp=-1., cs=False, with_rep=True,
+            outpref="mc.cluster.output", maxiter=50, precision="fp32"):
+    """kmeans++ then hcluster (minicore/__init__.py:235-261); soft clustering (temp > 0) is
+    outside the implemented hot path."""
+    if temp > 0:
+        raise NotImplementedError("Soft clustering not supported")
+    seed = _seed(seed)
+    ids, asn, costs = kmeanspp(data, k, msr=msr, prior=prior, seed=seed, ntimes=ntimes, lspp=lspp,
+                               n_local_trials=n_local_trials, weights=weights)
+    return hcluster(data, ids.astype(np.int64), prior=prior, msr=msr, weights=weights, eps=clustereps,
+                    maxiter=maxiter, seed=seed, precision=precision)
+
+
+# ------------------------------------------------------------------------------------
+# coreset sampler
+# ------------------------------------------------------------------------------------
+class CoresetSampler:
+    """CoresetSampler<float, uint32_t> (include/minicore/coreset/coreset.h:228-701)."""
+
+    def __init__(self, ctx: Context | None = None):
+        self._ctx = ctx or default_context()
+        self._h = None
+        self.np_ = 0
+
+    def make_sampler(self, ncenters, costs, assignments, weights=None, seed=13, sens=0):
+        costs = np.asarray(costs)
+        if costs.ndim != 1:
+            raise ValueError("costs must be 1-dimensional")
+        if costs.dtype == np.float64:
+            c, f64 = np.ascontiguousarray(costs), 1
+        elif costs.dtype == np.float32:
+            c, f64 = np.ascontiguousarray(costs), 0
+        else:
+            raise ValueError("Costs is not double or float")
+        a = np.ascontiguousarray(assignments, dtype=np.uint32)
+        w = None
+        if weights is not None:
+            wa = np.asarray(weights)
+            if wa.ndim != 1:
+                raise ValueError("weightss must be 1-dimensional")
+            if wa.dtype not in (np.float32, np.float64):
+                raise ValueError("Weights can only be double or float")
+            w = np.ascontiguousarray(wa, dtype=np.float32)
+        self._release()
+        h = ctypes.c_void_p()
+        check(_lib.load().mc_sampler_create(self._ctx.handle, c.size, int(ncenters), int(ncenters), _p(c), f64,
+                                            _p(a), _p(w), int(sens), 0.0, ctypes.byref(h)))
+        self._h = h
+        self.np_ = c.size
+        self.seed_ = int(seed)
+        self.sens_ = int(sens)
+        return None
+
+    def get_probs(self):
+        out = np.empty(self.np_, dtype=np.float32)
+        check(_lib.load().mc_sampler_probs(self._h, _p(out)))
+        return out
+
+    def alias_table(self):
+        pt = np.empty(self.np_, dtype=np.float64)
+        at = np.empty(self.np_, dtype=np.uint32)
+        check(_lib.load().mc_sampler_alias(self._h, _p(pt), _p(at)))
+        return pt, at
+
+    def sample(self, size, seed=0, unique=False, eps=0.1):
+        if self._h is None:
+            raise ValueError("Can't sample without created sampler. Call make_ampler")
+        size = int(size)
+        wo = np.empty(size, dtype=np.float32)
+        io = np.empty(size, dtype=np.uint64)
+        check(_lib.load().mc_sampler_sample(self._h, size, _seed(seed), int(bool(unique)), _p(wo), _p(io)))
+        return wo, io
+
+    def _release(self):
+        if self._h is not None:
+            _lib.load().mc_sampler_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self._release()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------------------------
+# resident jobs (device state kept between calls)
+# ------------------------------------------------------------------------------------
+class Job:
+    """A clustering job whose matrix, centers, assignments and costs stay on the GPU."""
+
+    def __init__(self, matrix, centers, *, msr=2, prior=0., weights=None, precision="fp32", seed=1,
+                 ctx: Context | None = None):
+        self._ctx = ctx or default_context()
+        self._M = _MatrixArg(matrix)
+        if hasattr(centers, "data_ptr"):
+            self._C = centers
+            k = centers.shape[0]
+        else:
+            self._C = _centers_array(self._M, centers)
+            k = self._C.shape[0]
+        self.k = k
+        self._w = None if weights is None else (weights if hasattr(weights, "data_ptr")
+                                                else np.ascontiguousarray(weights, dtype=np.float64))
+        h = ctypes.c_void_p()
+        check(_lib.load().mc_job_create(self._ctx.handle, self._M.ref, _p(self._C), k, _msr(msr), float(prior),
+                                        _p(self._w), _PREC[precision], int(seed), ctypes.byref(h)))
+        self._h = h
+
+    def assign(self):
+        check(_lib.load().mc_job_assign(self._h))
+
+    def lloyd_step(self) -> bool:
+        r = ctypes.c_int()
+        check(_lib.load().mc_job_lloyd_step(self._h, ctypes.byref(r)))
+        return bool(r.value)
+
+    def cost(self) -> float:
+        c = ctypes.c_double()
+        check(_lib.load().mc_job_cost(self._h, ctypes.byref(c)))
+        return c.value
+
+    def run(self, eps=1e-10, maxiter=100):
+        ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        check(_lib.load().mc_job_run(self._h, float(eps), int(maxiter), ctypes.byref(ic), ctypes.byref(fc),
+                                     ctypes.byref(it)))
+        return ic.value, fc.value, it.value
+
+    def read(self, centers=None, asn=None, costs=None):
+        check(_lib.load().mc_job_read(self._h, _p(centers), _p(asn), _p(costs)))
+
+    def recheck_count(self) -> int:
+        c = ctypes.c_uint64()
+        check(_lib.load().mc_job_recheck_count(self._h, ctypes.byref(c)))
+        return c.value
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            _lib.load().mc_job_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,762 @@
+// C ABI of minicore_gb300 (include/minicore_gb300.h): context, device-resident jobs, the
+// perform_hard_clustering loop (include/minicore/clustering/solve.h:98-175), kmeans++
+// (include/minicore/optim/kmeans.h:49-215) and the coreset sampler
+// (include/minicore/coreset/coreset.h:228-701).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "mc_assign.cuh"
+#include "mc_coreset.cuh"
+#include "mc_internal.cuh"
+#include "mc_kmpp.cuh"
+#include "mc_reduce.cuh"
+#include "mc_tc.cuh"
+
+namespace mc {
+
+static thread_local std::string g_last_error;
+static std::atomic<uint64_t> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+int fail(int status, const std::string &msg) {
+    g_last_error = msg;
+    return status;
+}
+
+bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+// copy `bytes` from src (host or device) into a device buffer unless src already lives on
+// the device, in which case it is borrowed
+template <class T>
+static int stage(const T *src, size_t count, DBuf<T> &own, const T *&out, cudaStream_t st) {
+    if (!src) {
+        out = nullptr;
+        return MC_OK;
+    }
+    if (is_device_ptr(src)) {
+        out = src;
+        return MC_OK;
+    }
+    MC_TRY(own.alloc(count, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(own.p, src, count * sizeof(T), cudaMemcpyDefault, st));
+    out = own.p;
+    return MC_OK;
+}
+
+template <class T>
+static int copy_out(T *dst, const T *src, size_t count, cudaStream_t st) {
+    if (!dst || count == 0) return MC_OK;
+    MC_CUDA_TRY(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDefault, st));
+    return MC_OK;
+}
+
+// CSR structure check (every kernel relies on it): indptr[0] == 0, nondecreasing,
+// indptr[n] == nnz, column indices < d and strictly increasing within each row.
+__global__ void k_validate_csr(const uint64_t *indptr, const uint32_t *idx, uint64_t n, uint64_t d, uint64_t nnz,
+                               int *bad) {
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (i == 0 && (indptr[0] != 0 || indptr[n] != nnz)) atomicExch(bad, 1);
+    if (i >= n) return;
+    const uint64_t b = indptr[i], e = indptr[i + 1];
+    if (e < b || e > nnz) {
+        atomicExch(bad, 2);
+        return;
+    }
+    for (uint64_t p = b; p < e; ++p) {
+        if (idx[p] >= d || (p > b && idx[p] <= idx[p - 1])) {
+            atomicExch(bad, 3);
+            return;
+        }
+    }
+}
+
+static int validate_csr(const uint64_t *indptr, const uint32_t *idx, uint64_t n, uint64_t d, uint64_t nnz,
+                        cudaStream_t st) {
+    DBuf<int> flag;
+    MC_TRY(flag.alloc(1, st));
+    MC_CUDA_TRY(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+    k_validate_csr<<<unsigned((n + 255) / 256), 256, 0, st>>>(indptr, idx, n, d, nnz, flag.p), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    int bad = 0;
+    MC_CUDA_TRY(cudaMemcpyAsync(&bad, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (bad == 1) return fail(MC_EINVAL, "CSR indptr must start at 0 and end at nnz");
+    if (bad == 2) return fail(MC_EINVAL, "CSR indptr must be nondecreasing");
+    if (bad == 3) return fail(MC_EINVAL, "CSR column indices must be < ncols and strictly increasing in each row");
+    return MC_OK;
+}
+
+struct DevMatrix {
+    int kind = MC_DENSE_F32;
+    uint64_t n = 0, d = 0, nnz = 0;
+    const float *X = nullptr, *vals = nullptr;
+    const uint32_t *idx = nullptr;
+    const uint64_t *indptr = nullptr;
+    DBuf<float> X_own, vals_own;
+    DBuf<uint32_t> idx_own;
+    DBuf<uint64_t> indptr_own;
+
+    int load(const mc_matrix *m, cudaStream_t st) {
+        if (!m) return fail(MC_EINVAL, "matrix is null");
+        kind = m->kind;
+        n = m->nrows;
+        d = m->ncols;
+        if (n == 0 || d == 0) return fail(MC_EINVAL, "matrix has no rows or no columns");
+        if (n >= (1ull << 32)) return fail(MC_EINVAL, "more than 2^32-1 rows");
+        if (kind == MC_DENSE_F32) {
+            if (!m->values) return fail(MC_EINVAL, "dense matrix without values");
+            return stage(m->values, n * d, X_own, X, st);
+        }
+        if (kind != MC_CSR_F32) return fail(MC_EINVAL, "unknown matrix kind");
+        if (!m->indptr) return fail(MC_EINVAL, "CSR matrix without indptr");
+        nnz = m->nnz;
+        if (nnz && (!m->values || !m->indices)) return fail(MC_EINVAL, "CSR matrix without values/indices");
+        if (d >= (1ull << 32)) return fail(MC_EINVAL, "more than 2^32-1 columns");
+        MC_TRY(stage(m->indptr, n + 1, indptr_own, indptr, st));
+        MC_TRY(stage(m->values, nnz, vals_own, vals, st));
+        MC_TRY(stage(m->indices, nnz, idx_own, idx, st));
+        return validate_csr(indptr, idx, n, d, nnz, st);
+    }
+};
+
+}  // namespace mc
+
+using namespace mc;
+
+struct mc_context {
+    int device = 0;
+    int sms = 152;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+struct mc_job {
+    mc_context *ctx = nullptr;
+    cudaStream_t st = nullptr;
+    DevMatrix M;
+    int msr = SQRL2;
+    double prior = 0.0;
+    int precision = MC_FP32;
+    uint64_t seed = 0, restart_counter = 0;
+    uint32_t k = 0, kp = 0;
+    bool pair = false;
+    bool sparse_path = false;
+    float pv = 0.f;
+    double psum = 0.0;
+    DBuf<double> rowsum, w, costs, csum, consts, det_tmp, scal;
+    DBuf<float> rownorm, rsi, rinc, C, Cw, CT0, CT1, cnorm;
+    DBuf<uint32_t> asn, asn2;
+    DBuf<int> flag;
+    DBuf<uint64_t> idxbuf;
+    SortWork sort;
+    TcState tc;
+    uint64_t last_recheck = 0;
+};
+
+struct mc_sampler {
+    mc_context *ctx = nullptr;
+    uint64_t np = 0, nc = 0, k = 0;
+    int method = MC_BFL;
+    DBuf<float> probs, wf;
+    DBuf<double> prob_tab, cost_d, wt_d;
+    DBuf<uint32_t> alias, asn;
+    AliasWork aw;
+    SensWork sw;
+    SampleWork smp;
+};
+
+namespace {
+
+int sync(cudaStream_t st) {
+    MC_CUDA_TRY(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+// the assignment pass with the centers in `C` (center sums / transforms refreshed here)
+int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exact) {
+    const uint64_t n = j->M.n, d = j->M.d;
+    MC_TRY(launch_center_sums(C, j->k, d, j->csum.p, j->cnorm.p, j->st));
+    const bool csr = j->M.kind == MC_CSR_F32;
+    const bool tc = !csr && !force_exact && j->msr == SQRL2 && j->precision != MC_FP32;
+    if (tc) {
+        MC_TRY(tc_assign(j->tc, j->M.X, n, d, C, j->cnorm.p, j->k, j->precision, j->rownorm.p, j->asn.p,
+                         j->costs.p, j->ctx->sms, j->st, &j->last_recheck));
+        return MC_OK;
+    }
+    j->last_recheck = 0;
+    AssignArgs a;
+    a.msr = j->msr;
+    a.n = n;
+    a.d = d;
+    a.k = j->k;
+    a.X = j->M.X;
+    a.vals = j->M.vals;
+    a.idx = j->M.idx;
+    a.indptr = j->M.indptr;
+    a.rowsum = j->rowsum.p;
+    a.rsi = j->rsi.p;
+    a.rinc = j->rinc.p;
+    a.csum = j->csum.p;
+    a.pv = j->pv;
+    a.prior = j->prior;
+    a.prior_sum = prior_sum;
+    a.asn = j->asn.p;
+    a.costs = j->costs.p;
+    const bool sparse = csr && j->sparse_path;
+    a.kp = sparse ? sparse_center_pad(j->k) : tiled_center_pad(j->k, j->pair, j->msr);
+    MC_TRY(j->CT0.alloc(uint64_t(a.kp) * d, j->st));
+    if (!j->pair && (j->msr == MKL || j->msr == JSD)) MC_TRY(j->CT1.alloc(uint64_t(a.kp) * d, j->st));
+    a.CT0 = j->CT0.p;
+    a.CT1 = (!j->pair && (j->msr == MKL || j->msr == JSD)) ? j->CT1.p : nullptr;
+    if (sparse) {
+        MC_TRY(j->consts.alloc(uint64_t(j->k) * 4, j->st));
+        a.consts = j->consts.p;
+    }
+    MC_TRY(launch_prep_centers(a, C, j->pair, sparse, j->st));
+    if (sparse) return launch_assign_sparse(a, j->st, j->ctx->sms);
+    return launch_assign_tiled(a, csr, j->pair, j->st);
+}
+
+int job_cost(mc_job *j, float *out) {
+    DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, j->M.n};
+    MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, j->st));
+    double s = 0.0;
+    MC_CUDA_TRY(cudaMemcpyAsync(&s, j->scal.p, sizeof(double), cudaMemcpyDeviceToHost, j->st));
+    MC_TRY(sync(j->st));
+    *out = float(s);
+    return MC_OK;
+}
+
+__global__ void k_count_keys(const uint32_t *keys, uint64_t n, uint32_t k, uint64_t *cnt) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x))
+        atomicAdd((unsigned long long *)&cnt[keys[i]], 1ull);
+}
+
+__global__ void k_copy_row_dense(const float *X, uint64_t d, const uint64_t *r, float *dst) {
+    for (uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; j < d; j += gridDim.x * uint64_t(blockDim.x))
+        dst[j] = X[*r * d + j];
+}
+__global__ void k_copy_row_csr_zero(uint64_t d, float *dst) {
+    for (uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; j < d; j += gridDim.x * uint64_t(blockDim.x))
+        dst[j] = 0.f;
+}
+__global__ void k_copy_row_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, const uint64_t *r,
+                               float *dst) {
+    for (uint64_t p = indptr[*r] + blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; p < indptr[*r + 1];
+         p += gridDim.x * uint64_t(blockDim.x))
+        dst[idx[p]] = vals[p];
+}
+
+// set_centroids_full_mean (centroid.h:649-779); returns 1 if a center was restarted
+int job_set_centroids(mc_job *j, int *restarted) {
+    const uint64_t n = j->M.n, d = j->M.d;
+    const uint32_t k = j->k;
+    cudaStream_t st = j->st;
+    *restarted = 0;
+    MC_TRY(j->idxbuf.alloc(uint64_t(k) + 2, st));
+    MC_CUDA_TRY(cudaMemsetAsync(j->idxbuf.p, 0, (uint64_t(k) + 2) * sizeof(uint64_t), st));
+    k_count_keys<<<unsigned(umin64((n + 255) / 256, uint64_t(j->ctx->sms) * 16)), 256, 0, st>>>(j->asn.p, n, k,
+                                                                                                  j->idxbuf.p), note_launch();
+    std::vector<uint64_t> cnt(k);
+    MC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), j->idxbuf.p, k * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MC_TRY(sync(st));
+    std::vector<uint32_t> empty;
+    for (uint32_t c = 0; c < k; ++c)
+        if (cnt[c] == 0) empty.push_back(c);
+    const uint32_t *keys2 = nullptr;
+    uint64_t extra = 0;
+    if (!empty.empty()) {
+        *restarted = 1;
+        // D^2 draws over the current costs, one per empty center, all from the same costs
+        std::vector<uint64_t> rsel;
+        for (uint32_t id : empty) {
+            const double u = uniform_at(j->seed, j->restart_counter++);
+            DetInput in{DET_F64, j->costs.p, nullptr, nullptr, n};
+            MC_TRY(launch_det_draw(in, j->det_tmp.p, nullptr, u, 0, nullptr, j->idxbuf.p + k, st));
+            uint64_t r = 0;
+            MC_CUDA_TRY(cudaMemcpyAsync(&r, j->idxbuf.p + k, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            MC_TRY(sync(st));
+            rsel.push_back(r);
+            float *dst = j->Cw.p + uint64_t(id) * d;
+            if (j->M.kind == MC_DENSE_F32) {
+                k_copy_row_dense<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(j->M.X, d, j->idxbuf.p + k,
+                                                                                          dst), note_launch();
+            } else {
+                k_copy_row_csr_zero<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(d, dst), note_launch();
+                k_copy_row_csr<<<64, 256, 0, st>>>(j->M.vals, j->M.idx, j->M.indptr, j->idxbuf.p + k, dst), note_launch();
+            }
+            MC_CUDA_TRY(cudaGetLastError());
+        }
+        // full exact reassignment (the reference passes prior[0] as the prior sum here)
+        MC_TRY(job_assign_with(j, j->Cw.p, double(float(j->prior)), true));
+        MC_TRY(j->asn2.alloc(n, st));
+        MC_CUDA_TRY(cudaMemsetAsync(j->asn2.p, 0xff, n * sizeof(uint32_t), st));
+        std::vector<uint32_t> cur(rsel.size());
+        for (size_t e = 0; e < rsel.size(); ++e)
+            MC_CUDA_TRY(cudaMemcpyAsync(&cur[e], j->asn.p + rsel[e], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        MC_TRY(sync(st));
+        const double zero = 0.0;
+        for (size_t e = 0; e < rsel.size(); ++e) {
+            const uint64_t pid = rsel[e];
+            const uint32_t cid = empty[e];
+            uint32_t now = cur[e];
+            for (size_t e2 = 0; e2 < e; ++e2)
+                if (rsel[e2] == pid) now = empty[e2];
+            if (now != cid) {
+                // the row stays in its previous bucket too (centroid.h:743-751)
+                MC_CUDA_TRY(cudaMemcpyAsync(j->asn2.p + pid, &now, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+                MC_CUDA_TRY(cudaMemcpyAsync(j->asn.p + pid, &cid, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+                MC_CUDA_TRY(cudaMemcpyAsync(j->costs.p + pid, &zero, sizeof(double), cudaMemcpyHostToDevice, st));
+                MC_TRY(sync(st));
+                ++extra;
+            }
+        }
+        if (extra) keys2 = j->asn2.p;
+    }
+    CentroidArgs ca;
+    ca.csr = j->M.kind == MC_CSR_F32;
+    ca.n = n;
+    ca.d = d;
+    ca.k = k;
+    ca.X = j->M.X;
+    ca.vals = j->M.vals;
+    ca.idx = j->M.idx;
+    ca.indptr = j->M.indptr;
+    ca.keys = j->asn.p;
+    ca.keys2 = keys2;
+    ca.extra_members = extra;
+    ca.w = j->w.p;
+    ca.centers = j->Cw.p;
+    ca.nan_flag = j->flag.p;
+    MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), st));
+    MC_TRY(launch_centroids(ca, j->sort, st));
+    int nanf = 0;
+    MC_CUDA_TRY(cudaMemcpyAsync(&nanf, j->flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MC_TRY(sync(st));
+    if (nanf) return fail(MC_ENAN, "Unexpected nan in ctr");
+    return MC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mc_version(void) { return "minicore_gb300 0.1 (sm_103a)"; }
+uint64_t mc_kernel_launches(void) { return g_launches.load(); }
+const char *mc_last_error(void) { return g_last_error.c_str(); }
+
+int mc_uniforms(uint64_t seed, uint64_t offset, uint64_t m, double *out) {
+    if (!out && m) return fail(MC_EINVAL, "out is null");
+    for (uint64_t i = 0; i < m; ++i) out[i] = uniform_at(seed, offset + i);
+    return MC_OK;
+}
+
+int mc_context_create(int device, mc_context **out) {
+    if (!out) return fail(MC_EINVAL, "out is null");
+    int ndev = 0;
+    MC_CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(MC_EINVAL, "no such CUDA device");
+    MC_CUDA_TRY(cudaSetDevice(device));
+    auto *c = new mc_context();
+    c->device = device;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) c->sms = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return fail(MC_ECUDA, "stream creation failed");
+    }
+    c->stream = c->own;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    *out = c;
+    return MC_OK;
+}
+
+int mc_context_destroy(mc_context *ctx) {
+    if (!ctx) return MC_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return MC_OK;
+}
+
+int mc_context_set_stream(mc_context *ctx, void *s) {
+    if (!ctx) return fail(MC_EINVAL, "ctx is null");
+    ctx->stream = s ? (cudaStream_t)s : ctx->own;
+    return MC_OK;
+}
+
+int mc_context_synchronize(mc_context *ctx) {
+    if (!ctx) return fail(MC_EINVAL, "ctx is null");
+    MC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// jobs
+// ------------------------------------------------------------------------------------
+int mc_job_create(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_t k, int msr, double prior,
+                  const double *weights, int precision, uint64_t seed, mc_job **out) {
+    if (!ctx || !out) return fail(MC_EINVAL, "null context or output");
+    if (!measure_supported(msr)) return fail(MC_EUNSUPPORTED, "measure not implemented on this path");
+    if (precision != MC_FP32 && precision != MC_TF32 && precision != MC_BF16)
+        return fail(MC_EINVAL, "unknown precision");
+    if (k == 0 || !centers) return fail(MC_EINVAL, "no centers");
+    MC_CUDA_TRY(cudaSetDevice(ctx->device));
+    std::unique_ptr<mc_job> j(new mc_job());
+    j->ctx = ctx;
+    j->st = ctx->stream;
+    cudaStream_t st = j->st;
+    MC_TRY(j->M.load(X, st));
+    if (precision != MC_FP32 && (msr != SQRL2 || j->M.kind != MC_DENSE_F32))
+        return fail(MC_EUNSUPPORTED, "BF16/TF32 tensor-core assignment covers dense SQRL2 only");
+    const uint64_t n = j->M.n, d = j->M.d;
+    j->msr = msr;
+    j->prior = prior;
+    j->precision = precision;
+    j->seed = seed;
+    j->k = k;
+    j->psum = double(float(prior * double(d)));
+    MC_TRY(j->rowsum.alloc(n, st));
+    MC_TRY(j->costs.alloc(n, st));
+    MC_TRY(j->asn.alloc(n, st));
+    MC_TRY(j->C.alloc(uint64_t(k) * d, st));
+    MC_TRY(j->Cw.alloc(uint64_t(k) * d, st));
+    MC_TRY(j->csum.alloc(k, st));
+    MC_TRY(j->cnorm.alloc(k, st));
+    MC_TRY(j->det_tmp.alloc(det_chunks(n) + 1, st));
+    MC_TRY(j->scal.alloc(4, st));
+    MC_TRY(j->flag.alloc(1, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(j->C.p, centers, uint64_t(k) * d * sizeof(float), cudaMemcpyDefault, st));
+    if (weights) {
+        MC_TRY(j->w.alloc(n, st));
+        MC_CUDA_TRY(cudaMemcpyAsync(j->w.p, weights, n * sizeof(double), cudaMemcpyDefault, st));
+    }
+    if (j->M.kind == MC_DENSE_F32) {
+        MC_TRY(j->rownorm.alloc(n, st));
+        MC_TRY(launch_row_sums_dense(j->M.X, n, d, j->rowsum.p, j->rownorm.p, st));
+    } else {
+        MC_TRY(launch_row_sums_csr(j->M.vals, j->M.indptr, n, j->rowsum.p, st));
+    }
+    // constant-prior check: pv == prior for every pair when prior >= smallest_pv at the
+    // largest row and center sums (centers are means or rows, so bounded by the rows)
+    if (msr != SQRL2) {
+        MC_TRY(launch_center_sums(j->C.p, k, d, j->csum.p, j->cnorm.p, st));
+        std::vector<double> rs(n), cs(k);
+        MC_CUDA_TRY(cudaMemcpyAsync(rs.data(), j->rowsum.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MC_CUDA_TRY(cudaMemcpyAsync(cs.data(), j->csum.p, k * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MC_TRY(sync(st));
+        double mr = rs.empty() ? 0.0 : *std::max_element(rs.begin(), rs.end());
+        const double mc_ = cs.empty() ? 0.0 : *std::max_element(cs.begin(), cs.end());
+        mr = std::max(mr, mc_);
+        const float fp = float(prior);
+        const float s0 = float(mr + j->psum);
+        const float smallest = 7.0069e-42f * (s0 + s0);
+        j->pair = !(fp > 0.f) || (fp < smallest);
+        j->pv = fp;
+        if (!j->pair) {
+            MC_TRY(j->rsi.alloc(n, st));
+            MC_TRY(j->rinc.alloc(n, st));
+            MC_TRY(launch_row_scalars(j->rowsum.p, n, d, j->pv, j->rsi.p, j->rinc.p, st));
+        }
+    }
+    j->sparse_path = j->M.kind == MC_CSR_F32 && !j->pair && msr != JSD;
+    *out = j.release();
+    return MC_OK;
+}
+
+int mc_job_destroy(mc_job *job) {
+    if (!job) return MC_OK;
+    cudaStreamSynchronize(job->st);
+    delete job;
+    return MC_OK;
+}
+
+int mc_job_assign(mc_job *j) {
+    if (!j) return fail(MC_EINVAL, "job is null");
+    return job_assign_with(j, j->C.p, j->psum, false);
+}
+
+int mc_job_cost(mc_job *j, double *cost) {
+    if (!j || !cost) return fail(MC_EINVAL, "null argument");
+    float c = 0.f;
+    MC_TRY(job_cost(j, &c));
+    *cost = c;
+    return MC_OK;
+}
+
+int mc_job_lloyd_step(mc_job *j, int *restarted) {
+    if (!j) return fail(MC_EINVAL, "job is null");
+    int res = 0;
+    MC_CUDA_TRY(cudaMemcpyAsync(j->Cw.p, j->C.p, uint64_t(j->k) * j->M.d * sizeof(float), cudaMemcpyDeviceToDevice,
+                                j->st));
+    MC_TRY(job_set_centroids(j, &res));
+    MC_TRY(job_assign_with(j, j->Cw.p, j->psum, false));
+    std::swap(j->C.p, j->Cw.p);
+    std::swap(j->C.n, j->Cw.n);
+    if (restarted) *restarted = res;
+    return MC_OK;
+}
+
+int mc_job_run(mc_job *j, double eps, uint64_t maxiter, double *initcost_out, double *finalcost_out,
+               uint64_t *numiter_out) {
+    if (!j) return fail(MC_EINVAL, "job is null");
+    MC_TRY(job_assign_with(j, j->C.p, j->psum, false));
+    float initcost = 0.f;
+    MC_TRY(job_cost(j, &initcost));
+    float cost = initcost;
+    uint64_t iternum = 0;
+    if (cost == 0.f) {
+        if (initcost_out) *initcost_out = 0.0;
+        if (finalcost_out) *finalcost_out = 0.0;
+        if (numiter_out) *numiter_out = 0;
+        return MC_OK;
+    }
+    const size_t cbytes = uint64_t(j->k) * j->M.d * sizeof(float);
+    MC_CUDA_TRY(cudaMemcpyAsync(j->Cw.p, j->C.p, cbytes, cudaMemcpyDeviceToDevice, j->st));
+    for (;;) {
+        int res = 0;
+        MC_TRY(job_set_centroids(j, &res));
+        MC_TRY(job_assign_with(j, j->Cw.p, j->psum, false));
+        float newcost = 0.f;
+        MC_TRY(job_cost(j, &newcost));
+        if (newcost > cost && !res) {
+            MC_TRY(job_assign_with(j, j->C.p, j->psum, false));
+            break;
+        }
+        MC_CUDA_TRY(cudaMemcpyAsync(j->C.p, j->Cw.p, cbytes, cudaMemcpyDeviceToDevice, j->st));
+        ++iternum;
+        const float oldcost = cost;
+        cost = newcost;
+        if (double(oldcost - newcost) < eps * std::max(double(newcost), double(oldcost)) || iternum > maxiter) break;
+    }
+    MC_TRY(sync(j->st));
+    if (initcost_out) *initcost_out = initcost;
+    if (finalcost_out) *finalcost_out = cost;
+    if (numiter_out) *numiter_out = iternum;
+    return MC_OK;
+}
+
+int mc_job_read(mc_job *j, float *centers, uint32_t *asn, double *costs) {
+    if (!j) return fail(MC_EINVAL, "job is null");
+    MC_TRY(copy_out(centers, j->C.p, uint64_t(j->k) * j->M.d, j->st));
+    MC_TRY(copy_out(asn, j->asn.p, j->M.n, j->st));
+    MC_TRY(copy_out(costs, j->costs.p, j->M.n, j->st));
+    MC_TRY(sync(j->st));
+    return MC_OK;
+}
+
+int mc_job_recheck_count(mc_job *j, uint64_t *count) {
+    if (!j || !count) return fail(MC_EINVAL, "null argument");
+    *count = j->last_recheck;
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// one-shot entry points
+// ------------------------------------------------------------------------------------
+int mc_assign(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_t k, int msr, double prior,
+              int precision, uint32_t *asn, double *costs) {
+    mc_job *j = nullptr;
+    MC_TRY(mc_job_create(ctx, X, centers, k, msr, prior, nullptr, precision, 0, &j));
+    std::unique_ptr<mc_job> guard(j);
+    MC_TRY(mc_job_assign(j));
+    return mc_job_read(j, nullptr, asn, costs);
+}
+
+int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr, double prior,
+                const double *weights, double eps, uint64_t maxiter, uint64_t seed, int precision,
+                float *centers_out, uint32_t *asn, double *costs, double *initcost, double *finalcost,
+                uint64_t *numiter) {
+    mc_job *j = nullptr;
+    MC_TRY(mc_job_create(ctx, X, centers_in, k, msr, prior, weights, precision, seed, &j));
+    std::unique_ptr<mc_job> guard(j);
+    MC_TRY(mc_job_run(j, eps, maxiter, initcost, finalcost, numiter));
+    return mc_job_read(j, centers_out, asn, costs);
+}
+
+int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
+                const double *uniforms, uint32_t *center_ids, uint32_t *asn, double *costs) {
+    if (!ctx) return fail(MC_EINVAL, "ctx is null");
+    if (!measure_supported(msr)) return fail(MC_EUNSUPPORTED, "measure not implemented on this path");
+    if (!uniforms) return fail(MC_EINVAL, "uniforms is null");
+    MC_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    DevMatrix M;
+    MC_TRY(M.load(X, st));
+    const uint64_t n = M.n, d = M.d;
+    if (k == 0) return fail(MC_EINVAL, "k must be positive");
+    if (k > n) k = uint32_t(n);
+    DBuf<double> rowsum, dist, u, w, tmp;
+    DBuf<float> cbuf, rn;
+    DBuf<uint32_t> asnb, ids;
+    DBuf<uint64_t> newc;
+    MC_TRY(rowsum.alloc(n, st));
+    MC_TRY(dist.alloc(n, st));
+    MC_TRY(u.alloc(k, st));
+    MC_TRY(tmp.alloc(det_chunks(n) + 1, st));
+    MC_TRY(cbuf.alloc(d, st));
+    MC_TRY(asnb.alloc(n, st));
+    MC_TRY(ids.alloc(k, st));
+    MC_TRY(newc.alloc(1, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(u.p, uniforms, k * sizeof(double), cudaMemcpyDefault, st));
+    if (weights) {
+        MC_TRY(w.alloc(n, st));
+        MC_CUDA_TRY(cudaMemcpyAsync(w.p, weights, n * sizeof(double), cudaMemcpyDefault, st));
+    }
+    if (M.kind == MC_DENSE_F32) MC_TRY(launch_row_sums_dense(M.X, n, d, rowsum.p, nullptr, st));
+    else MC_TRY(launch_row_sums_csr(M.vals, M.indptr, n, rowsum.p, st));
+    KmppArgs a;
+    a.msr = msr;
+    a.csr = M.kind == MC_CSR_F32;
+    a.n = n;
+    a.d = d;
+    a.k = k;
+    a.X = M.X;
+    a.vals = M.vals;
+    a.idx = M.idx;
+    a.indptr = M.indptr;
+    a.rowsum = rowsum.p;
+    a.w = w.p;
+    a.prior = prior;
+    a.prior_sum = prior * double(d);
+    a.cbuf = cbuf.p;
+    a.dist = dist.p;
+    a.asn = asnb.p;
+    a.center_ids = ids.p;
+    a.newc = newc.p;
+    MC_TRY(run_kmeanspp(a, u.p, tmp.p, ctx->sms, st));
+    MC_TRY(copy_out(center_ids, ids.p, k, st));
+    MC_TRY(copy_out(asn, asnb.p, n, st));
+    MC_TRY(copy_out(costs, dist.p, n, st));
+    MC_CUDA_TRY(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// coreset sampler
+// ------------------------------------------------------------------------------------
+__global__ void k_widen_costs(const float *c, uint64_t n, double *out) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x))
+        out[i] = double(c[i]);
+}
+
+int mc_sampler_create(mc_context *ctx, uint64_t np, uint64_t ncenters, uint64_t k, const void *costs, int costs_f64,
+                      const uint32_t *asn, const float *weights, int method, double alpha_est, mc_sampler **out) {
+    if (!ctx || !out) return fail(MC_EINVAL, "null context or output");
+    if (np == 0 || ncenters == 0 || !costs || !asn) return fail(MC_EINVAL, "empty input");
+    if (method < MC_BFL || method > MC_LBK) return fail(MC_EINVAL, "Invalid SensitivityMethod");
+    if (np >= (1ull << 32)) return fail(MC_EINVAL, "more than 2^32-1 points");
+    MC_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    std::unique_ptr<mc_sampler> s(new mc_sampler());
+    s->ctx = ctx;
+    s->np = np;
+    s->nc = ncenters;
+    s->k = k ? k : ncenters;
+    s->method = method;
+    MC_TRY(s->cost_d.alloc(np, st));
+    if (costs_f64) {
+        MC_CUDA_TRY(cudaMemcpyAsync(s->cost_d.p, costs, np * sizeof(double), cudaMemcpyDefault, st));
+    } else {
+        DBuf<float> cf;
+        const float *cp = nullptr;
+        MC_TRY(stage((const float *)costs, np, cf, cp, st));
+        k_widen_costs<<<unsigned(umin64((np + 255) / 256, 65535)), 256, 0, st>>>(cp, np, s->cost_d.p), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        MC_TRY(sync(st));
+    }
+    MC_TRY(s->asn.alloc(np, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(s->asn.p, asn, np * sizeof(uint32_t), cudaMemcpyDefault, st));
+    if (weights) {
+        MC_TRY(s->wf.alloc(np, st));
+        MC_TRY(s->wt_d.alloc(np, st));
+        MC_CUDA_TRY(cudaMemcpyAsync(s->wf.p, weights, np * sizeof(float), cudaMemcpyDefault, st));
+        MC_TRY(launch_to_double(s->wf.p, np, s->wt_d.p, st));
+    }
+    MC_TRY(s->probs.alloc(np, st));
+    SensInput in;
+    in.method = method;
+    in.n = np;
+    in.nc = uint32_t(ncenters);
+    in.k = s->k;
+    in.alpha_est = alpha_est;
+    in.cost = s->cost_d.p;
+    in.wt = weights ? s->wt_d.p : nullptr;
+    in.asn = s->asn.p;
+    in.probs = s->probs.p;
+    MC_TRY(compute_sensitivities(in, s->sw, st, ctx->sms));
+    MC_TRY(s->prob_tab.alloc(np, st));
+    MC_TRY(s->alias.alloc(np, st));
+    MC_TRY(build_alias(s->probs.p, np, s->prob_tab.p, s->alias.p, s->aw, st, ctx->sms));
+    MC_TRY(sync(st));
+    *out = s.release();
+    return MC_OK;
+}
+
+int mc_sampler_destroy(mc_sampler *s) {
+    if (!s) return MC_OK;
+    cudaStreamSynchronize(s->ctx->stream);
+    delete s;
+    return MC_OK;
+}
+
+int mc_sampler_probs(mc_sampler *s, float *probs) {
+    if (!s || !probs) return fail(MC_EINVAL, "null argument");
+    MC_TRY(copy_out(probs, s->probs.p, s->np, s->ctx->stream));
+    return sync(s->ctx->stream);
+}
+
+int mc_sampler_alias(mc_sampler *s, double *prob_table, uint32_t *alias_table) {
+    if (!s) return fail(MC_EINVAL, "null argument");
+    MC_TRY(copy_out(prob_table, s->prob_tab.p, s->np, s->ctx->stream));
+    MC_TRY(copy_out(alias_table, s->alias.p, s->np, s->ctx->stream));
+    return sync(s->ctx->stream);
+}
+
+int mc_sampler_sample(mc_sampler *s, uint64_t m, uint64_t seed, int unique, float *weights, uint64_t *indices) {
+    if (!s || !weights || !indices) return fail(MC_EINVAL, "null argument");
+    if (m == 0) return MC_OK;
+    cudaStream_t st = s->ctx->stream;
+    DBuf<float> wo;
+    DBuf<uint64_t> io;
+    MC_TRY(wo.alloc(m, st));
+    MC_TRY(io.alloc(m, st));
+    SampleArgs a;
+    a.np = s->np;
+    a.m = m;
+    a.direct = (s->method == MC_FL) ? (m > s->nc ? m - s->nc : 0) : m;
+    a.seed = seed;
+    a.unique = unique;
+    a.probs = s->probs.p;
+    a.prob_tab = s->prob_tab.p;
+    a.alias_tab = s->alias.p;
+    a.wf = s->wf.p;
+    a.w_out = wo.p;
+    a.idx_out = io.p;
+    MC_TRY(run_sample(a, s->smp, st, s->ctx->sms));
+    MC_TRY(copy_out(weights, wo.p, m, st));
+    MC_TRY(copy_out(indices, io.p, m, st));
+    return sync(st);
+}
+
+}  // extern "C"

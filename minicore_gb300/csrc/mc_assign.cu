@@ -1,0 +1,596 @@
+// Hard assignment kernels: argmin over centers of cmp::msr_with_prior
+// (include/minicore/clustering/solve.h:234-285, include/minicore/dist/applicator.h:1632-1915).
+//
+// k_assign_tiled   FP32 CUDA-core tiles of BM rows x BN centers, the column loop sequential
+//                  per pair (bit-identical to the oracle's dense path).  Rows come from a
+//                  dense matrix or from CSR rows densified in the tile loader (the exact
+//                  O(d)-per-pair form used for JSD and for the pair-dependent prior).
+// k_assign_sparse  CSR rows, one warp per row: for the measures whose sum over the zero
+//                  columns of a row folds into per-center constants (SQRL2, L1, MKL,
+//                  Hellinger), only the row's nonzeros are visited:
+//                    MKL:  H_c - log(rhinc) A_c + sum_nz a_j (log rhinc - log b_j)
+//                    HELL: A_c + B_x - 2 sqrt(rhinc) Q_c + 2 sum_nz sqrt(a_j)(sqrt(rhinc) - sqrt(b_j))
+//                    SQRL2: |c|^2 + sum_nz x_j (x_j - 2 c_j)
+//                    L1:   E_c + sum_nz (|c'_j - x'_j| - |c'_j - pv|),  c' = c + pv, x' = x + pv
+// The pair scalars (pv, lhrsi, lhinc, rhrsi, rhinc) follow applicator.h:1642-1656.  When
+// pv is the same for every pair ("constant prior", any prior > 0 in practice) the
+// center-side and row-side transforms are precomputed; otherwise (prior 0) every pair
+// recomputes them ("pair mode").
+#include "mc_assign.cuh"
+
+namespace mc {
+
+// ------------------------------------------------------------------------------------
+// center preparation
+// ------------------------------------------------------------------------------------
+// CT0/CT1: [d][kp] transposed center transforms; consts: per-center FP64 constants
+//   consts[c*4+0]: MKL H_c = sum a log a | HELL A_c | SQRL2 |c|^2 | L1 E_c
+//   consts[c*4+1]: MKL A_c = sum a      | HELL Q_c = sum sqrt(a)
+template <int MSR, bool PAIR>
+__global__ void k_prep_centers(const float *__restrict__ C, uint32_t k, uint32_t kp, uint64_t d,
+                               const double *__restrict__ csum, float pv, float *CT0, float *CT1) {
+    const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (j >= d) return;
+    for (uint32_t c = blockIdx.y; c < kp; c += gridDim.y) {
+    float v0 = 0.f, v1 = 0.f;
+    if (c < k) {
+        const float x = C[uint64_t(c) * d + j];
+        if (PAIR || MSR == SQRL2) {
+            v0 = x;
+        } else {
+            float rsi, inc;
+            side_scalars(pv, csum[c], d, rsi, inc);
+            if (MSR == L1) v0 = x + pv;
+            else if (MSR == HELLINGER) v0 = sqrtf(x * rsi + inc);
+            else {
+                const float a = x * rsi + inc;
+                v0 = a;
+                v1 = (MSR == MKL) ? logf(a) : a * logf(a);
+            }
+        }
+    }
+    CT0[j * kp + c] = v0;
+    if (CT1) CT1[j * kp + c] = v1;
+    }
+}
+
+// per-center FP64 constants for the sparse-dot kernels (sequential over columns)
+template <int MSR>
+__global__ void k_center_consts(const float *__restrict__ C, uint32_t k, uint64_t d, const double *__restrict__ csum,
+                                float pv, double *consts) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    float rsi = 0.f, inc = 0.f;
+    if (MSR != SQRL2) side_scalars(pv, csum[c], d, rsi, inc);
+    double s0 = 0.0, s1 = 0.0;
+    const float *r = C + uint64_t(c) * d;
+    for (uint64_t j = 0; j < d; ++j) {
+        const float x = r[j];
+        if (MSR == SQRL2) {
+            s0 = s0 + double(x) * double(x);
+        } else if (MSR == L1) {
+            s0 = s0 + double(fabsf((x + pv) - pv));
+        } else {
+            const float a = x * rsi + inc;
+            if (MSR == MKL) {
+                s0 = s0 + double(a) * double(logf(a));
+                s1 = s1 + double(a);
+            } else {  // HELLINGER
+                s0 = s0 + double(a);
+                s1 = s1 + double(sqrtf(a));
+            }
+        }
+    }
+    consts[uint64_t(c) * 4 + 0] = s0;
+    consts[uint64_t(c) * 4 + 1] = s1;
+}
+
+// row-side scalars for the constant-prior path
+__global__ void k_row_scalars(const double *__restrict__ rowsum, uint64_t n, uint64_t d, float pv, float *rsi,
+                              float *rinc) {
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    float a, b;
+    side_scalars(pv, rowsum[i], d, a, b);
+    rsi[i] = a;
+    rinc[i] = b;
+}
+
+// ------------------------------------------------------------------------------------
+// argmin bookkeeping: lexicographic (value, index); NaN at center 0 wins (the reference's
+// sequential scan then never moves off center 0), NaN elsewhere never wins.
+// ------------------------------------------------------------------------------------
+struct Best {
+    float v;
+    uint32_t j;
+};
+
+__device__ inline void best_init(Best &b) {
+    b.v = __int_as_float(0x7f800000);
+    b.j = 0xffffffffu;
+}
+
+__device__ inline void best_offer(Best &b, float v, uint32_t j) {
+    if (v != v) {
+        if (j != 0) return;
+        v = __int_as_float(0xff800000);  // -inf marks "NaN at center 0"
+    }
+    if (v < b.v || (v == b.v && j < b.j)) {
+        b.v = v;
+        b.j = j;
+    }
+}
+
+__device__ inline void best_merge_shfl(Best &b, int lanemask_xor) {
+    const float ov = __shfl_xor_sync(0xffffffffu, b.v, lanemask_xor);
+    const uint32_t oj = __shfl_xor_sync(0xffffffffu, b.j, lanemask_xor);
+    if (ov < b.v || (ov == b.v && oj < b.j)) {
+        b.v = ov;
+        b.j = oj;
+    }
+}
+
+// final value of a pair: compare key (float) and cost (double) per measure
+template <int MSR>
+__device__ inline float finish_key(float acc) {
+    if (MSR == SQRL2) return acc;
+    if (MSR == L1) return acc * 0.5f;
+    if (MSR == HELLINGER) return sqrtf(acc);
+    if (MSR == MKL) return post_divergence(acc);
+    return post_divergence(acc * 0.5f);  // JSD
+}
+
+template <int MSR>
+__device__ inline double key_to_cost(float key) {
+    if (MSR == L1) return double(key) * 2.0;
+    if (MSR == HELLINGER) return double(key) * kSqrt1_2;
+    return double(key);
+}
+
+// ------------------------------------------------------------------------------------
+// tiled kernel
+// ------------------------------------------------------------------------------------
+constexpr int kBK = 16;
+
+template <int MSR>
+struct Ops {
+    static constexpr bool two_center = (MSR == MKL || MSR == JSD);
+    static constexpr bool two_row = (MSR == JSD);
+};
+
+// element step.  c0/c1: center-side values, x0/x1: row-side values (constant-prior
+// transforms), or raw values + pair scalars in pair mode.
+template <int MSR, bool PAIR>
+__device__ inline void elem(float &acc, float c0, float c1, float x0, float x1, const PairScalars &s) {
+    if (!PAIR) {
+        if (MSR == SQRL2 || MSR == HELLINGER) {
+            const float df = c0 - x0;
+            acc = fmaf(df, df, acc);
+        } else if (MSR == L1) {
+            acc = acc + fabsf(c0 - x0);
+        } else if (MSR == MKL) {
+            acc = fmaf(c0, c1 - x0, acc);
+        } else {  // JSD: c0 = a, c1 = a log a, x0 = b, x1 = b log b
+            const float m = c0 + x0;
+            const float t = (c1 + x1) - m * logf(m * 0.5f);
+            acc = acc + t;
+        }
+    } else {
+        if (MSR == SQRL2) {
+            const float df = c0 - x0;
+            acc = fmaf(df, df, acc);
+        } else if (MSR == L1) {
+            const float a = c0 + s.pv, b = x0 + s.pv;
+            acc = acc + fabsf(a - b);
+        } else if (MSR == HELLINGER) {
+            const float a = sqrtf(c0 * s.lhrsi + s.lhinc), b = sqrtf(x0 * s.rhrsi + s.rhinc);
+            const float df = a - b;
+            acc = fmaf(df, df, acc);
+        } else if (MSR == MKL) {
+            const float a = c0 * s.lhrsi + s.lhinc, b = x0 * s.rhrsi + s.rhinc;
+            acc = fmaf(a, logf(a) - logf(b), acc);
+        } else {
+            const float a = c0 * s.lhrsi + s.lhinc, b = x0 * s.rhrsi + s.rhinc;
+            const float m = a + b;
+            const float t = (a * logf(a) + b * logf(b)) - m * logf(m * 0.5f);
+            acc = acc + t;
+        }
+    }
+}
+
+// row-side transform of a raw value x for the constant-prior path
+template <int MSR>
+__device__ inline void row_xform(float x, float pv, float rsi, float rinc, float &x0, float &x1) {
+    if (MSR == SQRL2) { x0 = x; x1 = 0.f; }
+    else if (MSR == L1) { x0 = x + pv; x1 = 0.f; }
+    else if (MSR == HELLINGER) { x0 = sqrtf(x * rsi + rinc); x1 = 0.f; }
+    else {
+        const float b = x * rsi + rinc;
+        if (MSR == MKL) { x0 = logf(b); x1 = 0.f; }
+        else { x0 = b; x1 = b * logf(b); }
+    }
+}
+
+template <int MSR, bool PAIR, int TM, int TN, bool CSR>
+__global__ void __launch_bounds__(256) k_assign_tiled(AssignArgs a) {
+    constexpr int BM = 16 * TM, BN = 16 * TN;
+    constexpr bool C2 = !PAIR && Ops<MSR>::two_center;
+    constexpr bool R2 = !PAIR && Ops<MSR>::two_row;
+    __shared__ float Xs0[BM][kBK + 1];
+    __shared__ float Xs1[R2 ? BM : 1][kBK + 1];
+    __shared__ __align__(16) float Cs0[kBK][BN];
+    __shared__ __align__(16) float Cs1[C2 ? kBK : 1][C2 ? BN : 4];
+    __shared__ uint64_t cursor[CSR ? BM : 1];
+
+    const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
+    const uint64_t row0 = uint64_t(blockIdx.x) * BM;
+    const uint64_t d = a.d;
+
+    float rpv = a.pv;
+    Best best[TM];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) best_init(best[i]);
+
+    double rsum_reg[TM];
+    if (PAIR) {
+#pragma unroll
+        for (int i = 0; i < TM; ++i) {
+            const uint64_t r = row0 + ty * TM + i;
+            rsum_reg[i] = r < a.n ? a.rowsum[r] : 0.0;
+        }
+    }
+
+    for (uint32_t cbase = 0; cbase < a.k; cbase += BN) {
+        float acc[TM][TN];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+        PairScalars ps[PAIR ? TM : 1][PAIR ? TN : 1];
+        if (PAIR) {
+#pragma unroll
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) {
+                    const uint32_t c = cbase + tx * TN + j;
+                    const double cs = c < a.k ? a.csum[c] : 0.0;
+                    ps[i][j] = pair_scalars(a.prior, a.prior_sum, rsum_reg[i], cs, d);
+                }
+        }
+        if (CSR) {
+            if (t < BM) {
+                const uint64_t r = row0 + t;
+                cursor[t] = r < a.n ? a.indptr[r] : 0;
+            }
+            __syncthreads();
+        }
+        for (uint64_t k0 = 0; k0 < d; k0 += kBK) {
+            const int kmax = int(umin64(kBK, d - k0));
+            // ---- row tile ----
+            if (!CSR) {
+                for (int e = t; e < BM * kBK; e += 256) {
+                    const int r = e / kBK, kk = e % kBK;
+                    const uint64_t row = row0 + r;
+                    float x = 0.f;
+                    if (row < a.n && kk < kmax) x = a.X[row * d + k0 + kk];
+                    if (PAIR) {
+                        Xs0[r][kk] = x;
+                    } else {
+                        float x0, x1;
+                        const float rsi = (MSR == SQRL2 || MSR == L1 || row >= a.n) ? 0.f : a.rsi[row];
+                        const float rinc = (MSR == SQRL2 || MSR == L1 || row >= a.n) ? 0.f : a.rinc[row];
+                        row_xform<MSR>(x, rpv, rsi, rinc, x0, x1);
+                        Xs0[r][kk] = x0;
+                        if (R2) Xs1[r][kk] = x1;
+                    }
+                }
+            } else {
+                // densify: fill with the transform of 0, then scatter this window's nonzeros
+                for (int e = t; e < BM * kBK; e += 256) {
+                    const int r = e / kBK, kk = e % kBK;
+                    const uint64_t row = row0 + r;
+                    if (PAIR) {
+                        Xs0[r][kk] = 0.f;
+                    } else {
+                        float x0, x1;
+                        const float rsi = (MSR == SQRL2 || MSR == L1 || row >= a.n) ? 0.f : a.rsi[row];
+                        const float rinc = (MSR == SQRL2 || MSR == L1 || row >= a.n) ? 0.f : a.rinc[row];
+                        row_xform<MSR>(0.f, rpv, rsi, rinc, x0, x1);
+                        Xs0[r][kk] = x0;
+                        if (R2) Xs1[r][kk] = x1;
+                    }
+                }
+                __syncthreads();
+                if (t < BM) {
+                    const uint64_t row = row0 + t;
+                    if (row < a.n) {
+                        uint64_t p = cursor[t];
+                        const uint64_t pe = a.indptr[row + 1];
+                        const float rsi = (PAIR || MSR == SQRL2 || MSR == L1) ? 0.f : a.rsi[row];
+                        const float rinc = (PAIR || MSR == SQRL2 || MSR == L1) ? 0.f : a.rinc[row];
+                        while (p < pe) {
+                            const uint64_t col = a.idx[p];
+                            if (col >= k0 + kBK) break;
+                            const float x = a.vals[p];
+                            if (PAIR) {
+                                Xs0[t][col - k0] = x;
+                            } else {
+                                float x0, x1;
+                                row_xform<MSR>(x, rpv, rsi, rinc, x0, x1);
+                                Xs0[t][col - k0] = x0;
+                                if (R2) Xs1[t][col - k0] = x1;
+                            }
+                            ++p;
+                        }
+                        cursor[t] = p;
+                    }
+                }
+            }
+            // ---- center tile (CT is [d][kp]) ----
+            for (int e = t; e < BN * kBK; e += 256) {
+                const int kk = e / BN, c = e % BN;
+                float v0 = 0.f, v1 = 0.f;
+                if (kk < kmax) {
+                    const uint64_t off = (k0 + kk) * a.kp + cbase + c;
+                    v0 = a.CT0[off];
+                    if (C2) v1 = a.CT1[off];
+                }
+                Cs0[kk][c] = v0;
+                if (C2) Cs1[kk][c] = v1;
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int kk = 0; kk < kBK; ++kk) {
+                if (kk < kmax) {
+                    float xv0[TM], xv1[TM];
+#pragma unroll
+                    for (int i = 0; i < TM; ++i) {
+                        xv0[i] = Xs0[ty * TM + i][kk];
+                        xv1[i] = R2 ? Xs1[ty * TM + i][kk] : 0.f;
+                    }
+                    float cv0[TN], cv1[TN];
+#pragma unroll
+                    for (int j = 0; j < TN; ++j) {
+                        cv0[j] = Cs0[kk][tx * TN + j];
+                        cv1[j] = C2 ? Cs1[kk][tx * TN + j] : 0.f;
+                    }
+#pragma unroll
+                    for (int i = 0; i < TM; ++i)
+#pragma unroll
+                        for (int j = 0; j < TN; ++j)
+                            elem<MSR, PAIR>(acc[i][j], cv0[j], cv1[j], xv0[i], xv1[i], ps[PAIR ? i : 0][PAIR ? j : 0]);
+                }
+            }
+            __syncthreads();
+        }
+        // ---- fold this center tile into the running argmin ----
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const uint32_t c = cbase + tx * TN + j;
+            if (c < a.k) {
+#pragma unroll
+                for (int i = 0; i < TM; ++i) best_offer(best[i], finish_key<MSR>(acc[i][j]), c);
+            }
+        }
+    }
+    // reduce across the 16 tx lanes that share rows (same half-warp)
+#pragma unroll
+    for (int i = 0; i < TM; ++i) {
+#pragma unroll
+        for (int m = 8; m >= 1; m >>= 1) best_merge_shfl(best[i], m);
+    }
+    if (tx == 0) {
+#pragma unroll
+        for (int i = 0; i < TM; ++i) {
+            const uint64_t row = row0 + ty * TM + i;
+            if (row < a.n) {
+                const bool nan0 = best[i].v == __int_as_float(0xff800000);
+                double cost = nan0 ? __longlong_as_double(0x7ff8000000000000ll) : key_to_cost<MSR>(best[i].v);
+                if (CSR) cost = double(float(cost));
+                a.asn[row] = best[i].j;
+                a.costs[row] = cost;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// sparse-dot CSR kernel (constant prior; SQRL2, L1, MKL, HELLINGER)
+// one warp per row; lane l owns centers l, l+32, ... of the current group of 32*KPL
+// ------------------------------------------------------------------------------------
+template <int MSR, int KPL>
+__global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+    const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    const float pv = a.pv;
+    for (uint64_t row = warp; row < a.n; row += nwarps) {
+        const uint64_t pb = a.indptr[row], pe = a.indptr[row + 1];
+        float rsi = 0.f, rinc = 0.f;
+        if (MSR == MKL || MSR == HELLINGER) {
+            rsi = a.rsi[row];
+            rinc = a.rinc[row];
+        }
+        const float rl = (MSR == MKL) ? logf(rinc) : 0.f;
+        const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
+        Best best;
+        best_init(best);
+        double bx = 0.0;  // HELLINGER: sum of b over all columns
+        if (MSR == HELLINGER) {
+            double s = 0.0;
+            for (uint64_t p = pb + lane; p < pe; p += 32) s += double(a.vals[p] * rsi + rinc);
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+            bx = s + double(a.d - (pe - pb)) * double(rinc);
+        }
+        for (uint32_t g0 = 0; g0 < a.k; g0 += 32 * KPL) {
+            float acc[KPL];
+#pragma unroll
+            for (int q = 0; q < KPL; ++q) acc[q] = 0.f;
+            for (uint64_t p0 = pb; p0 < pe; p0 += 32) {
+                const uint64_t p = p0 + lane;
+                uint32_t col = 0;
+                float g = 0.f, x = 0.f;
+                if (p < pe) {
+                    col = a.idx[p];
+                    x = a.vals[p];
+                    if (MSR == MKL) g = rl - logf(x * rsi + rinc);
+                    else if (MSR == HELLINGER) g = srinc - sqrtf(x * rsi + rinc);
+                    else if (MSR == L1) g = x + pv;
+                    else g = x;
+                }
+                const int cnt = int(umin64(32, pe - p0));
+                for (int q = 0; q < cnt; ++q) {
+                    const uint32_t cj = __shfl_sync(0xffffffffu, col, q);
+                    const float gj = __shfl_sync(0xffffffffu, g, q);
+                    const float *ct = a.CT0 + uint64_t(cj) * a.kp + g0 + lane;
+#pragma unroll
+                    for (int r = 0; r < KPL; ++r) {
+                        const float cv = __ldg(ct + 32 * r);
+                        if (MSR == MKL || MSR == HELLINGER) acc[r] = fmaf(cv, gj, acc[r]);
+                        else if (MSR == SQRL2) acc[r] = fmaf(gj, gj - 2.f * cv, acc[r]);
+                        else acc[r] = acc[r] + (fabsf(cv - gj) - fabsf(cv - pv));
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < KPL; ++r) {
+                const uint32_t c = g0 + lane + 32 * r;
+                if (c < a.k) {
+                    const double k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
+                    float key;
+                    if (MSR == MKL) {
+                        key = post_divergence(float(k0 - double(rl) * k1 + double(acc[r])));
+                    } else if (MSR == HELLINGER) {
+                        double s = k0 + bx - 2.0 * double(srinc) * k1 + 2.0 * double(acc[r]);
+                        if (s < 0.0) s = 0.0;
+                        key = float(sqrt(s));
+                    } else if (MSR == SQRL2) {
+                        double s = k0 + double(acc[r]);
+                        if (s < 0.0) s = 0.0;
+                        key = float(s);
+                    } else {
+                        key = float(k0 + double(acc[r])) * 0.5f;
+                    }
+                    best_offer(best, key, c);
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) best_merge_shfl(best, m);
+        if (lane == 0) {
+            const bool nan0 = best.v == __int_as_float(0xff800000);
+            const double cost = nan0 ? __longlong_as_double(0x7ff8000000000000ll) : key_to_cost<MSR>(best.v);
+            a.asn[row] = best.j;
+            a.costs[row] = double(float(cost));
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------
+template <int MSR>
+static int prep_centers_t(const AssignArgs &a, bool pair, float *C, cudaStream_t st) {
+    dim3 g(unsigned((a.d + 255) / 256), a.kp < 65535 ? a.kp : 65535);
+    if (pair) k_prep_centers<MSR, true><<<g, 256, 0, st>>>(C, a.k, a.kp, a.d, a.csum, a.pv, a.CT0, a.CT1), note_launch();
+    else k_prep_centers<MSR, false><<<g, 256, 0, st>>>(C, a.k, a.kp, a.d, a.csum, a.pv, a.CT0, a.CT1), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+int launch_prep_centers(const AssignArgs &a, const float *C, bool pair, bool sparse_consts, cudaStream_t st) {
+    float *Cm = const_cast<float *>(C);
+    switch (a.msr) {
+        case SQRL2: MC_TRY(prep_centers_t<SQRL2>(a, pair, Cm, st)); break;
+        case L1: MC_TRY(prep_centers_t<L1>(a, pair, Cm, st)); break;
+        case HELLINGER: MC_TRY(prep_centers_t<HELLINGER>(a, pair, Cm, st)); break;
+        case MKL: MC_TRY(prep_centers_t<MKL>(a, pair, Cm, st)); break;
+        case JSD: MC_TRY(prep_centers_t<JSD>(a, pair, Cm, st)); break;
+        default: return fail(MC_EUNSUPPORTED, "measure not supported");
+    }
+    if (sparse_consts) {
+        const unsigned g = (a.k + 63) / 64;
+        switch (a.msr) {
+            case SQRL2: k_center_consts<SQRL2><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            case L1: k_center_consts<L1><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            case HELLINGER: k_center_consts<HELLINGER><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            case MKL: k_center_consts<MKL><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            default: break;
+        }
+        MC_CUDA_TRY(cudaGetLastError());
+    }
+    return MC_OK;
+}
+
+int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, float *rsi, float *rinc,
+                       cudaStream_t st) {
+    if (n == 0) return MC_OK;
+    k_row_scalars<<<unsigned((n + 255) / 256), 256, 0, st>>>(rowsum, n, d, pv, rsi, rinc), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+template <int MSR, bool CSR>
+static int tiled_t(const AssignArgs &a, bool pair, bool big, cudaStream_t st) {
+    if (pair) {
+        constexpr int BM = 32;
+        k_assign_tiled<MSR, true, 2, 2, CSR><<<unsigned((a.n + BM - 1) / BM), 256, 0, st>>>(a), note_launch();
+    } else if (big) {
+        constexpr int BM = 128;
+        k_assign_tiled<MSR, false, 8, 8, CSR><<<unsigned((a.n + BM - 1) / BM), 256, 0, st>>>(a), note_launch();
+    } else {
+        constexpr int BM = 64;
+        k_assign_tiled<MSR, false, 4, 4, CSR><<<unsigned((a.n + BM - 1) / BM), 256, 0, st>>>(a), note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+uint32_t tiled_center_pad(uint32_t k, bool pair, int msr) {
+    const uint32_t bn = pair ? 32 : ((msr == SQRL2 && k >= 128) ? 128 : 64);
+    return (k + bn - 1) / bn * bn;
+}
+
+int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st) {
+    if (a.n == 0) return MC_OK;
+    // 8x8 register tiles for SQRL2 with many centers, 4x4 otherwise
+    const bool big = (a.msr == SQRL2 && a.kp % 128 == 0);
+    switch (a.msr) {
+        case SQRL2: return csr ? tiled_t<SQRL2, true>(a, pair, big, st) : tiled_t<SQRL2, false>(a, pair, big, st);
+        case L1: return csr ? tiled_t<L1, true>(a, pair, false, st) : tiled_t<L1, false>(a, pair, false, st);
+        case HELLINGER:
+            return csr ? tiled_t<HELLINGER, true>(a, pair, false, st) : tiled_t<HELLINGER, false>(a, pair, false, st);
+        case MKL: return csr ? tiled_t<MKL, true>(a, pair, false, st) : tiled_t<MKL, false>(a, pair, false, st);
+        case JSD: return csr ? tiled_t<JSD, true>(a, pair, false, st) : tiled_t<JSD, false>(a, pair, false, st);
+        default: return fail(MC_EUNSUPPORTED, "measure not supported");
+    }
+}
+
+template <int MSR>
+static int sparse_t(const AssignArgs &a, cudaStream_t st, int sms) {
+    const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 8));
+    if (a.kp <= 32) k_assign_sparse<MSR, 1><<<blocks, 256, 0, st>>>(a), note_launch();
+    else if (a.kp <= 64) k_assign_sparse<MSR, 2><<<blocks, 256, 0, st>>>(a), note_launch();
+    else k_assign_sparse<MSR, 4><<<blocks, 256, 0, st>>>(a), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+uint32_t sparse_center_pad(uint32_t k) {
+    const uint32_t g = k <= 32 ? 32 : (k <= 64 ? 64 : 128);
+    return (k + g - 1) / g * g;
+}
+
+int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms) {
+    if (a.n == 0) return MC_OK;
+    switch (a.msr) {
+        case SQRL2: return sparse_t<SQRL2>(a, st, sms);
+        case L1: return sparse_t<L1>(a, st, sms);
+        case HELLINGER: return sparse_t<HELLINGER>(a, st, sms);
+        case MKL: return sparse_t<MKL>(a, st, sms);
+        default: return fail(MC_EUNSUPPORTED, "sparse-dot path does not cover this measure");
+    }
+}
+
+}  // namespace mc

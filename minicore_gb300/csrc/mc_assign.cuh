@@ -1,0 +1,36 @@
+// Assignment kernel arguments and launchers (mc_assign.cu).
+#pragma once
+#include "mc_internal.cuh"
+
+namespace mc {
+
+struct AssignArgs {
+    int msr = SQRL2;
+    uint64_t n = 0, d = 0;
+    uint32_t k = 0, kp = 0;           // centers, padded center count of CT0/CT1
+    const float *X = nullptr;         // dense rows
+    const float *vals = nullptr;      // CSR rows
+    const uint32_t *idx = nullptr;
+    const uint64_t *indptr = nullptr;
+    const double *rowsum = nullptr;   // per row (pair mode, sparse HELL)
+    const float *rsi = nullptr;       // per-row 1/rhsum (constant prior)
+    const float *rinc = nullptr;      // per-row pv/rhsum (constant prior)
+    const double *csum = nullptr;     // per-center sums
+    float *CT0 = nullptr;             // [d][kp] center transform
+    float *CT1 = nullptr;             // [d][kp] second center transform (MKL, JSD)
+    double *consts = nullptr;         // [k][4] per-center FP64 constants (sparse-dot path)
+    float pv = 0.f;                   // constant-prior pv
+    double prior = 0.0, prior_sum = 0.0;
+    uint32_t *asn = nullptr;
+    double *costs = nullptr;
+};
+
+int launch_prep_centers(const AssignArgs &a, const float *C, bool pair, bool sparse_consts, cudaStream_t st);
+int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, float *rsi, float *rinc,
+                       cudaStream_t st);
+int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st);
+int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms);
+uint32_t tiled_center_pad(uint32_t k, bool pair, int msr);
+uint32_t sparse_center_pad(uint32_t k);
+
+}  // namespace mc

@@ -1,0 +1,207 @@
+// D^2 / k-means++ seeding (include/minicore/optim/kmeans.h:49-215, n_local_trials == 1).
+//
+// Round c: draw newc from (w *) dist with uniform u[c] (FP64 inverse CDF, mc_reduce.cu),
+// set asn[newc] = c, then update every row i != newc with dist[i] > 0:
+// dist[i] = min(dist[i], msr(row i, row newc)) (COMPUTE_X, kmeans.h:189-201), and finally
+// dist[newc] = 0.  Nothing returns to the host between rounds, so the k rounds are queued
+// back to back on one stream.
+#include "mc_kmpp.cuh"
+
+namespace mc {
+
+template <int MSR>
+__device__ inline float kp_finish_key(float acc) {
+    if (MSR == SQRL2) return acc;
+    if (MSR == L1) return acc * 0.5f;
+    if (MSR == HELLINGER) return sqrtf(acc);
+    if (MSR == MKL) return post_divergence(acc);
+    return post_divergence(acc * 0.5f);
+}
+
+template <int MSR>
+__device__ inline double kp_cost(float acc) {
+    const float key = kp_finish_key<MSR>(acc);
+    if (MSR == L1) return double(key) * 2.0;
+    if (MSR == HELLINGER) return double(key) * kSqrt1_2;
+    return double(key);
+}
+
+template <int MSR>
+__device__ inline void kp_elem(float &acc, float c, float x, const PairScalars &s) {
+    if (MSR == SQRL2) {
+        const float df = c - x;
+        acc = fmaf(df, df, acc);
+    } else if (MSR == L1) {
+        const float a = c + s.pv, b = x + s.pv;
+        acc = acc + fabsf(a - b);
+    } else if (MSR == HELLINGER) {
+        const float a = sqrtf(c * s.lhrsi + s.lhinc), b = sqrtf(x * s.rhrsi + s.rhinc);
+        const float df = a - b;
+        acc = fmaf(df, df, acc);
+    } else if (MSR == MKL) {
+        const float a = c * s.lhrsi + s.lhinc, b = x * s.rhrsi + s.rhinc;
+        acc = fmaf(a, logf(a) - logf(b), acc);
+    } else {
+        const float a = c * s.lhrsi + s.lhinc, b = x * s.rhrsi + s.rhinc;
+        const float m = a + b;
+        const float t = (a * logf(a) + b * logf(b)) - m * logf(m * 0.5f);
+        acc = acc + t;
+    }
+}
+
+// first center from u[0]
+__global__ void k_kmpp_first(const double *u, uint64_t n, uint64_t *newc, uint32_t *center_ids) {
+    uint64_t fc = uint64_t(u[0] * double(n));
+    if (fc >= n) fc = n - 1;
+    *newc = fc;
+    center_ids[0] = uint32_t(fc);
+}
+
+// after a draw: record the center, densify its row into cbuf
+__global__ void k_kmpp_take(const KmppArgs a, uint32_t ci) {
+    const uint64_t c = *a.newc;
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        a.center_ids[ci] = uint32_t(c);
+        a.asn[c] = ci;
+    }
+    if (!a.csr) {
+        for (uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; j < a.d; j += gridDim.x * uint64_t(blockDim.x))
+            a.cbuf[j] = a.X[c * a.d + j];
+    } else {
+        for (uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; j < a.d; j += gridDim.x * uint64_t(blockDim.x))
+            a.cbuf[j] = 0.f;
+    }
+}
+
+__global__ void k_kmpp_scatter(const KmppArgs a) {
+    const uint64_t c = *a.newc;
+    for (uint64_t p = a.indptr[c] + blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; p < a.indptr[c + 1];
+         p += gridDim.x * uint64_t(blockDim.x))
+        a.cbuf[a.idx[p]] = a.vals[p];
+}
+
+__global__ void k_kmpp_zero(const KmppArgs a) { a.dist[*a.newc] = 0.0; }
+
+// dense rows: a CTA stages 128 rows x 32 columns in shared memory; each thread reduces its
+// row sequentially over the columns (the oracle's order).
+template <int MSR>
+__global__ void __launch_bounds__(128) k_kmpp_dense(const KmppArgs a, int first) {
+    __shared__ float tile[128][33];
+    __shared__ float cs[32];
+    const uint64_t c = *a.newc;
+    const uint64_t row0 = uint64_t(blockIdx.x) * 128;
+    const uint64_t i = row0 + threadIdx.x;
+    const double csum = a.rowsum[c];
+    PairScalars s = {};
+    if (i < a.n && MSR != SQRL2) s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], csum, a.d);
+    float acc = 0.f;
+    for (uint64_t k0 = 0; k0 < a.d; k0 += 32) {
+        const int kmax = int(umin64(32, a.d - k0));
+        for (int e = threadIdx.x; e < 128 * 32; e += 128) {
+            const int r = e >> 5, kk = e & 31;
+            const uint64_t row = row0 + r;
+            tile[r][kk] = (row < a.n && kk < kmax) ? a.X[row * a.d + k0 + kk] : 0.f;
+        }
+        if (threadIdx.x < 32) cs[threadIdx.x] = threadIdx.x < kmax ? a.cbuf[k0 + threadIdx.x] : 0.f;
+        __syncthreads();
+        for (int kk = 0; kk < kmax; ++kk) kp_elem<MSR>(acc, cs[kk], tile[threadIdx.x][kk], s);
+        __syncthreads();
+    }
+    if (i >= a.n) return;
+    const double v = kp_cost<MSR>(acc);
+    if (first) {
+        a.dist[i] = (i == c) ? 0.0 : v;
+    } else {
+        if (i == c) return;
+        const double cur = a.dist[i];
+        if (cur <= 0.0) return;
+        if (v < cur) {
+            a.dist[i] = v;
+            a.asn[i] = a.round;
+        }
+    }
+}
+
+// CSR rows (any measure, any prior): one warp per row.  sum over all columns of
+// f(a_j, b0) (b0: transform of a zero entry) plus, over the row's nonzeros,
+// f(a_j, b_j) - f(a_j, b0).
+template <int MSR>
+__global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, uint32_t round) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+    const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    const uint64_t c = *a.newc;
+    const double csum = a.rowsum[c];
+    for (uint64_t i = warp; i < a.n; i += nwarps) {
+        if (!first && (i == c || a.dist[i] <= 0.0)) continue;
+        const PairScalars s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], csum, a.d);
+        float acc = 0.f;
+        for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, a.cbuf[j], 0.f, s);
+        for (uint64_t p = a.indptr[i] + lane; p < a.indptr[i + 1]; p += 32) {
+            const float cj = a.cbuf[a.idx[p]];
+            float t1 = 0.f, t0 = 0.f;
+            kp_elem<MSR>(t1, cj, a.vals[p], s);
+            kp_elem<MSR>(t0, cj, 0.f, s);
+            acc = acc + (t1 - t0);
+        }
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
+        if (lane == 0) {
+            double v = kp_cost<MSR>(acc);
+            if (MSR == SQRL2 && v < 0.0) v = 0.0;
+            if (first) {
+                a.dist[i] = (i == c) ? 0.0 : v;
+            } else if (v < a.dist[i]) {
+                a.dist[i] = v;
+                a.asn[i] = round;
+            }
+        }
+    }
+}
+
+template <int MSR>
+static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaStream_t st) {
+    if (!a.csr) {
+        KmppArgs b = a;
+        b.round = round;
+        k_kmpp_dense<MSR><<<unsigned((a.n + 127) / 128), 128, 0, st>>>(b, first), note_launch();
+    } else {
+        const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
+        k_kmpp_csr<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+static int update(const KmppArgs &a, int first, uint32_t round, int sms, cudaStream_t st) {
+    switch (a.msr) {
+        case SQRL2: return update_t<SQRL2>(a, first, round, sms, st);
+        case L1: return update_t<L1>(a, first, round, sms, st);
+        case HELLINGER: return update_t<HELLINGER>(a, first, round, sms, st);
+        case MKL: return update_t<MKL>(a, first, round, sms, st);
+        case JSD: return update_t<JSD>(a, first, round, sms, st);
+        default: return fail(MC_EUNSUPPORTED, "measure not supported");
+    }
+}
+
+int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st) {
+    KmppArgs a = a0;
+    const unsigned tb = 256, tg = unsigned(umin64((a.d + tb - 1) / tb, 1024));
+    MC_CUDA_TRY(cudaMemsetAsync(a.asn, 0, a.n * sizeof(uint32_t), st));
+    k_kmpp_first<<<1, 1, 0, st>>>(u_dev, a.n, a.newc, a.center_ids), note_launch();
+    k_kmpp_take<<<tg, tb, 0, st>>>(a, 0), note_launch();
+    if (a.csr) k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
+    MC_TRY(update(a, 1, 0, sms, st));
+    DetInput in{a.w ? DET_F64_W : DET_F64, a.dist, nullptr, a.w, a.n};
+    for (uint32_t ci = 1; ci < a.k; ++ci) {
+        MC_TRY(launch_det_draw(in, chunk_tmp, u_dev + ci, 0.0, 1, a.dist, a.newc, st));
+        k_kmpp_take<<<tg, tb, 0, st>>>(a, ci), note_launch();
+        if (a.csr) k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
+        MC_TRY(update(a, 0, ci, sms, st));
+        k_kmpp_zero<<<1, 1, 0, st>>>(a), note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+}  // namespace mc

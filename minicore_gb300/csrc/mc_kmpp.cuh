@@ -1,0 +1,29 @@
+// k-means++ launcher (mc_kmpp.cu).
+#pragma once
+#include "mc_internal.cuh"
+
+namespace mc {
+
+struct KmppArgs {
+    int msr = SQRL2;
+    bool csr = false;
+    uint64_t n = 0, d = 0;
+    uint32_t k = 0;
+    uint32_t round = 0;
+    const float *X = nullptr;
+    const float *vals = nullptr;
+    const uint32_t *idx = nullptr;
+    const uint64_t *indptr = nullptr;
+    const double *rowsum = nullptr;
+    const double *w = nullptr;
+    double prior = 0.0, prior_sum = 0.0;
+    float *cbuf = nullptr;        // densified current center row [d]
+    double *dist = nullptr;       // [n]
+    uint32_t *asn = nullptr;      // [n]
+    uint32_t *center_ids = nullptr;  // [k]
+    uint64_t *newc = nullptr;     // device scalar
+};
+
+int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);
+
+}  // namespace mc

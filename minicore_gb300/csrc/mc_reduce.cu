@@ -1,0 +1,582 @@
+// Deterministic reductions, D^2 draws, row statistics, the stable counting sort of rows by
+// cluster, and the chunked centroid sums.
+//
+// Reference behaviour these kernels implement:
+//  * objective totals: perform_hard_clustering's compute_cost (clustering/solve.h:120-123);
+//  * D^2 draws: kmeanspp's sampling step (optim/kmeans.h:115-135) and the empty-cluster
+//    restart (clustering/centroid.h:687-713), as an FP64 inverse CDF on a supplied uniform;
+//  * centroid sums: set_centroids_full_mean + set_center (clustering/centroid.h:81-178,
+//    649-779): rows bucketed by assignment in ascending order, weighted mean per bucket.
+#include "mc_reduce.cuh"
+
+namespace mc {
+
+// ------------------------------------------------------------------------------------
+// det sum: one CTA (256 threads) per 8192-element chunk
+// ------------------------------------------------------------------------------------
+__device__ inline double warp_butterfly_sum(double v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__device__ inline double det_thread_partial(const DetInput &in, uint64_t base, int t) {
+    double acc = 0.0;
+#pragma unroll 4
+    for (int m = 0; m < kDetPer; ++m) {
+        const uint64_t i = base + uint64_t(t) + uint64_t(kDetThreads) * m;
+        if (i < in.n) acc = acc + in.get(i);
+    }
+    return acc;
+}
+
+// chunk total in the canonical order; every thread of the CTA must call it
+__device__ inline double det_chunk_total(const DetInput &in, uint64_t g, double *sm_warp, double *partial_out) {
+    const int t = threadIdx.x;
+    const double p = det_thread_partial(in, g * uint64_t(kDetChunk), t);
+    if (partial_out) partial_out[t] = p;
+    const double w = warp_butterfly_sum(p);
+    if ((t & 31) == 0) sm_warp[t >> 5] = w;
+    __syncthreads();
+    double tot = sm_warp[0];
+    for (int i = 1; i < kDetThreads / 32; ++i) tot = tot + sm_warp[i];
+    __syncthreads();
+    return tot;
+}
+
+__global__ void __launch_bounds__(kDetThreads) k_det_chunks(DetInput in, double *chunk_tot) {
+    __shared__ double sm_warp[kDetThreads / 32];
+    const double tot = det_chunk_total(in, blockIdx.x, sm_warp, nullptr);
+    if (threadIdx.x == 0) chunk_tot[blockIdx.x] = tot;
+}
+
+__global__ void k_det_final(const double *chunk_tot, uint64_t G, double *out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (uint64_t g = 0; g < G; ++g) s = s + chunk_tot[g];
+        *out = s;
+    }
+}
+
+int launch_det_sum(const DetInput &in, double *chunk_tmp, double *out, cudaStream_t st) {
+    const uint64_t G = det_chunks(in.n);
+    if (G > 0) k_det_chunks<<<unsigned(G), kDetThreads, 0, st>>>(in, chunk_tmp), note_launch();
+    k_det_final<<<1, 32, 0, st>>>(chunk_tmp, G, out), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// det draw: chunk totals (k_det_chunks), then a single CTA walks the canonical order.
+// If the total is not positive, the first maximum of fallback_vals (or index 0) is taken,
+// as kmeanspp's argmax fallback does (kmeans.h:179-186).
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, const double *chunk_tot, const double *u_dev,
+                                                          double u_host, int use_dev_u, const double *fallback_vals,
+                                                          uint64_t *out_idx) {
+    __shared__ double sm_warp[kDetThreads / 32];
+    __shared__ double sm_part[kDetThreads];
+    __shared__ int64_t sm_sel;
+    __shared__ double sm_r;
+    __shared__ int sm_clamp;
+    const int t = threadIdx.x;
+    const uint64_t G = det_chunks(in.n);
+    if (t == 0) {
+        double S = 0.0;
+        for (uint64_t g = 0; g < G; ++g) S = S + chunk_tot[g];
+        int64_t gs = -1;
+        int clamp = 0;
+        double C = 0.0, tt = 0.0;
+        if (S > 0.0) {
+            const double u = use_dev_u ? *u_dev : u_host;
+            tt = u * S;
+            for (uint64_t g = 0; g < G; ++g) {
+                if (C + chunk_tot[g] > tt) { gs = int64_t(g); break; }
+                C = C + chunk_tot[g];
+            }
+            if (gs < 0) {
+                for (int64_t g = int64_t(G) - 1; g >= 0; --g)
+                    if (chunk_tot[g] > 0.0) { gs = g; break; }
+                clamp = 1;
+            }
+        }
+        sm_sel = gs;
+        sm_r = tt - C;
+        sm_clamp = clamp;
+    }
+    __syncthreads();
+    const int64_t gs = sm_sel;
+    if (gs < 0) {  // total not positive: argmax fallback (first maximum) over fallback_vals
+        if (t == 0) {
+            uint64_t am = 0;
+            if (fallback_vals) {
+                for (uint64_t i = 1; i < in.n; ++i)
+                    if (fallback_vals[i] > fallback_vals[am]) am = i;
+            }
+            *out_idx = am;
+        }
+        return;
+    }
+    (void)det_chunk_total(in, uint64_t(gs), sm_warp, sm_part);
+    __syncthreads();
+    if (t == 0) {
+        const uint64_t base = uint64_t(gs) * kDetChunk;
+        auto last_pos_in_thread = [&](int th) -> uint64_t {
+            uint64_t best = in.n;
+            for (int m = 0; m < kDetPer; ++m) {
+                const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * m;
+                if (i < in.n && in.get(i) > 0.0) best = i;
+            }
+            return best;
+        };
+        const double r = sm_r;
+        int tau = -1;
+        double Q = 0.0;
+        if (!sm_clamp) {
+            for (int th = 0; th < kDetThreads; ++th) {
+                if (Q + sm_part[th] > r) { tau = th; break; }
+                Q = Q + sm_part[th];
+            }
+        }
+        uint64_t res = in.n;
+        if (tau < 0) {
+            for (int th = kDetThreads - 1; th >= 0; --th)
+                if (sm_part[th] > 0.0) { res = last_pos_in_thread(th); break; }
+        } else {
+            const double r2 = r - Q;
+            double R = 0.0;
+            for (int m = 0; m < kDetPer; ++m) {
+                const uint64_t i = base + uint64_t(tau) + uint64_t(kDetThreads) * m;
+                const double val = i < in.n ? in.get(i) : 0.0;
+                if (R + val > r2) { res = i; break; }
+                R = R + val;
+            }
+            if (res == in.n) res = last_pos_in_thread(tau);
+        }
+        if (res >= in.n) res = 0;
+        *out_idx = res;
+    }
+}
+
+int launch_det_draw(const DetInput &in, double *chunk_tmp, const double *u_dev, double u_host, int use_dev_u,
+                    const double *fallback_vals, uint64_t *out_idx, cudaStream_t st) {
+    const uint64_t G = det_chunks(in.n);
+    if (G > 0) k_det_chunks<<<unsigned(G), kDetThreads, 0, st>>>(in, chunk_tmp), note_launch();
+    k_det_draw<<<1, kDetThreads, 0, st>>>(in, chunk_tmp, u_dev, u_host, use_dev_u, fallback_vals, out_idx), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// row statistics: sequential FP64 row sums (and float squared norms for dense rows)
+// ------------------------------------------------------------------------------------
+__global__ void k_row_sums_dense(const float *__restrict__ X, uint64_t n, uint64_t d, double *rowsum,
+                                 float *rownorm) {
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const float *r = X + i * d;
+    double s = 0.0;
+    float q = 0.f;
+    for (uint64_t j = 0; j < d; ++j) {
+        const float v = r[j];
+        s = s + double(v);
+        q = fmaf(v, v, q);
+    }
+    rowsum[i] = s;
+    if (rownorm) rownorm[i] = q;
+}
+
+__global__ void k_row_sums_csr(const float *__restrict__ vals, const uint64_t *__restrict__ indptr, uint64_t n,
+                               double *rowsum) {
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    double s = 0.0;
+    for (uint64_t p = indptr[i]; p < indptr[i + 1]; ++p) s = s + double(vals[p]);
+    rowsum[i] = s;
+}
+
+int launch_row_sums_dense(const float *X, uint64_t n, uint64_t d, double *rowsum, float *rownorm, cudaStream_t st) {
+    if (n == 0) return MC_OK;
+    k_row_sums_dense<<<unsigned((n + 127) / 128), 128, 0, st>>>(X, n, d, rowsum, rownorm), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+int launch_row_sums_csr(const float *vals, const uint64_t *indptr, uint64_t n, double *rowsum, cudaStream_t st) {
+    if (n == 0) return MC_OK;
+    k_row_sums_csr<<<unsigned((n + 127) / 128), 128, 0, st>>>(vals, indptr, n, rowsum), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Stable counting sort of rows by cluster id.
+// keys[i] in [0,k); optional keys2[i] (second membership, 0xffffffff = none).
+// Tiles of kSortTile rows; per-tile counts -> per (key, tile) offsets -> one warp per tile
+// scatters its rows in order (match_any ranks), so each bucket lists rows ascending.
+// ------------------------------------------------------------------------------------
+__global__ void k_sort_count(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ keys2, uint64_t n,
+                             uint32_t k, uint32_t *tile_counts /* [ntiles][k] */) {
+    const uint64_t tile = blockIdx.x;
+    const uint64_t b = tile * kSortTile, e = umin64(n, b + kSortTile);
+    uint32_t *tc = tile_counts + tile * uint64_t(k);
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        atomicAdd(&tc[keys[i]], 1u);
+        if (keys2) {
+            const uint32_t k2 = keys2[i];
+            if (k2 != 0xffffffffu) atomicAdd(&tc[k2], 1u);
+        }
+    }
+}
+
+// per key: sequential over tiles -> tile offsets (relative to the bucket start) and totals
+__global__ void k_sort_key_scan(uint32_t *tile_counts, uint64_t ntiles, uint32_t k, uint64_t *bucket_count) {
+    const uint32_t key = blockIdx.x * blockDim.x + threadIdx.x;
+    if (key >= k) return;
+    uint64_t acc = 0;
+    for (uint64_t t = 0; t < ntiles; ++t) {
+        const uint32_t c = tile_counts[t * k + key];
+        tile_counts[t * k + key] = uint32_t(acc);
+        acc += c;
+    }
+    bucket_count[key] = acc;
+}
+
+// exclusive scan of bucket counts (single CTA, sequential per thread chunk + smem)
+__global__ void k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m) {
+    __shared__ uint64_t part[1024];
+    const int t = threadIdx.x;
+    const uint64_t per = (m + blockDim.x - 1) / blockDim.x;
+    const uint64_t b = t * per, e = umin64(m, b + per);
+    uint64_t s = 0;
+    for (uint64_t i = b; i < e; ++i) s += in[i];
+    part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        uint64_t acc = 0;
+        for (unsigned i = 0; i < blockDim.x; ++i) {
+            const uint64_t v = part[i];
+            part[i] = acc;
+            acc += v;
+        }
+        out[m] = acc;
+    }
+    __syncthreads();
+    uint64_t acc = part[t];
+    for (uint64_t i = b; i < e; ++i) {
+        const uint64_t v = in[i];
+        out[i] = acc;
+        acc += v;
+    }
+}
+
+__global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, uint32_t k, uint32_t *tile_offsets,
+                               const uint64_t *__restrict__ bucket_start, uint32_t *perm) {
+    // one warp per tile; rows in order, 32 at a time; ranks from match_any
+    const uint64_t tile = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    const uint64_t b = tile * kSortTile;
+    if (b >= n) return;
+    const uint64_t e = umin64(n, b + kSortTile);
+    uint32_t *cur = tile_offsets + tile * uint64_t(k);
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint64_t base = b; base < e; base += 32) {
+        const uint64_t i = base + lane;
+        const bool act = i < e;
+        const uint32_t key = act ? keys[i] : 0xffffffffu;
+        const unsigned actmask = __ballot_sync(0xffffffffu, act);
+        const unsigned peers = __match_any_sync(0xffffffffu, key) & actmask;
+        uint32_t off = 0;
+        if (act) off = cur[key];
+        __syncwarp();
+        if (act) {
+            perm[bucket_start[key] + off + __popc(peers & lt)] = uint32_t(i);
+            if ((peers & lt) == 0) cur[key] = off + __popc(peers);
+        }
+        __syncwarp();
+    }
+}
+
+// Rare path (rows with a second membership after an empty-cluster restart): one thread
+// per tile walks its rows in order so that every bucket stays ascending.
+__global__ void k_sort_scatter2(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ keys2, uint64_t n,
+                                uint32_t k, uint32_t *tile_offsets, const uint64_t *__restrict__ bucket_start,
+                                uint32_t *perm) {
+    const uint64_t tile = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    const uint64_t b = tile * kSortTile;
+    if (b >= n) return;
+    const uint64_t e = umin64(n, b + kSortTile);
+    uint32_t *cur = tile_offsets + tile * uint64_t(k);
+    for (uint64_t i = b; i < e; ++i) {
+        const uint32_t k1 = keys[i], k2 = keys2[i];
+        perm[bucket_start[k1] + cur[k1]++] = uint32_t(i);
+        if (k2 != 0xffffffffu) perm[bucket_start[k2] + cur[k2]++] = uint32_t(i);
+    }
+}
+
+int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st) {
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(in, out, m), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, uint32_t k, SortWork &w,
+                       cudaStream_t st) {
+    const uint64_t ntiles = (n + kSortTile - 1) / kSortTile;
+    MC_TRY(w.tile_counts.alloc(ntiles * k, st));
+    MC_TRY(w.bucket_count.alloc(k, st));
+    MC_TRY(w.bucket_start.alloc(uint64_t(k) + 1, st));
+    MC_TRY(w.perm.alloc(keys2 ? 2 * n : n, st));
+    MC_CUDA_TRY(cudaMemsetAsync(w.tile_counts.p, 0, ntiles * k * sizeof(uint32_t), st));
+    if (ntiles) k_sort_count<<<unsigned(ntiles), 256, 0, st>>>(keys, keys2, n, k, w.tile_counts.p), note_launch();
+    k_sort_key_scan<<<(k + 127) / 128, 128, 0, st>>>(w.tile_counts.p, ntiles, k, w.bucket_count.p), note_launch();
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.bucket_count.p, w.bucket_start.p, k), note_launch();
+    if (ntiles) {
+        if (!keys2)
+            k_sort_scatter<<<unsigned((ntiles + 3) / 4), 128, 0, st>>>(keys, n, k, w.tile_counts.p,
+                                                                       w.bucket_start.p, w.perm.p), note_launch();
+        else
+            k_sort_scatter2<<<unsigned((ntiles + 63) / 64), 64, 0, st>>>(keys, keys2, n, k, w.tile_counts.p,
+                                                                         w.bucket_start.p, w.perm.p), note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Centroid sums.  Chunks: bucket c is split into ceil(cnt_c / ch) chunks of ch rows.
+// chunk_start[c] = exclusive scan of the chunk counts (computed on device); a grid of
+// ceil(n/ch)+k CTAs maps its chunk id by binary search, extra CTAs exit.
+// ------------------------------------------------------------------------------------
+__global__ void k_chunk_counts(const uint64_t *bucket_count, uint32_t k, uint64_t ch, uint64_t *chunk_count) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < k) chunk_count[c] = (bucket_count[c] + ch - 1) / ch;
+}
+
+__device__ inline uint32_t find_bucket(const uint64_t *chunk_start, uint32_t k, uint64_t q) {
+    // largest c with chunk_start[c] <= q (chunk_start has k+1 entries, nondecreasing)
+    uint32_t lo = 0, hi = k;  // invariant: chunk_start[lo] <= q < chunk_start[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (chunk_start[mid] <= q) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__device__ inline void two_sum_add(float &s, float &e, float x) {
+    const float t = __fadd_rn(s, x);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    s = t;
+    e = __fadd_rn(e, err);
+}
+
+// dense: one CTA per chunk, threads over columns, rows sequential
+__global__ void k_centroid_chunks_dense(const float *__restrict__ X, uint64_t d, const uint32_t *__restrict__ perm,
+                                        const uint64_t *__restrict__ bucket_start,
+                                        const uint64_t *__restrict__ bucket_count,
+                                        const uint64_t *__restrict__ chunk_start, uint32_t k, uint64_t ch,
+                                        const double *__restrict__ w, double *partial /* [chunk][d] */,
+                                        double *partial_w /* [chunk] */) {
+    const uint64_t q = blockIdx.x;
+    if (q >= chunk_start[k]) return;
+    const uint32_t c = find_bucket(chunk_start, k, q);
+    const uint64_t local = q - chunk_start[c];
+    const uint64_t r0 = local * ch, r1 = umin64(bucket_count[c], r0 + ch);
+    const uint32_t *rows = perm + bucket_start[c];
+    for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) {
+        if (w) {
+            double acc = 0.0;
+            for (uint64_t r = r0; r < r1; ++r) {
+                const uint32_t row = rows[r];
+                acc = fma(w[row], double(X[uint64_t(row) * d + j]), acc);
+            }
+            partial[q * d + j] = acc;
+        } else {
+            float s = 0.f, e = 0.f;
+            for (uint64_t r = r0; r < r1; ++r) {
+                const uint32_t row = rows[r];
+                two_sum_add(s, e, X[uint64_t(row) * d + j]);
+            }
+            partial[q * d + j] = double(s) + double(e);
+        }
+    }
+    if (w && threadIdx.x == 0) {
+        double wq = 0.0;
+        for (uint64_t r = r0; r < r1; ++r) wq = wq + w[rows[r]];
+        partial_w[q] = wq;
+    }
+}
+
+// CSR: one CTA per (chunk, column band); dense band accumulator in shared memory.
+// Rows are visited in order; within a row every nonzero touches a distinct column, so
+// each column's additions happen in row order.
+__global__ void k_centroid_chunks_csr(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                                      const uint64_t *__restrict__ indptr, uint64_t d, uint64_t band,
+                                      const uint32_t *__restrict__ perm, const uint64_t *__restrict__ bucket_start,
+                                      const uint64_t *__restrict__ bucket_count,
+                                      const uint64_t *__restrict__ chunk_start, uint32_t k, uint64_t ch,
+                                      const double *__restrict__ w, double *partial, double *partial_w) {
+    extern __shared__ unsigned char smraw[];
+    const uint64_t q = blockIdx.x;
+    if (q >= chunk_start[k]) return;
+    const uint32_t c = find_bucket(chunk_start, k, q);
+    const uint64_t local = q - chunk_start[c];
+    const uint64_t r0 = local * ch, r1 = umin64(bucket_count[c], r0 + ch);
+    const uint32_t *rows = perm + bucket_start[c];
+    const uint64_t j0 = blockIdx.y * band, j1 = umin64(d, j0 + band);
+    const uint64_t bw = j1 - j0;
+    if (w) {
+        double *acc = reinterpret_cast<double *>(smraw);
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x) acc[j] = 0.0;
+        __syncthreads();
+        for (uint64_t r = r0; r < r1; ++r) {
+            const uint32_t row = rows[r];
+            const double wr = w[row];
+            for (uint64_t p = indptr[row] + threadIdx.x; p < indptr[row + 1]; p += blockDim.x) {
+                const uint32_t col = idx[p];
+                if (col >= j0 && col < j1) acc[col - j0] = fma(wr, double(vals[p]), acc[col - j0]);
+            }
+            __syncthreads();
+        }
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x) partial[q * d + j0 + j] = acc[j];
+        if (blockIdx.y == 0 && threadIdx.x == 0) {
+            double wq = 0.0;
+            for (uint64_t r = r0; r < r1; ++r) wq = wq + w[rows[r]];
+            partial_w[q] = wq;
+        }
+    } else {
+        float *s = reinterpret_cast<float *>(smraw);
+        float *e = s + band;
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x) { s[j] = 0.f; e[j] = 0.f; }
+        __syncthreads();
+        for (uint64_t r = r0; r < r1; ++r) {
+            const uint32_t row = rows[r];
+            for (uint64_t p = indptr[row] + threadIdx.x; p < indptr[row + 1]; p += blockDim.x) {
+                const uint32_t col = idx[p];
+                if (col >= j0 && col < j1) two_sum_add(s[col - j0], e[col - j0], vals[p]);
+            }
+            __syncthreads();
+        }
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x)
+            partial[q * d + j0 + j] = double(s[j]) + double(e[j]);
+    }
+}
+
+// finalize: per (bucket, column): FP64 sum of chunk partials in order, divide, round.
+// Buckets with one row copy the row; empty buckets keep the old center.
+__global__ void k_centroid_finalize(const double *__restrict__ partial, const double *__restrict__ partial_w,
+                                    const uint64_t *__restrict__ chunk_start, const uint64_t *__restrict__ bucket_count,
+                                    uint32_t k, uint64_t d, int weighted, float *centers, int *nan_flag) {
+    const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (j >= d) return;
+    for (uint32_t c = blockIdx.y; c < k; c += gridDim.y) {
+        const uint64_t cnt = bucket_count[c];
+        if (cnt <= 1) continue;  // empty: keep; singleton: row copy (separate kernel)
+        const uint64_t q0 = chunk_start[c], q1 = chunk_start[c + 1];
+        double S = partial[q0 * d + j];
+        for (uint64_t q = q0 + 1; q < q1; ++q) S = S + partial[q * d + j];
+        double den;
+        if (weighted) {
+            den = partial_w[q0];
+            for (uint64_t q = q0 + 1; q < q1; ++q) den = den + partial_w[q];
+        } else {
+            den = double(cnt);
+        }
+        const float v = float(S / den);
+        centers[uint64_t(c) * d + j] = v;
+        if (v != v) atomicExch(nan_flag, 1);
+    }
+}
+
+// singleton buckets copy the row verbatim (centroid.h:761-768)
+__global__ void k_centroid_singletons_dense(const float *__restrict__ X, uint64_t d, const uint32_t *perm,
+                                            const uint64_t *bucket_start, const uint64_t *bucket_count, uint32_t k,
+                                            float *centers) {
+    for (uint32_t c = blockIdx.x; c < k; c += gridDim.x) {
+        if (bucket_count[c] != 1) continue;
+        const uint32_t row = perm[bucket_start[c]];
+        for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) centers[uint64_t(c) * d + j] = X[uint64_t(row) * d + j];
+    }
+}
+
+__global__ void k_centroid_singletons_csr(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                                          const uint64_t *__restrict__ indptr, uint64_t d, const uint32_t *perm,
+                                          const uint64_t *bucket_start, const uint64_t *bucket_count, uint32_t k,
+                                          float *centers) {
+    for (uint32_t c = blockIdx.x; c < k; c += gridDim.x) {
+        if (bucket_count[c] != 1) continue;
+        const uint32_t row = perm[bucket_start[c]];
+        float *dst = centers + uint64_t(c) * d;
+        for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) dst[j] = 0.f;
+        __syncthreads();
+        for (uint64_t p = indptr[row] + threadIdx.x; p < indptr[row + 1]; p += blockDim.x) dst[idx[p]] = vals[p];
+        __syncthreads();
+    }
+}
+
+int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st) {
+    const uint64_t n = a.n, d = a.d;
+    const uint32_t k = a.k;
+    const uint64_t ch = a.csr ? 4096 : 256;
+    MC_TRY(launch_sort_by_key(a.keys, a.keys2, n, k, w, st));
+    MC_TRY(w.chunk_count.alloc(k, st));
+    MC_TRY(w.chunk_start.alloc(uint64_t(k) + 1, st));
+    k_chunk_counts<<<(k + 255) / 256, 256, 0, st>>>(w.bucket_count.p, k, ch, w.chunk_count.p), note_launch();
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.chunk_count.p, w.chunk_start.p, k), note_launch();
+    const uint64_t members = n + (a.keys2 ? a.extra_members : 0);
+    const uint64_t max_chunks = (members + ch - 1) / ch + k;
+    MC_TRY(w.partial.alloc(max_chunks * d, st));
+    MC_TRY(w.partial_w.alloc(max_chunks, st));
+    if (!a.csr) {
+        k_centroid_chunks_dense<<<unsigned(max_chunks), 128, 0, st>>>(a.X, d, w.perm.p, w.bucket_start.p,
+                                                                     w.bucket_count.p, w.chunk_start.p, k, ch, a.w,
+                                                                     w.partial.p, w.partial_w.p), note_launch();
+    } else {
+        const uint64_t band = a.w ? 12288 : 24576;  // 96 KB (double) or 192 KB (two floats)
+        const uint64_t bw = band < d ? band : d;
+        const size_t smem = a.w ? bw * sizeof(double) : 2 * bw * sizeof(float);
+        const unsigned nb = unsigned((d + band - 1) / band);
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_centroid_chunks_csr, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+        k_centroid_chunks_csr<<<dim3(unsigned(max_chunks), nb), 256, smem, st>>>(
+            a.vals, a.idx, a.indptr, d, bw, w.perm.p, w.bucket_start.p, w.bucket_count.p, w.chunk_start.p, k, ch,
+            a.w, w.partial.p, w.partial_w.p), note_launch();
+    }
+    k_centroid_finalize<<<dim3(unsigned((d + 127) / 128), k < 65535 ? k : 65535), 128, 0, st>>>(
+        w.partial.p, w.partial_w.p, w.chunk_start.p, w.bucket_count.p, k, d, a.w ? 1 : 0, a.centers, a.nan_flag), note_launch();
+    if (!a.csr)
+        k_centroid_singletons_dense<<<k < 65535 ? k : 65535, 128, 0, st>>>(a.X, d, w.perm.p, w.bucket_start.p, w.bucket_count.p, k,
+                                                       a.centers), note_launch();
+    else
+        k_centroid_singletons_csr<<<k < 65535 ? k : 65535, 256, 0, st>>>(a.vals, a.idx, a.indptr, d, w.perm.p, w.bucket_start.p,
+                                                     w.bucket_count.p, k, a.centers), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// per-center sums (sequential FP64 over columns) and squared norms
+// ------------------------------------------------------------------------------------
+__global__ void k_center_sums(const float *__restrict__ C, uint32_t k, uint64_t d, double *csum, float *cnorm) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= k) return;
+    const float *r = C + uint64_t(c) * d;
+    double s = 0.0;
+    float q = 0.f;
+    for (uint64_t j = 0; j < d; ++j) {
+        s = s + double(r[j]);
+        q = fmaf(r[j], r[j], q);
+    }
+    csum[c] = s;
+    if (cnorm) cnorm[c] = q;
+}
+
+int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, float *cnorm, cudaStream_t st) {
+    if (k == 0) return MC_OK;
+    k_center_sums<<<(k + 63) / 64, 64, 0, st>>>(C, k, d, csum, cnorm), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+}  // namespace mc

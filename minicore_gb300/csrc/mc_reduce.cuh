@@ -1,0 +1,42 @@
+// Sorting / centroid / statistics launchers (mc_reduce.cu).
+#pragma once
+#include "mc_internal.cuh"
+
+namespace mc {
+
+constexpr uint64_t kSortTile = 8192;
+
+struct SortWork {
+    DBuf<uint32_t> tile_counts;   // [ntiles][k] counts, then per-tile cursors
+    DBuf<uint64_t> bucket_count;  // [k]
+    DBuf<uint64_t> bucket_start;  // [k+1]
+    DBuf<uint32_t> perm;          // rows grouped by bucket, ascending within a bucket
+    DBuf<uint64_t> chunk_count;   // [k]
+    DBuf<uint64_t> chunk_start;   // [k+1]
+    DBuf<double> partial;         // [chunks][d]
+    DBuf<double> partial_w;       // [chunks]
+};
+
+struct CentroidArgs {
+    bool csr = false;
+    uint64_t n = 0, d = 0;
+    uint32_t k = 0;
+    const float *X = nullptr;                 // dense
+    const float *vals = nullptr;              // CSR
+    const uint32_t *idx = nullptr;
+    const uint64_t *indptr = nullptr;
+    const uint32_t *keys = nullptr;           // cluster of each row
+    const uint32_t *keys2 = nullptr;          // optional second membership (0xffffffff none)
+    uint64_t extra_members = 0;               // number of valid keys2 entries
+    const double *w = nullptr;                // optional row weights
+    float *centers = nullptr;                 // [k][d], updated in place
+    int *nan_flag = nullptr;
+};
+
+int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, uint32_t k, SortWork &w,
+                       cudaStream_t st);
+int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st);
+int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st);
+int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, float *cnorm, cudaStream_t st);
+
+}  // namespace mc

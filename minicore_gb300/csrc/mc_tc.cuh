@@ -1,0 +1,27 @@
+// Tensor-core (tcgen05) SQRL2 assignment: BF16 / TF32 GEMM with FP32 accumulation in
+// TMEM, fused ||x||^2 - 2 x.c + ||c||^2 epilogue with row min / second min / argmin, and
+// an exact FP32 re-check of the rows whose margin falls below the rounding bound.
+#pragma once
+#include "mc_internal.cuh"
+
+namespace mc {
+
+struct TcState {
+    DBuf<__nv_bfloat16> Xb;      // [n][dp] bf16 copy of the rows (BF16 path)
+    DBuf<float> Xt;              // [n][dp] tf32-ready copy (TF32 path, d padded)
+    DBuf<__nv_bfloat16> Cb;      // [kp][dp]
+    DBuf<float> Ct;              // [kp][dp]
+    DBuf<float> cnorm_p;         // [kp] padded center norms
+    DBuf<uint32_t> flagged;      // rows to re-check
+    DBuf<uint64_t> nflag;        // device counter
+    DBuf<float> best2;           // scratch
+    const float *X_src = nullptr;
+    uint64_t n = 0, d = 0, dp = 0;
+    int prec = -1;
+};
+
+int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
+              int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
+              uint64_t *recheck_count);
+
+}  // namespace mc

@@ -742,32 +742,78 @@ int orc_sensitivity(uint64_t n, uint64_t ncenters, uint64_t k, const void *costs
     return 0;
 }
 
-// Vose alias table in FP64 over float weights: scaled q_i = p_i * n / sum(p) (sum in the
-// canonical det order).  Light (q < 1) and heavy (q >= 1) items are FIFO worklists in index
-// order; each light item takes the current heavy item as alias; a heavy item whose
-// residual drops below 1 moves to the back of the light list.
+// Canonical FP64 scan (mirrors the CUDA scan kernels): chunks of 8192 elements, 256
+// threads each owning a contiguous run of 32 elements scanned sequentially; run totals
+// scanned sequentially within the chunk; chunk totals scanned sequentially.  Exclusive
+// prefix of element e = (chunk offset + run offset) + local exclusive prefix.
+static void canon_exclusive_scan(const std::vector<double> &v, std::vector<double> &P) {
+    const uint64_t m = v.size();
+    P.assign(m + 1, 0.0);
+    const uint64_t G = (m + kChunk - 1) / kChunk;
+    double chunk_off = 0.0;
+    for (uint64_t g = 0; g < G; ++g) {
+        double run_off = 0.0;
+        for (uint64_t t = 0; t < kThreads; ++t) {
+            const uint64_t b = g * kChunk + t * kPer;
+            double loc = 0.0;
+            for (uint64_t e = b; e < std::min<uint64_t>(m, b + kPer); ++e) {
+                P[e] = (chunk_off + run_off) + loc;
+                loc = loc + v[e];
+            }
+            run_off = run_off + loc;
+        }
+        chunk_off = chunk_off + run_off;
+    }
+    P[m] = chunk_off;
+}
+
+// Alias table ("sweep" construction in closed form, FP64).  q_i = p_i * n / sum(p) with
+// the sum in the canonical det order.  Light items (q < 1, index order) have deficits
+// 1 - q, heavy items (q >= 1, index order) have excesses q - 1; D and E are their
+// canonical exclusive prefix sums.  Sweeping the lights in order against the heavies in
+// order, light i is served by the first heavy j with E[j+1] >= D[i]; heavy j runs out
+// while serving the first light i with D[i+1] > E[j+1] and then keeps probability
+// 1 - (D[i+1] - E[j+1]) with heavy j+1 as its alias.  The result is the table the
+// sequential sweep builds in exact arithmetic; every entry is computed independently.
 int orc_alias_build(uint64_t n, const float *probs, double *prob_tab, uint32_t *alias_tab) {
     if (n == 0) return 1;
     const double S = det_sum([&](uint64_t i) { return double(probs[i]); }, n);
     if (!(S > 0.0)) return 1;
     const double scale = double(n) / S;
-    std::vector<double> q(n);
-    std::vector<uint32_t> light, heavy;
+    std::vector<uint32_t> L, H;
+    std::vector<double> dl, eh;
+    auto q = [&](uint64_t i) { return double(probs[i]) * scale; };
     for (uint64_t i = 0; i < n; ++i) {
-        q[i] = double(probs[i]) * scale;
-        if (q[i] < 1.0) light.push_back(uint32_t(i)); else heavy.push_back(uint32_t(i));
+        if (q(i) < 1.0) { L.push_back(uint32_t(i)); dl.push_back(1.0 - q(i)); }
+        else { H.push_back(uint32_t(i)); eh.push_back(q(i) - 1.0); }
     }
-    size_t li = 0, hi = 0;
-    while (li < light.size() && hi < heavy.size()) {
-        const uint32_t l = light[li++];
-        const uint32_t g = heavy[hi];
-        prob_tab[l] = q[l];
-        alias_tab[l] = g;
-        q[g] = (q[g] + q[l]) - 1.0;
-        if (q[g] < 1.0) { light.push_back(g); ++hi; }
+    if (H.empty()) {
+        for (uint64_t i = 0; i < n; ++i) { prob_tab[i] = 1.0; alias_tab[i] = uint32_t(i); }
+        return 0;
     }
-    while (hi < heavy.size()) { const uint32_t g = heavy[hi++]; prob_tab[g] = 1.0; alias_tab[g] = g; }
-    while (li < light.size()) { const uint32_t l = light[li++]; prob_tab[l] = 1.0; alias_tab[l] = l; }
+    std::vector<double> D, E;
+    canon_exclusive_scan(dl, D);
+    canon_exclusive_scan(eh, E);
+    const uint64_t nl = L.size(), nh = H.size();
+    for (uint64_t i = 0; i < nl; ++i) {
+        // first j with E[j+1] >= D[i]
+        uint64_t lo = 0, hi = nh;  // search j in [0, nh)
+        while (lo < hi) { uint64_t mid = (lo + hi) / 2; if (E[mid + 1] >= D[i]) hi = mid; else lo = mid + 1; }
+        const uint64_t j = lo < nh ? lo : nh - 1;
+        prob_tab[L[i]] = q(L[i]);
+        alias_tab[L[i]] = H[j];
+    }
+    for (uint64_t j = 0; j < nh; ++j) {
+        uint64_t i = nl;
+        if (j + 1 < nh) {
+            // first i with D[i+1] > E[j+1]
+            uint64_t lo = 0, hi = nl;
+            while (lo < hi) { uint64_t mid = (lo + hi) / 2; if (D[mid + 1] > E[j + 1]) hi = mid; else lo = mid + 1; }
+            i = lo;
+        }
+        if (i < nl) { prob_tab[H[j]] = 1.0 - (D[i + 1] - E[j + 1]); alias_tab[H[j]] = H[j + 1]; }
+        else { prob_tab[H[j]] = 1.0; alias_tab[H[j]] = H[j]; }
+    }
     return 0;
 }
 

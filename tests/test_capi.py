@@ -1,0 +1,76 @@
+"""CPU checks of the drop-in boundary: the C-ABI library builds for sm_103a, loads, and
+exports every entry point that include/minicore_gb300.h declares (no GPU needed)."""
+import ctypes
+import os
+import re
+import subprocess
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "minicore_gb300.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    from minicore_gb300 import _lib
+    lib = _lib.load()
+    path = _lib.library_path()
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (mc_[a-z0-9_]+)", out))
+    declared = declared_symbols()
+    assert declared, "no declarations parsed"
+    missing = [s for s in declared if s not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    for s in declared:
+        assert hasattr(lib, s)
+        assert s in _lib.SIGNATURES, f"no ctypes signature for {s}"
+
+
+def test_library_targets_sm_103a():
+    from minicore_gb300 import _lib
+    path = _lib.library_path()
+    out = subprocess.run(["cuobjdump", "--list-elf", path], capture_output=True, text=True)
+    if out.returncode == 0:
+        assert "sm_103a" in out.stdout
+
+
+def test_host_only_entry_points():
+    from minicore_gb300 import _lib
+    lib = _lib.load()
+    assert b"sm_103a" in lib.mc_version()
+    import numpy as np
+    import oracle
+    u = np.empty(16)
+    assert lib.mc_uniforms(7, 3, 16, u.ctypes.data_as(ctypes.c_void_p)) == 0
+    assert np.array_equal(u, oracle.uniforms(7, 16, offset=3))
+
+
+def test_context_create_fails_cleanly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        return
+    from minicore_gb300 import _lib
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    rc = lib.mc_context_create(0, ctypes.byref(h))
+    assert rc != 0
+    assert lib.mc_last_error()
+
+
+def test_python_api_rejects_out_of_scope_options():
+    import numpy as np
+    import pytest
+    import minicore_gb300 as mc
+    X = np.zeros((4, 3), np.float32)
+    with pytest.raises(NotImplementedError):
+        mc.kmeanspp(X, 2, lspp=1)
+    with pytest.raises(NotImplementedError):
+        mc.kmeanspp(X, 2, n_local_trials=3)
+    with pytest.raises(NotImplementedError):
+        mc.hcluster(X, [0, 1], mbsize=2)
+    with pytest.raises(NotImplementedError):
+        mc.cluster(X, msr=2, k=2, temp=1.0)

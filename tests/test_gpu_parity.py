@@ -1,0 +1,266 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same seeded inputs.
+
+Bars: integer/index results (assignments, center ids, sampled indices) bit-exact; FP32
+distances bit-exact where both sides evaluate the same sequential float expression (dense
+SQRL2, L1, Hellinger), otherwise within the tolerance stated per test; FP64 sums exact where
+the canonical order is shared.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+pytestmark = pytest.mark.gpu
+
+MEASURES = [0, 2, 4, 5, 6]
+LOG_MEASURES = {4, 5}  # logf on the GPU and in glibc may differ in the last ulp
+REL = 2e-5             # distance tolerance for measures with logarithms / decompositions
+
+
+@pytest.fixture(scope="module")
+def mc():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import minicore_gb300
+    return minicore_gb300
+
+
+def _mixture(n, d, k, seed, spread=10.0, nonneg=False):
+    rng = np.random.default_rng(seed)
+    mu = rng.uniform(-spread, spread, (k, d))
+    X = mu[rng.integers(0, k, n)] + rng.normal(size=(n, d))
+    if nonneg:
+        X = np.abs(X)
+    return X.astype(np.float32)
+
+
+def _counts(n, d, density, seed):
+    rng = np.random.default_rng(seed)
+    M = sp.random(n, d, density=density, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.integers(1, 6, s).astype(np.float32))
+    M.sort_indices()
+    # every row non-empty
+    M = M.tolil()
+    for i in range(n):
+        if M.rows[i] == []:
+            M[i, int(rng.integers(0, d))] = 1.0
+    M = M.tocsr()
+    M.sort_indices()
+    return M.astype(np.float32)
+
+
+def _assign_gpu(mc, X, C, msr, prior, precision="fp32"):
+    import ctypes
+    from minicore_gb300 import _lib
+    M = mc._MatrixArg(X)
+    C = np.ascontiguousarray(C, np.float32)
+    asn = np.empty(M.n, np.uint32)
+    costs = np.empty(M.n, np.float64)
+    _lib.check(_lib.load().mc_assign(mc.default_context().handle, M.ref, mc._p(C), C.shape[0], msr, prior,
+                                     mc._PREC[precision], mc._p(asn), mc._p(costs)))
+    return asn, costs
+
+
+def _check_assign(orc, X, C, msr, prior, asn, costs, exact):
+    oasn, ocost = orc.assign(X, C, msr, prior)
+    if exact:
+        assert np.array_equal(asn, oasn)
+        assert np.array_equal(costs, ocost)
+        return
+    np.testing.assert_allclose(costs, ocost, rtol=REL, atol=1e-6)
+    diff = asn != oasn
+    if diff.any():
+        # only near-ties may differ: the oracle's distance to our center equals its best
+        Xd = X.toarray() if sp.issparse(X) else X
+        for i in np.nonzero(diff)[0][:50]:
+            d_ours = orc.msr_dense(msr, Xd[i], C[asn[i]], prior) if not sp.issparse(X) else \
+                orc.msr_sparse(msr, Xd[i], C[asn[i]], prior)
+            assert d_ours <= ocost[i] * (1 + 10 * REL) + 1e-6
+        assert diff.mean() < 1e-3
+
+
+@pytest.mark.parametrize("msr", MEASURES)
+@pytest.mark.parametrize("prior", [0.0, 1.0])
+def test_dense_assign_matches_oracle(mc, orc, msr, prior):
+    X = _mixture(3000, 37, 9, seed=msr, nonneg=msr != 2)
+    rng = np.random.default_rng(100 + msr)
+    C = X[rng.choice(len(X), 13, replace=False)] + 0.01
+    asn, costs = _assign_gpu(mc, X, C, msr, prior)
+    _check_assign(orc, X, C, msr, prior, asn, costs, exact=msr not in LOG_MEASURES)
+
+
+@pytest.mark.parametrize("msr", MEASURES)
+@pytest.mark.parametrize("prior", [0.0, 1.0])
+def test_csr_assign_matches_oracle(mc, orc, msr, prior):
+    X = _counts(1500, 300, 0.05, seed=msr)
+    rng = np.random.default_rng(7 + msr)
+    ids = rng.choice(X.shape[0], 7, replace=False)
+    C = np.asarray(X[ids].toarray(), np.float32)
+    C[:, ::7] += 0.5  # dense-ish centers, as means are
+    asn, costs = _assign_gpu(mc, X, C, msr, prior)
+    _check_assign(orc, X, C, msr, prior, asn, costs, exact=False)
+
+
+def test_assign_edge_cases(mc, orc):
+    # k = 1, ragged d, a single row, duplicate centers (ties -> lowest index)
+    X = _mixture(257, 5, 3, seed=1)
+    C = X[:1].copy()
+    asn, costs = _assign_gpu(mc, X, C, 2, 0.0)
+    assert np.all(asn == 0)
+    _check_assign(orc, X, C, 2, 0.0, asn, costs, exact=True)
+    C2 = np.concatenate([X[3:4], X[3:4], X[7:8]])
+    asn, costs = _assign_gpu(mc, X, C2, 2, 0.0)
+    assert not np.any(asn == 1)  # exact ties resolve to the lower index
+    _check_assign(orc, X, C2, 2, 0.0, asn, costs, exact=True)
+    asn, costs = _assign_gpu(mc, X[:1], C2, 2, 0.0)
+    _check_assign(orc, X[:1], C2, 2, 0.0, asn, costs, exact=True)
+    # many centers (several center tiles)
+    C3 = X[np.random.default_rng(0).choice(257, 200, replace=False)]
+    asn, costs = _assign_gpu(mc, X, C3, 2, 0.0)
+    _check_assign(orc, X, C3, 2, 0.0, asn, costs, exact=True)
+
+
+@pytest.mark.parametrize("msr", MEASURES)
+def test_kmeanspp_dense_matches_oracle(mc, orc, msr):
+    X = _mixture(4000, 24, 12, seed=3 + msr, nonneg=msr != 2)
+    prior = 0.5
+    k = 12
+    seed = 1234 + msr
+    ids, asn, costs = mc.kmeanspp(X, k, msr=msr, prior=prior, seed=seed)
+    oids, oasn, ocosts = orc.kmeanspp(X, k, msr, prior, orc.uniforms(seed, k))
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(asn.astype(np.uint32), oasn)
+    if msr in LOG_MEASURES:
+        np.testing.assert_allclose(costs, ocosts.astype(np.float32), rtol=REL, atol=1e-6)
+    else:
+        assert np.array_equal(costs, ocosts.astype(np.float32))
+
+
+def test_kmeanspp_weighted_and_csr(mc, orc):
+    X = _mixture(3000, 16, 8, seed=11)
+    w = np.random.default_rng(2).random(3000) + 0.1
+    ids, asn, costs = mc.kmeanspp(X, 8, msr=2, seed=99, weights=w)
+    oids, oasn, ocosts = orc.kmeanspp(X, 8, 2, 0.0, orc.uniforms(99, 8), weights=w)
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(costs, ocosts.astype(np.float32))
+    S = _counts(2000, 200, 0.05, seed=4)
+    for msr in (2, 5, 4):
+        ids, asn, costs = mc.kmeanspp(S, 10, msr=msr, prior=1.0, seed=5)
+        oids, oasn, ocosts = orc.kmeanspp(S, 10, msr, 1.0, orc.uniforms(5, 10))
+        assert costs.dtype == np.float64
+        np.testing.assert_allclose(costs, ocosts, rtol=1e-4, atol=1e-5)
+        assert (ids == oids).mean() >= 0.8
+
+
+def test_hcluster_dense_sqrl2_bit_exact(mc, orc):
+    # the small reference configuration: 25-component mixture, kmeans++, 20 updates
+    rng = np.random.default_rng(0)
+    mu = rng.uniform(-10, 10, (25, 50))
+    X = (mu[rng.integers(0, 25, 10000)] + rng.normal(size=(10000, 50))).astype(np.float32)
+    ids, _, _ = mc.kmeanspp(X, 25, msr=2, seed=42)
+    C0 = X[ids.astype(np.int64)]
+    res = mc.hcluster(X, ids.astype(np.int64), msr=2, eps=0.0, maxiter=19, seed=3)
+    ores = orc.hcluster(X, C0, 2, 0.0, eps=0.0, maxiter=19, seed=3)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(res["centers"], ores["centers"])
+    assert np.array_equal(res["costs"], ores["costs"].astype(np.float32))
+    assert res["initcost"] == ores["initcost"] and res["finalcost"] == ores["finalcost"]
+
+
+@pytest.mark.parametrize("msr", [0, 4, 5, 6])
+def test_hcluster_other_measures(mc, orc, msr):
+    X = _mixture(2000, 20, 6, seed=20 + msr, nonneg=True)
+    C0 = X[:6].copy()
+    res = mc.hcluster(X, C0, msr=msr, prior=1.0, eps=1e-10, maxiter=8, seed=5)
+    ores = orc.hcluster(X, C0, msr, 1.0, eps=1e-10, maxiter=8, seed=5)
+    np.testing.assert_allclose(res["finalcost"], ores["finalcost"], rtol=1e-5)
+    assert (res["asn"] == ores["asn"]).mean() > 0.999
+    np.testing.assert_allclose(res["centers"], ores["centers"], rtol=1e-5, atol=1e-6)
+
+
+def test_hcluster_csr_mkl(mc, orc):
+    X = _counts(3000, 400, 0.04, seed=9)
+    ids = np.arange(0, 3000, 300)
+    C0 = np.asarray(X[ids].toarray(), np.float32)
+    res = mc.hcluster(X, ids, msr=5, prior=1.0, eps=1e-10, maxiter=6, seed=1)
+    ores = orc.hcluster(X, C0, 5, 1.0, eps=1e-10, maxiter=6, seed=1)
+    np.testing.assert_allclose(res["finalcost"], ores["finalcost"], rtol=1e-4)
+    assert (res["asn"] == ores["asn"]).mean() > 0.995
+    (data, idx, indptr), shape = res["centers"]
+    Cg = sp.csr_matrix((data, idx.astype(np.int64), indptr.astype(np.int64)), shape=tuple(shape)).toarray()
+    np.testing.assert_allclose(Cg, ores["centers"], rtol=1e-4, atol=1e-6)
+
+
+def test_hcluster_empty_cluster_restart(mc, orc):
+    # a far-away duplicate center attracts no rows -> D^2 restart path
+    X = _mixture(3000, 8, 4, seed=31)
+    C0 = np.concatenate([X[:4], np.full((1, 8), 1e3, np.float32)])
+    res = mc.hcluster(X, C0, msr=2, eps=0.0, maxiter=4, seed=77)
+    ores = orc.hcluster(X, C0, 2, 0.0, eps=0.0, maxiter=4, seed=77)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(res["centers"], ores["centers"])
+
+
+def test_hcluster_weighted(mc, orc):
+    X = _mixture(5000, 12, 7, seed=41)
+    w = np.random.default_rng(1).random(5000) * 3
+    C0 = X[:7].copy()
+    res = mc.hcluster(X, C0, msr=2, weights=w, eps=0.0, maxiter=6, seed=2)
+    ores = orc.hcluster(X, C0, 2, 0.0, weights=w, eps=0.0, maxiter=6, seed=2)
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(res["centers"], ores["centers"])
+    assert res["finalcost"] == ores["finalcost"]
+
+
+@pytest.mark.parametrize("method", [0, 1, 2, 3, 4])
+def test_coreset_sampler_bit_exact(mc, orc, method):
+    rng = np.random.default_rng(method)
+    n, nc = 20000, 20
+    asn = rng.integers(0, nc, n).astype(np.uint32)
+    costs = (rng.integers(0, 3, n) + rng.random(n)).astype(np.float32)
+    w = (1.0 / (rng.integers(0, 5, n) + 1)).astype(np.float32)
+    for weights in (None, w):
+        cs = mc.CoresetSampler()
+        cs.make_sampler(nc, costs, asn, weights=weights, sens=method)
+        p = cs.get_probs()
+        op = orc.sensitivity(costs, asn, nc, method, weights=weights)
+        assert np.array_equal(p, op)
+        pt, at = cs.alias_table()
+        opt, oat = orc.alias_build(op)
+        assert np.array_equal(at, oat)
+        assert np.array_equal(pt, opt)
+        for unique in (False, True):
+            wo, io = cs.sample(3000, seed=17, unique=unique)
+            owo, oio = orc.coreset_sample(op, opt, oat, 3000, seed=17, unique=unique, weights=weights,
+                                          method=method, b=nc)
+            assert np.array_equal(io, oio)
+            assert np.array_equal(wo, owo)
+
+
+def test_coreset_sampler_costs_f64_and_errors(mc, orc):
+    rng = np.random.default_rng(5)
+    n = 5000
+    asn = rng.integers(0, 10, n).astype(np.uint32)
+    costs = rng.random(n)
+    cs = mc.CoresetSampler()
+    cs.make_sampler(10, costs, asn, sens=4)
+    assert np.array_equal(cs.get_probs(), orc.sensitivity(costs, asn, 10, 4))
+    bad = asn.copy()
+    bad[3] = 10
+    with pytest.raises(ValueError):
+        mc.CoresetSampler().make_sampler(10, costs, bad)
+    with pytest.raises(ValueError):
+        mc.CoresetSampler().make_sampler(10, costs.astype(np.int32), asn)
+
+
+def test_det_sums_match(mc, orc):
+    # objective totals share the canonical FP64 order
+    X = _mixture(100_003, 4, 3, seed=8)
+    C = X[:3].copy()
+    j = mc.Job(X, C, msr=2)
+    j.assign()
+    c = j.cost()
+    _, ocosts = orc.assign(X, C, 2, 0.0)
+    assert c == float(np.float32(orc.det_sum(ocosts)))
