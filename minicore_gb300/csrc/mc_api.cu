@@ -302,8 +302,9 @@ int job_set_centroids(mc_job *j, int *restarted) {
             }
             MC_CUDA_TRY(cudaGetLastError());
         }
-        // full exact reassignment (the reference passes prior[0] as the prior sum here)
-        MC_TRY(job_assign_with(j, j->Cw.p, double(float(j->prior)), true));
+        // full reassignment (the reference passes prior[0] as the prior sum here); the
+        // tensor-core path returns the exact FP32 assignment, so it serves here too
+        MC_TRY(job_assign_with(j, j->Cw.p, double(float(j->prior)), false));
         MC_TRY(j->asn2.alloc(n, st));
         MC_CUDA_TRY(cudaMemsetAsync(j->asn2.p, 0xff, n * sizeof(uint32_t), st));
         std::vector<uint32_t> cur(rsel.size());

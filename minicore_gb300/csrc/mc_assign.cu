@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(256) k_assign_tiled(AssignArgs a) {
                     const int r = e / kBK, kk = e % kBK;
                     const uint64_t row = row0 + r;
                     float x = 0.f;
-                    if (row < a.n && kk < kmax) x = a.X[row * d + k0 + kk];
+                    if (row < a.n && kk < kmax) x = a.X[(a.rows ? uint64_t(a.rows[row]) : row) * d + k0 + kk];
                     if (PAIR) {
                         Xs0[r][kk] = x;
                     } else {
@@ -387,8 +387,9 @@ __global__ void __launch_bounds__(256) k_assign_tiled(AssignArgs a) {
                 const bool nan0 = best[i].v == __int_as_float(0xff800000);
                 double cost = nan0 ? __longlong_as_double(0x7ff8000000000000ll) : key_to_cost<MSR>(best[i].v);
                 if (CSR) cost = double(float(cost));
-                a.asn[row] = best[i].j;
-                a.costs[row] = cost;
+                const uint64_t orow = a.rows ? uint64_t(a.rows[row]) : row;
+                a.asn[orow] = best[i].j;
+                a.costs[orow] = cost;
             }
         }
     }

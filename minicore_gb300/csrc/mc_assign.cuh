@@ -9,6 +9,7 @@ struct AssignArgs {
     uint64_t n = 0, d = 0;
     uint32_t k = 0, kp = 0;           // centers, padded center count of CT0/CT1
     const float *X = nullptr;         // dense rows
+    const uint32_t *rows = nullptr;   // dense only: optional row list (row r of the pass = X row rows[r])
     const float *vals = nullptr;      // CSR rows
     const uint32_t *idx = nullptr;
     const uint64_t *indptr = nullptr;

@@ -1,10 +1,688 @@
+// Tensor-core SQRL2 assignment for dense rows (tcgen05, sm_103a).
+//
+// For SQRL2 the argmin over centers of ||x - c||^2 equals the argmin of
+// v_j = ||c_j||^2 - 2 x.c_j.  The dot products x.c_j come from a BF16 (or TF32) GEMM with
+// FP32 accumulation: A = rows (128-row tiles, K-major), B = centers (256-center chunks,
+// K-major), both staged in shared memory by TMA (128-byte swizzle), accumulators in TMEM
+// (two 256-column buffers so the epilogue drains one while the MMA fills the other).
+//
+// Rounding bound.  With per-operand relative rounding u (BF16 round-to-nearest: 2^-9;
+// TF32 operands taken by truncation: 2^-10) and FP32 accumulation over d products,
+//   |v_j - v*_j| <= 2 eta ||x|| ||c_j||,   eta = 2u + u^2 + d 2^-22.
+// Every center whose exact distance can be the row's minimum satisfies v_j <= b1 + Delta,
+//   Delta = 4 eta ||x|| Cmax + 4 gamma_d (||x|| + Cmax)^2,
+// where b1 is the row's smallest tensor-core value, Cmax = max_j ||c_j|| and the gamma term
+// covers FP32 rounding of the norms and of the exact sequential distance
+// (gamma_d = d 2^-24 / (1 - d 2^-24)).
+//
+// Two passes over the same MMAs (the tensor cores are deterministic, so both passes see
+// identical values): pass 1 keeps only each row's minimum b1 (branch-free epilogue);
+// pass 2 lists every center with v_j <= b1 + Delta (up to 4 per column half).  The
+// finalize pass evaluates the exact FP32 distance (sequential fmaf over columns, the FP32
+// path's expression) of each candidate and keeps the smallest, lowest index on ties; rows
+// with more candidates than slots are rescanned exactly over all centers.  So the
+// assignment equals the FP32 path's on every row and costs are exact FP32 distances.
+//
+// Every mbarrier wait is bounded (about one second of clock64 cycles); on a timeout the
+// kernel records an error code, stops issuing, waits (bounded) for its copies and MMAs in
+// flight, frees its TMEM and returns.
+#include <cuda.h>
+
+#include <cmath>
+
+#include "mc_assign.cuh"
 #include "mc_tc.cuh"
 
 namespace mc {
 
-int tc_assign(TcState &, const float *, uint64_t, uint64_t, const float *, const float *, uint32_t, int,
-              const float *, uint32_t *, double *, int, cudaStream_t, uint64_t *) {
-    return fail(MC_EUNSUPPORTED, "tensor-core assignment not built");
+namespace tc {
+
+constexpr int BM = 128;           // rows per tile (MMA M)
+constexpr int BN = 256;           // centers per chunk (MMA N)
+constexpr int KBYTES = 128;       // bytes of K per k-block (one 128B swizzle row)
+constexpr int STAGES = 4;
+constexpr int A_STAGE = BM * KBYTES;   // 16 KB
+constexpr int B_STAGE = BN * KBYTES;   // 32 KB
+constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
+constexpr int NCAND = 4;             // candidate slots per row and column half
+constexpr int EPI_WARPS = 8;      // two per TMEM lane quarter, each taking half of a chunk's columns
+constexpr int THREADS = 64 + 32 * EPI_WARPS;  // warp 0 TMA, warp 1 MMA (+TMEM alloc), warps 2-9 epilogue
+constexpr int CN_SMEM = 4096;     // center norms staged in shared memory when kp <= CN_SMEM
+constexpr uint32_t TMEM_COLS = 512;
+constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
+
+struct Smem {
+    uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], drain;
+    uint32_t tmem_base;
+    int abort;
+    int outstanding[STAGES];
+    uint32_t out_parity[STAGES];
+};
+
+__device__ inline uint32_t smem_u32(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ inline void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ inline void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ inline void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ inline bool mbar_try(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// bounded wait; returns false on timeout or when another role aborted
+__device__ inline bool mbar_wait(uint64_t *bar, uint32_t parity, Smem *sm, int *err, int code) {
+    if (mbar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try(bar, parity)) return true;
+        if ((it & 255u) == 0) {
+            if (*(volatile int *)&sm->abort) return false;
+            if (clock64() - t0 > WAIT_CYCLES) {
+                atomicExch(&sm->abort, 1);
+                atomicCAS(err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+
+// wait with a bound but without the abort check (used while draining after an abort)
+__device__ inline void mbar_drain(uint64_t *bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity)) {
+        if (clock64() - t0 > WAIT_CYCLES) return;
+    }
+}
+
+__device__ inline void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+        : "memory");
+}
+
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row atoms 1024 B apart
+__device__ inline uint64_t sdesc(const void *p) {
+    const uint64_t addr = smem_u32(p);
+    uint64_t d = 0;
+    d |= (addr >> 4) & 0x3FFFull;          // start address
+    d |= uint64_t(1) << 16;                // leading byte offset (unused for K-major swizzle)
+    d |= uint64_t(1024 >> 4) << 32;        // stride byte offset: 8 rows x 128 B
+    d |= uint64_t(1) << 46;                // descriptor version
+    d |= uint64_t(2) << 61;                // 128-byte swizzle
+    return d;
+}
+
+template <bool TF32>
+__device__ inline uint32_t idesc() {
+    // D = F32 (bits 4-5 = 1); A/B format BF16 = 1 or TF32 = 2 (bits 7-9, 10-12); both
+    // K-major; N >> 3 at bits 17-22; M >> 4 at bits 24-28
+    const uint32_t fmt = TF32 ? 2u : 1u;
+    return (1u << 4) | (fmt << 7) | (fmt << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
+}
+
+template <bool TF32>
+__device__ inline void mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+    const uint32_t id = idesc<TF32>();
+    if (TF32) {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(id), "r"(accumulate)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(adesc), "l"(bdesc), "r"(id), "r"(accumulate)
+            : "memory");
+    }
+}
+
+__device__ inline void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ inline void tmem_ld16(uint32_t taddr, float *v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ inline void tmem_ld32(uint32_t taddr, float *v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ inline void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ inline void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+}  // namespace tc
+
+struct TcArgs {
+    uint64_t n, d;
+    uint32_t k, kb, nchunks, ntiles;
+    const float *rownorm;  // [n] row squared norms
+    float eta, gamma;
+    const float *cnp;      // [kp] center norms, +inf past k; [kp] holds Cmax
+    uint32_t kp;
+    float *b1;             // [n][2] pass 1 output: minimum per row and column half
+    uint8_t *cnt;          // [n][2] pass 2 output: candidates per column half (255: too many)
+    uint32_t *cand;        // [n][2][NCAND] pass 2 output: candidate centers
+    int *err;
+};
+
+enum TcMode { TC_MIN = 0, TC_CAND = 1 };
+
+template <bool TF32, int MODE>
+__global__ void __launch_bounds__(tc::THREADS, 1)
+    k_tc_assign(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
+    using namespace tc;
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char *base = reinterpret_cast<unsigned char *>((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
+    unsigned char *stages = base;
+    float *cn_s = reinterpret_cast<float *>(base + STAGES * STAGE_BYTES);
+    Smem *sm = reinterpret_cast<Smem *>(base + STAGES * STAGE_BYTES + CN_SMEM * sizeof(float));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool cn_in_smem = a.kp <= CN_SMEM;
+    if (cn_in_smem)
+        for (uint32_t j = threadIdx.x; j < a.kp; j += THREADS) cn_s[j] = a.cnp[j];
+    const float *cnp = cn_in_smem ? cn_s : a.cnp;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&sm->full[s], 1);
+            mbar_init(&sm->empty[s], 1);
+            sm->outstanding[s] = 0;
+            sm->out_parity[s] = 0;
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&sm->acc_full[b], 1);
+            mbar_init(&sm->acc_empty[b], 32 * EPI_WARPS);
+        }
+        mbar_init(&sm->drain, 1);
+        sm->abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm->tmem_base)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = sm->tmem_base;
+    const uint32_t total_it = a.nchunks * a.kb;  // k-block iterations per row tile
+
+    if (warp == 0) {
+        // ---------------- TMA producer ----------------
+        if (lane == 0) {
+            uint32_t s = 0, ph = 0;
+            bool ok = true;
+            for (uint32_t m = blockIdx.x; m < a.ntiles && ok; m += gridDim.x) {
+                for (uint32_t it = 0; it < total_it && ok; ++it) {
+                    const uint32_t nc = it / a.kb, kb = it % a.kb;
+                    if (!mbar_wait(&sm->empty[s], ph ^ 1, sm, a.err, 1)) { ok = false; break; }
+                    unsigned char *st = stages + s * STAGE_BYTES;
+                    mbar_expect_tx(&sm->full[s], STAGE_BYTES);
+                    sm->outstanding[s] = 1;
+                    sm->out_parity[s] = ph;
+                    const int kcoord = int(kb) * (TF32 ? 32 : 64);
+                    tma_load_2d(st, &tmA, &sm->full[s], kcoord, int(m * BM));
+                    tma_load_2d(st + A_STAGE, &tmB, &sm->full[s], kcoord, int(nc * BN));
+                    if (++s == STAGES) { s = 0; ph ^= 1; }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0) {
+            uint32_t s = 0, ph = 0;
+            uint32_t acc_it = 0;
+            bool ok = true;
+            for (uint32_t m = blockIdx.x; m < a.ntiles && ok; m += gridDim.x) {
+                for (uint32_t nc = 0; nc < a.nchunks && ok; ++nc, ++acc_it) {
+                    const uint32_t buf = acc_it & 1, use = acc_it >> 1;
+                    if (!mbar_wait(&sm->acc_empty[buf], (use & 1) ^ 1, sm, a.err, 2)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d_tmem = tmem + buf * BN;
+                    for (uint32_t kb = 0; kb < a.kb; ++kb) {
+                        if (!mbar_wait(&sm->full[s], ph, sm, a.err, 3)) { ok = false; break; }
+                        sm->outstanding[s] = 0;
+                        fence_after();
+                        unsigned char *st = stages + s * STAGE_BYTES;
+                        const uint64_t ad = sdesc(st), bd = sdesc(st + A_STAGE);
+#pragma unroll
+                        for (int ks = 0; ks < 4; ++ks) {
+                            // +32 bytes of K per MMA within the 128-byte swizzle row
+                            mma<TF32>(d_tmem, ad + uint64_t(ks * 2), bd + uint64_t(ks * 2), (kb | ks) ? 1u : 0u);
+                        }
+                        mma_commit(&sm->empty[s]);
+                        if (++s == STAGES) { s = 0; ph ^= 1; }
+                    }
+                    if (ok) mma_commit(&sm->acc_full[buf]);
+                }
+            }
+            // all MMAs issued by this thread complete before the drain barrier fires
+            mma_commit(&sm->drain);
+            mbar_drain(&sm->drain, 0);
+        }
+    } else {
+        // ---------------- epilogue (warps 2-9) ----------------
+        const int quarter = warp & 3;                 // TMEM lanes 32*quarter .. +31
+        const int half = (warp - 2) >> 2;             // columns [128*half, 128*half + 128) of a chunk
+        const uint32_t lane_base = uint32_t(quarter * 32) << 16;
+        const int rloc = quarter * 32 + lane;
+        uint32_t acc_it = 0;
+        bool ok = true;
+        const float cmax = a.cnp[a.kp];
+        for (uint32_t m = blockIdx.x; m < a.ntiles && ok; m += gridDim.x) {
+            const uint64_t row = uint64_t(m) * BM + rloc;
+            const bool valid = row < a.n;
+            float b1 = __int_as_float(0x7f800000);   // pass 1: running minimum
+            float thr = __int_as_float(0xff800000);  // pass 2: fixed candidate threshold
+            int ncand = 0;
+            if (MODE == TC_CAND && valid) {
+                const float bb = fminf(a.b1[2 * row], a.b1[2 * row + 1]);
+                const float xn = sqrtf(a.rownorm[row]);
+                const float delta = 4.f * a.eta * xn * cmax * 1.0001f + 4.f * a.gamma * (xn + cmax) * (xn + cmax);
+                // no finite minimum or a non-finite bound proves nothing: no candidates, and
+                // the finalize pass rescans the row exactly
+                if (bb < __int_as_float(0x7f800000) && delta <= 3.402823466e+38f) thr = bb + delta;
+            }
+            uint32_t *cdst = a.cand + (row * 2 + half) * NCAND;
+            for (uint32_t nc = 0; nc < a.nchunks; ++nc, ++acc_it) {
+                const uint32_t buf = acc_it & 1, use = acc_it >> 1;
+                // one lane waits, the warp follows converged (tcgen05.ld is warp-collective)
+                int got = 0;
+                if (lane == 0) got = mbar_wait(&sm->acc_full[buf], use & 1, sm, a.err, 4) ? 1 : 0;
+                got = __shfl_sync(0xffffffffu, got, 0);
+                __syncwarp();
+                if (!got) { ok = false; break; }
+                fence_after();
+                const uint32_t taddr = tmem + lane_base + buf * BN + half * (BN / 2);
+#pragma unroll 1
+                for (int g = 0; g < BN / 2 / 32; ++g) {
+                    float v[32];
+                    tmem_ld32(taddr + g * 32, v);
+                    const uint32_t j0 = nc * BN + half * (BN / 2) + g * 32;
+                    const float4 *c4 = reinterpret_cast<const float4 *>(cnp + j0);
+#pragma unroll
+                    for (int q4 = 0; q4 < 8; ++q4) {
+                        const float4 c = c4[q4];
+                        v[4 * q4 + 0] = fmaf(-2.f, v[4 * q4 + 0], c.x);
+                        v[4 * q4 + 1] = fmaf(-2.f, v[4 * q4 + 1], c.y);
+                        v[4 * q4 + 2] = fmaf(-2.f, v[4 * q4 + 2], c.z);
+                        v[4 * q4 + 3] = fmaf(-2.f, v[4 * q4 + 3], c.w);
+                    }
+                    float smin[4];
+#pragma unroll
+                    for (int sg = 0; sg < 4; ++sg) {
+                        const float *w = v + 8 * sg;
+                        smin[sg] = fminf(fminf(fminf(w[0], w[1]), fminf(w[2], w[3])),
+                                         fminf(fminf(w[4], w[5]), fminf(w[6], w[7])));
+                    }
+                    if (MODE == TC_MIN) {
+                        b1 = fminf(b1, fminf(fminf(smin[0], smin[1]), fminf(smin[2], smin[3])));
+                    } else {
+                        const float gmin = fminf(fminf(smin[0], smin[1]), fminf(smin[2], smin[3]));
+                        if (gmin <= thr) {  // candidates in this group (rare per row)
+#pragma unroll
+                            for (int sg = 0; sg < 4; ++sg) {
+                                if (smin[sg] <= thr) {
+#pragma unroll
+                                    for (int q8 = 0; q8 < 8; ++q8) {
+                                        if (v[8 * sg + q8] <= thr) {
+                                            if (ncand < NCAND) cdst[ncand] = j0 + uint32_t(8 * sg + q8);
+                                            ++ncand;
+                                        }
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                fence_before();
+                mbar_arrive(&sm->acc_empty[buf]);
+            }
+            if (!ok) break;
+            if (valid) {
+                if (MODE == TC_MIN) a.b1[2 * row + half] = b1;
+                else a.cnt[2 * row + half] = ncand > NCAND ? uint8_t(255) : uint8_t(ncand);
+            }
+        }
+    }
+    // ---------------- teardown ----------------
+    __syncthreads();
+    if (threadIdx.x == 0 && sm->abort) {
+        // copies still in flight into this CTA's shared memory: wait for them (bounded)
+        for (int s = 0; s < STAGES; ++s)
+            if (sm->outstanding[s]) mbar_drain(&sm->full[s], sm->out_parity[s]);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// ------------------------------------------------------------------------------------
+// support kernels
+// ------------------------------------------------------------------------------------
+__global__ void k_to_bf16_pad(const float *__restrict__ X, uint64_t n, uint64_t d, uint64_t dp,
+                              __nv_bfloat16 *__restrict__ Y) {
+    const uint64_t total = n * dp;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x)) {
+        const uint64_t r = e / dp, c = e % dp;
+        Y[e] = __float2bfloat16_rn(c < d ? X[r * d + c] : 0.f);
+    }
+}
+
+__global__ void k_pad_f32(const float *__restrict__ X, uint64_t n, uint64_t d, uint64_t dp, float *__restrict__ Y) {
+    const uint64_t total = n * dp;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x)) {
+        const uint64_t r = e / dp, c = e % dp;
+        Y[e] = c < d ? X[r * d + c] : 0.f;
+    }
+}
+
+__global__ void k_center_prep_tc(const float *__restrict__ C, uint32_t k, uint32_t kp, uint64_t d, uint64_t dp,
+                                 int tf32, __nv_bfloat16 *Cb, float *Ct, const float *cn, float *cnp) {
+    const uint64_t total = uint64_t(kp) * dp;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x)) {
+        const uint64_t r = e / dp, c = e % dp;
+        const float v = (r < k && c < d) ? C[r * d + c] : 0.f;
+        if (tf32) Ct[e] = v;
+        else Cb[e] = __float2bfloat16_rn(v);
+    }
+    // padded norms (+inf past k) and the max center norm at cnp[kp] (norms are non-negative,
+    // so their bit patterns order like the values)
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < kp; j += gridDim.x * blockDim.x) {
+        cnp[j] = j < k ? cn[j] : __int_as_float(0x7f800000);
+        if (j < k) atomicMax(reinterpret_cast<int *>(cnp + kp), __float_as_int(sqrtf(cn[j])));
+    }
+}
+
+// Exact FP32 distances for the candidate centers of every row (sequential fmaf over the
+// columns: the FP32 path's expression).  A CTA stages 128 rows x 32 columns in shared
+// memory (coalesced); each thread walks its row against its candidates (up to 4 per column
+// half).  Rows with too many candidates, or none (NaN rows, non-finite bound), are listed
+// for an exact scan over all centers.
+constexpr int NSLOT = 2 * tc::NCAND;
+
+__global__ void __launch_bounds__(128) k_tc_finalize(const float *__restrict__ X, uint64_t n, uint64_t d,
+                                                      const float *__restrict__ C, uint32_t k, uint32_t *asn,
+                                                      const uint8_t *__restrict__ cnt,
+                                                      const uint32_t *__restrict__ cand, double *costs,
+                                                      unsigned long long *nrecheck, uint32_t *over_rows,
+                                                      unsigned long long *nover) {
+    __shared__ float xs[128][33];
+    const int t = threadIdx.x;
+    const uint64_t row0 = uint64_t(blockIdx.x) * 128;
+    const uint64_t row = row0 + t;
+    // cj[q] == 0xffffffff marks an unused slot
+    uint32_t cj[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) cj[q] = 0xffffffffu;
+    if (row < n) {
+        const int c0 = cnt[2 * row], c1 = cnt[2 * row + 1];
+        if (c0 == 255 || c1 == 255 || c0 + c1 == 0) {
+            over_rows[atomicAdd(nover, 1ull)] = uint32_t(row);
+        } else {
+            if (c0 + c1 > 1) atomicAdd(nrecheck, 1ull);
+#pragma unroll
+            for (int q = 0; q < NSLOT; ++q) {
+                const int h = q / tc::NCAND, s = q % tc::NCAND;
+                if (s < (h ? c1 : c0)) {
+                    const uint32_t j = cand[row * NSLOT + q];
+                    cj[q] = j < k ? j : 0xffffffffu;
+                }
+            }
+        }
+    }
+    float acc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) acc[q] = 0.f;
+    const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+    for (uint64_t k0 = 0; k0 < d; k0 += 32) {
+        const int kmax = int(umin64(32, d - k0));
+        __syncthreads();
+        for (int e = t; e < 128 * 32; e += 128) {
+            const int r = e >> 5, kk = e & 31;
+            const uint64_t rr = row0 + r;
+            xs[r][kk] = (rr < n && kk < kmax) ? X[rr * d + k0 + kk] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < NSLOT; ++q) {
+            if (cj[q] != 0xffffffffu) {
+                const float *cr = C + uint64_t(cj[q]) * d + k0;
+                float a = acc[q];
+                if (vec4 && kmax == 32) {
+                    const float4 *c4 = reinterpret_cast<const float4 *>(cr);
+#pragma unroll
+                    for (int k4 = 0; k4 < 8; ++k4) {
+                        const float4 c = __ldg(c4 + k4);
+                        float df = c.x - xs[t][4 * k4 + 0];
+                        a = fmaf(df, df, a);
+                        df = c.y - xs[t][4 * k4 + 1];
+                        a = fmaf(df, df, a);
+                        df = c.z - xs[t][4 * k4 + 2];
+                        a = fmaf(df, df, a);
+                        df = c.w - xs[t][4 * k4 + 3];
+                        a = fmaf(df, df, a);
+                    }
+                } else {
+                    for (int kk = 0; kk < kmax; ++kk) {
+                        const float df = __ldg(cr + kk) - xs[t][kk];
+                        a = fmaf(df, df, a);
+                    }
+                }
+                acc[q] = a;
+            }
+        }
+    }
+    uint32_t best = 0xffffffffu;
+    float bv = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int q = 0; q < NSLOT; ++q) {
+        if (cj[q] != 0xffffffffu && (best == 0xffffffffu || acc[q] < bv || (acc[q] == bv && cj[q] < best))) {
+            bv = acc[q];
+            best = cj[q];
+        }
+    }
+    if (best == 0xffffffffu) return;
+    asn[row] = best;
+    costs[row] = double(bv);
+}
+
+// ------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+static int make_map(CUtensorMap *map, const void *ptr, bool tf32, uint64_t rows, uint64_t cols, uint64_t pitch_elems,
+                    uint32_t box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return fail(MC_ECUDA, "cuTensorMapEncodeTiled unavailable");
+    const uint64_t esz = tf32 ? 4 : 2;
+    cuuint64_t dims[2] = {cuuint64_t(cols), cuuint64_t(rows)};
+    cuuint64_t strides[1] = {cuuint64_t(pitch_elems * esz)};
+    cuuint32_t box[2] = {cuuint32_t(tc::KBYTES / esz), box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                    const_cast<void *>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(MC_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(int(r)));
+    return MC_OK;
+}
+
+int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
+              int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
+              uint64_t *recheck_count) {
+    const bool tf32 = precision == MC_TF32;
+    const uint64_t esz = tf32 ? 4 : 2;
+    const uint64_t kelems = tc::KBYTES / esz;            // K elements per k-block
+    const uint64_t dp = (d + 7) / 8 * 8;                 // 16-byte row pitch for both types
+    const uint32_t kb = uint32_t((d + kelems - 1) / kelems);
+    const uint32_t kp = (k + tc::BN - 1) / tc::BN * tc::BN;
+    const unsigned cg = unsigned(umin64((n * dp + 255) / 256, uint64_t(sms) * 64));
+    // resident operand copy of the rows (once per matrix / precision)
+    if (s.X_src != X || s.prec != precision || s.n != n || s.d != d) {
+        if (tf32) {
+            if (d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0) {
+                s.Xt.release();
+            } else {
+                MC_TRY(s.Xt.alloc(n * dp, st));
+                k_pad_f32<<<cg, 256, 0, st>>>(X, n, d, dp, s.Xt.p), note_launch();
+            }
+        } else {
+            MC_TRY(s.Xb.alloc(n * dp, st));
+            k_to_bf16_pad<<<cg, 256, 0, st>>>(X, n, d, dp, s.Xb.p), note_launch();
+        }
+        MC_CUDA_TRY(cudaGetLastError());
+        s.X_src = X;
+        s.prec = precision;
+        s.n = n;
+        s.d = d;
+        s.dp = dp;
+    }
+    const void *Aptr = tf32 ? (s.Xt.p ? (const void *)s.Xt.p : (const void *)X) : (const void *)s.Xb.p;
+    const uint64_t apitch = tf32 ? (s.Xt.p ? dp : d) : dp;
+    // centers: padded operand copy + max norm
+    MC_TRY(s.cnorm_p.alloc(uint64_t(kp) + 1, st));  // padded norms + Cmax
+    MC_CUDA_TRY(cudaMemsetAsync(s.cnorm_p.p + kp, 0, sizeof(float), st));
+    if (tf32) MC_TRY(s.Ct.alloc(uint64_t(kp) * dp, st));
+    else MC_TRY(s.Cb.alloc(uint64_t(kp) * dp, st));
+    k_center_prep_tc<<<unsigned(umin64((uint64_t(kp) * dp + 255) / 256, 4096)), 256, 0, st>>>(
+        C, k, kp, d, dp, tf32 ? 1 : 0, s.Cb.p, s.Ct.p, cnorm, s.cnorm_p.p), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    CUtensorMap mA, mB;
+    MC_TRY(make_map(&mA, Aptr, tf32, n, d, apitch, tc::BM));
+    MC_TRY(make_map(&mB, tf32 ? (const void *)s.Ct.p : (const void *)s.Cb.p, tf32, kp, d, dp, tc::BN));
+    MC_TRY(s.b1.alloc(2 * n, st));
+    MC_TRY(s.cnt.alloc(2 * n, st));
+    MC_TRY(s.cand.alloc(n * NSLOT, st));
+    MC_TRY(s.err.alloc(1, st));
+    MC_TRY(s.nrecheck.alloc(2, st));
+    MC_CUDA_TRY(cudaMemsetAsync(s.err.p, 0, sizeof(int), st));
+    MC_CUDA_TRY(cudaMemsetAsync(s.nrecheck.p, 0, 2 * sizeof(unsigned long long), st));
+    TcArgs a;
+    a.n = n;
+    a.d = d;
+    a.k = k;
+    a.kb = kb;
+    a.nchunks = kp / tc::BN;
+    a.ntiles = uint32_t((n + tc::BM - 1) / tc::BM);
+    a.rownorm = rownorm;
+    a.cnp = s.cnorm_p.p;
+    a.kp = kp;
+    const double u = tf32 ? 1.0 / 1024.0 : 1.0 / 512.0;
+    a.eta = float(2 * u + u * u + double(d) * std::ldexp(1.0, -22));
+    const double g = double(d) * std::ldexp(1.0, -24);
+    a.gamma = float(g / (1.0 - g) * 2.0);
+    a.b1 = s.b1.p;
+    a.cnt = s.cnt.p;
+    a.cand = s.cand.p;
+    a.err = s.err.p;
+    const size_t smem = size_t(tc::STAGES) * tc::STAGE_BYTES + tc::CN_SMEM * sizeof(float) + sizeof(tc::Smem) + 1024;
+    const unsigned grid = unsigned(umin64(a.ntiles, uint64_t(sms)));
+    // pass 1 (row minima) and pass 2 (candidates under the fixed threshold)
+    if (tf32) {
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<true, TC_MIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<true, TC_CAND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+        k_tc_assign<true, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        k_tc_assign<true, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+    } else {
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<false, TC_MIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<false, TC_CAND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(smem)));
+        k_tc_assign<false, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        k_tc_assign<false, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    MC_TRY(s.over_rows.alloc(n, st));
+    k_tc_finalize<<<unsigned((n + 127) / 128), 128, 0, st>>>(X, n, d, C, k, asn, s.cnt.p, s.cand.p, costs,
+                                                             s.nrecheck.p, s.over_rows.p, s.nrecheck.p + 1),
+        note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    int err = 0;
+    unsigned long long nr[2] = {0, 0};
+    MC_CUDA_TRY(cudaMemcpyAsync(&err, s.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(nr, s.nrecheck.p, sizeof(nr), cudaMemcpyDeviceToHost, st));
+    MC_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err) return fail(MC_ETIMEOUT, "tensor-core assignment: bounded wait expired (code " + std::to_string(err) + ")");
+    if (nr[1]) {
+        // rows with more candidates than the epilogue keeps: exact FP32 scan over all centers
+        AssignArgs b;
+        b.msr = SQRL2;
+        b.n = nr[1];
+        b.d = d;
+        b.k = k;
+        b.kp = tiled_center_pad(k, false, SQRL2);
+        b.X = X;
+        b.rows = s.over_rows.p;
+        MC_TRY(s.CT0.alloc(uint64_t(b.kp) * d, st));
+        b.CT0 = s.CT0.p;
+        b.asn = asn;
+        b.costs = costs;
+        MC_TRY(launch_prep_centers(b, C, false, false, st));
+        MC_TRY(launch_assign_tiled(b, false, false, st));
+    }
+    if (recheck_count) *recheck_count = nr[0] + nr[1];
+    return MC_OK;
 }
 
 }  // namespace mc

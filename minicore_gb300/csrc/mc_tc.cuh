@@ -11,10 +11,14 @@ struct TcState {
     DBuf<float> Xt;              // [n][dp] tf32-ready copy (TF32 path, d padded)
     DBuf<__nv_bfloat16> Cb;      // [kp][dp]
     DBuf<float> Ct;              // [kp][dp]
-    DBuf<float> cnorm_p;         // [kp] padded center norms
-    DBuf<uint32_t> flagged;      // rows to re-check
-    DBuf<uint64_t> nflag;        // device counter
-    DBuf<float> best2;           // scratch
+    DBuf<float> cnorm_p;         // device scalar: max center norm
+    DBuf<float> b1;              // [n][2] per-row minima of the tensor-core values (pass 1)
+    DBuf<uint8_t> cnt;           // [n][2] candidates per column half (255: too many)
+    DBuf<uint32_t> cand;         // [n][2][4] candidate centers
+    DBuf<int> err;               // bounded-wait error code
+    DBuf<unsigned long long> nrecheck;   // [0] rows re-checked among candidates, [1] rows rescanned
+    DBuf<uint32_t> over_rows;    // rows rescanned over all centers
+    DBuf<float> CT0;             // transposed centers for that rescan
     const float *X_src = nullptr;
     uint64_t n = 0, d = 0, dp = 0;
     int prec = -1;
