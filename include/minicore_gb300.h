@@ -149,6 +149,23 @@ int mc_job_read(mc_job *job, float *centers, uint32_t *asn, double *costs);
 /* rows whose BF16/TF32 margin fell below the bound in the last pass (0 for FP32) */
 int mc_job_recheck_count(mc_job *job, uint64_t *count);
 
+/* Capacity of mc_assign_sqrl2_noalloc's fixed scratch array, in floats (4 MiB). */
+#define MC_NOALLOC_SCRATCH_FLOATS (1u << 20)
+
+/* Dense SQRL2 FP32 assignment that allocates no device memory (no counterpart in the
+ * reference; it exists for callers that cannot allocate on the call path, e.g. hosts that
+ * reserve their whole GPU memory budget up front or that only hand the library buffers
+ * they own).  Same results as mc_assign(..., MC_SQRL2, prior, MC_FP32, ...).
+ * X (n x d row-major float32), centers (k x d float32), asn (n) and costs (n) must be
+ * device pointers; the work is queued on cuda_stream (a cudaStream_t, may be NULL) and the
+ * call returns without waiting.  Its scratch (the centers transposed) lives in one fixed
+ * device array of MC_NOALLOC_SCRATCH_FLOATS floats per GPU: kp * d must fit, kp being k
+ * rounded up to a multiple of 64 (k < 128) or 128 (k >= 128), else MC_EINVAL.  The first
+ * call on a device looks up that array's address, so make it before any stream capture.
+ * All calls on a device share the array: calls that overlap on the GPU race. */
+int mc_assign_sqrl2_noalloc(const float *X, uint64_t n, uint64_t d, const float *centers, uint32_t k,
+                            uint32_t *asn, double *costs, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

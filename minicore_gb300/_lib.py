@@ -48,6 +48,7 @@ SIGNATURES = {
     "mc_job_run": (I, [P, D, U64, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(U64)]),
     "mc_job_read": (I, [P, P, P, P]),
     "mc_job_recheck_count": (I, [P, ctypes.POINTER(U64)]),
+    "mc_assign_sqrl2_noalloc": (I, [P, U64, U64, P, U32, P, P, P]),
 }
 
 _lib = None
