@@ -16,6 +16,7 @@ A step is one Lloyd iteration (centroid update + hard assignment) over all rows.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -42,6 +43,10 @@ def parse():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd"],
+                    help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
+                         "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass")
+    ap.add_argument("--csr-rows", type=int, default=1_000_000)
     return ap.parse_args()
 
 
@@ -61,6 +66,109 @@ def make_data(n, seed=0):
     X = torch.randn(n, D, generator=g, device="cuda")
     X.add_(mu[lab])
     return X.contiguous()
+
+
+def make_csr_counts(n, d=20_000, nnz_row=1500, seed=0, chunk=4096):
+    """CSR count matrix: per row nnz_row distinct columns drawn by Zipf(1.1) rank weights
+    without replacement (Gumbel top-k on the log weights, columns ranked by a seeded
+    permutation); values negative binomial (mean 3, dispersion 0.5: r = 2) with zeros
+    redrawn.  Generated on the GPU in row chunks; returns (values, indices, indptr)."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    rank = torch.randperm(d, generator=g, device="cuda").float() + 1.0
+    logw = -1.1 * torch.log(rank)
+    vals = torch.empty(n * nnz_row, dtype=torch.float32, device="cuda")
+    idx = torch.empty(n * nnz_row, dtype=torch.int32, device="cuda")
+    for r0 in range(0, n, chunk):
+        r1 = min(n, r0 + chunk)
+        m = r1 - r0
+        u = torch.rand((m, d), generator=g, device="cuda").clamp_(1e-12, 1.0)
+        key = logw[None, :] - torch.log(-torch.log(u))
+        top = torch.topk(key, nnz_row, dim=1, sorted=False).indices
+        top, _ = torch.sort(top, dim=1)
+        # NB(mean 3, r=2): Poisson(Gamma(shape 2, scale 1.5)), zeros redrawn
+        lam = torch._standard_gamma(torch.full((m, nnz_row), 2.0, device="cuda"), generator=g) * 1.5
+        x = torch.poisson(lam, generator=g)
+        for _ in range(64):
+            z = x == 0
+            if not bool(z.any()):
+                break
+            lam2 = torch._standard_gamma(torch.full((int(z.sum()),), 2.0, device="cuda"), generator=g) * 1.5
+            x[z] = torch.poisson(lam2, generator=g)
+        x.clamp_(min=1.0)
+        vals[r0 * nnz_row:r1 * nnz_row] = x.reshape(-1)
+        idx[r0 * nnz_row:r1 * nnz_row] = top.reshape(-1).int()
+    indptr = torch.arange(0, n + 1, device="cuda", dtype=torch.int64) * nnz_row
+    return vals, idx, indptr
+
+
+def csr_bench(args):
+    """Sparse count workload: D^2 seeding (k=50) then the timed assignment pass (MKL or JSD,
+    prior 1) with rows resident in HBM."""
+    import torch
+    import minicore_gb300 as mc
+    from minicore_gb300 import _lib
+    torch.cuda.set_device(0)
+    ctx = mc.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    n, d, k = args.csr_rows, 20_000, 50
+    msr = 5 if args.workload == "csr_mkl" else 4
+    vals, idx, indptr = make_csr_counts(n, d, seed=0)
+    torch.cuda.synchronize()
+    A = mc.CSparseMatrix(data=vals, indices=idx, indptr=indptr, shape=(n, d))
+    M = mc._MatrixArg(A)
+    lib = _lib.load()
+    u = torch.from_numpy(mc.uniforms(99, k)).cuda()
+    ids = torch.empty(k, dtype=torch.int32, device="cuda")
+    asn = torch.empty(n, dtype=torch.int32, device="cuda")
+    costs = torch.empty(n, dtype=torch.float64, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    _lib.check(lib.mc_kmeanspp(ctx.handle, M.ref, k, msr, 1.0, None, mc._p(u), mc._p(ids), mc._p(asn),
+                               mc._p(costs)))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    kmpp_ms = e0.elapsed_time(e1)
+    C = torch.zeros((k, d), dtype=torch.float32, device="cuda")
+    ipc = indptr.cpu()
+    for c, r in enumerate(ids.cpu().tolist()):
+        b, e = int(ipc[r]), int(ipc[r + 1])
+        C[c, idx[b:e].long()] = vals[b:e]
+    job = mc.Job(A, C, msr=msr, prior=1.0, ctx=ctx)
+    for _ in range(args.warmup):
+        job.assign()
+    torch.cuda.synchronize()
+    lib.mc_profile_reset()
+    lib.mc_profile_enable(1)
+    e0.record(stream)
+    for _ in range(args.steps):
+        job.assign()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    lib.mc_profile_enable(0)
+    buf = ctypes.create_string_buffer(1 << 16)
+    _lib.check(lib.mc_profile_report(buf, len(buf)))
+    phases = json.loads(buf.value.decode())
+    ms = e0.elapsed_time(e1) / args.steps
+    nnz = n * 1500
+    algo_bytes = nnz * 8 + (n + 1) * 8 + n * 8 + n * 12 + k * d * 4
+    pk, pk_kind = peaks()
+    kern = phases.get("assign_csr_sparse") or phases.get("assign_csr_tiled") or {}
+    kms = kern.get("ms", float("nan")) / max(kern.get("count", 1), 1)
+    out = {"metric": f"CSR {'MKL' if msr == 5 else 'JSD'} assignment passes/s 1Mx20000 k=50",
+           "value": 1000.0 / ms, "unit": "passes/s", "ms_per_pass": ms, "steps": args.steps,
+           "warmup": args.warmup, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"CSR {n}x{d}, 1500 nnz/row Zipf(1.1) columns, NB(3,0.5) counts, "
+                                  f"msr={msr}, prior=1, k={k}, kmeans++ centers"},
+           "kmeanspp_ms": kmpp_ms,
+           "roofline": {"bound": "hbm" if msr == 5 else "compute", "achieved": algo_bytes / (kms * 1e-3) / 1e9,
+                        "peak": pk.get("hbm_gbs", 6767.7), "unit": "GB/s",
+                        "frac": algo_bytes / (kms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6767.7),
+                        "algorithmic_bytes": algo_bytes, "kernel_ms": kms, "peak_source": pk_kind},
+           "phases_ms": phases}
+    print(json.dumps(out))
 
 
 class Clocks:
@@ -155,6 +263,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload != "dense":
+        return csr_bench(args)
     import torch
     import torch.distributed as dist
     rank = int(os.environ.get("RANK", "0"))
@@ -200,6 +310,8 @@ def main():
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     lib = _lib.load()
+    lib.mc_profile_reset()
+    lib.mc_profile_enable(1)  # CUDA events around the library's phases, on this stream
     l0 = lib.mc_kernel_launches()
     ev0.record(stream)
     for _ in range(args.steps):
@@ -208,6 +320,10 @@ def main():
     launches = int(lib.mc_kernel_launches() - l0)
     torch.cuda.synchronize()
     clk = clocks.stop()
+    lib.mc_profile_enable(0)
+    buf = ctypes.create_string_buffer(1 << 16)
+    _lib.check(lib.mc_profile_report(buf, len(buf)))
+    phases = json.loads(buf.value.decode())
     ms = ev0.elapsed_time(ev1)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -217,25 +333,27 @@ def main():
     value = world * 1000.0 / ms_per_step  # independent replicas: iterations completed per second
     recheck = job.recheck_count()
 
-    # dominant kernel: the assignment pass, timed alone
-    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 5
-    job.assign()
-    torch.cuda.synchronize()
-    a0.record(stream)
-    for _ in range(reps):
-        job.assign()
-    a1.record(stream)
-    torch.cuda.synchronize()
-    assign_ms = a0.elapsed_time(a1) / reps
+    # dominant kernel: the tensor-core assignment kernel (two passes per assignment) or the
+    # FP32 tiled kernel, from the events recorded over the timed region
     pk, pk_kind = peaks()
     flops = 2.0 * n * K * D
-    achieved = flops / (assign_ms * 1e-3) / 1e12
-    peak = pk.get("bf16_tflops", 1935.7)
-    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None, "peak_source": pk_kind,
-                "kernel": f"assignment pass ({args.precision})", "kernel_ms": assign_ms,
-                "algorithmic": "2*n*k*d FLOP per pass"}
+    if args.precision == "fp32":
+        kname, kinfo = "assign_dense_fp32 (k_assign_tiled)", phases.get("assign_dense_fp32", {})
+        launches_k = kinfo.get("count", 0)
+        avg_ms = kinfo.get("ms", float("nan")) / max(launches_k, 1)
+        peak, unit = None, "TFLOP/s"
+    else:
+        p1, p2 = phases.get("tc_pass1_min", {}), phases.get("tc_pass2_candidates", {})
+        launches_k = p1.get("count", 0) + p2.get("count", 0)
+        avg_ms = (p1.get("ms", 0.0) + p2.get("ms", 0.0)) / max(launches_k, 1)
+        kname = f"k_tc_assign ({args.precision}; pass 1 minima + pass 2 candidates)"
+        peak, unit = pk.get("bf16_tflops", 1935.7), "TFLOP/s"
+    achieved = flops / (avg_ms * 1e-3) / 1e12
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": unit,
+                "frac": (achieved / peak) if peak else None, "traffic": None,
+                "peak_source": f"{pk_kind} bf16_tflops (burst)", "kernel": kname,
+                "kernel_ms_per_launch": avg_ms, "launches": launches_k,
+                "algorithmic": f"2*n*k*d = {flops:.4g} FLOP per launch (n={n}, k={K}, d={D})"}
 
     # FP32 plain kernel for the same iteration (the comparison named by the metric)
     fp32 = None
@@ -295,7 +413,8 @@ def main():
                 "fp32_gpu_iters_per_s": fp32,
                 "speedup_vs_fp32_gpu": (value / world / fp32) if fp32 else None,
                 "recheck_rows_last_pass": recheck,
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "roofline": roofline, "phases_ms_timed_region": phases,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk}
         print(json.dumps(line))
     if world > 1:

@@ -91,6 +91,12 @@ const char *mc_version(void);
 const char *mc_last_error(void);
 /* Number of CUDA kernels this library has launched in this process (diagnostics). */
 uint64_t mc_kernel_launches(void);
+/* Phase profiler (diagnostics, off by default): CUDA events around the library's phases
+ * (tensor-core passes, exact finalize, FP32/CSR assignment, centroid update, objective).
+ * mc_profile_report writes {"phase": {"count": c, "ms": total}, ...} as JSON. */
+int mc_profile_enable(int on);
+int mc_profile_reset(void);
+int mc_profile_report(char *json, uint64_t capacity);
 
 int mc_context_create(int device, mc_context **out);
 int mc_context_destroy(mc_context *ctx);

@@ -27,6 +27,9 @@ SIGNATURES = {
     "mc_version": (ctypes.c_char_p, []),
     "mc_last_error": (ctypes.c_char_p, []),
     "mc_kernel_launches": (U64, []),
+    "mc_profile_enable": (I, [I]),
+    "mc_profile_reset": (I, []),
+    "mc_profile_report": (I, [ctypes.c_char_p, U64]),
     "mc_context_create": (I, [I, ctypes.POINTER(P)]),
     "mc_context_destroy": (I, [P]),
     "mc_context_set_stream": (I, [P, P]),

@@ -4,6 +4,8 @@
 // (include/minicore/coreset/coreset.h:228-701).
 #include <algorithm>
 #include <atomic>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -22,6 +24,20 @@ static thread_local std::string g_last_error;
 static std::atomic<uint64_t> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+static std::atomic<bool> g_prof_on{false};
+static std::mutex g_prof_mu;
+struct ProfRec {
+    std::string name;
+    cudaEvent_t a, b;
+};
+static std::vector<ProfRec> g_prof;
+
+bool profiling_enabled() { return g_prof_on.load(std::memory_order_relaxed); }
+void profile_record(const char *name, cudaEvent_t a, cudaEvent_t b) {
+    std::lock_guard<std::mutex> lock(g_prof_mu);
+    g_prof.push_back({name, a, b});
+}
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int status, const std::string &msg) {
@@ -228,11 +244,16 @@ int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exac
         a.consts = j->consts.p;
     }
     MC_TRY(launch_prep_centers(a, C, j->pair, sparse, j->st));
-    if (sparse) return launch_assign_sparse(a, j->st, j->ctx->sms);
+    if (sparse) {
+        Phase ph("assign_csr_sparse", j->st);
+        return launch_assign_sparse(a, j->st, j->ctx->sms);
+    }
+    Phase ph(csr ? "assign_csr_tiled" : "assign_dense_fp32", j->st);
     return launch_assign_tiled(a, csr, j->pair, j->st);
 }
 
 int job_cost(mc_job *j, float *out) {
+    Phase ph("objective", j->st);
     DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, j->M.n};
     MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, j->st));
     double s = 0.0;
@@ -240,11 +261,6 @@ int job_cost(mc_job *j, float *out) {
     MC_TRY(sync(j->st));
     *out = float(s);
     return MC_OK;
-}
-
-__global__ void k_count_keys(const uint32_t *keys, uint64_t n, uint32_t k, uint64_t *cnt) {
-    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x))
-        atomicAdd((unsigned long long *)&cnt[keys[i]], 1ull);
 }
 
 __global__ void k_copy_row_dense(const float *X, uint64_t d, const uint64_t *r, float *dst) {
@@ -269,11 +285,14 @@ int job_set_centroids(mc_job *j, int *restarted) {
     cudaStream_t st = j->st;
     *restarted = 0;
     MC_TRY(j->idxbuf.alloc(uint64_t(k) + 2, st));
-    MC_CUDA_TRY(cudaMemsetAsync(j->idxbuf.p, 0, (uint64_t(k) + 2) * sizeof(uint64_t), st));
-    k_count_keys<<<unsigned(umin64((n + 255) / 256, uint64_t(j->ctx->sms) * 16)), 256, 0, st>>>(j->asn.p, n, k,
-                                                                                                  j->idxbuf.p), note_launch();
+    // the counting sort of the rows by cluster gives the bucket sizes; it is reused for the
+    // centroid sums when no cluster is empty
+    {
+        Phase ph("centroid_update", st);
+        MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+    }
     std::vector<uint64_t> cnt(k);
-    MC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), j->idxbuf.p, k * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), j->sort.bucket_count.p, k * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     MC_TRY(sync(st));
     std::vector<uint32_t> empty;
     for (uint32_t c = 0; c < k; ++c)
@@ -329,6 +348,7 @@ int job_set_centroids(mc_job *j, int *restarted) {
         }
         if (extra) keys2 = j->asn2.p;
     }
+    Phase ph("centroid_update", st);
     CentroidArgs ca;
     ca.csr = j->M.kind == MC_CSR_F32;
     ca.n = n;
@@ -345,7 +365,7 @@ int job_set_centroids(mc_job *j, int *restarted) {
     ca.centers = j->Cw.p;
     ca.nan_flag = j->flag.p;
     MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), st));
-    MC_TRY(launch_centroids(ca, j->sort, st));
+    MC_TRY(launch_centroids(ca, j->sort, st, /*presorted=*/!*restarted));
     int nanf = 0;
     MC_CUDA_TRY(cudaMemcpyAsync(&nanf, j->flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     MC_TRY(sync(st));
@@ -359,6 +379,47 @@ extern "C" {
 
 const char *mc_version(void) { return "minicore_gb300 0.1 (sm_103a)"; }
 uint64_t mc_kernel_launches(void) { return g_launches.load(); }
+
+int mc_profile_enable(int on) {
+    g_prof_on.store(on != 0);
+    return MC_OK;
+}
+
+int mc_profile_reset(void) {
+    std::lock_guard<std::mutex> lock(g_prof_mu);
+    for (auto &r : g_prof) {
+        cudaEventSynchronize(r.b);
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    g_prof.clear();
+    return MC_OK;
+}
+
+int mc_profile_report(char *json, uint64_t cap) {
+    std::lock_guard<std::mutex> lock(g_prof_mu);
+    std::map<std::string, std::pair<uint64_t, double>> agg;
+    for (auto &r : g_prof) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            auto &e = agg[r.name];
+            e.first += 1;
+            e.second += ms;
+        }
+    }
+    std::string out = "{";
+    bool first = true;
+    for (auto &kv : agg) {
+        out += (first ? "\"" : ", \"") + kv.first + "\": {\"count\": " + std::to_string(kv.second.first) +
+               ", \"ms\": " + std::to_string(kv.second.second) + "}";
+        first = false;
+    }
+    out += "}";
+    if (!json || cap == 0) return fail(MC_EINVAL, "no output buffer");
+    if (out.size() + 1 > cap) return fail(MC_EINVAL, "profile report needs " + std::to_string(out.size() + 1) + " bytes");
+    std::memcpy(json, out.c_str(), out.size() + 1);
+    return MC_OK;
+}
 const char *mc_last_error(void) { return g_last_error.c_str(); }
 
 int mc_uniforms(uint64_t seed, uint64_t offset, uint64_t m, double *out) {

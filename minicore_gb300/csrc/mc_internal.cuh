@@ -169,6 +169,28 @@ bool is_device_ptr(const void *p);
 // process-wide count of kernel launches issued by this library
 void note_launch();
 
+// Phase profiler (off by default): when enabled, Phase records a CUDA event pair on the
+// stream around a scope; mc_profile_report() sums the elapsed times per phase name.
+bool profiling_enabled();
+void profile_record(const char *name, cudaEvent_t a, cudaEvent_t b);
+struct Phase {
+    const char *name;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Phase(const char *n, cudaStream_t s) : name(n), st(s) {
+        if (profiling_enabled() && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess)
+            cudaEventRecord(a, st);
+        else
+            a = b = nullptr;
+    }
+    ~Phase() {
+        if (a && b) {
+            cudaEventRecord(b, st);
+            profile_record(name, a, b);
+        }
+    }
+};
+
 __host__ __device__ inline uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
 
 // ------------------------------------------------------------------------------------

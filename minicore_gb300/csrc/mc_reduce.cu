@@ -215,17 +215,31 @@ int launch_row_sums_csr(const float *vals, const uint64_t *indptr, uint64_t n, d
 // Tiles of kSortTile rows; per-tile counts -> per (key, tile) offsets -> one warp per tile
 // scatters its rows in order (match_any ranks), so each bucket lists rows ascending.
 // ------------------------------------------------------------------------------------
+// per-tile counts; a shared-memory histogram when k is small enough
+constexpr uint32_t kSmemKeys = 8192;
+
 __global__ void k_sort_count(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ keys2, uint64_t n,
                              uint32_t k, uint32_t *tile_counts /* [ntiles][k] */) {
+    __shared__ uint32_t hist[kSmemKeys];
     const uint64_t tile = blockIdx.x;
     const uint64_t b = tile * kSortTile, e = umin64(n, b + kSortTile);
     uint32_t *tc = tile_counts + tile * uint64_t(k);
+    const bool sm = k <= kSmemKeys;
+    if (sm) {
+        for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) hist[j] = 0;
+        __syncthreads();
+    }
+    uint32_t *h = sm ? hist : tc;
     for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        atomicAdd(&tc[keys[i]], 1u);
+        atomicAdd(&h[keys[i]], 1u);
         if (keys2) {
             const uint32_t k2 = keys2[i];
-            if (k2 != 0xffffffffu) atomicAdd(&tc[k2], 1u);
+            if (k2 != 0xffffffffu) atomicAdd(&h[k2], 1u);
         }
+    }
+    if (sm) {
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) tc[j] = hist[j];
     }
 }
 
@@ -272,13 +286,22 @@ __global__ void k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t
 
 __global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, uint32_t k, uint32_t *tile_offsets,
                                const uint64_t *__restrict__ bucket_start, uint32_t *perm) {
-    // one warp per tile; rows in order, 32 at a time; ranks from match_any
-    const uint64_t tile = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    // one warp per tile; rows in order, 32 at a time; ranks from match_any.  Cursors live in
+    // shared memory when k is small enough (one warp per block), else in the tile's row of
+    // tile_offsets.
+    __shared__ uint32_t scur[kSmemKeys];
+    const uint64_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31;
     const uint64_t b = tile * kSortTile;
     if (b >= n) return;
     const uint64_t e = umin64(n, b + kSortTile);
-    uint32_t *cur = tile_offsets + tile * uint64_t(k);
+    uint32_t *gcur = tile_offsets + tile * uint64_t(k);
+    const bool sm = k <= kSmemKeys;
+    if (sm) {
+        for (uint32_t j = lane; j < k; j += 32) scur[j] = gcur[j];
+        __syncwarp();
+    }
+    uint32_t *cur = sm ? scur : gcur;
     const unsigned lt = (1u << lane) - 1u;
     for (uint64_t base = b; base < e; base += 32) {
         const uint64_t i = base + lane;
@@ -333,8 +356,8 @@ int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, 
     k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.bucket_count.p, w.bucket_start.p, k), note_launch();
     if (ntiles) {
         if (!keys2)
-            k_sort_scatter<<<unsigned((ntiles + 3) / 4), 128, 0, st>>>(keys, n, k, w.tile_counts.p,
-                                                                       w.bucket_start.p, w.perm.p), note_launch();
+            k_sort_scatter<<<unsigned(ntiles), 32, 0, st>>>(keys, n, k, w.tile_counts.p, w.bucket_start.p,
+                                                            w.perm.p), note_launch();
         else
             k_sort_scatter2<<<unsigned((ntiles + 63) / 64), 64, 0, st>>>(keys, keys2, n, k, w.tile_counts.p,
                                                                          w.bucket_start.p, w.perm.p), note_launch();
@@ -515,11 +538,11 @@ __global__ void k_centroid_singletons_csr(const float *__restrict__ vals, const 
     }
 }
 
-int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st) {
+int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool presorted) {
     const uint64_t n = a.n, d = a.d;
     const uint32_t k = a.k;
     const uint64_t ch = a.csr ? 4096 : 256;
-    MC_TRY(launch_sort_by_key(a.keys, a.keys2, n, k, w, st));
+    if (!presorted) MC_TRY(launch_sort_by_key(a.keys, a.keys2, n, k, w, st));
     MC_TRY(w.chunk_count.alloc(k, st));
     MC_TRY(w.chunk_start.alloc(uint64_t(k) + 1, st));
     k_chunk_counts<<<(k + 255) / 256, 256, 0, st>>>(w.bucket_count.p, k, ch, w.chunk_count.p), note_launch();

@@ -35,7 +35,8 @@ struct CentroidArgs {
 
 int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, uint32_t k, SortWork &w,
                        cudaStream_t st);
-int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st);
+// presorted: w already holds the counting sort of a.keys (no second membership)
+int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool presorted = false);
 int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st);
 int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, float *cnorm, cudaStream_t st);
 

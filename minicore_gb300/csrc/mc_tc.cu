@@ -444,26 +444,41 @@ __global__ void k_center_prep_tc(const float *__restrict__ C, uint32_t k, uint32
 // for an exact scan over all centers.
 constexpr int NSLOT = 2 * tc::NCAND;
 
-__global__ void __launch_bounds__(128) k_tc_finalize(const float *__restrict__ X, uint64_t n, uint64_t d,
+__global__ void __launch_bounds__(256) k_tc_finalize(const float *__restrict__ X, uint64_t n, uint64_t d,
                                                       const float *__restrict__ C, uint32_t k, uint32_t *asn,
                                                       const uint8_t *__restrict__ cnt,
                                                       const uint32_t *__restrict__ cand, double *costs,
                                                       unsigned long long *nrecheck, uint32_t *over_rows,
                                                       unsigned long long *nover) {
-    __shared__ float xs[128][33];
+    constexpr int R = 256;
+    __shared__ float xs[R][33];
     const int t = threadIdx.x;
-    const uint64_t row0 = uint64_t(blockIdx.x) * 128;
+    const uint64_t row0 = uint64_t(blockIdx.x) * R;
     const uint64_t row = row0 + t;
     // cj[q] == 0xffffffff marks an unused slot
     uint32_t cj[NSLOT];
 #pragma unroll
     for (int q = 0; q < NSLOT; ++q) cj[q] = 0xffffffffu;
+    bool over = false, multi = false;
+    int c0 = 0, c1 = 0;
     if (row < n) {
-        const int c0 = cnt[2 * row], c1 = cnt[2 * row + 1];
-        if (c0 == 255 || c1 == 255 || c0 + c1 == 0) {
-            over_rows[atomicAdd(nover, 1ull)] = uint32_t(row);
-        } else {
-            if (c0 + c1 > 1) atomicAdd(nrecheck, 1ull);
+        c0 = cnt[2 * row];
+        c1 = cnt[2 * row + 1];
+        over = c0 == 255 || c1 == 255 || c0 + c1 == 0;
+        multi = !over && c0 + c1 > 1;
+    }
+    // warp-aggregated counters: one atomic per warp
+    const int lane = t & 31;
+    const unsigned ob = __ballot_sync(0xffffffffu, over), mb = __ballot_sync(0xffffffffu, multi);
+    unsigned long long obase = 0;
+    if (lane == 0) {
+        if (ob) obase = atomicAdd(nover, (unsigned long long)__popc(ob));
+        if (mb) atomicAdd(nrecheck, (unsigned long long)__popc(mb));
+    }
+    obase = __shfl_sync(0xffffffffu, obase, 0);
+    if (over) over_rows[obase + __popc(ob & ((1u << lane) - 1u))] = uint32_t(row);
+    if (row < n && !over) {
+        {
 #pragma unroll
             for (int q = 0; q < NSLOT; ++q) {
                 const int h = q / tc::NCAND, s = q % tc::NCAND;
@@ -477,14 +492,28 @@ __global__ void __launch_bounds__(128) k_tc_finalize(const float *__restrict__ X
     float acc[NSLOT];
 #pragma unroll
     for (int q = 0; q < NSLOT; ++q) acc[q] = 0.f;
-    const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0);
+    const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0) &&
+                      ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
     for (uint64_t k0 = 0; k0 < d; k0 += 32) {
         const int kmax = int(umin64(32, d - k0));
         __syncthreads();
-        for (int e = t; e < 128 * 32; e += 128) {
-            const int r = e >> 5, kk = e & 31;
-            const uint64_t rr = row0 + r;
-            xs[r][kk] = (rr < n && kk < kmax) ? X[rr * d + k0 + kk] : 0.f;
+        if (vec4 && kmax == 32) {
+            for (int e = t; e < R * 8; e += R) {
+                const int r = e >> 3, q4 = e & 7;
+                const uint64_t rr = row0 + r;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (rr < n) v = __ldg(reinterpret_cast<const float4 *>(X + rr * d + k0) + q4);
+                xs[r][4 * q4 + 0] = v.x;
+                xs[r][4 * q4 + 1] = v.y;
+                xs[r][4 * q4 + 2] = v.z;
+                xs[r][4 * q4 + 3] = v.w;
+            }
+        } else {
+            for (int e = t; e < R * 32; e += R) {
+                const int r = e >> 5, kk = e & 31;
+                const uint64_t rr = row0 + r;
+                xs[r][kk] = (rr < n && kk < kmax) ? X[rr * d + k0 + kk] : 0.f;
+            }
         }
         __syncthreads();
 #pragma unroll
@@ -642,21 +671,36 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
                                          int(smem)));
         MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<true, TC_CAND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(smem)));
-        k_tc_assign<true, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
-        k_tc_assign<true, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        {
+            Phase ph("tc_pass1_min", st);
+            k_tc_assign<true, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        }
+        {
+            Phase ph("tc_pass2_candidates", st);
+            k_tc_assign<true, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        }
     } else {
         MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<false, TC_MIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(smem)));
         MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<false, TC_CAND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(smem)));
-        k_tc_assign<false, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
-        k_tc_assign<false, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        {
+            Phase ph("tc_pass1_min", st);
+            k_tc_assign<false, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        }
+        {
+            Phase ph("tc_pass2_candidates", st);
+            k_tc_assign<false, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        }
     }
     MC_CUDA_TRY(cudaGetLastError());
     MC_TRY(s.over_rows.alloc(n, st));
-    k_tc_finalize<<<unsigned((n + 127) / 128), 128, 0, st>>>(X, n, d, C, k, asn, s.cnt.p, s.cand.p, costs,
-                                                             s.nrecheck.p, s.over_rows.p, s.nrecheck.p + 1),
-        note_launch();
+    {
+        Phase phf("tc_finalize_exact", st);
+        k_tc_finalize<<<unsigned((n + 255) / 256), 256, 0, st>>>(X, n, d, C, k, asn, s.cnt.p, s.cand.p, costs,
+                                                                 s.nrecheck.p, s.over_rows.p, s.nrecheck.p + 1),
+            note_launch();
+    }
     MC_CUDA_TRY(cudaGetLastError());
     int err = 0;
     unsigned long long nr[2] = {0, 0};
@@ -678,6 +722,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
         b.CT0 = s.CT0.p;
         b.asn = asn;
         b.costs = costs;
+        Phase ph("tc_rescan_fp32", st);
         MC_TRY(launch_prep_centers(b, C, false, false, st));
         MC_TRY(launch_assign_tiled(b, false, false, st));
     }
