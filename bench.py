@@ -313,10 +313,12 @@ def main():
     lib.mc_profile_reset()
     lib.mc_profile_enable(1)  # CUDA events around the library's phases, on this stream
     l0 = lib.mc_kernel_launches()
+    torch.cuda.nvtx.range_push("lloyd_timed")
     ev0.record(stream)
     for _ in range(args.steps):
         job.lloyd_step()
     ev1.record(stream)
+    torch.cuda.nvtx.range_pop()
     launches = int(lib.mc_kernel_launches() - l0)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -349,8 +351,16 @@ def main():
         kname = f"k_tc_assign ({args.precision}; pass 1 minima + pass 2 candidates)"
         peak, unit = pk.get("bf16_tflops", 1935.7), "TFLOP/s"
     achieved = flops / (avg_ms * 1e-3) / 1e12
+    traffic = None  # DRAM bytes per launch from the committed ncu summary (scaled to 4M rows)
+    if args.precision == "bf16" and n == N:
+        try:
+            for line in open(os.path.join(ROOT, "profiles", "k_tc_assign_bf16_4Mx128_k1024.md")):
+                if line.startswith("traffic_bytes_per_launch_scaled_to_4M:"):
+                    traffic = float(line.split(":")[1].split()[0])
+        except OSError:
+            traffic = None
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": unit,
-                "frac": (achieved / peak) if peak else None, "traffic": None,
+                "frac": (achieved / peak) if peak else None, "traffic": traffic,
                 "peak_source": f"{pk_kind} bf16_tflops (burst)", "kernel": kname,
                 "kernel_ms_per_launch": avg_ms, "launches": launches_k,
                 "algorithmic": f"2*n*k*d = {flops:.4g} FLOP per launch (n={n}, k={K}, d={D})"}
