@@ -43,9 +43,16 @@ def parse():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd"],
+    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving"],
                     help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
-                         "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass")
+                         "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass; serving: "
+                         "the Poisson job stream through the continuous-batching server")
+    ap.add_argument("--serving-jobs", type=int, default=4000,
+                    help="jobs in the --workload serving stream (the full stream is 20000)")
+    ap.add_argument("--serving-rate", type=float, default=200.0)
+    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the short serving run (p50/p99 job latency) in the default line")
     ap.add_argument("--csr-rows", type=int, default=1_000_000)
     return ap.parse_args()
 
@@ -171,6 +178,186 @@ def csr_bench(args):
     print(json.dumps(out))
 
 
+SERVE_DS = (32, 64, 128, 512)
+SERVE_POOL_ROWS = 200_000
+
+
+def _nb_counts(m, g):
+    """m negative-binomial counts (mean 3, dispersion 0.5: Poisson(Gamma(2, 1.5))), zeros
+    redrawn (a few rounds, then set to 1)."""
+    import torch
+    lam = torch._standard_gamma(torch.full((m,), 2.0, device="cuda"), generator=g) * 1.5
+    x = torch.poisson(lam, generator=g)
+    for _ in range(32):
+        z = x == 0
+        nz = int(z.sum())
+        if nz == 0:
+            break
+        lam2 = torch._standard_gamma(torch.full((nz,), 2.0, device="cuda"), generator=g) * 1.5
+        x[z] = torch.poisson(lam2, generator=g)
+    return x.clamp_(min=1.0).float()
+
+
+def make_serving_pool(seed=0):
+    """Device-resident row pools the serving jobs slice: per d in {32, 64, 128, 512}, a dense
+    200-component Gaussian mixture (means ~N(0, 4I), sigma 1) and a CSR count matrix at 1%
+    density (Bernoulli(0.01) columns, every row at least one entry, NB counts), 200k rows."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    dense, csr = {}, {}
+    for d in SERVE_DS:
+        mu = torch.randn(200, d, generator=g, device="cuda") * 2.0
+        lab = torch.randint(0, 200, (SERVE_POOL_ROWS,), generator=g, device="cuda")
+        dense[d] = torch.randn(SERVE_POOL_ROWS, d, generator=g, device="cuda").add_(mu[lab]).contiguous()
+        mask = torch.rand(SERVE_POOL_ROWS, d, generator=g, device="cuda") < 0.01
+        force = torch.randint(0, d, (SERVE_POOL_ROWS,), generator=g, device="cuda")
+        empty = (~mask.any(1)).nonzero().squeeze(1)
+        mask[empty, force[empty]] = True
+        rows, cols = mask.nonzero(as_tuple=True)  # row-major: columns ascending in each row
+        indptr = torch.zeros(SERVE_POOL_ROWS + 1, dtype=torch.int64, device="cuda")
+        indptr[1:] = torch.cumsum(torch.bincount(rows, minlength=SERVE_POOL_ROWS), 0)
+        csr[d] = (_nb_counts(rows.numel(), g).contiguous(), cols.int().contiguous(), indptr)
+        del mask
+    return dense, csr
+
+
+def make_serving_jobs(pool, njobs, rate, seed):
+    """Seeded request stream: Poisson arrivals at `rate`/s; n log-uniform in [1e3, 2e5], d
+    from {32, 64, 128, 512}, k log-uniform in [5, 200]; half dense SQRL2 in BF16 tensor-core
+    form, half CSR MKL (prior 1); k-means++ seeding then Lloyd to eps 1e-4 or 10 updates."""
+    import minicore_gb300 as mc
+    dense, csr = pool
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs)) if rate > 0 else np.zeros(njobs)
+    jobs = []
+    for i in range(njobs):
+        n = int(np.exp(rng.uniform(np.log(1e3), np.log(2e5))))
+        d = int(rng.choice(SERVE_DS))
+        k = int(np.exp(rng.uniform(np.log(5), np.log(200))))
+        off = int(rng.integers(0, SERVE_POOL_ROWS - n + 1))
+        if rng.random() < 0.5:
+            X = dense[d][off:off + n]
+            spec = dict(matrix=X, k=k, msr=2, prior=0.0, precision="bf16")
+            kind = "dense_sqrl2_bf16"
+        else:
+            v, c, ip = csr[d]
+            b, e = int(ip[off]), int(ip[off + n])
+            X = mc.CSparseMatrix(data=v[b:e], indices=c[b:e], indptr=(ip[off:off + n + 1] - b).contiguous(),
+                                 shape=(n, d))
+            spec = dict(matrix=X, k=k, msr=5, prior=1.0, precision="fp32")
+            kind = "csr_mkl"
+        spec.update(eps=1e-4, maxiter=10, seed=1000 + i)
+        jobs.append({"spec": spec, "t": float(arrivals[i]), "n": n, "d": d, "k": k, "kind": kind})
+    return jobs
+
+
+def run_serving(srv, jobs, open_loop=True):
+    """Submit `jobs` at their arrival times (open_loop) or all at once; returns the results
+    and the wall time from the first submission to the last completion."""
+    import queue
+    q = queue.Queue()
+    results = [None] * len(jobs)
+
+    def collect():
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            i, t = item
+            results[i] = srv.wait(t)
+
+    th = threading.Thread(target=collect)
+    th.start()
+    t0 = time.perf_counter()
+    try:
+        for i, j in enumerate(jobs):
+            if open_loop:
+                delay = t0 + j["t"] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+            q.put((i, srv.submit(**j["spec"])))
+    finally:
+        q.put(None)
+        th.join()
+    return results, time.perf_counter() - t0
+
+
+def serving_bench(njobs, rate=200.0, slots=8, seed=0, saturation_jobs=None, serial=False):
+    """The serving form: a seeded Poisson stream of uneven jobs through mc_server (continuous
+    batching over `slots` concurrent slots, admission by free device memory)."""
+    import torch
+    import minicore_gb300 as mc
+    from minicore_gb300 import _lib
+    lib = _lib.load()
+    pool = make_serving_pool(seed)
+    torch.cuda.synchronize()
+    jobs = make_serving_jobs(pool, njobs, rate, seed + 1)
+    warm = make_serving_jobs(pool, 16, 0.0, seed + 2)
+    sat = make_serving_jobs(pool, saturation_jobs or max(njobs // 4, 64), 0.0, seed + 3)
+    torch.cuda.synchronize()
+    out = {}
+    with mc.Server(slots=slots) as srv:
+        run_serving(srv, warm, open_loop=False)
+        srv.reset_stats()
+        clocks = Clocks()
+        clocks.start()
+        l0 = lib.mc_kernel_launches()
+        res, wall = run_serving(srv, jobs, open_loop=True)
+        launches = int(lib.mc_kernel_launches() - l0)
+        clk = clocks.stop()
+        st = srv.stats()
+        srv.reset_stats()
+        res_s, wall_s = run_serving(srv, sat, open_loop=False)
+        st_s = srv.stats()
+    tot = np.array([r["total_ms"] for r in res])
+    run = np.array([r["run_ms"] for r in res])
+    qms = np.array([r["queue_ms"] for r in res])
+    rows_iters = sum(j["n"] * (r["numiter"] + 1) for j, r in zip(jobs, res))
+    d2h = sum(j["k"] * j["d"] * 4 + j["n"] * 12 for j in jobs)
+
+    def pct(a):
+        return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)), "mean": float(a.mean())}
+
+    by_kind = {}
+    for kind in ("dense_sqrl2_bf16", "csr_mkl"):
+        sel = np.array([j["kind"] == kind for j in jobs])
+        if sel.any():
+            by_kind[kind] = {"jobs": int(sel.sum()), "total_ms": pct(tot[sel])}
+    out = {"jobs": njobs, "rate_per_s": rate, "slots": slots, "wall_s": wall, "jobs_per_s": njobs / wall,
+           "latency_ms": {"total": pct(tot), "queue": pct(qms), "run": pct(run)},
+           "server_stats": st, "by_kind": by_kind, "row_iterations_per_s": rows_iters / wall,
+           "gpu_launches": launches, "clocks": clk, "d2h_bytes": int(d2h),
+           "saturated": {"jobs": len(sat), "jobs_per_s": len(sat) / wall_s, "wall_s": wall_s,
+                         "max_running": st_s.get("max_running"),
+                         "latency_ms": pct(np.array([r["total_ms"] for r in res_s]))}}
+    if serial:
+        with mc.Server(slots=1) as srv1:
+            run_serving(srv1, warm[:4], open_loop=False)
+            _, wall_1 = run_serving(srv1, sat, open_loop=False)
+        out["saturated_one_slot"] = {"jobs": len(sat), "jobs_per_s": len(sat) / wall_1, "wall_s": wall_1}
+    return out
+
+
+def serving_main(args):
+    import torch
+    torch.cuda.set_device(0)
+    s = serving_bench(args.serving_jobs, rate=args.serving_rate, slots=args.slots, serial=True)
+    line = {"metric": "serving jobs/s (Poisson 200/s mix of uneven clustering jobs); p50/p99 job latency",
+            "value": s["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": s["jobs"], "warmup": 16,
+            "ms_per_step": 1000.0 * s["wall_s"] / s["jobs"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (dense SQRL2) / f32 (CSR MKL)", "data": "synthetic",
+            "config": {"workload": f"{s['jobs']} jobs, Poisson {args.serving_rate}/s, n logU[1e3,2e5], "
+                                   f"d in {{32,64,128,512}}, k logU[5,200], half dense SQRL2 BF16, half CSR "
+                                   f"MKL 1% density; kmeans++ then Lloyd (eps 1e-4, 10 updates)",
+                       "slots": args.slots, "l2": "row pools 0.6 GB dense + CSR, jobs slice them"},
+            "latency_ms": s["latency_ms"], "serving": s, "gpu_launches": s["gpu_launches"],
+            "clocks": s["clocks"],
+            "e2e": {"value": s["jobs_per_s"], "unit": "jobs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(s["d2h_bytes"] / s["jobs"]),
+                    "call": "minicore_gb300.Server.submit/wait (rows resident, outputs to host)"}}
+    print(json.dumps(line))
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -263,6 +450,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "serving":
+        return serving_main(args)
     if args.workload != "dense":
         return csr_bench(args)
     import torch
@@ -411,6 +600,12 @@ def main():
         cpu = {"value": 1.0 / (per * n / S), "unit": "iters/s", "cores": threads, "kind": "port",
                "sample": f"{S} rows x k={K}: one assignment + centroid update of the oracle, scaled by {n}/{S}"}
 
+    serving = None
+    if not args.no_serving and rank == 0:
+        del job
+        torch.cuda.synchronize()
+        serving = serving_bench(1000, rate=200.0, slots=args.slots, saturation_jobs=250)
+
     if rank == 0:
         line = {"metric": "Lloyd iters/s 4M x128 k=1024", "value": value, "unit": "iters/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
@@ -425,7 +620,9 @@ def main():
                 "recheck_rows_last_pass": recheck,
                 "roofline": roofline, "phases_ms_timed_region": phases,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk}
+                "clocks": clk,
+                "job_latency_ms": (serving or {}).get("latency_ms"),
+                "serving": serving}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

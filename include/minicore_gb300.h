@@ -154,6 +154,56 @@ int mc_job_run(mc_job *job, double eps, uint64_t maxiter, double *initcost, doub
 int mc_job_read(mc_job *job, float *centers, uint32_t *asn, double *costs);
 /* rows whose BF16/TF32 margin fell below the bound in the last pass (0 for FP32) */
 int mc_job_recheck_count(mc_job *job, uint64_t *count);
+/* A job whose k centers are seeded on the device by D^2 sampling with uniforms U(seed, i),
+ * i < k (what minicore.cluster does between kmeanspp and hcluster,
+ * python/minicore/__init__.py:235-261, without the host round trip).  center_ids: optional
+ * k seed row ids.  Requires k <= nrows. */
+int mc_job_create_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior,
+                           const double *weights, int precision, uint64_t seed, uint32_t *center_ids,
+                           mc_job **out);
+
+/* Continuous-batching server (no reference counterpart).  S slots, each a host thread with
+ * its own stream; queued jobs are admitted first-fit against a device-memory budget
+ * (mem_budget_bytes, 0 = 90% of free memory) and the device's free memory; a job that would
+ * run alone is always admitted.  Every pointer in a job description (rows, centers,
+ * weights, outputs) must stay valid until the job's result has been returned. */
+typedef struct mc_job_desc {
+    mc_matrix X;               /* rows: host or device memory                                */
+    const float *centers;      /* k x ncols initial centers, or NULL for k-means++ seeding   */
+    uint32_t k;
+    int msr;
+    double prior;
+    const double *weights;     /* optional, n                                                */
+    int precision;             /* MC_FP32 / MC_TF32 / MC_BF16                                */
+    double eps;
+    uint64_t maxiter;
+    uint64_t seed;             /* seeding uniforms and empty-cluster restarts                */
+    float *centers_out;        /* optional outputs, host or device: k x ncols                */
+    uint32_t *asn_out;         /* n                                                          */
+    double *costs_out;         /* n                                                          */
+    uint32_t *center_ids_out;  /* k seed row ids (only when centers == NULL)                 */
+} mc_job_desc;
+
+typedef struct mc_job_result {
+    int status;                /* mc_status of the job                                       */
+    uint64_t numiter;
+    double initcost, finalcost;
+    double queue_ms, run_ms, total_ms;  /* submit->admit, admit->done, submit->done          */
+    char error[256];           /* mc_last_error() text when status != MC_OK                  */
+} mc_job_result;
+
+int mc_server_create(int device, uint32_t slots, uint64_t mem_budget_bytes, mc_server **out);
+int mc_server_submit(mc_server *s, const mc_job_desc *job, uint64_t *ticket);
+/* MC_EBUSY while the job runs; MC_OK with the result, after which the ticket is released. */
+int mc_server_poll(mc_server *s, uint64_t ticket, mc_job_result *result);
+/* Blocks up to timeout_ms (MC_ETIMEOUT after); releases the ticket on MC_OK. */
+int mc_server_wait(mc_server *s, uint64_t ticket, uint64_t timeout_ms, mc_job_result *result);
+/* JSON: completed, failed, queued, running, max_running, slots, budget_bytes and p50/p99 of
+ * the total, queue and run latencies (ms) of the jobs completed since the last reset. */
+int mc_server_stats(mc_server *s, char *json, uint64_t capacity);
+int mc_server_reset_stats(mc_server *s);
+/* Runs every queued job to completion, then stops the slots. */
+int mc_server_destroy(mc_server *s);
 
 /* Capacity of mc_assign_sqrl2_noalloc's fixed scratch array, in floats (4 MiB). */
 #define MC_NOALLOC_SCRATCH_FLOATS (1u << 20)

@@ -31,7 +31,7 @@ import threading
 import numpy as np
 
 from . import _lib
-from ._lib import McMatrix, check
+from ._lib import McError, McMatrix, check
 
 __all__ = ["kmeanspp", "hcluster", "cluster", "CoresetSampler", "CSparseMatrix", "Context", "Job",
            "uniforms", "library_path", "L1", "SQRL2", "JSD", "MKL", "HELLINGER",
@@ -440,6 +440,27 @@ class Job:
                                         _p(self._w), _PREC[precision], int(seed), ctypes.byref(h)))
         self._h = h
 
+    @classmethod
+    def from_kmeanspp(cls, matrix, k, *, msr=2, prior=0., weights=None, precision="fp32", seed=1,
+                      ctx: Context | None = None):
+        """A job whose k centers are seeded on the device by D^2 sampling with U(seed, i): the
+        centers minicore.cluster() passes from kmeanspp to hcluster
+        (python/minicore/__init__.py:235-261).  The seed row ids are in ``center_ids``."""
+        self = cls.__new__(cls)
+        self._ctx = ctx or default_context()
+        self._M = _MatrixArg(matrix)
+        self._C = None
+        self.k = int(k)
+        self._w = None if weights is None else (weights if hasattr(weights, "data_ptr")
+                                                else np.ascontiguousarray(weights, dtype=np.float64))
+        self.center_ids = np.empty(self.k, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        check(_lib.load().mc_job_create_kmeanspp(self._ctx.handle, self._M.ref, self.k, _msr(msr), float(prior),
+                                                 _p(self._w), _PREC[precision], int(seed), _p(self.center_ids),
+                                                 ctypes.byref(h)))
+        self._h = h
+        return self
+
     def assign(self):
         check(_lib.load().mc_job_assign(self._h))
 
@@ -471,6 +492,116 @@ class Job:
         if getattr(self, "_h", None) is not None:
             _lib.load().mc_job_destroy(self._h)
             self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------------------------
+# continuous-batching server
+# ------------------------------------------------------------------------------------
+class Server:
+    """Continuous-batching clustering server over the mc_server_* C ABI: ``slots`` jobs run
+    at once, each on its own stream; queued jobs are admitted first-fit against a device
+    memory budget.  ``submit`` returns a ticket; ``wait`` returns the job's outputs and its
+    queue / run / total latency."""
+
+    def __init__(self, slots: int = 4, mem_budget: int = 0, device: int = 0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.mc_server_create(int(device), int(slots), int(mem_budget), ctypes.byref(h)))
+        self._h = h
+        self._live = {}
+
+    def submit(self, matrix, k=None, centers=None, *, msr=2, prior=0., weights=None, precision="fp32",
+               eps=1e-10, maxiter=100, seed=1, outputs=True) -> int:
+        """Queue one job: explicit ``centers`` (as for hcluster), or ``k`` centers seeded by
+        k-means++ on the device with ``seed``.  ``outputs=False`` returns costs only."""
+        M = _MatrixArg(matrix)
+        if centers is not None:
+            C = centers if hasattr(centers, "data_ptr") else _centers_array(M, centers)
+            k = C.shape[0]
+        elif k is None:
+            raise ValueError("give k or centers")
+        else:
+            C = None
+        k = int(k)
+        if prior < 0:
+            prior = 1.0 / M.d
+        w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+        out = {}
+        if outputs:
+            out["centers"] = np.empty((k, M.d), dtype=np.float32)
+            out["asn"] = np.empty(M.n, dtype=np.uint32)
+            out["costs"] = np.empty(M.n, dtype=np.float64)
+            if C is None:
+                out["center_ids"] = np.empty(k, dtype=np.uint32)
+        desc = _lib.McJobDesc()
+        desc.X = M.m
+        desc.centers = _p(C)
+        desc.k = k
+        desc.msr = _msr(msr)
+        desc.prior = float(prior)
+        desc.weights = _p(w)
+        desc.precision = _PREC[precision]
+        desc.eps = float(eps)
+        desc.maxiter = int(maxiter)
+        desc.seed = _seed(seed)
+        desc.centers_out = _p(out.get("centers"))
+        desc.asn_out = _p(out.get("asn"))
+        desc.costs_out = _p(out.get("costs"))
+        desc.center_ids_out = _p(out.get("center_ids"))
+        t = ctypes.c_uint64()
+        check(self._lib.mc_server_submit(self._h, ctypes.byref(desc), ctypes.byref(t)))
+        self._live[t.value] = (M, C, w, out)
+        return t.value
+
+    def _finish(self, ticket, r) -> dict:
+        _, _, _, out = self._live.pop(ticket)
+        if r.status != _lib.MC_OK:
+            raise McError(r.status, r.error.decode(errors="replace"))
+        res = {"initcost": r.initcost, "finalcost": r.finalcost, "numiter": r.numiter, "queue_ms": r.queue_ms,
+               "run_ms": r.run_ms, "total_ms": r.total_ms}
+        res.update(out)
+        return res
+
+    def wait(self, ticket: int, timeout: float = 3600.0) -> dict:
+        r = _lib.McJobResult()
+        check(self._lib.mc_server_wait(self._h, int(ticket), int(timeout * 1000), ctypes.byref(r)))
+        return self._finish(ticket, r)
+
+    def poll(self, ticket: int):
+        """The result dict, or None while the job is queued or running."""
+        r = _lib.McJobResult()
+        st = self._lib.mc_server_poll(self._h, int(ticket), ctypes.byref(r))
+        if st == _lib.MC_EBUSY:
+            return None
+        check(st)
+        return self._finish(ticket, r)
+
+    def stats(self) -> dict:
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        check(self._lib.mc_server_stats(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
+
+    def reset_stats(self):
+        check(self._lib.mc_server_reset_stats(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            self._lib.mc_server_destroy(self._h)
+            self._h = None
+            self._live.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:

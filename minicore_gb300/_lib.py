@@ -22,6 +22,17 @@ class McMatrix(ctypes.Structure):
                 ("values", P), ("indices", P), ("indptr", P), ("nnz", U64)]
 
 
+class McJobDesc(ctypes.Structure):
+    _fields_ = [("X", McMatrix), ("centers", P), ("k", U32), ("msr", I), ("prior", D), ("weights", P),
+                ("precision", I), ("eps", D), ("maxiter", U64), ("seed", U64), ("centers_out", P),
+                ("asn_out", P), ("costs_out", P), ("center_ids_out", P)]
+
+
+class McJobResult(ctypes.Structure):
+    _fields_ = [("status", I), ("numiter", U64), ("initcost", D), ("finalcost", D), ("queue_ms", D),
+                ("run_ms", D), ("total_ms", D), ("error", ctypes.c_char * 256)]
+
+
 # name -> (restype, argtypes); every symbol the header declares
 SIGNATURES = {
     "mc_version": (ctypes.c_char_p, []),
@@ -52,6 +63,14 @@ SIGNATURES = {
     "mc_job_read": (I, [P, P, P, P]),
     "mc_job_recheck_count": (I, [P, ctypes.POINTER(U64)]),
     "mc_assign_sqrl2_noalloc": (I, [P, U64, U64, P, U32, P, P, P]),
+    "mc_job_create_kmeanspp": (I, [P, P, U32, I, D, P, I, U64, P, ctypes.POINTER(P)]),
+    "mc_server_create": (I, [I, U32, U64, ctypes.POINTER(P)]),
+    "mc_server_submit": (I, [P, ctypes.POINTER(McJobDesc), ctypes.POINTER(U64)]),
+    "mc_server_poll": (I, [P, U64, ctypes.POINTER(McJobResult)]),
+    "mc_server_wait": (I, [P, U64, U64, ctypes.POINTER(McJobResult)]),
+    "mc_server_stats": (I, [P, ctypes.c_char_p, U64]),
+    "mc_server_reset_stats": (I, [P]),
+    "mc_server_destroy": (I, [P]),
 }
 
 _lib = None

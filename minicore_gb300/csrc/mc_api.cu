@@ -476,13 +476,18 @@ int mc_context_synchronize(mc_context *ctx) {
 // ------------------------------------------------------------------------------------
 // jobs
 // ------------------------------------------------------------------------------------
-int mc_job_create(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_t k, int msr, double prior,
-                  const double *weights, int precision, uint64_t seed, mc_job **out) {
+// centers == nullptr: seed them by D^2 sampling with U(seed, i), i < k, on the job's own
+// device copy of the rows (kmeans.h:49-215), then copy the chosen rows into the centers,
+// which is what minicore.cluster() does between kmeanspp and hcluster
+// (python/minicore/__init__.py:235-261), without a host round trip.
+static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_t k, int msr,
+                           double prior, const double *weights, int precision, uint64_t seed, uint32_t *center_ids,
+                           mc_job **out) {
     if (!ctx || !out) return fail(MC_EINVAL, "null context or output");
     if (!measure_supported(msr)) return fail(MC_EUNSUPPORTED, "measure not implemented on this path");
     if (precision != MC_FP32 && precision != MC_TF32 && precision != MC_BF16)
         return fail(MC_EINVAL, "unknown precision");
-    if (k == 0 || !centers) return fail(MC_EINVAL, "no centers");
+    if (k == 0) return fail(MC_EINVAL, "no centers");
     MC_CUDA_TRY(cudaSetDevice(ctx->device));
     std::unique_ptr<mc_job> j(new mc_job());
     j->ctx = ctx;
@@ -508,7 +513,8 @@ int mc_job_create(mc_context *ctx, const mc_matrix *X, const float *centers, uin
     MC_TRY(j->det_tmp.alloc(det_chunks(n) + 1, st));
     MC_TRY(j->scal.alloc(4, st));
     MC_TRY(j->flag.alloc(1, st));
-    MC_CUDA_TRY(cudaMemcpyAsync(j->C.p, centers, uint64_t(k) * d * sizeof(float), cudaMemcpyDefault, st));
+    if (centers)
+        MC_CUDA_TRY(cudaMemcpyAsync(j->C.p, centers, uint64_t(k) * d * sizeof(float), cudaMemcpyDefault, st));
     if (weights) {
         MC_TRY(j->w.alloc(n, st));
         MC_CUDA_TRY(cudaMemcpyAsync(j->w.p, weights, n * sizeof(double), cudaMemcpyDefault, st));
@@ -518,6 +524,46 @@ int mc_job_create(mc_context *ctx, const mc_matrix *X, const float *centers, uin
         MC_TRY(launch_row_sums_dense(j->M.X, n, d, j->rowsum.p, j->rownorm.p, st));
     } else {
         MC_TRY(launch_row_sums_csr(j->M.vals, j->M.indptr, n, j->rowsum.p, st));
+    }
+    if (!centers) {
+        if (k > n) return fail(MC_EINVAL, "k-means++ seeding needs k <= number of rows");
+        std::vector<double> uh(k);
+        for (uint32_t i = 0; i < k; ++i) uh[i] = uniform_at(seed, i);
+        DBuf<double> u, dist, tmp;
+        DBuf<float> cbuf;
+        DBuf<uint32_t> ids;
+        DBuf<uint64_t> newc;
+        MC_TRY(u.alloc(k, st));
+        MC_TRY(dist.alloc(n, st));
+        MC_TRY(tmp.alloc(det_chunks(n) + 1, st));
+        MC_TRY(cbuf.alloc(d, st));
+        MC_TRY(ids.alloc(k, st));
+        MC_TRY(newc.alloc(1, st));
+        MC_CUDA_TRY(cudaMemcpyAsync(u.p, uh.data(), k * sizeof(double), cudaMemcpyHostToDevice, st));
+        KmppArgs a;
+        a.msr = msr;
+        a.csr = j->M.kind == MC_CSR_F32;
+        a.n = n;
+        a.d = d;
+        a.k = k;
+        a.X = j->M.X;
+        a.vals = j->M.vals;
+        a.idx = j->M.idx;
+        a.indptr = j->M.indptr;
+        a.rowsum = j->rowsum.p;
+        a.w = j->w.p;
+        a.prior = prior;
+        a.prior_sum = prior * double(d);
+        a.cbuf = cbuf.p;
+        a.dist = dist.p;
+        a.asn = j->asn.p;
+        a.center_ids = ids.p;
+        a.newc = newc.p;
+        MC_TRY(run_kmeanspp(a, u.p, tmp.p, ctx->sms, st));
+        MC_TRY(launch_gather_rows(j->M.kind == MC_CSR_F32, j->M.X, j->M.vals, j->M.idx, j->M.indptr, d, ids.p, k,
+                                  j->C.p, st));
+        if (center_ids) MC_TRY(copy_out(center_ids, ids.p, k, st));
+        MC_TRY(sync(st));
     }
     // constant-prior check: pv == prior for every pair when prior >= smallest_pv at the
     // largest row and center sums (centers are means or rows, so bounded by the rows)
@@ -544,6 +590,17 @@ int mc_job_create(mc_context *ctx, const mc_matrix *X, const float *centers, uin
     j->sparse_path = j->M.kind == MC_CSR_F32 && !j->pair && msr != JSD;
     *out = j.release();
     return MC_OK;
+}
+
+int mc_job_create(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_t k, int msr, double prior,
+                  const double *weights, int precision, uint64_t seed, mc_job **out) {
+    if (!centers) return fail(MC_EINVAL, "no centers");
+    return job_create_impl(ctx, X, centers, k, msr, prior, weights, precision, seed, nullptr, out);
+}
+
+int mc_job_create_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior,
+                           const double *weights, int precision, uint64_t seed, uint32_t *center_ids, mc_job **out) {
+    return job_create_impl(ctx, X, nullptr, k, msr, prior, weights, precision, seed, center_ids, out);
 }
 
 int mc_job_destroy(mc_job *job) {

@@ -204,4 +204,39 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     return MC_OK;
 }
 
+// centers[c] = row ids[c] (dense copy, or a zero-filled row with the CSR entries scattered)
+__global__ void k_gather_rows_dense(const float *__restrict__ X, uint64_t d, const uint32_t *__restrict__ ids,
+                                    uint32_t k, float *__restrict__ C) {
+    const uint64_t total = uint64_t(k) * d;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x))
+        C[e] = X[uint64_t(ids[e / d]) * d + e % d];
+}
+
+__global__ void k_gather_rows_csr(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                                  const uint64_t *__restrict__ indptr, uint64_t d, const uint32_t *__restrict__ ids,
+                                  uint32_t k, float *__restrict__ C) {
+    for (uint32_t c = blockIdx.x; c < k; c += gridDim.x) {
+        float *row = C + uint64_t(c) * d;
+        for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) row[j] = 0.f;
+        __syncthreads();
+        const uint32_t r = ids[c];
+        for (uint64_t p = indptr[r] + threadIdx.x; p < indptr[r + 1]; p += blockDim.x) row[idx[p]] = vals[p];
+        __syncthreads();
+    }
+}
+
+int launch_gather_rows(bool csr, const float *X, const float *vals, const uint32_t *idx, const uint64_t *indptr,
+                       uint64_t d, const uint32_t *ids, uint32_t k, float *C, cudaStream_t st) {
+    if (k == 0) return MC_OK;
+    if (csr) {
+        k_gather_rows_csr<<<unsigned(umin64(k, 4096)), 256, 0, st>>>(vals, idx, indptr, d, ids, k, C), note_launch();
+    } else {
+        const uint64_t total = uint64_t(k) * d;
+        k_gather_rows_dense<<<unsigned(umin64((total + 255) / 256, 4096)), 256, 0, st>>>(X, d, ids, k, C),
+            note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 }  // namespace mc

@@ -26,4 +26,8 @@ struct KmppArgs {
 
 int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);
 
+// C[c] = row ids[c], c < k (CSR rows densified into d columns)
+int launch_gather_rows(bool csr, const float *X, const float *vals, const uint32_t *idx, const uint64_t *indptr,
+                       uint64_t d, const uint32_t *ids, uint32_t k, float *C, cudaStream_t st);
+
 }  // namespace mc

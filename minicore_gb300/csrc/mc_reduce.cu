@@ -560,8 +560,10 @@ int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool p
         const uint64_t bw = band < d ? band : d;
         const size_t smem = a.w ? bw * sizeof(double) : 2 * bw * sizeof(float);
         const unsigned nb = unsigned((d + band - 1) / band);
+        // always the largest band's size: a per-call value could be lowered by another host
+        // thread between this call's set and its launch
         MC_CUDA_TRY(cudaFuncSetAttribute(k_centroid_chunks_csr, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem)));
+                                         int(2 * 24576 * sizeof(float))));
         k_centroid_chunks_csr<<<dim3(unsigned(max_chunks), nb), 256, smem, st>>>(
             a.vals, a.idx, a.indptr, d, bw, w.perm.p, w.bucket_start.p, w.bucket_count.p, w.chunk_start.p, k, ch,
             a.w, w.partial.p, w.partial_w.p), note_launch();

@@ -74,3 +74,44 @@ def test_python_api_rejects_out_of_scope_options():
         mc.hcluster(X, [0, 1], mbsize=2)
     with pytest.raises(NotImplementedError):
         mc.cluster(X, msr=2, k=2, temp=1.0)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """ctypes mirrors of mc_matrix / mc_job_desc / mc_job_result have the C layout."""
+    import shutil
+    import subprocess
+    from minicore_gb300 import _lib
+    if not shutil.which("gcc"):
+        import pytest
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "layout.c"
+    fields = {"mc_matrix": _lib.McMatrix, "mc_job_desc": _lib.McJobDesc, "mc_job_result": _lib.McJobResult}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "minicore_gb300.h"', "int main(void) {"]
+    for cname, cls in fields.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(root, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                 text=True).stdout.splitlines())
+    for cname, cls in fields.items():
+        assert int(out[cname]) == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert int(out[f"{cname}.{f}"]) == getattr(cls, f).offset, f"{cname}.{f}"
+
+
+def test_server_create_fails_cleanly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        return
+    from minicore_gb300 import _lib
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.mc_server_create(0, 2, 0, ctypes.byref(h)) != 0
+    assert not h.value
+    assert lib.mc_server_create(0, 0, 0, ctypes.byref(h)) == _lib.MC_EINVAL
+    assert lib.mc_server_destroy(None) == 0
