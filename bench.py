@@ -43,10 +43,12 @@ def parse():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving"],
+    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving", "coreset"],
                     help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
                          "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass; serving: "
-                         "the Poisson job stream through the continuous-batching server")
+                         "the Poisson job stream through the continuous-batching server; coreset: the "
+                         "2M x 64 kmeans++ -> sensitivity -> sampling -> weighted Lloyd pipeline")
+    ap.add_argument("--coreset-rows", type=int, default=2_000_000)
     ap.add_argument("--serving-jobs", type=int, default=4000,
                     help="jobs in the --workload serving stream (the full stream is 20000)")
     ap.add_argument("--serving-rate", type=float, default=200.0)
@@ -176,6 +178,127 @@ def csr_bench(args):
                         "algorithmic_bytes": algo_bytes, "kernel_ms": kms, "peak_source": pk_kind},
            "phases_ms": phases}
     print(json.dumps(out))
+
+
+def coreset_bench(args):
+    """Coreset pipeline on 2M x 64 (200-component mixture, Dirichlet(0.3) component
+    weights): kmeans++ (k=100) -> LBK sensitivities + alias table -> 50,000 weighted draws
+    -> weighted Lloyd on the coreset -> full-data objective of the coreset centers, against
+    the objective of Lloyd on the full data from the same seeds.  Rows stay in HBM; every
+    stage is timed with CUDA events on the library's stream."""
+    import torch
+    import minicore_gb300 as mc
+    from minicore_gb300 import _lib
+    torch.cuda.set_device(0)
+    lib = _lib.load()
+    ctx = mc.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    n, d, k, m, comps = args.coreset_rows, 64, 100, 50_000, 200
+    rng = np.random.default_rng(0)
+    wts = torch.from_numpy(rng.dirichlet(np.full(comps, 0.3))).cuda()
+    g = torch.Generator(device="cuda").manual_seed(0)
+    mu = torch.randn(comps, d, generator=g, device="cuda") * 2.0
+    lab = torch.multinomial(wts, n, replacement=True, generator=g)
+    X = torch.randn(n, d, generator=g, device="cuda").add_(mu[lab]).contiguous()
+    del lab
+    M = mc._MatrixArg(X)
+    u = torch.from_numpy(mc.uniforms(77, k)).cuda()
+    ids = torch.empty(k, dtype=torch.int32, device="cuda")
+    asn = torch.empty(n, dtype=torch.int32, device="cuda")
+    costs = torch.empty(n, dtype=torch.float64, device="cuda")
+    cw = torch.empty(m, dtype=torch.float32, device="cuda")
+    cidx = torch.empty(m, dtype=torch.int64, device="cuda")
+    precision = args.precision
+
+    def ev():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(stream)
+        return e
+
+    def pipeline():
+        t = [ev()]
+        _lib.check(lib.mc_kmeanspp(ctx.handle, M.ref, k, 2, 0.0, None, mc._p(u), mc._p(ids), mc._p(asn),
+                                   mc._p(costs)))
+        t.append(ev())
+        h = ctypes.c_void_p()
+        _lib.check(lib.mc_sampler_create(ctx.handle, n, k, k, mc._p(costs), 1, mc._p(asn), None, 4, 0.0,
+                                         ctypes.byref(h)))
+        t.append(ev())
+        _lib.check(lib.mc_sampler_sample(h, m, 1234, 0, mc._p(cw), mc._p(cidx)))
+        t.append(ev())
+        lib.mc_sampler_destroy(h)
+        Xc = X[cidx].contiguous()
+        C0 = X[ids.long()].contiguous()
+        jc = mc.Job(Xc, C0, msr=2, weights=cw.double(), precision="fp32", seed=9, ctx=ctx)
+        jc.run(eps=1e-4, maxiter=20)
+        Cc = torch.empty((k, d), dtype=torch.float32, device="cuda")
+        jc.read(Cc, None, None)
+        t.append(ev())
+        # the coreset centers on the full data: one assignment pass + FP64 objective
+        jf = mc.Job(X, Cc, msr=2, precision=precision, seed=9, ctx=ctx)
+        jf.assign()
+        obj_core = jf.cost()
+        t.append(ev())
+        jc.close()
+        jf.close()
+        return t, obj_core, C0
+
+    for _ in range(max(args.warmup, 1)):
+        pipeline()
+    torch.cuda.synchronize()
+    clocks = Clocks()
+    clocks.start()
+    l0 = lib.mc_kernel_launches()
+    stage_ms = []
+    for _ in range(args.steps):
+        t, obj_core, C0 = pipeline()
+        torch.cuda.synchronize()
+        stage_ms.append([t[i].elapsed_time(t[i + 1]) for i in range(len(t) - 1)])
+    launches = int(lib.mc_kernel_launches() - l0)
+    clk = clocks.stop()
+    stage = np.mean(np.array(stage_ms), axis=0)
+    names = ["kmeanspp", "sensitivity_alias", "sample", "coreset_lloyd", "full_data_assign"]
+    total_ms = float(stage.sum())
+    # the full-data solution from the same seeds, for the objective ratio (untimed)
+    jfull = mc.Job(X, C0, msr=2, precision=precision, seed=9, ctx=ctx)
+    jfull.run(eps=1e-4, maxiter=20)
+    obj_full = jfull.cost()
+    jfull.close()
+    pk, pk_kind = peaks()
+    kmpp_bytes = k * n * d * 4 + k * n * 8 * 2
+    achieved = kmpp_bytes / (stage[0] * 1e-3) / 1e9
+    hbm = pk.get("hbm_gbs", 6800.0)
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        S = 100_000
+        Xs = X[:S].cpu().numpy()
+        t0 = time.perf_counter()
+        oracle.kmeanspp(Xs, k, 2, 0.0, mc.uniforms(77, k))
+        per = (time.perf_counter() - t0) * (n / S)
+        cpu = {"value": 1.0 / per, "unit": "kmeans++ runs/s (k=100, 2M x 64)", "cores": os.cpu_count() or 1,
+               "kind": "port", "sample": f"oracle kmeans++ on {S} rows, k={k}, scaled by {n}/{S}"}
+    line = {"metric": "coreset pipelines/s 2M x 64 (kmeans++ k=100 -> LBK -> 50k draws -> weighted Lloyd)",
+            "value": 1000.0 / total_ms, "unit": "pipelines/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32" if precision == "fp32" else f"f32 ({precision} full-data assign)",
+            "data": "synthetic",
+            "config": {"workload": f"dense {n}x{d}, {comps} components N(0,4I) means, Dirichlet(0.3) weights; "
+                                   f"kmeans++ k={k}; LBK sensitivities; alias; m={m}; weighted Lloyd eps 1e-4 "
+                                   f"<= 20 updates", "l2": "rows 512 MB > L2"},
+            "stages_ms": dict(zip(names, map(float, stage))),
+            "objective": {"coreset_centers_on_full_data": obj_core, "full_data_lloyd": obj_full,
+                          "ratio": obj_core / obj_full},
+            "roofline": {"bound": "hbm", "kernel": "kmeans++ (k passes over the rows)", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_source": f"{pk_kind} hbm_gbs",
+                         "algorithmic": f"k*n*d*4 + 2*k*n*8 = {kmpp_bytes:.4g} bytes"},
+            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk,
+            "e2e": None}
+    print(json.dumps(line))
 
 
 SERVE_DS = (32, 64, 128, 512)
@@ -402,6 +525,41 @@ class Clocks:
                 "reasons": reasons, "samples": len(s)}
 
 
+def fp64_objective_check(job, X, n, sample=100_000, seed=5):
+    """After the timed steps: the job's assignment and objective on a fixed row subsample
+    against an FP64 computation (numpy, float64 GEMM form of the squared distances) with
+    the same centers."""
+    import torch
+    k, d = job.k, X.shape[1]
+    C = np.empty((k, d), np.float32)
+    asn = np.empty(n, np.uint32)
+    costs = np.empty(n, np.float64)
+    job.read(C, asn, costs)
+    S = np.sort(np.random.default_rng(seed).choice(n, min(sample, n), replace=False))
+    Xs = X[torch.from_numpy(S).cuda()].cpu().numpy().astype(np.float64)
+    C64 = C.astype(np.float64)
+    cn = (C64 * C64).sum(1)
+    best = np.empty(len(S))
+    arg = np.empty(len(S), np.int64)
+    for i in range(0, len(S), 8192):
+        x = Xs[i:i + 8192]
+        dist = (x * x).sum(1)[:, None] - 2.0 * (x @ C64.T) + cn[None, :]
+        arg[i:i + 8192] = dist.argmin(1)
+        best[i:i + 8192] = np.maximum(dist.min(1), 0.0)
+    obj64 = float(best.sum())
+    obj_gpu = float(costs[S].sum())
+    # the FP64 distance to the center the GPU picked, where the argmins differ
+    diff = np.nonzero(arg != asn[S])[0]
+    gap = 0.0
+    if len(diff):
+        xd = Xs[diff]
+        cd = C64[asn[S][diff].astype(np.int64)]
+        gap = float((((xd - cd) ** 2).sum(1) - best[diff]).max())
+    return {"sample_rows": int(len(S)), "objective_gpu": obj_gpu, "objective_fp64": obj64,
+            "rel_err": abs(obj_gpu - obj64) / obj64, "argmin_agreement": float(1.0 - len(diff) / len(S)),
+            "max_fp64_gap_where_argmin_differs": gap}
+
+
 def cpu_baseline(X_sample, C, threads):
     """One Lloyd iteration (assignment + centroid update) of the oracle on a row sample."""
     import oracle
@@ -452,6 +610,8 @@ def main():
         return reference_arm(args)
     if args.workload == "serving":
         return serving_main(args)
+    if args.workload == "coreset":
+        return coreset_bench(args)
     if args.workload != "dense":
         return csr_bench(args)
     import torch
@@ -523,6 +683,7 @@ def main():
     ms_per_step = ms / args.steps
     value = world * 1000.0 / ms_per_step  # independent replicas: iterations completed per second
     recheck = job.recheck_count()
+    accuracy = fp64_objective_check(job, X, n) if rank == 0 else None
 
     # dominant kernel: the tensor-core assignment kernel (two passes per assignment) or the
     # FP32 tiled kernel, from the events recorded over the timed region
@@ -618,6 +779,7 @@ def main():
                 "fp32_gpu_iters_per_s": fp32,
                 "speedup_vs_fp32_gpu": (value / world / fp32) if fp32 else None,
                 "recheck_rows_last_pass": recheck,
+                "accuracy_vs_fp64": accuracy,
                 "roofline": roofline, "phases_ms_timed_region": phases,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk,
