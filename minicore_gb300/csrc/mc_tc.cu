@@ -15,13 +15,19 @@
 // covers FP32 rounding of the norms and of the exact sequential distance
 // (gamma_d = d 2^-24 / (1 - d 2^-24)).
 //
-// Two passes over the same MMAs (the tensor cores are deterministic, so both passes see
-// identical values): pass 1 keeps only each row's minimum b1 (branch-free epilogue);
-// pass 2 lists every center with v_j <= b1 + Delta (up to 4 per column half).  The
-// finalize pass evaluates the exact FP32 distance (sequential fmaf over columns, the FP32
-// path's expression) of each candidate and keeps the smallest, lowest index on ties; rows
-// with more candidates than slots are rescanned exactly over all centers.  So the
-// assignment equals the FP32 path's on every row and costs are exact FP32 distances.
+// Pass 1 (branch-free epilogue) takes the minimum of every subgroup of 8 consecutive
+// centers and keeps, per row, the two smallest subgroup minima m1 <= m2 and the subgroup
+// of m1.  If m2 > m1 + Delta, every candidate lies in that subgroup ("single" rows: m1 is
+// the row's b1).  The other rows ("multi", about 12 % of the 4M x 128 mixture) are gathered
+// into a compact operand copy, and pass 2 (the same MMAs over those rows; the tensor cores
+// are deterministic) lists every center with v_j <= m1 + Delta (up to 3 per column part).
+// The finalize pass walks the rows sorted by their subgroup (so a warp's center loads are
+// mostly one broadcast), evaluates the exact FP32 distance (sequential fmaf over columns,
+// the FP32 path's expression) of the 8 centers of a single row's subgroup or of a multi
+// row's candidates, and keeps the smallest, lowest index on ties; rows with more
+// candidates than slots, or with a non-finite minimum or bound, are rescanned exactly over
+// all centers.  So the assignment equals the FP32 path's on every row and costs are exact
+// FP32 distances.
 //
 // Every mbarrier wait is bounded (about one second of clock64 cycles); on a timeout the
 // kernel records an error code, stops issuing, waits (bounded) for its copies and MMAs in
@@ -44,15 +50,19 @@ constexpr int STAGES = 4;
 constexpr int A_STAGE = BM * KBYTES;   // 16 KB
 constexpr int B_STAGE = BN * KBYTES;   // 32 KB
 constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
-constexpr int NCAND = 4;             // candidate slots per row and column half
-constexpr int EPI_WARPS = 8;      // two per TMEM lane quarter, each taking half of a chunk's columns
-constexpr int THREADS = 64 + 32 * EPI_WARPS;  // warp 0 TMA, warp 1 MMA (+TMEM alloc), warps 2-9 epilogue
+constexpr int PARTS = 4;          // column parts of a chunk: one epilogue warp per (lane quarter, part)
+constexpr int PCOLS = BN / PARTS;  // 64 columns per epilogue warp and chunk
+constexpr int NCAND = 3;          // pass 2 candidate slots per row and column part
+constexpr int EPI_WARPS = 4 * PARTS;
+constexpr int THREADS = 64 + 32 * EPI_WARPS;  // warp 0 TMA, warp 1 MMA (+TMEM alloc), warps 2-17 epilogue
 constexpr int CN_SMEM = 4096;     // center norms staged in shared memory when kp <= CN_SMEM
 constexpr uint32_t TMEM_COLS = 512;
 constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
 
 struct Smem {
     uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], drain;
+    uint64_t nrows;      // rows of this launch (pass 2: the compact row count read on the device)
+    uint32_t ntiles;
     uint32_t tmem_base;
     int abort;
     int outstanding[STAGES];
@@ -198,13 +208,23 @@ struct TcArgs {
     float eta, gamma;
     const float *cnp;      // [kp] center norms, +inf past k; [kp] holds Cmax
     uint32_t kp;
-    float *b1;             // [n][2] pass 1 output: minimum per row and column half
-    uint8_t *cnt;          // [n][2] pass 2 output: candidates per column half (255: too many)
-    uint32_t *cand;        // [n][2][NCAND] pass 2 output: candidate centers
+    float *b1;             // [n][PARTS] pass 1: smallest subgroup minimum per row and column part
+    float *b2;             // [n][PARTS] pass 1: second smallest subgroup minimum
+    uint32_t *j1;          // [n][PARTS] pass 1: subgroup (8 centers) of b1 (0xffffffff: none)
+    const unsigned *count; // pass 2: device count of compact rows (rows = min(*count, n))
+    const float *thrc;     // [rows] pass 2: candidate threshold per compact row
+    uint8_t *cnt;          // [rows][PARTS] pass 2: candidates per column part (255: too many)
+    uint32_t *cand;        // [rows][PARTS][NCAND] pass 2: candidate centers
     int *err;
 };
 
-enum TcMode { TC_MIN = 0, TC_CAND = 1 };
+enum TcMode { TC_TOP2 = 0, TC_CAND = 1 };
+
+// (a1, a2) <- top-2 of the union of (a1, a2) and (b1, b2)
+__device__ __forceinline__ void top2_merge(float &a1, float &a2, float b1, float b2) {
+    a2 = fminf(fminf(a2, b2), fmaxf(a1, b1));
+    a1 = fminf(a1, b1);
+}
 
 template <bool TF32, int MODE>
 __global__ void __launch_bounds__(tc::THREADS, 1)
@@ -234,6 +254,10 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         }
         mbar_init(&sm->drain, 1);
         sm->abort = 0;
+        uint64_t rows = a.n;
+        if (a.count) rows = umin64(uint64_t(*a.count), a.n);
+        sm->nrows = rows;
+        sm->ntiles = uint32_t((rows + BM - 1) / BM);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -247,13 +271,15 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     fence_after();
     const uint32_t tmem = sm->tmem_base;
     const uint32_t total_it = a.nchunks * a.kb;  // k-block iterations per row tile
+    const uint32_t ntiles = sm->ntiles;
+    const uint64_t nrows = sm->nrows;
 
     if (warp == 0) {
         // ---------------- TMA producer ----------------
         if (lane == 0) {
             uint32_t s = 0, ph = 0;
             bool ok = true;
-            for (uint32_t m = blockIdx.x; m < a.ntiles && ok; m += gridDim.x) {
+            for (uint32_t m = blockIdx.x; m < ntiles && ok; m += gridDim.x) {
                 for (uint32_t it = 0; it < total_it && ok; ++it) {
                     const uint32_t nc = it / a.kb, kb = it % a.kb;
                     if (!mbar_wait(&sm->empty[s], ph ^ 1, sm, a.err, 1)) { ok = false; break; }
@@ -274,7 +300,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
             uint32_t s = 0, ph = 0;
             uint32_t acc_it = 0;
             bool ok = true;
-            for (uint32_t m = blockIdx.x; m < a.ntiles && ok; m += gridDim.x) {
+            for (uint32_t m = blockIdx.x; m < ntiles && ok; m += gridDim.x) {
                 for (uint32_t nc = 0; nc < a.nchunks && ok; ++nc, ++acc_it) {
                     const uint32_t buf = acc_it & 1, use = acc_it >> 1;
                     if (!mbar_wait(&sm->acc_empty[buf], (use & 1) ^ 1, sm, a.err, 2)) { ok = false; break; }
@@ -297,34 +323,31 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
                     if (ok) mma_commit(&sm->acc_full[buf]);
                 }
             }
-            // all MMAs issued by this thread complete before the drain barrier fires
-            mma_commit(&sm->drain);
-            mbar_drain(&sm->drain, 0);
+            // all MMAs issued by this thread complete before the drain barrier fires (a CTA
+            // without tiles, possible in pass 2, issued none and has nothing to drain)
+            if (blockIdx.x < ntiles) {
+                mma_commit(&sm->drain);
+                mbar_drain(&sm->drain, 0);
+            }
         }
     } else {
-        // ---------------- epilogue (warps 2-9) ----------------
+        // ---------------- epilogue (warps 2-17) ----------------
         const int quarter = warp & 3;                 // TMEM lanes 32*quarter .. +31
-        const int half = (warp - 2) >> 2;             // columns [128*half, 128*half + 128) of a chunk
+        const int part = (warp - 2) >> 2;             // columns [64*part, 64*part + 64) of a chunk
         const uint32_t lane_base = uint32_t(quarter * 32) << 16;
         const int rloc = quarter * 32 + lane;
+        const float INF = __int_as_float(0x7f800000);
         uint32_t acc_it = 0;
         bool ok = true;
-        const float cmax = a.cnp[a.kp];
-        for (uint32_t m = blockIdx.x; m < a.ntiles && ok; m += gridDim.x) {
-            const uint64_t row = uint64_t(m) * BM + rloc;
-            const bool valid = row < a.n;
-            float b1 = __int_as_float(0x7f800000);   // pass 1: running minimum
-            float thr = __int_as_float(0xff800000);  // pass 2: fixed candidate threshold
+        for (uint32_t m = blockIdx.x; m < ntiles && ok; m += gridDim.x) {
+            const uint64_t row = uint64_t(m) * BM + rloc;  // pass 2: compact row
+            const bool valid = row < nrows;
+            float m1 = INF, m2 = INF;                      // pass 1: top-2 of the subgroup minima
+            uint32_t sg1 = 0xffffffffu;                    // pass 1: subgroup (8 centers) of m1
+            float thr = __int_as_float(0xff800000);        // pass 2: fixed candidate threshold
             int ncand = 0;
-            if (MODE == TC_CAND && valid) {
-                const float bb = fminf(a.b1[2 * row], a.b1[2 * row + 1]);
-                const float xn = sqrtf(a.rownorm[row]);
-                const float delta = 4.f * a.eta * xn * cmax * 1.0001f + 4.f * a.gamma * (xn + cmax) * (xn + cmax);
-                // no finite minimum or a non-finite bound proves nothing: no candidates, and
-                // the finalize pass rescans the row exactly
-                if (bb < __int_as_float(0x7f800000) && delta <= 3.402823466e+38f) thr = bb + delta;
-            }
-            uint32_t *cdst = a.cand + (row * 2 + half) * NCAND;
+            if (MODE == TC_CAND && valid) thr = a.thrc[row];
+            uint32_t *cdst = a.cand + (row * PARTS + part) * NCAND;
             for (uint32_t nc = 0; nc < a.nchunks; ++nc, ++acc_it) {
                 const uint32_t buf = acc_it & 1, use = acc_it >> 1;
                 // one lane waits, the warp follows converged (tcgen05.ld is warp-collective)
@@ -334,12 +357,12 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
                 __syncwarp();
                 if (!got) { ok = false; break; }
                 fence_after();
-                const uint32_t taddr = tmem + lane_base + buf * BN + half * (BN / 2);
+                const uint32_t taddr = tmem + lane_base + buf * BN + part * PCOLS;
 #pragma unroll 1
-                for (int g = 0; g < BN / 2 / 32; ++g) {
+                for (int g = 0; g < PCOLS / 32; ++g) {
                     float v[32];
                     tmem_ld32(taddr + g * 32, v);
-                    const uint32_t j0 = nc * BN + half * (BN / 2) + g * 32;
+                    const uint32_t j0 = nc * BN + part * PCOLS + g * 32;
                     const float4 *c4 = reinterpret_cast<const float4 *>(cnp + j0);
 #pragma unroll
                     for (int q4 = 0; q4 < 8; ++q4) {
@@ -349,18 +372,38 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
                         v[4 * q4 + 2] = fmaf(-2.f, v[4 * q4 + 2], c.z);
                         v[4 * q4 + 3] = fmaf(-2.f, v[4 * q4 + 3], c.w);
                     }
-                    float smin[4];
+                    if (MODE == TC_TOP2) {
+                        if (j0 + 32 > a.k) {  // the chunk's padding centers take no part
 #pragma unroll
-                    for (int sg = 0; sg < 4; ++sg) {
-                        const float *w = v + 8 * sg;
-                        smin[sg] = fminf(fminf(fminf(w[0], w[1]), fminf(w[2], w[3])),
-                                         fminf(fminf(w[4], w[5]), fminf(w[6], w[7])));
-                    }
-                    if (MODE == TC_MIN) {
-                        b1 = fminf(b1, fminf(fminf(smin[0], smin[1]), fminf(smin[2], smin[3])));
+                            for (int i = 0; i < 32; ++i)
+                                if (j0 + uint32_t(i) >= a.k) v[i] = INF;
+                        }
+                        float smin[4];
+#pragma unroll
+                        for (int sg = 0; sg < 4; ++sg) {
+                            const float *w = v + 8 * sg;
+                            smin[sg] = fminf(fminf(fminf(w[0], w[1]), fminf(w[2], w[3])),
+                                             fminf(fminf(w[4], w[5]), fminf(w[6], w[7])));
+                        }
+                        // top-2 over the row's subgroup minima, with the subgroup of the minimum
+#pragma unroll
+                        for (int sg = 0; sg < 4; ++sg) {
+                            const float sv = smin[sg];
+                            const bool lower = sv < m1;
+                            m2 = fminf(m2, fmaxf(m1, sv));
+                            sg1 = lower ? (j0 >> 3) + uint32_t(sg) : sg1;
+                            m1 = fminf(m1, sv);
+                        }
                     } else {
+                        float smin[4];
+#pragma unroll
+                        for (int sg = 0; sg < 4; ++sg) {
+                            const float *w = v + 8 * sg;
+                            smin[sg] = fminf(fminf(fminf(w[0], w[1]), fminf(w[2], w[3])),
+                                             fminf(fminf(w[4], w[5]), fminf(w[6], w[7])));
+                        }
                         const float gmin = fminf(fminf(smin[0], smin[1]), fminf(smin[2], smin[3]));
-                        if (gmin <= thr) {  // candidates in this group (rare per row)
+                        if (gmin <= thr) {  // candidates in this group
 #pragma unroll
                             for (int sg = 0; sg < 4; ++sg) {
                                 if (smin[sg] <= thr) {
@@ -381,8 +424,14 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
             }
             if (!ok) break;
             if (valid) {
-                if (MODE == TC_MIN) a.b1[2 * row + half] = b1;
-                else a.cnt[2 * row + half] = ncand > NCAND ? uint8_t(255) : uint8_t(ncand);
+                const uint64_t o = row * PARTS + part;
+                if (MODE == TC_TOP2) {
+                    a.b1[o] = m1;
+                    a.b2[o] = m2;
+                    a.j1[o] = m1 < INF ? sg1 : 0xffffffffu;
+                } else {
+                    a.cnt[o] = ncand > NCAND ? uint8_t(255) : uint8_t(ncand);
+                }
             }
         }
     }
@@ -437,111 +486,298 @@ __global__ void k_center_prep_tc(const float *__restrict__ C, uint32_t k, uint32
     }
 }
 
-// Exact FP32 distances for the candidate centers of every row (sequential fmaf over the
-// columns: the FP32 path's expression).  A CTA stages 128 rows x 32 columns in shared
-// memory (coalesced); each thread walks its row against its candidates (up to 4 per column
-// half).  Rows with too many candidates, or none (NaN rows, non-finite bound), are listed
-// for an exact scan over all centers.
-constexpr int NSLOT = 2 * tc::NCAND;
+// Row status after pass 1 (k_tc_select): the subgroup holding every candidate (< 2^31),
+// MULTI | compact slot, or OVER (rescanned over all centers).  key[] orders the finalize:
+// the subgroup for single rows, nsg for multi rows, nsg + 1 for OVER rows.
+constexpr uint32_t ST_MULTI = 0x80000000u;
+constexpr uint32_t ST_OVER = 0xffffffffu;
 
-__global__ void __launch_bounds__(256) k_tc_finalize(const float *__restrict__ X, uint64_t n, uint64_t d,
-                                                      const float *__restrict__ C, uint32_t k, uint32_t *asn,
-                                                      const uint8_t *__restrict__ cnt,
-                                                      const uint32_t *__restrict__ cand, double *costs,
-                                                      unsigned long long *nrecheck, uint32_t *over_rows,
-                                                      unsigned long long *nover) {
-    constexpr int R = 256;
-    __shared__ float xs[R][33];
-    const int t = threadIdx.x;
-    const uint64_t row0 = uint64_t(blockIdx.x) * R;
-    const uint64_t row = row0 + t;
+// Combines the column parts' top-2 of every row, decides single / multi / over, and for
+// multi rows takes a compact slot: the row's operand copy goes to Xc[slot], its pass 2
+// threshold to thrc[slot].  Slots come from warp-aggregated atomics, so their order varies
+// from run to run; no result depends on it.
+__global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__restrict__ b1,
+                                                    const float *__restrict__ b2, const uint32_t *__restrict__ j1,
+                                                    const float *__restrict__ rownorm, const float *__restrict__ cmaxp,
+                                                    float eta, float gamma, uint32_t nsg, uint32_t *status,
+                                                    uint32_t *key, uint32_t *crow, float *thrc, unsigned *count,
+                                                    uint32_t cap, const uint4 *__restrict__ A, uint64_t row_u4,
+                                                    uint4 *Xc, uint32_t *over_rows, unsigned long long *nover,
+                                                    unsigned long long *nmulti) {
+    const uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const float INF = __int_as_float(0x7f800000);
+    bool over = false, multi = false;
+    float thr = 0.f;
+    if (row < n) {
+        float m1 = INF, m2 = INF;
+        uint32_t gr = ST_OVER;
+#pragma unroll
+        for (int p = 0; p < tc::PARTS; ++p) {
+            const float c1 = b1[row * tc::PARTS + p], c2 = b2[row * tc::PARTS + p];
+            if (c1 < m1) gr = j1[row * tc::PARTS + p];
+            top2_merge(m1, m2, c1, c2);
+        }
+        const float cmax = *cmaxp;
+        const float xn = sqrtf(rownorm[row]);
+        const float delta = 4.f * eta * xn * cmax * 1.0001f + 4.f * gamma * (xn + cmax) * (xn + cmax);
+        // no finite minimum or a non-finite bound proves nothing: exact rescan
+        if (!(m1 < INF) || !(delta <= 3.402823466e+38f) || gr >= nsg) {
+            over = true;
+        } else if (m2 > m1 + delta) {
+            status[row] = gr;
+            key[row] = gr;
+        } else {
+            multi = true;
+            thr = m1 + delta;
+        }
+    }
+    const unsigned mb = __ballot_sync(0xffffffffu, multi);
+    unsigned base = 0;
+    if (lane == 0 && mb) base = atomicAdd(count, unsigned(__popc(mb)));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (multi) {
+        const unsigned slot = base + unsigned(__popc(mb & ((1u << lane) - 1u)));
+        if (slot < cap) {
+            status[row] = ST_MULTI | slot;
+            key[row] = nsg;
+            crow[slot] = uint32_t(row);
+            thrc[slot] = thr;
+            const uint4 *src = A + row * row_u4;
+            uint4 *dst = Xc + uint64_t(slot) * row_u4;
+            for (uint64_t q = 0; q < row_u4; ++q) dst[q] = src[q];
+        } else {
+            over = true;  // compact buffer full: exact rescan
+        }
+    }
+    const unsigned ob = __ballot_sync(0xffffffffu, over);
+    unsigned long long obase = 0;
+    if (lane == 0) {
+        if (ob) obase = atomicAdd(nover, (unsigned long long)__popc(ob));
+        if (mb) atomicAdd(nmulti, (unsigned long long)__popc(mb));
+    }
+    obase = __shfl_sync(0xffffffffu, obase, 0);
+    if (over) {
+        status[row] = ST_OVER;
+        key[row] = nsg + 1;
+        over_rows[obase + __popc(ob & ((1u << lane) - 1u))] = uint32_t(row);
+    }
+}
+
+// Exact FP32 distances for the candidate centers of every row (sequential fmaf over the
+// columns: the FP32 path's expression).  Rows are taken in `order` (sorted by subgroup).
+// A CTA handles 128 consecutive rows of that order: it stages the centers of the first two
+// subgroups it meets in shared memory (when 16 d floats fit), and 32 columns of its rows
+// at a time; each thread keeps its row's staged columns in registers and walks its
+// candidates: the 8 centers of a single row's subgroup, or a multi row's pass 2 list (up
+// to 3 per column part).  A warp whose rows all use staged centers reads them from shared
+// memory (one broadcast per warp); any other warp reads its candidates from global memory.
+// Multi rows with too many candidates, or none, are listed for an exact scan over all
+// centers; OVER rows were listed by k_tc_select.
+constexpr int NSLOT = tc::PARTS * tc::NCAND;
+constexpr int FIN_ROWS = 128;
+constexpr int FIN_SG = 2;  // subgroups whose centers a CTA stages
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src),
+                 "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// 32 columns of one candidate: c - x for the staged columns, sequential fmaf
+__device__ __forceinline__ void fin_chunk32(const float *cr, const float (&xr)[32], float &a) {
+    const float4 *c4 = reinterpret_cast<const float4 *>(cr);
+#pragma unroll
+    for (int k4 = 0; k4 < 8; ++k4) {
+        const float4 c = c4[k4];
+        float df = c.x - xr[4 * k4 + 0];
+        a = fmaf(df, df, a);
+        df = c.y - xr[4 * k4 + 1];
+        a = fmaf(df, df, a);
+        df = c.z - xr[4 * k4 + 2];
+        a = fmaf(df, df, a);
+        df = c.w - xr[4 * k4 + 3];
+        a = fmaf(df, df, a);
+    }
+}
+
+// the same for a chunk of kmax < 32 columns or unaligned rows (columns read from shared memory)
+__device__ __forceinline__ void fin_chunk_scalar(const float *cr, const float *xrow, int kmax, float &a) {
+    for (int kk = 0; kk < kmax; ++kk) {
+        const float df = cr[kk] - xrow[kk];
+        a = fmaf(df, df, a);
+    }
+}
+
+template <bool VEC4>
+__global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restrict__ X, uint64_t n, uint64_t d,
+                                                           const float *__restrict__ C, uint32_t k, uint32_t nsg,
+                                                           int stage_centers, uint32_t *asn,
+                                                           const uint32_t *__restrict__ order,
+                                                           const uint32_t *__restrict__ status,
+                                                           const uint8_t *__restrict__ cnt,
+                                                           const uint32_t *__restrict__ cand, double *costs,
+                                                           uint32_t *over_rows, unsigned long long *nover) {
+    constexpr int R = FIN_ROWS;
+    extern __shared__ __align__(16) float cs[];  // [FIN_SG][8][d] staged centers
+    __shared__ __align__(16) float xs4[2][R][36];  // two 32-column stages (rows 144 B apart)
+    __shared__ uint32_t rows_s[R];
+    __shared__ uint32_t sg_first;
+    const int t = threadIdx.x, lane = t & 31;
+    const uint64_t pos = uint64_t(blockIdx.x) * R + t;
+    const uint64_t row = pos < n ? order[pos] : n;
+    rows_s[t] = uint32_t(row < n ? row : 0xffffffffu);
+    const uint32_t st = row < n ? status[row] : ST_OVER;
+    if (t == 0) sg_first = (stage_centers && st != ST_OVER && !(st & ST_MULTI)) ? st : 0xffffffffu;
     // cj[q] == 0xffffffff marks an unused slot
     uint32_t cj[NSLOT];
 #pragma unroll
     for (int q = 0; q < NSLOT; ++q) cj[q] = 0xffffffffu;
-    bool over = false, multi = false;
-    int c0 = 0, c1 = 0;
-    if (row < n) {
-        c0 = cnt[2 * row];
-        c1 = cnt[2 * row + 1];
-        over = c0 == 255 || c1 == 255 || c0 + c1 == 0;
-        multi = !over && c0 + c1 > 1;
-    }
-    // warp-aggregated counters: one atomic per warp
-    const int lane = t & 31;
-    const unsigned ob = __ballot_sync(0xffffffffu, over), mb = __ballot_sync(0xffffffffu, multi);
-    unsigned long long obase = 0;
-    if (lane == 0) {
-        if (ob) obase = atomicAdd(nover, (unsigned long long)__popc(ob));
-        if (mb) atomicAdd(nrecheck, (unsigned long long)__popc(mb));
-    }
-    obase = __shfl_sync(0xffffffffu, obase, 0);
-    if (over) over_rows[obase + __popc(ob & ((1u << lane) - 1u))] = uint32_t(row);
-    if (row < n && !over) {
-        {
+    bool over = false;
+    if (st != ST_OVER && (st & ST_MULTI)) {
+        const uint64_t slot = st & ~ST_MULTI;
+        int tot = 0;
 #pragma unroll
-            for (int q = 0; q < NSLOT; ++q) {
-                const int h = q / tc::NCAND, s = q % tc::NCAND;
-                if (s < (h ? c1 : c0)) {
-                    const uint32_t j = cand[row * NSLOT + q];
-                    cj[q] = j < k ? j : 0xffffffffu;
+        for (int p = 0; p < tc::PARTS; ++p) {
+            const int c = cnt[slot * tc::PARTS + p];
+            if (c == 255) over = true;
+            tot += c;
+#pragma unroll
+            for (int q = 0; q < tc::NCAND; ++q) {
+                if (q < c && c != 255) {
+                    const uint32_t j = cand[(slot * tc::PARTS + p) * tc::NCAND + q];
+                    cj[p * tc::NCAND + q] = j < k ? j : 0xffffffffu;
                 }
             }
         }
+        if (tot == 0) over = true;
+    } else if (st != ST_OVER) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint32_t j = st * 8u + uint32_t(q);
+            cj[q] = j < k ? j : 0xffffffffu;
+        }
     }
+    // warp-aggregated counter: one atomic per warp
+    const unsigned ob = __ballot_sync(0xffffffffu, over);
+    unsigned long long obase = 0;
+    if (lane == 0 && ob) obase = atomicAdd(nover, (unsigned long long)__popc(ob));
+    obase = __shfl_sync(0xffffffffu, obase, 0);
+    if (over) {
+        over_rows[obase + __popc(ob & ((1u << lane) - 1u))] = uint32_t(row);
+#pragma unroll
+        for (int q = 0; q < NSLOT; ++q) cj[q] = 0xffffffffu;
+    }
+    __syncthreads();
+    // staged centers: subgroups sg_first .. sg_first + FIN_SG - 1
+    const uint32_t sgf = sg_first;
+    if (sgf != 0xffffffffu) {
+        const uint64_t tot = uint64_t(FIN_SG) * 8 * d;
+        for (uint64_t e = t; e < tot; e += R) {
+            const uint64_t jl = e / d, col = e % d;
+            const uint64_t j = uint64_t(sgf) * 8 + jl;
+            cs[e] = (j < k) ? C[j * d + col] : 0.f;
+        }
+    }
+    const bool mine_local = sgf != 0xffffffffu && st != ST_OVER && !(st & ST_MULTI) && !over && st - sgf < FIN_SG;
+    const bool warp_local = __all_sync(0xffffffffu, mine_local || st == ST_OVER || over || row >= n);
+    const float *lbase = cs + uint64_t(mine_local ? st - sgf : 0) * 8 * d;
     float acc[NSLOT];
 #pragma unroll
     for (int q = 0; q < NSLOT; ++q) acc[q] = 0.f;
-    const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0) &&
-                      ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
-    for (uint64_t k0 = 0; k0 < d; k0 += 32) {
-        const int kmax = int(umin64(32, d - k0));
-        __syncthreads();
-        if (vec4 && kmax == 32) {
+    if (VEC4) {
+        // d % 4 == 0: 32-column chunks (the last one may be narrower) double-buffered with
+        // cp.async, so the next chunk's rows load while this one is evaluated
+        const uint64_t nchunk = (d + 31) / 32;
+        auto stage = [&](uint64_t ci, int buf) {
+            const uint64_t k0 = ci * 32;
+            const int kmax = int(umin64(32, d - k0));
             for (int e = t; e < R * 8; e += R) {
                 const int r = e >> 3, q4 = e & 7;
-                const uint64_t rr = row0 + r;
-                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (rr < n) v = __ldg(reinterpret_cast<const float4 *>(X + rr * d + k0) + q4);
-                xs[r][4 * q4 + 0] = v.x;
-                xs[r][4 * q4 + 1] = v.y;
-                xs[r][4 * q4 + 2] = v.z;
-                xs[r][4 * q4 + 3] = v.w;
+                const uint32_t rr = rows_s[r];
+                const bool ok = rr != 0xffffffffu && 4 * q4 < kmax;
+                const float *src = ok ? X + uint64_t(rr) * d + k0 + 4 * q4 : X;
+                cp_async16(&xs4[buf][r][4 * q4], src, ok ? 16 : 0);
             }
-        } else {
-            for (int e = t; e < R * 32; e += R) {
-                const int r = e >> 5, kk = e & 31;
-                const uint64_t rr = row0 + r;
-                xs[r][kk] = (rr < n && kk < kmax) ? X[rr * d + k0 + kk] : 0.f;
+            cp_async_commit();
+        };
+        stage(0, 0);
+        for (uint64_t ci = 0; ci < nchunk; ++ci) {
+            const int buf = int(ci & 1);
+            if (ci + 1 < nchunk) {
+                stage(ci + 1, buf ^ 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
-        }
-        __syncthreads();
+            __syncthreads();
+            const uint64_t k0 = ci * 32;
+            const int kmax = int(umin64(32, d - k0));
+            if (kmax == 32) {
+                // the row's 32 staged columns in registers, reused by every candidate
+                float xr[32];
 #pragma unroll
-        for (int q = 0; q < NSLOT; ++q) {
-            if (cj[q] != 0xffffffffu) {
-                const float *cr = C + uint64_t(cj[q]) * d + k0;
-                float a = acc[q];
-                if (vec4 && kmax == 32) {
-                    const float4 *c4 = reinterpret_cast<const float4 *>(cr);
+                for (int c4 = 0; c4 < 8; ++c4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(&xs4[buf][t][4 * c4]);
+                    xr[4 * c4 + 0] = v.x;
+                    xr[4 * c4 + 1] = v.y;
+                    xr[4 * c4 + 2] = v.z;
+                    xr[4 * c4 + 3] = v.w;
+                }
+                if (warp_local) {
+                    if (mine_local) {
 #pragma unroll
-                    for (int k4 = 0; k4 < 8; ++k4) {
-                        const float4 c = __ldg(c4 + k4);
-                        float df = c.x - xs[t][4 * k4 + 0];
-                        a = fmaf(df, df, a);
-                        df = c.y - xs[t][4 * k4 + 1];
-                        a = fmaf(df, df, a);
-                        df = c.z - xs[t][4 * k4 + 2];
-                        a = fmaf(df, df, a);
-                        df = c.w - xs[t][4 * k4 + 3];
-                        a = fmaf(df, df, a);
+                        for (int q = 0; q < 8; ++q)
+                            if (cj[q] != 0xffffffffu) fin_chunk32(lbase + uint64_t(q) * d + k0, xr, acc[q]);
                     }
                 } else {
-                    for (int kk = 0; kk < kmax; ++kk) {
-                        const float df = __ldg(cr + kk) - xs[t][kk];
-                        a = fmaf(df, df, a);
-                    }
+#pragma unroll
+                    for (int q = 0; q < NSLOT; ++q)
+                        if (cj[q] != 0xffffffffu) fin_chunk32(C + uint64_t(cj[q]) * d + k0, xr, acc[q]);
                 }
-                acc[q] = a;
+            } else {
+                if (warp_local) {
+                    if (mine_local) {
+#pragma unroll
+                        for (int q = 0; q < 8; ++q)
+                            if (cj[q] != 0xffffffffu)
+                                fin_chunk_scalar(lbase + uint64_t(q) * d + k0, xs4[buf][t], kmax, acc[q]);
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < NSLOT; ++q)
+                        if (cj[q] != 0xffffffffu)
+                            fin_chunk_scalar(C + uint64_t(cj[q]) * d + k0, xs4[buf][t], kmax, acc[q]);
+                }
+            }
+            __syncthreads();  // buffer buf is restaged two chunks later
+        }
+    } else {
+        for (uint64_t k0 = 0; k0 < d; k0 += 32) {
+            const int kmax = int(umin64(32, d - k0));
+            __syncthreads();
+            for (int e = t; e < R * 32; e += R) {
+                const int r = e >> 5, kk = e & 31;
+                const uint32_t rr = rows_s[r];
+                xs4[0][r][kk] = (rr != 0xffffffffu && kk < kmax) ? X[uint64_t(rr) * d + k0 + kk] : 0.f;
+            }
+            __syncthreads();
+            if (warp_local) {
+                if (mine_local) {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (cj[q] != 0xffffffffu)
+                            fin_chunk_scalar(lbase + uint64_t(q) * d + k0, xs4[0][t], kmax, acc[q]);
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < NSLOT; ++q)
+                    if (cj[q] != 0xffffffffu) fin_chunk_scalar(C + uint64_t(cj[q]) * d + k0, xs4[0][t], kmax, acc[q]);
             }
         }
     }
@@ -640,13 +876,31 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     CUtensorMap mA, mB;
     MC_TRY(make_map(&mA, Aptr, tf32, n, d, apitch, tc::BM));
     MC_TRY(make_map(&mB, tf32 ? (const void *)s.Ct.p : (const void *)s.Cb.p, tf32, kp, d, dp, tc::BN));
-    MC_TRY(s.b1.alloc(2 * n, st));
-    MC_TRY(s.cnt.alloc(2 * n, st));
-    MC_TRY(s.cand.alloc(n * NSLOT, st));
+    using tc::PARTS;
+    MC_TRY(s.b1.alloc(PARTS * n, st));
+    MC_TRY(s.b2.alloc(PARTS * n, st));
+    MC_TRY(s.j1.alloc(PARTS * n, st));
+    MC_TRY(s.status.alloc(n, st));
+    MC_TRY(s.key.alloc(n, st));
+    const uint32_t nsg = kp / 8;  // subgroups of 8 centers
+    // compact buffer for the multi rows: all rows up to 2^20, else a quarter of them (rows
+    // beyond the capacity are rescanned exactly)
+    const uint64_t cap = n <= (1u << 20) ? n : (n / 4 > (1u << 20) ? n / 4 : (1u << 20));
+    const uint64_t row_u4 = apitch * esz / 16;
+    MC_TRY(s.crow.alloc(cap, st));
+    MC_TRY(s.thrc.alloc(cap, st));
+    MC_TRY(s.Xc.alloc(cap * row_u4, st));
+    MC_TRY(s.cnt.alloc(PARTS * cap, st));
+    MC_TRY(s.cand.alloc(cap * NSLOT, st));
+    MC_TRY(s.count.alloc(1, st));
     MC_TRY(s.err.alloc(1, st));
     MC_TRY(s.nrecheck.alloc(2, st));
+    MC_TRY(s.over_rows.alloc(n, st));
     MC_CUDA_TRY(cudaMemsetAsync(s.err.p, 0, sizeof(int), st));
+    MC_CUDA_TRY(cudaMemsetAsync(s.count.p, 0, sizeof(unsigned), st));
     MC_CUDA_TRY(cudaMemsetAsync(s.nrecheck.p, 0, 2 * sizeof(unsigned long long), st));
+    CUtensorMap mC;
+    MC_TRY(make_map(&mC, s.Xc.p, tf32, cap, d, apitch, tc::BM));
     TcArgs a;
     a.n = n;
     a.d = d;
@@ -662,46 +916,67 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     const double g = double(d) * std::ldexp(1.0, -24);
     a.gamma = float(g / (1.0 - g) * 2.0);
     a.b1 = s.b1.p;
-    a.cnt = s.cnt.p;
-    a.cand = s.cand.p;
+    a.b2 = s.b2.p;
+    a.j1 = s.j1.p;
+    a.count = nullptr;
+    a.thrc = nullptr;
+    a.cnt = nullptr;
+    a.cand = nullptr;
     a.err = s.err.p;
+    TcArgs a2 = a;  // pass 2: compact rows, count read on the device
+    a2.n = cap;
+    a2.count = s.count.p;
+    a2.thrc = s.thrc.p;
+    a2.cnt = s.cnt.p;
+    a2.cand = s.cand.p;
     const size_t smem = size_t(tc::STAGES) * tc::STAGE_BYTES + tc::CN_SMEM * sizeof(float) + sizeof(tc::Smem) + 1024;
     const unsigned grid = unsigned(umin64(a.ntiles, uint64_t(sms)));
-    // pass 1 (row minima) and pass 2 (candidates under the fixed threshold)
-    if (tf32) {
-        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<true, TC_MIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem)));
-        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<true, TC_CAND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem)));
-        {
-            Phase ph("tc_pass1_min", st);
-            k_tc_assign<true, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
-        }
-        {
-            Phase ph("tc_pass2_candidates", st);
-            k_tc_assign<true, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
-        }
-    } else {
-        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<false, TC_MIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem)));
-        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_assign<false, TC_CAND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem)));
-        {
-            Phase ph("tc_pass1_min", st);
-            k_tc_assign<false, TC_MIN><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
-        }
-        {
-            Phase ph("tc_pass2_candidates", st);
-            k_tc_assign<false, TC_CAND><<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
-        }
+    const unsigned grid2 = unsigned(umin64((cap + tc::BM - 1) / tc::BM, uint64_t(sms)));
+    auto k1 = tf32 ? k_tc_assign<true, TC_TOP2> : k_tc_assign<false, TC_TOP2>;
+    auto k2 = tf32 ? k_tc_assign<true, TC_CAND> : k_tc_assign<false, TC_CAND>;
+    MC_CUDA_TRY(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    MC_CUDA_TRY(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    {
+        Phase ph("tc_pass1_top2", st);
+        k1<<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
     }
     MC_CUDA_TRY(cudaGetLastError());
-    MC_TRY(s.over_rows.alloc(n, st));
+    {
+        Phase ph("tc_select", st);
+        k_tc_select<<<unsigned((n + 255) / 256), 256, 0, st>>>(
+            n, s.b1.p, s.b2.p, s.j1.p, rownorm, s.cnorm_p.p + kp, a.eta, a.gamma, nsg, s.status.p, s.key.p,
+            s.crow.p, s.thrc.p, s.count.p, uint32_t(cap), static_cast<const uint4 *>(Aptr), row_u4, s.Xc.p,
+            s.over_rows.p, s.nrecheck.p + 1, s.nrecheck.p), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        // finalize order: rows grouped by subgroup, then multi rows, then OVER rows
+        MC_TRY(launch_sort_by_key(s.key.p, nullptr, n, nsg + 2, s.sort, st));
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    {
+        Phase ph("tc_pass2_candidates", st);
+        k2<<<grid2, tc::THREADS, smem, st>>>(mC, mB, a2), note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
     {
         Phase phf("tc_finalize_exact", st);
-        k_tc_finalize<<<unsigned((n + 255) / 256), 256, 0, st>>>(X, n, d, C, k, asn, s.cnt.p, s.cand.p, costs,
-                                                                 s.nrecheck.p, s.over_rows.p, s.nrecheck.p + 1),
-            note_launch();
+        const bool vec4 = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(C) & 15) == 0) &&
+                          ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
+        const size_t cs_bytes = size_t(FIN_SG) * 8 * d * sizeof(float);
+        const int stage = cs_bytes <= 48 * 1024 ? 1 : 0;
+        const size_t dyn = stage ? cs_bytes : 0;
+        const unsigned fg = unsigned((n + FIN_ROWS - 1) / FIN_ROWS);
+        // static (37 KB) + staged centers (up to 48 KB) exceeds the 48 KB default; always the
+        // largest value, so concurrent callers never lower it under another's launch
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_finalize<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024));
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_tc_finalize<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024));
+        if (vec4)
+            k_tc_finalize<true><<<fg, FIN_ROWS, dyn, st>>>(X, n, d, C, k, nsg, stage, asn, s.sort.perm.p, s.status.p,
+                                                           s.cnt.p, s.cand.p, costs, s.over_rows.p, s.nrecheck.p + 1),
+                note_launch();
+        else
+            k_tc_finalize<false><<<fg, FIN_ROWS, dyn, st>>>(X, n, d, C, k, nsg, stage, asn, s.sort.perm.p,
+                                                            s.status.p, s.cnt.p, s.cand.p, costs, s.over_rows.p,
+                                                            s.nrecheck.p + 1), note_launch();
     }
     MC_CUDA_TRY(cudaGetLastError());
     int err = 0;
@@ -711,7 +986,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     MC_CUDA_TRY(cudaStreamSynchronize(st));
     if (err) return fail(MC_ETIMEOUT, "tensor-core assignment: bounded wait expired (code " + std::to_string(err) + ")");
     if (nr[1]) {
-        // rows with more candidates than the epilogue keeps: exact FP32 scan over all centers
+        // rows without a usable candidate list: exact FP32 scan over all centers
         AssignArgs b;
         b.msr = SQRL2;
         b.n = nr[1];

@@ -3,6 +3,7 @@
 // an exact FP32 re-check of the rows whose margin falls below the rounding bound.
 #pragma once
 #include "mc_internal.cuh"
+#include "mc_reduce.cuh"
 
 namespace mc {
 
@@ -12,11 +13,19 @@ struct TcState {
     DBuf<__nv_bfloat16> Cb;      // [kp][dp]
     DBuf<float> Ct;              // [kp][dp]
     DBuf<float> cnorm_p;         // device scalar: max center norm
-    DBuf<float> b1;              // [n][2] per-row minima of the tensor-core values (pass 1)
-    DBuf<uint8_t> cnt;           // [n][2] candidates per column half (255: too many)
-    DBuf<uint32_t> cand;         // [n][2][4] candidate centers
+    DBuf<float> b1, b2;          // [n][4] pass 1 top-2 subgroup minima per row and column part
+    DBuf<uint32_t> j1;           // [n][4] subgroup of b1
+    DBuf<uint32_t> status;       // [n] candidate subgroup / multi slot / rescan
+    DBuf<uint32_t> key;          // [n] finalize order key (subgroup, multi, rescan)
+    SortWork sort;               // rows sorted by key
+    DBuf<uint32_t> crow;         // [cap] original row of each compact (multi) row
+    DBuf<float> thrc;            // [cap] pass 2 threshold of each compact row
+    DBuf<uint4> Xc;              // [cap][pitch] operand copy of the compact rows
+    DBuf<unsigned> count;        // compact rows taken
+    DBuf<uint8_t> cnt;           // [cap][4] pass 2 candidates per column part (255: too many)
+    DBuf<uint32_t> cand;         // [cap][4][3] pass 2 candidate centers
     DBuf<int> err;               // bounded-wait error code
-    DBuf<unsigned long long> nrecheck;   // [0] rows re-checked among candidates, [1] rows rescanned
+    DBuf<unsigned long long> nrecheck;   // [0] multi rows (pass 2), [1] rows rescanned
     DBuf<uint32_t> over_rows;    // rows rescanned over all centers
     DBuf<float> CT0;             // transposed centers for that rescan
     const float *X_src = nullptr;
