@@ -212,48 +212,72 @@ int launch_row_sums_csr(const float *vals, const uint64_t *indptr, uint64_t n, d
 // ------------------------------------------------------------------------------------
 // Stable counting sort of rows by cluster id.
 // keys[i] in [0,k); optional keys2[i] (second membership, 0xffffffff = none).
-// Tiles of kSortTile rows; per-tile counts -> per (key, tile) offsets -> one warp per tile
-// scatters its rows in order (match_any ranks), so each bucket lists rows ascending.
+// Tiles of kSortTile rows; per-tile counts (key-major: tile_counts[key][tile]) -> per
+// (key, tile) offsets by a parallel scan per key -> one warp per tile scatters its rows in
+// order (match_any ranks), so each bucket lists rows ascending.
 // ------------------------------------------------------------------------------------
 // per-tile counts; a shared-memory histogram when k is small enough
 constexpr uint32_t kSmemKeys = 8192;
 
 __global__ void k_sort_count(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ keys2, uint64_t n,
-                             uint32_t k, uint32_t *tile_counts /* [ntiles][k] */) {
+                             uint32_t k, uint64_t ntiles, uint32_t *tile_counts /* [k][ntiles] */) {
     __shared__ uint32_t hist[kSmemKeys];
     const uint64_t tile = blockIdx.x;
     const uint64_t b = tile * kSortTile, e = umin64(n, b + kSortTile);
-    uint32_t *tc = tile_counts + tile * uint64_t(k);
     const bool sm = k <= kSmemKeys;
     if (sm) {
         for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) hist[j] = 0;
         __syncthreads();
     }
-    uint32_t *h = sm ? hist : tc;
     for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        atomicAdd(&h[keys[i]], 1u);
+        const uint32_t k1 = keys[i];
+        if (sm) atomicAdd(&hist[k1], 1u);
+        else atomicAdd(&tile_counts[uint64_t(k1) * ntiles + tile], 1u);
         if (keys2) {
             const uint32_t k2 = keys2[i];
-            if (k2 != 0xffffffffu) atomicAdd(&h[k2], 1u);
+            if (k2 != 0xffffffffu) {
+                if (sm) atomicAdd(&hist[k2], 1u);
+                else atomicAdd(&tile_counts[uint64_t(k2) * ntiles + tile], 1u);
+            }
         }
     }
     if (sm) {
         __syncthreads();
-        for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) tc[j] = hist[j];
+        for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) tile_counts[uint64_t(j) * ntiles + tile] = hist[j];
     }
 }
 
-// per key: sequential over tiles -> tile offsets (relative to the bucket start) and totals
-__global__ void k_sort_key_scan(uint32_t *tile_counts, uint64_t ntiles, uint32_t k, uint64_t *bucket_count) {
-    const uint32_t key = blockIdx.x * blockDim.x + threadIdx.x;
+// one CTA per key: exclusive scan of the key's tile counts (in place: per-tile offsets
+// relative to the bucket start) and the bucket total
+__global__ void __launch_bounds__(256) k_sort_key_scan(uint32_t *tile_counts, uint64_t ntiles, uint32_t k,
+                                                       uint64_t *bucket_count) {
+    __shared__ uint64_t wsum[8];
+    const uint32_t key = blockIdx.x;
     if (key >= k) return;
-    uint64_t acc = 0;
-    for (uint64_t t = 0; t < ntiles; ++t) {
-        const uint32_t c = tile_counts[t * k + key];
-        tile_counts[t * k + key] = uint32_t(acc);
+    uint32_t *row = tile_counts + uint64_t(key) * ntiles;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const uint64_t per = (ntiles + 255) / 256;
+    const uint64_t b = uint64_t(t) * per, e = umin64(ntiles, b + per);
+    uint64_t s = 0;
+    for (uint64_t i = b; i < e; ++i) s += row[i];
+    // exclusive scan of the 256 thread sums
+    uint64_t incl = s;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint64_t v = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += v;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    uint64_t wbase = 0;
+    for (int i = 0; i < w; ++i) wbase += wsum[i];
+    uint64_t acc = wbase + incl - s;
+    for (uint64_t i = b; i < e; ++i) {
+        const uint32_t c = row[i];
+        row[i] = uint32_t(acc);
         acc += c;
     }
-    bucket_count[key] = acc;
+    if (t == 255) bucket_count[key] = acc;
 }
 
 // exclusive scan of bucket counts (single CTA, sequential per thread chunk + smem)
@@ -284,24 +308,24 @@ __global__ void k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t
     }
 }
 
-__global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, uint32_t k, uint32_t *tile_offsets,
-                               const uint64_t *__restrict__ bucket_start, uint32_t *perm) {
+__global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, uint32_t k, uint64_t ntiles,
+                               uint32_t *tile_offsets, const uint64_t *__restrict__ bucket_start, uint32_t *perm) {
     // one warp per tile; rows in order, 32 at a time; ranks from match_any.  Cursors live in
-    // shared memory when k is small enough (one warp per block), else in the tile's row of
-    // tile_offsets.
+    // shared memory when k is small enough (one warp per block), else in the tile's column
+    // of tile_offsets (stride ntiles).
     __shared__ uint32_t scur[kSmemKeys];
     const uint64_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31;
     const uint64_t b = tile * kSortTile;
     if (b >= n) return;
     const uint64_t e = umin64(n, b + kSortTile);
-    uint32_t *gcur = tile_offsets + tile * uint64_t(k);
     const bool sm = k <= kSmemKeys;
     if (sm) {
-        for (uint32_t j = lane; j < k; j += 32) scur[j] = gcur[j];
+        for (uint32_t j = lane; j < k; j += 32) scur[j] = tile_offsets[uint64_t(j) * ntiles + tile];
         __syncwarp();
     }
-    uint32_t *cur = sm ? scur : gcur;
+    uint32_t *cur = sm ? scur : tile_offsets + tile;
+    const uint64_t cstride = sm ? 1 : ntiles;
     const unsigned lt = (1u << lane) - 1u;
     for (uint64_t base = b; base < e; base += 32) {
         const uint64_t i = base + lane;
@@ -310,11 +334,11 @@ __global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, ui
         const unsigned actmask = __ballot_sync(0xffffffffu, act);
         const unsigned peers = __match_any_sync(0xffffffffu, key) & actmask;
         uint32_t off = 0;
-        if (act) off = cur[key];
+        if (act) off = cur[uint64_t(key) * cstride];
         __syncwarp();
         if (act) {
             perm[bucket_start[key] + off + __popc(peers & lt)] = uint32_t(i);
-            if ((peers & lt) == 0) cur[key] = off + __popc(peers);
+            if ((peers & lt) == 0) cur[uint64_t(key) * cstride] = off + __popc(peers);
         }
         __syncwarp();
     }
@@ -323,17 +347,17 @@ __global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, ui
 // Rare path (rows with a second membership after an empty-cluster restart): one thread
 // per tile walks its rows in order so that every bucket stays ascending.
 __global__ void k_sort_scatter2(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ keys2, uint64_t n,
-                                uint32_t k, uint32_t *tile_offsets, const uint64_t *__restrict__ bucket_start,
-                                uint32_t *perm) {
+                                uint32_t k, uint64_t ntiles, uint32_t *tile_offsets,
+                                const uint64_t *__restrict__ bucket_start, uint32_t *perm) {
     const uint64_t tile = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
     const uint64_t b = tile * kSortTile;
     if (b >= n) return;
     const uint64_t e = umin64(n, b + kSortTile);
-    uint32_t *cur = tile_offsets + tile * uint64_t(k);
+    uint32_t *cur = tile_offsets + tile;
     for (uint64_t i = b; i < e; ++i) {
         const uint32_t k1 = keys[i], k2 = keys2[i];
-        perm[bucket_start[k1] + cur[k1]++] = uint32_t(i);
-        if (k2 != 0xffffffffu) perm[bucket_start[k2] + cur[k2]++] = uint32_t(i);
+        perm[bucket_start[k1] + cur[uint64_t(k1) * ntiles]++] = uint32_t(i);
+        if (k2 != 0xffffffffu) perm[bucket_start[k2] + cur[uint64_t(k2) * ntiles]++] = uint32_t(i);
     }
 }
 
@@ -350,17 +374,21 @@ int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, 
     MC_TRY(w.bucket_count.alloc(k, st));
     MC_TRY(w.bucket_start.alloc(uint64_t(k) + 1, st));
     MC_TRY(w.perm.alloc(keys2 ? 2 * n : n, st));
-    MC_CUDA_TRY(cudaMemsetAsync(w.tile_counts.p, 0, ntiles * k * sizeof(uint32_t), st));
-    if (ntiles) k_sort_count<<<unsigned(ntiles), 256, 0, st>>>(keys, keys2, n, k, w.tile_counts.p), note_launch();
-    k_sort_key_scan<<<(k + 127) / 128, 128, 0, st>>>(w.tile_counts.p, ntiles, k, w.bucket_count.p), note_launch();
+    if (k > kSmemKeys) MC_CUDA_TRY(cudaMemsetAsync(w.tile_counts.p, 0, ntiles * k * sizeof(uint32_t), st));
+    if (ntiles)
+        k_sort_count<<<unsigned(ntiles), 256, 0, st>>>(keys, keys2, n, k, ntiles, w.tile_counts.p), note_launch();
+    else
+        MC_CUDA_TRY(cudaMemsetAsync(w.bucket_count.p, 0, k * sizeof(uint64_t), st));
+    if (ntiles) k_sort_key_scan<<<k, 256, 0, st>>>(w.tile_counts.p, ntiles, k, w.bucket_count.p), note_launch();
     k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.bucket_count.p, w.bucket_start.p, k), note_launch();
     if (ntiles) {
         if (!keys2)
-            k_sort_scatter<<<unsigned(ntiles), 32, 0, st>>>(keys, n, k, w.tile_counts.p, w.bucket_start.p,
+            k_sort_scatter<<<unsigned(ntiles), 32, 0, st>>>(keys, n, k, ntiles, w.tile_counts.p, w.bucket_start.p,
                                                             w.perm.p), note_launch();
         else
-            k_sort_scatter2<<<unsigned((ntiles + 63) / 64), 64, 0, st>>>(keys, keys2, n, k, w.tile_counts.p,
-                                                                         w.bucket_start.p, w.perm.p), note_launch();
+            k_sort_scatter2<<<unsigned((ntiles + 63) / 64), 64, 0, st>>>(keys, keys2, n, k, ntiles,
+                                                                         w.tile_counts.p, w.bucket_start.p,
+                                                                         w.perm.p), note_launch();
     }
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;

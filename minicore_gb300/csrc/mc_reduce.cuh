@@ -4,10 +4,10 @@
 
 namespace mc {
 
-constexpr uint64_t kSortTile = 8192;
+constexpr uint64_t kSortTile = 2048;
 
 struct SortWork {
-    DBuf<uint32_t> tile_counts;   // [ntiles][k] counts, then per-tile cursors
+    DBuf<uint32_t> tile_counts;   // [k][ntiles] counts, then per-tile cursors
     DBuf<uint64_t> bucket_count;  // [k]
     DBuf<uint64_t> bucket_start;  // [k+1]
     DBuf<uint32_t> perm;          // rows grouped by bucket, ascending within a bucket
