@@ -422,39 +422,62 @@ __device__ inline void two_sum_add(float &s, float &e, float x) {
     e = __fadd_rn(e, err);
 }
 
-// dense: one CTA per chunk, threads over columns, rows sequential
-__global__ void k_centroid_chunks_dense(const float *__restrict__ X, uint64_t d, const uint32_t *__restrict__ perm,
-                                        const uint64_t *__restrict__ bucket_start,
-                                        const uint64_t *__restrict__ bucket_count,
-                                        const uint64_t *__restrict__ chunk_start, uint32_t k, uint64_t ch,
-                                        const double *__restrict__ w, double *partial /* [chunk][d] */,
-                                        double *partial_w /* [chunk] */) {
+// dense: one CTA per chunk (at most kDenseChunk rows of one cluster), threads over
+// columns, rows sequential.  The chunk's row ids are staged in shared memory and each
+// thread loads 8 rows' values ahead of its sequential sum, so the loads overlap.
+constexpr uint64_t kDenseChunk = 256;
+
+__global__ void __launch_bounds__(128) k_centroid_chunks_dense(const float *__restrict__ X, uint64_t d,
+                                                               const uint32_t *__restrict__ perm,
+                                                               const uint64_t *__restrict__ bucket_start,
+                                                               const uint64_t *__restrict__ bucket_count,
+                                                               const uint64_t *__restrict__ chunk_start, uint32_t k,
+                                                               uint64_t ch, const double *__restrict__ w,
+                                                               double *partial /* [chunk][d] */,
+                                                               double *partial_w /* [chunk] */) {
+    __shared__ uint32_t srows[kDenseChunk];
+    __shared__ double sw[kDenseChunk];
     const uint64_t q = blockIdx.x;
     if (q >= chunk_start[k]) return;
     const uint32_t c = find_bucket(chunk_start, k, q);
     const uint64_t local = q - chunk_start[c];
     const uint64_t r0 = local * ch, r1 = umin64(bucket_count[c], r0 + ch);
-    const uint32_t *rows = perm + bucket_start[c];
+    const int cnt = int(r1 - r0);
+    const uint32_t *rows = perm + bucket_start[c] + r0;
+    for (int r = threadIdx.x; r < cnt; r += blockDim.x) {
+        srows[r] = rows[r];
+        if (w) sw[r] = w[rows[r]];
+    }
+    __syncthreads();
+    constexpr int U = 8;
     for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) {
         if (w) {
             double acc = 0.0;
-            for (uint64_t r = r0; r < r1; ++r) {
-                const uint32_t row = rows[r];
-                acc = fma(w[row], double(X[uint64_t(row) * d + j]), acc);
+            for (int r = 0; r < cnt; r += U) {
+                float xv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) xv[u] = (r + u < cnt) ? X[uint64_t(srows[r + u]) * d + j] : 0.f;
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (r + u < cnt) acc = fma(sw[r + u], double(xv[u]), acc);
             }
             partial[q * d + j] = acc;
         } else {
             float s = 0.f, e = 0.f;
-            for (uint64_t r = r0; r < r1; ++r) {
-                const uint32_t row = rows[r];
-                two_sum_add(s, e, X[uint64_t(row) * d + j]);
+            for (int r = 0; r < cnt; r += U) {
+                float xv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) xv[u] = (r + u < cnt) ? X[uint64_t(srows[r + u]) * d + j] : 0.f;
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (r + u < cnt) two_sum_add(s, e, xv[u]);
             }
             partial[q * d + j] = double(s) + double(e);
         }
     }
     if (w && threadIdx.x == 0) {
         double wq = 0.0;
-        for (uint64_t r = r0; r < r1; ++r) wq = wq + w[rows[r]];
+        for (int r = 0; r < cnt; ++r) wq = wq + sw[r];
         partial_w[q] = wq;
     }
 }
@@ -569,7 +592,7 @@ __global__ void k_centroid_singletons_csr(const float *__restrict__ vals, const 
 int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool presorted) {
     const uint64_t n = a.n, d = a.d;
     const uint32_t k = a.k;
-    const uint64_t ch = a.csr ? 4096 : 256;
+    const uint64_t ch = a.csr ? 4096 : kDenseChunk;
     if (!presorted) MC_TRY(launch_sort_by_key(a.keys, a.keys2, n, k, w, st));
     MC_TRY(w.chunk_count.alloc(k, st));
     MC_TRY(w.chunk_start.alloc(uint64_t(k) + 1, st));

@@ -677,11 +677,19 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
     // staged centers: subgroups sg_first .. sg_first + FIN_SG - 1
     const uint32_t sgf = sg_first;
     if (sgf != 0xffffffffu) {
-        const uint64_t tot = uint64_t(FIN_SG) * 8 * d;
-        for (uint64_t e = t; e < tot; e += R) {
-            const uint64_t jl = e / d, col = e % d;
-            const uint64_t j = uint64_t(sgf) * 8 + jl;
-            cs[e] = (j < k) ? C[j * d + col] : 0.f;
+        // the staged centers are contiguous rows of C: copy them as one run (zeros past k)
+        const uint64_t j0 = uint64_t(sgf) * 8;
+        const uint64_t jend = umin64(j0 + uint64_t(FIN_SG) * 8, k);
+        const uint32_t valid = uint32_t((jend > j0 ? jend - j0 : 0) * d);
+        const uint32_t tot = uint32_t(FIN_SG * 8 * d);
+        const float *src = C + j0 * d;
+        if (VEC4) {
+            const float4 *s4 = reinterpret_cast<const float4 *>(src);
+            float4 *d4 = reinterpret_cast<float4 *>(cs);
+            for (uint32_t e = t; e < tot / 4; e += R)
+                d4[e] = 4 * e < valid ? __ldg(s4 + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            for (uint32_t e = t; e < tot; e += R) cs[e] = e < valid ? src[e] : 0.f;
         }
     }
     const bool mine_local = sgf != 0xffffffffu && st != ST_OVER && !(st & ST_MULTI) && !over && st - sgf < FIN_SG;
@@ -731,9 +739,24 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
                 }
                 if (warp_local) {
                     if (mine_local) {
+                        // all 8 subgroup centers at once (padding centers are zeros and are
+                        // ignored below): 8 independent sequential chains per thread
+                        const float *cb = lbase + k0;
 #pragma unroll
-                        for (int q = 0; q < 8; ++q)
-                            if (cj[q] != 0xffffffffu) fin_chunk32(lbase + uint64_t(q) * d + k0, xr, acc[q]);
+                        for (int k4 = 0; k4 < 8; ++k4) {
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
+                                const float4 c = *reinterpret_cast<const float4 *>(cb + uint64_t(q) * d + 4 * k4);
+                                float df = c.x - xr[4 * k4 + 0];
+                                acc[q] = fmaf(df, df, acc[q]);
+                                df = c.y - xr[4 * k4 + 1];
+                                acc[q] = fmaf(df, df, acc[q]);
+                                df = c.z - xr[4 * k4 + 2];
+                                acc[q] = fmaf(df, df, acc[q]);
+                                df = c.w - xr[4 * k4 + 3];
+                                acc[q] = fmaf(df, df, acc[q]);
+                            }
+                        }
                     }
                 } else {
 #pragma unroll
