@@ -82,43 +82,67 @@ __global__ void k_kmpp_scatter(const KmppArgs a) {
 
 __global__ void k_kmpp_zero(const KmppArgs a) { a.dist[*a.newc] = 0.0; }
 
-// dense rows: a CTA stages 128 rows x 32 columns in shared memory; each thread reduces its
-// row sequentially over the columns (the oracle's order).
-template <int MSR>
-__global__ void __launch_bounds__(128) k_kmpp_dense(const KmppArgs a, int first) {
-    __shared__ float tile[128][33];
-    __shared__ float cs[32];
+// dense rows: one thread per row; the row and the new center are read with float4 loads
+// in 32-column chunks (16 loads in flight per thread), the reduction stays sequential over
+// the columns (the oracle's order).  Rounds after the first also record the center
+// (center_ids, asn) and zero its distance, so no separate launches are needed.
+template <int MSR, bool VEC4>
+__global__ void __launch_bounds__(256) k_kmpp_dense(const KmppArgs a, int first) {
     const uint64_t c = *a.newc;
-    const uint64_t row0 = uint64_t(blockIdx.x) * 128;
-    const uint64_t i = row0 + threadIdx.x;
-    const double csum = a.rowsum[c];
-    PairScalars s = {};
-    if (i < a.n && MSR != SQRL2) s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], csum, a.d);
-    float acc = 0.f;
-    for (uint64_t k0 = 0; k0 < a.d; k0 += 32) {
-        const int kmax = int(umin64(32, a.d - k0));
-        for (int e = threadIdx.x; e < 128 * 32; e += 128) {
-            const int r = e >> 5, kk = e & 31;
-            const uint64_t row = row0 + r;
-            tile[r][kk] = (row < a.n && kk < kmax) ? a.X[row * a.d + k0 + kk] : 0.f;
-        }
-        if (threadIdx.x < 32) cs[threadIdx.x] = threadIdx.x < kmax ? a.cbuf[k0 + threadIdx.x] : 0.f;
-        __syncthreads();
-        for (int kk = 0; kk < kmax; ++kk) kp_elem<MSR>(acc, cs[kk], tile[threadIdx.x][kk], s);
-        __syncthreads();
+    if (!first && blockIdx.x == 0 && threadIdx.x == 0) {
+        a.center_ids[a.round] = uint32_t(c);
+        a.asn[c] = a.round;
     }
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
     if (i >= a.n) return;
+    double cur = 0.0;
+    if (!first) {
+        if (i == c) {
+            a.dist[i] = 0.0;
+            return;
+        }
+        cur = a.dist[i];
+        if (cur <= 0.0) return;
+    }
+    PairScalars s = {};
+    if (MSR != SQRL2) s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], a.rowsum[c], a.d);
+    const float *xr = a.X + i * a.d, *cr = a.X + c * a.d;
+    float acc = 0.f;
+    if (VEC4) {
+        const float4 *x4 = reinterpret_cast<const float4 *>(xr), *c4 = reinterpret_cast<const float4 *>(cr);
+        const uint64_t d4 = a.d / 4;
+        uint64_t q = 0;
+        for (; q + 8 <= d4; q += 8) {
+            float4 xv[8], cv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                xv[u] = __ldg(x4 + q + u);
+                cv[u] = __ldg(c4 + q + u);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                kp_elem<MSR>(acc, cv[u].x, xv[u].x, s);
+                kp_elem<MSR>(acc, cv[u].y, xv[u].y, s);
+                kp_elem<MSR>(acc, cv[u].z, xv[u].z, s);
+                kp_elem<MSR>(acc, cv[u].w, xv[u].w, s);
+            }
+        }
+        for (; q < d4; ++q) {
+            const float4 xv = __ldg(x4 + q), cv = __ldg(c4 + q);
+            kp_elem<MSR>(acc, cv.x, xv.x, s);
+            kp_elem<MSR>(acc, cv.y, xv.y, s);
+            kp_elem<MSR>(acc, cv.z, xv.z, s);
+            kp_elem<MSR>(acc, cv.w, xv.w, s);
+        }
+    } else {
+        for (uint64_t j = 0; j < a.d; ++j) kp_elem<MSR>(acc, __ldg(cr + j), __ldg(xr + j), s);
+    }
     const double v = kp_cost<MSR>(acc);
     if (first) {
         a.dist[i] = (i == c) ? 0.0 : v;
-    } else {
-        if (i == c) return;
-        const double cur = a.dist[i];
-        if (cur <= 0.0) return;
-        if (v < cur) {
-            a.dist[i] = v;
-            a.asn[i] = a.round;
-        }
+    } else if (v < cur) {
+        a.dist[i] = v;
+        a.asn[i] = a.round;
     }
 }
 
@@ -159,12 +183,99 @@ __global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, u
     }
 }
 
+__device__ __forceinline__ void kp_cp_async16(void *dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(uint32_t(__cvta_generic_to_shared(dst))),
+                 "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+
+// dense rows with d % 4 == 0 and 16-byte aligned rows: a CTA of 128 threads (one row each)
+// stages 32-column chunks of its 128 rows and of the new center in shared memory with
+// cp.async (coalesced, double-buffered); each thread then reduces its row sequentially over
+// the columns.  Same per-row arithmetic and bookkeeping as k_kmpp_dense.
+template <int MSR>
+__global__ void __launch_bounds__(128) k_kmpp_dense_staged(const KmppArgs a, int first) {
+    __shared__ __align__(16) float xs[2][128][36];
+    __shared__ __align__(16) float cs[2][32];
+    const uint64_t c = *a.newc;
+    if (!first && blockIdx.x == 0 && threadIdx.x == 0) {
+        a.center_ids[a.round] = uint32_t(c);
+        a.asn[c] = a.round;
+    }
+    const int t = threadIdx.x;
+    const uint64_t row0 = uint64_t(blockIdx.x) * 128;
+    const uint64_t i = row0 + t;
+    bool active = i < a.n;
+    double cur = 0.0;
+    if (active && !first) {
+        if (i == c) {
+            a.dist[i] = 0.0;
+            active = false;
+        } else {
+            cur = a.dist[i];
+            if (cur <= 0.0) active = false;
+        }
+    }
+    PairScalars s = {};
+    if (active && MSR != SQRL2) s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], a.rowsum[c], a.d);
+    const uint64_t d = a.d;
+    const uint64_t nchunk = (d + 31) / 32;
+    auto stage = [&](uint64_t ci, int buf) {
+        const uint64_t k0 = ci * 32;
+        const int kmax = int(umin64(32, d - k0));
+        for (int e = t; e < 128 * 8; e += 128) {
+            const int r = e >> 3, q4 = e & 7;
+            const bool ok = row0 + r < a.n && 4 * q4 < kmax;
+            kp_cp_async16(&xs[buf][r][4 * q4], ok ? a.X + (row0 + r) * d + k0 + 4 * q4 : a.X, ok ? 16 : 0);
+        }
+        if (t < 8) {
+            const bool ok = 4 * t < kmax;
+            kp_cp_async16(&cs[buf][4 * t], ok ? a.X + c * d + k0 + 4 * t : a.X, ok ? 16 : 0);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    float acc = 0.f;
+    stage(0, 0);
+    for (uint64_t ci = 0; ci < nchunk; ++ci) {
+        const int buf = int(ci & 1);
+        if (ci + 1 < nchunk) {
+            stage(ci + 1, buf ^ 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        const int kmax = int(umin64(32, d - ci * 32));
+        if (active) {
+            if (kmax == 32) {
+#pragma unroll
+                for (int kk = 0; kk < 32; ++kk) kp_elem<MSR>(acc, cs[buf][kk], xs[buf][t][kk], s);
+            } else {
+                for (int kk = 0; kk < kmax; ++kk) kp_elem<MSR>(acc, cs[buf][kk], xs[buf][t][kk], s);
+            }
+        }
+        __syncthreads();  // buffer buf is restaged two chunks later
+    }
+    if (!active) return;
+    const double v = kp_cost<MSR>(acc);
+    if (first) {
+        a.dist[i] = (i == c) ? 0.0 : v;
+    } else if (v < cur) {
+        a.dist[i] = v;
+        a.asn[i] = a.round;
+    }
+}
+
 template <int MSR>
 static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaStream_t st) {
     if (!a.csr) {
         KmppArgs b = a;
         b.round = round;
-        k_kmpp_dense<MSR><<<unsigned((a.n + 127) / 128), 128, 0, st>>>(b, first), note_launch();
+        const bool vec4 = a.d % 4 == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
+        if (vec4)
+            k_kmpp_dense_staged<MSR><<<unsigned((a.n + 127) / 128), 128, 0, st>>>(b, first), note_launch();
+        else
+            k_kmpp_dense<MSR, false><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
     } else {
         const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
         k_kmpp_csr<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();
@@ -189,16 +300,21 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     const unsigned tb = 256, tg = unsigned(umin64((a.d + tb - 1) / tb, 1024));
     MC_CUDA_TRY(cudaMemsetAsync(a.asn, 0, a.n * sizeof(uint32_t), st));
     k_kmpp_first<<<1, 1, 0, st>>>(u_dev, a.n, a.newc, a.center_ids), note_launch();
-    k_kmpp_take<<<tg, tb, 0, st>>>(a, 0), note_launch();
-    if (a.csr) k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
+    if (a.csr) {
+        k_kmpp_take<<<tg, tb, 0, st>>>(a, 0), note_launch();
+        k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
+    }
     MC_TRY(update(a, 1, 0, sms, st));
     DetInput in{a.w ? DET_F64_W : DET_F64, a.dist, nullptr, a.w, a.n};
     for (uint32_t ci = 1; ci < a.k; ++ci) {
         MC_TRY(launch_det_draw(in, chunk_tmp, u_dev + ci, 0.0, 1, a.dist, a.newc, st));
-        k_kmpp_take<<<tg, tb, 0, st>>>(a, ci), note_launch();
-        if (a.csr) k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
+        if (a.csr) {
+            // CSR centers are densified into cbuf; the dense update reads the center row itself
+            k_kmpp_take<<<tg, tb, 0, st>>>(a, ci), note_launch();
+            k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
+        }
         MC_TRY(update(a, 0, ci, sms, st));
-        k_kmpp_zero<<<1, 1, 0, st>>>(a), note_launch();
+        if (a.csr) k_kmpp_zero<<<1, 1, 0, st>>>(a), note_launch();
     }
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;

@@ -69,21 +69,33 @@ int launch_det_sum(const DetInput &in, double *chunk_tmp, double *out, cudaStrea
 // ------------------------------------------------------------------------------------
 // det draw: chunk totals (k_det_chunks), then a single CTA walks the canonical order.
 // If the total is not positive, the first maximum of fallback_vals (or index 0) is taken,
-// as kmeanspp's argmax fallback does (kmeans.h:179-186).
+// as kmeanspp's argmax fallback does (kmeans.h:179-186).  The sequential FP64 walks read
+// from shared memory: the chunk totals (up to kDrawSmemChunks of them), the selected
+// chunk's 256 thread partials and the selected thread's 32 elements are staged by all
+// threads first.
 // ------------------------------------------------------------------------------------
+constexpr uint64_t kDrawSmemChunks = 4096;
+
 __global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, const double *chunk_tot, const double *u_dev,
                                                           double u_host, int use_dev_u, const double *fallback_vals,
                                                           uint64_t *out_idx) {
     __shared__ double sm_warp[kDetThreads / 32];
     __shared__ double sm_part[kDetThreads];
+    __shared__ double sm_chunk[kDrawSmemChunks];
+    __shared__ double sm_elem[kDetPer];
     __shared__ int64_t sm_sel;
     __shared__ double sm_r;
-    __shared__ int sm_clamp;
+    __shared__ int sm_clamp, sm_tau;
     const int t = threadIdx.x;
     const uint64_t G = det_chunks(in.n);
+    const bool staged = G <= kDrawSmemChunks;
+    if (staged)
+        for (uint64_t g = t; g < G; g += kDetThreads) sm_chunk[g] = chunk_tot[g];
+    __syncthreads();
+    const double *ct = staged ? sm_chunk : chunk_tot;
     if (t == 0) {
         double S = 0.0;
-        for (uint64_t g = 0; g < G; ++g) S = S + chunk_tot[g];
+        for (uint64_t g = 0; g < G; ++g) S = S + ct[g];
         int64_t gs = -1;
         int clamp = 0;
         double C = 0.0, tt = 0.0;
@@ -91,12 +103,12 @@ __global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, const dou
             const double u = use_dev_u ? *u_dev : u_host;
             tt = u * S;
             for (uint64_t g = 0; g < G; ++g) {
-                if (C + chunk_tot[g] > tt) { gs = int64_t(g); break; }
-                C = C + chunk_tot[g];
+                if (C + ct[g] > tt) { gs = int64_t(g); break; }
+                C = C + ct[g];
             }
             if (gs < 0) {
                 for (int64_t g = int64_t(G) - 1; g >= 0; --g)
-                    if (chunk_tot[g] > 0.0) { gs = g; break; }
+                    if (ct[g] > 0.0) { gs = g; break; }
                 clamp = 1;
             }
         }
@@ -119,16 +131,8 @@ __global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, const dou
     }
     (void)det_chunk_total(in, uint64_t(gs), sm_warp, sm_part);
     __syncthreads();
+    const uint64_t base = uint64_t(gs) * kDetChunk;
     if (t == 0) {
-        const uint64_t base = uint64_t(gs) * kDetChunk;
-        auto last_pos_in_thread = [&](int th) -> uint64_t {
-            uint64_t best = in.n;
-            for (int m = 0; m < kDetPer; ++m) {
-                const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * m;
-                if (i < in.n && in.get(i) > 0.0) best = i;
-            }
-            return best;
-        };
         const double r = sm_r;
         int tau = -1;
         double Q = 0.0;
@@ -138,20 +142,46 @@ __global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, const dou
                 Q = Q + sm_part[th];
             }
         }
-        uint64_t res = in.n;
         if (tau < 0) {
+            // past the end (rounding) or clamped: the last thread with a positive partial
             for (int th = kDetThreads - 1; th >= 0; --th)
-                if (sm_part[th] > 0.0) { res = last_pos_in_thread(th); break; }
+                if (sm_part[th] > 0.0) { tau = -2 - th; break; }
+        }
+        sm_tau = tau;
+        sm_r = r - Q;
+    }
+    __syncthreads();
+    const int tau_code = sm_tau;
+    const int th = tau_code >= 0 ? tau_code : (tau_code <= -2 ? -2 - tau_code : -1);
+    if (th >= 0 && t < kDetPer) {
+        const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * t;
+        sm_elem[t] = i < in.n ? in.get(i) : 0.0;
+    }
+    __syncthreads();
+    if (t == 0) {
+        auto last_pos = [&]() -> uint64_t {
+            uint64_t best = in.n;
+            for (int m = 0; m < kDetPer; ++m) {
+                const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * m;
+                if (i < in.n && sm_elem[m] > 0.0) best = i;
+            }
+            return best;
+        };
+        uint64_t res = in.n;
+        if (th < 0) {
+            res = in.n;
+        } else if (tau_code < 0) {
+            res = last_pos();
         } else {
-            const double r2 = r - Q;
+            const double r2 = sm_r;
             double R = 0.0;
             for (int m = 0; m < kDetPer; ++m) {
-                const uint64_t i = base + uint64_t(tau) + uint64_t(kDetThreads) * m;
-                const double val = i < in.n ? in.get(i) : 0.0;
+                const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * m;
+                const double val = sm_elem[m];
                 if (R + val > r2) { res = i; break; }
                 R = R + val;
             }
-            if (res == in.n) res = last_pos_in_thread(tau);
+            if (res == in.n) res = last_pos();
         }
         if (res >= in.n) res = 0;
         *out_idx = res;
