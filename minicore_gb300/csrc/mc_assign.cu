@@ -399,9 +399,47 @@ __global__ void __launch_bounds__(256) k_assign_tiled(AssignArgs a) {
 // sparse-dot CSR kernel (constant prior; SQRL2, L1, MKL, HELLINGER)
 // one warp per row; lane l owns centers l, l+32, ... of the current group of 32*KPL
 // ------------------------------------------------------------------------------------
+template <int KPL>
+struct CenterVec;
+template <>
+struct CenterVec<1> {
+    float v[1];
+    __device__ __forceinline__ void load(const float *p) { v[0] = __ldg(p); }
+    __device__ __forceinline__ void zero() { v[0] = 0.f; }
+};
+template <>
+struct CenterVec<2> {
+    float v[2];
+    __device__ __forceinline__ void load(const float *p) {
+        const float2 t = __ldg(reinterpret_cast<const float2 *>(p));
+        v[0] = t.x;
+        v[1] = t.y;
+    }
+    __device__ __forceinline__ void zero() { v[0] = v[1] = 0.f; }
+};
+template <>
+struct CenterVec<4> {
+    float v[4];
+    __device__ __forceinline__ void load(const float *p) {
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+        v[0] = t.x;
+        v[1] = t.y;
+        v[2] = t.z;
+        v[3] = t.w;
+    }
+    __device__ __forceinline__ void zero() { v[0] = v[1] = v[2] = v[3] = 0.f; }
+};
+
+// Lane l owns centers g0 + KPL*l .. + KPL-1 of the current group of 32*KPL (one vector load
+// per nonzero; lanes past the padded centers idle).  Each
+// chunk of 32 nonzeros is staged per warp in shared memory as (column, g) and read back by
+// broadcast; SB nonzeros per batch have their center loads issued before the first use.
+// The per-(row, center) sum stays sequential over the nonzeros.
 template <int MSR, int KPL>
 __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
-    const int lane = threadIdx.x & 31;
+    constexpr int SB = 8;
+    __shared__ uint2 stage[8][32];  // per warp: (column, g bits) of the current 32 nonzeros
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
     const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
     const float pv = a.pv;
@@ -428,35 +466,52 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
             float acc[KPL];
 #pragma unroll
             for (int q = 0; q < KPL; ++q) acc[q] = 0.f;
+            const float *ctl = a.CT0 + g0 + KPL * lane;
+            const bool lane_on = g0 + KPL * lane < a.kp;  // lanes past the padded centers idle
             for (uint64_t p0 = pb; p0 < pe; p0 += 32) {
                 const uint64_t p = p0 + lane;
+                // past the row's end: center column 0 with a g that adds exactly nothing
+                // (MKL, Hellinger, SQRL2: g = 0 makes every term +-0 on a sum that is not
+                // -0; L1: g = pv makes |c - g| - |c - pv| = +0)
                 uint32_t col = 0;
-                float g = 0.f, x = 0.f;
+                float g = (MSR == L1) ? pv : 0.f;
                 if (p < pe) {
                     col = a.idx[p];
-                    x = a.vals[p];
+                    const float x = a.vals[p];
                     if (MSR == MKL) g = rl - logf(x * rsi + rinc);
                     else if (MSR == HELLINGER) g = srinc - sqrtf(x * rsi + rinc);
                     else if (MSR == L1) g = x + pv;
                     else g = x;
                 }
-                const int cnt = int(umin64(32, pe - p0));
-                for (int q = 0; q < cnt; ++q) {
-                    const uint32_t cj = __shfl_sync(0xffffffffu, col, q);
-                    const float gj = __shfl_sync(0xffffffffu, g, q);
-                    const float *ct = a.CT0 + uint64_t(cj) * a.kp + g0 + lane;
+                __syncwarp();
+                stage[wib][lane] = make_uint2(col, __float_as_uint(g));
+                __syncwarp();
+                const int cnt = int(umin64(32, pe - p0));  // warp-uniform
+                for (int q0 = 0; q0 < cnt; q0 += SB) {
+                    CenterVec<KPL> cv[SB];
+                    float gj[SB];
 #pragma unroll
-                    for (int r = 0; r < KPL; ++r) {
-                        const float cv = __ldg(ct + 32 * r);
-                        if (MSR == MKL || MSR == HELLINGER) acc[r] = fmaf(cv, gj, acc[r]);
-                        else if (MSR == SQRL2) acc[r] = fmaf(gj, gj - 2.f * cv, acc[r]);
-                        else acc[r] = acc[r] + (fabsf(cv - gj) - fabsf(cv - pv));
+                    for (int u = 0; u < SB; ++u) {
+                        const uint2 e = stage[wib][q0 + u];
+                        if (lane_on) cv[u].load(ctl + uint64_t(e.x) * a.kp);
+                        else cv[u].zero();
+                        gj[u] = __uint_as_float(e.y);
+                    }
+#pragma unroll
+                    for (int u = 0; u < SB; ++u) {
+#pragma unroll
+                        for (int r = 0; r < KPL; ++r) {
+                            const float c = cv[u].v[r];
+                            if (MSR == MKL || MSR == HELLINGER) acc[r] = fmaf(c, gj[u], acc[r]);
+                            else if (MSR == SQRL2) acc[r] = fmaf(gj[u], gj[u] - 2.f * c, acc[r]);
+                            else acc[r] = acc[r] + (fabsf(c - gj[u]) - fabsf(c - pv));
+                        }
                     }
                 }
             }
 #pragma unroll
             for (int r = 0; r < KPL; ++r) {
-                const uint32_t c = g0 + lane + 32 * r;
+                const uint32_t c = g0 + KPL * lane + r;
                 if (c < a.k) {
                     const double k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
                     float key;
@@ -486,128 +541,6 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
             a.costs[row] = double(float(cost));
         }
     }
-}
-
-// ------------------------------------------------------------------------------------
-// sparse-dot CSR kernel, one thread per row (constant prior; SQRL2, L1, MKL, HELLINGER;
-// k <= 64).  Each warp stages the next NZC nonzeros of its 32 rows in shared memory with
-// coalesced loads; every thread then walks its own nonzeros, loading the center column
-// c[j][0..KC) with float4 loads and updating KC register accumulators.
-// ------------------------------------------------------------------------------------
-template <int MSR, int KC>
-__global__ void __launch_bounds__(128) k_assign_csr_rows(AssignArgs a) {
-    constexpr int NZC = 16;
-    __shared__ uint32_t sidx[4][32][NZC + 1];
-    __shared__ float sval[4][32][NZC + 1];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint64_t row0 = (uint64_t(blockIdx.x) * 4 + w) * 32;
-    const uint64_t row = row0 + lane;
-    const bool valid = row < a.n;
-    const float pv = a.pv;
-    uint64_t pb = 0, pe = 0;
-    float rsi = 0.f, rinc = 0.f;
-    if (valid) {
-        pb = a.indptr[row];
-        pe = a.indptr[row + 1];
-        if (MSR == MKL || MSR == HELLINGER) {
-            rsi = a.rsi[row];
-            rinc = a.rinc[row];
-        }
-    }
-    const float rl = (MSR == MKL) ? logf(rinc) : 0.f;
-    const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
-    float acc[KC];
-#pragma unroll
-    for (int c = 0; c < KC; ++c) acc[c] = 0.f;
-    double bsum = 0.0;  // HELLINGER: sum of b over the row's nonzeros
-    const uint64_t mynnz = pe - pb;
-    uint64_t maxnnz = mynnz;
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) {
-        const uint64_t other = __shfl_xor_sync(0xffffffffu, maxnnz, m);
-        maxnnz = other > maxnnz ? other : maxnnz;
-    }
-    for (uint64_t o = 0; o < maxnnz; o += NZC) {
-        // stage: lane l loads element (o + l % NZC) of rows 2i + l / NZC, coalesced per row
-        __syncwarp();
-#pragma unroll 4
-        for (int i = 0; i < 16; ++i) {
-            const int r = 2 * i + (lane / NZC), q = lane % NZC;
-            const uint64_t rb = __shfl_sync(0xffffffffu, pb, r), re = __shfl_sync(0xffffffffu, pe, r);
-            const uint64_t p = rb + o + q;
-            uint32_t jj = 0;
-            float xv = 0.f;
-            if (p < re) {
-                jj = a.idx[p];
-                xv = a.vals[p];
-            }
-            sidx[w][r][q] = jj;
-            sval[w][r][q] = xv;
-        }
-        __syncwarp();
-        const int cnt = int(umin64(NZC, mynnz > o ? mynnz - o : 0));
-        for (int q = 0; q < cnt; ++q) {
-            const uint32_t j = sidx[w][lane][q];
-            const float x = sval[w][lane][q];
-            float g;
-            if (MSR == MKL) g = rl - logf(x * rsi + rinc);
-            else if (MSR == HELLINGER) {
-                const float b = x * rsi + rinc;
-                bsum += double(b);
-                g = srinc - sqrtf(b);
-            } else if (MSR == L1) g = x + pv;
-            else g = x;
-            const float4 *ct = reinterpret_cast<const float4 *>(a.CT0 + uint64_t(j) * KC);
-#pragma unroll
-            for (int c4 = 0; c4 < KC / 4; ++c4) {
-                const float4 cv = __ldg(ct + c4);
-                const float cc[4] = {cv.x, cv.y, cv.z, cv.w};
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int c = 4 * c4 + e;
-                    if (MSR == MKL || MSR == HELLINGER) acc[c] = fmaf(cc[e], g, acc[c]);
-                    else if (MSR == SQRL2) acc[c] = fmaf(g, g - 2.f * cc[e], acc[c]);
-                    else acc[c] = acc[c] + (fabsf(cc[e] - g) - fabsf(cc[e] - pv));
-                }
-            }
-        }
-    }
-    if (!valid) return;
-    const double bx = bsum + double(a.d - mynnz) * double(rinc);
-    float bestk = __int_as_float(0x7f800000);
-    uint32_t bestj = 0xffffffffu;
-    bool nan0 = false;
-#pragma unroll
-    for (int c = 0; c < KC; ++c) {
-        if (uint32_t(c) < a.k) {
-            const double k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
-            float key;
-            if (MSR == MKL) {
-                key = post_divergence(float(k0 - double(rl) * k1 + double(acc[c])));
-            } else if (MSR == HELLINGER) {
-                double sv = k0 + bx - 2.0 * double(srinc) * k1 + 2.0 * double(acc[c]);
-                if (sv < 0.0) sv = 0.0;
-                key = float(sqrt(sv));
-            } else if (MSR == SQRL2) {
-                double sv = k0 + double(acc[c]);
-                if (sv < 0.0) sv = 0.0;
-                key = float(sv);
-            } else {
-                key = float(k0 + double(acc[c])) * 0.5f;
-            }
-            // sequential scan semantics: strict <, NaN at center 0 sticks
-            if (c == 0) {
-                bestk = key;
-                bestj = 0;
-                nan0 = key != key;
-            } else if (!nan0 && key < bestk) {
-                bestk = key;
-                bestj = uint32_t(c);
-            }
-        }
-    }
-    a.asn[row] = bestj;
-    a.costs[row] = double(float(key_to_cost<MSR>(bestk)));
 }
 
 // ------------------------------------------------------------------------------------
@@ -690,25 +623,9 @@ int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t s
     }
 }
 
-uint32_t sparse_rows_pad(uint32_t k);
-
 template <int MSR>
 static int sparse_t(const AssignArgs &a, cudaStream_t st, int sms) {
-    if (a.kp <= 64 && a.kp % 4 == 0 && a.kp == sparse_rows_pad(a.k)) {
-        const unsigned blocks = unsigned((a.n + 127) / 128);
-        switch (a.kp) {
-#define MC_ROWS_CASE(KCV) \
-    case KCV: k_assign_csr_rows<MSR, KCV><<<blocks, 128, 0, st>>>(a), note_launch(); break;
-            MC_ROWS_CASE(4) MC_ROWS_CASE(8) MC_ROWS_CASE(12) MC_ROWS_CASE(16) MC_ROWS_CASE(20) MC_ROWS_CASE(24)
-            MC_ROWS_CASE(28) MC_ROWS_CASE(32) MC_ROWS_CASE(36) MC_ROWS_CASE(40) MC_ROWS_CASE(44) MC_ROWS_CASE(48)
-            MC_ROWS_CASE(52) MC_ROWS_CASE(56) MC_ROWS_CASE(60) MC_ROWS_CASE(64)
-#undef MC_ROWS_CASE
-            default: return fail(MC_ECUDA, "unexpected center padding");
-        }
-        MC_CUDA_TRY(cudaGetLastError());
-        return MC_OK;
-    }
-    const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 8));
+    const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
     if (a.kp <= 32) k_assign_sparse<MSR, 1><<<blocks, 256, 0, st>>>(a), note_launch();
     else if (a.kp <= 64) k_assign_sparse<MSR, 2><<<blocks, 256, 0, st>>>(a), note_launch();
     else k_assign_sparse<MSR, 4><<<blocks, 256, 0, st>>>(a), note_launch();
@@ -716,10 +633,11 @@ static int sparse_t(const AssignArgs &a, cudaStream_t st, int sms) {
     return MC_OK;
 }
 
-uint32_t sparse_rows_pad(uint32_t k) { return (k + 3) / 4 * 4; }
-
+// the warp-per-row kernel reads 32 * KPL consecutive centers of a column per group; whole
+// groups keep every column's gather 128-byte aligned (measured faster than padding to 4)
 uint32_t sparse_center_pad(uint32_t k) {
-    if (k <= 64) return sparse_rows_pad(k);  // thread-per-row kernel: k rounded up to 4
+    if (k <= 32) return 32;
+    if (k <= 64) return 64;
     return (k + 127) / 128 * 128;
 }
 

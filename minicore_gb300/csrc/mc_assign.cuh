@@ -33,6 +33,5 @@ int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t s
 int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms);
 uint32_t tiled_center_pad(uint32_t k, bool pair, int msr);
 uint32_t sparse_center_pad(uint32_t k);
-uint32_t sparse_rows_pad(uint32_t k);
 
 }  // namespace mc
