@@ -525,6 +525,21 @@ class Clocks:
                 "reasons": reasons, "samples": len(s)}
 
 
+def replica_throughput(ms_local, steps, world, device):
+    """Independent replicas (one per rank, no collective on the data path): the slowest
+    rank's time bounds the job, and every rank completed `steps` iterations.  Returns
+    (ms per step, whole-job iterations per second)."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / steps
+    return ms_per_step, world * 1000.0 / ms_per_step
+
+
 def fp64_objective_check(job, X, n, sample=100_000, seed=5):
     """After the timed steps: the job's assignment and objective on a fixed row subsample
     against an FP64 computation (numpy, float64 GEMM form of the squared distances) with
@@ -675,13 +690,7 @@ def main():
     buf = ctypes.create_string_buffer(1 << 16)
     _lib.check(lib.mc_profile_report(buf, len(buf)))
     phases = json.loads(buf.value.decode())
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_per_step = ms / args.steps
-    value = world * 1000.0 / ms_per_step  # independent replicas: iterations completed per second
+    ms_per_step, value = replica_throughput(ev0.elapsed_time(ev1), args.steps, world, "cuda")
     recheck = job.recheck_count()
     accuracy = fp64_objective_check(job, X, n) if rank == 0 else None
 
