@@ -8,7 +8,7 @@
  *                        driven by py_kmeanspp_noso(_dense) python/smw.h:179-412
  *   mc_assign            assign_points_hard            include/minicore/clustering/solve.h:234-285
  *                        (per-pair cmp::msr_with_prior include/minicore/dist/applicator.h:1632-1915)
- *   mc_set_centroids     set_centroids_full_mean       include/minicore/clustering/centroid.h:649-779
+ *   mc_job_lloyd_step    set_centroids_full_mean       include/minicore/clustering/centroid.h:649-779
  *                        + set_center                  centroid.h:81-112 (CSR), 137-178 (dense)
  *   mc_hcluster          perform_hard_clustering       include/minicore/clustering/solve.h:98-175
  *                        driven by cpp_pycluster_from_centers python/pycluster.h:10-63
@@ -204,6 +204,20 @@ int mc_server_stats(mc_server *s, char *json, uint64_t capacity);
 int mc_server_reset_stats(mc_server *s);
 /* Runs every queued job to completion, then stops the slots. */
 int mc_server_destroy(mc_server *s);
+
+/* Kernel-variant autotuner (no reference counterpart).  Some kernels come in variants that
+ * compute bit-identical results (same per-element arithmetic and summation order) at
+ * different speeds: the CSR sparse-dot batch size, the SQRL2 FP32 register tile and the
+ * kmeans++ distance-update load path.  The first call for a shape bucket times each variant
+ * and keeps the fastest.  Decisions persist in a cache file (MC_AUTOTUNE_CACHE, default
+ * $XDG_CACHE_HOME or $HOME/.cache + /minicore_gb300/autotune.tsv); MC_AUTOTUNE=0 or
+ * mc_autotune_enable(0) keeps the defaults. */
+int mc_autotune_enable(int on);
+int mc_autotune_reset(void);                    /* forget every decision (not the file)      */
+int mc_autotune_load(const char *path);         /* add decisions from a cache file           */
+int mc_autotune_save(const char *path);         /* write every decision to a cache file      */
+/* JSON: {"enabled": b, "entries": {key: {"variant": v, "ms": [per-variant best ms]}}} */
+int mc_autotune_report(char *json, uint64_t capacity);
 
 /* Capacity of mc_assign_sqrl2_noalloc's fixed scratch array, in floats (4 MiB). */
 #define MC_NOALLOC_SCRATCH_FLOATS (1u << 20)

@@ -608,3 +608,23 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------------------------------
+# kernel-variant autotuner
+# ------------------------------------------------------------------------------------
+def autotune(enable: bool = True):
+    """Turn the kernel-variant autotuner on or off (variants give bit-identical results;
+    only speed differs).  Decisions persist in MC_AUTOTUNE_CACHE or the user cache dir."""
+    check(_lib.load().mc_autotune_enable(1 if enable else 0))
+
+
+def autotune_report() -> dict:
+    import json
+    buf = ctypes.create_string_buffer(1 << 20)
+    check(_lib.load().mc_autotune_report(buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
+def autotune_reset():
+    check(_lib.load().mc_autotune_reset())

@@ -63,6 +63,11 @@ SIGNATURES = {
     "mc_job_read": (I, [P, P, P, P]),
     "mc_job_recheck_count": (I, [P, ctypes.POINTER(U64)]),
     "mc_assign_sqrl2_noalloc": (I, [P, U64, U64, P, U32, P, P, P]),
+    "mc_autotune_enable": (I, [I]),
+    "mc_autotune_reset": (I, []),
+    "mc_autotune_load": (I, [ctypes.c_char_p]),
+    "mc_autotune_save": (I, [ctypes.c_char_p]),
+    "mc_autotune_report": (I, [ctypes.c_char_p, U64]),
     "mc_job_create_kmeanspp": (I, [P, P, U32, I, D, P, I, U64, P, ctypes.POINTER(P)]),
     "mc_server_create": (I, [I, U32, U64, ctypes.POINTER(P)]),
     "mc_server_submit": (I, [P, ctypes.POINTER(McJobDesc), ctypes.POINTER(U64)]),

@@ -224,6 +224,7 @@ int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exac
     a.vals = j->M.vals;
     a.idx = j->M.idx;
     a.indptr = j->M.indptr;
+    a.nnz = j->M.nnz;
     a.rowsum = j->rowsum.p;
     a.rsi = j->rsi.p;
     a.rinc = j->rinc.p;

@@ -17,6 +17,7 @@
 // center-side and row-side transforms are precomputed; otherwise (prior 0) every pair
 // recomputes them ("pair mode").
 #include "mc_assign.cuh"
+#include "mc_tune.cuh"
 
 namespace mc {
 
@@ -433,11 +434,11 @@ struct CenterVec<4> {
 // Lane l owns centers g0 + KPL*l .. + KPL-1 of the current group of 32*KPL (one vector load
 // per nonzero; lanes past the padded centers idle).  Each
 // chunk of 32 nonzeros is staged per warp in shared memory as (column, g) and read back by
-// broadcast; SB nonzeros per batch have their center loads issued before the first use.
+// broadcast; SB nonzeros per batch (8, 4 or 16, picked by the autotuner) have their center
+// loads issued before the first use.
 // The per-(row, center) sum stays sequential over the nonzeros.
-template <int MSR, int KPL>
+template <int MSR, int KPL, int SB>
 __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
-    constexpr int SB = 8;
     __shared__ uint2 stage[8][32];  // per warp: (column, g bits) of the current 32 nonzeros
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
@@ -588,13 +589,23 @@ int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, f
 }
 
 template <int MSR, bool CSR>
-static int tiled_t(const AssignArgs &a, bool pair, bool big, cudaStream_t st) {
+static int tiled_t(const AssignArgs &a, bool pair, bool big, cudaStream_t st, bool tune) {
     if (pair) {
         constexpr int BM = 32;
         k_assign_tiled<MSR, true, 2, 2, CSR><<<unsigned((a.n + BM - 1) / BM), 256, 0, st>>>(a), note_launch();
     } else if (big) {
-        constexpr int BM = 128;
-        k_assign_tiled<MSR, false, 8, 8, CSR><<<unsigned((a.n + BM - 1) / BM), 256, 0, st>>>(a), note_launch();
+        // SQRL2 with kp % 128 == 0: 8x8 register tiles (128 rows per CTA) or 4x4 (64 rows);
+        // same per-pair arithmetic, so the autotuner may pick either
+        const std::string key = std::string("dense_sqrl2|") + (CSR ? "csr" : "dense") + "|k" +
+                                std::to_string(a.kp) + "|d" + tune_bucket(a.d) + "|n" + tune_bucket(a.n);
+        return tune_launch(key, 2, 0, st, tune, [&](int v) -> int {
+            if (v == 0)
+                k_assign_tiled<MSR, false, 8, 8, CSR><<<unsigned((a.n + 127) / 128), 256, 0, st>>>(a), note_launch();
+            else
+                k_assign_tiled<MSR, false, 4, 4, CSR><<<unsigned((a.n + 63) / 64), 256, 0, st>>>(a), note_launch();
+            MC_CUDA_TRY(cudaGetLastError());
+            return MC_OK;
+        });
     } else {
         constexpr int BM = 64;
         k_assign_tiled<MSR, false, 4, 4, CSR><<<unsigned((a.n + BM - 1) / BM), 256, 0, st>>>(a), note_launch();
@@ -608,29 +619,43 @@ uint32_t tiled_center_pad(uint32_t k, bool pair, int msr) {
     return (k + bn - 1) / bn * bn;
 }
 
-int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st) {
+int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st, bool tune) {
     if (a.n == 0) return MC_OK;
     // 8x8 register tiles for SQRL2 with many centers, 4x4 otherwise
     const bool big = (a.msr == SQRL2 && a.kp % 128 == 0);
     switch (a.msr) {
-        case SQRL2: return csr ? tiled_t<SQRL2, true>(a, pair, big, st) : tiled_t<SQRL2, false>(a, pair, big, st);
-        case L1: return csr ? tiled_t<L1, true>(a, pair, false, st) : tiled_t<L1, false>(a, pair, false, st);
+        case SQRL2:
+            return csr ? tiled_t<SQRL2, true>(a, pair, big, st, tune) : tiled_t<SQRL2, false>(a, pair, big, st, tune);
+        case L1: return csr ? tiled_t<L1, true>(a, pair, false, st, tune) : tiled_t<L1, false>(a, pair, false, st, tune);
         case HELLINGER:
-            return csr ? tiled_t<HELLINGER, true>(a, pair, false, st) : tiled_t<HELLINGER, false>(a, pair, false, st);
-        case MKL: return csr ? tiled_t<MKL, true>(a, pair, false, st) : tiled_t<MKL, false>(a, pair, false, st);
-        case JSD: return csr ? tiled_t<JSD, true>(a, pair, false, st) : tiled_t<JSD, false>(a, pair, false, st);
+            return csr ? tiled_t<HELLINGER, true>(a, pair, false, st, tune)
+                       : tiled_t<HELLINGER, false>(a, pair, false, st, tune);
+        case MKL: return csr ? tiled_t<MKL, true>(a, pair, false, st, tune) : tiled_t<MKL, false>(a, pair, false, st, tune);
+        case JSD: return csr ? tiled_t<JSD, true>(a, pair, false, st, tune) : tiled_t<JSD, false>(a, pair, false, st, tune);
         default: return fail(MC_EUNSUPPORTED, "measure not supported");
     }
 }
 
-template <int MSR>
-static int sparse_t(const AssignArgs &a, cudaStream_t st, int sms) {
+template <int MSR, int KPL>
+static int sparse_kpl(const AssignArgs &a, cudaStream_t st, int sms, bool tune) {
     const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
-    if (a.kp <= 32) k_assign_sparse<MSR, 1><<<blocks, 256, 0, st>>>(a), note_launch();
-    else if (a.kp <= 64) k_assign_sparse<MSR, 2><<<blocks, 256, 0, st>>>(a), note_launch();
-    else k_assign_sparse<MSR, 4><<<blocks, 256, 0, st>>>(a), note_launch();
-    MC_CUDA_TRY(cudaGetLastError());
-    return MC_OK;
+    const uint64_t avg = a.n ? (a.nnz + a.n - 1) / a.n : 0;
+    const std::string key = "csr_sparse|msr" + std::to_string(MSR) + "|kpl" + std::to_string(KPL) + "|g" +
+                            std::to_string((a.k + 32 * KPL - 1) / (32 * KPL)) + "|nnz" + tune_bucket(avg);
+    return tune_launch(key, 3, 0, st, tune, [&](int v) -> int {
+        if (v == 0) k_assign_sparse<MSR, KPL, 8><<<blocks, 256, 0, st>>>(a), note_launch();
+        else if (v == 1) k_assign_sparse<MSR, KPL, 4><<<blocks, 256, 0, st>>>(a), note_launch();
+        else k_assign_sparse<MSR, KPL, 16><<<blocks, 256, 0, st>>>(a), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        return MC_OK;
+    });
+}
+
+template <int MSR>
+static int sparse_t(const AssignArgs &a, cudaStream_t st, int sms, bool tune) {
+    if (a.kp <= 32) return sparse_kpl<MSR, 1>(a, st, sms, tune);
+    if (a.kp <= 64) return sparse_kpl<MSR, 2>(a, st, sms, tune);
+    return sparse_kpl<MSR, 4>(a, st, sms, tune);
 }
 
 // the warp-per-row kernel reads 32 * KPL consecutive centers of a column per group; whole
@@ -641,13 +666,13 @@ uint32_t sparse_center_pad(uint32_t k) {
     return (k + 127) / 128 * 128;
 }
 
-int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms) {
+int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms, bool tune) {
     if (a.n == 0) return MC_OK;
     switch (a.msr) {
-        case SQRL2: return sparse_t<SQRL2>(a, st, sms);
-        case L1: return sparse_t<L1>(a, st, sms);
-        case HELLINGER: return sparse_t<HELLINGER>(a, st, sms);
-        case MKL: return sparse_t<MKL>(a, st, sms);
+        case SQRL2: return sparse_t<SQRL2>(a, st, sms, tune);
+        case L1: return sparse_t<L1>(a, st, sms, tune);
+        case HELLINGER: return sparse_t<HELLINGER>(a, st, sms, tune);
+        case MKL: return sparse_t<MKL>(a, st, sms, tune);
         default: return fail(MC_EUNSUPPORTED, "sparse-dot path does not cover this measure");
     }
 }

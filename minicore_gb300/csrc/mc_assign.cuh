@@ -13,6 +13,7 @@ struct AssignArgs {
     const float *vals = nullptr;      // CSR rows
     const uint32_t *idx = nullptr;
     const uint64_t *indptr = nullptr;
+    uint64_t nnz = 0;                 // CSR nonzeros (autotuner shape bucket)
     const double *rowsum = nullptr;   // per row (pair mode, sparse HELL)
     const float *rsi = nullptr;       // per-row 1/rhsum (constant prior)
     const float *rinc = nullptr;      // per-row pv/rhsum (constant prior)
@@ -29,8 +30,10 @@ struct AssignArgs {
 int launch_prep_centers(const AssignArgs &a, const float *C, bool pair, bool sparse_consts, cudaStream_t st);
 int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, float *rsi, float *rinc,
                        cudaStream_t st);
-int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st);
-int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms);
+// tune: the autotuner may time kernel variants on the first call for a shape (callers that
+// must not synchronise or allocate pass false)
+int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st, bool tune = true);
+int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms, bool tune = true);
 uint32_t tiled_center_pad(uint32_t k, bool pair, int msr);
 uint32_t sparse_center_pad(uint32_t k);
 

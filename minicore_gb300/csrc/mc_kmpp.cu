@@ -6,6 +6,7 @@
 // dist[newc] = 0.  Nothing returns to the host between rounds, so the k rounds are queued
 // back to back on one stream.
 #include "mc_kmpp.cuh"
+#include "mc_tune.cuh"
 
 namespace mc {
 
@@ -272,10 +273,21 @@ static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaS
         KmppArgs b = a;
         b.round = round;
         const bool vec4 = a.d % 4 == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
-        if (vec4)
-            k_kmpp_dense_staged<MSR><<<unsigned((a.n + 127) / 128), 128, 0, st>>>(b, first), note_launch();
-        else
-            k_kmpp_dense<MSR, false><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
+        if (vec4) {
+            // rows staged through shared memory, or read directly with float4 loads (the same
+            // per-row arithmetic): the autotuner keeps the faster for this measure and width
+            const std::string key = "kmpp_dense|msr" + std::to_string(MSR) + "|d" + tune_bucket(a.d) + "|n" +
+                                    tune_bucket(a.n);
+            return tune_launch(key, 2, 0, st, true, [&](int v) -> int {
+                if (v == 0)
+                    k_kmpp_dense_staged<MSR><<<unsigned((a.n + 127) / 128), 128, 0, st>>>(b, first), note_launch();
+                else
+                    k_kmpp_dense<MSR, true><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
+                MC_CUDA_TRY(cudaGetLastError());
+                return MC_OK;
+            });
+        }
+        k_kmpp_dense<MSR, false><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
     } else {
         const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
         k_kmpp_csr<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();

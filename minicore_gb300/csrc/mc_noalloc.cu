@@ -81,5 +81,5 @@ extern "C" int mc_assign_sqrl2_noalloc(const float *X, uint64_t n, uint64_t d, c
     a.asn = asn;
     a.costs = costs;
     MC_TRY(launch_prep_centers(a, centers, false, false, st));
-    return launch_assign_tiled(a, false, false, st);
+    return launch_assign_tiled(a, false, false, st, /*tune=*/false);
 }

@@ -1024,7 +1024,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
         b.costs = costs;
         Phase ph("tc_rescan_fp32", st);
         MC_TRY(launch_prep_centers(b, C, false, false, st));
-        MC_TRY(launch_assign_tiled(b, false, false, st));
+        MC_TRY(launch_assign_tiled(b, false, false, st, /*tune=*/false));
     }
     if (recheck_count) *recheck_count = nr[0] + nr[1];
     return MC_OK;

@@ -115,3 +115,32 @@ def test_server_create_fails_cleanly_without_gpu():
     assert not h.value
     assert lib.mc_server_create(0, 0, 0, ctypes.byref(h)) == _lib.MC_EINVAL
     assert lib.mc_server_destroy(None) == 0
+
+
+def test_autotune_cache_roundtrip(tmp_path):
+    """Autotuner decisions load from and save to the cache file (host-only logic)."""
+    import json
+    from minicore_gb300 import _lib
+    lib = _lib.load()
+    assert lib.mc_autotune_reset() == 0
+    src = tmp_path / "in.tsv"
+    src.write_text("csr_sparse|msr5|kpl2|g1|nnz2^11|sm103x152\t1\t0.5,0.4,0.7\n"
+                   "garbage line without tabs\n"
+                   "dense_sqrl2|dense|k1024|d2^7|n2^22|sm103x152\t0\t1.0,1.2\n"
+                   "bad_variant\tx\t1\n")
+    assert lib.mc_autotune_load(str(src).encode()) == 0
+    buf = ctypes.create_string_buffer(1 << 16)
+    assert lib.mc_autotune_report(buf, len(buf)) == 0
+    rep = json.loads(buf.value.decode())
+    ent = rep["entries"]
+    assert ent["csr_sparse|msr5|kpl2|g1|nnz2^11|sm103x152"]["variant"] == 1
+    assert ent["dense_sqrl2|dense|k1024|d2^7|n2^22|sm103x152"]["ms"] == [1.0, 1.2]
+    assert not any(k.startswith("bad_variant") or k.startswith("garbage") for k in ent)
+    dst = tmp_path / "out.tsv"
+    assert lib.mc_autotune_save(str(dst).encode()) == 0
+    lines = sorted(dst.read_text().splitlines())
+    assert any(l.startswith("csr_sparse|msr5|kpl2|g1|nnz2^11|sm103x152\t1\t") for l in lines)
+    assert lib.mc_autotune_reset() == 0
+    assert lib.mc_autotune_report(buf, len(buf)) == 0
+    assert json.loads(buf.value.decode())["entries"] == {}
+    assert lib.mc_autotune_load(str(tmp_path / "missing.tsv").encode()) == _lib.MC_EINVAL

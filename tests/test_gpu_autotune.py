@@ -1,0 +1,77 @@
+"""Autotuner on the GPU: every tuned family gives the same results with tuning on (variants
+timed on first use) and off (defaults), and records its decision."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mc():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    import minicore_gb300
+    yield minicore_gb300
+    minicore_gb300.autotune(True)
+
+
+def _counts(n, d, density, seed):
+    rng = np.random.default_rng(seed)
+    M = sp.random(n, d, density=density, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.integers(1, 6, s).astype(np.float32)).tolil()
+    for i in range(n):
+        if M.rows[i] == []:
+            M[i, int(rng.integers(0, d))] = 1.0
+    M = M.tocsr()
+    M.sort_indices()
+    return M.astype(np.float32)
+
+
+def _assign(mc, X, C, msr, prior):
+    import ctypes
+    from minicore_gb300 import _lib
+    M = mc._MatrixArg(X)
+    C = np.ascontiguousarray(C, np.float32)
+    asn = np.empty(M.n, np.uint32)
+    costs = np.empty(M.n, np.float64)
+    _lib.check(_lib.load().mc_assign(mc.default_context().handle, M.ref, mc._p(C), C.shape[0], msr, prior,
+                                     mc._PREC["fp32"], mc._p(asn), mc._p(costs)))
+    return asn, costs
+
+
+@pytest.mark.parametrize("k", [20, 50, 150])
+def test_csr_sparse_tuned_equals_default(mc, k):
+    X = _counts(3000, 800, 0.03, seed=k)
+    C = np.asarray(X[np.arange(0, 3000, 3000 // k)[:k]].toarray(), np.float32)
+    mc.autotune(False)
+    a0, c0 = _assign(mc, X, C, 5, 1.0)
+    mc.autotune_reset()
+    mc.autotune(True)
+    a1, c1 = _assign(mc, X, C, 5, 1.0)   # tunes: every variant runs, the last one's output stays
+    a2, c2 = _assign(mc, X, C, 5, 1.0)   # the kept variant
+    assert np.array_equal(a0, a1) and np.array_equal(c0, c1)
+    assert np.array_equal(a0, a2) and np.array_equal(c0, c2)
+    ent = mc.autotune_report()["entries"]
+    assert any(key.startswith("csr_sparse|msr5|") for key in ent)
+    assert all(len(v["ms"]) == 3 and 0 <= v["variant"] < 3 for key, v in ent.items() if key.startswith("csr"))
+
+
+def test_dense_sqrl2_and_kmeanspp_tuned_equal_default(mc):
+    rng = np.random.default_rng(4)
+    X = (rng.normal(size=(20000, 64)) + rng.integers(0, 8, (20000, 1))).astype(np.float32)
+    C = X[rng.choice(20000, 256, replace=False)]
+    mc.autotune(False)
+    a0, c0 = _assign(mc, X, C, 2, 0.0)
+    ids0, asn0, cost0 = mc.kmeanspp(X, 40, msr=2, seed=11)
+    mc.autotune_reset()
+    mc.autotune(True)
+    for _ in range(2):
+        a1, c1 = _assign(mc, X, C, 2, 0.0)
+        ids1, asn1, cost1 = mc.kmeanspp(X, 40, msr=2, seed=11)
+        assert np.array_equal(a0, a1) and np.array_equal(c0, c1)
+        assert np.array_equal(ids0, ids1) and np.array_equal(asn0, asn1) and np.array_equal(cost0, cost1)
+    keys = list(mc.autotune_report()["entries"])
+    assert any(k.startswith("dense_sqrl2|dense|k256|") for k in keys)
+    assert any(k.startswith("kmpp_dense|msr2|") for k in keys)
