@@ -128,6 +128,16 @@ int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
                 int precision, float *centers_out, uint32_t *asn, double *costs,
                 double *initcost, double *finalcost, uint64_t *numiter);
 
+/* Pairwise distances (python/pycmp.cpp:15-300, python/pyarrcmp.cpp:52-144), exact FP32,
+ * written as float32.  Y: dense m x ncols float32.  reverse == 0: out[i][j] =
+ * msr(lh = Y[j], rh = X[i]) (the assignment's roles: Y as centers), reverse != 0:
+ * out[i][j] = msr(lh = X[i], rh = Y[j]).  out: nrows x m. */
+int mc_cmp(mc_context *ctx, const mc_matrix *X, const float *Y, uint64_t m, int msr, double prior,
+           int reverse, float *out);
+/* Condensed pairwise distances among the rows of X (pcmp): for i < j, entry
+ * i*n - i*(i+1)/2 + j - i - 1 = msr(lh = row i, rh = row j); out holds n*(n-1)/2 floats. */
+int mc_pcmp(mc_context *ctx, const mc_matrix *X, int msr, double prior, float *out);
+
 /* Coreset sampler (coreset.h:386-422).  costs: float32 or float64 (costs_f64 != 0);
  * weights: optional float32 (the reference stores them as float). k: the k of LBK's
  * alpha (pass ncenters for the reference default). */

@@ -345,6 +345,63 @@ def cluster(data, *, msr, k, prior=0., seed=0, nmkc=0, ntimes=1, lspp=0, use_exp
 
 
 # ------------------------------------------------------------------------------------
+# pairwise distances
+# ------------------------------------------------------------------------------------
+def cmp(matrix, data, msr=2, prior=0., reverse=None, use_float=-1, ctx: Context | None = None):
+    """Distances between the rows of ``matrix`` and the rows of ``data`` (python/pycmp.cpp:15-246,
+    python/pyarrcmp.cpp:52-144), float32, shape (rows of matrix, rows of data).
+
+    Default roles are the assignment's: out[i, j] = msr(lh = data[j], rh = matrix[i]).  As in
+    the reference, ``reverse`` flips them with opposite defaults per overload: for a NumPy
+    ``matrix`` reverse=True (its default) keeps those roles, for a sparse ``matrix``
+    reverse=False (its default) keeps them.  1-D ``data`` gives one value per row of
+    ``matrix``; 1-D ``matrix`` and ``data`` give a float."""
+    ctx = ctx or default_context()
+    scalar = False
+    if not _is_sparse(matrix) and not hasattr(matrix, "data_ptr"):
+        matrix = np.asarray(matrix)
+        if matrix.ndim == 1:
+            matrix = matrix[None, :]
+            scalar = True
+    M = _MatrixArg(matrix)
+    if _is_sparse(data):
+        data = data.toarray() if hasattr(data, "toarray") else np.asarray(data)
+    Y = np.asarray(data, dtype=np.float32)
+    one = Y.ndim == 1
+    if one:
+        Y = Y[None, :]
+    if Y.ndim != 2:
+        raise ValueError("NumPy array expected to have 1 or two dimensions.")
+    if Y.shape[1] != M.d:
+        raise ValueError("Array must be of the same dimensionality as the matrix")
+    Y = np.ascontiguousarray(Y)
+    if reverse is None:
+        assign_roles = True
+    elif M.kind == _lib.MC_DENSE_F32:
+        assign_roles = bool(reverse)
+    else:
+        assign_roles = not bool(reverse)
+    out = np.empty((M.n, Y.shape[0]), dtype=np.float32)
+    check(_lib.load().mc_cmp(ctx.handle, M.ref, _p(Y), Y.shape[0], _msr(msr), float(prior),
+                             0 if assign_roles else 1, _p(out)))
+    if scalar and one:
+        return float(out[0, 0])
+    return out[:, 0] if one else out
+
+
+def pcmp(matrix, msr=2, prior=0., use_float=-1, ctx: Context | None = None):
+    """Condensed pairwise distances among the rows of ``matrix`` (python/pycmp.cpp:249-300):
+    entry i*n - i*(i+1)/2 + j - i - 1 = msr(lh = row i, rh = row j) for i < j, float32."""
+    ctx = ctx or default_context()
+    M = _MatrixArg(matrix)
+    n = M.n
+    out = np.empty(max(n * (n - 1) // 2, 0), dtype=np.float32)
+    if n >= 2:
+        check(_lib.load().mc_pcmp(ctx.handle, M.ref, _msr(msr), float(prior), _p(out)))
+    return out
+
+
+# ------------------------------------------------------------------------------------
 # coreset sampler
 # ------------------------------------------------------------------------------------
 class CoresetSampler:

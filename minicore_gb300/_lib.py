@@ -48,6 +48,8 @@ SIGNATURES = {
     "mc_uniforms": (I, [U64, U64, U64, P]),
     "mc_kmeanspp": (I, [P, P, U32, I, D, P, P, P, P, P]),
     "mc_assign": (I, [P, P, P, U32, I, D, I, P, P]),
+    "mc_cmp": (I, [P, P, P, U64, I, D, I, P]),
+    "mc_pcmp": (I, [P, P, I, D, P]),
     "mc_hcluster": (I, [P, P, P, U32, I, D, P, D, U64, U64, I, P, P, P, P, P, P]),
     "mc_sampler_create": (I, [P, U64, U64, U64, P, I, P, P, I, D, ctypes.POINTER(P)]),
     "mc_sampler_destroy": (I, [P]),

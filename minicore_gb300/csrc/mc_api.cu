@@ -203,12 +203,19 @@ int sync(cudaStream_t st) {
     return MC_OK;
 }
 
+// optional distance output of an assignment pass (see AssignArgs::dmode)
+struct DistOut {
+    float *dmat = nullptr;
+    uint64_t ldm = 0;
+    int dmode = 0;
+};
+
 // the assignment pass with the centers in `C` (center sums / transforms refreshed here)
-int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exact) {
+int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exact, const DistOut *dout = nullptr) {
     const uint64_t n = j->M.n, d = j->M.d;
     MC_TRY(launch_center_sums(C, j->k, d, j->csum.p, j->cnorm.p, j->st));
     const bool csr = j->M.kind == MC_CSR_F32;
-    const bool tc = !csr && !force_exact && j->msr == SQRL2 && j->precision != MC_FP32;
+    const bool tc = !csr && !force_exact && !dout && j->msr == SQRL2 && j->precision != MC_FP32;
     if (tc) {
         MC_TRY(tc_assign(j->tc, j->M.X, n, d, C, j->cnorm.p, j->k, j->precision, j->rownorm.p, j->asn.p,
                          j->costs.p, j->ctx->sms, j->st, &j->last_recheck));
@@ -234,6 +241,11 @@ int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exac
     a.prior_sum = prior_sum;
     a.asn = j->asn.p;
     a.costs = j->costs.p;
+    if (dout) {
+        a.dmat = dout->dmat;
+        a.ldm = dout->ldm;
+        a.dmode = dout->dmode;
+    }
     const bool sparse = csr && j->sparse_path;
     a.kp = sparse ? sparse_center_pad(j->k) : tiled_center_pad(j->k, j->pair, j->msr);
     MC_TRY(j->CT0.alloc(uint64_t(a.kp) * d, j->st));
@@ -701,6 +713,92 @@ int mc_assign(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_
     std::unique_ptr<mc_job> guard(j);
     MC_TRY(mc_job_assign(j));
     return mc_job_read(j, nullptr, asn, costs);
+}
+
+// ------------------------------------------------------------------------------------
+// pairwise distance matrices (python/pycmp.cpp:15-300, python/pyarrcmp.cpp:52-144)
+// ------------------------------------------------------------------------------------
+__global__ void k_densify_csr(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                              const uint64_t *__restrict__ indptr, uint64_t n, uint64_t d, float *out) {
+    for (uint64_t r = blockIdx.x; r < n; r += gridDim.x) {
+        float *dst = out + r * d;
+        for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) dst[j] = 0.f;
+        __syncthreads();
+        for (uint64_t p = indptr[r] + threadIdx.x; p < indptr[r + 1]; p += blockDim.x) dst[idx[p]] = vals[p];
+        __syncthreads();
+    }
+}
+
+// the rows of X as a dense device matrix: borrowed when X is dense on the device, else a copy
+static int dense_rows(const mc_matrix *X, cudaStream_t st, int sms, DevMatrix &M, DBuf<float> &own,
+                      const float **out) {
+    MC_TRY(M.load(X, st));
+    if (M.kind == MC_DENSE_F32) {
+        *out = M.X;
+        return MC_OK;
+    }
+    MC_TRY(own.alloc(M.n * M.d, st));
+    k_densify_csr<<<unsigned(umin64(M.n, uint64_t(sms) * 8)), 256, 0, st>>>(M.vals, M.idx, M.indptr, M.n, M.d, own.p),
+        note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    *out = own.p;
+    return MC_OK;
+}
+
+// one exact FP32 assignment pass of `rows` against `centers` writing every pair's distance
+static int distance_pass(mc_context *ctx, const mc_matrix *rows, const float *centers, uint64_t k, int msr,
+                         double prior, float *out, uint64_t out_count, uint64_t ldm, int dmode) {
+    if (k == 0 || k >= (1ull << 32)) return fail(MC_EINVAL, "center count out of range");
+    mc_job *j = nullptr;
+    MC_TRY(mc_job_create(ctx, rows, centers, uint32_t(k), msr, prior, nullptr, MC_FP32, 1, &j));
+    std::unique_ptr<mc_job, int (*)(mc_job *)> guard(j, mc_job_destroy);
+    DBuf<float> dbuf;
+    float *D = out;
+    if (!is_device_ptr(out)) {
+        MC_TRY(dbuf.alloc(out_count, j->st));
+        D = dbuf.p;
+    }
+    DistOut o;
+    o.dmat = D;
+    o.ldm = ldm;
+    o.dmode = dmode;
+    MC_TRY(job_assign_with(j, j->C.p, j->psum, true, &o));
+    if (D != out) MC_CUDA_TRY(cudaMemcpyAsync(out, D, out_count * sizeof(float), cudaMemcpyDeviceToHost, j->st));
+    return sync(j->st);
+}
+
+int mc_cmp(mc_context *ctx, const mc_matrix *X, const float *Y, uint64_t m, int msr, double prior, int reverse,
+           float *out) {
+    if (!ctx || !X || !Y || !out) return fail(MC_EINVAL, "null argument");
+    if (m == 0) return fail(MC_EINVAL, "no rows in the second operand");
+    if (!measure_supported(msr)) return fail(MC_EUNSUPPORTED, "measure not implemented on this path");
+    MC_CUDA_TRY(cudaSetDevice(ctx->device));
+    const uint64_t n = X->nrows, d = X->ncols;
+    if (!reverse) {
+        // out[i][j] = msr(lh = Y[j], rh = X[i]): the rows of X against Y as centers
+        return distance_pass(ctx, X, Y, m, msr, prior, out, n * m, m, 1);
+    }
+    // out[i][j] = msr(lh = X[i], rh = Y[j]): the rows of Y against X (densified) as centers
+    DevMatrix M;
+    DBuf<float> own;
+    const float *Xd = nullptr;
+    MC_TRY(dense_rows(X, ctx->stream, ctx->sms, M, own, &Xd));
+    mc_matrix Ym{MC_DENSE_F32, 0, m, d, Y, nullptr, nullptr, 0};
+    return distance_pass(ctx, &Ym, Xd, n, msr, prior, out, n * m, m, 2);
+}
+
+int mc_pcmp(mc_context *ctx, const mc_matrix *X, int msr, double prior, float *out) {
+    if (!ctx || !X || !out) return fail(MC_EINVAL, "null argument");
+    if (!measure_supported(msr)) return fail(MC_EUNSUPPORTED, "measure not implemented on this path");
+    MC_CUDA_TRY(cudaSetDevice(ctx->device));
+    const uint64_t n = X->nrows;
+    if (n < 2) return MC_OK;
+    // condensed entry (i < j) = msr(lh = row i, rh = row j): rows of X against X as centers
+    DevMatrix M;
+    DBuf<float> own;
+    const float *Xd = nullptr;
+    MC_TRY(dense_rows(X, ctx->stream, ctx->sms, M, own, &Xd));
+    return distance_pass(ctx, X, Xd, n, msr, prior, out, n * (n - 1) / 2, n, 3);
 }
 
 int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr, double prior,

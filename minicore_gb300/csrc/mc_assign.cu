@@ -370,7 +370,14 @@ __global__ void __launch_bounds__(256) k_assign_tiled(AssignArgs a) {
             const uint32_t c = cbase + tx * TN + j;
             if (c < a.k) {
 #pragma unroll
-                for (int i = 0; i < TM; ++i) best_offer(best[i], finish_key<MSR>(acc[i][j]), c);
+                for (int i = 0; i < TM; ++i) {
+                    const float key = finish_key<MSR>(acc[i][j]);
+                    best_offer(best[i], key, c);
+                    if (a.dmode) {
+                        const uint64_t row = row0 + ty * TM + i;
+                        if (row < a.n) write_dist(a, a.rows ? uint64_t(a.rows[row]) : row, c, float(key_to_cost<MSR>(key)));
+                    }
+                }
             }
         }
     }
@@ -530,6 +537,7 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
                         key = float(k0 + double(acc[r])) * 0.5f;
                     }
                     best_offer(best, key, c);
+                    if (a.dmode) write_dist(a, row, c, float(key_to_cost<MSR>(key)));
                 }
             }
         }

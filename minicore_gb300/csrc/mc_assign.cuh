@@ -25,7 +25,24 @@ struct AssignArgs {
     double prior = 0.0, prior_sum = 0.0;
     uint32_t *asn = nullptr;
     double *costs = nullptr;
+    // optional distance output (cmp / pcmp): every pair's distance as float
+    //   dmode 1: dmat[row * ldm + c]   2: dmat[c * ldm + row]
+    //   dmode 3: condensed upper triangle, pairs c < row at c*ldm - c(c+1)/2 + row - c - 1
+    float *dmat = nullptr;
+    uint64_t ldm = 0;
+    int dmode = 0;
 };
+
+__device__ __forceinline__ void write_dist(const AssignArgs &a, uint64_t row, uint32_t c, float v) {
+    if (a.dmode == 1) {
+        a.dmat[row * a.ldm + c] = v;
+    } else if (a.dmode == 2) {
+        a.dmat[uint64_t(c) * a.ldm + row] = v;
+    } else if (a.dmode == 3 && uint64_t(c) < row) {
+        const uint64_t cc = c;
+        a.dmat[cc * a.ldm - cc * (cc + 1) / 2 + row - cc - 1] = v;
+    }
+}
 
 int launch_prep_centers(const AssignArgs &a, const float *C, bool pair, bool sparse_consts, cudaStream_t st);
 int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, float *rsi, float *rinc,
