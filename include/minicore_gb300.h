@@ -144,6 +144,13 @@ int mc_pcmp(mc_context *ctx, const mc_matrix *X, int msr, double prior, float *o
 int mc_sampler_create(mc_context *ctx, uint64_t np, uint64_t ncenters, uint64_t k,
                       const void *costs, int costs_f64, const uint32_t *asn, const float *weights,
                       int method, double alpha_est, mc_sampler **out);
+/* A sampler over stored probabilities (what CoresetSampler::read restores,
+ * coreset.h:306-338): the alias table is rebuilt, sampling is the plain form.  weights:
+ * optional float32 per point. */
+int mc_sampler_from_probs(mc_context *ctx, uint64_t np, const float *probs, const float *weights,
+                          mc_sampler **out);
+int mc_sampler_info(mc_sampler *s, uint64_t *np, int *method, int *has_weights);
+int mc_sampler_weights(mc_sampler *s, float *weights);   /* MC_EINVAL without weights */
 int mc_sampler_destroy(mc_sampler *s);
 int mc_sampler_probs(mc_sampler *s, float *probs);
 int mc_sampler_alias(mc_sampler *s, double *prob_table, uint32_t *alias_table);

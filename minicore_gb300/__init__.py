@@ -25,7 +25,9 @@ Differences from the reference, by design:
 from __future__ import annotations
 
 import ctypes
+import gzip
 import os
+import struct
 import threading
 
 import numpy as np
@@ -461,6 +463,54 @@ class CoresetSampler:
         check(_lib.load().mc_sampler_sample(self._h, size, _seed(seed), int(bool(unique)), _p(wo), _p(io)))
         return wo, io
 
+    # ---- on-disk form (coreset.h:279-338): uint64 n, uint64 seed, float32 probs[n],
+    # uint32 137 (weights follow: float32[n]) or 0.  Written gzip-compressed as the
+    # reference's path-based write does (gzopen); read from gzip or plain files.
+    def write(self, path):
+        if self._h is None:
+            raise ValueError("no sampler to write")
+        if getattr(self, "sens_", 0) == FL:
+            raise RuntimeError("Not implemented: serialization for FL coreset samplers")
+        lib = _lib.load()
+        probs = self.get_probs()
+        hw = ctypes.c_int()
+        check(lib.mc_sampler_info(self._h, None, None, ctypes.byref(hw)))
+        parts = [struct.pack("<QQ", self.np_, getattr(self, "seed_", 137) & 0xFFFFFFFFFFFFFFFF), probs.tobytes()]
+        if hw.value:
+            w = np.empty(self.np_, dtype=np.float32)
+            check(lib.mc_sampler_weights(self._h, _p(w)))
+            parts += [struct.pack("<I", 137), w.tobytes()]
+        else:
+            parts.append(struct.pack("<I", 0))
+        with gzip.open(path, "wb") as f:
+            f.write(b"".join(parts))
+
+    def read(self, path):
+        raw = _read_maybe_gz(path)
+        if len(raw) < 20:
+            raise RuntimeError("Failed to read from file")
+        n, seed = struct.unpack_from("<QQ", raw, 0)
+        off = 16
+        if len(raw) < off + 4 * n + 4:
+            raise RuntimeError("Failed to read from file")
+        probs = np.frombuffer(raw, dtype=np.float32, count=n, offset=off).copy()
+        off += 4 * n
+        (present,) = struct.unpack_from("<I", raw, off)
+        off += 4
+        w = None
+        if present:
+            if present != 137 or len(raw) < off + 4 * n:
+                raise RuntimeError("Failed to read from file")
+            w = np.frombuffer(raw, dtype=np.float32, count=n, offset=off).copy()
+        self._release()
+        h = ctypes.c_void_p()
+        check(_lib.load().mc_sampler_from_probs(self._ctx.handle, n, _p(probs), _p(w), ctypes.byref(h)))
+        self._h = h
+        self.np_ = int(n)
+        self.seed_ = int(seed)
+        self.sens_ = BFL
+        return self
+
     def _release(self):
         if self._h is not None:
             _lib.load().mc_sampler_destroy(self._h)
@@ -471,6 +521,64 @@ class CoresetSampler:
             self._release()
         except Exception:
             pass
+
+
+def _read_maybe_gz(path) -> bytes:
+    with open(path, "rb") as f:
+        head = f.read(2)
+    if head == b"\x1f\x8b":
+        with gzip.open(path, "rb") as f:
+            return f.read()
+    with open(path, "rb") as f:
+        return f.read()
+
+
+class IndexCoreset:
+    """Indices and weights of a sampled coreset (IndexCoreset<IT, FT>,
+    include/minicore/coreset/coreset.h:79-178).  On disk: uint64 size, IT indices[size],
+    FT weights[size] (written gzip-compressed; read from gzip or plain files)."""
+
+    def __init__(self, indices=None, weights=None, itype=np.uint32, ftype=np.float32):
+        self.itype, self.ftype = np.dtype(itype), np.dtype(ftype)
+        self.indices = np.asarray([] if indices is None else indices).astype(self.itype)
+        self.weights = np.asarray([] if weights is None else weights).astype(self.ftype)
+        if self.indices.shape != self.weights.shape:
+            raise ValueError("indices and weights differ in length")
+
+    def size(self):
+        return int(self.indices.size)
+
+    def write(self, path):
+        with gzip.open(path, "wb") as f:
+            f.write(struct.pack("<Q", self.size()) + self.indices.tobytes() + self.weights.tobytes())
+
+    def read(self, path):
+        raw = _read_maybe_gz(path)
+        if len(raw) < 8:
+            raise RuntimeError("Failed to read from file")
+        (n,) = struct.unpack_from("<Q", raw, 0)
+        ib, fb = self.itype.itemsize * n, self.ftype.itemsize * n
+        if len(raw) < 8 + ib + fb:
+            raise RuntimeError("Failed to read from file")
+        self.indices = np.frombuffer(raw, dtype=self.itype, count=n, offset=8).copy()
+        self.weights = np.frombuffer(raw, dtype=self.ftype, count=n, offset=8 + ib).copy()
+        return self
+
+    def compact(self):
+        """Merge repeated (index, weight) pairs into one entry of weight count * weight,
+        ordered by (index, weight); unchanged when every pair is distinct (coreset.h:138-163)."""
+        pairs = {}
+        for i, w in zip(self.indices.tolist(), self.weights.tolist()):
+            key = (i, w)
+            pairs[key] = pairs.get(key, 0) + 1
+        if len(pairs) == self.size():
+            return self
+        keys = sorted(pairs)
+        self.indices = np.array([k[0] for k in keys], dtype=self.itype)
+        # count * weight in the weight type, as the reference multiplies
+        self.weights = (np.array([pairs[k] for k in keys], dtype=self.ftype) *
+                        np.array([k[1] for k in keys], dtype=self.ftype)).astype(self.ftype)
+        return self
 
 
 # ------------------------------------------------------------------------------------

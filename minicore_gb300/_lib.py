@@ -52,6 +52,9 @@ SIGNATURES = {
     "mc_pcmp": (I, [P, P, I, D, P]),
     "mc_hcluster": (I, [P, P, P, U32, I, D, P, D, U64, U64, I, P, P, P, P, P, P]),
     "mc_sampler_create": (I, [P, U64, U64, U64, P, I, P, P, I, D, ctypes.POINTER(P)]),
+    "mc_sampler_from_probs": (I, [P, U64, P, P, ctypes.POINTER(P)]),
+    "mc_sampler_info": (I, [P, ctypes.POINTER(U64), ctypes.POINTER(I), ctypes.POINTER(I)]),
+    "mc_sampler_weights": (I, [P, P]),
     "mc_sampler_destroy": (I, [P]),
     "mc_sampler_probs": (I, [P, P]),
     "mc_sampler_alias": (I, [P, P, P]),

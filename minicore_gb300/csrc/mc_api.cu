@@ -931,6 +931,50 @@ int mc_sampler_create(mc_context *ctx, uint64_t np, uint64_t ncenters, uint64_t 
     return MC_OK;
 }
 
+// A sampler over given probabilities (the state CoresetSampler::read restores,
+// coreset.h:306-338): the alias table is rebuilt from them; sampling is the plain (non-FL)
+// form.  weights: optional float32 per point.
+int mc_sampler_from_probs(mc_context *ctx, uint64_t np, const float *probs, const float *weights, mc_sampler **out) {
+    if (!ctx || !out || !probs) return fail(MC_EINVAL, "null argument");
+    if (np == 0) return fail(MC_EINVAL, "empty input");
+    if (np >= (1ull << 32)) return fail(MC_EINVAL, "more than 2^32-1 points");
+    MC_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    std::unique_ptr<mc_sampler> s(new mc_sampler());
+    s->ctx = ctx;
+    s->np = np;
+    s->method = MC_BFL;
+    MC_TRY(s->probs.alloc(np, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(s->probs.p, probs, np * sizeof(float), cudaMemcpyDefault, st));
+    if (weights) {
+        MC_TRY(s->wf.alloc(np, st));
+        MC_TRY(s->wt_d.alloc(np, st));
+        MC_CUDA_TRY(cudaMemcpyAsync(s->wf.p, weights, np * sizeof(float), cudaMemcpyDefault, st));
+        MC_TRY(launch_to_double(s->wf.p, np, s->wt_d.p, st));
+    }
+    MC_TRY(s->prob_tab.alloc(np, st));
+    MC_TRY(s->alias.alloc(np, st));
+    MC_TRY(build_alias(s->probs.p, np, s->prob_tab.p, s->alias.p, s->aw, st, ctx->sms));
+    MC_TRY(sync(st));
+    *out = s.release();
+    return MC_OK;
+}
+
+int mc_sampler_info(mc_sampler *s, uint64_t *np, int *method, int *has_weights) {
+    if (!s) return fail(MC_EINVAL, "sampler is null");
+    if (np) *np = s->np;
+    if (method) *method = s->method;
+    if (has_weights) *has_weights = s->wf.p ? 1 : 0;
+    return MC_OK;
+}
+
+int mc_sampler_weights(mc_sampler *s, float *weights) {
+    if (!s || !weights) return fail(MC_EINVAL, "null argument");
+    if (!s->wf.p) return fail(MC_EINVAL, "the sampler has no weights");
+    MC_TRY(copy_out(weights, s->wf.p, s->np, s->ctx->stream));
+    return sync(s->ctx->stream);
+}
+
 int mc_sampler_destroy(mc_sampler *s) {
     if (!s) return MC_OK;
     cudaStreamSynchronize(s->ctx->stream);
