@@ -169,6 +169,25 @@ int mc_job_cost(mc_job *job, double *cost);           /* FP64 objective of curre
 int mc_job_run(mc_job *job, double eps, uint64_t maxiter, double *initcost, double *finalcost,
                uint64_t *numiter);                    /* the perform_hard_clustering loop */
 int mc_job_read(mc_job *job, float *centers, uint32_t *asn, double *costs);
+/* Minibatch hard clustering on a job (perform_hard_minibatch_clustering,
+ * clustering/solve.h:386-582): every calc_cost_freq iterations (and at the last) an
+ * exhaustive assignment, restarts of the centers holding <= reseed_after rows (D^2 draws
+ * U(seed, r) over the costs), and the objective; between them, a sample of mbsize rows
+ * (U(seed ^ 0x6A09E667F3BCC908, t), with or without replacement) is assigned and every hit
+ * center is replaced by its group's mean.  Distances use the prior as the prior sum, as
+ * the reference's minibatch code does.  The centers of the best objective are kept; asn and
+ * costs are those of the last exhaustive assignment. */
+int mc_job_minibatch(mc_job *job, uint64_t mbsize, uint64_t maxiter, uint64_t calc_cost_freq,
+                     uint64_t reseed_after, int with_replacement, double *initcost, double *finalcost,
+                     uint64_t *numiter);
+/* hcluster with mbsize > 0 (python/pycluster.h:31-40): checkin frequency
+ * ceil(maxiter / ncheckins), ncheckins 0 -> 10. */
+int mc_hcluster_minibatch(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k,
+                          int msr, double prior, const double *weights, uint64_t mbsize,
+                          uint64_t maxiter, uint64_t ncheckins, uint64_t reseed_count,
+                          int with_replacement, uint64_t seed, int precision, float *centers_out,
+                          uint32_t *asn, double *costs, double *initcost, double *finalcost,
+                          uint64_t *numiter);
 /* rows whose BF16/TF32 margin fell below the bound in the last pass (0 for FP32) */
 int mc_job_recheck_count(mc_job *job, uint64_t *count);
 /* A job whose k centers are seeded on the device by D^2 sampling with uniforms U(seed, i),

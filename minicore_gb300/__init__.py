@@ -306,9 +306,12 @@ def _centers_to_csr(C: np.ndarray):
 def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxiter=1000, mbsize=-1,
              ncheckins=-1, with_rep=False, cs=False, seed=0, reseed_count=5, precision="fp32",
              ctx: Context | None = None):
-    """Hard Lloyd/Bregman EM from explicit centers (clustering/solve.h:98-175)."""
-    if mbsize is not None and int(mbsize) > 0:
-        raise NotImplementedError("minibatch clustering is outside the implemented hot path")
+    """Hard Lloyd/Bregman EM from explicit centers (clustering/solve.h:98-175); with
+    mbsize >= 0, minibatch EM (solve.h:386-582) with maxiter iterations, a check-in every
+    ceil(maxiter / ncheckins), restarts of centers holding <= reseed_count rows, and
+    with_rep sampling."""
+    if cs:
+        raise NotImplementedError("coreset minibatch clustering (cs=True) is outside the implemented path")
     ctx = ctx or default_context()
     M = _MatrixArg(matrix)
     C = _centers_array(M, centers)
@@ -320,9 +323,18 @@ def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxit
     asn = np.empty(M.n, dtype=np.uint32)
     costs = np.empty(M.n, dtype=np.float64)
     ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
-    check(_lib.load().mc_hcluster(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(eps),
-                                  int(maxiter), _seed(seed), _PREC[precision], _p(cout), _p(asn), _p(costs),
-                                  ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
+    if mbsize is not None and int(mbsize) >= 0:
+        # perform_hard_minibatch_clustering (python/pycluster.h:31-40): ncheckins < 0 -> 10
+        nchk = int(ncheckins) if ncheckins is not None and int(ncheckins) > 0 else 10
+        check(_lib.load().mc_hcluster_minibatch(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w),
+                                                max(int(mbsize), 1), int(maxiter), nchk, int(reseed_count),
+                                                int(bool(with_rep)), _seed(seed), _PREC[precision], _p(cout),
+                                                _p(asn), _p(costs), ctypes.byref(ic), ctypes.byref(fc),
+                                                ctypes.byref(it)))
+    else:
+        check(_lib.load().mc_hcluster(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(eps),
+                                      int(maxiter), _seed(seed), _PREC[precision], _p(cout), _p(asn), _p(costs),
+                                      ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
     centers_out = cout if M.kind == _lib.MC_DENSE_F32 else _centers_to_csr(cout)
     return {"initcost": ic.value, "finalcost": fc.value, "numiter": it.value, "centers": centers_out,
             "costs": costs.astype(np.float32), "asn": asn}

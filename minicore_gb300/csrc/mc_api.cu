@@ -388,6 +388,134 @@ int job_set_centroids(mc_job *j, int *restarted) {
 
 }  // namespace
 
+namespace {
+
+__global__ void k_gather_dense_rows(const float *__restrict__ X, uint64_t d, const uint32_t *__restrict__ rows,
+                                    uint64_t m, float *out) {
+    const uint64_t total = m * d;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x))
+        out[e] = X[uint64_t(rows[e / d]) * d + e % d];
+}
+
+__global__ void k_gather_row_lens(const uint64_t *__restrict__ indptr, const uint32_t *__restrict__ rows, uint64_t m,
+                                  uint64_t *lens) {
+    const uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (t < m) lens[t] = indptr[rows[t] + 1] - indptr[rows[t]];
+}
+
+__global__ void k_gather_csr_rows(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                                  const uint64_t *__restrict__ indptr, const uint32_t *__restrict__ rows, uint64_t m,
+                                  const uint64_t *__restrict__ subptr, float *ovals, uint32_t *oidx) {
+    const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (uint64_t t = warp; t < m; t += (gridDim.x * uint64_t(blockDim.x)) >> 5) {
+        const uint64_t b = indptr[rows[t]], e = indptr[rows[t] + 1], o = subptr[t];
+        for (uint64_t p = b + lane; p < e; p += 32) {
+            ovals[o + p - b] = vals[p];
+            oidx[o + p - b] = idx[p];
+        }
+    }
+}
+
+__global__ void k_gather_f64(const double *__restrict__ v, const uint32_t *__restrict__ rows, uint64_t m, double *out) {
+    const uint64_t t = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (t < m) out[t] = v[rows[t]];
+}
+
+// rows whose best restarted center beats their current cost take it (strict <; the
+// restarted centers were searched in ascending order)
+__global__ void k_merge_restarts(uint64_t n, const uint32_t *__restrict__ sub_asn, const double *__restrict__ sub_cost,
+                                 const uint32_t *__restrict__ found, uint32_t *asn, double *costs) {
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (i < n && sub_cost[i] < costs[i]) {
+        asn[i] = found[sub_asn[i]];
+        costs[i] = sub_cost[i];
+    }
+}
+
+__global__ void k_gather_center_rows(const float *__restrict__ C, uint64_t d, const uint32_t *__restrict__ ids,
+                                     uint64_t m, float *out) {
+    const uint64_t total = m * d;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x))
+        out[e] = C[uint64_t(ids[e / d]) * d + e % d];
+}
+
+// Sample of the minibatch (the definition the oracle shares): U(seed ^ 0x6A09E667F3BCC908,
+// counter++) -> floor(u * n); with replacement mbsize draws, otherwise draws until mbsize
+// distinct rows (at most n); returned ascending (repeats adjacent).
+std::vector<uint32_t> minibatch_sample(uint64_t seed, uint64_t &counter, uint64_t n, uint64_t mbsize, bool with_rep) {
+    const uint64_t s = seed ^ 0x6A09E667F3BCC908ull;
+    std::vector<uint32_t> out;
+    auto draw = [&]() {
+        uint64_t r = uint64_t(uniform_at(s, counter++) * double(n));
+        return uint32_t(r >= n ? n - 1 : r);
+    };
+    if (with_rep) {
+        out.resize(mbsize);
+        for (auto &v : out) v = draw();
+    } else {
+        const uint64_t target = std::min(mbsize, n);
+        std::vector<uint8_t> seen;
+        std::map<uint32_t, bool> seen_sparse;
+        const bool dense_mark = n <= (uint64_t(64) << 20);
+        if (dense_mark) seen.assign(n, 0);
+        while (out.size() < target) {
+            const uint32_t r = draw();
+            if (dense_mark) {
+                if (seen[r]) continue;
+                seen[r] = 1;
+            } else {
+                if (seen_sparse.count(r)) continue;
+                seen_sparse[r] = true;
+            }
+            out.push_back(r);
+        }
+    }
+    std::sort(out.begin(), out.end());
+    return out;
+}
+
+// the job's rows restricted to `rows` (device list of m ids) as a compact device matrix
+struct SubRows {
+    DBuf<float> X, vals;
+    DBuf<uint32_t> idx;
+    DBuf<uint64_t> lens, indptr;
+    DBuf<double> w;
+};
+
+int gather_job_rows(mc_job *j, const uint32_t *rows, uint64_t m, SubRows &s, mc_matrix *out) {
+    cudaStream_t st = j->st;
+    const uint64_t d = j->M.d;
+    if (j->w.p) {
+        MC_TRY(s.w.alloc(m, st));
+        k_gather_f64<<<unsigned((m + 255) / 256), 256, 0, st>>>(j->w.p, rows, m, s.w.p), note_launch();
+    }
+    if (j->M.kind == MC_DENSE_F32) {
+        MC_TRY(s.X.alloc(m * d, st));
+        k_gather_dense_rows<<<unsigned(umin64((m * d + 255) / 256, 65535)), 256, 0, st>>>(j->M.X, d, rows, m, s.X.p),
+            note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        *out = mc_matrix{MC_DENSE_F32, 0, m, d, s.X.p, nullptr, nullptr, 0};
+        return MC_OK;
+    }
+    MC_TRY(s.lens.alloc(m, st));
+    MC_TRY(s.indptr.alloc(m + 1, st));
+    k_gather_row_lens<<<unsigned((m + 255) / 256), 256, 0, st>>>(j->M.indptr, rows, m, s.lens.p), note_launch();
+    MC_TRY(launch_exclusive_scan_u64(s.lens.p, s.indptr.p, m, st));
+    uint64_t nnz = 0;
+    MC_CUDA_TRY(cudaMemcpyAsync(&nnz, s.indptr.p + m, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MC_TRY(sync(st));
+    MC_TRY(s.vals.alloc(nnz ? nnz : 1, st));
+    MC_TRY(s.idx.alloc(nnz ? nnz : 1, st));
+    k_gather_csr_rows<<<unsigned(umin64((m + 7) / 8, 4096)), 256, 0, st>>>(j->M.vals, j->M.idx, j->M.indptr, rows, m,
+                                                                         s.indptr.p, s.vals.p, s.idx.p), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    *out = mc_matrix{MC_CSR_F32, 0, m, d, s.vals.p, s.idx.p, s.indptr.p, nnz};
+    return MC_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char *mc_version(void) { return "minicore_gb300 0.1 (sm_103a)"; }
@@ -686,6 +814,143 @@ int mc_job_run(mc_job *j, double eps, uint64_t maxiter, double *initcost_out, do
     if (finalcost_out) *finalcost_out = cost;
     if (numiter_out) *numiter_out = iternum;
     return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// minibatch hard clustering (perform_hard_minibatch_clustering, clustering/solve.h:386-582)
+// ------------------------------------------------------------------------------------
+
+int mc_job_minibatch(mc_job *j, uint64_t mbsize, uint64_t maxiter, uint64_t calc_cost_freq, uint64_t reseed_after,
+                     int with_replacement, double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
+    if (!j) return fail(MC_EINVAL, "job is null");
+    if (mbsize == 0) return fail(MC_EINVAL, "mbsize must be positive");
+    if (maxiter == 0) return fail(MC_EINVAL, "maxiter must be positive");
+    if (calc_cost_freq == 0) calc_cost_freq = 1;
+    cudaStream_t st = j->st;
+    const uint64_t n = j->M.n, d = j->M.d;
+    const uint32_t k = j->k;
+    const size_t cbytes = uint64_t(k) * d * sizeof(float);
+    // every distance in this routine takes the prior itself as the prior sum, as the
+    // reference's minibatch code does (solve.h:405: prior.size() * prior[0])
+    const double psum_mb = double(float(j->prior));
+    DBuf<float> save;
+    MC_TRY(save.alloc(uint64_t(k) * d, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(save.p, j->C.p, cbytes, cudaMemcpyDeviceToDevice, st));
+    MC_TRY(j->idxbuf.alloc(uint64_t(k) + 2, st));
+    DBuf<uint32_t> rows_dev, found_dev;
+    DBuf<float> Cs;
+    double initcost = 0.0, bestcost = 0.0, cost = 0.0;
+    uint64_t iternum = 0, sample_counter = 0;
+    for (;;) {
+        if (iternum % calc_cost_freq == 0 || iternum == maxiter - 1) {
+            // exhaustive assignment; restart the centers holding few rows
+            MC_TRY(job_assign_with(j, j->C.p, psum_mb, false));
+            MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+            std::vector<uint64_t> cnt(k);
+            MC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), j->sort.bucket_count.p, k * sizeof(uint64_t),
+                                        cudaMemcpyDeviceToHost, st));
+            MC_TRY(sync(st));
+            std::vector<uint32_t> found;
+            for (uint32_t c = 0; c < k; ++c)
+                if (cnt[c] <= reseed_after) found.push_back(c);
+            if (!found.empty()) {
+                for (uint32_t c : found) {
+                    const double u = uniform_at(j->seed, j->restart_counter++);
+                    DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
+                    MC_TRY(launch_det_draw(in, j->det_tmp.p, nullptr, u, 0, nullptr, j->idxbuf.p + k, st));
+                    float *dst = j->C.p + uint64_t(c) * d;
+                    if (j->M.kind == MC_DENSE_F32) {
+                        k_copy_row_dense<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(
+                            j->M.X, d, j->idxbuf.p + k, dst), note_launch();
+                    } else {
+                        k_copy_row_csr_zero<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(d, dst), note_launch();
+                        k_copy_row_csr<<<64, 256, 0, st>>>(j->M.vals, j->M.idx, j->M.indptr, j->idxbuf.p + k, dst),
+                            note_launch();
+                    }
+                    MC_CUDA_TRY(cudaGetLastError());
+                }
+                // every row against the restarted centers only; better ones take over
+                const uint64_t nf = found.size();
+                MC_TRY(found_dev.alloc(nf, st));
+                MC_CUDA_TRY(cudaMemcpyAsync(found_dev.p, found.data(), nf * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+                MC_TRY(Cs.alloc(nf * d, st));
+                k_gather_center_rows<<<unsigned(umin64((nf * d + 255) / 256, 65535)), 256, 0, st>>>(j->C.p, d,
+                                                                                                  found_dev.p, nf, Cs.p),
+                    note_launch();
+                mc_matrix all{j->M.kind, 0, n, d, j->M.kind == MC_DENSE_F32 ? j->M.X : j->M.vals, j->M.idx,
+                              j->M.indptr, j->M.nnz};
+                mc_job *rj = nullptr;
+                MC_TRY(job_create_impl(j->ctx, &all, Cs.p, uint32_t(nf), j->msr, j->prior, nullptr, MC_FP32, j->seed,
+                                       nullptr, &rj));
+                std::unique_ptr<mc_job, int (*)(mc_job *)> rguard(rj, mc_job_destroy);
+                MC_TRY(job_assign_with(rj, rj->C.p, psum_mb, true));
+                k_merge_restarts<<<unsigned((n + 255) / 256), 256, 0, st>>>(n, rj->asn.p, rj->costs.p, found_dev.p,
+                                                                            j->asn.p, j->costs.p), note_launch();
+                MC_CUDA_TRY(cudaGetLastError());
+            }
+            DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
+            MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(&cost, j->scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MC_TRY(sync(st));
+            if (iternum == 0) initcost = bestcost = cost;
+            if (cost < bestcost) {
+                bestcost = cost;
+                MC_CUDA_TRY(cudaMemcpyAsync(save.p, j->C.p, cbytes, cudaMemcpyDeviceToDevice, st));
+            }
+        }
+        if (++iternum == maxiter) break;
+        // sample, assign the sampled rows exactly, replace every hit center by its group's mean
+        const std::vector<uint32_t> smp = minibatch_sample(j->seed, sample_counter, n, mbsize, with_replacement != 0);
+        const uint64_t m = smp.size();
+        MC_TRY(rows_dev.alloc(m, st));
+        MC_CUDA_TRY(cudaMemcpyAsync(rows_dev.p, smp.data(), m * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        SubRows sr;
+        mc_matrix subm;
+        MC_TRY(gather_job_rows(j, rows_dev.p, m, sr, &subm));
+        mc_job *sj = nullptr;
+        MC_TRY(job_create_impl(j->ctx, &subm, j->C.p, k, j->msr, j->prior, sr.w.p, MC_FP32, j->seed, nullptr, &sj));
+        std::unique_ptr<mc_job, int (*)(mc_job *)> sguard(sj, mc_job_destroy);
+        MC_TRY(job_assign_with(sj, sj->C.p, psum_mb, true));
+        CentroidArgs ca;
+        ca.csr = sj->M.kind == MC_CSR_F32;
+        ca.n = m;
+        ca.d = d;
+        ca.k = k;
+        ca.X = sj->M.X;
+        ca.vals = sj->M.vals;
+        ca.idx = sj->M.idx;
+        ca.indptr = sj->M.indptr;
+        ca.keys = sj->asn.p;
+        ca.w = sj->w.p;
+        ca.centers = j->C.p;  // groups with no sampled row keep their center
+        ca.nan_flag = j->flag.p;
+        MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), st));
+        MC_TRY(launch_centroids(ca, sj->sort, st));
+        int nanf = 0;
+        MC_CUDA_TRY(cudaMemcpyAsync(&nanf, j->flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MC_TRY(sync(st));
+        if (nanf) return fail(MC_ENAN, "Unexpected nan in ctr");
+    }
+    MC_CUDA_TRY(cudaMemcpyAsync(j->C.p, save.p, cbytes, cudaMemcpyDeviceToDevice, st));
+    MC_TRY(sync(st));
+    if (initcost_out) *initcost_out = initcost;
+    if (finalcost_out) *finalcost_out = bestcost;
+    if (numiter_out) *numiter_out = iternum;
+    return MC_OK;
+}
+
+int mc_hcluster_minibatch(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
+                          double prior, const double *weights, uint64_t mbsize, uint64_t maxiter, uint64_t ncheckins,
+                          uint64_t reseed_count, int with_replacement, uint64_t seed, int precision,
+                          float *centers_out, uint32_t *asn, double *costs, double *initcost, double *finalcost,
+                          uint64_t *numiter) {
+    mc_job *j = nullptr;
+    MC_TRY(mc_job_create(ctx, X, centers_in, k, msr, prior, weights, precision, seed, &j));
+    std::unique_ptr<mc_job, int (*)(mc_job *)> guard(j, mc_job_destroy);
+    if (ncheckins == 0) ncheckins = 10;
+    const uint64_t freq = (maxiter + ncheckins - 1) / ncheckins;  // pycluster.h:36-37
+    MC_TRY(mc_job_minibatch(j, mbsize, maxiter, freq, reseed_count, with_replacement, initcost, finalcost, numiter));
+    return mc_job_read(j, centers_out, asn, costs);
 }
 
 int mc_job_read(mc_job *j, float *centers, uint32_t *asn, double *costs) {

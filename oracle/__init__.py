@@ -62,6 +62,7 @@ def lib():
             "orc_assign": (I, [P, P, U32, I, D, P, P]),
             "orc_kmeanspp": (I, [P, U32, I, D, P, P, P, P, P]),
             "orc_hcluster": (I, [P, P, U32, I, D, P, D, U64, U64, P, P, P, P, P, P]),
+            "orc_minibatch": (I, [P, P, U32, I, D, P, U64, U64, U64, U64, I, U64, P, P, P, P, P, P]),
             "orc_sensitivity": (I, [U64, U64, U64, P, I, P, P, I, D, P]),
             "orc_alias_build": (I, [U64, P, P, P]),
             "orc_alias_draw": (U64, [U64, P, P, U64, U64]),
@@ -183,6 +184,24 @@ def hcluster(X, centers, msr, prior, weights=None, eps=1e-10, maxiter=100, seed=
         raise RuntimeError("Unexpected nan in ctr")
     return dict(initcost=ic.value, finalcost=fc.value, numiter=it.value, centers=cout, asn=asn,
                 costs=costs)
+
+
+def minibatch(X, centers, msr, prior, weights=None, mbsize=100, maxiter=20, freq=5, reseed_after=1,
+              with_rep=False, seed=1):
+    M = Matrix(X)
+    C = np.ascontiguousarray(centers, dtype=np.float32)
+    k = C.shape[0]
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    cout = np.empty_like(C)
+    asn = np.empty(M.n, dtype=np.uint32)
+    costs = np.empty(M.n, dtype=np.float64)
+    ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+    rc = lib().orc_minibatch(M.ref(), _p(C), k, msr, prior, _p(w), mbsize, maxiter, freq, reseed_after,
+                             int(bool(with_rep)), seed, _p(cout), _p(asn), _p(costs), ctypes.byref(ic),
+                             ctypes.byref(fc), ctypes.byref(it))
+    if rc == 2:
+        raise RuntimeError("Unexpected nan in ctr")
+    return dict(initcost=ic.value, finalcost=fc.value, numiter=it.value, centers=cout, asn=asn, costs=costs)
 
 
 def sensitivity(costs, asn, ncenters, method, weights=None, k=None, alpha_est=0.0):

@@ -34,6 +34,7 @@
 #include <functional>
 #include <limits>
 #include <map>
+#include <set>
 #include <numeric>
 #include <vector>
 
@@ -648,6 +649,118 @@ int orc_hcluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
     std::copy(asn.begin(), asn.end(), asn_out);
     std::copy(costs.begin(), costs.end(), costs_out);
     return rc;
+}
+
+// perform_hard_minibatch_clustering (clustering/solve.h:386-582).  Every freq iterations
+// (and at the last): exhaustive assignment, restart of centers with <= reseed_after rows
+// (D^2 draw U(seed, r) over the costs, all restarts from the same costs; then every row
+// takes the best restarted center if strictly cheaper), FP64 objective; between
+// checkins: a sample of rows (minibatch_sample below), each assigned exactly, and each
+// hit center replaced by the mean of its sampled rows (ascending, repeats included;
+// singletons copy the row).  Distances use the prior itself as the prior sum
+// (solve.h:405).  The centers of the best objective are returned.
+static std::vector<uint32_t> minibatch_sample(uint64_t seed, uint64_t &counter, uint64_t n, uint64_t mbsize,
+                                              bool with_rep) {
+    const uint64_t s = seed ^ 0x6A09E667F3BCC908ull;
+    std::vector<uint32_t> out;
+    auto draw = [&]() {
+        uint64_t r = uint64_t(uniform_at(s, counter++) * double(n));
+        return uint32_t(r >= n ? n - 1 : r);
+    };
+    if (with_rep) {
+        out.resize(mbsize);
+        for (auto &v : out) v = draw();
+    } else {
+        const uint64_t target = std::min(mbsize, n);
+        std::set<uint32_t> seen;
+        while (out.size() < target) {
+            const uint32_t r = draw();
+            if (seen.insert(r).second) out.push_back(r);
+        }
+    }
+    std::sort(out.begin(), out.end());
+    return out;
+}
+
+int orc_minibatch(const orc_matrix *mm, const float *centers_in, uint32_t k, int msr, double prior, const double *w,
+                  uint64_t mbsize, uint64_t maxiter, uint64_t freq, uint64_t reseed_after, int with_rep,
+                  uint64_t seed, float *centers_out, uint32_t *asn_out, double *costs_out, double *initcost_out,
+                  double *finalcost_out, uint64_t *numiter_out) {
+    const Mat m = to_mat(mm);
+    const uint64_t n = m.n, d = m.d;
+    const bool sparse = m.kind == 1;
+    if (freq == 0) freq = 1;
+    std::vector<double> rs(n);
+    for (uint64_t i = 0; i < n; ++i) rs[i] = row_sum(m, i);
+    const double psum = double(float(prior));
+    CenterSet C;
+    C.set_from_dense(centers_in, k, d, sparse);
+    std::vector<float> save = C.dense;
+    std::vector<uint32_t> asn(n);
+    std::vector<double> costs(n);
+    uint64_t rc = 0, sc = 0, iternum = 0;
+    double initcost = 0.0, bestcost = 0.0, cost = 0.0;
+    for (;;) {
+        if (iternum % freq == 0 || iternum == maxiter - 1) {
+            assign_all(m, C, msr, prior, psum, rs, asn.data(), costs.data());
+            std::vector<uint64_t> cnt(k, 0);
+            for (uint64_t i = 0; i < n; ++i) ++cnt[asn[i]];
+            std::vector<uint32_t> found;
+            for (uint32_t c = 0; c < k; ++c) if (cnt[c] <= reseed_after) found.push_back(c);
+            if (!found.empty()) {
+                for (uint32_t c : found) {
+                    const double u = uniform_at(seed, rc++);
+                    uint64_t r = w ? det_draw([&](uint64_t i) { return costs[i] * w[i]; }, n, u)
+                                   : det_draw([&](uint64_t i) { return costs[i]; }, n, u);
+                    if (r >= n) r = 0;
+                    C.set_row(c, dense_row(m, r), sparse);
+                }
+#pragma omp parallel for schedule(dynamic, 64)
+                for (int64_t i = 0; i < int64_t(n); ++i) {
+                    double best = dist_row_center(m, uint64_t(i), C, found[0], msr, prior, psum, rs[i]);
+                    uint32_t bc = found[0];
+                    for (size_t f = 1; f < found.size(); ++f) {
+                        const double v = dist_row_center(m, uint64_t(i), C, found[f], msr, prior, psum, rs[i]);
+                        if (v < best) { best = v; bc = found[f]; }
+                    }
+                    if (sparse) best = double(float(best));
+                    if (best < costs[i]) { costs[i] = best; asn[i] = bc; }
+                }
+            }
+            cost = w ? det_sum([&](uint64_t i) { return costs[i] * w[i]; }, n)
+                     : det_sum([&](uint64_t i) { return costs[i]; }, n);
+            if (iternum == 0) initcost = bestcost = cost;
+            if (cost < bestcost) { bestcost = cost; save = C.dense; }
+        }
+        if (++iternum == maxiter) break;
+        const std::vector<uint32_t> smp = minibatch_sample(seed, sc, n, mbsize, with_rep != 0);
+        std::vector<std::vector<uint64_t>> groups(k);
+        for (uint32_t r : smp) {
+            double best = dist_row_center(m, r, C, 0, msr, prior, psum, rs[r]);
+            uint32_t bc = 0;
+            for (uint32_t c = 1; c < k; ++c) {
+                const double v = dist_row_center(m, r, C, c, msr, prior, psum, rs[r]);
+                if (v < best) { best = v; bc = c; }
+            }
+            groups[bc].push_back(r);
+        }
+        std::vector<float> out(d);
+        for (uint32_t c = 0; c < k; ++c) {
+            const auto &g = groups[c];
+            if (g.empty()) continue;
+            if (g.size() == 1) { C.set_row(c, dense_row(m, g[0]), sparse); continue; }
+            mean_of_rows(m, g, w, out.data());
+            for (float v : out) if (std::isnan(v)) return 2;
+            C.set_row(c, out, sparse);
+        }
+    }
+    std::copy(save.begin(), save.end(), centers_out);
+    std::copy(asn.begin(), asn.end(), asn_out);
+    std::copy(costs.begin(), costs.end(), costs_out);
+    *initcost_out = initcost;
+    *finalcost_out = bestcost;
+    *numiter_out = iternum;
+    return 0;
 }
 
 // CoresetSampler (coreset.h:340-578).  The sampler keeps point weights as float
