@@ -188,6 +188,17 @@ int mc_hcluster_minibatch(mc_context *ctx, const mc_matrix *X, const float *cent
                           int with_replacement, uint64_t seed, int precision, float *centers_out,
                           uint32_t *asn, double *costs, double *initcost, double *finalcost,
                           uint64_t *numiter);
+/* Soft clustering (perform_soft_clustering, clustering/solve.h:287-374, with the soft
+ * weighted means of centroid.h:795-866) over dense rows: per iteration asn = row softmax of
+ * -temp * costs (NaN rows: equal shares over the minimal costs), objective sum_i w_i
+ * dot(costs_i, asn_i) (FP64), centers = soft weighted means, costs = msr(rows, centers).
+ * Stops when the objective improves by <= eps * max(old, new) or after maxiter iterations;
+ * centers are taken only on improvement.  costs_out / asn_out: nrows x k float32 (the last
+ * ones computed).  L1 (median centers) is not covered. */
+int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
+                double prior, const double *weights, double temp, uint64_t maxiter, double eps,
+                float *centers_out, float *costs_out, float *asn_out, double *initcost,
+                double *finalcost, uint64_t *numiter);
 /* rows whose BF16/TF32 margin fell below the bound in the last pass (0 for FP32) */
 int mc_job_recheck_count(mc_job *job, uint64_t *count);
 /* A job whose k centers are seeded on the device by D^2 sampling with uniforms U(seed, i),

@@ -340,6 +340,33 @@ def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxit
             "costs": costs.astype(np.float32), "asn": asn}
 
 
+def scluster(matrix, centers, msr=2, prior=0., temp=1., maxiter=1000, mbsize=-1, mbn=-1, savepref="",
+             weights=None, ctx: Context | None = None):
+    """Soft clustering from explicit centers (perform_soft_clustering, clustering/solve.h:287-374;
+    python/pycluster_softdense.cpp:66-90).  Returns initcost, finalcost, numiter, centers, and
+    the last (rows x k) float32 cost and soft-assignment matrices.  Dense rows; eps 1e-8."""
+    if mbsize is not None and int(mbsize) > 0:
+        raise NotImplementedError("Not yet completed: minibatch soft clustering")
+    if _is_sparse(matrix):
+        raise NotImplementedError("soft clustering of CSR rows is outside the implemented path")
+    ctx = ctx or default_context()
+    M = _MatrixArg(matrix)
+    C = _centers_array(M, centers)
+    k = C.shape[0]
+    if prior < 0:
+        prior = 0.
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    cout = np.empty_like(C)
+    costs = np.empty((M.n, k), dtype=np.float32)
+    asn = np.empty((M.n, k), dtype=np.float32)
+    ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+    check(_lib.load().mc_scluster(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(temp),
+                                  int(maxiter), 1e-8, _p(cout), _p(costs), _p(asn), ctypes.byref(ic),
+                                  ctypes.byref(fc), ctypes.byref(it)))
+    return {"initcost": ic.value, "finalcost": fc.value, "numiter": it.value, "centers": cout, "costs": costs,
+            "asn": asn}
+
+
 def cluster_from_centers(*args, **kwargs):
     return hcluster(*args, **kwargs)
 
@@ -347,13 +374,13 @@ def cluster_from_centers(*args, **kwargs):
 def cluster(data, *, msr, k, prior=0., seed=0, nmkc=0, ntimes=1, lspp=0, use_exponential_skips=False,
             n_local_trials=1, weights=None, mbsize=-1, clustereps=1e-4, temp=-1., cs=False, with_rep=True,
             outpref="mc.cluster.output", maxiter=50, precision="fp32"):
-    """kmeans++ then hcluster (minicore/__init__.py:235-261); soft clustering (temp > 0) is
-    outside the implemented hot path."""
-    if temp > 0:
-        raise NotImplementedError("Soft clustering not supported")
+    """kmeans++ then hcluster, or scluster when temp > 0 (minicore/__init__.py:235-261)."""
     seed = _seed(seed)
     ids, asn, costs = kmeanspp(data, k, msr=msr, prior=prior, seed=seed, ntimes=ntimes, lspp=lspp,
                                n_local_trials=n_local_trials, weights=weights)
+    if temp > 0:
+        return scluster(data, ids.astype(np.int64), msr=msr, prior=prior, temp=temp, maxiter=maxiter,
+                        weights=weights)
     return hcluster(data, ids.astype(np.int64), prior=prior, msr=msr, weights=weights, eps=clustereps,
                     maxiter=maxiter, seed=seed, precision=precision)
 

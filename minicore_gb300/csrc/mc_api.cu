@@ -8,6 +8,7 @@
 #include <mutex>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <vector>
 
@@ -516,6 +517,69 @@ int gather_job_rows(mc_job *j, const uint32_t *rows, uint64_t m, SubRows &s, mc_
 
 }  // namespace
 
+// ------------------------------------------------------------------------------------
+// soft clustering kernels (perform_soft_clustering, clustering/solve.h:287-374;
+// set_centroids_full_mean soft form, clustering/centroid.h:795-866)
+// ------------------------------------------------------------------------------------
+// per row: asn = softmax(-temp * costs) (max-shifted, sequential sums in float); a NaN in
+// the first entry is replaced by equal shares over the row's minimal costs (correct_softmax,
+// centroid.h:782-793); rowval = dot(costs, asn) (sequential float) as double
+__global__ void k_soft_rows(const float *__restrict__ costs, uint64_t n, uint32_t k, float temp, float *asn,
+                            double *rowval) {
+    const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    if (i >= n) return;
+    const float *cr = costs + i * k;
+    float *ar = asn + i * k;
+    float m = -temp * cr[0];
+    for (uint32_t c = 1; c < k; ++c) m = fmaxf(m, -temp * cr[c]);
+    float s = 0.f;
+    for (uint32_t c = 0; c < k; ++c) {
+        const float e = expf(-temp * cr[c] - m);
+        ar[c] = e;
+        s = s + e;
+    }
+    for (uint32_t c = 0; c < k; ++c) ar[c] = ar[c] / s;
+    if (ar[0] != ar[0]) {
+        float best = cr[0];
+        for (uint32_t c = 1; c < k; ++c) if (cr[c] < best) best = cr[c];
+        uint32_t ties = 0;
+        for (uint32_t c = 0; c < k; ++c) ties += (cr[c] == best) ? 1u : 0u;
+        const float per = 1.f / float(ties ? ties : 1u);
+        for (uint32_t c = 0; c < k; ++c) ar[c] = (cr[c] == best) ? per : 0.f;
+    }
+    float dot = 0.f;
+    for (uint32_t c = 0; c < k; ++c) dot = dot + cr[c] * ar[c];
+    rowval[i] = double(dot);
+}
+
+// soft weighted means: thread (c, j) walks the rows in chunks of 256 with a compensated
+// float sum of coef * x (coef = asn * float(w)), FP64 across chunks; center = num * (1/den)
+__global__ void k_soft_centers(const float *__restrict__ X, uint64_t n, uint64_t d, const float *__restrict__ asn,
+                               uint32_t k, const double *__restrict__ w, float *centers) {
+    const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    const uint32_t c = blockIdx.y;
+    if (j >= d || c >= k) return;
+    double num = 0.0, den = 0.0;
+    for (uint64_t r0 = 0; r0 < n; r0 += 256) {
+        const uint64_t r1 = umin64(n, r0 + 256);
+        float s = 0.f, e = 0.f, sw = 0.f, ew = 0.f;
+        for (uint64_t r = r0; r < r1; ++r) {
+            const float coef = w ? asn[r * k + c] * float(w[r]) : asn[r * k + c];
+            const float t = coef * X[r * d + j];
+            float tt = __fadd_rn(s, t), bp = __fsub_rn(tt, s);
+            e = __fadd_rn(e, __fadd_rn(__fsub_rn(s, __fsub_rn(tt, bp)), __fsub_rn(t, bp)));
+            s = tt;
+            tt = __fadd_rn(sw, coef);
+            bp = __fsub_rn(tt, sw);
+            ew = __fadd_rn(ew, __fadd_rn(__fsub_rn(sw, __fsub_rn(tt, bp)), __fsub_rn(coef, bp)));
+            sw = tt;
+        }
+        num = num + (double(s) + double(e));
+        den = den + (double(sw) + double(ew));
+    }
+    centers[uint64_t(c) * d + j] = float(num * (1.0 / den));
+}
+
 extern "C" {
 
 const char *mc_version(void) { return "minicore_gb300 0.1 (sm_103a)"; }
@@ -951,6 +1015,58 @@ int mc_hcluster_minibatch(mc_context *ctx, const mc_matrix *X, const float *cent
     const uint64_t freq = (maxiter + ncheckins - 1) / ncheckins;  // pycluster.h:36-37
     MC_TRY(mc_job_minibatch(j, mbsize, maxiter, freq, reseed_count, with_replacement, initcost, finalcost, numiter));
     return mc_job_read(j, centers_out, asn, costs);
+}
+
+int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr, double prior,
+                const double *weights, double temp, uint64_t maxiter, double eps, float *centers_out,
+                float *costs_out, float *asn_out, double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
+    if (!ctx || !X || !centers_in) return fail(MC_EINVAL, "null argument");
+    if (X->kind != MC_DENSE_F32) return fail(MC_EUNSUPPORTED, "soft clustering covers dense rows");
+    if (msr == L1) return fail(MC_EUNSUPPORTED, "soft L1 centers are medians (outside the implemented path)");
+    mc_job *j = nullptr;
+    MC_TRY(mc_job_create(ctx, X, centers_in, k, msr, prior, weights, MC_FP32, 1, &j));
+    std::unique_ptr<mc_job, int (*)(mc_job *)> guard(j, mc_job_destroy);
+    cudaStream_t st = j->st;
+    const uint64_t n = j->M.n, d = j->M.d;
+    const size_t cbytes = uint64_t(k) * d * sizeof(float);
+    DBuf<float> costs, asn;
+    DBuf<double> rowval;
+    MC_TRY(costs.alloc(n * k, st));
+    MC_TRY(asn.alloc(n * k, st));
+    MC_TRY(rowval.alloc(n, st));
+    DistOut o;
+    o.dmat = costs.p;
+    o.ldm = k;
+    o.dmode = 1;
+    // centers_cpy evolves in Cw; accepted centers in C
+    MC_CUDA_TRY(cudaMemcpyAsync(j->Cw.p, j->C.p, cbytes, cudaMemcpyDeviceToDevice, st));
+    MC_TRY(job_assign_with(j, j->Cw.p, j->psum, true, &o));
+    double cost = std::numeric_limits<double>::max(), initcost = -1.0;
+    uint64_t iternum = 0;
+    for (;;) {
+        const double oldcost = cost;
+        k_soft_rows<<<unsigned((n + 255) / 256), 256, 0, st>>>(costs.p, n, k, float(temp), asn.p, rowval.p),
+            note_launch();
+        DetInput in{j->w.p ? DET_F64_W : DET_F64, rowval.p, nullptr, j->w.p, n};
+        MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
+        k_soft_centers<<<dim3(unsigned((d + 127) / 128), k), 128, 0, st>>>(j->M.X, n, d, asn.p, k, j->w.p, j->Cw.p),
+            note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        MC_TRY(job_assign_with(j, j->Cw.p, j->psum, true, &o));
+        MC_CUDA_TRY(cudaMemcpyAsync(&cost, j->scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        MC_TRY(sync(st));
+        if (initcost < 0) initcost = cost;
+        if (oldcost >= cost) MC_CUDA_TRY(cudaMemcpyAsync(j->C.p, j->Cw.p, cbytes, cudaMemcpyDeviceToDevice, st));
+        if (oldcost - cost <= eps * std::max(oldcost, cost) || ++iternum == maxiter) break;
+    }
+    MC_TRY(copy_out(centers_out, j->C.p, uint64_t(k) * d, st));
+    MC_TRY(copy_out(costs_out, costs.p, n * k, st));
+    MC_TRY(copy_out(asn_out, asn.p, n * k, st));
+    MC_TRY(sync(st));
+    if (initcost_out) *initcost_out = initcost;
+    if (finalcost_out) *finalcost_out = cost;
+    if (numiter_out) *numiter_out = iternum;
+    return MC_OK;
 }
 
 int mc_job_read(mc_job *j, float *centers, uint32_t *asn, double *costs) {

@@ -62,6 +62,7 @@ def lib():
             "orc_assign": (I, [P, P, U32, I, D, P, P]),
             "orc_kmeanspp": (I, [P, U32, I, D, P, P, P, P, P]),
             "orc_hcluster": (I, [P, P, U32, I, D, P, D, U64, U64, P, P, P, P, P, P]),
+            "orc_scluster": (I, [P, P, U32, I, D, P, D, U64, D, P, P, P, P, P, P]),
             "orc_minibatch": (I, [P, P, U32, I, D, P, U64, U64, U64, U64, I, U64, P, P, P, P, P, P]),
             "orc_sensitivity": (I, [U64, U64, U64, P, I, P, P, I, D, P]),
             "orc_alias_build": (I, [U64, P, P, P]),
@@ -202,6 +203,22 @@ def minibatch(X, centers, msr, prior, weights=None, mbsize=100, maxiter=20, freq
     if rc == 2:
         raise RuntimeError("Unexpected nan in ctr")
     return dict(initcost=ic.value, finalcost=fc.value, numiter=it.value, centers=cout, asn=asn, costs=costs)
+
+
+def scluster(X, centers, msr, prior, weights=None, temp=1.0, maxiter=1000, eps=1e-8):
+    M = Matrix(X)
+    C = np.ascontiguousarray(centers, dtype=np.float32)
+    k = C.shape[0]
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    cout = np.empty_like(C)
+    costs = np.empty((M.n, k), dtype=np.float32)
+    asn = np.empty((M.n, k), dtype=np.float32)
+    ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+    rc = lib().orc_scluster(M.ref(), _p(C), k, msr, prior, _p(w), temp, maxiter, eps, _p(cout), _p(costs),
+                            _p(asn), ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it))
+    if rc:
+        raise ValueError("orc_scluster failed")
+    return dict(initcost=ic.value, finalcost=fc.value, numiter=it.value, centers=cout, costs=costs, asn=asn)
 
 
 def sensitivity(costs, asn, ncenters, method, weights=None, k=None, alpha_est=0.0):

@@ -763,6 +763,93 @@ int orc_minibatch(const orc_matrix *mm, const float *centers_in, uint32_t k, int
     return 0;
 }
 
+// perform_soft_clustering (clustering/solve.h:287-374) over dense rows with the soft
+// weighted means of set_centroids_full_mean (centroid.h:795-866): asn = row softmax of
+// -temp * costs (max-shifted, sequential float sums; a NaN first entry becomes equal shares
+// over the minimal costs, centroid.h:782-793), objective sum_i w_i dot(costs_i, asn_i) in the
+// canonical FP64 order, center_c = (sum_i coef x_i) * (1 / sum_i coef) with coef = asn *
+// float(w), compensated float sums over chunks of 256 rows and FP64 across chunks.
+int orc_scluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int msr, double prior, const double *w,
+                 double temp, uint64_t maxiter, double eps, float *centers_out, float *costs_out, float *asn_out,
+                 double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
+    const Mat m = to_mat(mm);
+    if (m.kind != 0) return 3;
+    const uint64_t n = m.n, d = m.d;
+    std::vector<double> rs(n);
+    for (uint64_t i = 0; i < n; ++i) rs[i] = row_sum(m, i);
+    const double psum = double(float(prior * double(d)));
+    CenterSet acc, cpy;
+    acc.set_from_dense(centers_in, k, d, false);
+    cpy = acc;
+    std::vector<float> costs(n * k), asn(n * k);
+    auto fill_costs = [&]() {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t i = 0; i < int64_t(n); ++i)
+            for (uint32_t c = 0; c < k; ++c)
+                costs[uint64_t(i) * k + c] = float(dist_row_center(m, uint64_t(i), cpy, c, msr, prior, psum, rs[i]));
+    };
+    fill_costs();
+    double cost = std::numeric_limits<double>::max(), initcost = -1.0;
+    uint64_t iternum = 0;
+    const float ft = float(temp);
+    std::vector<double> rowval(n);
+    for (;;) {
+        const double oldcost = cost;
+        for (uint64_t i = 0; i < n; ++i) {
+            const float *cr = &costs[i * k];
+            float *ar = &asn[i * k];
+            float mx = -ft * cr[0];
+            for (uint32_t c = 1; c < k; ++c) mx = std::max(mx, -ft * cr[c]);
+            float s = 0.f;
+            for (uint32_t c = 0; c < k; ++c) { ar[c] = std::exp(-ft * cr[c] - mx); s = s + ar[c]; }
+            for (uint32_t c = 0; c < k; ++c) ar[c] = ar[c] / s;
+            if (std::isnan(ar[0])) {
+                float best = cr[0];
+                for (uint32_t c = 1; c < k; ++c) if (cr[c] < best) best = cr[c];
+                uint32_t ties = 0;
+                for (uint32_t c = 0; c < k; ++c) ties += cr[c] == best;
+                const float per = 1.f / float(ties ? ties : 1u);
+                for (uint32_t c = 0; c < k; ++c) ar[c] = cr[c] == best ? per : 0.f;
+            }
+            float dot = 0.f;
+            for (uint32_t c = 0; c < k; ++c) dot = dot + cr[c] * ar[c];
+            rowval[i] = double(dot);
+        }
+        cost = w ? det_sum([&](uint64_t i) { return rowval[i] * w[i]; }, n)
+                 : det_sum([&](uint64_t i) { return rowval[i]; }, n);
+        std::vector<float> nc(uint64_t(k) * d);
+        for (uint32_t c = 0; c < k; ++c) {
+            for (uint64_t j = 0; j < d; ++j) {
+                double num = 0.0, den = 0.0;
+                for (uint64_t r0 = 0; r0 < n; r0 += 256) {
+                    const uint64_t r1 = std::min<uint64_t>(n, r0 + 256);
+                    float s = 0.f, e = 0.f, sw = 0.f, ew = 0.f;
+                    for (uint64_t r = r0; r < r1; ++r) {
+                        const float coef = w ? asn[r * k + c] * float(w[r]) : asn[r * k + c];
+                        two_sum_add(s, e, coef * m.vals[r * d + j]);
+                        two_sum_add(sw, ew, coef);
+                    }
+                    num = num + (double(s) + double(e));
+                    den = den + (double(sw) + double(ew));
+                }
+                nc[uint64_t(c) * d + j] = float(num * (1.0 / den));
+            }
+        }
+        cpy.set_from_dense(nc.data(), k, d, false);
+        fill_costs();
+        if (initcost < 0) initcost = cost;
+        if (oldcost >= cost) acc = cpy;
+        if (oldcost - cost <= eps * std::max(oldcost, cost) || ++iternum == maxiter) break;
+    }
+    std::copy(acc.dense.begin(), acc.dense.end(), centers_out);
+    std::copy(costs.begin(), costs.end(), costs_out);
+    std::copy(asn.begin(), asn.end(), asn_out);
+    *initcost_out = initcost;
+    *finalcost_out = cost;
+    *numiter_out = iternum;
+    return 0;
+}
+
 // CoresetSampler (coreset.h:340-578).  The sampler keeps point weights as float
 // (CoresetSampler<float,uint32_t>::weights_, coreset.h:234,290), so `w` is float here.
 // Per-cluster sums (weight, cost, count) are FP64 over the cluster's points in ascending

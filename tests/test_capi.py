@@ -73,7 +73,7 @@ def test_python_api_rejects_out_of_scope_options():
     with pytest.raises(NotImplementedError):
         mc.hcluster(X, [0, 1], mbsize=2, cs=True)
     with pytest.raises(NotImplementedError):
-        mc.cluster(X, msr=2, k=2, temp=1.0)
+        mc.scluster(X, [0, 1], mbsize=2)
 
 
 def test_struct_layouts_match_the_header(tmp_path):
