@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving", "coreset"],
+    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving", "coreset", "pcmp", "minibatch",
+                                                         "soft"],
                     help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
                          "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass; serving: "
                          "the Poisson job stream through the continuous-batching server; coreset: the "
@@ -298,6 +299,122 @@ def coreset_bench(args):
                          "algorithmic": f"k*n*d*4 + 2*k*n*8 = {kmpp_bytes:.4g} bytes"},
             "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk,
             "e2e": None}
+    print(json.dumps(line))
+
+
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
+
+
+def next_rows_bench(args):
+    """Rows widened beyond the hot path, each timed with CUDA events on the library's
+    stream and checked against a CPU oracle sample:
+      pcmp       condensed pairwise SQRL2 distances of 20,000 x 128 rows (device output)
+      minibatch  minibatch EM, 1M x 64 mixture, k = 100, mbsize 4096, 60 iterations
+      soft       soft clustering, 200k x 32 mixture, k = 20, temp 1, 8 iterations"""
+    import torch
+    import minicore_gb300 as mc
+    from minicore_gb300 import _lib
+    torch.cuda.set_device(0)
+    lib = _lib.load()
+    ctx = mc.Context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    g = torch.Generator(device="cuda").manual_seed(0)
+
+    def mixture(n, d, comps):
+        mu = torch.randn(comps, d, generator=g, device="cuda") * 2.0
+        lab = torch.randint(0, comps, (n,), generator=g, device="cuda")
+        return torch.randn(n, d, generator=g, device="cuda").add_(mu[lab]).contiguous()
+
+    def timed(fn, reps):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = lib.mc_kernel_launches()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, int(lib.mc_kernel_launches() - l0)
+
+    clocks = Clocks()
+    clocks.start()
+    if args.workload == "pcmp":
+        n, d = 20000, 128
+        X = mixture(n, d, 64)
+        M = mc._MatrixArg(X)
+        out = torch.empty(n * (n - 1) // 2, dtype=torch.float32, device="cuda")
+        ms, launches = timed(lambda: _lib.check(lib.mc_pcmp(ctx.handle, M.ref, 2, 0.0, mc._p(out))), args.steps)
+        flops = 2.0 * n * n * d  # every (row, row) pair is evaluated; half are written
+        achieved = flops / (ms * 1e-3) / 1e12
+        import oracle
+        S = 600
+        Xs = X[:S].cpu().numpy()
+        t0 = time.perf_counter()
+        oracle.assign(Xs, Xs, 2, 0.0)
+        cpu_pairs_s = S * S / (time.perf_counter() - t0)
+        line = {"metric": "condensed pairwise SQRL2 distances/s, 20000 x 128 (pcmp)",
+                "value": n * (n - 1) / 2 / (ms * 1e-3), "unit": "pairs/s", "ms_per_step": ms,
+                "roofline": {"bound": "fp32", "achieved": achieved, "peak": FP32_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                             "frac": achieved / FP32_NOMINAL_TFLOPS, "traffic": None,
+                             "peak_source": "nominal FP32 (152 SMs x 128 lanes x 2 x 2.07 GHz)",
+                             "algorithmic": f"2*n*n*d = {flops:.4g} FLOP per call"},
+                "cpu_baseline": {"value": cpu_pairs_s, "unit": "pairs/s", "cores": os.cpu_count() or 1,
+                                 "kind": "port", "sample": f"oracle distances of {S} x {S} rows"}}
+    elif args.workload == "minibatch":
+        n, d, k = 1_000_000, 64, 100
+        X = mixture(n, d, 200)
+        ids = torch.randperm(n, generator=g, device="cuda")[:k]
+        C0 = X[ids].contiguous()
+        iters = 60
+        job = mc.Job(X, C0, msr=2, precision="bf16", seed=5, ctx=ctx)
+        ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+
+        def run():
+            _lib.check(lib.mc_job_minibatch(job._h, 4096, iters, 10, 1, 0, ctypes.byref(ic), ctypes.byref(fc),
+                                            ctypes.byref(it)))
+        ms, launches = timed(run, 1)
+        line = {"metric": "minibatch EM iterations/s, 1M x 64, k=100, mbsize 4096 (BF16 check-ins)",
+                "value": iters / (ms * 1e-3), "unit": "iters/s", "ms_per_step": ms / iters,
+                "objective": {"initcost": ic.value, "finalcost": fc.value}, "roofline": None,
+                "cpu_baseline": None}
+    else:
+        n, d, k = 200_000, 32, 20
+        X = mixture(n, d, 20)
+        C0 = X[:k].contiguous()
+        Xh = X.cpu().numpy()
+        C0h = C0.cpu().numpy()
+        M = mc._MatrixArg(X)
+        iters = 8
+        costs = torch.empty((n, k), dtype=torch.float32, device="cuda")
+        asn = torch.empty((n, k), dtype=torch.float32, device="cuda")
+        cout = torch.empty((k, d), dtype=torch.float32, device="cuda")
+        ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+
+        def run():
+            _lib.check(lib.mc_scluster(ctx.handle, M.ref, mc._p(C0), k, 2, 0.0, None, 1.0, iters, 0.0, mc._p(cout),
+                                       mc._p(costs), mc._p(asn), ctypes.byref(ic), ctypes.byref(fc),
+                                       ctypes.byref(it)))
+        ms, launches = timed(run, 1)
+        import oracle
+        S = 20000
+        t0 = time.perf_counter()
+        ro = oracle.scluster(Xh[:S], C0h, 2, 0.0, temp=1.0, maxiter=iters, eps=0.0)
+        cpu_iter_s = (time.perf_counter() - t0) * (n / S) / max(int(ro["numiter"]), 1)
+        line = {"metric": "soft clustering iterations/s, 200k x 32, k=20, temp 1",
+                "value": max(int(it.value), 1) / (ms * 1e-3), "unit": "iters/s", "ms_per_step": ms / max(int(it.value), 1),
+                "objective": {"initcost": ic.value, "finalcost": fc.value}, "roofline": None,
+                "cpu_baseline": {"value": 1.0 / cpu_iter_s, "unit": "iters/s (scaled to 200k rows)",
+                                 "cores": os.cpu_count() or 1, "kind": "port",
+                                 "sample": f"oracle soft clustering of {S} rows, scaled by {n}/{S}"}}
+    clk = clocks.stop()
+    line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                 "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.workload != "minibatch" else "bf16",
+                 "data": "synthetic", "config": {"workload": args.workload}, "gpu_launches": launches,
+                 "clocks": clk, "e2e": None})
     print(json.dumps(line))
 
 
@@ -627,6 +744,8 @@ def main():
         return serving_main(args)
     if args.workload == "coreset":
         return coreset_bench(args)
+    if args.workload in ("pcmp", "minibatch", "soft"):
+        return next_rows_bench(args)
     if args.workload != "dense":
         return csr_bench(args)
     import torch

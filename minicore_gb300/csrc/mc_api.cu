@@ -552,16 +552,19 @@ __global__ void k_soft_rows(const float *__restrict__ costs, uint64_t n, uint32_
     rowval[i] = double(dot);
 }
 
-// soft weighted means: thread (c, j) walks the rows in chunks of 256 with a compensated
-// float sum of coef * x (coef = asn * float(w)), FP64 across chunks; center = num * (1/den)
-__global__ void k_soft_centers(const float *__restrict__ X, uint64_t n, uint64_t d, const float *__restrict__ asn,
-                               uint32_t k, const double *__restrict__ w, float *centers) {
-    const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+// soft weighted means in two steps with the order of a sequential walk: per chunk of 256
+// rows and center c, thread j keeps a compensated float sum of coef * x[r][j] (coef = asn *
+// float(w)) and of coef; then per (c, j) the chunk values are added in FP64 in chunk order,
+// and center = num * (1 / den)
+constexpr uint64_t kSoftChunk = 256;
+
+__global__ void k_soft_center_chunks(const float *__restrict__ X, uint64_t n, uint64_t d,
+                                     const float *__restrict__ asn, uint32_t k, const double *__restrict__ w,
+                                     double *num /* [chunk][k][d] */, double *den /* [chunk][k] */) {
+    const uint64_t q = blockIdx.x;
     const uint32_t c = blockIdx.y;
-    if (j >= d || c >= k) return;
-    double num = 0.0, den = 0.0;
-    for (uint64_t r0 = 0; r0 < n; r0 += 256) {
-        const uint64_t r1 = umin64(n, r0 + 256);
+    const uint64_t r0 = q * kSoftChunk, r1 = umin64(n, r0 + kSoftChunk);
+    for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) {
         float s = 0.f, e = 0.f, sw = 0.f, ew = 0.f;
         for (uint64_t r = r0; r < r1; ++r) {
             const float coef = w ? asn[r * k + c] * float(w[r]) : asn[r * k + c];
@@ -574,10 +577,32 @@ __global__ void k_soft_centers(const float *__restrict__ X, uint64_t n, uint64_t
             ew = __fadd_rn(ew, __fadd_rn(__fsub_rn(sw, __fsub_rn(tt, bp)), __fsub_rn(coef, bp)));
             sw = tt;
         }
-        num = num + (double(s) + double(e));
-        den = den + (double(sw) + double(ew));
+        num[(q * k + c) * d + j] = double(s) + double(e);
+        if (j == 0) den[q * k + c] = double(sw) + double(ew);
     }
-    centers[uint64_t(c) * d + j] = float(num * (1.0 / den));
+}
+
+// adds the partials of chunks [0, nq) of one batch to the running FP64 sums, in chunk order
+__global__ void k_soft_center_accumulate(const double *__restrict__ num, const double *__restrict__ den, uint64_t nq,
+                                         uint32_t k, uint64_t d, double *acc_num, double *acc_den) {
+    const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    const uint32_t c = blockIdx.y;
+    if (j >= d) return;
+    double a = acc_num[uint64_t(c) * d + j], b = acc_den[c];
+    for (uint64_t q = 0; q < nq; ++q) {
+        a = a + num[(q * k + c) * d + j];
+        b = b + den[q * k + c];
+    }
+    acc_num[uint64_t(c) * d + j] = a;
+    if (j == 0) acc_den[c] = b;
+}
+
+__global__ void k_soft_center_finalize(const double *__restrict__ acc_num, const double *__restrict__ acc_den,
+                                       uint32_t k, uint64_t d, float *centers) {
+    const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+    const uint32_t c = blockIdx.y;
+    if (j >= d) return;
+    centers[uint64_t(c) * d + j] = float(acc_num[uint64_t(c) * d + j] * (1.0 / acc_den[c]));
 }
 
 extern "C" {
@@ -1030,7 +1055,14 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
     const uint64_t n = j->M.n, d = j->M.d;
     const size_t cbytes = uint64_t(k) * d * sizeof(float);
     DBuf<float> costs, asn;
-    DBuf<double> rowval;
+    // chunk partials in batches of at most 256 MB, added in chunk order
+    const uint64_t nq_all = (n + kSoftChunk - 1) / kSoftChunk;
+    const uint64_t batch = std::max<uint64_t>(1, std::min<uint64_t>(nq_all, (256ull << 20) / (8ull * k * d + 8ull * k)));
+    DBuf<double> rowval, snum, sden, acc_num, acc_den;
+    MC_TRY(snum.alloc(batch * k * d, st));
+    MC_TRY(sden.alloc(batch * k, st));
+    MC_TRY(acc_num.alloc(uint64_t(k) * d, st));
+    MC_TRY(acc_den.alloc(k, st));
     MC_TRY(costs.alloc(n * k, st));
     MC_TRY(asn.alloc(n * k, st));
     MC_TRY(rowval.alloc(n, st));
@@ -1049,7 +1081,18 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
             note_launch();
         DetInput in{j->w.p ? DET_F64_W : DET_F64, rowval.p, nullptr, j->w.p, n};
         MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
-        k_soft_centers<<<dim3(unsigned((d + 127) / 128), k), 128, 0, st>>>(j->M.X, n, d, asn.p, k, j->w.p, j->Cw.p),
+        MC_CUDA_TRY(cudaMemsetAsync(acc_num.p, 0, uint64_t(k) * d * sizeof(double), st));
+        MC_CUDA_TRY(cudaMemsetAsync(acc_den.p, 0, uint64_t(k) * sizeof(double), st));
+        for (uint64_t q0 = 0; q0 < nq_all; q0 += batch) {
+            const uint64_t nq = umin64(batch, nq_all - q0), r0 = q0 * kSoftChunk;
+            k_soft_center_chunks<<<dim3(unsigned(nq), k), unsigned(umin64(d, 128)), 0, st>>>(
+                j->M.X + r0 * d, umin64(n - r0, nq * kSoftChunk), d, asn.p + r0 * k, k, j->w.p ? j->w.p + r0 : nullptr,
+                snum.p, sden.p), note_launch();
+            k_soft_center_accumulate<<<dim3(unsigned((d + 127) / 128), k), 128, 0, st>>>(snum.p, sden.p, nq, k, d,
+                                                                                         acc_num.p, acc_den.p),
+                note_launch();
+        }
+        k_soft_center_finalize<<<dim3(unsigned((d + 127) / 128), k), 128, 0, st>>>(acc_num.p, acc_den.p, k, d, j->Cw.p),
             note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         MC_TRY(job_assign_with(j, j->Cw.p, j->psum, true, &o));
