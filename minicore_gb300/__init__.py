@@ -832,3 +832,13 @@ def autotune_report() -> dict:
 
 def autotune_reset():
     check(_lib.load().mc_autotune_reset())
+
+
+def autotune_load(path: str):
+    """Merge decisions from a cache file ("key<TAB>variant<TAB>ms,..." lines; later lines win)."""
+    check(_lib.load().mc_autotune_load(os.fspath(path).encode()))
+
+
+def autotune_save(path: str):
+    """Write every decision of this process to a cache file."""
+    check(_lib.load().mc_autotune_save(os.fspath(path).encode()))

@@ -760,7 +760,8 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
         std::vector<double> uh(k);
         for (uint32_t i = 0; i < k; ++i) uh[i] = uniform_at(seed, i);
         DBuf<double> u, dist, tmp;
-        DBuf<float> cbuf;
+        DBuf<float> cbuf, ct;
+        DBuf<double> cconst;
         DBuf<uint32_t> ids;
         DBuf<uint64_t> newc;
         MC_TRY(u.alloc(k, st));
@@ -785,6 +786,12 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
         a.prior = prior;
         a.prior_sum = prior * double(d);
         a.cbuf = cbuf.p;
+        if (a.csr && msr != JSD) {
+            MC_TRY(ct.alloc(d, st));
+            MC_TRY(cconst.alloc(2, st));
+            a.ct = ct.p;
+            a.cconst = cconst.p;
+        }
         a.dist = dist.p;
         a.asn = j->asn.p;
         a.center_ids = ids.p;
@@ -1249,7 +1256,8 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     if (k == 0) return fail(MC_EINVAL, "k must be positive");
     if (k > n) k = uint32_t(n);
     DBuf<double> rowsum, dist, u, w, tmp;
-    DBuf<float> cbuf, rn;
+    DBuf<float> cbuf, rn, ct;
+    DBuf<double> cconst;
     DBuf<uint32_t> asnb, ids;
     DBuf<uint64_t> newc;
     MC_TRY(rowsum.alloc(n, st));
@@ -1282,6 +1290,12 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     a.prior = prior;
     a.prior_sum = prior * double(d);
     a.cbuf = cbuf.p;
+    if (a.csr && msr != JSD) {
+        MC_TRY(ct.alloc(d, st));
+        MC_TRY(cconst.alloc(2, st));
+        a.ct = ct.p;
+        a.cconst = cconst.p;
+    }
     a.dist = dist.p;
     a.asn = asnb.p;
     a.center_ids = ids.p;

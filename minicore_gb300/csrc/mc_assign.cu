@@ -55,17 +55,20 @@ __global__ void k_prep_centers(const float *__restrict__ C, uint32_t k, uint32_t
     }
 }
 
-// per-center FP64 constants for the sparse-dot kernels (sequential over columns)
+// per-center FP64 constants for the sparse-dot kernels.  One warp per center: lane l adds the
+// terms of columns l, l+32, ... (coalesced loads; the logs and square roots in parallel),
+// then the 32 lane partials are added in lane order.
 template <int MSR>
-__global__ void k_center_consts(const float *__restrict__ C, uint32_t k, uint64_t d, const double *__restrict__ csum,
-                                float pv, double *consts) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= k) return;
+__global__ void __launch_bounds__(128) k_center_consts(const float *__restrict__ C, uint32_t k, uint64_t d,
+                                                       const double *__restrict__ csum, float pv, double *consts) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * 4 + w;
+    if (c >= k) return;  // whole warp; the block has no barrier
     float rsi = 0.f, inc = 0.f;
     if (MSR != SQRL2) side_scalars(pv, csum[c], d, rsi, inc);
     double s0 = 0.0, s1 = 0.0;
     const float *r = C + uint64_t(c) * d;
-    for (uint64_t j = 0; j < d; ++j) {
+    for (uint64_t j = lane; j < d; j += 32) {
         const float x = r[j];
         if (MSR == SQRL2) {
             s0 = s0 + double(x) * double(x);
@@ -82,8 +85,16 @@ __global__ void k_center_consts(const float *__restrict__ C, uint32_t k, uint64_
             }
         }
     }
-    consts[uint64_t(c) * 4 + 0] = s0;
-    consts[uint64_t(c) * 4 + 1] = s1;
+    double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+        t0 = t0 + __shfl_sync(0xffffffffu, s0, l);
+        t1 = t1 + __shfl_sync(0xffffffffu, s1, l);
+    }
+    if (lane == 0) {
+        consts[uint64_t(c) * 4 + 0] = t0;
+        consts[uint64_t(c) * 4 + 1] = t1;
+    }
 }
 
 // row-side scalars for the constant-prior path
@@ -552,6 +563,118 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
     }
 }
 
+// Two rows per warp for 64 padded centers: half-warp h of warp w takes row 2w + h, lane l of
+// the half owns centers 4l .. 4l+3 (one float4 gather per nonzero), chunks of 16 nonzeros
+// per half are staged in shared memory.  Both halves walk max(chunks) chunks, the shorter row
+// padded with neutral entries (column 0, a g that adds exactly nothing), so the warp stays in
+// lock step.  Per-(row, center) sums stay sequential over the nonzeros, as in k_assign_sparse.
+template <int MSR, int SB>
+__global__ void __launch_bounds__(256) k_assign_sparse_pair(AssignArgs a) {
+    __shared__ uint2 stage[8][2][16];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, half = lane >> 4, hl = lane & 15;
+    const unsigned hmask = half ? 0xffff0000u : 0x0000ffffu;
+    const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+    const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    const float pv = a.pv;
+    for (uint64_t pair = warp; 2 * pair < a.n; pair += nwarps) {
+        const uint64_t row = 2 * pair + half;
+        const bool live = row < a.n;
+        const uint64_t pb = live ? a.indptr[row] : 0, pe = live ? a.indptr[row + 1] : 0;
+        float rsi = 0.f, rinc = 0.f;
+        if (live && (MSR == MKL || MSR == HELLINGER)) {
+            rsi = a.rsi[row];
+            rinc = a.rinc[row];
+        }
+        const float rl = (MSR == MKL) ? logf(rinc) : 0.f;
+        const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
+        double bx = 0.0;
+        if (MSR == HELLINGER) {
+            double sb = 0.0;
+            for (uint64_t p = pb + hl; p < pe; p += 16) sb += double(a.vals[p] * rsi + rinc);
+#pragma unroll
+            for (int m = 8; m >= 1; m >>= 1) sb += __shfl_xor_sync(0xffffffffu, sb, m);
+            bx = sb + double(a.d - (pe - pb)) * double(rinc);
+        }
+        // chunks: the longer of the two rows decides
+        const uint64_t mine = (pe - pb + 15) / 16;
+        const uint64_t other = __shfl_xor_sync(0xffffffffu, mine, 16);
+        const uint64_t nchunk = mine > other ? mine : other;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        const float *ctl = a.CT0 + 4 * hl;
+        for (uint64_t ch = 0; ch < nchunk; ++ch) {
+            const uint64_t p = pb + ch * 16 + hl;
+            uint32_t col = 0;
+            float g = (MSR == L1) ? pv : 0.f;
+            if (p < pe) {
+                col = a.idx[p];
+                const float x = a.vals[p];
+                if (MSR == MKL) g = rl - logf(x * rsi + rinc);
+                else if (MSR == HELLINGER) g = srinc - sqrtf(x * rsi + rinc);
+                else if (MSR == L1) g = x + pv;
+                else g = x;
+            }
+            __syncwarp();
+            stage[wib][half][hl] = make_uint2(col, __float_as_uint(g));
+            __syncwarp();
+#pragma unroll
+            for (int q0 = 0; q0 < 16; q0 += SB) {
+                float4 cv[SB];
+                float gj[SB];
+#pragma unroll
+                for (int u = 0; u < SB; ++u) {
+                    const uint2 e = stage[wib][half][q0 + u];
+                    cv[u] = __ldg(reinterpret_cast<const float4 *>(ctl + uint64_t(e.x) * a.kp));
+                    gj[u] = __uint_as_float(e.y);
+                }
+#pragma unroll
+                for (int u = 0; u < SB; ++u) {
+                    const float cc[4] = {cv[u].x, cv[u].y, cv[u].z, cv[u].w};
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        if (MSR == MKL || MSR == HELLINGER) acc[r] = fmaf(cc[r], gj[u], acc[r]);
+                        else if (MSR == SQRL2) acc[r] = fmaf(gj[u], gj[u] - 2.f * cc[r], acc[r]);
+                        else acc[r] = acc[r] + (fabsf(cc[r] - gj[u]) - fabsf(cc[r] - pv));
+                    }
+                }
+            }
+        }
+        Best best;
+        best_init(best);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t c = 4 * hl + r;
+            if (live && c < a.k) {
+                const double k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
+                float key;
+                if (MSR == MKL) {
+                    key = post_divergence(float(k0 - double(rl) * k1 + double(acc[r])));
+                } else if (MSR == HELLINGER) {
+                    double sv = k0 + bx - 2.0 * double(srinc) * k1 + 2.0 * double(acc[r]);
+                    if (sv < 0.0) sv = 0.0;
+                    key = float(sqrt(sv));
+                } else if (MSR == SQRL2) {
+                    double sv = k0 + double(acc[r]);
+                    if (sv < 0.0) sv = 0.0;
+                    key = float(sv);
+                } else {
+                    key = float(k0 + double(acc[r])) * 0.5f;
+                }
+                best_offer(best, key, c);
+                if (a.dmode) write_dist(a, row, c, float(key_to_cost<MSR>(key)));
+            }
+        }
+#pragma unroll
+        for (int m = 8; m >= 1; m >>= 1) best_merge_shfl(best, m);
+        (void)hmask;
+        if (live && hl == 0) {
+            const bool nan0 = best.v == __int_as_float(0xff800000);
+            const double cost = nan0 ? __longlong_as_double(0x7ff8000000000000ll) : key_to_cost<MSR>(best.v);
+            a.asn[row] = best.j;
+            a.costs[row] = double(float(cost));
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------
@@ -575,12 +698,12 @@ int launch_prep_centers(const AssignArgs &a, const float *C, bool pair, bool spa
         default: return fail(MC_EUNSUPPORTED, "measure not supported");
     }
     if (sparse_consts) {
-        const unsigned g = (a.k + 63) / 64;
+        const unsigned g = (a.k + 3) / 4;
         switch (a.msr) {
-            case SQRL2: k_center_consts<SQRL2><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
-            case L1: k_center_consts<L1><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
-            case HELLINGER: k_center_consts<HELLINGER><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
-            case MKL: k_center_consts<MKL><<<g, 64, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            case SQRL2: k_center_consts<SQRL2><<<g, 128, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            case L1: k_center_consts<L1><<<g, 128, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            case HELLINGER: k_center_consts<HELLINGER><<<g, 128, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
+            case MKL: k_center_consts<MKL><<<g, 128, 0, st>>>(C, a.k, a.d, a.csum, a.pv, a.consts), note_launch(); break;
             default: break;
         }
         MC_CUDA_TRY(cudaGetLastError());
@@ -647,13 +770,19 @@ int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t s
 template <int MSR, int KPL>
 static int sparse_kpl(const AssignArgs &a, cudaStream_t st, int sms, bool tune) {
     const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
+    const unsigned pblocks = unsigned(umin64((a.n + 15) / 16, uint64_t(sms) * 16));
     const uint64_t avg = a.n ? (a.nnz + a.n - 1) / a.n : 0;
+    // 64 padded centers also admit the two-rows-per-warp kernel
+    const int nvar = (KPL == 2 && a.kp == 64) ? 5 : 3;
     const std::string key = "csr_sparse|msr" + std::to_string(MSR) + "|kpl" + std::to_string(KPL) + "|g" +
-                            std::to_string((a.k + 32 * KPL - 1) / (32 * KPL)) + "|nnz" + tune_bucket(avg);
-    return tune_launch(key, 3, 0, st, tune, [&](int v) -> int {
+                            std::to_string((a.k + 32 * KPL - 1) / (32 * KPL)) + "|nnz" + tune_bucket(avg) + "|v" +
+                            std::to_string(nvar);
+    return tune_launch(key, nvar, 0, st, tune, [&](int v) -> int {
         if (v == 0) k_assign_sparse<MSR, KPL, 8><<<blocks, 256, 0, st>>>(a), note_launch();
         else if (v == 1) k_assign_sparse<MSR, KPL, 4><<<blocks, 256, 0, st>>>(a), note_launch();
-        else k_assign_sparse<MSR, KPL, 16><<<blocks, 256, 0, st>>>(a), note_launch();
+        else if (v == 2) k_assign_sparse<MSR, KPL, 16><<<blocks, 256, 0, st>>>(a), note_launch();
+        else if (v == 3) k_assign_sparse_pair<MSR, 8><<<pblocks, 256, 0, st>>>(a), note_launch();
+        else k_assign_sparse_pair<MSR, 4><<<pblocks, 256, 0, st>>>(a), note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         return MC_OK;
     });

@@ -184,6 +184,157 @@ __global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, u
     }
 }
 
+// CSR rows against the new center in O(nnz) per row (SQRL2, L1, MKL, Hellinger; rows whose
+// pair keeps the prior pv = prior): per-center FP64 constants over all columns plus a float
+// sum over the row's nonzeros, the arithmetic of the sparse-dot assignment kernel:
+//   SQRL2  key = max(K0 + sum x (x - 2c), 0)                  K0 = sum c^2
+//   L1     key = (K0 + sum |c' - (x+pv)| - |c' - pv|) / 2     K0 = sum |c' - pv|, c' = c + pv
+//   MKL    key = K0 - log(rinc) K1 + sum a (log rinc - log b) K0 = sum a log a, K1 = sum a
+//   Hell.  key = sqrt(K0 + B - 2 sqrt(rinc) K1 + 2 sum sqrt(a) (sqrt(rinc) - sqrt(b)))
+//          K0 = sum a, K1 = sum sqrt a, B = sum over all columns of b
+// with a = c * lhrsi + lhinc (center side), b = x * rhrsi + rhinc (row side).  Rows whose pair
+// moves the prior to the smallest-pv floor take the column loop of k_kmpp_csr.
+// k_kmpp_center_prep (one CTA) writes ct (c, c', a or sqrt a per column) and K0, K1: thread t
+// adds columns t, t+1024, ... in FP64; the 32 lanes of a warp, then the 32 warps, are added in
+// order.
+template <int MSR>
+__global__ void __launch_bounds__(1024) k_kmpp_center_prep(const KmppArgs a) {
+    __shared__ double w0[32], w1[32];
+    const uint64_t c = *a.newc;
+    const float pv = float(a.prior);
+    float rsi = 0.f, inc = 0.f;
+    if (MSR != SQRL2) side_scalars(pv, a.rowsum[c], a.d, rsi, inc);
+    double s0 = 0.0, s1 = 0.0;
+    for (uint64_t j = threadIdx.x; j < a.d; j += 1024) {
+        const float x = a.cbuf[j];
+        float t;
+        if (MSR == SQRL2) {
+            t = x;
+            s0 = s0 + double(x) * double(x);
+        } else if (MSR == L1) {
+            t = x + pv;
+            s0 = s0 + double(fabsf(t - pv));
+        } else {
+            const float av = x * rsi + inc;
+            if (MSR == MKL) {
+                t = av;
+                s0 = s0 + double(av) * double(logf(av));
+                s1 = s1 + double(av);
+            } else {
+                t = sqrtf(av);
+                s0 = s0 + double(av);
+                s1 = s1 + double(t);
+            }
+        }
+        a.ct[j] = t;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+        t0 = t0 + __shfl_sync(0xffffffffu, s0, l);
+        t1 = t1 + __shfl_sync(0xffffffffu, s1, l);
+    }
+    if (lane == 0) {
+        w0[wid] = t0;
+        w1[wid] = t1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double u0 = 0.0, u1 = 0.0;
+        for (int q = 0; q < 32; ++q) {
+            u0 = u0 + w0[q];
+            u1 = u1 + w1[q];
+        }
+        a.cconst[0] = u0;
+        a.cconst[1] = u1;
+    }
+}
+
+template <int MSR>
+__global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int first, uint32_t round) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+    const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    const uint64_t c = *a.newc;
+    const double csum = a.rowsum[c];
+    const double K0 = a.cconst[0], K1 = a.cconst[1];
+    const float fp = float(a.prior);
+    for (uint64_t i = warp; i < a.n; i += nwarps) {
+        if (!first && (i == c || a.dist[i] <= 0.0)) continue;
+        const PairScalars s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], csum, a.d);
+        const uint64_t pb = a.indptr[i], pe = a.indptr[i + 1];
+        double v;
+        if (MSR == SQRL2 || s.pv == fp) {
+            const float rsi = s.rhrsi, rinc = s.rhinc;
+            const float rl = (MSR == MKL) ? logf(rinc) : 0.f;
+            const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
+            float acc = 0.f;
+            double bsum = 0.0;
+#pragma unroll 4
+            for (uint64_t p = pb + lane; p < pe; p += 32) {
+                const float x = a.vals[p];
+                const float cj = __ldg(a.ct + a.idx[p]);
+                if (MSR == SQRL2) {
+                    acc = fmaf(x, x - 2.f * cj, acc);
+                } else if (MSR == L1) {
+                    acc = acc + (fabsf(cj - (x + fp)) - fabsf(cj - fp));
+                } else if (MSR == MKL) {
+                    acc = fmaf(cj, rl - logf(x * rsi + rinc), acc);
+                } else {
+                    const float b = x * rsi + rinc;
+                    acc = fmaf(cj, srinc - sqrtf(b), acc);
+                    bsum = bsum + double(b);
+                }
+            }
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) {
+                acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
+                if (MSR == HELLINGER) bsum = bsum + __shfl_xor_sync(0xffffffffu, bsum, m);
+            }
+            float key;
+            if (MSR == SQRL2) {
+                double t = K0 + double(acc);
+                key = float(t < 0.0 ? 0.0 : t);
+                v = double(key);
+            } else if (MSR == L1) {
+                key = float(K0 + double(acc)) * 0.5f;
+                v = double(key) * 2.0;
+            } else if (MSR == MKL) {
+                key = post_divergence(float(K0 - double(rl) * K1 + double(acc)));
+                v = double(key);
+            } else {
+                const double bx = bsum + double(a.d - (pe - pb)) * double(rinc);
+                double t = K0 + bx - 2.0 * double(srinc) * K1 + 2.0 * double(acc);
+                key = float(sqrt(t < 0.0 ? 0.0 : t));
+                v = double(key) * kSqrt1_2;
+            }
+        } else {
+            float acc = 0.f;
+            for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, a.cbuf[j], 0.f, s);
+            for (uint64_t p = pb + lane; p < pe; p += 32) {
+                const float cj = a.cbuf[a.idx[p]];
+                float t1 = 0.f, t0 = 0.f;
+                kp_elem<MSR>(t1, cj, a.vals[p], s);
+                kp_elem<MSR>(t0, cj, 0.f, s);
+                acc = acc + (t1 - t0);
+            }
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
+            v = kp_cost<MSR>(acc);
+            if (MSR == SQRL2 && v < 0.0) v = 0.0;
+        }
+        if (lane == 0) {
+            if (first) {
+                a.dist[i] = (i == c) ? 0.0 : v;
+            } else if (v < a.dist[i]) {
+                a.dist[i] = v;
+                a.asn[i] = round;
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ void kp_cp_async16(void *dst, const void *src, int src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(uint32_t(__cvta_generic_to_shared(dst))),
                  "l"(src), "r"(src_bytes)
@@ -290,7 +441,12 @@ static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaS
         k_kmpp_dense<MSR, false><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
     } else {
         const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
-        k_kmpp_csr<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();
+        if (MSR != JSD && a.ct) {
+            k_kmpp_center_prep<MSR><<<1, 1024, 0, st>>>(a), note_launch();
+            k_kmpp_csr_nnz<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();
+        } else {
+            k_kmpp_csr<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();
+        }
     }
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;

@@ -22,6 +22,8 @@ struct KmppArgs {
     uint32_t *asn = nullptr;      // [n]
     uint32_t *center_ids = nullptr;  // [k]
     uint64_t *newc = nullptr;     // device scalar
+    float *ct = nullptr;          // CSR, SQRL2/L1/MKL/Hellinger: transformed center row [d]
+    double *cconst = nullptr;     // CSR, SQRL2/L1/MKL/Hellinger: center constants [2]
 };
 
 int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);

@@ -664,23 +664,54 @@ int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool p
 // ------------------------------------------------------------------------------------
 // per-center sums (sequential FP64 over columns) and squared norms
 // ------------------------------------------------------------------------------------
-__global__ void k_center_sums(const float *__restrict__ C, uint32_t k, uint64_t d, double *csum, float *cnorm) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= k) return;
+__global__ void __launch_bounds__(128) k_center_sums(const float *__restrict__ C, uint32_t k, uint64_t d, double *csum,
+                                                     float *cnorm) {
+    // one warp per center.  csum: lane l adds columns l, l+32, l+64, ... in FP64, then the 32
+    // lane partials are added in lane order (the canonical center-sum order).  cnorm: a FP32
+    // fmaf chain in column order, by lane 0 from coalesced shared-memory chunks.
+    __shared__ float t[4][256];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * 4 + w;
+    if (c >= k) return;  // whole warp; the block has no barrier
     const float *r = C + uint64_t(c) * d;
     double s = 0.0;
     float q = 0.f;
-    for (uint64_t j = 0; j < d; ++j) {
-        s = s + double(r[j]);
-        q = fmaf(r[j], r[j], q);
+    for (uint64_t j0 = 0; j0 < d; j0 += 256) {
+        const int cnt = int(d - j0 < 256 ? d - j0 : 256);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = lane + 32 * u;
+            if (i < cnt) {
+                const float x = r[j0 + i];
+                s = s + double(x);
+                if (cnorm) t[w][i] = x;
+            }
+        }
+        if (cnorm) {
+            __syncwarp();
+            if (lane == 0) {
+                if (cnt == 256) {
+#pragma unroll 16
+                    for (int i = 0; i < 256; ++i) q = fmaf(t[w][i], t[w][i], q);
+                } else {
+                    for (int i = 0; i < cnt; ++i) q = fmaf(t[w][i], t[w][i], q);
+                }
+            }
+            __syncwarp();
+        }
     }
-    csum[c] = s;
-    if (cnorm) cnorm[c] = q;
+    double tot = 0.0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) tot = tot + __shfl_sync(0xffffffffu, s, l);
+    if (lane == 0) {
+        csum[c] = tot;
+        if (cnorm) cnorm[c] = q;
+    }
 }
 
 int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, float *cnorm, cudaStream_t st) {
     if (k == 0) return MC_OK;
-    k_center_sums<<<(k + 63) / 64, 64, 0, st>>>(C, k, d, csum, cnorm), note_launch();
+    k_center_sums<<<(k + 3) / 4, 128, 0, st>>>(C, k, d, csum, cnorm), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }

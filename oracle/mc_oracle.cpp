@@ -314,7 +314,15 @@ inline double row_sum(const Mat &m, uint64_t r) {  // Blaze rowwise sum into dou
     return s;
 }
 
-inline double vec_sum(const float *v, uint64_t d) { double s = 0.; for (uint64_t j = 0; j < d; ++j) s += v[j]; return s; }
+// center sums (canonical order of the device's k_center_sums): 32 strided FP64 partials
+// (partial l holds columns l, l+32, ... in order), then the partials in order 0..31
+inline double vec_sum(const float *v, uint64_t d) {
+    double part[32] = {0.};
+    for (uint64_t j = 0; j < d; ++j) part[j % 32] += v[j];
+    double s = 0.;
+    for (int l = 0; l < 32; ++l) s += part[l];
+    return s;
+}
 
 SparseVec to_sparse(const float *dense, uint64_t d) {
     SparseVec s;

@@ -55,7 +55,42 @@ def test_csr_sparse_tuned_equals_default(mc, k):
     assert np.array_equal(a0, a2) and np.array_equal(c0, c2)
     ent = mc.autotune_report()["entries"]
     assert any(key.startswith("csr_sparse|msr5|") for key in ent)
-    assert all(len(v["ms"]) == 3 and 0 <= v["variant"] < 3 for key, v in ent.items() if key.startswith("csr"))
+    assert all(len(v["ms"]) in (3, 5) and 0 <= v["variant"] < len(v["ms"])
+               for key, v in ent.items() if key.startswith("csr"))
+
+
+@pytest.mark.parametrize("msr,prior", [(5, 1.0), (6, 1.0), (2, 0.0), (0, 0.5)])
+def test_csr_every_variant_equals_default(mc, msr, prior, tmp_path):
+    """Each CSR kernel variant, forced through a loaded decision, matches variant 0 bit for bit
+    (k = 50 pads to 64 centers, which adds the two-rows-per-warp kernel; odd n leaves the last
+    warp a single row; empty and long rows are included)."""
+    X = _counts(3001, 900, 0.02, seed=msr).tolil()
+    for i in range(0, 3001, 97):
+        X.rows[i], X.data[i] = [], []
+    for i in range(5, 3001, 211):
+        cols = np.arange(0, 900, 2)
+        X.rows[i], X.data[i] = list(cols), list(np.full(cols.size, 2.0, np.float32))
+    X = X.tocsr().astype(np.float32)
+    X.sort_indices()
+    C = np.asarray(X[np.arange(1, 3001, 60)[:50]].toarray(), np.float32) + 0.25
+    mc.autotune_reset()
+    mc.autotune(True)
+    _assign(mc, X, C, msr, prior)
+    keys = [k for k in mc.autotune_report()["entries"] if k.startswith("csr_sparse|")]
+    assert len(keys) == 1 and mc.autotune_report()["entries"][keys[0]]["ms"].__len__() == 5
+    ref = None
+    for v in range(5):
+        mc.autotune_reset()
+        path = tmp_path / f"v{v}.tsv"
+        path.write_text(f"{keys[0]}\t{v}\t\n")
+        mc.autotune_load(str(path))
+        got = _assign(mc, X, C, msr, prior)
+        assert mc.autotune_report()["entries"][keys[0]]["variant"] == v
+        if ref is None:
+            ref = got
+        assert np.array_equal(ref[0], got[0]), v
+        assert np.array_equal(ref[1], got[1], equal_nan=True), v
+    mc.autotune_reset()
 
 
 def test_dense_sqrl2_and_kmeanspp_tuned_equal_default(mc):

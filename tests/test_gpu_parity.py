@@ -152,6 +152,25 @@ def test_kmeanspp_weighted_and_csr(mc, orc):
         assert (ids == oids).mean() >= 0.8
 
 
+@pytest.mark.parametrize("msr,prior", [(0, 1.0), (2, 0.0), (5, 1.0), (6, 0.5), (5, 1e-44), (6, 1e-44)])
+def test_kmeanspp_csr_nnz_path(mc, orc, msr, prior):
+    """CSR seeding in O(nnz) per row (per-center FP64 constants) against the oracle's merge
+    of the two sparse rows; the tiny priors move the pair to the smallest-pv floor, where
+    rows take the column loop."""
+    S = _counts(2500, 300, 0.04, seed=40 + msr).tolil()
+    for i in range(0, 2500, 101):
+        S.rows[i], S.data[i] = [], []          # empty rows
+    S = S.tocsr().astype(np.float32)
+    S.sort_indices()
+    if msr in (5, 6) and prior < 1e-30:
+        S = S[np.diff(S.indptr) > 0]           # rows with no mass have no divergence then
+    ids, asn, costs = mc.kmeanspp(S, 9, msr=msr, prior=prior, seed=17)
+    oids, oasn, ocosts = orc.kmeanspp(S, 9, msr, prior, orc.uniforms(17, 9))
+    np.testing.assert_allclose(costs, ocosts, rtol=1e-4, atol=1e-5)
+    assert (ids == oids).mean() >= 0.8
+    assert ids[0] == oids[0]
+
+
 def test_hcluster_dense_sqrl2_bit_exact(mc, orc):
     # the small reference configuration: 25-component mixture, kmeans++, 20 updates
     rng = np.random.default_rng(0)
