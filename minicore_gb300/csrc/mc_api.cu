@@ -10,6 +10,7 @@
 #include <cstring>
 #include <limits>
 #include <memory>
+#include <unordered_map>
 #include <vector>
 
 #include "mc_assign.cuh"
@@ -180,6 +181,11 @@ struct mc_job {
     DBuf<uint32_t> asn, asn2;
     DBuf<int> flag;
     DBuf<uint64_t> idxbuf;
+    // CSR JSD sparse-dot path: rows grouped by their zero-entry value rinc
+    DBuf<uint32_t> grp;
+    DBuf<float> gval;
+    DBuf<double> ztab;
+    uint32_t ngrp = 0;
     SortWork sort;
     TcState tc;
     uint64_t last_recheck = 0;
@@ -201,6 +207,46 @@ namespace {
 
 int sync(cudaStream_t st) {
     MC_CUDA_TRY(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+// CSR JSD with a constant prior: the zero entries of row i all take the value
+// rinc_i = pv / (rowsum_i + pv d), so sum over all columns of f(a_cj, rinc_i) depends on the row
+// only through rinc_i.  Rows with equal rinc (count data: equal row sums) form a group; one
+// FP64 sum per (group, center) then leaves O(nnz) work per (row, center).  The grouping is
+// kept only while the table (groups x d per center) costs at most half the nonzeros.
+int build_rinc_groups(const double *rowsum, uint64_t n, uint64_t d, uint64_t nnz, float pv, cudaStream_t st,
+                      DBuf<uint32_t> &grp, DBuf<float> &gval, uint32_t &ngrp) {
+    ngrp = 0;
+    if (n == 0 || !(pv > 0.f)) return MC_OK;
+    DBuf<float> rsi, rinc;
+    MC_TRY(rsi.alloc(n, st));
+    MC_TRY(rinc.alloc(n, st));
+    MC_TRY(launch_row_scalars(rowsum, n, d, pv, rsi.p, rinc.p, st));
+    std::vector<float> h(n);
+    MC_CUDA_TRY(cudaMemcpyAsync(h.data(), rinc.p, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    MC_TRY(sync(st));
+    const uint64_t limit = std::max<uint64_t>(1, nnz / 2 / std::max<uint64_t>(d, 1));
+    std::unordered_map<uint32_t, uint32_t> id;
+    std::vector<uint32_t> g(n);
+    std::vector<float> vals;
+    for (uint64_t i = 0; i < n; ++i) {
+        uint32_t bits;
+        std::memcpy(&bits, &h[i], 4);
+        auto it = id.find(bits);
+        if (it == id.end()) {
+            if (vals.size() >= limit) return MC_OK;  // too many distinct values: no grouping
+            it = id.emplace(bits, uint32_t(vals.size())).first;
+            vals.push_back(h[i]);
+        }
+        g[i] = it->second;
+    }
+    MC_TRY(grp.alloc(n, st));
+    MC_TRY(gval.alloc(vals.size(), st));
+    MC_CUDA_TRY(cudaMemcpyAsync(grp.p, g.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(gval.p, vals.data(), vals.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    MC_TRY(sync(st));  // the host vectors go out of scope
+    ngrp = uint32_t(vals.size());
     return MC_OK;
 }
 
@@ -250,14 +296,21 @@ int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exac
     const bool sparse = csr && j->sparse_path;
     a.kp = sparse ? sparse_center_pad(j->k) : tiled_center_pad(j->k, j->pair, j->msr);
     MC_TRY(j->CT0.alloc(uint64_t(a.kp) * d, j->st));
-    if (!j->pair && (j->msr == MKL || j->msr == JSD)) MC_TRY(j->CT1.alloc(uint64_t(a.kp) * d, j->st));
+    const bool ct1 = !sparse && !j->pair && (j->msr == MKL || j->msr == JSD);
+    if (ct1) MC_TRY(j->CT1.alloc(uint64_t(a.kp) * d, j->st));
     a.CT0 = j->CT0.p;
-    a.CT1 = (!j->pair && (j->msr == MKL || j->msr == JSD)) ? j->CT1.p : nullptr;
+    a.CT1 = ct1 ? j->CT1.p : nullptr;
     if (sparse) {
         MC_TRY(j->consts.alloc(uint64_t(j->k) * 4, j->st));
         a.consts = j->consts.p;
     }
     MC_TRY(launch_prep_centers(a, C, j->pair, sparse, j->st));
+    if (sparse && j->msr == JSD) {
+        MC_TRY(j->ztab.alloc(uint64_t(j->ngrp) * j->k, j->st));
+        MC_TRY(launch_jsd_ztable(C, j->k, d, j->csum.p, j->pv, j->gval.p, j->ngrp, j->ztab.p, j->st));
+        a.grp = j->grp.p;
+        a.ztab = j->ztab.p;
+    }
     if (sparse) {
         Phase ph("assign_csr_sparse", j->st);
         return launch_assign_sparse(a, j->st, j->ctx->sms);
@@ -755,6 +808,8 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
     } else {
         MC_TRY(launch_row_sums_csr(j->M.vals, j->M.indptr, n, j->rowsum.p, st));
     }
+    if (j->M.kind == MC_CSR_F32 && msr == JSD)
+        MC_TRY(build_rinc_groups(j->rowsum.p, n, d, j->M.nnz, float(prior), st, j->grp, j->gval, j->ngrp));
     if (!centers) {
         if (k > n) return fail(MC_EINVAL, "k-means++ seeding needs k <= number of rows");
         std::vector<double> uh(k);
@@ -786,11 +841,14 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
         a.prior = prior;
         a.prior_sum = prior * double(d);
         a.cbuf = cbuf.p;
-        if (a.csr && msr != JSD) {
+        if (a.csr && (msr != JSD || j->ngrp)) {
             MC_TRY(ct.alloc(d, st));
-            MC_TRY(cconst.alloc(2, st));
+            MC_TRY(cconst.alloc(msr == JSD ? j->ngrp : 2, st));
             a.ct = ct.p;
             a.cconst = cconst.p;
+            a.grp = j->grp.p;
+            a.gval = j->gval.p;
+            a.ngrp = j->ngrp;
         }
         a.dist = dist.p;
         a.asn = j->asn.p;
@@ -824,7 +882,7 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
             MC_TRY(launch_row_scalars(j->rowsum.p, n, d, j->pv, j->rsi.p, j->rinc.p, st));
         }
     }
-    j->sparse_path = j->M.kind == MC_CSR_F32 && !j->pair && msr != JSD;
+    j->sparse_path = j->M.kind == MC_CSR_F32 && !j->pair && (msr != JSD || j->ngrp > 0);
     *out = j.release();
     return MC_OK;
 }
@@ -1256,8 +1314,9 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     if (k == 0) return fail(MC_EINVAL, "k must be positive");
     if (k > n) k = uint32_t(n);
     DBuf<double> rowsum, dist, u, w, tmp;
-    DBuf<float> cbuf, rn, ct;
+    DBuf<float> cbuf, rn, ct, gval;
     DBuf<double> cconst;
+    DBuf<uint32_t> grp;
     DBuf<uint32_t> asnb, ids;
     DBuf<uint64_t> newc;
     MC_TRY(rowsum.alloc(n, st));
@@ -1290,11 +1349,16 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     a.prior = prior;
     a.prior_sum = prior * double(d);
     a.cbuf = cbuf.p;
-    if (a.csr && msr != JSD) {
+    uint32_t ngrp = 0;
+    if (a.csr && msr == JSD) MC_TRY(build_rinc_groups(rowsum.p, n, d, M.nnz, float(prior), st, grp, gval, ngrp));
+    if (a.csr && (msr != JSD || ngrp)) {
         MC_TRY(ct.alloc(d, st));
-        MC_TRY(cconst.alloc(2, st));
+        MC_TRY(cconst.alloc(msr == JSD ? ngrp : 2, st));
         a.ct = ct.p;
         a.cconst = cconst.p;
+        a.grp = grp.p;
+        a.gval = gval.p;
+        a.ngrp = ngrp;
     }
     a.dist = dist.p;
     a.asn = asnb.p;

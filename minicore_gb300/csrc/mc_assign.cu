@@ -97,6 +97,41 @@ __global__ void __launch_bounds__(128) k_center_consts(const float *__restrict__
     }
 }
 
+// JSD sparse-dot table (see launch_jsd_ztable): one warp per (group, center); lane l adds the
+// float terms of columns l, l+32, ... in FP64, the 32 lane partials are added in lane order.
+__global__ void __launch_bounds__(256) k_jsd_ztable(const float *__restrict__ C, uint32_t k, uint64_t d,
+                                                    const double *__restrict__ csum, float pv,
+                                                    const float *__restrict__ gval, uint32_t ngrp, double *ztab) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t wid = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+    if (wid >= uint64_t(ngrp) * k) return;  // whole warp
+    const uint32_t g = uint32_t(wid / k), c = uint32_t(wid % k);
+    float rsi, inc;
+    side_scalars(pv, csum[c], d, rsi, inc);
+    const float b = gval[g];
+    const float blb = b * logf(b);
+    const float *r = C + uint64_t(c) * d;
+    double s = 0.0;
+    for (uint64_t j = lane; j < d; j += 32) {
+        const float av = r[j] * rsi + inc;
+        const float m = av + b;
+        s = s + double((av * logf(av) + blb) - m * logf(m * 0.5f));
+    }
+    double t = 0.0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) t = t + __shfl_sync(0xffffffffu, s, l);
+    if (lane == 0) ztab[wid] = t;
+}
+
+int launch_jsd_ztable(const float *C, uint32_t k, uint64_t d, const double *csum, float pv, const float *gval,
+                      uint32_t ngrp, double *ztab, cudaStream_t st) {
+    const uint64_t warps = uint64_t(ngrp) * k;
+    if (warps == 0) return MC_OK;
+    k_jsd_ztable<<<unsigned((warps + 7) / 8), 256, 0, st>>>(C, k, d, csum, pv, gval, ngrp, ztab), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 // row-side scalars for the constant-prior path
 __global__ void k_row_scalars(const double *__restrict__ rowsum, uint64_t n, uint64_t d, float pv, float *rsi,
                               float *rinc) {
@@ -465,7 +500,7 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
     for (uint64_t row = warp; row < a.n; row += nwarps) {
         const uint64_t pb = a.indptr[row], pe = a.indptr[row + 1];
         float rsi = 0.f, rinc = 0.f;
-        if (MSR == MKL || MSR == HELLINGER) {
+        if (MSR == MKL || MSR == HELLINGER || MSR == JSD) {
             rsi = a.rsi[row];
             rinc = a.rinc[row];
         }
@@ -473,14 +508,20 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
         const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
         Best best;
         best_init(best);
-        double bx = 0.0;  // HELLINGER: sum of b over all columns
-        if (MSR == HELLINGER) {
+        // HELLINGER: sum of b over all columns; JSD: sum over the nonzeros of b log b - r log r
+        double bx = 0.0;
+        if (MSR == HELLINGER || MSR == JSD) {
+            const float rlr = (MSR == JSD) ? rinc * logf(rinc) : 0.f;
             double s = 0.0;
-            for (uint64_t p = pb + lane; p < pe; p += 32) s += double(a.vals[p] * rsi + rinc);
+            for (uint64_t p = pb + lane; p < pe; p += 32) {
+                const float b = a.vals[p] * rsi + rinc;
+                s += (MSR == JSD) ? double(b * logf(b) - rlr) : double(b);
+            }
 #pragma unroll
             for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
-            bx = s + double(a.d - (pe - pb)) * double(rinc);
+            bx = (MSR == JSD) ? s : s + double(a.d - (pe - pb)) * double(rinc);
         }
+        const double *zrow = (MSR == JSD) ? a.ztab + uint64_t(a.grp[row]) * a.k : nullptr;
         for (uint32_t g0 = 0; g0 < a.k; g0 += 32 * KPL) {
             float acc[KPL];
 #pragma unroll
@@ -491,15 +532,17 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
                 const uint64_t p = p0 + lane;
                 // past the row's end: center column 0 with a g that adds exactly nothing
                 // (MKL, Hellinger, SQRL2: g = 0 makes every term +-0 on a sum that is not
-                // -0; L1: g = pv makes |c - g| - |c - pv| = +0)
+                // -0; L1: g = pv makes |c - g| - |c - pv| = +0; JSD: g = rinc makes the two
+                // products of the term equal)
                 uint32_t col = 0;
-                float g = (MSR == L1) ? pv : 0.f;
+                float g = (MSR == L1) ? pv : (MSR == JSD) ? rinc : 0.f;
                 if (p < pe) {
                     col = a.idx[p];
                     const float x = a.vals[p];
                     if (MSR == MKL) g = rl - logf(x * rsi + rinc);
                     else if (MSR == HELLINGER) g = srinc - sqrtf(x * rsi + rinc);
                     else if (MSR == L1) g = x + pv;
+                    else if (MSR == JSD) g = x * rsi + rinc;
                     else g = x;
                 }
                 __syncwarp();
@@ -521,9 +564,16 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
 #pragma unroll
                         for (int r = 0; r < KPL; ++r) {
                             const float c = cv[u].v[r];
-                            if (MSR == MKL || MSR == HELLINGER) acc[r] = fmaf(c, gj[u], acc[r]);
-                            else if (MSR == SQRL2) acc[r] = fmaf(gj[u], gj[u] - 2.f * c, acc[r]);
-                            else acc[r] = acc[r] + (fabsf(c - gj[u]) - fabsf(c - pv));
+                            if (MSR == MKL || MSR == HELLINGER) {
+                                acc[r] = fmaf(c, gj[u], acc[r]);
+                            } else if (MSR == SQRL2) {
+                                acc[r] = fmaf(gj[u], gj[u] - 2.f * c, acc[r]);
+                            } else if (MSR == JSD) {
+                                const float m0 = c + rinc, m1 = c + gj[u];
+                                acc[r] = acc[r] + (m0 * logf(m0 * 0.5f) - m1 * logf(m1 * 0.5f));
+                            } else {
+                                acc[r] = acc[r] + (fabsf(c - gj[u]) - fabsf(c - pv));
+                            }
                         }
                     }
                 }
@@ -532,9 +582,12 @@ __global__ void __launch_bounds__(256) k_assign_sparse(AssignArgs a) {
             for (int r = 0; r < KPL; ++r) {
                 const uint32_t c = g0 + KPL * lane + r;
                 if (c < a.k) {
-                    const double k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
                     float key;
-                    if (MSR == MKL) {
+                    double k0 = 0.0, k1 = 0.0;
+                    if (MSR != JSD) k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
+                    if (MSR == JSD) {
+                        key = post_divergence(float((zrow[c] + bx + double(acc[r])) * 0.5));
+                    } else if (MSR == MKL) {
                         key = post_divergence(float(k0 - double(rl) * k1 + double(acc[r])));
                     } else if (MSR == HELLINGER) {
                         double s = k0 + bx - 2.0 * double(srinc) * k1 + 2.0 * double(acc[r]);
@@ -581,19 +634,23 @@ __global__ void __launch_bounds__(256) k_assign_sparse_pair(AssignArgs a) {
         const bool live = row < a.n;
         const uint64_t pb = live ? a.indptr[row] : 0, pe = live ? a.indptr[row + 1] : 0;
         float rsi = 0.f, rinc = 0.f;
-        if (live && (MSR == MKL || MSR == HELLINGER)) {
+        if (live && (MSR == MKL || MSR == HELLINGER || MSR == JSD)) {
             rsi = a.rsi[row];
             rinc = a.rinc[row];
         }
         const float rl = (MSR == MKL) ? logf(rinc) : 0.f;
         const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
         double bx = 0.0;
-        if (MSR == HELLINGER) {
+        if (MSR == HELLINGER || MSR == JSD) {
+            const float rlr = (MSR == JSD) ? rinc * logf(rinc) : 0.f;
             double sb = 0.0;
-            for (uint64_t p = pb + hl; p < pe; p += 16) sb += double(a.vals[p] * rsi + rinc);
+            for (uint64_t p = pb + hl; p < pe; p += 16) {
+                const float b = a.vals[p] * rsi + rinc;
+                sb += (MSR == JSD) ? double(b * logf(b) - rlr) : double(b);
+            }
 #pragma unroll
             for (int m = 8; m >= 1; m >>= 1) sb += __shfl_xor_sync(0xffffffffu, sb, m);
-            bx = sb + double(a.d - (pe - pb)) * double(rinc);
+            bx = (MSR == JSD) ? sb : sb + double(a.d - (pe - pb)) * double(rinc);
         }
         // chunks: the longer of the two rows decides
         const uint64_t mine = (pe - pb + 15) / 16;
@@ -604,13 +661,14 @@ __global__ void __launch_bounds__(256) k_assign_sparse_pair(AssignArgs a) {
         for (uint64_t ch = 0; ch < nchunk; ++ch) {
             const uint64_t p = pb + ch * 16 + hl;
             uint32_t col = 0;
-            float g = (MSR == L1) ? pv : 0.f;
+            float g = (MSR == L1) ? pv : (MSR == JSD) ? rinc : 0.f;
             if (p < pe) {
                 col = a.idx[p];
                 const float x = a.vals[p];
                 if (MSR == MKL) g = rl - logf(x * rsi + rinc);
                 else if (MSR == HELLINGER) g = srinc - sqrtf(x * rsi + rinc);
                 else if (MSR == L1) g = x + pv;
+                else if (MSR == JSD) g = x * rsi + rinc;
                 else g = x;
             }
             __syncwarp();
@@ -631,9 +689,16 @@ __global__ void __launch_bounds__(256) k_assign_sparse_pair(AssignArgs a) {
                     const float cc[4] = {cv[u].x, cv[u].y, cv[u].z, cv[u].w};
 #pragma unroll
                     for (int r = 0; r < 4; ++r) {
-                        if (MSR == MKL || MSR == HELLINGER) acc[r] = fmaf(cc[r], gj[u], acc[r]);
-                        else if (MSR == SQRL2) acc[r] = fmaf(gj[u], gj[u] - 2.f * cc[r], acc[r]);
-                        else acc[r] = acc[r] + (fabsf(cc[r] - gj[u]) - fabsf(cc[r] - pv));
+                        if (MSR == MKL || MSR == HELLINGER) {
+                            acc[r] = fmaf(cc[r], gj[u], acc[r]);
+                        } else if (MSR == SQRL2) {
+                            acc[r] = fmaf(gj[u], gj[u] - 2.f * cc[r], acc[r]);
+                        } else if (MSR == JSD) {
+                            const float m0 = cc[r] + rinc, m1 = cc[r] + gj[u];
+                            acc[r] = acc[r] + (m0 * logf(m0 * 0.5f) - m1 * logf(m1 * 0.5f));
+                        } else {
+                            acc[r] = acc[r] + (fabsf(cc[r] - gj[u]) - fabsf(cc[r] - pv));
+                        }
                     }
                 }
             }
@@ -644,9 +709,12 @@ __global__ void __launch_bounds__(256) k_assign_sparse_pair(AssignArgs a) {
         for (int r = 0; r < 4; ++r) {
             const uint32_t c = 4 * hl + r;
             if (live && c < a.k) {
-                const double k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
                 float key;
-                if (MSR == MKL) {
+                double k0 = 0.0, k1 = 0.0;
+                if (MSR != JSD) k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
+                if (MSR == JSD) {
+                    key = post_divergence(float((a.ztab[uint64_t(a.grp[row]) * a.k + c] + bx + double(acc[r])) * 0.5));
+                } else if (MSR == MKL) {
                     key = post_divergence(float(k0 - double(rl) * k1 + double(acc[r])));
                 } else if (MSR == HELLINGER) {
                     double sv = k0 + bx - 2.0 * double(srinc) * k1 + 2.0 * double(acc[r]);
@@ -810,6 +878,7 @@ int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms, bool tun
         case L1: return sparse_t<L1>(a, st, sms, tune);
         case HELLINGER: return sparse_t<HELLINGER>(a, st, sms, tune);
         case MKL: return sparse_t<MKL>(a, st, sms, tune);
+        case JSD: return sparse_t<JSD>(a, st, sms, tune);
         default: return fail(MC_EUNSUPPORTED, "sparse-dot path does not cover this measure");
     }
 }

@@ -21,6 +21,8 @@ struct AssignArgs {
     float *CT0 = nullptr;             // [d][kp] center transform
     float *CT1 = nullptr;             // [d][kp] second center transform (MKL, JSD)
     double *consts = nullptr;         // [k][4] per-center FP64 constants (sparse-dot path)
+    const uint32_t *grp = nullptr;    // JSD sparse-dot: per-row group of rows with equal rinc
+    const double *ztab = nullptr;     // JSD sparse-dot: [group][k] zero-entry sums (k_jsd_ztable)
     float pv = 0.f;                   // constant-prior pv
     double prior = 0.0, prior_sum = 0.0;
     uint32_t *asn = nullptr;
@@ -51,6 +53,10 @@ int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, f
 // must not synchronise or allocate pass false)
 int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st, bool tune = true);
 int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms, bool tune = true);
+// JSD sparse-dot table: ztab[g * k + c] = sum over all columns j of f(a_cj, gval[g]) with
+// f(a, b) = a log a + b log b - (a + b) log((a + b) / 2) and a_cj the center transform
+int launch_jsd_ztable(const float *C, uint32_t k, uint64_t d, const double *csum, float pv, const float *gval,
+                      uint32_t ngrp, double *ztab, cudaStream_t st);
 uint32_t tiled_center_pad(uint32_t k, bool pair, int msr);
 uint32_t sparse_center_pad(uint32_t k);
 

@@ -192,6 +192,9 @@ __global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, u
 //   MKL    key = K0 - log(rinc) K1 + sum a (log rinc - log b) K0 = sum a log a, K1 = sum a
 //   Hell.  key = sqrt(K0 + B - 2 sqrt(rinc) K1 + 2 sum sqrt(a) (sqrt(rinc) - sqrt(b)))
 //          K0 = sum a, K1 = sum sqrt a, B = sum over all columns of b
+//   JSD    key = (Z[g] + sum (b log b - r log r) + sum (m0 log(m0/2) - m1 log(m1/2))) / 2
+//          m0 = a + r, m1 = a + b, r = rinc of the row's group g, Z[g] = sum over all
+//          columns of f(a, r) (k_kmpp_jsd_zcol)
 // with a = c * lhrsi + lhinc (center side), b = x * rhrsi + rhinc (row side).  Rows whose pair
 // moves the prior to the smallest-pv floor take the column loop of k_kmpp_csr.
 // k_kmpp_center_prep (one CTA) writes ct (c, c', a or sqrt a per column) and K0, K1: thread t
@@ -216,7 +219,9 @@ __global__ void __launch_bounds__(1024) k_kmpp_center_prep(const KmppArgs a) {
             s0 = s0 + double(fabsf(t - pv));
         } else {
             const float av = x * rsi + inc;
-            if (MSR == MKL) {
+            if (MSR == JSD) {
+                t = av;
+            } else if (MSR == MKL) {
                 t = av;
                 s0 = s0 + double(av) * double(logf(av));
                 s1 = s1 + double(av);
@@ -240,7 +245,7 @@ __global__ void __launch_bounds__(1024) k_kmpp_center_prep(const KmppArgs a) {
         w1[wid] = t1;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && MSR != JSD) {
         double u0 = 0.0, u1 = 0.0;
         for (int q = 0; q < 32; ++q) {
             u0 = u0 + w0[q];
@@ -251,6 +256,26 @@ __global__ void __launch_bounds__(1024) k_kmpp_center_prep(const KmppArgs a) {
     }
 }
 
+// JSD: Z[g] = sum over all columns of f(a_j, r_g), one warp per group (lane l adds columns l,
+// l+32, ... in FP64; the lane partials are added in lane order)
+__global__ void __launch_bounds__(256) k_kmpp_jsd_zcol(const KmppArgs a) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t g = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+    if (g >= a.ngrp) return;  // whole warp
+    const float b = a.gval[g];
+    const float blb = b * logf(b);
+    double s = 0.0;
+    for (uint64_t j = lane; j < a.d; j += 32) {
+        const float av = a.ct[j];
+        const float m = av + b;
+        s = s + double((av * logf(av) + blb) - m * logf(m * 0.5f));
+    }
+    double t = 0.0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) t = t + __shfl_sync(0xffffffffu, s, l);
+    if (lane == 0) a.cconst[g] = t;
+}
+
 template <int MSR>
 __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int first, uint32_t round) {
     const int lane = threadIdx.x & 31;
@@ -258,7 +283,7 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
     const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
     const uint64_t c = *a.newc;
     const double csum = a.rowsum[c];
-    const double K0 = a.cconst[0], K1 = a.cconst[1];
+    const double K0 = (MSR == JSD) ? 0.0 : a.cconst[0], K1 = (MSR == JSD) ? 0.0 : a.cconst[1];
     const float fp = float(a.prior);
     for (uint64_t i = warp; i < a.n; i += nwarps) {
         if (!first && (i == c || a.dist[i] <= 0.0)) continue;
@@ -266,7 +291,8 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
         const uint64_t pb = a.indptr[i], pe = a.indptr[i + 1];
         double v;
         if (MSR == SQRL2 || s.pv == fp) {
-            const float rsi = s.rhrsi, rinc = s.rhinc;
+            const float rsi = s.rhrsi, rinc = (MSR == JSD) ? a.gval[a.grp[i]] : s.rhinc;
+            const float rlr = (MSR == JSD) ? rinc * logf(rinc) : 0.f;
             const float rl = (MSR == MKL) ? logf(rinc) : 0.f;
             const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
             float acc = 0.f;
@@ -281,6 +307,11 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
                     acc = acc + (fabsf(cj - (x + fp)) - fabsf(cj - fp));
                 } else if (MSR == MKL) {
                     acc = fmaf(cj, rl - logf(x * rsi + rinc), acc);
+                } else if (MSR == JSD) {
+                    const float b = x * rsi + rinc;
+                    const float m0 = cj + rinc, m1 = cj + b;
+                    acc = acc + (m0 * logf(m0 * 0.5f) - m1 * logf(m1 * 0.5f));
+                    bsum = bsum + double(b * logf(b) - rlr);
                 } else {
                     const float b = x * rsi + rinc;
                     acc = fmaf(cj, srinc - sqrtf(b), acc);
@@ -290,7 +321,7 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
 #pragma unroll
             for (int m = 16; m >= 1; m >>= 1) {
                 acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
-                if (MSR == HELLINGER) bsum = bsum + __shfl_xor_sync(0xffffffffu, bsum, m);
+                if (MSR == HELLINGER || MSR == JSD) bsum = bsum + __shfl_xor_sync(0xffffffffu, bsum, m);
             }
             float key;
             if (MSR == SQRL2) {
@@ -302,6 +333,9 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
                 v = double(key) * 2.0;
             } else if (MSR == MKL) {
                 key = post_divergence(float(K0 - double(rl) * K1 + double(acc)));
+                v = double(key);
+            } else if (MSR == JSD) {
+                key = post_divergence(float((a.cconst[a.grp[i]] + bsum + double(acc)) * 0.5));
                 v = double(key);
             } else {
                 const double bx = bsum + double(a.d - (pe - pb)) * double(rinc);
@@ -441,8 +475,9 @@ static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaS
         k_kmpp_dense<MSR, false><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
     } else {
         const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
-        if (MSR != JSD && a.ct) {
+        if (a.ct) {
             k_kmpp_center_prep<MSR><<<1, 1024, 0, st>>>(a), note_launch();
+            if (MSR == JSD) k_kmpp_jsd_zcol<<<unsigned((a.ngrp + 7) / 8), 256, 0, st>>>(a), note_launch();
             k_kmpp_csr_nnz<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();
         } else {
             k_kmpp_csr<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();

@@ -22,8 +22,11 @@ struct KmppArgs {
     uint32_t *asn = nullptr;      // [n]
     uint32_t *center_ids = nullptr;  // [k]
     uint64_t *newc = nullptr;     // device scalar
-    float *ct = nullptr;          // CSR, SQRL2/L1/MKL/Hellinger: transformed center row [d]
-    double *cconst = nullptr;     // CSR, SQRL2/L1/MKL/Hellinger: center constants [2]
+    float *ct = nullptr;          // CSR O(nnz) path: transformed center row [d]
+    double *cconst = nullptr;     // CSR O(nnz) path: center constants [2] (JSD: [ngrp])
+    const uint32_t *grp = nullptr;  // CSR JSD: per-row group of equal rinc
+    const float *gval = nullptr;    // CSR JSD: rinc of each group
+    uint32_t ngrp = 0;
 };
 
 int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);

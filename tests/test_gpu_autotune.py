@@ -59,16 +59,16 @@ def test_csr_sparse_tuned_equals_default(mc, k):
                for key, v in ent.items() if key.startswith("csr"))
 
 
-@pytest.mark.parametrize("msr,prior", [(5, 1.0), (6, 1.0), (2, 0.0), (0, 0.5)])
+@pytest.mark.parametrize("msr,prior", [(5, 1.0), (6, 1.0), (2, 0.0), (0, 0.5), (4, 1.0)])
 def test_csr_every_variant_equals_default(mc, msr, prior, tmp_path):
     """Each CSR kernel variant, forced through a loaded decision, matches variant 0 bit for bit
     (k = 50 pads to 64 centers, which adds the two-rows-per-warp kernel; odd n leaves the last
     warp a single row; empty and long rows are included)."""
-    X = _counts(3001, 900, 0.02, seed=msr).tolil()
+    X = _counts(3001, 300, 0.12, seed=msr).tolil()
     for i in range(0, 3001, 97):
         X.rows[i], X.data[i] = [], []
     for i in range(5, 3001, 211):
-        cols = np.arange(0, 900, 2)
+        cols = np.arange(0, 300, 2)
         X.rows[i], X.data[i] = list(cols), list(np.full(cols.size, 2.0, np.float32))
     X = X.tocsr().astype(np.float32)
     X.sort_indices()

@@ -101,6 +101,38 @@ def test_csr_assign_matches_oracle(mc, orc, msr, prior):
     _check_assign(orc, X, C, msr, prior, asn, costs, exact=False)
 
 
+@pytest.mark.parametrize("k", [7, 50, 130])
+def test_csr_jsd_grouped_sparse_dot(mc, orc, k):
+    """CSR JSD with a constant prior on count rows: rows with equal row sums share one
+    zero-entry sum per center, the rest is a sparse dot (k = 50 also runs the two-rows-per-
+    warp kernel); checked against the oracle's union walk, and the sparse-dot kernels ran."""
+    X = _counts(4000, 100, 0.2, seed=k)   # ~100 distinct row sums, table <= nnz / 2
+    rng = np.random.default_rng(k)
+    C = np.asarray(X[rng.choice(4000, k, replace=False)].toarray(), np.float32)
+    C[:, ::5] += 0.5
+    mc.autotune(True)
+    mc.autotune_reset()
+    asn, costs = _assign_gpu(mc, X, C, 4, 1.0)
+    _check_assign(orc, X, C, 4, 1.0, asn, costs, exact=False)
+    assert any(key.startswith("csr_sparse|msr4|") for key in mc.autotune_report()["entries"])
+    mc.autotune_reset()
+
+
+def test_csr_jsd_real_valued_rows_fall_back(mc, orc):
+    """Real-valued rows have (almost) no equal row sums: the grouping is dropped and the
+    tiled column loop runs; results still match the oracle."""
+    rng = np.random.default_rng(3)
+    X = sp.random(1500, 200, density=0.05, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.random(s).astype(np.float32) * 4).astype(np.float32)
+    X.sort_indices()
+    C = np.asarray(X[rng.choice(1500, 6, replace=False)].toarray(), np.float32) + 0.1
+    mc.autotune(True)
+    mc.autotune_reset()
+    asn, costs = _assign_gpu(mc, X, C, 4, 1.0)
+    _check_assign(orc, X, C, 4, 1.0, asn, costs, exact=False)
+    assert not any(key.startswith("csr_sparse|msr4|") for key in mc.autotune_report()["entries"])
+
+
 def test_assign_edge_cases(mc, orc):
     # k = 1, ragged d, a single row, duplicate centers (ties -> lowest index)
     X = _mixture(257, 5, 3, seed=1)
@@ -152,17 +184,18 @@ def test_kmeanspp_weighted_and_csr(mc, orc):
         assert (ids == oids).mean() >= 0.8
 
 
-@pytest.mark.parametrize("msr,prior", [(0, 1.0), (2, 0.0), (5, 1.0), (6, 0.5), (5, 1e-44), (6, 1e-44)])
+@pytest.mark.parametrize("msr,prior", [(0, 1.0), (2, 0.0), (5, 1.0), (6, 0.5), (4, 1.0), (5, 1e-44), (6, 1e-44),
+                                       (4, 1e-44)])
 def test_kmeanspp_csr_nnz_path(mc, orc, msr, prior):
     """CSR seeding in O(nnz) per row (per-center FP64 constants) against the oracle's merge
     of the two sparse rows; the tiny priors move the pair to the smallest-pv floor, where
     rows take the column loop."""
-    S = _counts(2500, 300, 0.04, seed=40 + msr).tolil()
+    S = _counts(2500, 100, 0.2, seed=40 + msr).tolil()
     for i in range(0, 2500, 101):
         S.rows[i], S.data[i] = [], []          # empty rows
     S = S.tocsr().astype(np.float32)
     S.sort_indices()
-    if msr in (5, 6) and prior < 1e-30:
+    if msr in (4, 5, 6) and prior < 1e-30:
         S = S[np.diff(S.indptr) > 0]           # rows with no mass have no divergence then
     ids, asn, costs = mc.kmeanspp(S, 9, msr=msr, prior=prior, seed=17)
     oids, oasn, ocosts = orc.kmeanspp(S, 9, msr, prior, orc.uniforms(17, 9))
