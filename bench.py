@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving", "coreset", "pcmp", "minibatch",
-                                                         "soft"],
+                                                         "soft", "small"],
                     help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
                          "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass; serving: "
                          "the Poisson job stream through the continuous-batching server; coreset: the "
@@ -736,6 +736,48 @@ def reference_arm(args):
     print(json.dumps(line))
 
 
+def small_bench(args):
+    """The small reference configuration (10,000 x 50, 25 Gaussian components ~U[-10, 10]^50,
+    unit variance): kmeans++ (k = 25) then hcluster(maxiter=19, eps=0), i.e. 20 updates, from
+    host NumPy arrays through the public API.  Timed per whole call, with the Lloyd loop as one
+    CUDA graph and as a host loop (identical results, checked)."""
+    import time
+    import torch
+    import minicore_gb300 as mc
+    rng = np.random.default_rng(0)
+    mu = rng.uniform(-10, 10, (25, 50))
+    X = (mu[rng.integers(0, 25, 10000)] + rng.normal(size=(10000, 50))).astype(np.float32)
+    ids, _, _ = mc.kmeanspp(X, 25, msr=2, seed=42)
+    C0 = X[ids.astype(np.int64)]
+    out = {}
+    res = {}
+    for mode in ("graph", "host"):
+        mc.loop_graph(mode == "graph")
+        for _ in range(args.warmup):
+            mc.hcluster(X, C0, msr=2, eps=0.0, maxiter=19, seed=3)
+        torch.cuda.synchronize()
+        l0 = mc.kernel_launches()
+        t = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = mc.hcluster(X, C0, msr=2, eps=0.0, maxiter=19, seed=3)
+            t.append((time.perf_counter() - t0) * 1e3)
+        res[mode] = r
+        t = np.sort(np.array(t))
+        out[mode] = {"ms_per_call_p50": float(np.percentile(t, 50)), "ms_per_call_min": float(t[0]),
+                     "updates": int(r["numiter"]), "launches_per_call": (mc.kernel_launches() - l0) / args.steps}
+    mc.loop_graph(True)
+    same = all(np.array_equal(res["graph"][key], res["host"][key]) for key in ("asn", "costs", "centers")) and \
+        res["graph"]["finalcost"] == res["host"]["finalcost"]
+    g = out["graph"]
+    print(json.dumps({"metric": "hcluster calls/s 10000x50 k=25 (20 updates, host arrays in and out)",
+                      "value": 1000.0 / g["ms_per_call_p50"], "unit": "calls/s",
+                      "lloyd_iters_per_s": g["updates"] * 1000.0 / g["ms_per_call_p50"],
+                      "loop_graph": g, "host_loop": out["host"], "identical": bool(same),
+                      "steps": args.steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": "10000x50, 25 components, k=25, kmeans++ seeds, maxiter=19, eps=0"}}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -746,6 +788,8 @@ def main():
         return coreset_bench(args)
     if args.workload in ("pcmp", "minibatch", "soft"):
         return next_rows_bench(args)
+    if args.workload == "small":
+        return small_bench(args)
     if args.workload != "dense":
         return csr_bench(args)
     import torch

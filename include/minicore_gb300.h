@@ -260,6 +260,15 @@ int mc_server_destroy(mc_server *s);
  * $XDG_CACHE_HOME or $HOME/.cache + /minicore_gb300/autotune.tsv); MC_AUTOTUNE=0 or
  * mc_autotune_enable(0) keeps the defaults. */
 int mc_autotune_enable(int on);
+
+/* mc_job_run (and mc_hcluster, the server's jobs) runs the Lloyd loop as one CUDA graph: a
+ * while-conditional node whose body is the centroid update, the assignment pass, the
+ * objective and the stop rule, evaluated on the device, so an iteration makes no host round
+ * trip (no reference counterpart; the reference's loop is solve.h:98-175).  The graph hands
+ * back to the host to finish, or for the D^2 restart of an empty cluster.  Results are those
+ * of the host loop.  MC_LOOP_GRAPH=0 or mc_loop_graph_enable(0) keeps the host loop; so does
+ * an active mc_profile_enable. */
+int mc_loop_graph_enable(int on);
 int mc_autotune_reset(void);                    /* forget every decision (not the file)      */
 int mc_autotune_load(const char *path);         /* add decisions from a cache file           */
 int mc_autotune_save(const char *path);         /* write every decision to a cache file      */

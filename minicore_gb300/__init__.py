@@ -823,6 +823,17 @@ def autotune(enable: bool = True):
     check(_lib.load().mc_autotune_enable(1 if enable else 0))
 
 
+def kernel_launches() -> int:
+    """Kernels this process has launched through the library (graph replays included)."""
+    return int(_lib.load().mc_kernel_launches())
+
+
+def loop_graph(enable: bool = True):
+    """Run the Lloyd loop of Job.run / hcluster as one CUDA graph (default) or as a host
+    loop (identical results)."""
+    check(_lib.load().mc_loop_graph_enable(1 if enable else 0))
+
+
 def autotune_report() -> dict:
     import json
     buf = ctypes.create_string_buffer(1 << 20)

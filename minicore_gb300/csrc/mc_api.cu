@@ -7,6 +7,7 @@
 #include <map>
 #include <mutex>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -24,8 +25,15 @@ namespace mc {
 
 static thread_local std::string g_last_error;
 static std::atomic<uint64_t> g_launches{0};
+static thread_local uint64_t t_launches = 0;  // this thread's share (graph captures count theirs)
 
-void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launch() {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    ++t_launches;
+}
+static thread_local uint64_t t_allocs = 0;
+void note_device_alloc() { ++t_allocs; }
+uint64_t device_allocs() { return t_allocs; }
 
 static std::atomic<bool> g_prof_on{false};
 static std::mutex g_prof_mu;
@@ -189,6 +197,14 @@ struct mc_job {
     SortWork sort;
     TcState tc;
     uint64_t last_recheck = 0;
+    // Lloyd loop as one CUDA graph (mc_job_run); captured per run, and again after a host
+    // iteration (which may have grown buffers the graph points at)
+    cudaGraphExec_t loop_exec = nullptr;
+    uint64_t loop_pre_launches = 0, loop_body_launches = 0;
+    DBuf<unsigned char> loop_state;
+    ~mc_job() {
+        if (loop_exec) cudaGraphExecDestroy(loop_exec);
+    }
 };
 
 struct mc_sampler {
@@ -258,14 +274,17 @@ struct DistOut {
 };
 
 // the assignment pass with the centers in `C` (center sums / transforms refreshed here)
-int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exact, const DistOut *dout = nullptr) {
+// graph_mode: no host round trip inside (for stream capture); the tensor-core path then
+// leaves its bounded-wait status in j->tc.err for the caller
+int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exact, const DistOut *dout = nullptr,
+                    bool graph_mode = false) {
     const uint64_t n = j->M.n, d = j->M.d;
     MC_TRY(launch_center_sums(C, j->k, d, j->csum.p, j->cnorm.p, j->st));
     const bool csr = j->M.kind == MC_CSR_F32;
     const bool tc = !csr && !force_exact && !dout && j->msr == SQRL2 && j->precision != MC_FP32;
     if (tc) {
         MC_TRY(tc_assign(j->tc, j->M.X, n, d, C, j->cnorm.p, j->k, j->precision, j->rownorm.p, j->asn.p,
-                         j->costs.p, j->ctx->sms, j->st, &j->last_recheck));
+                         j->costs.p, j->ctx->sms, j->st, &j->last_recheck, graph_mode));
         return MC_OK;
     }
     j->last_recheck = 0;
@@ -346,6 +365,30 @@ __global__ void k_copy_row_csr(const float *vals, const uint32_t *idx, const uin
 }
 
 // set_centroids_full_mean (centroid.h:649-779); returns 1 if a center was restarted
+// weighted means of the buckets into Cw (presorted: the counting sort of asn is current);
+// j->flag records a NaN center
+int job_launch_centroids(mc_job *j, const uint32_t *keys2, uint64_t extra, bool presorted) {
+    cudaStream_t st = j->st;
+    Phase ph("centroid_update", st);
+    CentroidArgs ca;
+    ca.csr = j->M.kind == MC_CSR_F32;
+    ca.n = j->M.n;
+    ca.d = j->M.d;
+    ca.k = j->k;
+    ca.X = j->M.X;
+    ca.vals = j->M.vals;
+    ca.idx = j->M.idx;
+    ca.indptr = j->M.indptr;
+    ca.keys = j->asn.p;
+    ca.keys2 = keys2;
+    ca.extra_members = extra;
+    ca.w = j->w.p;
+    ca.centers = j->Cw.p;
+    ca.nan_flag = j->flag.p;
+    MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), st));
+    return launch_centroids(ca, j->sort, st, presorted);
+}
+
 int job_set_centroids(mc_job *j, int *restarted) {
     const uint64_t n = j->M.n, d = j->M.d;
     const uint32_t k = j->k;
@@ -415,28 +458,222 @@ int job_set_centroids(mc_job *j, int *restarted) {
         }
         if (extra) keys2 = j->asn2.p;
     }
-    Phase ph("centroid_update", st);
-    CentroidArgs ca;
-    ca.csr = j->M.kind == MC_CSR_F32;
-    ca.n = n;
-    ca.d = d;
-    ca.k = k;
-    ca.X = j->M.X;
-    ca.vals = j->M.vals;
-    ca.idx = j->M.idx;
-    ca.indptr = j->M.indptr;
-    ca.keys = j->asn.p;
-    ca.keys2 = keys2;
-    ca.extra_members = extra;
-    ca.w = j->w.p;
-    ca.centers = j->Cw.p;
-    ca.nan_flag = j->flag.p;
-    MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), st));
-    MC_TRY(launch_centroids(ca, j->sort, st, /*presorted=*/!*restarted));
+    MC_TRY(job_launch_centroids(j, keys2, extra, /*presorted=*/!*restarted));
     int nanf = 0;
     MC_CUDA_TRY(cudaMemcpyAsync(&nanf, j->flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     MC_TRY(sync(st));
     if (nanf) return fail(MC_ENAN, "Unexpected nan in ctr");
+    return MC_OK;
+}
+
+}  // namespace
+
+namespace {
+
+// ------------------------------------------------------------------------------------
+// Lloyd loop as one CUDA graph: [sort asn, check] -> while { centroids, assignment, objective,
+// stop rule, commit, sort asn, check }.  The stop rule of the host loop runs on the device
+// (k_loop_decide); the loop leaves the graph for the host only to finish (converged,
+// maxiter, cost rose -> revert, NaN center, bounded wait expired) or when a cluster is empty
+// (the D^2 restart of set_centroids_full_mean runs on the host, then the graph resumes).
+// Each kernel and its order are those of the host loop, so the results are identical.
+// ------------------------------------------------------------------------------------
+enum : int { LOOP_RUN = 0, LOOP_DONE = 1, LOOP_REVERT = 2, LOOP_EMPTY = 3, LOOP_NAN = 4, LOOP_TIMEOUT = 5 };
+
+struct LoopState {
+    float cost;                  // objective of the committed centers C
+    int reason;                  // LOOP_*
+    unsigned long long iternum;  // committed updates
+    unsigned long long maxiter;
+    double eps;
+    int commit;                  // the last decision copies Cw to C
+    int pad;
+};
+
+__global__ void k_loop_check_empty(const uint64_t *__restrict__ bucket_count, uint32_t k, LoopState *ls,
+                                   cudaGraphConditionalHandle h) {
+    __shared__ int any;
+    if (ls->reason != LOOP_RUN) return;  // same value for the whole block
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (uint32_t c = threadIdx.x; c < k; c += blockDim.x)
+        if (bucket_count[c] == 0) any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0 && any) {
+        ls->reason = LOOP_EMPTY;
+        cudaGraphSetConditional(h, 0);
+    }
+}
+
+// the stop rule of the host loop (perform_hard_clustering, clustering/solve.h:98-175)
+__global__ void k_loop_decide(const double *__restrict__ cost_sum, const int *__restrict__ nan_flag,
+                              const int *__restrict__ tc_err, LoopState *ls, cudaGraphConditionalHandle h) {
+    ls->commit = 0;
+    if (*nan_flag) {
+        ls->reason = LOOP_NAN;
+        cudaGraphSetConditional(h, 0);
+        return;
+    }
+    if (tc_err && *tc_err) {
+        ls->reason = LOOP_TIMEOUT;
+        cudaGraphSetConditional(h, 0);
+        return;
+    }
+    const float newcost = float(*cost_sum);
+    if (newcost > ls->cost) {
+        ls->reason = LOOP_REVERT;
+        cudaGraphSetConditional(h, 0);
+        return;
+    }
+    ls->commit = 1;
+    ls->iternum += 1;
+    const float oldcost = ls->cost;
+    ls->cost = newcost;
+    const double mx = double(newcost) < double(oldcost) ? double(oldcost) : double(newcost);
+    if (double(oldcost - newcost) < ls->eps * mx || ls->iternum > ls->maxiter) {
+        ls->reason = LOOP_DONE;
+        cudaGraphSetConditional(h, 0);
+    } else {
+        cudaGraphSetConditional(h, 1);
+    }
+}
+
+__global__ void k_loop_commit(const LoopState *__restrict__ ls, float *C, const float *__restrict__ Cw, uint64_t m) {
+    if (!ls->commit) return;
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < m; e += gridDim.x * uint64_t(blockDim.x))
+        C[e] = Cw[e];
+}
+
+struct CaptureGuard {  // ends an unfinished capture on the error path
+    cudaStream_t st;
+    bool on = false;
+    ~CaptureGuard() {
+        if (on) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+        }
+    }
+};
+
+int job_build_loop_graph(mc_job *j) {
+    if (j->loop_exec) {
+        cudaGraphExecDestroy(j->loop_exec);
+        j->loop_exec = nullptr;
+    }
+    cudaStream_t st = j->st;
+    const uint64_t n = j->M.n, d = j->M.d;
+    const uint32_t k = j->k;
+    MC_TRY(j->loop_state.alloc(sizeof(LoopState), st));
+    LoopState *ls = reinterpret_cast<LoopState *>(j->loop_state.p);
+    const bool tc = j->M.kind == MC_DENSE_F32 && j->msr == SQRL2 && j->precision != MC_FP32;
+    const int *tc_err = tc ? j->tc.err.p : nullptr;
+    // every buffer the body touches exists before the capture: the sort and centroid work
+    // space and the tensor-core path's FP32 rescan transform.  The centroid launch writes Cw,
+    // which then takes the committed centers back (a restart on the host starts from Cw = C).
+    MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+    MC_TRY(job_launch_centroids(j, nullptr, 0, /*presorted=*/true));
+    MC_CUDA_TRY(cudaMemcpyAsync(j->Cw.p, j->C.p, uint64_t(k) * d * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    if (tc) MC_TRY(j->tc.CT0.alloc(uint64_t(tiled_center_pad(k, false, SQRL2)) * d, st));
+    CaptureGuard guard{st};
+    const uint64_t a0 = device_allocs();
+    const uint64_t l0 = t_launches;
+    MC_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    guard.on = true;
+    MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    MC_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+    cudaGraphConditionalHandle h;
+    MC_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    k_loop_check_empty<<<1, 256, 0, st>>>(j->sort.bucket_count.p, k, ls, h), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    MC_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    MC_CUDA_TRY(cudaGraphAddNode(&wnode, g, deps, nullptr, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    MC_CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    cudaGraph_t top = nullptr;
+    guard.on = false;
+    MC_CUDA_TRY(cudaStreamEndCapture(st, &top));
+    std::unique_ptr<CUgraph_st, cudaError_t (*)(cudaGraph_t)> top_owner(top, cudaGraphDestroy);
+    const uint64_t l1 = t_launches;
+    // the loop body, captured into the conditional node's graph
+    MC_CUDA_TRY(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    guard.on = true;
+    MC_TRY(job_launch_centroids(j, nullptr, 0, /*presorted=*/true));
+    MC_TRY(job_assign_with(j, j->Cw.p, j->psum, false, nullptr, /*graph_mode=*/true));
+    {
+        DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
+        MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
+    }
+    k_loop_decide<<<1, 1, 0, st>>>(j->scal.p, j->flag.p, tc_err, ls, h), note_launch();
+    const uint64_t m = uint64_t(k) * d;
+    k_loop_commit<<<unsigned(umin64((m + 255) / 256, 1024)), 256, 0, st>>>(ls, j->C.p, j->Cw.p, m), note_launch();
+    MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+    k_loop_check_empty<<<1, 256, 0, st>>>(j->sort.bucket_count.p, k, ls, h), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    cudaGraph_t body_out = nullptr;
+    guard.on = false;
+    MC_CUDA_TRY(cudaStreamEndCapture(st, &body_out));
+    const uint64_t l2 = t_launches;
+    g_launches.fetch_sub(l2 - l0);  // counted when the graph runs
+    if (device_allocs() != a0) return MC_EUNSUPPORTED;  // a buffer grew inside: stay on the host loop
+    cudaGraphExec_t ex = nullptr;
+    MC_CUDA_TRY(cudaGraphInstantiate(&ex, top, 0));
+    j->loop_exec = ex;
+    j->loop_pre_launches = l1 - l0;
+    j->loop_body_launches = l2 - l1;
+    return MC_OK;
+}
+
+std::atomic<int> g_loop_graph{-1};  // -1: from MC_LOOP_GRAPH
+thread_local int t_loop_graph = -1;  // -1: the process setting
+
+void drop_loop_graph(mc_job *j) {
+    if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
+    j->loop_exec = nullptr;
+}
+
+bool loop_graph_enabled() {
+    int on = t_loop_graph >= 0 ? t_loop_graph : g_loop_graph.load();
+    if (on < 0) {
+        const char *e = std::getenv("MC_LOOP_GRAPH");
+        on = (e && e[0] == '0') ? 0 : 1;
+    }
+    return on == 1 && !profiling_enabled();
+}
+
+// runs the loop graph from the host state (cost, iternum) until it hands back; the state
+// comes back in `h`
+// *ran = false: the loop could not be captured (the caller runs the host loop instead)
+int job_run_loop_graph(mc_job *j, LoopState &h, bool *ran) {
+    *ran = false;
+    if (!j->loop_exec) {
+        if (job_build_loop_graph(j) != MC_OK) {
+            if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
+            j->loop_exec = nullptr;
+            cudaGetLastError();
+            return MC_OK;
+        }
+    }
+    *ran = true;
+    const unsigned long long it0 = h.iternum;
+    MC_CUDA_TRY(cudaMemcpyAsync(j->loop_state.p, &h, sizeof(LoopState), cudaMemcpyHostToDevice, j->st));
+    MC_CUDA_TRY(cudaGraphLaunch(j->loop_exec, j->st));
+    MC_CUDA_TRY(cudaMemcpyAsync(&h, j->loop_state.p, sizeof(LoopState), cudaMemcpyDeviceToHost, j->st));
+    MC_TRY(sync(j->st));
+    const uint64_t bodies = (h.iternum - it0) + (h.reason == LOOP_REVERT || h.reason == LOOP_NAN ||
+                                                  h.reason == LOOP_TIMEOUT ? 1 : 0);
+    g_launches.fetch_add(j->loop_pre_launches + bodies * j->loop_body_launches);
     return MC_OK;
 }
 
@@ -662,6 +899,19 @@ extern "C" {
 
 const char *mc_version(void) { return "minicore_gb300 0.1 (sm_103a)"; }
 uint64_t mc_kernel_launches(void) { return g_launches.load(); }
+
+}  // extern "C"
+
+namespace mc {
+void set_thread_loop_graph(int on) { t_loop_graph = on; }
+}  // namespace mc
+
+extern "C" {
+
+int mc_loop_graph_enable(int on) {
+    g_loop_graph.store(on ? 1 : 0);
+    return MC_OK;
+}
 
 int mc_profile_enable(int on) {
     g_prof_on.store(on != 0);
@@ -947,7 +1197,33 @@ int mc_job_run(mc_job *j, double eps, uint64_t maxiter, double *initcost_out, do
     }
     const size_t cbytes = uint64_t(j->k) * j->M.d * sizeof(float);
     MC_CUDA_TRY(cudaMemcpyAsync(j->Cw.p, j->C.p, cbytes, cudaMemcpyDeviceToDevice, j->st));
+    bool graph = loop_graph_enabled();
+    drop_loop_graph(j);
     for (;;) {
+        LoopState h = {};
+        if (graph) {
+            h.cost = cost;
+            h.reason = LOOP_RUN;
+            h.iternum = iternum;
+            h.maxiter = maxiter;
+            h.eps = eps;
+            MC_TRY(job_run_loop_graph(j, h, &graph));
+        }
+        if (graph) {
+            cost = h.cost;
+            iternum = h.iternum;
+            if (h.reason == LOOP_DONE) break;
+            if (h.reason == LOOP_REVERT) {
+                MC_TRY(job_assign_with(j, j->C.p, j->psum, false));
+                break;
+            }
+            if (h.reason == LOOP_NAN) return fail(MC_ENAN, "Unexpected nan in ctr");
+            if (h.reason == LOOP_TIMEOUT)
+                return fail(MC_ETIMEOUT, "tensor-core assignment: bounded wait expired");
+            if (h.reason != LOOP_EMPTY) return fail(MC_ECUDA, "Lloyd loop graph returned without a decision");
+            // an empty cluster: one update with the D^2 restart on the host, then the graph again
+            drop_loop_graph(j);
+        }
         int res = 0;
         MC_TRY(job_set_centroids(j, &res));
         MC_TRY(job_assign_with(j, j->Cw.p, j->psum, false));

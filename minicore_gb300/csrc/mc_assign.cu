@@ -272,6 +272,11 @@ __global__ void __launch_bounds__(256) k_assign_tiled(AssignArgs a) {
     const int t = threadIdx.x, tx = t & 15, ty = t >> 4;
     const uint64_t row0 = uint64_t(blockIdx.x) * BM;
     const uint64_t d = a.d;
+    if (a.n_dev) {  // launched for the largest count: tiles past the device count leave at once
+        const uint64_t nd = *a.n_dev;
+        if (row0 >= nd) return;
+        if (nd < a.n) a.n = nd;
+    }
 
     float rpv = a.pv;
     Best best[TM];

@@ -10,6 +10,7 @@ struct AssignArgs {
     uint32_t k = 0, kp = 0;           // centers, padded center count of CT0/CT1
     const float *X = nullptr;         // dense rows
     const uint32_t *rows = nullptr;   // dense only: optional row list (row r of the pass = X row rows[r])
+    const unsigned long long *n_dev = nullptr;  // tiled kernel: row count read on the device (<= n)
     const float *vals = nullptr;      // CSR rows
     const uint32_t *idx = nullptr;
     const uint64_t *indptr = nullptr;

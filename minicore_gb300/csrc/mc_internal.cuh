@@ -134,6 +134,11 @@ struct DetInput {
 // ------------------------------------------------------------------------------------
 // device buffers
 // ------------------------------------------------------------------------------------
+// device allocations made through DBuf by the calling thread (a stream capture checks that
+// it made none)
+void note_device_alloc();
+uint64_t device_allocs();
+
 template <class T>
 struct DBuf {
     T *p = nullptr;
@@ -153,6 +158,7 @@ struct DBuf {
         release();
         st = stream;
         if (count == 0) count = 1;
+        note_device_alloc();
         cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(T), stream);
         if (e != cudaSuccess) {
             p = nullptr;
@@ -168,6 +174,9 @@ bool is_device_ptr(const void *p);
 
 // process-wide count of kernel launches issued by this library
 void note_launch();
+// mc_job_run's loop graph for jobs run by the calling thread: 1 on, 0 off, -1 the process
+// setting (mc_loop_graph_enable / MC_LOOP_GRAPH)
+void set_thread_loop_graph(int on);
 
 // Phase profiler (off by default): when enabled, Phase records a CUDA event pair on the
 // stream around a scope; mc_profile_report() sums the elapsed times per phase name.

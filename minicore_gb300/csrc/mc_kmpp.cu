@@ -276,14 +276,14 @@ __global__ void __launch_bounds__(256) k_kmpp_jsd_zcol(const KmppArgs a) {
     if (lane == 0) a.cconst[g] = t;
 }
 
+// the rows of one round (warp per row): ct = transformed center, raw = densified center
 template <int MSR>
-__global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int first, uint32_t round) {
+__device__ __forceinline__ void kp_nnz_rows(const KmppArgs &a, int first, uint32_t round, uint64_t c,
+                                            const float *ct, const float *raw, double K0, double K1) {
     const int lane = threadIdx.x & 31;
     const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
     const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
-    const uint64_t c = *a.newc;
     const double csum = a.rowsum[c];
-    const double K0 = (MSR == JSD) ? 0.0 : a.cconst[0], K1 = (MSR == JSD) ? 0.0 : a.cconst[1];
     const float fp = float(a.prior);
     for (uint64_t i = warp; i < a.n; i += nwarps) {
         if (!first && (i == c || a.dist[i] <= 0.0)) continue;
@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
 #pragma unroll 4
             for (uint64_t p = pb + lane; p < pe; p += 32) {
                 const float x = a.vals[p];
-                const float cj = __ldg(a.ct + a.idx[p]);
+                const float cj = ct[a.idx[p]];
                 if (MSR == SQRL2) {
                     acc = fmaf(x, x - 2.f * cj, acc);
                 } else if (MSR == L1) {
@@ -345,9 +345,9 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
             }
         } else {
             float acc = 0.f;
-            for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, a.cbuf[j], 0.f, s);
+            for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, raw[j], 0.f, s);
             for (uint64_t p = pb + lane; p < pe; p += 32) {
-                const float cj = a.cbuf[a.idx[p]];
+                const float cj = raw[a.idx[p]];
                 float t1 = 0.f, t0 = 0.f;
                 kp_elem<MSR>(t1, cj, a.vals[p], s);
                 kp_elem<MSR>(t0, cj, 0.f, s);
@@ -367,6 +367,86 @@ __global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int firs
             }
         }
     }
+}
+
+template <int MSR>
+__global__ void __launch_bounds__(256) k_kmpp_csr_nnz(const KmppArgs a, int first, uint32_t round) {
+    const uint64_t c = *a.newc;
+    const double K0 = (MSR == JSD) ? 0.0 : a.cconst[0], K1 = (MSR == JSD) ? 0.0 : a.cconst[1];
+    kp_nnz_rows<MSR>(a, first, round, c, a.ct, a.cbuf, K0, K1);
+}
+
+// Small d (2 d floats of shared memory): one launch per round.  Every CTA densifies the new
+// center's CSR row into shared memory, forms ct and K0, K1 with the code and summation order
+// of k_kmpp_center_prep (1024 threads), then runs its share of the rows; CTA 0 also records
+// the center and zeroes its distance (k_kmpp_take / k_kmpp_zero).  Same results as the
+// three-launch sequence.
+template <int MSR>
+__global__ void __launch_bounds__(1024) k_kmpp_csr_fused(const KmppArgs a, int first, uint32_t round) {
+    extern __shared__ float sm_kp[];
+    float *raw = sm_kp, *ct = sm_kp + a.d;
+    __shared__ double w0[32], w1[32], kk[2];
+    const uint64_t c = *a.newc;
+    const int tid = threadIdx.x;
+    for (uint64_t j = tid; j < a.d; j += 1024) raw[j] = 0.f;
+    __syncthreads();
+    for (uint64_t p = a.indptr[c] + tid; p < a.indptr[c + 1]; p += 1024) raw[a.idx[p]] = a.vals[p];
+    if (blockIdx.x == 0 && tid == 0) {
+        a.center_ids[round] = uint32_t(c);
+        a.asn[c] = round;
+        if (!first) a.dist[c] = 0.0;
+    }
+    __syncthreads();
+    const float pv = float(a.prior);
+    float rsi = 0.f, inc = 0.f;
+    if (MSR != SQRL2) side_scalars(pv, a.rowsum[c], a.d, rsi, inc);
+    double s0 = 0.0, s1 = 0.0;
+    for (uint64_t j = tid; j < a.d; j += 1024) {
+        const float x = raw[j];
+        float t;
+        if (MSR == SQRL2) {
+            t = x;
+            s0 = s0 + double(x) * double(x);
+        } else if (MSR == L1) {
+            t = x + pv;
+            s0 = s0 + double(fabsf(t - pv));
+        } else {
+            const float av = x * rsi + inc;
+            if (MSR == MKL) {
+                t = av;
+                s0 = s0 + double(av) * double(logf(av));
+                s1 = s1 + double(av);
+            } else {
+                t = sqrtf(av);
+                s0 = s0 + double(av);
+                s1 = s1 + double(t);
+            }
+        }
+        ct[j] = t;
+    }
+    const int lane = tid & 31, wid = tid >> 5;
+    double t0 = 0.0, t1 = 0.0;
+#pragma unroll
+    for (int l = 0; l < 32; ++l) {
+        t0 = t0 + __shfl_sync(0xffffffffu, s0, l);
+        t1 = t1 + __shfl_sync(0xffffffffu, s1, l);
+    }
+    if (lane == 0) {
+        w0[wid] = t0;
+        w1[wid] = t1;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double u0 = 0.0, u1 = 0.0;
+        for (int q = 0; q < 32; ++q) {
+            u0 = u0 + w0[q];
+            u1 = u1 + w1[q];
+        }
+        kk[0] = u0;
+        kk[1] = u1;
+    }
+    __syncthreads();
+    kp_nnz_rows<MSR>(a, first, round, c, ct, raw, kk[0], kk[1]);
 }
 
 __device__ __forceinline__ void kp_cp_async16(void *dst, const void *src, int src_bytes) {
@@ -452,6 +532,9 @@ __global__ void __launch_bounds__(128) k_kmpp_dense_staged(const KmppArgs a, int
     }
 }
 
+// CSR update in one launch per round: the center row and its transform fit in 32 KB
+static bool kmpp_csr_fused_ok(const KmppArgs &a) { return a.csr && a.msr != JSD && a.ct && a.d <= 4096; }
+
 template <int MSR>
 static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaStream_t st) {
     if (!a.csr) {
@@ -475,7 +558,10 @@ static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaS
         k_kmpp_dense<MSR, false><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
     } else {
         const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
-        if (a.ct) {
+        if (MSR != JSD && a.ct && kmpp_csr_fused_ok(a)) {
+            const unsigned fb = unsigned(umin64((a.n + 31) / 32, uint64_t(sms) * 2));
+            k_kmpp_csr_fused<MSR><<<fb, 1024, 2 * a.d * sizeof(float), st>>>(a, first, round), note_launch();
+        } else if (a.ct) {
             k_kmpp_center_prep<MSR><<<1, 1024, 0, st>>>(a), note_launch();
             if (MSR == JSD) k_kmpp_jsd_zcol<<<unsigned((a.ngrp + 7) / 8), 256, 0, st>>>(a), note_launch();
             k_kmpp_csr_nnz<MSR><<<blocks, 256, 0, st>>>(a, first, round), note_launch();
@@ -503,7 +589,8 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     const unsigned tb = 256, tg = unsigned(umin64((a.d + tb - 1) / tb, 1024));
     MC_CUDA_TRY(cudaMemsetAsync(a.asn, 0, a.n * sizeof(uint32_t), st));
     k_kmpp_first<<<1, 1, 0, st>>>(u_dev, a.n, a.newc, a.center_ids), note_launch();
-    if (a.csr) {
+    const bool fused = kmpp_csr_fused_ok(a);  // the update kernel takes the center itself
+    if (a.csr && !fused) {
         k_kmpp_take<<<tg, tb, 0, st>>>(a, 0), note_launch();
         k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
     }
@@ -511,13 +598,13 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     DetInput in{a.w ? DET_F64_W : DET_F64, a.dist, nullptr, a.w, a.n};
     for (uint32_t ci = 1; ci < a.k; ++ci) {
         MC_TRY(launch_det_draw(in, chunk_tmp, u_dev + ci, 0.0, 1, a.dist, a.newc, st));
-        if (a.csr) {
+        if (a.csr && !fused) {
             // CSR centers are densified into cbuf; the dense update reads the center row itself
             k_kmpp_take<<<tg, tb, 0, st>>>(a, ci), note_launch();
             k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
         }
         MC_TRY(update(a, 0, ci, sms, st));
-        if (a.csr) k_kmpp_zero<<<1, 1, 0, st>>>(a), note_launch();
+        if (a.csr && !fused) k_kmpp_zero<<<1, 1, 0, st>>>(a), note_launch();
     }
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;

@@ -129,6 +129,10 @@ uint64_t device_available(int device) {
 
 void worker_main(mc_server *s, int slot) {
     cudaSetDevice(s->device);
+    // the host loop: with several jobs in flight the GPU stays busy through each job's host
+    // round trips, while capturing and instantiating a loop graph per job costs more
+    // (measured on the serving stream: 201 jobs/s host loop against 154 with graphs)
+    set_thread_loop_graph(0);
     mc_context *ctx = s->ctxs[size_t(slot)];
     for (;;) {
         Ticket *t = nullptr;

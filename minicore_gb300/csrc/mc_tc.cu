@@ -858,7 +858,7 @@ static int make_map(CUtensorMap *map, const void *ptr, bool tf32, uint64_t rows,
 
 int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
               int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
-              uint64_t *recheck_count) {
+              uint64_t *recheck_count, bool graph_mode) {
     const bool tf32 = precision == MC_TF32;
     const uint64_t esz = tf32 ? 4 : 2;
     const uint64_t kelems = tc::KBYTES / esz;            // K elements per k-block
@@ -1002,6 +1002,27 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
                                                             s.nrecheck.p + 1), note_launch();
     }
     MC_CUDA_TRY(cudaGetLastError());
+    if (graph_mode) {
+        // no host round trip: the FP32 rescan is launched for every row and reads the count
+        // of rows without a candidate list on the device; s.err is read by the caller
+        AssignArgs b;
+        b.msr = SQRL2;
+        b.n = n;
+        b.n_dev = s.nrecheck.p + 1;
+        b.d = d;
+        b.k = k;
+        b.kp = tiled_center_pad(k, false, SQRL2);
+        b.X = X;
+        b.rows = s.over_rows.p;
+        MC_TRY(s.CT0.alloc(uint64_t(b.kp) * d, st));
+        b.CT0 = s.CT0.p;
+        b.asn = asn;
+        b.costs = costs;
+        MC_TRY(launch_prep_centers(b, C, false, false, st));
+        MC_TRY(launch_assign_tiled(b, false, false, st, /*tune=*/false));
+        if (recheck_count) *recheck_count = 0;
+        return MC_OK;
+    }
     int err = 0;
     unsigned long long nr[2] = {0, 0};
     MC_CUDA_TRY(cudaMemcpyAsync(&err, s.err.p, sizeof(int), cudaMemcpyDeviceToHost, st));

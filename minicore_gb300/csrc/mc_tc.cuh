@@ -35,6 +35,6 @@ struct TcState {
 
 int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
               int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
-              uint64_t *recheck_count);
+              uint64_t *recheck_count, bool graph_mode = false);
 
 }  // namespace mc

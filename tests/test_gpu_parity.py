@@ -204,6 +204,19 @@ def test_kmeanspp_csr_nnz_path(mc, orc, msr, prior):
     assert ids[0] == oids[0]
 
 
+@pytest.mark.parametrize("msr,prior", [(2, 0.0), (0, 1.0)])
+def test_kmeanspp_csr_fused_equals_three_launch_path(mc, msr, prior):
+    """d <= 4096 runs the one-launch CSR update (center densified per CTA); one more, empty
+    column (d = 4097) runs take / scatter / prep / update / zero.  For SQRL2 and L1 an empty
+    column adds exactly nothing, so both give the same seeds, assignments and costs."""
+    S = _counts(3000, 4096, 0.004, seed=5)
+    S2 = sp.csr_matrix((S.data, S.indices, S.indptr), shape=(3000, 4097))
+    a = mc.kmeanspp(S, 20, msr=msr, prior=prior, seed=8)
+    b = mc.kmeanspp(S2, 20, msr=msr, prior=prior, seed=8)
+    for u, v in zip(a, b):
+        assert np.array_equal(u, v)
+
+
 def test_hcluster_dense_sqrl2_bit_exact(mc, orc):
     # the small reference configuration: 25-component mixture, kmeans++, 20 updates
     rng = np.random.default_rng(0)
