@@ -1091,7 +1091,7 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
         a.prior = prior;
         a.prior_sum = prior * double(d);
         a.cbuf = cbuf.p;
-        if (a.csr && (msr != JSD || j->ngrp)) {
+        if (a.csr && kmpp_csr_nnz_path(d) && (msr != JSD || j->ngrp)) {
             MC_TRY(ct.alloc(d, st));
             MC_TRY(cconst.alloc(msr == JSD ? j->ngrp : 2, st));
             a.ct = ct.p;
@@ -1627,7 +1627,7 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     a.cbuf = cbuf.p;
     uint32_t ngrp = 0;
     if (a.csr && msr == JSD) MC_TRY(build_rinc_groups(rowsum.p, n, d, M.nnz, float(prior), st, grp, gval, ngrp));
-    if (a.csr && (msr != JSD || ngrp)) {
+    if (a.csr && kmpp_csr_nnz_path(d) && (msr != JSD || ngrp)) {
         MC_TRY(ct.alloc(d, st));
         MC_TRY(cconst.alloc(msr == JSD ? ngrp : 2, st));
         a.ct = ct.p;

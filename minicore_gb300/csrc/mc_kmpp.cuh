@@ -31,6 +31,12 @@ struct KmppArgs {
 
 int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);
 
+// CSR seeding takes the O(nnz)-per-row update (per-center FP64 constants, a.ct / a.cconst)
+// only for wide rows: each round then pays a few microseconds of dependent FP64 sums (about
+// 75 ns per dependent add on this GPU), which the float column loop of k_kmpp_csr, O(d) per
+// row, undercuts up to a couple of thousand columns
+inline bool kmpp_csr_nnz_path(uint64_t d) { return d > 2048; }
+
 // C[c] = row ids[c], c < k (CSR rows densified into d columns)
 int launch_gather_rows(bool csr, const float *X, const float *vals, const uint32_t *idx, const uint64_t *indptr,
                        uint64_t d, const uint32_t *ids, uint32_t k, float *C, cudaStream_t st);

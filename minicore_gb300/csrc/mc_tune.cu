@@ -122,10 +122,6 @@ std::string tune_bucket(uint64_t v) {
 int tune_launch(const std::string &key0, int nvariants, int default_variant, cudaStream_t st, bool allow,
                 const std::function<int(int)> &launch) {
     if (nvariants <= 1 || !allow) return launch(default_variant);
-    // a stream being captured into a graph cannot time anything: a recorded decision or the
-    // default (the variants give identical results)
-    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusNone;
     std::string key;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -135,6 +131,10 @@ int tune_launch(const std::string &key0, int nvariants, int default_variant, cud
         auto it = g_tune.find(key);
         if (it != g_tune.end() && it->second.variant < nvariants) return launch(it->second.variant);
     }
+    // a stream being captured into a graph cannot time anything: the default (the variants
+    // give identical results)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusNone;
     if (cap != cudaStreamCaptureStatusNone) return launch(default_variant);
     // time every variant twice (the first run also warms caches); outputs are identical, so
     // whatever ran last leaves the right result

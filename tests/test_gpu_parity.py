@@ -187,11 +187,18 @@ def test_kmeanspp_weighted_and_csr(mc, orc):
 @pytest.mark.parametrize("msr,prior", [(0, 1.0), (2, 0.0), (5, 1.0), (6, 0.5), (4, 1.0), (5, 1e-44), (6, 1e-44),
                                        (4, 1e-44)])
 def test_kmeanspp_csr_nnz_path(mc, orc, msr, prior):
-    """CSR seeding in O(nnz) per row (per-center FP64 constants) against the oracle's merge
-    of the two sparse rows; the tiny priors move the pair to the smallest-pv floor, where
-    rows take the column loop."""
-    S = _counts(2500, 100, 0.2, seed=40 + msr).tolil()
-    for i in range(0, 2500, 101):
+    """CSR seeding of wide rows in O(nnz) per row (per-center FP64 constants) against the
+    oracle's merge of the two sparse rows; the tiny priors move the pair to the smallest-pv
+    floor, where rows take the column loop."""
+    # wide rows (d > 2048 takes the O(nnz) update), 12 nonzeros each, few distinct row sums
+    # (JSD groups rows by their zero-entry value)
+    rng = np.random.default_rng(40 + msr)
+    n, d = 2500, 2600
+    cols = np.stack([np.sort(rng.choice(d, 12, replace=False)) for _ in range(n)])
+    vals = np.ones((n, 12), np.float32)
+    vals[:, 0] = rng.integers(1, 3, n)
+    S = sp.csr_matrix((vals.ravel(), cols.ravel(), np.arange(0, 12 * n + 1, 12)), shape=(n, d)).tolil()
+    for i in range(0, n, 101):
         S.rows[i], S.data[i] = [], []          # empty rows
     S = S.tocsr().astype(np.float32)
     S.sort_indices()
