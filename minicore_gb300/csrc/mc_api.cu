@@ -1043,7 +1043,7 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
     MC_TRY(j->Cw.alloc(uint64_t(k) * d, st));
     MC_TRY(j->csum.alloc(k, st));
     MC_TRY(j->cnorm.alloc(k, st));
-    MC_TRY(j->det_tmp.alloc(det_chunks(n) + 1, st));
+    MC_TRY(j->det_tmp.alloc(det_tmp_size(n), st));
     MC_TRY(j->scal.alloc(4, st));
     MC_TRY(j->flag.alloc(1, st));
     if (centers)
@@ -1071,7 +1071,7 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
         DBuf<uint64_t> newc;
         MC_TRY(u.alloc(k, st));
         MC_TRY(dist.alloc(n, st));
-        MC_TRY(tmp.alloc(det_chunks(n) + 1, st));
+        MC_TRY(tmp.alloc(det_tmp_size(n), st));
         MC_TRY(cbuf.alloc(d, st));
         MC_TRY(ids.alloc(k, st));
         MC_TRY(newc.alloc(1, st));
@@ -1598,7 +1598,7 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     MC_TRY(rowsum.alloc(n, st));
     MC_TRY(dist.alloc(n, st));
     MC_TRY(u.alloc(k, st));
-    MC_TRY(tmp.alloc(det_chunks(n) + 1, st));
+    MC_TRY(tmp.alloc(det_tmp_size(n), st));
     MC_TRY(cbuf.alloc(d, st));
     MC_TRY(asnb.alloc(n, st));
     MC_TRY(ids.alloc(k, st));

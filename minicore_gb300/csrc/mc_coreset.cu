@@ -218,7 +218,7 @@ int compute_sensitivities(const SensInput &in, SensWork &w, cudaStream_t st, int
     MC_TRY(w.wsum.alloc(nc, st));
     MC_TRY(w.csum.alloc(nc, st));
     MC_TRY(w.scal.alloc(4, st));
-    MC_TRY(w.det_tmp.alloc(det_chunks(n) + 1, st));
+    MC_TRY(w.det_tmp.alloc(det_tmp_size(n), st));
     MC_TRY(w.flag.alloc(1, st));
     MC_CUDA_TRY(cudaMemsetAsync(w.flag.p, 0, sizeof(int), st));
     k_check_asn<<<grid_for(n, sms), 256, 0, st>>>(in.asn, n, nc, w.flag.p), note_launch();
@@ -355,7 +355,7 @@ __global__ void k_alias_identity(uint64_t n, double *prob_tab, uint32_t *alias_t
 
 int build_alias(const float *probs, uint64_t n, double *prob_tab, uint32_t *alias_tab, AliasWork &w, cudaStream_t st,
                 int sms) {
-    MC_TRY(w.tmp.alloc(det_chunks(n) + 1, st));
+    MC_TRY(w.tmp.alloc(det_tmp_size(n), st));
     MC_TRY(w.S.alloc(1, st));
     MC_TRY(w.flag.alloc(n, st));
     MC_TRY(w.pos.alloc(n + 1, st));

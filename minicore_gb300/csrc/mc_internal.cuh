@@ -99,13 +99,22 @@ __host__ __device__ inline double uniform_at(uint64_t seed, uint64_t i) {
 }
 
 // ------------------------------------------------------------------------------------
-// deterministic FP64 sums: chunk 8192 = 256 threads x 32 strided elements
+// deterministic FP64 sums: chunks of 8192 consecutive elements, a pairwise tree inside each
+// chunk and a pairwise tree over the chunk totals (padded to a power of two)
 // ------------------------------------------------------------------------------------
 constexpr int kDetChunk = 8192;
 constexpr int kDetThreads = 256;
 constexpr int kDetPer = 32;
 
 __host__ __device__ inline uint64_t det_chunks(uint64_t n) { return (n + kDetChunk - 1) / kDetChunk; }
+// leaves of the tree over the chunk totals (a power of two, at least 1)
+__host__ __device__ inline uint64_t det_leaves(uint64_t n) {
+    uint64_t p = 1;
+    while (p < det_chunks(n)) p <<= 1;
+    return p;
+}
+// doubles of scratch that launch_det_sum / launch_det_draw need (the tree, heap layout)
+__host__ __device__ inline uint64_t det_tmp_size(uint64_t n) { return 2 * det_leaves(n); }
 
 // value sources for det sums
 enum DetSrc : int {

@@ -12,113 +12,130 @@
 namespace mc {
 
 // ------------------------------------------------------------------------------------
-// det sum: one CTA (256 threads) per 8192-element chunk
+// Deterministic FP64 sums and draws.  Chunks of 8192 consecutive elements (zeros past n);
+// inside a chunk a pairwise tree over consecutive elements (level 1 adds elements 2i and
+// 2i+1, level 2 adds those sums pairwise, ... 13 levels); the chunk totals, padded with
+// zeros to a power of two P, are the leaves of the same pairwise tree.  Every sum is a tree
+// of depth log2(n), so no step waits on a long chain of dependent FP64 adds (each costs
+// about 75 ns on this GPU).  The scratch holds the top tree in heap layout: node j has
+// children 2j and 2j+1, the leaves (chunk totals) sit at [P, 2P).
 // ------------------------------------------------------------------------------------
-__device__ inline double warp_butterfly_sum(double v) {
+// pairwise sum of 32 consecutive elements held one per lane; the result is in lane 0
+__device__ __forceinline__ double lane_pairwise32(double v) {
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
+    for (int sft = 1; sft < 32; sft <<= 1) v = v + __shfl_down_sync(0xffffffffu, v, sft);
     return v;
 }
 
-__device__ inline double det_thread_partial(const DetInput &in, uint64_t base, int t) {
-    double acc = 0.0;
-#pragma unroll 4
-    for (int m = 0; m < kDetPer; ++m) {
-        const uint64_t i = base + uint64_t(t) + uint64_t(kDetThreads) * m;
-        if (i < in.n) acc = acc + in.get(i);
+// one CTA of 256 threads (8 warps x 1024 elements) per chunk; the total goes to leaves[g]
+__global__ void __launch_bounds__(kDetThreads) k_det_chunks(DetInput in, double *leaves) {
+    __shared__ double wt[kDetThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint64_t base = uint64_t(blockIdx.x) * kDetChunk + uint64_t(w) * 1024;
+    double b[32];
+#pragma unroll
+    for (int m = 0; m < 32; ++m) {
+        const uint64_t i = base + uint64_t(m) * 32 + lane;
+        b[m] = i < in.n ? in.get(i) : 0.0;
     }
-    return acc;
-}
-
-// chunk total in the canonical order; every thread of the CTA must call it
-__device__ inline double det_chunk_total(const DetInput &in, uint64_t g, double *sm_warp, double *partial_out) {
-    const int t = threadIdx.x;
-    const double p = det_thread_partial(in, g * uint64_t(kDetChunk), t);
-    if (partial_out) partial_out[t] = p;
-    const double w = warp_butterfly_sum(p);
-    if ((t & 31) == 0) sm_warp[t >> 5] = w;
+#pragma unroll
+    for (int m = 0; m < 32; ++m) b[m] = lane_pairwise32(b[m]);
+#pragma unroll
+    for (int sft = 1; sft < 32; sft <<= 1)
+#pragma unroll
+        for (int m = 0; m < 32; m += 2 * sft) b[m] = b[m] + b[m + sft];
+    if (lane == 0) wt[w] = b[0];
     __syncthreads();
-    double tot = sm_warp[0];
-    for (int i = 1; i < kDetThreads / 32; ++i) tot = tot + sm_warp[i];
+    if (threadIdx.x == 0)
+        leaves[blockIdx.x] = ((wt[0] + wt[1]) + (wt[2] + wt[3])) + ((wt[4] + wt[5]) + (wt[6] + wt[7]));
+}
+
+// block-wide: zero-pads the leaves [P + G, 2P) and builds the internal nodes [1, P) of the
+// heap T (shared or global memory; every thread of the block calls it)
+__device__ void det_heap_build(double *T, uint64_t P, uint64_t G) {
+    for (uint64_t j = P + G + threadIdx.x; j < 2 * P; j += blockDim.x) T[j] = 0.0;
     __syncthreads();
-    return tot;
-}
-
-__global__ void __launch_bounds__(kDetThreads) k_det_chunks(DetInput in, double *chunk_tot) {
-    __shared__ double sm_warp[kDetThreads / 32];
-    const double tot = det_chunk_total(in, blockIdx.x, sm_warp, nullptr);
-    if (threadIdx.x == 0) chunk_tot[blockIdx.x] = tot;
-}
-
-__global__ void k_det_final(const double *chunk_tot, uint64_t G, double *out) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        double s = 0.0;
-        for (uint64_t g = 0; g < G; ++g) s = s + chunk_tot[g];
-        *out = s;
+    for (uint64_t lv = P >> 1; lv >= 1; lv >>= 1) {
+        for (uint64_t j = lv + threadIdx.x; j < 2 * lv; j += blockDim.x) T[j] = T[2 * j] + T[2 * j + 1];
+        __syncthreads();
     }
+}
+
+// from the root of a heap with P leaves: left when r < L or R is not positive, else r -= L
+__device__ inline uint64_t det_heap_descend(const double *T, uint64_t P, double &r) {
+    uint64_t j = 1;
+    while (j < P) {
+        const double L = T[2 * j], R = T[2 * j + 1];
+        if (r < L || !(R > 0.0)) {
+            j = 2 * j;
+        } else {
+            r = r - L;
+            j = 2 * j + 1;
+        }
+    }
+    return j - P;
+}
+
+constexpr uint64_t kDetSmemLeaves = 2048;  // tree in shared memory up to this many leaves
+
+__global__ void __launch_bounds__(kDetThreads) k_det_final(double *tree, uint64_t P, uint64_t G, double *out) {
+    __shared__ double sT[2 * kDetSmemLeaves];
+    double *T = tree;
+    if (P <= kDetSmemLeaves) {
+        for (uint64_t g = threadIdx.x; g < G; g += blockDim.x) sT[P + g] = tree[P + g];
+        T = sT;
+    }
+    det_heap_build(T, P, G);
+    if (threadIdx.x == 0) *out = T[1];
 }
 
 int launch_det_sum(const DetInput &in, double *chunk_tmp, double *out, cudaStream_t st) {
-    const uint64_t G = det_chunks(in.n);
-    if (G > 0) k_det_chunks<<<unsigned(G), kDetThreads, 0, st>>>(in, chunk_tmp), note_launch();
-    k_det_final<<<1, 32, 0, st>>>(chunk_tmp, G, out), note_launch();
+    const uint64_t G = det_chunks(in.n), P = det_leaves(in.n);
+    if (G == 0) {
+        MC_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double), st));
+        return MC_OK;
+    }
+    k_det_chunks<<<unsigned(G), kDetThreads, 0, st>>>(in, chunk_tmp + P), note_launch();
+    k_det_final<<<1, kDetThreads, 0, st>>>(chunk_tmp, P, G, out), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }
 
 // ------------------------------------------------------------------------------------
-// det draw: chunk totals (k_det_chunks), then a single CTA walks the canonical order.
-// If the total is not positive, the first maximum of fallback_vals (or index 0) is taken,
-// as kmeanspp's argmax fallback does (kmeans.h:179-186).  The sequential FP64 walks read
-// from shared memory: the chunk totals (up to kDrawSmemChunks of them), the selected
-// chunk's 256 thread partials and the selected thread's 32 elements are staged by all
-// threads first.
+// det draw: chunk totals (k_det_chunks), then one CTA builds the top tree, descends it with
+// r = u * S to a chunk, recomputes that chunk's 256 sums of 32 elements (the same pairwise
+// arithmetic as k_det_chunks), descends their tree to a 32-element block and that block's
+// tree to one element.  If the total is not positive, the first maximum of fallback_vals
+// (or index 0) is taken, as kmeanspp's argmax fallback does (kmeans.h:179-186).
 // ------------------------------------------------------------------------------------
-constexpr uint64_t kDrawSmemChunks = 4096;
-
-__global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, const double *chunk_tot, const double *u_dev,
+__global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, double *tree, const double *u_dev,
                                                           double u_host, int use_dev_u, const double *fallback_vals,
                                                           uint64_t *out_idx) {
-    __shared__ double sm_warp[kDetThreads / 32];
-    __shared__ double sm_part[kDetThreads];
-    __shared__ double sm_chunk[kDrawSmemChunks];
-    __shared__ double sm_elem[kDetPer];
-    __shared__ int64_t sm_sel;
+    __shared__ double sT[2 * kDetSmemLeaves];
+    __shared__ double H[2 * kDetThreads];
+    __shared__ double E[64];
+    __shared__ uint64_t sm_g, sm_b;
     __shared__ double sm_r;
-    __shared__ int sm_clamp, sm_tau;
+    __shared__ int sm_pos;
     const int t = threadIdx.x;
-    const uint64_t G = det_chunks(in.n);
-    const bool staged = G <= kDrawSmemChunks;
-    if (staged)
-        for (uint64_t g = t; g < G; g += kDetThreads) sm_chunk[g] = chunk_tot[g];
-    __syncthreads();
-    const double *ct = staged ? sm_chunk : chunk_tot;
+    const uint64_t G = det_chunks(in.n), P = det_leaves(in.n);
+    double *T = tree;
+    if (P <= kDetSmemLeaves) {
+        for (uint64_t g = t; g < G; g += blockDim.x) sT[P + g] = tree[P + g];
+        T = sT;
+    }
+    det_heap_build(T, P, G);
     if (t == 0) {
-        double S = 0.0;
-        for (uint64_t g = 0; g < G; ++g) S = S + ct[g];
-        int64_t gs = -1;
-        int clamp = 0;
-        double C = 0.0, tt = 0.0;
+        const double S = T[1];
+        sm_pos = S > 0.0;
         if (S > 0.0) {
-            const double u = use_dev_u ? *u_dev : u_host;
-            tt = u * S;
-            for (uint64_t g = 0; g < G; ++g) {
-                if (C + ct[g] > tt) { gs = int64_t(g); break; }
-                C = C + ct[g];
-            }
-            if (gs < 0) {
-                for (int64_t g = int64_t(G) - 1; g >= 0; --g)
-                    if (ct[g] > 0.0) { gs = g; break; }
-                clamp = 1;
-            }
+            double r = (use_dev_u ? *u_dev : u_host) * S;
+            sm_g = det_heap_descend(T, P, r);
+            sm_r = r;
         }
-        sm_sel = gs;
-        sm_r = tt - C;
-        sm_clamp = clamp;
     }
     __syncthreads();
-    const int64_t gs = sm_sel;
-    if (gs < 0) {  // total not positive: argmax fallback (first maximum) over fallback_vals
+    if (!sm_pos) {  // total not positive: argmax fallback (first maximum) over fallback_vals
         if (t == 0) {
             uint64_t am = 0;
             if (fallback_vals) {
@@ -129,69 +146,50 @@ __global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, const dou
         }
         return;
     }
-    (void)det_chunk_total(in, uint64_t(gs), sm_warp, sm_part);
-    __syncthreads();
-    const uint64_t base = uint64_t(gs) * kDetChunk;
-    if (t == 0) {
-        const double r = sm_r;
-        int tau = -1;
-        double Q = 0.0;
-        if (!sm_clamp) {
-            for (int th = 0; th < kDetThreads; ++th) {
-                if (Q + sm_part[th] > r) { tau = th; break; }
-                Q = Q + sm_part[th];
-            }
+    // the chosen chunk: thread t sums its 32 consecutive elements pairwise
+    const uint64_t base = sm_g * kDetChunk;
+    {
+        double v[32];
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+            const uint64_t i = base + uint64_t(t) * 32 + e;
+            v[e] = i < in.n ? in.get(i) : 0.0;
         }
-        if (tau < 0) {
-            // past the end (rounding) or clamped: the last thread with a positive partial
-            for (int th = kDetThreads - 1; th >= 0; --th)
-                if (sm_part[th] > 0.0) { tau = -2 - th; break; }
-        }
-        sm_tau = tau;
-        sm_r = r - Q;
+#pragma unroll
+        for (int sft = 1; sft < 32; sft <<= 1)
+#pragma unroll
+            for (int e = 0; e < 32; e += 2 * sft) v[e] = v[e] + v[e + sft];
+        H[kDetThreads + t] = v[0];
     }
     __syncthreads();
-    const int tau_code = sm_tau;
-    const int th = tau_code >= 0 ? tau_code : (tau_code <= -2 ? -2 - tau_code : -1);
-    if (th >= 0 && t < kDetPer) {
-        const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * t;
-        sm_elem[t] = i < in.n ? in.get(i) : 0.0;
+    det_heap_build(H, kDetThreads, kDetThreads);
+    if (t == 0) {
+        double r = sm_r;
+        sm_b = det_heap_descend(H, kDetThreads, r);
+        sm_r = r;
     }
     __syncthreads();
-    if (t == 0) {
-        auto last_pos = [&]() -> uint64_t {
-            uint64_t best = in.n;
-            for (int m = 0; m < kDetPer; ++m) {
-                const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * m;
-                if (i < in.n && sm_elem[m] > 0.0) best = i;
-            }
-            return best;
-        };
-        uint64_t res = in.n;
-        if (th < 0) {
-            res = in.n;
-        } else if (tau_code < 0) {
-            res = last_pos();
-        } else {
-            const double r2 = sm_r;
-            double R = 0.0;
-            for (int m = 0; m < kDetPer; ++m) {
-                const uint64_t i = base + uint64_t(th) + uint64_t(kDetThreads) * m;
-                const double val = sm_elem[m];
-                if (R + val > r2) { res = i; break; }
-                R = R + val;
-            }
-            if (res == in.n) res = last_pos();
+    if (t < 32) {  // the chosen block's 32 elements and their tree
+        const uint64_t i = base + sm_b * 32 + t;
+        E[32 + t] = i < in.n ? in.get(i) : 0.0;
+        __syncwarp();
+        for (int lv = 16; lv >= 1; lv >>= 1) {
+            if (t < lv) E[lv + t] = E[2 * (lv + t)] + E[2 * (lv + t) + 1];
+            __syncwarp();
         }
-        if (res >= in.n) res = 0;
-        *out_idx = res;
+        if (t == 0) {
+            double r = sm_r;
+            uint64_t res = base + sm_b * 32 + det_heap_descend(E, 32, r);
+            if (res >= in.n) res = 0;
+            *out_idx = res;
+        }
     }
 }
 
 int launch_det_draw(const DetInput &in, double *chunk_tmp, const double *u_dev, double u_host, int use_dev_u,
                     const double *fallback_vals, uint64_t *out_idx, cudaStream_t st) {
-    const uint64_t G = det_chunks(in.n);
-    if (G > 0) k_det_chunks<<<unsigned(G), kDetThreads, 0, st>>>(in, chunk_tmp), note_launch();
+    const uint64_t G = det_chunks(in.n), P = det_leaves(in.n);
+    if (G > 0) k_det_chunks<<<unsigned(G), kDetThreads, 0, st>>>(in, chunk_tmp + P), note_launch();
     k_det_draw<<<1, kDetThreads, 0, st>>>(in, chunk_tmp, u_dev, u_host, use_dev_u, fallback_vals, out_idx), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;

@@ -56,56 +56,70 @@ inline double uniform_at(uint64_t seed, uint64_t i) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Canonical deterministic FP64 sums (mirrors the CUDA det_sum kernels exactly).
-// A chunk is 8192 elements; 256 "threads" each sum 32 strided elements sequentially;
-// each warp of 32 partials is reduced by an xor butterfly (lane 0's value); the 8 warp
-// totals are summed sequentially; chunk totals are summed sequentially.
+// Canonical deterministic FP64 sums and draws (mirrors the CUDA det kernels exactly).
+// Chunks of 8192 consecutive elements (zeros past n).  Inside a chunk, a pairwise tree over
+// consecutive elements: level 1 adds elements (2i, 2i+1), level 2 adds the level-1 sums
+// (2i, 2i+1), ... 13 levels to the chunk total.  The chunk totals, padded with zeros to a
+// power of two P, form the leaves of the same pairwise tree, whose root is the sum.
+// A draw with uniform u descends the tree from the root with r = u * S: at a node with
+// children sums (L, R), go left when r < L or R is not positive, else r -= L and go right;
+// at the chunk it continues down the chunk's tree to one element.
 // ---------------------------------------------------------------------------------------
 constexpr uint64_t kChunk = 8192, kThreads = 256, kPer = 32;
 
-template <class Get>
-double thread_partial(const Get &get, uint64_t n, uint64_t base, uint64_t t) {
-    double acc = 0.0;
-    for (uint64_t m = 0; m < kPer; ++m) {
-        uint64_t i = base + t + kThreads * m;
-        if (i < n) acc = acc + get(i);
-    }
-    return acc;
-}
-
-inline double warp_butterfly(double *v) {  // v[32], returns lane 0 result of xor butterfly
-    double cur[32], nxt[32];
-    for (int l = 0; l < 32; ++l) cur[l] = v[l];
-    for (int off = 16; off >= 1; off >>= 1) {
-        for (int l = 0; l < 32; ++l) nxt[l] = cur[l] + cur[l ^ off];
-        std::memcpy(cur, nxt, sizeof(cur));
-    }
-    return cur[0];
+// heap layout: node j has children 2j, 2j+1; leaves at [P, 2P)
+inline void build_heap(std::vector<double> &T, uint64_t P) {
+    for (uint64_t j = P - 1; j >= 1; --j) T[j] = T[2 * j] + T[2 * j + 1];
 }
 
 template <class Get>
-double chunk_total(const Get &get, uint64_t n, uint64_t g, double *partials_out = nullptr) {
+void chunk_heap(const Get &get, uint64_t n, uint64_t g, std::vector<double> &H) {
+    H.assign(2 * kChunk, 0.0);
     const uint64_t base = g * kChunk;
-    double p[kThreads];
-    for (uint64_t t = 0; t < kThreads; ++t) p[t] = thread_partial(get, n, base, t);
-    if (partials_out) std::memcpy(partials_out, p, sizeof(p));
-    double wsum[8];
-    for (int w = 0; w < 8; ++w) wsum[w] = warp_butterfly(p + 32 * w);
-    double tot = wsum[0];
-    for (int w = 1; w < 8; ++w) tot = tot + wsum[w];
-    return tot;
+    for (uint64_t e = 0; e < kChunk; ++e) H[kChunk + e] = base + e < n ? get(base + e) : 0.0;
+    build_heap(H, kChunk);
 }
 
 template <class Get>
-double det_sum(const Get &get, uint64_t n, std::vector<double> *chunk_totals = nullptr) {
+double chunk_total(const Get &get, uint64_t n, uint64_t g) {
+    std::vector<double> H;
+    chunk_heap(get, n, g, H);
+    return H[1];
+}
+
+inline uint64_t pow2_at_least(uint64_t x) {
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+template <class Get>
+double det_sum(const Get &get, uint64_t n, std::vector<double> *top = nullptr) {
     const uint64_t G = (n + kChunk - 1) / kChunk;
-    std::vector<double> T(G);
+    if (G == 0) return 0.0;
+    const uint64_t P = pow2_at_least(G);
+    std::vector<double> T(2 * P, 0.0);
 #pragma omp parallel for schedule(static)
-    for (int64_t g = 0; g < int64_t(G); ++g) T[g] = chunk_total(get, n, uint64_t(g));
-    double s = 0.0;
-    for (uint64_t g = 0; g < G; ++g) s = s + T[g];
-    if (chunk_totals) *chunk_totals = std::move(T);
-    return s;
+    for (int64_t g = 0; g < int64_t(G); ++g) T[P + uint64_t(g)] = chunk_total(get, n, uint64_t(g));
+    build_heap(T, P);
+    const double S = P > 1 ? T[1] : T[P];
+    if (top) *top = std::move(T);
+    return S;
+}
+
+// descend a heap of P leaves from the root; returns the leaf and leaves the remainder in r
+inline uint64_t heap_descend(const std::vector<double> &T, uint64_t P, double &r) {
+    uint64_t j = 1;
+    while (j < P) {
+        const double L = T[2 * j], R = T[2 * j + 1];
+        if (r < L || !(R > 0.0)) {
+            j = 2 * j;
+        } else {
+            r = r - L;
+            j = 2 * j + 1;
+        }
+    }
+    return j - P;
 }
 
 // Inverse-CDF draw over non-negative weights v[0..n) with uniform u.  Returns n when the
@@ -115,53 +129,14 @@ uint64_t det_draw(const Get &get, uint64_t n, double u) {
     std::vector<double> T;
     const double S = det_sum(get, n, &T);
     if (!(S > 0.0)) return n;
-    const uint64_t G = T.size();
-    const double t = u * S;
-    double C = 0.0;
-    int64_t gs = -1;
-    for (uint64_t g = 0; g < G; ++g) {
-        if (C + T[g] > t) { gs = int64_t(g); break; }
-        C = C + T[g];
-    }
-    bool clamp = false;
-    if (gs < 0) {  // rounding pushed t past the running total: take the last positive chunk
-        for (int64_t g = int64_t(G) - 1; g >= 0; --g) if (T[g] > 0.0) { gs = g; break; }
-        clamp = true;
-    }
-    const uint64_t base = uint64_t(gs) * kChunk;
-    double P[kThreads];
-    chunk_total(get, n, uint64_t(gs), P);
-    const double r = t - C;
-    int64_t tau = -1;
-    double Q = 0.0;
-    if (!clamp) {
-        for (uint64_t th = 0; th < kThreads; ++th) {
-            if (Q + P[th] > r) { tau = int64_t(th); break; }
-            Q = Q + P[th];
-        }
-    }
-    auto last_pos_in_thread = [&](uint64_t th) -> uint64_t {
-        uint64_t best = n;
-        for (uint64_t m = 0; m < kPer; ++m) {
-            uint64_t i = base + th + kThreads * m;
-            if (i < n && get(i) > 0.0) best = i;
-        }
-        return best;
-    };
-    if (tau < 0) {
-        for (int64_t th = int64_t(kThreads) - 1; th >= 0; --th)
-            if (P[th] > 0.0) return last_pos_in_thread(uint64_t(th));
-        return n;
-    }
-    const double r2 = r - Q;
-    double R = 0.0;
-    for (uint64_t m = 0; m < kPer; ++m) {
-        uint64_t i = base + uint64_t(tau) + kThreads * m;
-        double val = i < n ? get(i) : 0.0;
-        if (R + val > r2) return i;
-        R = R + val;
-    }
-    return last_pos_in_thread(uint64_t(tau));
+    const uint64_t G = (n + kChunk - 1) / kChunk;
+    const uint64_t P = pow2_at_least(G);
+    double r = u * S;
+    const uint64_t g = P > 1 ? heap_descend(T, P, r) : 0;
+    std::vector<double> H;
+    chunk_heap(get, n, g, H);
+    const uint64_t e = heap_descend(H, kChunk, r);
+    return g * kChunk + e;
 }
 
 // ---------------------------------------------------------------------------------------

@@ -123,16 +123,11 @@ def test_det_sum_and_draw(orc):
     rng = np.random.default_rng(1)
     v = rng.random(100_003)
     assert orc.det_sum(v) == pytest.approx(v.sum(), rel=1e-13)
-    # canonical visiting order: chunks of 8192 in order; within a chunk, thread-major over
-    # 256 threads, each thread visiting its 32 strided elements (t, t+256, ...)
+    # canonical order: the elements in index order (pairwise trees inside 8192-element
+    # chunks and over the chunk totals)
     n = v.size
-    order = []
-    for base in range(0, n, 8192):
-        for t in range(256):
-            order.extend(i for i in range(base + t, min(n, base + 8192), 256))
-    order = np.array(order)
-    pos = np.empty(n, dtype=np.int64)
-    pos[order] = np.arange(n)
+    order = np.arange(n)
+    pos = np.arange(n)
     c = np.cumsum(v[order])
     for u in rng.random(200):
         i = orc.det_draw(v, u)
@@ -146,6 +141,30 @@ def test_det_sum_and_draw(orc):
     w = np.zeros(20000)
     w[12345] = 3.0
     assert orc.det_draw(w, 0.999) == 12345
+    assert orc.det_draw(w, 0.0) == 12345
+
+
+def test_det_sum_is_the_pairwise_tree(orc):
+    """The canonical sum: pairwise over consecutive elements inside 8192-element chunks,
+    then pairwise over the chunk totals padded with zeros to a power of two."""
+    rng = np.random.default_rng(5)
+    for n in (1, 31, 8192, 8193, 3 * 8192 + 17, 100_003):
+        v = rng.random(n) * 10.0 ** rng.integers(-8, 8, n)
+
+        def pairwise(x):
+            x = list(x)
+            while len(x) > 1:
+                x = [x[i] + x[i + 1] for i in range(0, len(x), 2)]
+            return x[0]
+
+        G = -(-n // 8192)
+        pad = np.zeros(G * 8192)
+        pad[:n] = v
+        tot = [pairwise(pad[g * 8192:(g + 1) * 8192]) for g in range(G)]
+        P = 1
+        while P < G:
+            P *= 2
+        assert orc.det_sum(v) == pairwise(tot + [0.0] * (P - G))
 
 
 def test_uniform_stream_properties(orc):
