@@ -1054,7 +1054,8 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
     }
     if (j->M.kind == MC_DENSE_F32) {
         MC_TRY(j->rownorm.alloc(n, st));
-        MC_TRY(launch_row_sums_dense(j->M.X, n, d, j->rowsum.p, j->rownorm.p, st));
+        // SQRL2 reads no row sums (the prior does not enter it)
+        MC_TRY(launch_row_sums_dense(j->M.X, n, d, msr == SQRL2 ? nullptr : j->rowsum.p, j->rownorm.p, st));
     } else {
         MC_TRY(launch_row_sums_csr(j->M.vals, j->M.indptr, n, j->rowsum.p, st));
     }
@@ -1608,8 +1609,8 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
         MC_TRY(w.alloc(n, st));
         MC_CUDA_TRY(cudaMemcpyAsync(w.p, weights, n * sizeof(double), cudaMemcpyDefault, st));
     }
-    if (M.kind == MC_DENSE_F32) MC_TRY(launch_row_sums_dense(M.X, n, d, rowsum.p, nullptr, st));
-    else MC_TRY(launch_row_sums_csr(M.vals, M.indptr, n, rowsum.p, st));
+    if (M.kind != MC_DENSE_F32) MC_TRY(launch_row_sums_csr(M.vals, M.indptr, n, rowsum.p, st));
+    else if (msr != SQRL2) MC_TRY(launch_row_sums_dense(M.X, n, d, rowsum.p, nullptr, st));  // SQRL2 reads none
     KmppArgs a;
     a.msr = msr;
     a.csr = M.kind == MC_CSR_F32;

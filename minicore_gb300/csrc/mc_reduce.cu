@@ -27,24 +27,28 @@ __device__ __forceinline__ double lane_pairwise32(double v) {
     return v;
 }
 
-// one CTA of 256 threads (8 warps x 1024 elements) per chunk; the total goes to leaves[g]
-__global__ void __launch_bounds__(kDetThreads) k_det_chunks(DetInput in, double *leaves) {
-    __shared__ double wt[kDetThreads / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint64_t base = uint64_t(blockIdx.x) * kDetChunk + uint64_t(w) * 1024;
-    double b[32];
+// pairwise sum of the 32 consecutive elements [b, b + 32) in registers (31 adds: GB300 issues
+// about two FP64 adds per SM clock, so no add is spent on idle lanes)
+__device__ __forceinline__ double det_block32(const DetInput &in, uint64_t b) {
+    double v[32];
 #pragma unroll
-    for (int m = 0; m < 32; ++m) {
-        const uint64_t i = base + uint64_t(m) * 32 + lane;
-        b[m] = i < in.n ? in.get(i) : 0.0;
-    }
-#pragma unroll
-    for (int m = 0; m < 32; ++m) b[m] = lane_pairwise32(b[m]);
+    for (int e = 0; e < 32; ++e) v[e] = b + e < in.n ? in.get(b + e) : 0.0;
 #pragma unroll
     for (int sft = 1; sft < 32; sft <<= 1)
 #pragma unroll
-        for (int m = 0; m < 32; m += 2 * sft) b[m] = b[m] + b[m + sft];
-    if (lane == 0) wt[w] = b[0];
+        for (int e = 0; e < 32; e += 2 * sft) v[e] = v[e] + v[e + sft];
+    return v[0];
+}
+
+// one CTA of 256 threads per chunk: thread t sums elements [32t, 32t + 32) of the chunk, the
+// lanes' block sums go pairwise to lane 0 (1024 elements per warp), the 8 warp totals
+// pairwise to the chunk total in leaves[g]
+__global__ void __launch_bounds__(kDetThreads) k_det_chunks(DetInput in, double *leaves) {
+    __shared__ double wt[kDetThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double b = det_block32(in, uint64_t(blockIdx.x) * kDetChunk + uint64_t(threadIdx.x) * 32);
+    b = lane_pairwise32(b);
+    if (lane == 0) wt[w] = b;
     __syncthreads();
     if (threadIdx.x == 0)
         leaves[blockIdx.x] = ((wt[0] + wt[1]) + (wt[2] + wt[3])) + ((wt[4] + wt[5]) + (wt[6] + wt[7]));
@@ -146,21 +150,9 @@ __global__ void __launch_bounds__(kDetThreads) k_det_draw(DetInput in, double *t
         }
         return;
     }
-    // the chosen chunk: thread t sums its 32 consecutive elements pairwise
+    // the chosen chunk: thread t sums its 32 consecutive elements pairwise (as k_det_chunks)
     const uint64_t base = sm_g * kDetChunk;
-    {
-        double v[32];
-#pragma unroll
-        for (int e = 0; e < 32; ++e) {
-            const uint64_t i = base + uint64_t(t) * 32 + e;
-            v[e] = i < in.n ? in.get(i) : 0.0;
-        }
-#pragma unroll
-        for (int sft = 1; sft < 32; sft <<= 1)
-#pragma unroll
-            for (int e = 0; e < 32; e += 2 * sft) v[e] = v[e] + v[e + sft];
-        H[kDetThreads + t] = v[0];
-    }
+    H[kDetThreads + t] = det_block32(in, base + uint64_t(t) * 32);
     __syncthreads();
     det_heap_build(H, kDetThreads, kDetThreads);
     if (t == 0) {
@@ -203,14 +195,18 @@ __global__ void k_row_sums_dense(const float *__restrict__ X, uint64_t n, uint64
     const uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
     if (i >= n) return;
     const float *r = X + i * d;
-    double s = 0.0;
     float q = 0.f;
-    for (uint64_t j = 0; j < d; ++j) {
-        const float v = r[j];
-        s = s + double(v);
-        q = fmaf(v, v, q);
+    if (rowsum) {
+        double s = 0.0;
+        for (uint64_t j = 0; j < d; ++j) {
+            const float v = r[j];
+            s = s + double(v);
+            q = fmaf(v, v, q);
+        }
+        rowsum[i] = s;
+    } else {  // norms only: no FP64 work (about two FP64 adds per SM clock on this GPU)
+        for (uint64_t j = 0; j < d; ++j) q = fmaf(r[j], r[j], q);
     }
-    rowsum[i] = s;
     if (rownorm) rownorm[i] = q;
 }
 
@@ -389,8 +385,70 @@ __global__ void k_sort_scatter2(const uint32_t *__restrict__ keys, const uint32_
     }
 }
 
+// long integer scans (row lists, flags over n rows): tiles of 4096 values, 16 consecutive per
+// thread; tile totals, one CTA scans them, then every tile writes its values
+constexpr int kScanTile = 4096;
+
+__device__ __forceinline__ uint64_t block_exclusive_scan_u64(uint64_t v, uint64_t *warp_tot) {
+    // exclusive scan over the 256 threads of the block; warp_tot: 8 slots of shared memory
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint64_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    uint64_t before = 0;
+    for (int q = 0; q < w; ++q) before += warp_tot[q];
+    __syncthreads();
+    return before + inc - v;
+}
+
+__global__ void __launch_bounds__(256) k_scan_tile_sums(const uint64_t *__restrict__ in, uint64_t m, uint64_t *tile_sum) {
+    __shared__ uint64_t wt[8];
+    const uint64_t b = uint64_t(blockIdx.x) * kScanTile + uint64_t(threadIdx.x) * 16;
+    uint64_t s = 0;
+#pragma unroll
+    for (int e = 0; e < 16; ++e)
+        if (b + e < m) s += in[b + e];
+    const uint64_t ex = block_exclusive_scan_u64(s, wt);
+    if (threadIdx.x == 255) tile_sum[blockIdx.x] = ex + s;
+}
+
+__global__ void __launch_bounds__(256) k_scan_tile_write(const uint64_t *__restrict__ in, uint64_t m,
+                                                         const uint64_t *__restrict__ tile_off, uint64_t *out) {
+    __shared__ uint64_t wt[8];
+    const uint64_t b = uint64_t(blockIdx.x) * kScanTile + uint64_t(threadIdx.x) * 16;
+    uint64_t v[16], s = 0;
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+        v[e] = b + e < m ? in[b + e] : 0;
+        s += v[e];
+    }
+    uint64_t acc = tile_off[blockIdx.x] + block_exclusive_scan_u64(s, wt);
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+        if (b + e < m) out[b + e] = acc;
+        acc += v[e];
+    }
+}
+
 int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st) {
-    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(in, out, m), note_launch();
+    if (m <= 16 * 1024) {  // one CTA
+        k_exclusive_scan_u64<<<1, 1024, 0, st>>>(in, out, m), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        return MC_OK;
+    }
+    const uint64_t nt = (m + kScanTile - 1) / kScanTile;
+    DBuf<uint64_t> tsum, toff;  // freed in stream order
+    MC_TRY(tsum.alloc(nt, st));
+    MC_TRY(toff.alloc(nt + 1, st));
+    k_scan_tile_sums<<<unsigned(nt), 256, 0, st>>>(in, m, tsum.p), note_launch();
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(tsum.p, toff.p, nt), note_launch();
+    k_scan_tile_write<<<unsigned(nt), 256, 0, st>>>(in, m, toff.p, out), note_launch();
+    MC_CUDA_TRY(cudaMemcpyAsync(out + m, toff.p + nt, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }
