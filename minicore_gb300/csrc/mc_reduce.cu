@@ -335,9 +335,10 @@ __global__ void k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t
 __global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, uint32_t k, uint64_t ntiles,
                                uint32_t *tile_offsets, const uint64_t *__restrict__ bucket_start, uint32_t *perm) {
     // one warp per tile; rows in order, 32 at a time; ranks from match_any.  Cursors live in
-    // shared memory when k is small enough (one warp per block), else in the tile's column
-    // of tile_offsets (stride ntiles).
-    __shared__ uint32_t scur[kSmemKeys];
+    // dynamic shared memory sized to k when k <= kSmemKeys (so that many one-warp blocks fit
+    // on an SM), else in the tile's column of tile_offsets (stride ntiles).  The keys of 16
+    // rounds are loaded ahead of their use.
+    extern __shared__ uint32_t scur[];
     const uint64_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31;
     const uint64_t b = tile * kSortTile;
@@ -351,20 +352,30 @@ __global__ void k_sort_scatter(const uint32_t *__restrict__ keys, uint64_t n, ui
     uint32_t *cur = sm ? scur : tile_offsets + tile;
     const uint64_t cstride = sm ? 1 : ntiles;
     const unsigned lt = (1u << lane) - 1u;
-    for (uint64_t base = b; base < e; base += 32) {
-        const uint64_t i = base + lane;
-        const bool act = i < e;
-        const uint32_t key = act ? keys[i] : 0xffffffffu;
-        const unsigned actmask = __ballot_sync(0xffffffffu, act);
-        const unsigned peers = __match_any_sync(0xffffffffu, key) & actmask;
-        uint32_t off = 0;
-        if (act) off = cur[uint64_t(key) * cstride];
-        __syncwarp();
-        if (act) {
-            perm[bucket_start[key] + off + __popc(peers & lt)] = uint32_t(i);
-            if ((peers & lt) == 0) cur[uint64_t(key) * cstride] = off + __popc(peers);
+    for (uint64_t base0 = b; base0 < e; base0 += 32 * 16) {
+        uint32_t kr[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const uint64_t i = base0 + uint64_t(r) * 32 + lane;
+            kr[r] = i < e ? keys[i] : 0xffffffffu;
         }
-        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const uint64_t i = base0 + uint64_t(r) * 32 + lane;
+            const bool act = i < e;
+            const uint32_t key = kr[r];
+            const unsigned actmask = __ballot_sync(0xffffffffu, act);
+            if (!actmask) break;
+            const unsigned peers = __match_any_sync(0xffffffffu, key) & actmask;
+            uint32_t off = 0;
+            if (act) off = cur[uint64_t(key) * cstride];
+            __syncwarp();
+            if (act) {
+                perm[bucket_start[key] + off + __popc(peers & lt)] = uint32_t(i);
+                if ((peers & lt) == 0) cur[uint64_t(key) * cstride] = off + __popc(peers);
+            }
+            __syncwarp();
+        }
     }
 }
 
@@ -469,7 +480,8 @@ int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, 
     k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.bucket_count.p, w.bucket_start.p, k), note_launch();
     if (ntiles) {
         if (!keys2)
-            k_sort_scatter<<<unsigned(ntiles), 32, 0, st>>>(keys, n, k, ntiles, w.tile_counts.p, w.bucket_start.p,
+            k_sort_scatter<<<unsigned(ntiles), 32, k <= kSmemKeys ? k * sizeof(uint32_t) : 0, st>>>(
+                keys, n, k, ntiles, w.tile_counts.p, w.bucket_start.p,
                                                             w.perm.p), note_launch();
         else
             k_sort_scatter2<<<unsigned((ntiles + 63) / 64), 64, 0, st>>>(keys, keys2, n, k, ntiles,

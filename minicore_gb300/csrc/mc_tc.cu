@@ -536,19 +536,24 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
     unsigned base = 0;
     if (lane == 0 && mb) base = atomicAdd(count, unsigned(__popc(mb)));
     base = __shfl_sync(0xffffffffu, base, 0);
+    const unsigned slot = base + unsigned(__popc(mb & ((1u << lane) - 1u)));
     if (multi) {
-        const unsigned slot = base + unsigned(__popc(mb & ((1u << lane) - 1u)));
         if (slot < cap) {
             status[row] = ST_MULTI | slot;
             key[row] = nsg;
             crow[slot] = uint32_t(row);
             thrc[slot] = thr;
-            const uint4 *src = A + row * row_u4;
-            uint4 *dst = Xc + uint64_t(slot) * row_u4;
-            for (uint64_t q = 0; q < row_u4; ++q) dst[q] = src[q];
         } else {
             over = true;  // compact buffer full: exact rescan
         }
+    }
+    // operand copies of the warp's multi rows, one row at a time by the whole warp (coalesced)
+    for (unsigned m = mb; m; m &= m - 1) {
+        const int src = __ffs(m) - 1;
+        const uint64_t r = __shfl_sync(0xffffffffu, row, src);
+        const unsigned sl = __shfl_sync(0xffffffffu, slot, src);
+        if (sl < cap)
+            for (uint64_t q = lane; q < row_u4; q += 32) Xc[uint64_t(sl) * row_u4 + q] = A[r * row_u4 + q];
     }
     const unsigned ob = __ballot_sync(0xffffffffu, over);
     unsigned long long obase = 0;
@@ -614,6 +619,39 @@ __device__ __forceinline__ void fin_chunk_scalar(const float *cr, const float *x
     }
 }
 
+// staged centers: two subgroups of 8, stored as 4 pairs per subgroup with the pair's two
+// values of a column side by side, so that one 64-bit word feeds a packed f32x2 operation
+// (center q of subgroup s, column j) -> ((4 s + q / 2) d + j) 2 + q % 2
+__device__ __forceinline__ const float *fin_pair_col(const float *sub_base, int q, uint64_t d, uint64_t j) {
+    return sub_base + ((uint64_t(q >> 1) * d + j) << 1) + (q & 1);
+}
+
+// fin_chunk_scalar over the pair layout (stride 2)
+__device__ __forceinline__ void fin_chunk_scalar2(const float *cr, const float *xrow, int kmax, float &a) {
+    for (int kk = 0; kk < kmax; ++kk) {
+        const float df = cr[2 * kk] - xrow[kk];
+        a = fmaf(df, df, a);
+    }
+}
+
+// packed f32x2 (sm_100 family): each half is the IEEE single operation of the scalar code
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+// a = fma(c - x, c - x, a) in both halves
+__device__ __forceinline__ unsigned long long f2_sqdiff_acc(unsigned long long c, unsigned long long x,
+                                                           unsigned long long a) {
+    unsigned long long df, r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(df) : "l"(c), "l"(x));
+    asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(r) : "l"(df), "l"(a));
+    return r;
+}
+
 template <bool VEC4>
 __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restrict__ X, uint64_t n, uint64_t d,
                                                            const float *__restrict__ C, uint32_t k, uint32_t nsg,
@@ -624,7 +662,7 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
                                                            const uint32_t *__restrict__ cand, double *costs,
                                                            uint32_t *over_rows, unsigned long long *nover) {
     constexpr int R = FIN_ROWS;
-    extern __shared__ __align__(16) float cs[];  // [FIN_SG][8][d] staged centers
+    extern __shared__ __align__(16) float cs[];  // [FIN_SG][4 pairs][d][2] staged centers
     __shared__ __align__(16) float xs4[2][R][36];  // two 32-column stages (rows 144 B apart)
     __shared__ uint32_t rows_s[R];
     __shared__ uint32_t sg_first;
@@ -684,12 +722,35 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
         const uint32_t tot = uint32_t(FIN_SG * 8 * d);
         const float *src = C + j0 * d;
         if (VEC4) {
-            const float4 *s4 = reinterpret_cast<const float4 *>(src);
-            float4 *d4 = reinterpret_cast<float4 *>(cs);
-            for (uint32_t e = t; e < tot / 4; e += R)
-                d4[e] = 4 * e < valid ? __ldg(s4 + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+            // float4 items (center cl, columns 4 j4 .. 4 j4 + 3), R apart, four loads in flight
+            const uint32_t dq = uint32_t(d / 4), items = tot / 4;
+            for (uint32_t e0 = t; e0 < items; e0 += 4 * R) {
+                float4 v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t e = e0 + uint32_t(u) * R;
+                    v[u] = (e < items && 4 * e < valid) ? __ldg(reinterpret_cast<const float4 *>(src) + e)
+                                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t e = e0 + uint32_t(u) * R;
+                    if (e < items) {
+                        const uint32_t cl = e / dq, j = 4 * (e - cl * dq);
+                        float *dst = cs + uint64_t(cl >> 3) * 8 * d + ((uint64_t((cl & 7) >> 1) * d + j) << 1) + (cl & 1);
+                        dst[0] = v[u].x;
+                        dst[2] = v[u].y;
+                        dst[4] = v[u].z;
+                        dst[6] = v[u].w;
+                    }
+                }
+            }
         } else {
-            for (uint32_t e = t; e < tot; e += R) cs[e] = e < valid ? src[e] : 0.f;
+            for (uint32_t e = t; e < tot; e += R) {
+                const uint32_t cl = e / uint32_t(d), j = e - cl * uint32_t(d);
+                cs[uint64_t(cl >> 3) * 8 * d + ((uint64_t((cl & 7) >> 1) * d + j) << 1) + (cl & 1)] =
+                    e < valid ? src[e] : 0.f;
+            }
         }
     }
     const bool mine_local = sgf != 0xffffffffu && st != ST_OVER && !(st & ST_MULTI) && !over && st - sgf < FIN_SG;
@@ -740,23 +801,25 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
                 if (warp_local) {
                     if (mine_local) {
                         // all 8 subgroup centers at once (padding centers are zeros and are
-                        // ignored below): 8 independent sequential chains per thread
-                        const float *cb = lbase + k0;
+                        // ignored below): 8 independent sequential chains per thread, two per
+                        // packed f32x2 accumulator (pairs of centers side by side in shared memory)
+                        unsigned long long a2[4];
 #pragma unroll
-                        for (int k4 = 0; k4 < 8; ++k4) {
+                        for (int pq = 0; pq < 4; ++pq) a2[pq] = f2_pack(acc[2 * pq], acc[2 * pq + 1]);
 #pragma unroll
-                            for (int q = 0; q < 8; ++q) {
-                                const float4 c = *reinterpret_cast<const float4 *>(cb + uint64_t(q) * d + 4 * k4);
-                                float df = c.x - xr[4 * k4 + 0];
-                                acc[q] = fmaf(df, df, acc[q]);
-                                df = c.y - xr[4 * k4 + 1];
-                                acc[q] = fmaf(df, df, acc[q]);
-                                df = c.z - xr[4 * k4 + 2];
-                                acc[q] = fmaf(df, df, acc[q]);
-                                df = c.w - xr[4 * k4 + 3];
-                                acc[q] = fmaf(df, df, acc[q]);
+                        for (int k2 = 0; k2 < 16; ++k2) {
+                            const unsigned long long x0 = f2_pack(xr[2 * k2], xr[2 * k2]);
+                            const unsigned long long x1 = f2_pack(xr[2 * k2 + 1], xr[2 * k2 + 1]);
+#pragma unroll
+                            for (int pq = 0; pq < 4; ++pq) {
+                                const ulonglong2 c = *reinterpret_cast<const ulonglong2 *>(
+                                    lbase + ((uint64_t(pq) * d + k0 + 2 * k2) << 1));
+                                a2[pq] = f2_sqdiff_acc(c.x, x0, a2[pq]);
+                                a2[pq] = f2_sqdiff_acc(c.y, x1, a2[pq]);
                             }
                         }
+#pragma unroll
+                        for (int pq = 0; pq < 4; ++pq) f2_unpack(a2[pq], acc[2 * pq], acc[2 * pq + 1]);
                     }
                 } else {
 #pragma unroll
@@ -769,7 +832,7 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
 #pragma unroll
                         for (int q = 0; q < 8; ++q)
                             if (cj[q] != 0xffffffffu)
-                                fin_chunk_scalar(lbase + uint64_t(q) * d + k0, xs4[buf][t], kmax, acc[q]);
+                                fin_chunk_scalar2(fin_pair_col(lbase, q, d, k0), xs4[buf][t], kmax, acc[q]);
                     }
                 } else {
 #pragma unroll
@@ -795,7 +858,7 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
 #pragma unroll
                     for (int q = 0; q < 8; ++q)
                         if (cj[q] != 0xffffffffu)
-                            fin_chunk_scalar(lbase + uint64_t(q) * d + k0, xs4[0][t], kmax, acc[q]);
+                            fin_chunk_scalar2(fin_pair_col(lbase, q, d, k0), xs4[0][t], kmax, acc[q]);
                 }
             } else {
 #pragma unroll
