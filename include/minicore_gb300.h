@@ -261,14 +261,20 @@ int mc_server_destroy(mc_server *s);
  * mc_autotune_enable(0) keeps the defaults. */
 int mc_autotune_enable(int on);
 
-/* mc_job_run (and mc_hcluster, the server's jobs) runs the Lloyd loop as one CUDA graph: a
- * while-conditional node whose body is the centroid update, the assignment pass, the
- * objective and the stop rule, evaluated on the device, so an iteration makes no host round
- * trip (no reference counterpart; the reference's loop is solve.h:98-175).  The graph hands
- * back to the host to finish, or for the D^2 restart of an empty cluster.  Results are those
- * of the host loop.  MC_LOOP_GRAPH=0 or mc_loop_graph_enable(0) keeps the host loop; so does
- * an active mc_profile_enable. */
-int mc_loop_graph_enable(int on);
+/* How mc_job_run (and mc_hcluster, the server's jobs) runs the Lloyd loop (no reference
+ * counterpart; the reference's loop is solve.h:98-175).  Every mode gives the same results.
+ *   MC_LOOP_HOST   the host decides after each step (one round trip per decision)
+ *   MC_LOOP_FUSED  the stop rule (objective test, revert, empty-cluster check) runs on the
+ *                  device after each iteration: one round trip per iteration
+ *   MC_LOOP_GRAPH  one CUDA graph: a while-conditional node whose body is the centroid update,
+ *                  the assignment pass, the objective and the stop rule; one round trip per
+ *                  run, plus one capture and instantiation
+ * Every mode hands back to the host for the D^2 restart of an empty cluster.  -1 (default)
+ * picks the graph for runs of >= 16 iterations over n*d <= 2^24 values, else the fused loop;
+ * the server's workers never use the graph.  MC_LOOP_MODE=0|1|2 sets the mode from the
+ * environment; an active mc_profile_enable keeps the graph off. */
+enum { MC_LOOP_HOST = 0, MC_LOOP_FUSED = 1, MC_LOOP_GRAPH = 2 };
+int mc_loop_mode(int mode);
 int mc_autotune_reset(void);                    /* forget every decision (not the file)      */
 int mc_autotune_load(const char *path);         /* add decisions from a cache file           */
 int mc_autotune_save(const char *path);         /* write every decision to a cache file      */

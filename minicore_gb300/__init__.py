@@ -828,10 +828,14 @@ def kernel_launches() -> int:
     return int(_lib.load().mc_kernel_launches())
 
 
-def loop_graph(enable: bool = True):
-    """Run the Lloyd loop of Job.run / hcluster as one CUDA graph (default) or as a host
-    loop (identical results)."""
-    check(_lib.load().mc_loop_graph_enable(1 if enable else 0))
+LOOP_AUTO, LOOP_HOST, LOOP_FUSED, LOOP_GRAPH = -1, 0, 1, 2
+
+
+def loop_mode(mode: int = LOOP_AUTO):
+    """How Job.run / hcluster run the Lloyd loop: LOOP_HOST (a host round trip per
+    decision), LOOP_FUSED (the stop rule on the device, one round trip per iteration),
+    LOOP_GRAPH (the whole loop as one CUDA graph), LOOP_AUTO.  Results are identical."""
+    check(_lib.load().mc_loop_mode(int(mode)))
 
 
 def autotune_report() -> dict:

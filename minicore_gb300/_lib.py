@@ -74,7 +74,7 @@ SIGNATURES = {
     "mc_job_recheck_count": (I, [P, ctypes.POINTER(U64)]),
     "mc_assign_sqrl2_noalloc": (I, [P, U64, U64, P, U32, P, P, P]),
     "mc_autotune_enable": (I, [I]),
-    "mc_loop_graph_enable": (I, [I]),
+    "mc_loop_mode": (I, [I]),
     "mc_autotune_reset": (I, []),
     "mc_autotune_load": (I, [ctypes.c_char_p]),
     "mc_autotune_save": (I, [ctypes.c_char_p]),

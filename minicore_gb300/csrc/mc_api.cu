@@ -490,8 +490,9 @@ struct LoopState {
     int pad;
 };
 
+// graph != 0: the kernel runs inside the loop graph and also sets its while-condition h
 __global__ void k_loop_check_empty(const uint64_t *__restrict__ bucket_count, uint32_t k, LoopState *ls,
-                                   cudaGraphConditionalHandle h) {
+                                   cudaGraphConditionalHandle h, int graph) {
     __shared__ int any;
     if (ls->reason != LOOP_RUN) return;  // same value for the whole block
     if (threadIdx.x == 0) any = 0;
@@ -501,28 +502,29 @@ __global__ void k_loop_check_empty(const uint64_t *__restrict__ bucket_count, ui
     __syncthreads();
     if (threadIdx.x == 0 && any) {
         ls->reason = LOOP_EMPTY;
-        cudaGraphSetConditional(h, 0);
+        if (graph) cudaGraphSetConditional(h, 0);
     }
 }
 
 // the stop rule of the host loop (perform_hard_clustering, clustering/solve.h:98-175)
 __global__ void k_loop_decide(const double *__restrict__ cost_sum, const int *__restrict__ nan_flag,
-                              const int *__restrict__ tc_err, LoopState *ls, cudaGraphConditionalHandle h) {
+                              const int *__restrict__ tc_err, LoopState *ls, cudaGraphConditionalHandle h,
+                              int graph) {
     ls->commit = 0;
     if (*nan_flag) {
         ls->reason = LOOP_NAN;
-        cudaGraphSetConditional(h, 0);
+        if (graph) cudaGraphSetConditional(h, 0);
         return;
     }
     if (tc_err && *tc_err) {
         ls->reason = LOOP_TIMEOUT;
-        cudaGraphSetConditional(h, 0);
+        if (graph) cudaGraphSetConditional(h, 0);
         return;
     }
     const float newcost = float(*cost_sum);
     if (newcost > ls->cost) {
         ls->reason = LOOP_REVERT;
-        cudaGraphSetConditional(h, 0);
+        if (graph) cudaGraphSetConditional(h, 0);
         return;
     }
     ls->commit = 1;
@@ -532,9 +534,9 @@ __global__ void k_loop_decide(const double *__restrict__ cost_sum, const int *__
     const double mx = double(newcost) < double(oldcost) ? double(oldcost) : double(newcost);
     if (double(oldcost - newcost) < ls->eps * mx || ls->iternum > ls->maxiter) {
         ls->reason = LOOP_DONE;
-        cudaGraphSetConditional(h, 0);
+        if (graph) cudaGraphSetConditional(h, 0);
     } else {
-        cudaGraphSetConditional(h, 1);
+        if (graph) cudaGraphSetConditional(h, 1);
     }
 }
 
@@ -557,6 +559,34 @@ struct CaptureGuard {  // ends an unfinished capture on the error path
     }
 };
 
+// the loop's launch sequences (identical in the graph and in the fused host loop)
+int job_loop_pre(mc_job *j, LoopState *ls, cudaGraphConditionalHandle h, int graph) {
+    MC_TRY(launch_sort_by_key(j->asn.p, nullptr, j->M.n, j->k, j->sort, j->st));
+    k_loop_check_empty<<<1, 256, 0, j->st>>>(j->sort.bucket_count.p, j->k, ls, h, graph), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+int job_loop_body(mc_job *j, LoopState *ls, cudaGraphConditionalHandle h, int graph) {
+    cudaStream_t st = j->st;
+    const uint64_t n = j->M.n, d = j->M.d;
+    const uint32_t k = j->k;
+    const bool tc = j->M.kind == MC_DENSE_F32 && j->msr == SQRL2 && j->precision != MC_FP32;
+    MC_TRY(job_launch_centroids(j, nullptr, 0, /*presorted=*/true));
+    MC_TRY(job_assign_with(j, j->Cw.p, j->psum, false, nullptr, /*graph_mode=*/true));
+    {
+        DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
+        MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
+    }
+    k_loop_decide<<<1, 1, 0, st>>>(j->scal.p, j->flag.p, tc ? j->tc.err.p : nullptr, ls, h, graph), note_launch();
+    const uint64_t m = uint64_t(k) * d;
+    k_loop_commit<<<unsigned(umin64((m + 255) / 256, 1024)), 256, 0, st>>>(ls, j->C.p, j->Cw.p, m), note_launch();
+    MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+    k_loop_check_empty<<<1, 256, 0, st>>>(j->sort.bucket_count.p, k, ls, h, graph), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 int job_build_loop_graph(mc_job *j) {
     if (j->loop_exec) {
         cudaGraphExecDestroy(j->loop_exec);
@@ -568,7 +598,6 @@ int job_build_loop_graph(mc_job *j) {
     MC_TRY(j->loop_state.alloc(sizeof(LoopState), st));
     LoopState *ls = reinterpret_cast<LoopState *>(j->loop_state.p);
     const bool tc = j->M.kind == MC_DENSE_F32 && j->msr == SQRL2 && j->precision != MC_FP32;
-    const int *tc_err = tc ? j->tc.err.p : nullptr;
     // every buffer the body touches exists before the capture: the sort and centroid work
     // space and the tensor-core path's FP32 rescan transform.  The centroid launch writes Cw,
     // which then takes the committed centers back (a restart on the host starts from Cw = C).
@@ -581,7 +610,6 @@ int job_build_loop_graph(mc_job *j) {
     const uint64_t l0 = t_launches;
     MC_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     guard.on = true;
-    MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
     cudaStreamCaptureStatus cs;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t *deps = nullptr;
@@ -589,8 +617,7 @@ int job_build_loop_graph(mc_job *j) {
     MC_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
     cudaGraphConditionalHandle h;
     MC_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
-    k_loop_check_empty<<<1, 256, 0, st>>>(j->sort.bucket_count.p, k, ls, h), note_launch();
-    MC_CUDA_TRY(cudaGetLastError());
+    MC_TRY(job_loop_pre(j, ls, h, 1));
     MC_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &ndeps));
     cudaGraphNodeParams cp = {};
     cp.type = cudaGraphNodeTypeConditional;
@@ -609,18 +636,7 @@ int job_build_loop_graph(mc_job *j) {
     // the loop body, captured into the conditional node's graph
     MC_CUDA_TRY(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     guard.on = true;
-    MC_TRY(job_launch_centroids(j, nullptr, 0, /*presorted=*/true));
-    MC_TRY(job_assign_with(j, j->Cw.p, j->psum, false, nullptr, /*graph_mode=*/true));
-    {
-        DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
-        MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
-    }
-    k_loop_decide<<<1, 1, 0, st>>>(j->scal.p, j->flag.p, tc_err, ls, h), note_launch();
-    const uint64_t m = uint64_t(k) * d;
-    k_loop_commit<<<unsigned(umin64((m + 255) / 256, 1024)), 256, 0, st>>>(ls, j->C.p, j->Cw.p, m), note_launch();
-    MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
-    k_loop_check_empty<<<1, 256, 0, st>>>(j->sort.bucket_count.p, k, ls, h), note_launch();
-    MC_CUDA_TRY(cudaGetLastError());
+    MC_TRY(job_loop_body(j, ls, h, 1));
     cudaGraph_t body_out = nullptr;
     guard.on = false;
     MC_CUDA_TRY(cudaStreamEndCapture(st, &body_out));
@@ -635,21 +651,30 @@ int job_build_loop_graph(mc_job *j) {
     return MC_OK;
 }
 
-std::atomic<int> g_loop_graph{-1};  // -1: from MC_LOOP_GRAPH
-thread_local int t_loop_graph = -1;  // -1: the process setting
+// how mc_job_run runs the Lloyd loop (mc_loop_mode): MC_LOOP_HOST one host round trip per
+// decision, MC_LOOP_FUSED one per iteration, MC_LOOP_GRAPH one per run; -1 = automatic
+std::atomic<int> g_loop_mode{-2};  // -2: from MC_LOOP_MODE
+thread_local int t_loop_graph = -1;  // 0: this thread never uses the graph
 
 void drop_loop_graph(mc_job *j) {
     if (j->loop_exec) cudaGraphExecDestroy(j->loop_exec);
     j->loop_exec = nullptr;
 }
 
-bool loop_graph_enabled() {
-    int on = t_loop_graph >= 0 ? t_loop_graph : g_loop_graph.load();
-    if (on < 0) {
-        const char *e = std::getenv("MC_LOOP_GRAPH");
-        on = (e && e[0] == '0') ? 0 : 1;
+int loop_mode_for(const mc_job *j, uint64_t maxiter) {
+    int mode = g_loop_mode.load();
+    if (mode == -2) {
+        const char *e = std::getenv("MC_LOOP_MODE");
+        mode = (e && e[0] >= '0' && e[0] <= '2' && !e[1]) ? e[0] - '0' : -1;
     }
-    return on == 1 && !profiling_enabled();
+    if (mode < 0) {
+        // the graph pays one capture + instantiation per run; it wins when the run has many
+        // iterations of little device work each
+        const bool small = j->M.n * j->M.d <= (uint64_t(1) << 24);
+        mode = (small && maxiter >= 16) ? MC_LOOP_GRAPH : MC_LOOP_FUSED;
+    }
+    if (mode == MC_LOOP_GRAPH && (t_loop_graph == 0 || profiling_enabled())) mode = MC_LOOP_FUSED;
+    return mode;
 }
 
 // runs the loop graph from the host state (cost, iternum) until it hands back; the state
@@ -674,6 +699,26 @@ int job_run_loop_graph(mc_job *j, LoopState &h, bool *ran) {
     const uint64_t bodies = (h.iternum - it0) + (h.reason == LOOP_REVERT || h.reason == LOOP_NAN ||
                                                   h.reason == LOOP_TIMEOUT ? 1 : 0);
     g_launches.fetch_add(j->loop_pre_launches + bodies * j->loop_body_launches);
+    return MC_OK;
+}
+
+// The same launch sequence without a graph: one host round trip per iteration (the state
+// after the body), instead of one per decision of the host loop.  Runs from the host state
+// until the loop hands back.
+int job_run_loop_fused(mc_job *j, LoopState &h) {
+    cudaStream_t st = j->st;
+    MC_TRY(j->loop_state.alloc(sizeof(LoopState), st));
+    LoopState *ls = reinterpret_cast<LoopState *>(j->loop_state.p);
+    cudaGraphConditionalHandle none = 0;
+    MC_CUDA_TRY(cudaMemcpyAsync(ls, &h, sizeof(LoopState), cudaMemcpyHostToDevice, st));
+    MC_TRY(job_loop_pre(j, ls, none, 0));
+    MC_CUDA_TRY(cudaMemcpyAsync(&h, ls, sizeof(LoopState), cudaMemcpyDeviceToHost, st));
+    MC_TRY(sync(st));
+    while (h.reason == LOOP_RUN) {
+        MC_TRY(job_loop_body(j, ls, none, 0));
+        MC_CUDA_TRY(cudaMemcpyAsync(&h, ls, sizeof(LoopState), cudaMemcpyDeviceToHost, st));
+        MC_TRY(sync(st));
+    }
     return MC_OK;
 }
 
@@ -908,8 +953,9 @@ void set_thread_loop_graph(int on) { t_loop_graph = on; }
 
 extern "C" {
 
-int mc_loop_graph_enable(int on) {
-    g_loop_graph.store(on ? 1 : 0);
+int mc_loop_mode(int mode) {
+    if (mode < -1 || mode > 2) return fail(MC_EINVAL, "loop mode is -1 (automatic), 0, 1 or 2");
+    g_loop_mode.store(mode);
     return MC_OK;
 }
 
@@ -1198,19 +1244,19 @@ int mc_job_run(mc_job *j, double eps, uint64_t maxiter, double *initcost_out, do
     }
     const size_t cbytes = uint64_t(j->k) * j->M.d * sizeof(float);
     MC_CUDA_TRY(cudaMemcpyAsync(j->Cw.p, j->C.p, cbytes, cudaMemcpyDeviceToDevice, j->st));
-    bool graph = loop_graph_enabled();
+    const int mode = loop_mode_for(j, maxiter);
+    bool graph = mode == MC_LOOP_GRAPH, fused = mode != MC_LOOP_HOST;
     drop_loop_graph(j);
     for (;;) {
         LoopState h = {};
-        if (graph) {
-            h.cost = cost;
-            h.reason = LOOP_RUN;
-            h.iternum = iternum;
-            h.maxiter = maxiter;
-            h.eps = eps;
-            MC_TRY(job_run_loop_graph(j, h, &graph));
-        }
-        if (graph) {
+        h.cost = cost;
+        h.reason = LOOP_RUN;
+        h.iternum = iternum;
+        h.maxiter = maxiter;
+        h.eps = eps;
+        if (graph) MC_TRY(job_run_loop_graph(j, h, &graph));  // graph = false: not capturable
+        if (!graph && fused) MC_TRY(job_run_loop_fused(j, h));
+        if (fused) {
             cost = h.cost;
             iternum = h.iternum;
             if (h.reason == LOOP_DONE) break;

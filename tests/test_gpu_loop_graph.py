@@ -1,8 +1,10 @@
-"""The Lloyd loop as one CUDA graph (device-side stop rule, while-conditional node) gives the
-results of the host loop: same iterations, objective, centers, assignments and costs, on
-the tensor-core, FP32 tiled and CSR sparse-dot paths, with weights, with an empty-cluster
-restart (the graph hands back to the host and resumes) and with eps = 0 (the loop runs
-until the objective rises and the last update is reverted)."""
+"""The three ways of running the Lloyd loop give the same results: the host loop (a round
+trip per decision), the fused loop (device-side stop rule, a round trip per iteration) and
+the CUDA graph (while-conditional node, a round trip per run): same iterations, objective,
+centers, assignments and costs, on the tensor-core, FP32 tiled and CSR sparse-dot paths,
+with weights, with an empty-cluster restart (the device loops hand back to the host and
+resume) and with eps = 0 (the loop runs until the objective rises and the last update is
+reverted)."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -17,7 +19,7 @@ def mc():
         pytest.skip("no GPU")
     import minicore_gb300
     yield minicore_gb300
-    minicore_gb300.loop_graph(True)
+    minicore_gb300.loop_mode(minicore_gb300.LOOP_AUTO)
 
 
 def _mixture(n, d, k, seed, nonneg=False):
@@ -42,13 +44,18 @@ def _counts(n, d, density, seed):
 
 
 def _both(mc, X, centers, **kw):
-    mc.loop_graph(False)
+    """Host loop result, and the fused and graph results checked equal to it."""
+    mc.loop_mode(mc.LOOP_HOST)
     a = mc.hcluster(X, centers, **kw)
-    mc.loop_graph(True)
-    l0 = mc.kernel_launches()
-    b = mc.hcluster(X, centers, **kw)
-    assert mc.kernel_launches() > l0
-    return a, b
+    out = []
+    for mode in (mc.LOOP_FUSED, mc.LOOP_GRAPH):
+        mc.loop_mode(mode)
+        l0 = mc.kernel_launches()
+        out.append(mc.hcluster(X, centers, **kw))
+        assert mc.kernel_launches() > l0
+    mc.loop_mode(mc.LOOP_AUTO)
+    _same(a, out[0])
+    return a, out[1]
 
 
 def _same(a, b):
