@@ -582,6 +582,7 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
 constexpr int NSLOT = tc::PARTS * tc::NCAND;
 constexpr int FIN_ROWS = 128;
 constexpr int FIN_SG = 2;  // subgroups whose centers a CTA stages
+constexpr int FIN_COLS = 16;  // columns per cp.async stage (smaller stages: more CTAs per SM)
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src),
@@ -594,11 +595,11 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// 32 columns of one candidate: c - x for the staged columns, sequential fmaf
-__device__ __forceinline__ void fin_chunk32(const float *cr, const float (&xr)[32], float &a) {
+// FIN_COLS columns of one candidate: c - x for the staged columns, sequential fmaf
+__device__ __forceinline__ void fin_chunk32(const float *cr, const float (&xr)[FIN_COLS], float &a) {
     const float4 *c4 = reinterpret_cast<const float4 *>(cr);
 #pragma unroll
-    for (int k4 = 0; k4 < 8; ++k4) {
+    for (int k4 = 0; k4 < FIN_COLS / 4; ++k4) {
         const float4 c = c4[k4];
         float df = c.x - xr[4 * k4 + 0];
         a = fmaf(df, df, a);
@@ -663,7 +664,7 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
                                                            uint32_t *over_rows, unsigned long long *nover) {
     constexpr int R = FIN_ROWS;
     extern __shared__ __align__(16) float cs[];  // [FIN_SG][4 pairs][d][2] staged centers
-    __shared__ __align__(16) float xs4[2][R][36];  // two 32-column stages (rows 144 B apart)
+    __shared__ __align__(16) float xs4[2][R][FIN_COLS + 4];  // two column stages (rows padded by 16 B)
     __shared__ uint32_t rows_s[R];
     __shared__ uint32_t sg_first;
     const int t = threadIdx.x, lane = t & 31;
@@ -762,12 +763,12 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
     if (VEC4) {
         // d % 4 == 0: 32-column chunks (the last one may be narrower) double-buffered with
         // cp.async, so the next chunk's rows load while this one is evaluated
-        const uint64_t nchunk = (d + 31) / 32;
+        const uint64_t nchunk = (d + FIN_COLS - 1) / FIN_COLS;
         auto stage = [&](uint64_t ci, int buf) {
-            const uint64_t k0 = ci * 32;
-            const int kmax = int(umin64(32, d - k0));
-            for (int e = t; e < R * 8; e += R) {
-                const int r = e >> 3, q4 = e & 7;
+            const uint64_t k0 = ci * FIN_COLS;
+            const int kmax = int(umin64(FIN_COLS, d - k0));
+            for (int e = t; e < R * (FIN_COLS / 4); e += R) {
+                const int r = e / (FIN_COLS / 4), q4 = e % (FIN_COLS / 4);
                 const uint32_t rr = rows_s[r];
                 const bool ok = rr != 0xffffffffu && 4 * q4 < kmax;
                 const float *src = ok ? X + uint64_t(rr) * d + k0 + 4 * q4 : X;
@@ -785,13 +786,13 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
                 cp_async_wait<0>();
             }
             __syncthreads();
-            const uint64_t k0 = ci * 32;
-            const int kmax = int(umin64(32, d - k0));
-            if (kmax == 32) {
+            const uint64_t k0 = ci * FIN_COLS;
+            const int kmax = int(umin64(FIN_COLS, d - k0));
+            if (kmax == FIN_COLS) {
                 // the row's 32 staged columns in registers, reused by every candidate
-                float xr[32];
+                float xr[FIN_COLS];
 #pragma unroll
-                for (int c4 = 0; c4 < 8; ++c4) {
+                for (int c4 = 0; c4 < FIN_COLS / 4; ++c4) {
                     const float4 v = *reinterpret_cast<const float4 *>(&xs4[buf][t][4 * c4]);
                     xr[4 * c4 + 0] = v.x;
                     xr[4 * c4 + 1] = v.y;
@@ -807,7 +808,7 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
 #pragma unroll
                         for (int pq = 0; pq < 4; ++pq) a2[pq] = f2_pack(acc[2 * pq], acc[2 * pq + 1]);
 #pragma unroll
-                        for (int k2 = 0; k2 < 16; ++k2) {
+                        for (int k2 = 0; k2 < FIN_COLS / 2; ++k2) {
                             const unsigned long long x0 = f2_pack(xr[2 * k2], xr[2 * k2]);
                             const unsigned long long x1 = f2_pack(xr[2 * k2 + 1], xr[2 * k2 + 1]);
 #pragma unroll
@@ -844,11 +845,11 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
             __syncthreads();  // buffer buf is restaged two chunks later
         }
     } else {
-        for (uint64_t k0 = 0; k0 < d; k0 += 32) {
-            const int kmax = int(umin64(32, d - k0));
+        for (uint64_t k0 = 0; k0 < d; k0 += FIN_COLS) {
+            const int kmax = int(umin64(FIN_COLS, d - k0));
             __syncthreads();
-            for (int e = t; e < R * 32; e += R) {
-                const int r = e >> 5, kk = e & 31;
+            for (int e = t; e < R * FIN_COLS; e += R) {
+                const int r = e / FIN_COLS, kk = e % FIN_COLS;
                 const uint32_t rr = rows_s[r];
                 xs4[0][r][kk] = (rr != 0xffffffffu && kk < kmax) ? X[uint64_t(rr) * d + k0 + kk] : 0.f;
             }
