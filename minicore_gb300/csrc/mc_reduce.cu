@@ -304,27 +304,36 @@ __global__ void __launch_bounds__(256) k_sort_key_scan(uint32_t *tile_counts, ui
     if (t == 255) bucket_count[key] = acc;
 }
 
-// exclusive scan of bucket counts (single CTA, sequential per thread chunk + smem)
-__global__ void k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m) {
-    __shared__ uint64_t part[1024];
-    const int t = threadIdx.x;
+// exclusive scan of up to a few thousand counts (single CTA of 1024 threads): per-thread
+// sequential runs, then a parallel scan of the 1024 run totals (warp shuffles, 32 warp
+// totals); out[m] = total
+__global__ void __launch_bounds__(1024) k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m) {
+    __shared__ uint64_t wtot[32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const uint64_t per = (m + blockDim.x - 1) / blockDim.x;
     const uint64_t b = t * per, e = umin64(m, b + per);
     uint64_t s = 0;
     for (uint64_t i = b; i < e; ++i) s += in[i];
-    part[t] = s;
+    uint64_t inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wtot[w] = inc;
     __syncthreads();
-    if (t == 0) {
-        uint64_t acc = 0;
-        for (unsigned i = 0; i < blockDim.x; ++i) {
-            const uint64_t v = part[i];
-            part[i] = acc;
-            acc += v;
+    if (w == 0) {
+        uint64_t v = lane < int(blockDim.x >> 5) ? wtot[lane] : 0, vi = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, vi, o);
+            if (lane >= o) vi += y;
         }
-        out[m] = acc;
+        if (lane < int(blockDim.x >> 5)) wtot[lane] = vi - v;  // exclusive warp offsets
+        if (lane == 31) out[m] = vi;
     }
     __syncthreads();
-    uint64_t acc = part[t];
+    uint64_t acc = wtot[w] + inc - s;
     for (uint64_t i = b; i < e; ++i) {
         const uint64_t v = in[i];
         out[i] = acc;

@@ -504,19 +504,24 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
                                                     uint32_t cap, const uint4 *__restrict__ A, uint64_t row_u4,
                                                     uint4 *Xc, uint32_t *over_rows, unsigned long long *nover,
                                                     unsigned long long *nmulti) {
+    static_assert(tc::PARTS == 4, "one 16-byte load per row and array");
+    __shared__ uint32_t mrow[8][32], mslot[8][32];  // the warp's multi rows and their slots
     const uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const float INF = __int_as_float(0x7f800000);
     bool over = false, multi = false;
     float thr = 0.f;
     if (row < n) {
         float m1 = INF, m2 = INF;
         uint32_t gr = ST_OVER;
+        const float4 v1 = reinterpret_cast<const float4 *>(b1)[row], v2 = reinterpret_cast<const float4 *>(b2)[row];
+        const uint4 vj = reinterpret_cast<const uint4 *>(j1)[row];
+        const float c1s[4] = {v1.x, v1.y, v1.z, v1.w}, c2s[4] = {v2.x, v2.y, v2.z, v2.w};
+        const uint32_t js[4] = {vj.x, vj.y, vj.z, vj.w};
 #pragma unroll
         for (int p = 0; p < tc::PARTS; ++p) {
-            const float c1 = b1[row * tc::PARTS + p], c2 = b2[row * tc::PARTS + p];
-            if (c1 < m1) gr = j1[row * tc::PARTS + p];
-            top2_merge(m1, m2, c1, c2);
+            if (c1s[p] < m1) gr = js[p];
+            top2_merge(m1, m2, c1s[p], c2s[p]);
         }
         const float cmax = *cmaxp;
         const float xn = sqrtf(rownorm[row]);
@@ -547,13 +552,19 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
             over = true;  // compact buffer full: exact rescan
         }
     }
-    // operand copies of the warp's multi rows, one row at a time by the whole warp (coalesced)
-    for (unsigned m = mb; m; m &= m - 1) {
-        const int src = __ffs(m) - 1;
-        const uint64_t r = __shfl_sync(0xffffffffu, row, src);
-        const unsigned sl = __shfl_sync(0xffffffffu, slot, src);
-        if (sl < cap)
-            for (uint64_t q = lane; q < row_u4; q += 32) Xc[uint64_t(sl) * row_u4 + q] = A[r * row_u4 + q];
+    // operand copies of the warp's multi rows: the (row, 16-byte word) items spread over the
+    // lanes, so the copies of several rows are in flight at once
+    if (multi) {
+        const int r = __popc(mb & ((1u << lane) - 1u));
+        mrow[wib][r] = uint32_t(row);
+        mslot[wib][r] = slot;
+    }
+    __syncwarp();
+    const uint32_t ru4 = uint32_t(row_u4), items = uint32_t(__popc(mb)) * ru4;
+    for (uint32_t it = lane; it < items; it += 32) {
+        const uint32_t r = it / ru4, q = it - r * ru4;
+        const unsigned sl = mslot[wib][r];
+        if (sl < cap) Xc[uint64_t(sl) * row_u4 + q] = A[uint64_t(mrow[wib][r]) * row_u4 + q];
     }
     const unsigned ob = __ballot_sync(0xffffffffu, over);
     unsigned long long obase = 0;
