@@ -389,6 +389,43 @@ int job_launch_centroids(mc_job *j, const uint32_t *keys2, uint64_t extra, bool 
     return launch_centroids(ca, j->sort, st, presorted);
 }
 
+// L1 over dense rows: coordinate-wise medians (set_centroids_l1, clustering/centroid.h:203,
+// 435-504) instead of means
+bool l1_medians(const mc_job *j) { return j->msr == L1 && j->M.kind == MC_DENSE_F32; }
+
+// set_centroids_l1: empty clusters are reseeded one at a time (D^2 draw over the current
+// costs, then rows closer to the new center in plain L1 move to it), until none is empty;
+// then the medians.  The reference reports no restart from this policy.
+int job_set_centroids_l1(mc_job *j) {
+    const uint64_t n = j->M.n, d = j->M.d;
+    const uint32_t k = j->k;
+    cudaStream_t st = j->st;
+    std::vector<uint64_t> cnt(k);
+    for (;;) {
+        MC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), j->sort.bucket_count.p, k * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                    st));
+        MC_TRY(sync(st));
+        std::vector<uint32_t> empty;
+        for (uint32_t c = 0; c < k; ++c)
+            if (cnt[c] == 0) empty.push_back(c);
+        if (empty.empty()) break;
+        for (uint32_t id : empty) {
+            const double u = uniform_at(j->seed, j->restart_counter++);
+            DetInput in{DET_F64, j->costs.p, nullptr, nullptr, n};
+            MC_TRY(launch_det_draw(in, j->det_tmp.p, nullptr, u, 0, nullptr, j->idxbuf.p + k, st));
+            float *dst = j->Cw.p + uint64_t(id) * d;
+            k_copy_row_dense<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(j->M.X, d, j->idxbuf.p + k, dst),
+                note_launch();
+            MC_CUDA_TRY(cudaGetLastError());
+            MC_TRY(launch_l1_reseed_update(j->M.X, n, d, dst, id, j->asn.p, j->costs.p, st));
+        }
+        MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+    }
+    Phase ph("centroid_update", st);
+    MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), st));
+    return launch_l1_medians(j->M.X, d, k, j->sort, j->w.p, j->Cw.p, st);
+}
+
 int job_set_centroids(mc_job *j, int *restarted) {
     const uint64_t n = j->M.n, d = j->M.d;
     const uint32_t k = j->k;
@@ -401,6 +438,7 @@ int job_set_centroids(mc_job *j, int *restarted) {
         Phase ph("centroid_update", st);
         MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
     }
+    if (l1_medians(j)) return job_set_centroids_l1(j);
     std::vector<uint64_t> cnt(k);
     MC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), j->sort.bucket_count.p, k * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
     MC_TRY(sync(st));
@@ -567,12 +605,22 @@ int job_loop_pre(mc_job *j, LoopState *ls, cudaGraphConditionalHandle h, int gra
     return MC_OK;
 }
 
+// the centers of the current (sorted) assignment into Cw, no cluster empty
+int job_update_centers(mc_job *j) {
+    if (l1_medians(j)) {
+        Phase ph("centroid_update", j->st);
+        MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), j->st));
+        return launch_l1_medians(j->M.X, j->M.d, j->k, j->sort, j->w.p, j->Cw.p, j->st);
+    }
+    return job_launch_centroids(j, nullptr, 0, /*presorted=*/true);
+}
+
 int job_loop_body(mc_job *j, LoopState *ls, cudaGraphConditionalHandle h, int graph) {
     cudaStream_t st = j->st;
     const uint64_t n = j->M.n, d = j->M.d;
     const uint32_t k = j->k;
     const bool tc = j->M.kind == MC_DENSE_F32 && j->msr == SQRL2 && j->precision != MC_FP32;
-    MC_TRY(job_launch_centroids(j, nullptr, 0, /*presorted=*/true));
+    MC_TRY(job_update_centers(j));
     MC_TRY(job_assign_with(j, j->Cw.p, j->psum, false, nullptr, /*graph_mode=*/true));
     {
         DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
@@ -602,7 +650,7 @@ int job_build_loop_graph(mc_job *j) {
     // space and the tensor-core path's FP32 rescan transform.  The centroid launch writes Cw,
     // which then takes the committed centers back (a restart on the host starts from Cw = C).
     MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
-    MC_TRY(job_launch_centroids(j, nullptr, 0, /*presorted=*/true));
+    MC_TRY(job_update_centers(j));
     MC_CUDA_TRY(cudaMemcpyAsync(j->Cw.p, j->C.p, uint64_t(k) * d * sizeof(float), cudaMemcpyDeviceToDevice, st));
     if (tc) MC_TRY(j->tc.CT0.alloc(uint64_t(tiled_center_pad(k, false, SQRL2)) * d, st));
     CaptureGuard guard{st};

@@ -793,4 +793,145 @@ int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, flo
     return MC_OK;
 }
 
+// ------------------------------------------------------------------------------------
+// L1 medians: one CTA (8 warps) per (cluster, 32 columns).  Unweighted: a 4-pass radix select
+// (one byte of the order-preserving key per pass, histograms in shared memory) for the ranks
+// (m - 1) / 2 and m / 2 at once.  Weighted: the largest weight of the cluster, then per
+// column the smallest value among the rows that carry it.
+// ------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t f2ord(float v) {
+    const uint32_t u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+__global__ void __launch_bounds__(256) k_l1_median_dense(const float *__restrict__ X, uint64_t d,
+                                                         const uint32_t *__restrict__ perm,
+                                                         const uint64_t *__restrict__ bstart,
+                                                         const uint64_t *__restrict__ bcount, float *centers) {
+    extern __shared__ uint32_t hist[];  // [2][32][256]
+    __shared__ uint32_t prefix[2][32];
+    __shared__ uint64_t rank[2][32];
+    const uint32_t c = blockIdx.x;
+    const uint64_t c0 = uint64_t(blockIdx.y) * 32;
+    const uint64_t m = bcount[c], b = bstart[c];
+    if (m == 0) return;  // whole block
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint64_t col = c0 + lane;
+    if (t < 64) {
+        const int s = t >> 5;
+        prefix[s][lane] = 0;
+        rank[s][lane] = s == 0 ? (m - 1) / 2 : m / 2;
+    }
+    for (int pass = 3; pass >= 0; --pass) {
+        for (int e = t; e < 2 * 32 * 256; e += 256) hist[e] = 0;
+        __syncthreads();
+        if (col < d) {
+            const uint32_t p0 = prefix[0][lane], p1 = prefix[1][lane];
+            for (uint64_t r = warp; r < m; r += 8) {
+                const uint32_t key = f2ord(X[uint64_t(perm[b + r]) * d + col]);
+                const uint32_t bin = (key >> (8 * pass)) & 255u;
+                const bool top = pass == 3;
+                if (top || (key >> (8 * (pass + 1))) == p0) atomicAdd(&hist[(0 * 32 + lane) * 256 + bin], 1u);
+                if (top || (key >> (8 * (pass + 1))) == p1) atomicAdd(&hist[(1 * 32 + lane) * 256 + bin], 1u);
+            }
+        }
+        __syncthreads();
+        if (t < 64) {
+            const int s = t >> 5;
+            const uint32_t *h = hist + (s * 32 + lane) * 256;
+            uint64_t rk = rank[s][lane], cum = 0;
+            uint32_t bin = 255;
+            for (uint32_t q = 0; q < 256; ++q) {
+                if (cum + h[q] > rk) { bin = q; break; }
+                cum += h[q];
+            }
+            rank[s][lane] = rk - cum;
+            prefix[s][lane] = (prefix[s][lane] << 8) | bin;
+        }
+        __syncthreads();
+    }
+    if (t < 32 && col < d) {
+        const float lo = ord2f(prefix[0][lane]), hi = ord2f(prefix[1][lane]);
+        centers[uint64_t(c) * d + col] = (m & 1) ? hi : 0.5f * (lo + hi);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_l1_median_weighted(const float *__restrict__ X, uint64_t d,
+                                                            const uint32_t *__restrict__ perm,
+                                                            const uint64_t *__restrict__ bstart,
+                                                            const uint64_t *__restrict__ bcount,
+                                                            const double *__restrict__ w, float *centers) {
+    __shared__ double wmax[8];
+    __shared__ uint32_t best[8][32];
+    const uint32_t c = blockIdx.x;
+    const uint64_t c0 = uint64_t(blockIdx.y) * 32;
+    const uint64_t m = bcount[c], b = bstart[c];
+    if (m == 0) return;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    double mx = -1.7976931348623157e308;
+    for (uint64_t r = t; r < m; r += 256) mx = fmax(mx, w[perm[b + r]]);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) wmax[warp] = mx;
+    __syncthreads();
+    mx = wmax[0];
+    for (int q = 1; q < 8; ++q) mx = fmax(mx, wmax[q]);
+    const uint64_t col = c0 + lane;
+    uint32_t bk = 0xffffffffu;
+    if (col < d)
+        for (uint64_t r = warp; r < m; r += 8) {
+            const uint32_t row = perm[b + r];
+            if (w[row] == mx) bk = min(bk, f2ord(X[uint64_t(row) * d + col]));
+        }
+    best[warp][lane] = bk;
+    __syncthreads();
+    if (t < 32 && col < d) {
+        uint32_t v = best[0][lane];
+        for (int q = 1; q < 8; ++q) v = min(v, best[q][lane]);
+        centers[uint64_t(c) * d + col] = ord2f(v);
+    }
+}
+
+int launch_l1_medians(const float *X, uint64_t d, uint32_t k, const SortWork &w, const double *weights,
+                      float *centers, cudaStream_t st) {
+    if (k == 0 || d == 0) return MC_OK;
+    const dim3 g(k, unsigned((d + 31) / 32));
+    if (weights) {
+        k_l1_median_weighted<<<g, 256, 0, st>>>(X, d, w.perm.p, w.bucket_start.p, w.bucket_count.p, weights,
+                                               centers), note_launch();
+    } else {
+        const int smem = 2 * 32 * 256 * int(sizeof(uint32_t));
+        MC_CUDA_TRY(cudaFuncSetAttribute(k_l1_median_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        k_l1_median_dense<<<g, 256, smem, st>>>(X, d, w.perm.p, w.bucket_start.p, w.bucket_count.p, centers),
+            note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+__global__ void k_l1_reseed_update(const float *__restrict__ X, uint64_t n, uint64_t d,
+                                   const float *__restrict__ center, uint32_t id, uint32_t *asn, double *costs) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x)) {
+        const float *x = X + i * d;
+        float a = 0.f;
+        for (uint64_t j = 0; j < d; ++j) a = a + fabsf(center[j] - x[j]);
+        if (double(a) < costs[i]) {
+            asn[i] = id;
+            costs[i] = double(a);
+        }
+    }
+}
+
+int launch_l1_reseed_update(const float *X, uint64_t n, uint64_t d, const float *center, uint32_t id,
+                            uint32_t *asn, double *costs, cudaStream_t st) {
+    if (n == 0) return MC_OK;
+    k_l1_reseed_update<<<unsigned(umin64((n + 255) / 256, 4096)), 256, 0, st>>>(X, n, d, center, id, asn, costs),
+        note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 }  // namespace mc

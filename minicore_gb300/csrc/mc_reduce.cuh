@@ -37,6 +37,18 @@ int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, 
                        cudaStream_t st);
 // presorted: w already holds the counting sort of a.keys (no second membership)
 int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool presorted = false);
+
+// L1 centers over dense rows (set_centroids_l1, clustering/centroid.h:435-504), from the
+// current counting sort of the rows by cluster: per cluster the coordinate-wise median
+// (unweighted: odd -> middle, even -> 0.5f * (the two middles)); with weights, per column
+// the value of the row with the largest weight (smallest such value on ties), which is what
+// the reference's weighted_median returns.  Clusters without rows keep their center.
+int launch_l1_medians(const float *X, uint64_t d, uint32_t k, const SortWork &w, const double *weights,
+                      float *centers, cudaStream_t st);
+// the L1 restart's pass after reseeding center `id` at `center`: rows whose plain L1
+// distance (sequential float sum of |c - x|) is below their cost move to it
+int launch_l1_reseed_update(const float *X, uint64_t n, uint64_t d, const float *center, uint32_t id,
+                            uint32_t *asn, double *costs, cudaStream_t st);
 int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st);
 int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, float *cnorm, cudaStream_t st);
 

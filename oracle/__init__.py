@@ -62,6 +62,7 @@ def lib():
             "orc_assign": (I, [P, P, U32, I, D, P, P]),
             "orc_kmeanspp": (I, [P, U32, I, D, P, P, P, P, P]),
             "orc_hcluster": (I, [P, P, U32, I, D, P, D, U64, U64, P, P, P, P, P, P]),
+            "orc_l1_centers": (I, [P, P, U32, P, P]),
             "orc_scluster": (I, [P, P, U32, I, D, P, D, U64, D, P, P, P, P, P, P]),
             "orc_minibatch": (I, [P, P, U32, I, D, P, U64, U64, U64, U64, I, U64, P, P, P, P, P, P]),
             "orc_sensitivity": (I, [U64, U64, U64, P, I, P, P, I, D, P]),
@@ -168,6 +169,18 @@ def kmeanspp(X, k, msr, prior, uniforms_, weights=None):
     if rc:
         raise ValueError("orc_kmeanspp failed")
     return ids, asn, costs
+
+
+def l1_centers(X, asn, k, weights=None):
+    """The L1 center rule (set_centroids_l1's medians) for a given assignment, dense rows."""
+    M = Matrix(X)
+    a = np.ascontiguousarray(asn, dtype=np.uint32)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    out = np.empty((k, M.d), np.float32)
+    rc = lib().orc_l1_centers(M.ref(), _p(a), k, _p(w), _p(out))
+    if rc:
+        raise ValueError(f"orc_l1_centers failed ({rc})")
+    return out
 
 
 def hcluster(X, centers, msr, prior, weights=None, eps=1e-10, maxiter=100, seed=1):

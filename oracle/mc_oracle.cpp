@@ -588,6 +588,93 @@ int orc_kmeanspp(const orc_matrix *mm, uint32_t k, int msr, double prior, const 
 
 // perform_hard_clustering (solve.h:98-175) from explicit dense centers.
 // Returns 0 on success, 2 if a NaN center appeared.
+// L1 centers: set_centroids_l1 (clustering/centroid.h:435-504), dense rows.  Empty clusters
+// are reseeded one at a time (D^2 draw over the current costs, U(seed, r) with the restart
+// counter), each followed by a pass that moves every row whose plain L1 distance to the new
+// center (sequential float sum of |c - x|) is below its cost; repeated while clusters are
+// empty.  Then every cluster takes the coordinate-wise median of its rows
+// (optim/kmedian.h: l1_unweighted_median: sorted column, odd -> middle, even -> 0.5f * (the
+// two middles)); with weights, weighted_median (kmedian.h:249-290) keeps wsum at 0, so it
+// returns, per column, the value of the row with the largest weight (the smallest such value
+// on ties).  Returns 0: the reference reports no restart from this policy.
+inline float l1_plain(const float *c, const float *x, uint64_t d) {
+    float a = 0.f;
+    for (uint64_t j = 0; j < d; ++j) a = a + std::fabs(c[j] - x[j]);
+    return a;
+}
+
+int set_centroids_l1_dense(const Mat &m, std::vector<uint32_t> &asn, std::vector<double> &costs, CenterSet &C,
+                           const double *w, uint64_t seed, uint64_t &restart_counter) {
+    const uint64_t n = m.n, k = C.k, d = m.d;
+    std::vector<std::vector<uint64_t>> assigned(k);
+    auto rebuild = [&](std::vector<uint32_t> &empty) {
+        for (auto &a : assigned) a.clear();
+        for (uint64_t i = 0; i < n; ++i) assigned[asn[i]].push_back(i);
+        empty.clear();
+        for (uint32_t c = 0; c < k; ++c) if (assigned[c].empty()) empty.push_back(c);
+    };
+    std::vector<uint32_t> empty;
+    rebuild(empty);
+    while (!empty.empty()) {
+        for (uint32_t id : empty) {
+            const double u = uniform_at(seed, restart_counter++);
+            uint64_t r = det_draw([&](uint64_t i) { return costs[i]; }, n, u);
+            if (r >= n) r = 0;
+            C.set_row(id, dense_row(m, r), false);
+            const float *cr = &C.dense[uint64_t(id) * d];
+            for (uint64_t i = 0; i < n; ++i) {
+                const double c = l1_plain(cr, m.vals + i * d, d);
+                if (c < costs[i]) { asn[i] = id; costs[i] = c; }
+            }
+        }
+        rebuild(empty);
+    }
+    std::vector<float> col, out(d);
+    for (uint32_t c = 0; c < k; ++c) {
+        const auto &rows = assigned[c];  // ascending
+        const uint64_t mc = rows.size();
+        if (w) {
+            double maxw = -std::numeric_limits<double>::max();
+            for (uint64_t r : rows) maxw = std::max(maxw, w[r]);
+            for (uint64_t j = 0; j < d; ++j) {
+                float best = std::numeric_limits<float>::infinity();
+                for (uint64_t r : rows)
+                    if (w[r] == maxw) best = std::min(best, m.vals[r * d + j]);
+                out[j] = best;
+            }
+        } else {
+            col.resize(mc);
+            for (uint64_t j = 0; j < d; ++j) {
+                for (uint64_t q = 0; q < mc; ++q) col[q] = m.vals[rows[q] * d + j];
+                std::sort(col.begin(), col.end());
+                const uint64_t h = mc / 2;
+                out[j] = (mc & 1) ? col[h] : 0.5f * (col[h - 1] + col[h]);
+            }
+        }
+        C.set_row(c, out, false);
+    }
+    return 0;
+}
+
+// the L1 center rule alone (no empty cluster allowed): centers_out[k][d]
+int orc_l1_centers(const orc_matrix *mm, const uint32_t *asn_in, uint32_t k, const double *w, float *centers_out) {
+    const Mat m = to_mat(mm);
+    if (m.kind != 0) return 1;
+    std::vector<uint32_t> asn(asn_in, asn_in + m.n);
+    std::vector<double> costs(m.n, 0.0);
+    CenterSet C;
+    std::vector<float> zero(uint64_t(k) * m.d, 0.f);
+    C.set_from_dense(zero.data(), k, m.d, false);
+    uint64_t rc = 0;
+    for (uint64_t i = 0; i < m.n; ++i) if (asn[i] >= k) return 2;
+    std::vector<uint64_t> cnt(k, 0);
+    for (uint64_t i = 0; i < m.n; ++i) ++cnt[asn[i]];
+    for (uint32_t c = 0; c < k; ++c) if (!cnt[c]) return 3;
+    set_centroids_l1_dense(m, asn, costs, C, w, 0, rc);
+    std::copy(C.dense.begin(), C.dense.end(), centers_out);
+    return 0;
+}
+
 int orc_hcluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int msr, double prior, const double *w,
                  double eps, uint64_t maxiter, uint64_t seed, float *centers_out, uint32_t *asn_out, double *costs_out,
                  double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
@@ -612,7 +699,11 @@ int orc_hcluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
     } else {
         cpy = centers;
         for (;;) {
-            int res = set_centroids_full_mean(m, msr, prior, asn, costs, cpy, w, rs, seed, restart_counter);
+            // L1 over dense rows takes coordinate-wise medians (centroid.h:203, 487-504); the
+            // CSR L1 median (util/csc.h:829-893) is not restated: CSR L1 keeps the weighted mean
+            int res = (msr == L1 && !sparse)
+                          ? set_centroids_l1_dense(m, asn, costs, cpy, w, seed, restart_counter)
+                          : set_centroids_full_mean(m, msr, prior, asn, costs, cpy, w, rs, seed, restart_counter);
             if (res < 0) { rc = 2; break; }
             assign_all(m, cpy, msr, prior, psum, rs, asn.data(), costs.data());
             const float newcost = compute_cost(costs.data(), w, n);

@@ -264,6 +264,39 @@ def test_hcluster_csr_mkl(mc, orc):
     np.testing.assert_allclose(Cg, ores["centers"], rtol=1e-4, atol=1e-6)
 
 
+@pytest.mark.parametrize("weighted", [False, True])
+def test_hcluster_l1_medians(mc, orc, weighted):
+    """L1 centers are coordinate-wise medians (set_centroids_l1): odd and even cluster sizes,
+    weights (the reference's weighted_median keeps the largest-weight row's value), bit-exact
+    against the oracle."""
+    X = _mixture(3001, 11, 5, seed=77, nonneg=False)
+    C0 = X[[0, 500, 1000, 1500, 2000, 2500]].copy()
+    w = np.random.default_rng(3).integers(1, 6, 3001).astype(np.float64) if weighted else None
+    res = mc.hcluster(X, C0, msr=0, prior=0.0, weights=w, eps=0.0, maxiter=6, seed=9)
+    ores = orc.hcluster(X, C0, 0, 0.0, eps=0.0, maxiter=6, seed=9, weights=w)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(res["centers"], ores["centers"])
+    assert res["finalcost"] == ores["finalcost"]
+    # one update from a known assignment: the GPU centers are the oracle's median rule
+    a0, _ = orc.assign(X, C0, 0, 0.0)
+    one = mc.hcluster(X, C0, msr=0, prior=0.0, weights=w, eps=0.0, maxiter=0, seed=9)
+    if one["numiter"] == 1:
+        assert np.array_equal(one["centers"], orc.l1_centers(X, a0, 6, weights=w))
+
+
+def test_hcluster_l1_empty_cluster_reseed(mc, orc):
+    """An L1 center far from every row: the L1 restart reseeds it by a D^2 draw and moves
+    the rows that are closer in plain L1, then takes medians (oracle bit-exact)."""
+    X = _mixture(2000, 6, 4, seed=5)
+    C0 = np.concatenate([X[:4], np.full((1, 6), 1e4, np.float32)])
+    res = mc.hcluster(X, C0, msr=0, prior=0.0, eps=0.0, maxiter=4, seed=21)
+    ores = orc.hcluster(X, C0, 0, 0.0, eps=0.0, maxiter=4, seed=21)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(res["centers"], ores["centers"])
+
+
 def test_hcluster_empty_cluster_restart(mc, orc):
     # a far-away duplicate center attracts no rows -> D^2 restart path
     X = _mixture(3000, 8, 4, seed=31)

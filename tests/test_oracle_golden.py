@@ -234,3 +234,28 @@ def test_alias_table_is_exact_distribution(orc):
     np.add.at(mass_alias, at, (1 - pt) / n)
     q = p.astype(np.float64) / p.astype(np.float64).sum()
     assert np.allclose(mass + mass_alias, q, atol=1e-12)
+
+
+def test_oracle_l1_centers_are_medians(orc):
+    """set_centroids_l1 restated: after an update every L1 center is the coordinate-wise
+    median of its rows (even sizes: 0.5f * (the two middles)); with weights, the value of the
+    largest-weight row (the reference's weighted_median never accumulates its total)."""
+    rng = np.random.default_rng(12)
+    X = (rng.normal(size=(400, 5)) * 3).astype(np.float32)
+    C0 = X[[0, 100, 200, 300]].copy()
+    r = orc.hcluster(X, C0, 0, 0.0, eps=0.0, maxiter=0, seed=1)
+    # maxiter 0: one update; rows reassigned to the medians of the first assignment
+    a0, _ = orc.assign(X, C0, 0, 0.0)
+    for c in range(4):
+        col = np.sort(X[a0 == c], axis=0)
+        m = col.shape[0]
+        med = col[m // 2] if m % 2 else np.float32(0.5) * (col[m // 2 - 1] + col[m // 2])
+        assert np.array_equal(r["centers"][c], med.astype(np.float32))
+    w = rng.integers(1, 4, 400).astype(np.float64)
+    cw = orc.l1_centers(X, a0, 4, weights=w)
+    cu = orc.l1_centers(X, a0, 4)
+    for c in range(4):
+        sel = a0 == c
+        top = sel & (w == w[sel].max())
+        assert np.array_equal(cw[c], X[top].min(axis=0))
+        assert np.array_equal(cu[c], r["centers"][c])
