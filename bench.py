@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving", "coreset", "pcmp", "minibatch",
-                                                         "soft", "small"],
+                                                         "soft", "small", "coreset_mb"],
                     help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
                          "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass; serving: "
                          "the Poisson job stream through the continuous-batching server; coreset: the "
@@ -364,6 +364,26 @@ def next_rows_bench(args):
                              "algorithmic": f"2*n*n*d = {flops:.4g} FLOP per call"},
                 "cpu_baseline": {"value": cpu_pairs_s, "unit": "pairs/s", "cores": os.cpu_count() or 1,
                                  "kind": "port", "sample": f"oracle distances of {S} x {S} rows"}}
+    elif args.workload == "coreset_mb":
+        n, d, k = 1_000_000, 64, 100
+        X = mixture(n, d, 200)
+        ids = torch.randperm(n, generator=g, device="cuda")[:k]
+        C0 = X[ids].contiguous()
+        M = mc._MatrixArg(X)
+        cout = torch.empty((k, d), dtype=torch.float32, device="cuda")
+        asn = torch.empty(n, dtype=torch.int32, device="cuda")
+        cst = torch.empty(n, dtype=torch.float64, device="cuda")
+        ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+
+        def run():
+            _lib.check(lib.mc_hcluster_coreset(ctx.handle, M.ref, mc._p(C0), k, 2, 0.0, None, 4096, 20, 5, 1, 5,
+                                               mc._PREC["bf16"], mc._p(cout), mc._p(asn), mc._p(cst),
+                                               ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
+        ms, launches = timed(run, 1)
+        line = {"metric": "coreset-minibatch EM runs/s, 1M x 64, k=100, coreset 4096, maxiter 20, 5 check-ins",
+                "value": 1000.0 / ms, "unit": "runs/s", "ms_per_step": ms,
+                "rounds": int(it.value), "objective": {"initcost": ic.value, "finalcost": fc.value},
+                "roofline": None, "cpu_baseline": None}
     elif args.workload == "minibatch":
         n, d, k = 1_000_000, 64, 100
         X = mixture(n, d, 200)
@@ -788,7 +808,7 @@ def main():
         return serving_main(args)
     if args.workload == "coreset":
         return coreset_bench(args)
-    if args.workload in ("pcmp", "minibatch", "soft"):
+    if args.workload in ("pcmp", "minibatch", "soft", "coreset_mb"):
         return next_rows_bench(args)
     if args.workload == "small":
         return small_bench(args)

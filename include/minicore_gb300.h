@@ -188,6 +188,21 @@ int mc_hcluster_minibatch(mc_context *ctx, const mc_matrix *X, const float *cent
                           int with_replacement, uint64_t seed, int precision, float *centers_out,
                           uint32_t *asn, double *costs, double *initcost, double *finalcost,
                           uint64_t *numiter);
+/* hcluster with mbsize > 0 and cs=True: minibatch-by-coreset EM (hmb_coreset_clustering,
+ * clustering/solve.h:593-789; python/pycluster.h:36-38).  Rounds of an exhaustive
+ * assignment, restarts of centers holding <= reseed_count rows (D^2 draws U(seed, r); rows
+ * move to a restarted center when strictly cheaper), the FP64 objective (best centers kept),
+ * then ceil(maxiter / ncheckins) times: a coreset of min(mbsize, n) distinct rows (LBK
+ * sensitivities, VX for L1; alpha 1 for L1, 2 for SQRL2, 4 otherwise; sample seed
+ * floor(U(seed, r) * 2^53)) clustered by perform_hard_clustering (eps 1e-3, 1 update, 3 in
+ * the first two rounds; weights = coreset weights x row weights; restart seed = coreset
+ * size).  One uniform counter r serves the restarts and the sample seeds in order.
+ * centers_out: the best centers; asn, costs: the last exhaustive assignment. */
+int mc_hcluster_coreset(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k,
+                        int msr, double prior, const double *weights, uint64_t mbsize,
+                        uint64_t maxiter, uint64_t ncheckins, uint64_t reseed_count, uint64_t seed,
+                        int precision, float *centers_out, uint32_t *asn, double *costs,
+                        double *initcost, double *finalcost, uint64_t *numiter);
 /* Soft clustering (perform_soft_clustering, clustering/solve.h:287-374, with the soft
  * weighted means of centroid.h:795-866) over dense rows: per iteration asn = row softmax of
  * -temp * costs (NaN rows: equal shares over the minimal costs), objective sum_i w_i

@@ -309,9 +309,8 @@ def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxit
     """Hard Lloyd/Bregman EM from explicit centers (clustering/solve.h:98-175); with
     mbsize >= 0, minibatch EM (solve.h:386-582) with maxiter iterations, a check-in every
     ceil(maxiter / ncheckins), restarts of centers holding <= reseed_count rows, and
-    with_rep sampling."""
-    if cs:
-        raise NotImplementedError("coreset minibatch clustering (cs=True) is outside the implemented path")
+    with_rep sampling; with cs=True as well, minibatch-by-coreset EM (hmb_coreset_clustering,
+    solve.h:593-789)."""
     ctx = ctx or default_context()
     M = _MatrixArg(matrix)
     C = _centers_array(M, centers)
@@ -326,11 +325,17 @@ def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxit
     if mbsize is not None and int(mbsize) >= 0:
         # perform_hard_minibatch_clustering (python/pycluster.h:31-40): ncheckins < 0 -> 10
         nchk = int(ncheckins) if ncheckins is not None and int(ncheckins) > 0 else 10
-        check(_lib.load().mc_hcluster_minibatch(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w),
-                                                max(int(mbsize), 1), int(maxiter), nchk, int(reseed_count),
-                                                int(bool(with_rep)), _seed(seed), _PREC[precision], _p(cout),
-                                                _p(asn), _p(costs), ctypes.byref(ic), ctypes.byref(fc),
-                                                ctypes.byref(it)))
+        if cs:  # pycluster.h:36-38
+            check(_lib.load().mc_hcluster_coreset(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w),
+                                                  max(int(mbsize), 1), int(maxiter), nchk, int(reseed_count),
+                                                  _seed(seed), _PREC[precision], _p(cout), _p(asn), _p(costs),
+                                                  ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
+        else:
+            check(_lib.load().mc_hcluster_minibatch(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w),
+                                                    max(int(mbsize), 1), int(maxiter), nchk, int(reseed_count),
+                                                    int(bool(with_rep)), _seed(seed), _PREC[precision], _p(cout),
+                                                    _p(asn), _p(costs), ctypes.byref(ic), ctypes.byref(fc),
+                                                    ctypes.byref(it)))
     else:
         check(_lib.load().mc_hcluster(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(eps),
                                       int(maxiter), _seed(seed), _PREC[precision], _p(cout), _p(asn), _p(costs),

@@ -69,6 +69,8 @@ SIGNATURES = {
     "mc_job_minibatch": (I, [P, U64, U64, U64, U64, I, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(U64)]),
     "mc_hcluster_minibatch": (I, [P, P, P, U32, I, D, P, U64, U64, U64, U64, I, U64, I, P, P, P, ctypes.POINTER(D),
                                   ctypes.POINTER(D), ctypes.POINTER(U64)]),
+    "mc_hcluster_coreset": (I, [P, P, P, U32, I, D, P, U64, U64, U64, U64, U64, I, P, P, P, ctypes.POINTER(D),
+                                ctypes.POINTER(D), ctypes.POINTER(U64)]),
     "mc_scluster": (I, [P, P, P, U32, I, D, P, D, U64, D, P, P, P, ctypes.POINTER(D), ctypes.POINTER(D),
                         ctypes.POINTER(U64)]),
     "mc_job_recheck_count": (I, [P, ctypes.POINTER(U64)]),

@@ -1478,6 +1478,191 @@ int mc_hcluster_minibatch(mc_context *ctx, const mc_matrix *X, const float *cent
     return mc_job_read(j, centers_out, asn, costs);
 }
 
+}  // extern "C"
+
+namespace {
+
+__global__ void k_f64_to_f32(const double *__restrict__ a, uint64_t n, float *b) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x))
+        b[i] = float(a[i]);
+}
+
+// after an assignment against the restarted centers only (asn holds their positions in
+// `found`): a row moves to the best restarted center when that is strictly cheaper than
+// its previous cost, else it keeps (save_asn, save_cost)
+__global__ void k_merge_restarted(uint64_t n, const uint32_t *__restrict__ found, const uint32_t *__restrict__ save_asn,
+                                  const double *__restrict__ save_cost, uint32_t *asn, double *costs) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x)) {
+        if (costs[i] < save_cost[i]) {
+            asn[i] = found[asn[i]];
+        } else {
+            asn[i] = save_asn[i];
+            costs[i] = save_cost[i];
+        }
+    }
+}
+
+// minibatch-by-coreset EM (hmb_coreset_clustering, clustering/solve.h:593-789), the
+// reference's cs=True path (python/pycluster.h:36-39): rounds of an exhaustive assignment,
+// restarts of the centers holding <= reseed_after rows (D^2 draws U(seed, r) over the costs,
+// weighted by the row weights; each row then moves to a restarted center that is strictly
+// cheaper), the objective (best centers kept), then calc_cost_freq times: a coreset of
+// min(mbsize, n) distinct rows (LBK sensitivities, VX for L1, alpha = msr2alpha; sample seed
+// floor(U(seed, r) 2^53)) and perform_hard_clustering on it (eps 1e-3, 1 update, 3 in the
+// first two rounds; weights = coreset weights times row weights; restart seed = coreset
+// size).  The uniform counter r is shared by the restarts and the sample seeds, in order.
+int job_coreset_minibatch(mc_job *j, uint64_t mbsize, uint64_t maxiter, uint64_t calc_cost_freq,
+                          uint64_t reseed_after, float *best_centers, double *initcost_out, double *finalcost_out,
+                          uint64_t *numiter_out) {
+    cudaStream_t st = j->st;
+    const uint64_t n = j->M.n, d = j->M.d;
+    const uint32_t k = j->k;
+    const size_t cbytes = uint64_t(k) * d * sizeof(float);
+    if (calc_cost_freq == 0) calc_cost_freq = 1;
+    const uint64_t rounds = (calc_cost_freq - 1 + maxiter) / calc_cost_freq;
+    const uint64_t m = std::min<uint64_t>(std::max<uint64_t>(mbsize, 1), n);
+    const double alpha = j->msr == L1 ? 1.0 : j->msr == SQRL2 ? 2.0 : 4.0;  // msr2alpha, distance.h:310-318
+    const int method = j->msr == L1 ? MC_VX : MC_LBK;
+    uint64_t counter = 0;
+    DBuf<float> wf;
+    if (j->w.p) {
+        MC_TRY(wf.alloc(n, st));
+        k_f64_to_f32<<<unsigned(umin64((n + 255) / 256, 4096)), 256, 0, st>>>(j->w.p, n, wf.p), note_launch();
+    }
+    MC_CUDA_TRY(cudaMemcpyAsync(best_centers, j->C.p, cbytes, cudaMemcpyDefault, st));
+    DBuf<uint32_t> save_asn, found_dev, rows_dev;
+    DBuf<double> save_cost;
+    DBuf<float> Cs;
+    MC_TRY(j->idxbuf.alloc(uint64_t(k) + 2, st));
+    double initcost = 0.0, bestcost = 0.0, cost = 0.0;
+    uint64_t iternum = 0;
+    std::vector<float> cw_f(m);
+    std::vector<uint64_t> cidx(m);
+    std::vector<uint32_t> rows32(m);
+    std::vector<double> cw(m), wrow(j->w.p ? n : 0);
+    if (j->w.p) {
+        MC_CUDA_TRY(cudaMemcpyAsync(wrow.data(), j->w.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MC_TRY(sync(st));
+    }
+    for (;;) {
+        MC_TRY(job_assign_with(j, j->C.p, j->psum, false));
+        MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
+        std::vector<uint64_t> cnt(k);
+        MC_CUDA_TRY(cudaMemcpyAsync(cnt.data(), j->sort.bucket_count.p, k * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+        MC_TRY(sync(st));
+        std::vector<uint32_t> found;
+        for (uint32_t c = 0; c < k; ++c)
+            if (cnt[c] <= reseed_after) found.push_back(c);
+        if (!found.empty()) {
+            for (uint32_t fidx : found) {
+                const double u = uniform_at(j->seed, counter++);
+                DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
+                MC_TRY(launch_det_draw(in, j->det_tmp.p, nullptr, u, 0, nullptr, j->idxbuf.p + k, st));
+                float *dst = j->C.p + uint64_t(fidx) * d;
+                if (j->M.kind == MC_DENSE_F32) {
+                    k_copy_row_dense<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(j->M.X, d, j->idxbuf.p + k,
+                                                                                              dst), note_launch();
+                } else {
+                    k_copy_row_csr_zero<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(d, dst), note_launch();
+                    k_copy_row_csr<<<64, 256, 0, st>>>(j->M.vals, j->M.idx, j->M.indptr, j->idxbuf.p + k, dst),
+                        note_launch();
+                }
+                MC_CUDA_TRY(cudaGetLastError());
+            }
+            // the rows against the restarted centers only, then the strict-improvement merge
+            const uint32_t nf = uint32_t(found.size());
+            MC_TRY(save_asn.alloc(n, st));
+            MC_TRY(save_cost.alloc(n, st));
+            MC_TRY(found_dev.alloc(nf, st));
+            MC_TRY(Cs.alloc(uint64_t(nf) * d, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(save_asn.p, j->asn.p, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(save_cost.p, j->costs.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(found_dev.p, found.data(), nf * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            for (uint32_t q = 0; q < nf; ++q)
+                MC_CUDA_TRY(cudaMemcpyAsync(Cs.p + uint64_t(q) * d, j->C.p + uint64_t(found[q]) * d, d * sizeof(float),
+                                            cudaMemcpyDeviceToDevice, st));
+            const uint32_t k_all = j->k;
+            j->k = nf;
+            const int rc = job_assign_with(j, Cs.p, j->psum, false);
+            j->k = k_all;
+            MC_TRY(rc);
+            k_merge_restarted<<<unsigned(umin64((n + 255) / 256, 4096)), 256, 0, st>>>(n, found_dev.p, save_asn.p,
+                                                                                     save_cost.p, j->asn.p, j->costs.p),
+                note_launch();
+            MC_CUDA_TRY(cudaGetLastError());
+            MC_TRY(sync(st));  // host vectors above go out of scope
+        }
+        {
+            DetInput in{j->w.p ? DET_F64_W : DET_F64, j->costs.p, nullptr, j->w.p, n};
+            MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(&cost, j->scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MC_TRY(sync(st));
+        }
+        if (iternum == 0) {
+            initcost = bestcost = cost;
+        } else if (cost < bestcost) {
+            bestcost = cost;
+            MC_CUDA_TRY(cudaMemcpyAsync(best_centers, j->C.p, cbytes, cudaMemcpyDefault, st));
+        }
+        if (++iternum > rounds) break;
+        mc_sampler *smp = nullptr;
+        MC_TRY(mc_sampler_create(j->ctx, n, k, k, j->costs.p, 1, j->asn.p, j->w.p ? wf.p : nullptr, method, alpha, &smp));
+        std::unique_ptr<mc_sampler, int (*)(mc_sampler *)> sguard(smp, mc_sampler_destroy);
+        for (uint64_t jj = 0; jj < calc_cost_freq; ++jj) {
+            const uint64_t sseed = uint64_t(uniform_at(j->seed, counter++) * 9007199254740992.0);
+            MC_TRY(mc_sampler_sample(smp, m, sseed, 1, cw_f.data(), cidx.data()));
+            for (uint64_t q = 0; q < m; ++q) {
+                rows32[q] = uint32_t(cidx[q]);
+                cw[q] = j->w.p ? double(cw_f[q]) * wrow[cidx[q]] : double(cw_f[q]);
+            }
+            MC_TRY(rows_dev.alloc(m, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(rows_dev.p, rows32.data(), m * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            SubRows sub;
+            mc_matrix subm;
+            MC_TRY(gather_job_rows(j, rows_dev.p, m, sub, &subm));
+            DBuf<uint32_t> sasn;
+            DBuf<double> scost, sw;
+            MC_TRY(sasn.alloc(m, st));
+            MC_TRY(scost.alloc(m, st));
+            MC_TRY(sw.alloc(m, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(sw.p, cw.data(), m * sizeof(double), cudaMemcpyHostToDevice, st));
+            double ic = 0, fc = 0;
+            uint64_t it = 0;
+            const uint64_t subiter = 1 + (iternum < 2 ? 2 : 0);
+            MC_TRY(mc_hcluster(j->ctx, &subm, j->C.p, k, j->msr, j->prior, sw.p, 1e-3, subiter, m, j->precision,
+                               j->C.p, sasn.p, scost.p, &ic, &fc, &it));
+            MC_TRY(sync(st));
+        }
+    }
+    if (initcost_out) *initcost_out = initcost;
+    if (finalcost_out) *finalcost_out = bestcost;
+    if (numiter_out) *numiter_out = iternum;
+    return sync(st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int mc_hcluster_coreset(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
+                        double prior, const double *weights, uint64_t mbsize, uint64_t maxiter, uint64_t ncheckins,
+                        uint64_t reseed_count, uint64_t seed, int precision, float *centers_out, uint32_t *asn,
+                        double *costs, double *initcost, double *finalcost, uint64_t *numiter) {
+    if (!centers_out) return fail(MC_EINVAL, "centers_out is null");
+    mc_job *j = nullptr;
+    MC_TRY(mc_job_create(ctx, X, centers_in, k, msr, prior, weights, precision, seed, &j));
+    std::unique_ptr<mc_job, int (*)(mc_job *)> guard(j, mc_job_destroy);
+    if (ncheckins == 0) ncheckins = 10;
+    const uint64_t freq = (maxiter + ncheckins - 1) / ncheckins;  // pycluster.h:34-38
+    DBuf<float> best;
+    MC_TRY(best.alloc(uint64_t(k) * j->M.d, j->st));
+    MC_TRY(job_coreset_minibatch(j, mbsize, maxiter, freq, reseed_count, best.p, initcost, finalcost, numiter));
+    // the best centers; assignments and costs of the last exhaustive pass
+    MC_TRY(mc_job_read(j, nullptr, asn, costs));
+    MC_CUDA_TRY(cudaMemcpyAsync(centers_out, best.p, uint64_t(k) * j->M.d * sizeof(float), cudaMemcpyDefault, j->st));
+    return sync(j->st);
+}
+
 int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr, double prior,
                 const double *weights, double temp, uint64_t maxiter, double eps, float *centers_out,
                 float *costs_out, float *asn_out, double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {

@@ -266,3 +266,62 @@ def coreset_sample(probs, prob_tab, alias_tab, m, seed, unique=False, weights=No
     lib().orc_coreset_sample(probs.size, _p(probs), _p(prob_tab), _p(alias_tab), _p(w), method, b, m, seed,
                              int(bool(unique)), _p(wo), _p(io))
     return wo, io
+
+
+def coreset_minibatch(X, centers, msr, prior, mbsize, maxiter, ncheckins=10, reseed_count=5, seed=0, weights=None):
+    """Minibatch-by-coreset EM (hmb_coreset_clustering, clustering/solve.h:593-789, as called
+    by python/pycluster.h:36-38), restated over the oracle's pieces with the canonical
+    randomness of the device path: restarts draw U(seed, r) over costs (x row weights), the
+    coreset sample seed is floor(U(seed, r) * 2^53), one counter r for both, in order; the
+    coreset sub-clustering is perform_hard_clustering with eps 1e-3, 1 update (3 in the first
+    two rounds) and restart seed = coreset size.  Returns (best centers, asn, costs of the last
+    exhaustive assignment, initcost, bestcost, rounds)."""
+    import scipy.sparse as sp
+    C = np.array(centers, dtype=np.float32, copy=True)
+    k = C.shape[0]
+    n = X.shape[0]
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    freq = (maxiter + ncheckins - 1) // ncheckins
+    rounds = (freq - 1 + maxiter) // freq
+    m = min(max(int(mbsize), 1), n)
+    alpha = 1.0 if msr == 0 else 2.0 if msr == 2 else 4.0
+    method = 3 if msr == 0 else 4            # VX for L1, else LBK
+    counter = 0
+    best = C.copy()
+    initcost = bestcost = 0.0
+    it = 0
+    dense_row = (lambda i: np.asarray(X[i].toarray(), np.float32).ravel()) if sp.issparse(X) else (lambda i: X[i])
+    while True:
+        asn, costs = assign(X, C, msr, prior)
+        cnt = np.bincount(asn, minlength=k)
+        found = [c for c in range(k) if cnt[c] <= reseed_count]
+        if found:
+            for f in found:
+                u = float(uniforms(seed, 1, offset=counter)[0])
+                counter += 1
+                r = det_draw(costs * w if w is not None else costs, u)
+                C[f] = dense_row(r if r < n else 0)
+            a2, c2 = assign(X, C[found], msr, prior)
+            better = c2 < costs
+            asn = np.where(better, np.asarray(found, np.uint32)[a2], asn).astype(np.uint32)
+            costs = np.where(better, c2, costs)
+        cost = det_sum(costs * w if w is not None else costs)
+        if it == 0:
+            initcost = bestcost = cost
+        elif cost < bestcost:
+            bestcost = cost
+            best = C.copy()
+        it += 1
+        if it > rounds:
+            break
+        probs = sensitivity(costs, asn, k, method, weights=w, k=k, alpha_est=alpha)
+        pt, at = alias_build(probs)
+        for _ in range(freq):
+            sseed = int(float(uniforms(seed, 1, offset=counter)[0]) * 9007199254740992.0)
+            counter += 1
+            wo, io = coreset_sample(probs, pt, at, m, sseed, unique=True, weights=w, method=method, b=k)
+            io = io.astype(np.int64)
+            cw = wo.astype(np.float64) * (w[io] if w is not None else 1.0)
+            sub = hcluster(X[io], C, msr, prior, weights=cw, eps=1e-3, maxiter=1 + (2 if it < 2 else 0), seed=m)
+            C = np.asarray(sub["centers"], np.float32)
+    return best, asn, costs, initcost, bestcost, it

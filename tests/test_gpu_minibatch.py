@@ -76,3 +76,26 @@ def test_minibatch_csr_mkl(mc, orc):
     np.testing.assert_allclose(g["finalcost"], o["finalcost"], rtol=1e-4)
     np.testing.assert_allclose(g["initcost"], o["initcost"], rtol=1e-4)
     assert (g["asn"] == o["asn"]).mean() > 0.99
+
+
+@pytest.mark.parametrize("msr,weighted,precision", [(2, False, "fp32"), (2, True, "fp32"), (2, False, "bf16"),
+                                                    (0, False, "fp32")])
+def test_coreset_minibatch_matches_oracle(mc, orc, msr, weighted, precision):
+    """cs=True: minibatch-by-coreset EM (hmb_coreset_clustering) against the oracle's
+    restatement: best centers, last assignment and costs, objectives and rounds bit for bit
+    (SQRL2 in FP32 and BF16, which give the FP32 assignment; L1 with VX sensitivities and
+    median centers)."""
+    rng = np.random.default_rng(40 + msr)
+    mu = rng.uniform(-8, 8, (6, 8))
+    X = (mu[rng.integers(0, 6, 3000)] + rng.normal(size=(3000, 8))).astype(np.float32)
+    C0 = X[rng.choice(3000, 6, replace=False)].copy()
+    w = rng.integers(1, 4, 3000).astype(np.float64) if weighted else None
+    res = mc.hcluster(X, C0, msr=msr, weights=w, mbsize=500, maxiter=20, ncheckins=5, reseed_count=1, seed=13,
+                      cs=True, precision=precision)
+    best, asn, costs, ic, fc, it = orc.coreset_minibatch(X, C0, msr, 0.0, 500, 20, ncheckins=5, reseed_count=1,
+                                                         seed=13, weights=w)
+    assert res["numiter"] == it
+    assert res["initcost"] == ic and res["finalcost"] == fc
+    assert np.array_equal(res["asn"], asn)
+    assert np.array_equal(res["costs"], costs.astype(np.float32))
+    assert np.array_equal(res["centers"], best)
