@@ -349,11 +349,10 @@ def scluster(matrix, centers, msr=2, prior=0., temp=1., maxiter=1000, mbsize=-1,
              weights=None, ctx: Context | None = None):
     """Soft clustering from explicit centers (perform_soft_clustering, clustering/solve.h:287-374;
     python/pycluster_softdense.cpp:66-90).  Returns initcost, finalcost, numiter, centers, and
-    the last (rows x k) float32 cost and soft-assignment matrices.  Dense rows; eps 1e-8."""
+    the last (rows x k) float32 cost and soft-assignment matrices; eps 1e-8.  CSR rows give CSR
+    centers, as hcluster does."""
     if mbsize is not None and int(mbsize) > 0:
         raise NotImplementedError("Not yet completed: minibatch soft clustering")
-    if _is_sparse(matrix):
-        raise NotImplementedError("soft clustering of CSR rows is outside the implemented path")
     ctx = ctx or default_context()
     M = _MatrixArg(matrix)
     C = _centers_array(M, centers)
@@ -368,8 +367,9 @@ def scluster(matrix, centers, msr=2, prior=0., temp=1., maxiter=1000, mbsize=-1,
     check(_lib.load().mc_scluster(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(temp),
                                   int(maxiter), 1e-8, _p(cout), _p(costs), _p(asn), ctypes.byref(ic),
                                   ctypes.byref(fc), ctypes.byref(it)))
-    return {"initcost": ic.value, "finalcost": fc.value, "numiter": it.value, "centers": cout, "costs": costs,
-            "asn": asn}
+    centers_out = cout if M.kind == _lib.MC_DENSE_F32 else _centers_to_csr(cout)
+    return {"initcost": ic.value, "finalcost": fc.value, "numiter": it.value, "centers": centers_out,
+            "costs": costs, "asn": asn}
 
 
 def cluster_from_centers(*args, **kwargs):

@@ -966,6 +966,41 @@ __global__ void k_soft_center_chunks(const float *__restrict__ X, uint64_t n, ui
 }
 
 // adds the partials of chunks [0, nq) of one batch to the running FP64 sums, in chunk order
+// CSR rows: the same chunk partials, accumulated over each row's nonzeros (a zero term adds
+// exactly nothing to the compensated sums).  The running (s, e) of every column live in
+// sb / eb ([chunk][k][d], zeroed by the caller); rows are taken in order, one after the
+// other, and the columns of one row are distinct, so each column's sum keeps the row order.
+__global__ void __launch_bounds__(256) k_soft_center_chunks_csr(const float *__restrict__ vals,
+                                                                const uint32_t *__restrict__ idx,
+                                                                const uint64_t *__restrict__ indptr, uint64_t n,
+                                                                uint64_t d, const float *__restrict__ asn, uint32_t k,
+                                                                const double *__restrict__ w, float *sb, float *eb,
+                                                                double *num, double *den) {
+    const uint64_t q = blockIdx.x;
+    const uint32_t c = blockIdx.y;
+    const uint64_t r0 = q * kSoftChunk, r1 = umin64(n, r0 + kSoftChunk);
+    float *s = sb + (q * k + c) * d, *e = eb + (q * k + c) * d;
+    float sw = 0.f, ew = 0.f;
+    for (uint64_t r = r0; r < r1; ++r) {
+        const float coef = w ? asn[r * k + c] * float(w[r]) : asn[r * k + c];
+        for (uint64_t p = indptr[r] + threadIdx.x; p < indptr[r + 1]; p += blockDim.x) {
+            const uint32_t j = idx[p];
+            const float t = coef * vals[p];
+            float tt = __fadd_rn(s[j], t), bp = __fsub_rn(tt, s[j]);
+            e[j] = __fadd_rn(e[j], __fadd_rn(__fsub_rn(s[j], __fsub_rn(tt, bp)), __fsub_rn(t, bp)));
+            s[j] = tt;
+        }
+        if (threadIdx.x == 0) {
+            const float tt = __fadd_rn(sw, coef), bp = __fsub_rn(tt, sw);
+            ew = __fadd_rn(ew, __fadd_rn(__fsub_rn(sw, __fsub_rn(tt, bp)), __fsub_rn(coef, bp)));
+            sw = tt;
+        }
+        __syncthreads();
+    }
+    for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) num[(q * k + c) * d + j] = double(s[j]) + double(e[j]);
+    if (threadIdx.x == 0) den[q * k + c] = double(sw) + double(ew);
+}
+
 __global__ void k_soft_center_accumulate(const double *__restrict__ num, const double *__restrict__ den, uint64_t nq,
                                          uint32_t k, uint64_t d, double *acc_num, double *acc_den) {
     const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
@@ -1667,7 +1702,6 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
                 const double *weights, double temp, uint64_t maxiter, double eps, float *centers_out,
                 float *costs_out, float *asn_out, double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
     if (!ctx || !X || !centers_in) return fail(MC_EINVAL, "null argument");
-    if (X->kind != MC_DENSE_F32) return fail(MC_EUNSUPPORTED, "soft clustering covers dense rows");
     if (msr == L1) return fail(MC_EUNSUPPORTED, "soft L1 centers are medians (outside the implemented path)");
     mc_job *j = nullptr;
     MC_TRY(mc_job_create(ctx, X, centers_in, k, msr, prior, weights, MC_FP32, 1, &j));
@@ -1678,8 +1712,15 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
     DBuf<float> costs, asn;
     // chunk partials in batches of at most 256 MB, added in chunk order
     const uint64_t nq_all = (n + kSoftChunk - 1) / kSoftChunk;
-    const uint64_t batch = std::max<uint64_t>(1, std::min<uint64_t>(nq_all, (256ull << 20) / (8ull * k * d + 8ull * k)));
+    const bool csr = j->M.kind == MC_CSR_F32;
+    const uint64_t per_chunk = (csr ? 16ull : 8ull) * k * d + 8ull * k;
+    const uint64_t batch = std::max<uint64_t>(1, std::min<uint64_t>(nq_all, (256ull << 20) / per_chunk));
     DBuf<double> rowval, snum, sden, acc_num, acc_den;
+    DBuf<float> sbuf, ebuf;
+    if (csr) {
+        MC_TRY(sbuf.alloc(batch * k * d, st));
+        MC_TRY(ebuf.alloc(batch * k * d, st));
+    }
     MC_TRY(snum.alloc(batch * k * d, st));
     MC_TRY(sden.alloc(batch * k, st));
     MC_TRY(acc_num.alloc(uint64_t(k) * d, st));
@@ -1706,9 +1747,17 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
         MC_CUDA_TRY(cudaMemsetAsync(acc_den.p, 0, uint64_t(k) * sizeof(double), st));
         for (uint64_t q0 = 0; q0 < nq_all; q0 += batch) {
             const uint64_t nq = umin64(batch, nq_all - q0), r0 = q0 * kSoftChunk;
-            k_soft_center_chunks<<<dim3(unsigned(nq), k), unsigned(umin64(d, 128)), 0, st>>>(
-                j->M.X + r0 * d, umin64(n - r0, nq * kSoftChunk), d, asn.p + r0 * k, k, j->w.p ? j->w.p + r0 : nullptr,
-                snum.p, sden.p), note_launch();
+            if (csr) {
+                MC_CUDA_TRY(cudaMemsetAsync(sbuf.p, 0, nq * k * d * sizeof(float), st));
+                MC_CUDA_TRY(cudaMemsetAsync(ebuf.p, 0, nq * k * d * sizeof(float), st));
+                k_soft_center_chunks_csr<<<dim3(unsigned(nq), k), 256, 0, st>>>(
+                    j->M.vals, j->M.idx, j->M.indptr + r0, umin64(n - r0, nq * kSoftChunk), d, asn.p + r0 * k, k,
+                    j->w.p ? j->w.p + r0 : nullptr, sbuf.p, ebuf.p, snum.p, sden.p), note_launch();
+            } else {
+                k_soft_center_chunks<<<dim3(unsigned(nq), k), unsigned(umin64(d, 128)), 0, st>>>(
+                    j->M.X + r0 * d, umin64(n - r0, nq * kSoftChunk), d, asn.p + r0 * k, k,
+                    j->w.p ? j->w.p + r0 : nullptr, snum.p, sden.p), note_launch();
+            }
             k_soft_center_accumulate<<<dim3(unsigned((d + 127) / 128), k), 128, 0, st>>>(snum.p, sden.p, nq, k, d,
                                                                                          acc_num.p, acc_den.p),
                 note_launch();

@@ -847,13 +847,22 @@ int orc_scluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
                  double temp, uint64_t maxiter, double eps, float *centers_out, float *costs_out, float *asn_out,
                  double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
     const Mat m = to_mat(mm);
-    if (m.kind != 0) return 3;
     const uint64_t n = m.n, d = m.d;
+    const bool sparse = m.kind == 1;
+    // CSR rows: the soft means read a dense copy (a zero adds exactly nothing to the
+    // compensated sums, so this is the per-nonzero accumulation of the device path)
+    std::vector<float> dense_all;
+    if (sparse) {
+        dense_all.assign(n * d, 0.f);
+        for (uint64_t i = 0; i < n; ++i)
+            for (uint64_t p = m.indptr[i]; p < m.indptr[i + 1]; ++p) dense_all[i * d + m.idx[p]] = m.vals[p];
+    }
+    const float *xv = sparse ? dense_all.data() : m.vals;
     std::vector<double> rs(n);
     for (uint64_t i = 0; i < n; ++i) rs[i] = row_sum(m, i);
     const double psum = double(float(prior * double(d)));
     CenterSet acc, cpy;
-    acc.set_from_dense(centers_in, k, d, false);
+    acc.set_from_dense(centers_in, k, d, sparse);
     cpy = acc;
     std::vector<float> costs(n * k), asn(n * k);
     auto fill_costs = [&]() {
@@ -900,7 +909,7 @@ int orc_scluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
                     float s = 0.f, e = 0.f, sw = 0.f, ew = 0.f;
                     for (uint64_t r = r0; r < r1; ++r) {
                         const float coef = w ? asn[r * k + c] * float(w[r]) : asn[r * k + c];
-                        two_sum_add(s, e, coef * m.vals[r * d + j]);
+                        two_sum_add(s, e, coef * xv[r * d + j]);
                         two_sum_add(sw, ew, coef);
                     }
                     num = num + (double(s) + double(e));
@@ -909,7 +918,7 @@ int orc_scluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
                 nc[uint64_t(c) * d + j] = float(num * (1.0 / den));
             }
         }
-        cpy.set_from_dense(nc.data(), k, d, false);
+        cpy.set_from_dense(nc.data(), k, d, sparse);
         fill_costs();
         if (initcost < 0) initcost = cost;
         if (oldcost >= cost) acc = cpy;

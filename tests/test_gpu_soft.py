@@ -45,3 +45,26 @@ def test_cluster_soft_entry(mc):
     X = _mixture(1500, 8, 4, seed=1)
     r = mc.cluster(X, msr=2, k=4, temp=0.5, maxiter=5, seed=3)
     assert r["asn"].shape == (1500, 4) and r["centers"].shape == (4, 8)
+
+
+@pytest.mark.parametrize("msr,prior,temp", [(2, 0.0, 0.5), (5, 1.0, 2.0), (6, 1.0, 1.0)])
+@pytest.mark.parametrize("weighted", [False, True])
+def test_scluster_csr_matches_oracle(mc, orc, msr, prior, temp, weighted):
+    """CSR rows: the soft means accumulate over each row's nonzeros (a zero adds nothing to
+    the compensated sums); distances come from the CSR assignment kernels."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(30 + msr)
+    X = sp.random(1800, 120, density=0.08, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.integers(1, 6, s).astype(np.float32)).astype(np.float32)
+    X.sort_indices()
+    C0 = np.asarray(X[rng.choice(1800, 5, replace=False)].toarray(), np.float32) + 0.1
+    w = rng.uniform(0.5, 2.0, 1800) if weighted else None
+    g = mc.scluster(X, C0, msr=msr, prior=prior, temp=temp, maxiter=5, weights=w)
+    o = orc.scluster(X, C0, msr, prior, weights=w, temp=temp, maxiter=5)
+    assert g["numiter"] == o["numiter"]
+    np.testing.assert_allclose(g["initcost"], o["initcost"], rtol=1e-4)
+    np.testing.assert_allclose(g["finalcost"], o["finalcost"], rtol=1e-4)
+    (data, idx, indptr), shape = g["centers"]
+    Cg = sp.csr_matrix((data, idx.astype(np.int64), indptr.astype(np.int64)), shape=tuple(shape)).toarray()
+    np.testing.assert_allclose(Cg, o["centers"], rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(g["asn"], o["asn"], atol=1e-4)
