@@ -114,6 +114,15 @@ int mc_uniforms(uint64_t seed, uint64_t offset, uint64_t m, double *out);
 int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior,
                 const double *weights, const double *uniforms,
                 uint32_t *center_ids, uint32_t *asn, double *costs);
+/* Greedy k-means++ (n_local_trials > 1, kmeans.h:79-177; python/pydense.cpp:34-77): the
+ * first center is the best of n_local_trials uniform picks; each later round draws
+ * n_local_trials candidates from the distances without replacement and keeps the one with
+ * the lowest objective.  Candidate 0 extends the current distances; later candidates extend
+ * the distances of the first center alone, as the reference does (kmeans.h:140-144).
+ * Uniforms U(seed, r), one counter r.  n_local_trials = 1 is mc_kmeanspp with U(seed, i). */
+int mc_kmeanspp_greedy(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior,
+                       const double *weights, uint32_t n_local_trials, uint64_t seed,
+                       uint32_t *center_ids, uint32_t *asn, double *costs);
 
 /* One hard assignment pass (solve.h:234-285): asn[i] = argmin_j msr(row i, center j),
  * lowest index on ties; costs[i] = that distance.  centers: dense k x ncols float32. */

@@ -253,11 +253,11 @@ def kmeanspp(matrix, k, *, msr=2, prior=0., seed=0, ntimes=1, lspp=0, expskips=0
              weights=None, ctx: Context | None = None):
     """D^2 seeding (include/minicore/optim/kmeans.h:49-215).  Returns (center ids,
     assignments, costs); costs are float32 for dense input and float64 for CSR input, as in
-    the reference bindings.  ``lspp`` rounds and ``n_local_trials > 1`` are not implemented."""
+    the reference bindings.  ``n_local_trials > 1``: greedy seeding (mc_kmeanspp_greedy, uniforms
+    U(seed + run, r)).  ``lspp`` rounds are not implemented."""
     if lspp:
         raise NotImplementedError("localsearch++ rounds are outside the implemented hot path")
-    if n_local_trials and int(n_local_trials) > 1:
-        raise NotImplementedError("n_local_trials > 1 is outside the implemented hot path")
+    trials = max(int(n_local_trials or 1), 1)
     ctx = ctx or default_context()
     M = _MatrixArg(matrix)
     k = int(k)
@@ -274,12 +274,16 @@ def kmeanspp(matrix, k, *, msr=2, prior=0., seed=0, ntimes=1, lspp=0, expskips=0
     runs = max(int(ntimes), 1) if M.kind == _lib.MC_DENSE_F32 else 1
     best = None
     for t in range(runs):
-        u = uniforms(seed, k, offset=t * k)
         ids = np.empty(kk, dtype=np.uint32)
         asn = np.empty(M.n, dtype=np.uint32)
         costs = np.empty(M.n, dtype=np.float64)
-        check(_lib.load().mc_kmeanspp(ctx.handle, M.ref, k, _msr(msr), float(prior), _p(w), _p(u), _p(ids),
-                                      _p(asn), _p(costs)))
+        if trials > 1:
+            check(_lib.load().mc_kmeanspp_greedy(ctx.handle, M.ref, k, _msr(msr), float(prior), _p(w), trials,
+                                                 (seed + t) & 0xFFFFFFFFFFFFFFFF, _p(ids), _p(asn), _p(costs)))
+        else:
+            u = uniforms(seed, k, offset=t * k)
+            check(_lib.load().mc_kmeanspp(ctx.handle, M.ref, k, _msr(msr), float(prior), _p(w), _p(u), _p(ids),
+                                          _p(asn), _p(costs)))
         c = costs.sum()
         if best is None or c < best[0]:
             best = (c, ids, asn, costs)

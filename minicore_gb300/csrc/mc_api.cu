@@ -1906,11 +1906,14 @@ int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
     return mc_job_read(j, centers_out, asn, costs);
 }
 
-int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
-                const double *uniforms, uint32_t *center_ids, uint32_t *asn, double *costs) {
+}  // extern "C"
+
+static int kmeanspp_impl(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
+                         const double *uniforms, uint32_t local_trials, uint64_t seed, uint32_t *center_ids,
+                         uint32_t *asn, double *costs) {
     if (!ctx) return fail(MC_EINVAL, "ctx is null");
     if (!measure_supported(msr)) return fail(MC_EUNSUPPORTED, "measure not implemented on this path");
-    if (!uniforms) return fail(MC_EINVAL, "uniforms is null");
+    if (!uniforms && local_trials <= 1) return fail(MC_EINVAL, "uniforms is null");
     MC_CUDA_TRY(cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     DevMatrix M;
@@ -1932,7 +1935,7 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     MC_TRY(asnb.alloc(n, st));
     MC_TRY(ids.alloc(k, st));
     MC_TRY(newc.alloc(1, st));
-    MC_CUDA_TRY(cudaMemcpyAsync(u.p, uniforms, k * sizeof(double), cudaMemcpyDefault, st));
+    if (local_trials <= 1) MC_CUDA_TRY(cudaMemcpyAsync(u.p, uniforms, k * sizeof(double), cudaMemcpyDefault, st));
     if (weights) {
         MC_TRY(w.alloc(n, st));
         MC_CUDA_TRY(cudaMemcpyAsync(w.p, weights, n * sizeof(double), cudaMemcpyDefault, st));
@@ -1969,12 +1972,31 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
     a.asn = asnb.p;
     a.center_ids = ids.p;
     a.newc = newc.p;
-    MC_TRY(run_kmeanspp(a, u.p, tmp.p, ctx->sms, st));
+    if (local_trials > 1) MC_TRY(run_kmeanspp_greedy(a, local_trials, seed, tmp.p, ctx->sms, st));
+    else MC_TRY(run_kmeanspp(a, u.p, tmp.p, ctx->sms, st));
     MC_TRY(copy_out(center_ids, ids.p, k, st));
     MC_TRY(copy_out(asn, asnb.p, n, st));
     MC_TRY(copy_out(costs, dist.p, n, st));
     MC_CUDA_TRY(cudaStreamSynchronize(st));
     return MC_OK;
+}
+
+extern "C" {
+
+int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
+                const double *uniforms, uint32_t *center_ids, uint32_t *asn, double *costs) {
+    return kmeanspp_impl(ctx, X, k, msr, prior, weights, uniforms, 1, 0, center_ids, asn, costs);
+}
+
+int mc_kmeanspp_greedy(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
+                       uint32_t n_local_trials, uint64_t seed, uint32_t *center_ids, uint32_t *asn, double *costs) {
+    if (n_local_trials == 0) return fail(MC_EINVAL, "n_local_trials must be positive");
+    if (n_local_trials == 1) {
+        std::vector<double> u(k);
+        for (uint32_t i = 0; i < k; ++i) u[i] = uniform_at(seed, i);
+        return kmeanspp_impl(ctx, X, k, msr, prior, weights, u.data(), 1, 0, center_ids, asn, costs);
+    }
+    return kmeanspp_impl(ctx, X, k, msr, prior, weights, nullptr, n_local_trials, seed, center_ids, asn, costs);
 }
 
 // ------------------------------------------------------------------------------------

@@ -610,6 +610,157 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     return MC_OK;
 }
 
+// ------------------------------------------------------------------------------------
+// Greedy k-means++ (n_local_trials = L > 1, kmeans.h:79-177): the first center is the best
+// (lowest objective) of L uniform picks; every later round draws L candidates from the
+// distances without replacement (a drawn row's weight is zeroed for the next draw), adds
+// each to the distances and keeps the one with the lowest objective.  As in the reference,
+// candidate 0 updates the current distances in place while candidates 1.. start from the
+// distances and assignments of the first center alone (`odists`, `oasn`, set once before the
+// rounds, kmeans.h:106-107, 140-144).  Uniforms U(seed, r), one counter; draws and sums in
+// the canonical FP64 order.
+// ------------------------------------------------------------------------------------
+__global__ void k_kmpp_exclude(double *dist, const uint64_t *cand, double *saved) {
+    const uint64_t c = *cand;
+    *saved = dist[c];
+    dist[c] = 0.0;
+}
+__global__ void k_kmpp_restore(double *dist, const uint64_t *cand, const double *saved, uint32_t L) {
+    for (int s = int(L) - 1; s >= 0; --s) dist[cand[s]] = saved[s];
+}
+// the candidate's own row: distance 0 (the plain update of the reference visits it too)
+__global__ void k_kmpp_self(double *dist, uint32_t *asn, const uint64_t *cand, uint32_t round) {
+    const uint64_t c = *cand;
+    if (dist[c] > 0.0) {
+        dist[c] = 0.0;
+        asn[c] = round;
+    }
+}
+__global__ void k_kmpp_set_center(double *dist, uint32_t *asn, uint32_t *center_ids, const uint64_t *cand,
+                                  uint32_t round) {
+    const uint64_t c = *cand;
+    center_ids[round] = uint32_t(c);
+    asn[c] = round;
+    dist[c] = 0.0;
+}
+__global__ void k_kmpp_pick(const double *u, uint64_t n, uint64_t *out) {
+    uint64_t fc = uint64_t(*u * double(n));
+    if (fc >= n) fc = n - 1;
+    *out = fc;
+}
+
+// the distances of b (dist, asn) with candidate *b.newc added in round `round` (first: the
+// distances to the first center)
+static int kmpp_add_candidate(const KmppArgs &b, int first, uint32_t round, int sms, cudaStream_t st) {
+    const unsigned tb = 256, tg = unsigned(umin64((b.d + tb - 1) / tb, 1024));
+    const bool fused = kmpp_csr_fused_ok(b);
+    if (b.csr && !fused) {
+        k_kmpp_take<<<tg, tb, 0, st>>>(b, round), note_launch();
+        k_kmpp_scatter<<<64, 256, 0, st>>>(b), note_launch();
+    }
+    MC_TRY(update(b, first, round, sms, st));
+    if (!first) k_kmpp_self<<<1, 1, 0, st>>>(b.dist, b.asn, b.newc, round), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+static int kmpp_cost(const KmppArgs &b, double *chunk_tmp, double *scal, cudaStream_t st, double *out) {
+    DetInput in{b.w ? DET_F64_W : DET_F64, b.dist, nullptr, b.w, b.n};
+    MC_TRY(launch_det_sum(in, chunk_tmp, scal, st));
+    MC_CUDA_TRY(cudaMemcpyAsync(out, scal, sizeof(double), cudaMemcpyDeviceToHost, st));
+    MC_CUDA_TRY(cudaStreamSynchronize(st));
+    return MC_OK;
+}
+
+int run_kmeanspp_greedy(const KmppArgs &a0, uint32_t L, uint64_t seed, double *chunk_tmp, int sms, cudaStream_t st) {
+    KmppArgs a = a0;
+    const uint64_t n = a.n;
+    uint64_t counter = 0;
+    DBuf<double> ubuf, T, O, S, sav, scal;
+    DBuf<uint32_t> OA, SA;
+    DBuf<uint64_t> cand;
+    MC_TRY(ubuf.alloc(1, st));
+    MC_TRY(T.alloc(n, st));
+    MC_TRY(O.alloc(n, st));
+    MC_TRY(S.alloc(n, st));
+    MC_TRY(sav.alloc(L, st));
+    MC_TRY(scal.alloc(1, st));
+    MC_TRY(OA.alloc(n, st));
+    MC_TRY(SA.alloc(n, st));
+    MC_TRY(cand.alloc(L, st));
+    auto put_u = [&](double u) -> int {
+        MC_CUDA_TRY(cudaMemcpyAsync(ubuf.p, &u, sizeof(double), cudaMemcpyHostToDevice, st));
+        MC_CUDA_TRY(cudaStreamSynchronize(st));  // u lives on this frame
+        return MC_OK;
+    };
+    // first center: the best of L uniform picks
+    MC_CUDA_TRY(cudaMemsetAsync(a.asn, 0, n * sizeof(uint32_t), st));
+    MC_TRY(put_u(uniform_at(seed, counter++)));
+    k_kmpp_pick<<<1, 1, 0, st>>>(ubuf.p, n, a.newc), note_launch();
+    MC_TRY(kmpp_add_candidate(a, 1, 0, sms, st));
+    double fcost = 0.0;
+    MC_TRY(kmpp_cost(a, chunk_tmp, scal.p, st, &fcost));
+    uint64_t fc = 0;
+    MC_CUDA_TRY(cudaMemcpyAsync(&fc, a.newc, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+    MC_CUDA_TRY(cudaStreamSynchronize(st));
+    for (uint32_t t = 1; t < L; ++t) {
+        KmppArgs b = a;
+        b.dist = T.p;
+        b.newc = cand.p;
+        MC_TRY(put_u(uniform_at(seed, counter++)));
+        k_kmpp_pick<<<1, 1, 0, st>>>(ubuf.p, n, cand.p), note_launch();
+        MC_TRY(kmpp_add_candidate(b, 1, 0, sms, st));
+        double oc = 0.0;
+        MC_TRY(kmpp_cost(b, chunk_tmp, scal.p, st, &oc));
+        if (oc < fcost) {
+            fcost = oc;
+            MC_CUDA_TRY(cudaMemcpyAsync(&fc, cand.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(a.dist, T.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            MC_CUDA_TRY(cudaStreamSynchronize(st));
+        }
+    }
+    uint32_t fc32 = uint32_t(fc);
+    MC_CUDA_TRY(cudaMemcpyAsync(a.center_ids, &fc32, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    MC_CUDA_TRY(cudaMemsetAsync(a.asn, 0, n * sizeof(uint32_t), st));
+    MC_CUDA_TRY(cudaMemcpyAsync(O.p, a.dist, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    MC_CUDA_TRY(cudaMemsetAsync(OA.p, 0, n * sizeof(uint32_t), st));
+    MC_CUDA_TRY(cudaStreamSynchronize(st));
+    DetInput in{a.w ? DET_F64_W : DET_F64, a.dist, nullptr, a.w, n};
+    for (uint32_t ci = 1; ci < a.k; ++ci) {
+        for (uint32_t s = 0; s < L; ++s) {
+            MC_TRY(launch_det_draw(in, chunk_tmp, nullptr, uniform_at(seed, counter++), 0, nullptr, cand.p + s, st));
+            k_kmpp_exclude<<<1, 1, 0, st>>>(a.dist, cand.p + s, sav.p + s), note_launch();
+        }
+        k_kmpp_restore<<<1, 1, 0, st>>>(a.dist, cand.p, sav.p, L), note_launch();
+        double dsum = -1.0;
+        uint32_t best = 0;
+        for (uint32_t s = 0; s < L; ++s) {
+            KmppArgs b = a;
+            b.newc = cand.p + s;
+            if (s > 0) {
+                MC_CUDA_TRY(cudaMemcpyAsync(S.p, O.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+                MC_CUDA_TRY(cudaMemcpyAsync(SA.p, OA.p, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+                b.dist = S.p;
+                b.asn = SA.p;
+            }
+            MC_TRY(kmpp_add_candidate(b, 0, ci, sms, st));
+            double nsum = 0.0;
+            MC_TRY(kmpp_cost(b, chunk_tmp, scal.p, st, &nsum));
+            if (s == 0) {
+                dsum = nsum;
+            } else if (nsum < dsum) {
+                dsum = nsum;
+                best = s;
+                MC_CUDA_TRY(cudaMemcpyAsync(a.dist, S.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+                MC_CUDA_TRY(cudaMemcpyAsync(a.asn, SA.p, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+            }
+        }
+        k_kmpp_set_center<<<1, 1, 0, st>>>(a.dist, a.asn, a.center_ids, cand.p + best, ci), note_launch();
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 // centers[c] = row ids[c] (dense copy, or a zero-filled row with the CSR entries scattered)
 __global__ void k_gather_rows_dense(const float *__restrict__ X, uint64_t d, const uint32_t *__restrict__ ids,
                                     uint32_t k, float *__restrict__ C) {

@@ -30,6 +30,8 @@ struct KmppArgs {
 };
 
 int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);
+// n_local_trials = L > 1: greedy seeding with uniforms U(seed, r) (see mc_kmpp.cu)
+int run_kmeanspp_greedy(const KmppArgs &a, uint32_t L, uint64_t seed, double *chunk_tmp, int sms, cudaStream_t st);
 
 // CSR seeding takes the O(nnz)-per-row update (per-center FP64 constants, a.ct / a.cconst)
 // only for wide rows: each round then pays a few microseconds of dependent FP64 sums (about

@@ -61,6 +61,7 @@ def lib():
             "orc_msr_sparse": (D, [I, P, P, U64, P, P, U64, U64, D, D, D, D]),
             "orc_assign": (I, [P, P, U32, I, D, P, P]),
             "orc_kmeanspp": (I, [P, U32, I, D, P, P, P, P, P]),
+            "orc_kmeanspp_greedy": (I, [P, U32, I, D, P, U32, U64, P, P, P]),
             "orc_hcluster": (I, [P, P, U32, I, D, P, D, U64, U64, P, P, P, P, P, P]),
             "orc_l1_centers": (I, [P, P, U32, P, P]),
             "orc_scluster": (I, [P, P, U32, I, D, P, D, U64, D, P, P, P, P, P, P]),
@@ -181,6 +182,19 @@ def l1_centers(X, asn, k, weights=None):
     if rc:
         raise ValueError(f"orc_l1_centers failed ({rc})")
     return out
+
+
+def kmeanspp_greedy(X, k, msr, prior, n_local_trials, seed, weights=None):
+    M = Matrix(X)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    kk = min(k, M.n)
+    ids = np.empty(kk, dtype=np.uint32)
+    asn = np.empty(M.n, dtype=np.uint32)
+    costs = np.empty(M.n, dtype=np.float64)
+    rc = lib().orc_kmeanspp_greedy(M.ref(), k, msr, prior, _p(w), n_local_trials, seed, _p(ids), _p(asn), _p(costs))
+    if rc:
+        raise ValueError("orc_kmeanspp_greedy failed")
+    return ids, asn, costs
 
 
 def hcluster(X, centers, msr, prior, weights=None, eps=1e-10, maxiter=100, seed=1):

@@ -544,6 +544,86 @@ int orc_assign(const orc_matrix *mm, const float *centers, uint32_t k, int msr, 
 
 // coresets::kmeanspp (kmeans.h:49-215) with n_local_trials == 1 and no ls++.
 // uniforms[0] picks the first center (floor(u * n)); uniforms[c] drives round c.
+// greedy k-means++ (n_local_trials = L > 1, kmeans.h:79-177) with uniforms U(seed, r) from one
+// counter: the first center is the best of L uniform picks (strictly lower objective wins);
+// each round draws L candidates from (w *) dist without replacement (a drawn row's weight is
+// zeroed for the next draw; index n -> 0), candidate 0 updates dist / asn in place (every row,
+// its own included), candidates 1.. update copies of the first center's distances and
+// assignments (odists, oasn) and replace dist / asn when their objective is strictly lower.
+int orc_kmeanspp_greedy(const orc_matrix *mm, uint32_t k, int msr, double prior, const double *w, uint32_t L,
+                        uint64_t seed, uint32_t *centers, uint32_t *asn_out, double *costs) {
+    const Mat m = to_mat(mm);
+    const uint64_t n = m.n;
+    if (n == 0 || k == 0 || L < 2) return 1;
+    if (k > n) k = uint32_t(n);
+    std::vector<double> rs(n);
+    for (uint64_t i = 0; i < n; ++i) rs[i] = row_sum(m, i);
+    const double psum = prior * double(m.d);
+    uint64_t counter = 0;
+    auto U = [&]() { return uniform_at(seed, counter++); };
+    auto pick = [&](double u) { uint64_t c = uint64_t(u * double(n)); return c >= n ? n - 1 : c; };
+    auto cost_of = [&](const std::vector<double> &v) {
+        return w ? det_sum([&](uint64_t i) { return w[i] * v[i]; }, n) : det_sum([&](uint64_t i) { return v[i]; }, n);
+    };
+    auto first_dists = [&](uint64_t c, std::vector<double> &v) {
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t i = 0; i < int64_t(n); ++i)
+            v[i] = (uint64_t(i) == c) ? 0. : dist_row_row(m, uint64_t(i), c, msr, prior, psum, rs[i], rs[c]);
+    };
+    std::vector<double> dist(n), tmp(n);
+    uint64_t fc = pick(U());
+    first_dists(fc, dist);
+    double fcost = cost_of(dist);
+    for (uint32_t t = 1; t < L; ++t) {
+        const uint64_t ofc = pick(U());
+        first_dists(ofc, tmp);
+        const double oc = cost_of(tmp);
+        if (oc < fcost) { std::swap(dist, tmp); fcost = oc; fc = ofc; }
+    }
+    std::vector<uint32_t> asn(n, 0u);
+    centers[0] = uint32_t(fc);
+    const std::vector<double> odists = dist;
+    const std::vector<uint32_t> oasn = asn;
+    std::vector<uint64_t> cand(L);
+    std::vector<double> sv(n);
+    std::vector<uint32_t> sa(n);
+    for (uint32_t ci = 1; ci < k; ++ci) {
+        std::vector<double> saved(L);
+        for (uint32_t s = 0; s < L; ++s) {
+            uint64_t c = w ? det_draw([&](uint64_t i) { return w[i] * dist[i]; }, n, U())
+                           : det_draw([&](uint64_t i) { return dist[i]; }, n, U());
+            if (c >= n) c = 0;
+            cand[s] = c;
+            saved[s] = dist[c];
+            dist[c] = 0.;
+        }
+        for (int s = int(L) - 1; s >= 0; --s) dist[cand[s]] = saved[s];
+        double dsum = -1.;
+        uint32_t best = 0;
+        for (uint32_t s = 0; s < L; ++s) {
+            const uint64_t c = cand[s];
+            std::vector<double> &V = s == 0 ? dist : sv;
+            std::vector<uint32_t> &A = s == 0 ? asn : sa;
+            if (s > 0) { sv = odists; sa = oasn; }
+#pragma omp parallel for schedule(dynamic, 64)
+            for (int64_t i = 0; i < int64_t(n); ++i) {
+                const double dv = uint64_t(i) == c ? 0. : dist_row_row(m, uint64_t(i), c, msr, prior, psum, rs[i], rs[c]);
+                if (dv < V[i]) { V[i] = dv; A[i] = ci; }
+            }
+            const double nsum = cost_of(V);
+            if (s == 0) dsum = nsum;
+            else if (nsum < dsum) { dsum = nsum; best = s; dist = sv; asn = sa; }
+        }
+        const uint64_t newc = cand[best];
+        centers[ci] = uint32_t(newc);
+        asn[newc] = ci;
+        dist[newc] = 0.;
+    }
+    std::copy(asn.begin(), asn.end(), asn_out);
+    std::copy(dist.begin(), dist.end(), costs);
+    return 0;
+}
+
 int orc_kmeanspp(const orc_matrix *mm, uint32_t k, int msr, double prior, const double *w, const double *uniforms,
                  uint32_t *centers, uint32_t *asn, double *costs) {
     const Mat m = to_mat(mm);

@@ -69,8 +69,6 @@ def test_python_api_rejects_out_of_scope_options():
     with pytest.raises(NotImplementedError):
         mc.kmeanspp(X, 2, lspp=1)
     with pytest.raises(NotImplementedError):
-        mc.kmeanspp(X, 2, n_local_trials=3)
-    with pytest.raises(NotImplementedError):
         mc.scluster(X, [0, 1], mbsize=2)
 
 

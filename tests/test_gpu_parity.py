@@ -168,6 +168,19 @@ def test_kmeanspp_dense_matches_oracle(mc, orc, msr):
         assert np.array_equal(costs, ocosts.astype(np.float32))
 
 
+@pytest.mark.parametrize("msr,trials,weighted", [(2, 3, False), (2, 2, True), (0, 4, False)])
+def test_kmeanspp_greedy_matches_oracle(mc, orc, msr, trials, weighted):
+    """n_local_trials > 1 (greedy seeding, kmeans.h:79-177): ids, assignments and distances
+    bit-exact against the oracle's restatement."""
+    X = _mixture(3000, 12, 9, seed=50 + msr, nonneg=msr != 2)
+    w = np.random.default_rng(6).uniform(0.5, 2.0, 3000) if weighted else None
+    ids, asn, costs = mc.kmeanspp(X, 10, msr=msr, seed=21, n_local_trials=trials, weights=w)
+    oids, oasn, ocosts = orc.kmeanspp_greedy(X, 10, msr, 0.0, trials, 21, weights=w)
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(asn.astype(np.uint32), oasn)
+    assert np.array_equal(costs, ocosts.astype(np.float32))
+
+
 def test_kmeanspp_weighted_and_csr(mc, orc):
     X = _mixture(3000, 16, 8, seed=11)
     w = np.random.default_rng(2).random(3000) + 0.1
