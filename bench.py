@@ -178,6 +178,23 @@ def csr_bench(args):
                         "frac": algo_bytes / (kms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6767.7),
                         "algorithmic_bytes": algo_bytes, "kernel_ms": kms, "peak_source": pk_kind},
            "phases_ms": phases}
+    if not args.no_cpu:
+        # the oracle (CPU restatement, 16-thread OpenMP union walk of the reference's sparse
+        # measures) on the first rows of the same matrix and centers, scaled to all n rows
+        import scipy.sparse as sp
+        import oracle
+        S = 2000 if msr == 5 else 1000
+        ipc_s = ipc[:S + 1].numpy().astype(np.int64)
+        sub = sp.csr_matrix((vals[:int(ipc_s[-1])].cpu().numpy(), idx[:int(ipc_s[-1])].cpu().numpy().astype(np.int64),
+                             ipc_s), shape=(S, d))
+        Ch = C.cpu().numpy()
+        t0 = time.perf_counter()
+        oracle.assign(sub, Ch, msr, 1.0)
+        cpu_s = (time.perf_counter() - t0) * (n / S)
+        out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "passes/s", "cores": os.cpu_count() or 1,
+                               "kind": "port",
+                               "sample": f"oracle assignment of the first {S} rows against the same {k} centers, "
+                                         f"scaled by {n}/{S}"}
     print(json.dumps(out))
 
 
@@ -792,10 +809,17 @@ def small_bench(args):
                for m in ("graph", "fused") for key in ("asn", "costs", "centers"))
     best = min(out, key=lambda m: out[m]["ms_per_call_p50"])
     g = out[best]
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        t0 = time.perf_counter()
+        oracle.hcluster(X, C0, 2, 0.0, eps=0.0, maxiter=19, seed=3)
+        cpu = {"value": 1.0 / (time.perf_counter() - t0), "unit": "calls/s", "cores": os.cpu_count() or 1,
+               "kind": "port", "sample": "the whole oracle hcluster on the same 10000 x 50 rows and seeds"}
     print(json.dumps({"metric": "hcluster calls/s 10000x50 k=25 (20 updates, host arrays in and out)",
                       "value": 1000.0 / g["ms_per_call_p50"], "unit": "calls/s", "loop_mode": best,
                       "lloyd_iters_per_s": g["updates"] * 1000.0 / g["ms_per_call_p50"],
-                      "modes": out, "identical": bool(same),
+                      "modes": out, "identical": bool(same), "cpu_baseline": cpu,
                       "steps": args.steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic",
                       "config": {"workload": "10000x50, 25 components, k=25, kmeans++ seeds, maxiter=19, eps=0"}}))
 
