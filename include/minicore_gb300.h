@@ -123,6 +123,15 @@ int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double
 int mc_kmeanspp_greedy(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior,
                        const double *weights, uint32_t n_local_trials, uint64_t seed,
                        uint32_t *center_ids, uint32_t *asn, double *costs);
+/* mc_kmeanspp_greedy followed by lspp_rounds of localsearch++ (localsearchpp_rounds,
+ * optim/lsearchpp.h:21-123; kmeanspp's lspp argument, kmeans.h:209-212): swaps a center for
+ * a D^2-drawn row when that lowers the objective.  Charges and gains are canonical FP64
+ * sums; draws use U(seed ^ 0x4C53505053454544, r).  On return costs are the row minima of
+ * the reference's lspp matrix (msr(lh = row, rh = center)) and asn their first argmin.
+ * lspp_rounds > 0 needs k >= 2. */
+int mc_kmeanspp_ex(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior,
+                   const double *weights, uint32_t n_local_trials, uint64_t lspp_rounds, uint64_t seed,
+                   uint32_t *center_ids, uint32_t *asn, double *costs);
 
 /* One hard assignment pass (solve.h:234-285): asn[i] = argmin_j msr(row i, center j),
  * lowest index on ties; costs[i] = that distance.  centers: dense k x ncols float32. */

@@ -254,10 +254,9 @@ def kmeanspp(matrix, k, *, msr=2, prior=0., seed=0, ntimes=1, lspp=0, expskips=0
     """D^2 seeding (include/minicore/optim/kmeans.h:49-215).  Returns (center ids,
     assignments, costs); costs are float32 for dense input and float64 for CSR input, as in
     the reference bindings.  ``n_local_trials > 1``: greedy seeding (mc_kmeanspp_greedy, uniforms
-    U(seed + run, r)).  ``lspp`` rounds are not implemented."""
-    if lspp:
-        raise NotImplementedError("localsearch++ rounds are outside the implemented hot path")
+    U(seed + run, r)); ``lspp`` > 0: that many localsearch++ rounds afterwards (mc_kmeanspp_ex)."""
     trials = max(int(n_local_trials or 1), 1)
+    lspp = max(int(lspp or 0), 0)
     ctx = ctx or default_context()
     M = _MatrixArg(matrix)
     k = int(k)
@@ -277,7 +276,10 @@ def kmeanspp(matrix, k, *, msr=2, prior=0., seed=0, ntimes=1, lspp=0, expskips=0
         ids = np.empty(kk, dtype=np.uint32)
         asn = np.empty(M.n, dtype=np.uint32)
         costs = np.empty(M.n, dtype=np.float64)
-        if trials > 1:
+        if lspp:
+            check(_lib.load().mc_kmeanspp_ex(ctx.handle, M.ref, k, _msr(msr), float(prior), _p(w), trials, lspp,
+                                             (seed + t) & 0xFFFFFFFFFFFFFFFF, _p(ids), _p(asn), _p(costs)))
+        elif trials > 1:
             check(_lib.load().mc_kmeanspp_greedy(ctx.handle, M.ref, k, _msr(msr), float(prior), _p(w), trials,
                                                  (seed + t) & 0xFFFFFFFFFFFFFFFF, _p(ids), _p(asn), _p(costs)))
         else:

@@ -48,6 +48,7 @@ SIGNATURES = {
     "mc_uniforms": (I, [U64, U64, U64, P]),
     "mc_kmeanspp": (I, [P, P, U32, I, D, P, P, P, P, P]),
     "mc_kmeanspp_greedy": (I, [P, P, U32, I, D, P, U32, U64, P, P, P]),
+    "mc_kmeanspp_ex": (I, [P, P, U32, I, D, P, U32, U64, U64, P, P, P]),
     "mc_assign": (I, [P, P, P, U32, I, D, I, P, P]),
     "mc_cmp": (I, [P, P, P, U64, I, D, I, P]),
     "mc_pcmp": (I, [P, P, I, D, P]),

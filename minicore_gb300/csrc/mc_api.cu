@@ -1908,9 +1908,141 @@ int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
 
 }  // extern "C"
 
+namespace {
+
+// ------------------------------------------------------------------------------------
+// localsearch++ rounds after the seeding (localsearchpp_rounds, optim/lsearchpp.h:21-123).
+// M[i][j] is the reference's oracle(i, center j) = msr(lh = row i, rh = center row j) (its
+// kmeans++ oracle takes the first index as the center), distances the row minima of M.
+// Each round draws a row sel (from the distances; with weights, from the previous round's
+// new costs times the weights, as the reference does, zeros before the first round), takes
+// new[i] = msr(lh = row sel, rh = row i); a row with new[i] > dist[i] charges
+// top2 - top1 of its M row to its top1 center (none on a tie), any other row adds
+// dist[i] - new[i] to the gain; the center with the smallest charge (first on ties) is
+// swapped for sel when charge - gain < 0.  Per-center charges and the gain are canonical
+// FP64 sums; the reference adds them with atomics.  Uniforms U(seed ^ 0x4C53505053454544, r).
+// ------------------------------------------------------------------------------------
+constexpr uint64_t kLsppStream = 0x4C53505053454544ull;
+
+__global__ void k_lspp_rowmin(const float *__restrict__ M, uint64_t n, uint32_t k, double *dist, uint32_t *asn) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x)) {
+        const float *r = M + i * k;
+        float b = r[0];
+        uint32_t bj = 0;
+        for (uint32_t j = 1; j < k; ++j)
+            if (r[j] < b) { b = r[j]; bj = j; }
+        dist[i] = double(b);
+        if (asn) asn[i] = bj;
+    }
+}
+
+__global__ void k_lspp_rows(const float *__restrict__ M, uint64_t n, uint32_t k, const double *__restrict__ dist,
+                            const double *__restrict__ nc, uint32_t *key, double *charge, double *gterm) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x)) {
+        key[i] = 0xffffffffu;
+        charge[i] = 0.0;
+        gterm[i] = 0.0;
+        if (nc[i] > dist[i]) {
+            const float *r = M + i * k;
+            double v1 = r[0], v2 = r[1];
+            uint32_t j1 = 0, j2 = 1;
+            if (v2 < v1) { const double tv = v1; v1 = v2; v2 = tv; const uint32_t tj = j1; j1 = j2; j2 = tj; }
+            for (uint32_t j = 2; j < k; ++j) {
+                const double v = r[j];
+                if (v < v2) {
+                    if (v < v1) { v2 = v1; j2 = j1; v1 = v; j1 = j; }
+                    else { v2 = v; j2 = j; }
+                }
+            }
+            (void)j2;
+            if (v1 != v2) {
+                key[i] = j1;
+                charge[i] = v2 - v1;
+            }
+        } else {
+            gterm[i] = dist[i] - nc[i];
+        }
+    }
+}
+
+__global__ void k_lspp_set_col(float *M, uint64_t n, uint32_t k, uint32_t col, const double *__restrict__ nc) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x))
+        M[i * k + col] = float(nc[i]);
+}
+
+int run_lspp(mc_context *ctx, const mc_matrix *X, const KmppArgs &a, uint32_t k, int msr, double prior,
+             uint64_t rounds, uint64_t seed, uint32_t *ids, uint32_t *asn, double *dist, double *det_tmp,
+             cudaStream_t st) {
+    const uint64_t n = a.n, d = a.d;
+    if (k < 2) return fail(MC_EINVAL, "localsearch++ needs k >= 2");
+    DBuf<float> C, M;
+    DBuf<double> nc, charge, gterm, scal;
+    DBuf<uint32_t> key, ids_scratch;
+    DBuf<uint64_t> sel_dev;
+    MC_TRY(C.alloc(uint64_t(k) * d, st));
+    MC_TRY(M.alloc(n * k, st));
+    MC_TRY(nc.alloc(n, st));
+    MC_TRY(charge.alloc(n, st));
+    MC_TRY(gterm.alloc(n, st));
+    MC_TRY(scal.alloc(1, st));
+    MC_TRY(key.alloc(n, st));
+    MC_TRY(ids_scratch.alloc(1, st));
+    MC_TRY(sel_dev.alloc(1, st));
+    MC_TRY(launch_gather_rows(a.csr, a.X, a.vals, a.idx, a.indptr, d, ids, k, C.p, st));
+    MC_TRY(sync(st));
+    MC_TRY(mc_cmp(ctx, X, C.p, k, msr, prior, 1, M.p));
+    const unsigned g = unsigned(umin64((n + 255) / 256, 4096));
+    k_lspp_rowmin<<<g, 256, 0, st>>>(M.p, n, k, dist, nullptr), note_launch();
+    MC_CUDA_TRY(cudaMemsetAsync(nc.p, 0, n * sizeof(double), st));
+    std::vector<uint32_t> hids(k);
+    MC_CUDA_TRY(cudaMemcpyAsync(hids.data(), ids, k * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    MC_TRY(sync(st));
+    KmppArgs b = a;
+    b.center_ids = ids_scratch.p;
+    for (uint64_t r = 0; r < rounds; ++r) {
+        const double u = uniform_at(seed ^ kLsppStream, r);
+        DetInput din{a.w ? DET_F64_W : DET_F64, a.w ? nc.p : dist, nullptr, a.w, n};
+        MC_TRY(launch_det_draw(din, det_tmp, nullptr, u, 0, nullptr, sel_dev.p, st));
+        MC_TRY(kmpp_distances_to(b, sel_dev.p, nc.p, ctx->sms, st));
+        k_lspp_rows<<<g, 256, 0, st>>>(M.p, n, k, dist, nc.p, key.p, charge.p, gterm.p), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        std::vector<double> cc(k);
+        double gain = 0.0;
+        {
+            DetInput gi{DET_F64, gterm.p, nullptr, nullptr, n};
+            MC_TRY(launch_det_sum(gi, det_tmp, scal.p, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(&gain, scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MC_TRY(sync(st));
+        }
+        for (uint32_t c = 0; c < k; ++c) {
+            DetInput ci{DET_F64_KEY, charge.p, nullptr, nullptr, n, key.p, c};
+            MC_TRY(launch_det_sum(ci, det_tmp, scal.p, st));
+            MC_CUDA_TRY(cudaMemcpyAsync(&cc[c], scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MC_TRY(sync(st));
+        }
+        uint32_t am = 0;
+        for (uint32_t c = 1; c < k; ++c)
+            if (cc[c] < cc[am]) am = c;
+        if (cc[am] - gain < 0.0) {
+            uint64_t sel = 0;
+            MC_CUDA_TRY(cudaMemcpyAsync(&sel, sel_dev.p, sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
+            MC_TRY(sync(st));
+            hids[am] = uint32_t(sel);
+            k_lspp_set_col<<<g, 256, 0, st>>>(M.p, n, k, am, nc.p), note_launch();
+            k_lspp_rowmin<<<g, 256, 0, st>>>(M.p, n, k, dist, nullptr), note_launch();
+        }
+    }
+    MC_CUDA_TRY(cudaMemcpyAsync(ids, hids.data(), k * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    k_lspp_rowmin<<<g, 256, 0, st>>>(M.p, n, k, dist, asn), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return sync(st);
+}
+
+}  // namespace
+
 static int kmeanspp_impl(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
                          const double *uniforms, uint32_t local_trials, uint64_t seed, uint32_t *center_ids,
-                         uint32_t *asn, double *costs) {
+                         uint32_t *asn, double *costs, uint64_t lspp_rounds = 0) {
     if (!ctx) return fail(MC_EINVAL, "ctx is null");
     if (!measure_supported(msr)) return fail(MC_EUNSUPPORTED, "measure not implemented on this path");
     if (!uniforms && local_trials <= 1) return fail(MC_EINVAL, "uniforms is null");
@@ -1974,6 +2106,7 @@ static int kmeanspp_impl(mc_context *ctx, const mc_matrix *X, uint32_t k, int ms
     a.newc = newc.p;
     if (local_trials > 1) MC_TRY(run_kmeanspp_greedy(a, local_trials, seed, tmp.p, ctx->sms, st));
     else MC_TRY(run_kmeanspp(a, u.p, tmp.p, ctx->sms, st));
+    if (lspp_rounds) MC_TRY(run_lspp(ctx, X, a, k, msr, prior, lspp_rounds, seed, ids.p, asnb.p, dist.p, tmp.p, st));
     MC_TRY(copy_out(center_ids, ids.p, k, st));
     MC_TRY(copy_out(asn, asnb.p, n, st));
     MC_TRY(copy_out(costs, dist.p, n, st));
@@ -1986,6 +2119,19 @@ extern "C" {
 int mc_kmeanspp(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
                 const double *uniforms, uint32_t *center_ids, uint32_t *asn, double *costs) {
     return kmeanspp_impl(ctx, X, k, msr, prior, weights, uniforms, 1, 0, center_ids, asn, costs);
+}
+
+int mc_kmeanspp_ex(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,
+                   uint32_t n_local_trials, uint64_t lspp_rounds, uint64_t seed, uint32_t *center_ids, uint32_t *asn,
+                   double *costs) {
+    if (n_local_trials == 0) return fail(MC_EINVAL, "n_local_trials must be positive");
+    if (n_local_trials == 1) {
+        std::vector<double> u(k);
+        for (uint32_t i = 0; i < k; ++i) u[i] = uniform_at(seed, i);
+        return kmeanspp_impl(ctx, X, k, msr, prior, weights, u.data(), 1, seed, center_ids, asn, costs, lspp_rounds);
+    }
+    return kmeanspp_impl(ctx, X, k, msr, prior, weights, nullptr, n_local_trials, seed, center_ids, asn, costs,
+                         lspp_rounds);
 }
 
 int mc_kmeanspp_greedy(mc_context *ctx, const mc_matrix *X, uint32_t k, int msr, double prior, const double *weights,

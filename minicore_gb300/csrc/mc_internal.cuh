@@ -122,6 +122,7 @@ enum DetSrc : int {
     DET_F32 = 1,        // (double)xf[i]
     DET_F64_W = 2,      // x[i] * w[i]
     DET_F32_W = 3,      // (double)xf[i] * w[i]
+    DET_F64_KEY = 4,    // key[i] == kval ? x[i] : 0
 };
 
 struct DetInput {
@@ -130,11 +131,14 @@ struct DetInput {
     const float *xf;
     const double *w;
     uint64_t n;
+    const uint32_t *key = nullptr;
+    uint32_t kval = 0;
     __device__ inline double get(uint64_t i) const {
         switch (src) {
             case DET_F64: return x[i];
             case DET_F32: return double(xf[i]);
             case DET_F64_W: return x[i] * w[i];
+            case DET_F64_KEY: return key[i] == kval ? x[i] : 0.0;
             default: return double(xf[i]) * w[i];
         }
     }

@@ -761,6 +761,16 @@ int run_kmeanspp_greedy(const KmppArgs &a0, uint32_t L, uint64_t seed, double *c
     return MC_OK;
 }
 
+// out[i] = distance of row i to the row *cand (0 for that row): the first-round update of
+// the seeding kernels.  CSR centers pass through a.cbuf; a.center_ids[0] and a.asn[*cand]
+// may be written (callers pass scratch for the former).
+int kmpp_distances_to(const KmppArgs &a0, const uint64_t *cand, double *out, int sms, cudaStream_t st) {
+    KmppArgs b = a0;
+    b.dist = out;
+    b.newc = const_cast<uint64_t *>(cand);
+    return kmpp_add_candidate(b, 1, 0, sms, st);
+}
+
 // centers[c] = row ids[c] (dense copy, or a zero-filled row with the CSR entries scattered)
 __global__ void k_gather_rows_dense(const float *__restrict__ X, uint64_t d, const uint32_t *__restrict__ ids,
                                     uint32_t k, float *__restrict__ C) {

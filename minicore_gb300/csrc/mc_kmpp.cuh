@@ -30,6 +30,8 @@ struct KmppArgs {
 };
 
 int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);
+// distances of every row to row *cand (see mc_kmpp.cu)
+int kmpp_distances_to(const KmppArgs &a, const uint64_t *cand, double *out, int sms, cudaStream_t st);
 // n_local_trials = L > 1: greedy seeding with uniforms U(seed, r) (see mc_kmpp.cu)
 int run_kmeanspp_greedy(const KmppArgs &a, uint32_t L, uint64_t seed, double *chunk_tmp, int sms, cudaStream_t st);
 

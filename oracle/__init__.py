@@ -62,6 +62,7 @@ def lib():
             "orc_assign": (I, [P, P, U32, I, D, P, P]),
             "orc_kmeanspp": (I, [P, U32, I, D, P, P, P, P, P]),
             "orc_kmeanspp_greedy": (I, [P, U32, I, D, P, U32, U64, P, P, P]),
+            "orc_lspp": (I, [P, U32, I, D, P, U64, U64, P, P, P]),
             "orc_hcluster": (I, [P, P, U32, I, D, P, D, U64, U64, P, P, P, P, P, P]),
             "orc_l1_centers": (I, [P, P, U32, P, P]),
             "orc_scluster": (I, [P, P, U32, I, D, P, D, U64, D, P, P, P, P, P, P]),
@@ -194,6 +195,19 @@ def kmeanspp_greedy(X, k, msr, prior, n_local_trials, seed, weights=None):
     rc = lib().orc_kmeanspp_greedy(M.ref(), k, msr, prior, _p(w), n_local_trials, seed, _p(ids), _p(asn), _p(costs))
     if rc:
         raise ValueError("orc_kmeanspp_greedy failed")
+    return ids, asn, costs
+
+
+def lspp(X, ids, msr, prior, rounds, seed, weights=None):
+    """localsearch++ rounds on seeded center ids (returns ids, asn, costs)."""
+    M = Matrix(X)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
+    ids = np.array(ids, dtype=np.uint32, copy=True)
+    asn = np.empty(M.n, dtype=np.uint32)
+    costs = np.empty(M.n, dtype=np.float64)
+    rc = lib().orc_lspp(M.ref(), ids.size, msr, prior, _p(w), rounds, seed, _p(ids), _p(asn), _p(costs))
+    if rc:
+        raise ValueError("orc_lspp failed")
     return ids, asn, costs
 
 

@@ -624,6 +624,86 @@ int orc_kmeanspp_greedy(const orc_matrix *mm, uint32_t k, int msr, double prior,
     return 0;
 }
 
+// localsearch++ rounds (localsearchpp_rounds, optim/lsearchpp.h:21-123) on seeded centers.
+// M[i][j] = msr(lh = row i, rh = center row j) (the kmeans++ oracle takes its first index as
+// the center); dist = row minima of M.  Round r: u = U(seed ^ 0x4C53505053454544, r); sel drawn
+// from dist (with weights: from the previous round's new costs times the weights, zeros
+// before the first round; index n -> 0); nc[i] = msr(lh = row sel, rh = row i) (0 for sel);
+// rows with nc > dist charge top2 - top1 of their M row (the reference's top-2 scan) to the
+// top1 center unless tied, others add dist - nc to the gain; the first center with the least
+// charge is replaced by sel when charge - gain < 0.  Charges per center and the gain are
+// det_sum's of the masked per-row values.  Afterwards asn = first argmin of each M row.
+int orc_lspp(const orc_matrix *mm, uint32_t k, int msr, double prior, const double *w, uint64_t rounds,
+             uint64_t seed, uint32_t *centers, uint32_t *asn, double *costs) {
+    const Mat m = to_mat(mm);
+    const uint64_t n = m.n;
+    if (k < 2 || n == 0) return 1;
+    std::vector<double> rs(n);
+    for (uint64_t i = 0; i < n; ++i) rs[i] = row_sum(m, i);
+    const double psum = prior * double(m.d);
+    std::vector<float> M(n * k);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < int64_t(n); ++i)
+        for (uint32_t j = 0; j < k; ++j)
+            M[uint64_t(i) * k + j] = float(dist_row_row(m, centers[j], uint64_t(i), msr, prior, psum, rs[centers[j]],
+                                                        rs[uint64_t(i)]));
+    std::vector<double> dist(n), nc(n, 0.), charge(n), gterm(n);
+    std::vector<uint32_t> key(n);
+    auto rowmin = [&]() {
+        for (uint64_t i = 0; i < n; ++i) {
+            float b = M[i * k];
+            uint32_t bj = 0;
+            for (uint32_t j = 1; j < k; ++j) if (M[i * k + j] < b) { b = M[i * k + j]; bj = j; }
+            dist[i] = double(b);
+            asn[i] = bj;
+        }
+    };
+    rowmin();
+    for (uint64_t r = 0; r < rounds; ++r) {
+        const double u = uniform_at(seed ^ 0x4C53505053454544ull, r);
+        uint64_t sel = w ? det_draw([&](uint64_t i) { return nc[i] * w[i]; }, n, u)
+                         : det_draw([&](uint64_t i) { return dist[i]; }, n, u);
+        if (sel >= n) sel = 0;
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t i = 0; i < int64_t(n); ++i)
+            nc[i] = uint64_t(i) == sel ? 0. : dist_row_row(m, uint64_t(i), sel, msr, prior, psum, rs[uint64_t(i)], rs[sel]);
+        for (uint64_t i = 0; i < n; ++i) {
+            key[i] = 0xffffffffu; charge[i] = 0.; gterm[i] = 0.;
+            if (nc[i] > dist[i]) {
+                const float *row = &M[i * k];
+                double v1 = row[0], v2 = row[1];
+                uint32_t j1 = 0, j2 = 1;
+                if (v2 < v1) { std::swap(v1, v2); std::swap(j1, j2); }
+                for (uint32_t j = 2; j < k; ++j) {
+                    const double v = row[j];
+                    if (v < v2) {
+                        if (v < v1) { v2 = v1; j2 = j1; v1 = v; j1 = j; }
+                        else { v2 = v; j2 = j; }
+                    }
+                }
+                if (v1 != v2) { key[i] = j1; charge[i] = v2 - v1; }
+            } else {
+                gterm[i] = dist[i] - nc[i];
+            }
+        }
+        const double gain = det_sum([&](uint64_t i) { return gterm[i]; }, n);
+        uint32_t am = 0;
+        double best = 0.;
+        for (uint32_t c = 0; c < k; ++c) {
+            const double cc = det_sum([&](uint64_t i) { return key[i] == c ? charge[i] : 0.; }, n);
+            if (c == 0 || cc < best) { best = cc; am = c; }
+        }
+        if (best - gain < 0.) {
+            centers[am] = uint32_t(sel);
+            for (uint64_t i = 0; i < n; ++i) M[i * k + am] = float(nc[i]);
+            rowmin();
+        }
+    }
+    rowmin();
+    std::copy(dist.begin(), dist.end(), costs);
+    return 0;
+}
+
 int orc_kmeanspp(const orc_matrix *mm, uint32_t k, int msr, double prior, const double *w, const double *uniforms,
                  uint32_t *centers, uint32_t *asn, double *costs) {
     const Mat m = to_mat(mm);

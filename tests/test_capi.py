@@ -67,8 +67,6 @@ def test_python_api_rejects_out_of_scope_options():
     import minicore_gb300 as mc
     X = np.zeros((4, 3), np.float32)
     with pytest.raises(NotImplementedError):
-        mc.kmeanspp(X, 2, lspp=1)
-    with pytest.raises(NotImplementedError):
         mc.scluster(X, [0, 1], mbsize=2)
 
 

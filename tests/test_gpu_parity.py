@@ -181,6 +181,24 @@ def test_kmeanspp_greedy_matches_oracle(mc, orc, msr, trials, weighted):
     assert np.array_equal(costs, ocosts.astype(np.float32))
 
 
+@pytest.mark.parametrize("msr,trials,weighted", [(2, 1, False), (2, 2, True), (0, 1, False), (6, 1, False)])
+def test_kmeanspp_lspp_matches_oracle(mc, orc, msr, trials, weighted):
+    """lspp > 0: localsearch++ rounds after the seeding, against the oracle's restatement
+    run on the same seeds (ids, assignments, costs bit for bit)."""
+    X = _mixture(2500, 10, 8, seed=60 + msr, nonneg=msr != 2)
+    w = np.random.default_rng(7).uniform(0.5, 2.0, 2500) if weighted else None
+    prior = 1.0 if msr == 6 else 0.0
+    ids, asn, costs = mc.kmeanspp(X, 8, msr=msr, prior=prior, seed=33, n_local_trials=trials, lspp=6, weights=w)
+    if trials > 1:
+        sids, _, _ = orc.kmeanspp_greedy(X, 8, msr, prior, trials, 33, weights=w)
+    else:
+        sids, _, _ = orc.kmeanspp(X, 8, msr, prior, orc.uniforms(33, 8), weights=w)
+    oids, oasn, ocosts = orc.lspp(X, sids, msr, prior, 6, 33, weights=w)
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(asn.astype(np.uint32), oasn)
+    assert np.array_equal(costs, ocosts.astype(np.float32))
+
+
 def test_kmeanspp_weighted_and_csr(mc, orc):
     X = _mixture(3000, 16, 8, seed=11)
     w = np.random.default_rng(2).random(3000) + 0.1
