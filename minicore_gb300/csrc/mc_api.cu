@@ -195,6 +195,7 @@ struct mc_job {
     DBuf<double> ztab;
     uint32_t ngrp = 0;
     SortWork sort;
+    L1CsrWork l1csr;  // L1 medians over CSR rows
     TcState tc;
     uint64_t last_recheck = 0;
     // Lloyd loop as one CUDA graph (mc_job_run); captured per run, and again after a host
@@ -389,9 +390,21 @@ int job_launch_centroids(mc_job *j, const uint32_t *keys2, uint64_t extra, bool 
     return launch_centroids(ca, j->sort, st, presorted);
 }
 
-// L1 over dense rows: coordinate-wise medians (set_centroids_l1, clustering/centroid.h:203,
-// 435-504) instead of means
-bool l1_medians(const mc_job *j) { return j->msr == L1 && j->M.kind == MC_DENSE_F32; }
+// L1: coordinate-wise medians (set_centroids_l1, clustering/centroid.h:203, 435-504) instead
+// of means, over dense or CSR rows
+bool l1_medians(const mc_job *j) { return j->msr == L1; }
+
+// the medians of the current (sorted) assignment into Cw
+int job_l1_medians(mc_job *j) {
+    Phase ph("centroid_update", j->st);
+    MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), j->st));
+    if (j->M.kind == MC_DENSE_F32)
+        return launch_l1_medians(j->M.X, j->M.d, j->k, j->sort, j->w.p, j->Cw.p, j->st);
+    // the reference's CSR median takes no weights (util/csc.h:835)
+    if (j->w.p) return fail(MC_EUNSUPPORTED, "Not implemented: weighted L1 median for CSparseMatrix");
+    return launch_l1_medians_csr(j->M.vals, j->M.idx, j->M.indptr, j->M.n, j->M.d, j->M.nnz, j->k, j->asn.p,
+                                 j->sort, j->l1csr, j->Cw.p, j->st);
+}
 
 // set_centroids_l1: empty clusters are reseeded one at a time (D^2 draw over the current
 // costs, then rows closer to the new center in plain L1 move to it), until none is empty;
@@ -414,16 +427,23 @@ int job_set_centroids_l1(mc_job *j) {
             DetInput in{DET_F64, j->costs.p, nullptr, nullptr, n};
             MC_TRY(launch_det_draw(in, j->det_tmp.p, nullptr, u, 0, nullptr, j->idxbuf.p + k, st));
             float *dst = j->Cw.p + uint64_t(id) * d;
-            k_copy_row_dense<<<unsigned(umin64((d + 255) / 256, 1024)), 256, 0, st>>>(j->M.X, d, j->idxbuf.p + k, dst),
-                note_launch();
-            MC_CUDA_TRY(cudaGetLastError());
-            MC_TRY(launch_l1_reseed_update(j->M.X, n, d, dst, id, j->asn.p, j->costs.p, st));
+            const unsigned gb = unsigned(umin64((d + 255) / 256, 1024));
+            if (j->M.kind == MC_DENSE_F32) {
+                k_copy_row_dense<<<gb, 256, 0, st>>>(j->M.X, d, j->idxbuf.p + k, dst), note_launch();
+                MC_CUDA_TRY(cudaGetLastError());
+                MC_TRY(launch_l1_reseed_update(j->M.X, n, d, dst, id, j->asn.p, j->costs.p, st));
+            } else {
+                k_copy_row_csr_zero<<<gb, 256, 0, st>>>(d, dst), note_launch();
+                k_copy_row_csr<<<1, 256, 0, st>>>(j->M.vals, j->M.idx, j->M.indptr, j->idxbuf.p + k, dst),
+                    note_launch();
+                MC_CUDA_TRY(cudaGetLastError());
+                MC_TRY(launch_l1_reseed_update_csr(j->M.vals, j->M.idx, j->M.indptr, n, d, dst, id, j->asn.p,
+                                                   j->costs.p, st));
+            }
         }
         MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));
     }
-    Phase ph("centroid_update", st);
-    MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), st));
-    return launch_l1_medians(j->M.X, d, k, j->sort, j->w.p, j->Cw.p, st);
+    return job_l1_medians(j);
 }
 
 int job_set_centroids(mc_job *j, int *restarted) {
@@ -607,11 +627,7 @@ int job_loop_pre(mc_job *j, LoopState *ls, cudaGraphConditionalHandle h, int gra
 
 // the centers of the current (sorted) assignment into Cw, no cluster empty
 int job_update_centers(mc_job *j) {
-    if (l1_medians(j)) {
-        Phase ph("centroid_update", j->st);
-        MC_CUDA_TRY(cudaMemsetAsync(j->flag.p, 0, sizeof(int), j->st));
-        return launch_l1_medians(j->M.X, j->M.d, j->k, j->sort, j->w.p, j->Cw.p, j->st);
-    }
+    if (l1_medians(j)) return job_l1_medians(j);
     return job_launch_centroids(j, nullptr, 0, /*presorted=*/true);
 }
 
@@ -999,6 +1015,45 @@ __global__ void __launch_bounds__(256) k_soft_center_chunks_csr(const float *__r
     }
     for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) num[(q * k + c) * d + j] = double(s[j]) + double(e[j]);
     if (threadIdx.x == 0) den[q * k + c] = double(sw) + double(ew);
+}
+
+// soft L1 centers over dense rows (set_centroids_soft, clustering/centroid.h:815-838, with
+// optim/kmedian.h: weighted_median): per center c the weights are the soft assignments of
+// column c (times the row weights); weighted_median never accumulates its weight total, so
+// it returns per column the value of the row with the largest weight (the smallest such value
+// on ties).  One CTA per (center, 32 columns): the largest weight, then the minima.
+__global__ void __launch_bounds__(256) k_soft_l1_centers(const float *__restrict__ X, uint64_t n, uint64_t d,
+                                                         const float *__restrict__ asn, uint32_t k,
+                                                         const double *__restrict__ w, float *centers) {
+    __shared__ double wmax[8];
+    __shared__ float best[8][32];
+    const uint32_t c = blockIdx.x;
+    const uint64_t c0 = uint64_t(blockIdx.y) * 32;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    double mx = -1.7976931348623157e308;
+    for (uint64_t r = t; r < n; r += 256) {
+        const double wt = w ? w[r] * double(asn[r * k + c]) : double(asn[r * k + c]);
+        mx = fmax(mx, wt);
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) wmax[warp] = mx;
+    __syncthreads();
+    mx = wmax[0];
+    for (int q = 1; q < 8; ++q) mx = fmax(mx, wmax[q]);
+    const uint64_t col = c0 + lane;
+    float bv = __int_as_float(0x7f800000);
+    for (uint64_t r = warp; r < n; r += 8) {
+        const double wt = w ? w[r] * double(asn[r * k + c]) : double(asn[r * k + c]);
+        if (wt == mx && col < d) bv = fminf(bv, X[r * d + col]);
+    }
+    best[warp][lane] = bv;
+    __syncthreads();
+    if (t < 32 && col < d) {
+        float v = best[0][lane];
+        for (int q = 1; q < 8; ++q) v = fminf(v, best[q][lane]);
+        centers[uint64_t(c) * d + col] = v;
+    }
 }
 
 __global__ void k_soft_center_accumulate(const double *__restrict__ num, const double *__restrict__ den, uint64_t nq,
@@ -1471,6 +1526,20 @@ int mc_job_minibatch(mc_job *j, uint64_t mbsize, uint64_t maxiter, uint64_t calc
         MC_TRY(job_create_impl(j->ctx, &subm, j->C.p, k, j->msr, j->prior, sr.w.p, MC_FP32, j->seed, nullptr, &sj));
         std::unique_ptr<mc_job, int (*)(mc_job *)> sguard(sj, mc_job_destroy);
         MC_TRY(job_assign_with(sj, sj->C.p, psum_mb, true));
+        if (j->msr == L1) {
+            // l1_median over each group's sampled rows (solve.h:559-561; kmedian.h:329-344,
+            // util/csc.h:829-893); groups without rows keep their center
+            MC_TRY(launch_sort_by_key(sj->asn.p, nullptr, m, k, sj->sort, st));
+            if (sj->M.kind == MC_DENSE_F32) {
+                MC_TRY(launch_l1_medians(sj->M.X, d, k, sj->sort, j->w.p, j->C.p, st, n));
+            } else {
+                if (j->w.p) return fail(MC_EUNSUPPORTED, "Not implemented: weighted L1 median for CSparseMatrix");
+                MC_TRY(launch_l1_medians_csr(sj->M.vals, sj->M.idx, sj->M.indptr, m, d, sj->M.nnz, k, sj->asn.p,
+                                             sj->sort, sj->l1csr, j->C.p, st));
+            }
+            MC_TRY(sync(st));
+            continue;
+        }
         CentroidArgs ca;
         ca.csr = sj->M.kind == MC_CSR_F32;
         ca.n = m;
@@ -1702,7 +1771,9 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
                 const double *weights, double temp, uint64_t maxiter, double eps, float *centers_out,
                 float *costs_out, float *asn_out, double *initcost_out, double *finalcost_out, uint64_t *numiter_out) {
     if (!ctx || !X || !centers_in) return fail(MC_EINVAL, "null argument");
-    if (msr == L1) return fail(MC_EUNSUPPORTED, "soft L1 centers are medians (outside the implemented path)");
+    // the reference's weighted L1 median over CSR rows raises (util/csc.h:835)
+    if (msr == L1 && X->kind != MC_DENSE_F32)
+        return fail(MC_EUNSUPPORTED, "Not implemented: weighted L1 median for CSparseMatrix");
     mc_job *j = nullptr;
     MC_TRY(mc_job_create(ctx, X, centers_in, k, msr, prior, weights, MC_FP32, 1, &j));
     std::unique_ptr<mc_job, int (*)(mc_job *)> guard(j, mc_job_destroy);
@@ -1745,7 +1816,10 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
         MC_TRY(launch_det_sum(in, j->det_tmp.p, j->scal.p, st));
         MC_CUDA_TRY(cudaMemsetAsync(acc_num.p, 0, uint64_t(k) * d * sizeof(double), st));
         MC_CUDA_TRY(cudaMemsetAsync(acc_den.p, 0, uint64_t(k) * sizeof(double), st));
-        for (uint64_t q0 = 0; q0 < nq_all; q0 += batch) {
+        if (msr == L1)
+            k_soft_l1_centers<<<dim3(k, unsigned((d + 31) / 32)), 256, 0, st>>>(j->M.X, n, d, asn.p, k, j->w.p, j->Cw.p),
+                note_launch();
+        for (uint64_t q0 = 0; msr != L1 && q0 < nq_all; q0 += batch) {
             const uint64_t nq = umin64(batch, nq_all - q0), r0 = q0 * kSoftChunk;
             if (csr) {
                 MC_CUDA_TRY(cudaMemsetAsync(sbuf.p, 0, nq * k * d * sizeof(float), st));
@@ -1762,8 +1836,9 @@ int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
                                                                                          acc_num.p, acc_den.p),
                 note_launch();
         }
-        k_soft_center_finalize<<<dim3(unsigned((d + 127) / 128), k), 128, 0, st>>>(acc_num.p, acc_den.p, k, d, j->Cw.p),
-            note_launch();
+        if (msr != L1)
+            k_soft_center_finalize<<<dim3(unsigned((d + 127) / 128), k), 128, 0, st>>>(acc_num.p, acc_den.p, k, d,
+                                                                                       j->Cw.p), note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         MC_TRY(job_assign_with(j, j->Cw.p, j->psum, true, &o));
         MC_CUDA_TRY(cudaMemcpyAsync(&cost, j->scal.p, sizeof(double), cudaMemcpyDeviceToHost, st));

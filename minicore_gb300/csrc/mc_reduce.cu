@@ -9,6 +9,9 @@
 //    649-779): rows bucketed by assignment in ascending order, weighted mean per bucket.
 #include "mc_reduce.cuh"
 
+#include <algorithm>
+#include <vector>
+
 namespace mc {
 
 // ------------------------------------------------------------------------------------
@@ -863,7 +866,8 @@ __global__ void __launch_bounds__(256) k_l1_median_weighted(const float *__restr
                                                             const uint32_t *__restrict__ perm,
                                                             const uint64_t *__restrict__ bstart,
                                                             const uint64_t *__restrict__ bcount,
-                                                            const double *__restrict__ w, float *centers) {
+                                                            const double *__restrict__ w, uint64_t nw_local,
+                                                            float *centers) {
     __shared__ double wmax[8];
     __shared__ uint32_t best[8][32];
     const uint32_t c = blockIdx.x;
@@ -871,8 +875,13 @@ __global__ void __launch_bounds__(256) k_l1_median_weighted(const float *__restr
     const uint64_t m = bcount[c], b = bstart[c];
     if (m == 0) return;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // nw_local > 0: the r-th row of the cluster weighs w[r] (w holds nw_local entries)
+    auto wt = [&](uint64_t r) {
+        if (nw_local) return r < nw_local ? w[r] : -1.7976931348623157e308;
+        return w[perm[b + r]];
+    };
     double mx = -1.7976931348623157e308;
-    for (uint64_t r = t; r < m; r += 256) mx = fmax(mx, w[perm[b + r]]);
+    for (uint64_t r = t; r < m; r += 256) mx = fmax(mx, wt(r));
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (lane == 0) wmax[warp] = mx;
@@ -884,7 +893,7 @@ __global__ void __launch_bounds__(256) k_l1_median_weighted(const float *__restr
     if (col < d)
         for (uint64_t r = warp; r < m; r += 8) {
             const uint32_t row = perm[b + r];
-            if (w[row] == mx) bk = min(bk, f2ord(X[uint64_t(row) * d + col]));
+            if (wt(r) == mx) bk = min(bk, f2ord(X[uint64_t(row) * d + col]));
         }
     best[warp][lane] = bk;
     __syncthreads();
@@ -896,12 +905,12 @@ __global__ void __launch_bounds__(256) k_l1_median_weighted(const float *__restr
 }
 
 int launch_l1_medians(const float *X, uint64_t d, uint32_t k, const SortWork &w, const double *weights,
-                      float *centers, cudaStream_t st) {
+                      float *centers, cudaStream_t st, uint64_t nw_local) {
     if (k == 0 || d == 0) return MC_OK;
     const dim3 g(k, unsigned((d + 31) / 32));
     if (weights) {
         k_l1_median_weighted<<<g, 256, 0, st>>>(X, d, w.perm.p, w.bucket_start.p, w.bucket_count.p, weights,
-                                               centers), note_launch();
+                                               nw_local, centers), note_launch();
     } else {
         const int smem = 2 * 32 * 256 * int(sizeof(uint32_t));
         MC_CUDA_TRY(cudaFuncSetAttribute(k_l1_median_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -930,6 +939,202 @@ int launch_l1_reseed_update(const float *X, uint64_t n, uint64_t d, const float 
     if (n == 0) return MC_OK;
     k_l1_reseed_update<<<unsigned(umin64((n + 255) / 256, 4096)), 256, 0, st>>>(X, n, d, center, id, asn, costs),
         note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// L1 medians over CSR rows
+// ------------------------------------------------------------------------------------
+__global__ void k_l1_reseed_update_csr(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                                       const uint64_t *__restrict__ indptr, uint64_t n, uint64_t d,
+                                       const float *__restrict__ center, uint32_t id, uint32_t *asn, double *costs) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x)) {
+        uint64_t p = indptr[i];
+        const uint64_t pe = indptr[i + 1];
+        float a = 0.f;
+        for (uint64_t j = 0; j < d; ++j) {
+            float x = 0.f;
+            if (p < pe && idx[p] == j) x = vals[p++];
+            a = a + fabsf(center[j] - x);
+        }
+        if (double(a) < costs[i]) {
+            asn[i] = id;
+            costs[i] = double(a);
+        }
+    }
+}
+
+int launch_l1_reseed_update_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n,
+                                uint64_t d, const float *center, uint32_t id, uint32_t *asn, double *costs,
+                                cudaStream_t st) {
+    if (n == 0) return MC_OK;
+    k_l1_reseed_update_csr<<<unsigned(umin64((n + 255) / 256, 4096)), 256, 0, st>>>(vals, idx, indptr, n, d, center,
+                                                                                   id, asn, costs), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+// one warp per row: the row's nonzeros as (cluster << 32 | column, value key), CSR order
+__global__ void k_l1csr_fill(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                             const uint64_t *__restrict__ indptr, uint64_t n, const uint32_t *__restrict__ asn,
+                             uint64_t *key, uint32_t *val) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    for (uint64_t r = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; r < n; r += nw) {
+        const uint64_t hi = uint64_t(asn[r]) << 32, e = indptr[r + 1];
+        for (uint64_t p = indptr[r] + lane; p < e; p += 32) {
+            key[p] = hi | idx[p];
+            val[p] = f2ord(vals[p]);
+        }
+    }
+}
+
+__global__ void k_l1csr_digit(const uint64_t *__restrict__ key, const uint32_t *__restrict__ val, uint64_t m,
+                              int from_key, int shift, uint32_t mask, uint32_t *digit) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < m; i += gridDim.x * uint64_t(blockDim.x))
+        digit[i] = from_key ? uint32_t(key[i] >> shift) & mask : (val[i] >> shift) & mask;
+}
+
+__global__ void k_l1csr_gather(const uint32_t *__restrict__ perm, uint64_t m, const uint64_t *__restrict__ key,
+                               const uint32_t *__restrict__ val, uint64_t *key2, uint32_t *val2) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < m; i += gridDim.x * uint64_t(blockDim.x)) {
+        const uint32_t s = perm[i];
+        key2[i] = key[s];
+        val2[i] = val[s];
+    }
+}
+
+// clusters of two or more rows start from zero (the median writes only the columns that
+// have nonzeros); a cluster of one row takes that row
+__global__ void k_l1csr_init(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                             const uint64_t *__restrict__ indptr, uint64_t d, const uint32_t *__restrict__ perm,
+                             const uint64_t *__restrict__ bstart, const uint64_t *__restrict__ bcount,
+                             float *centers) {
+    const uint32_t c = blockIdx.x;
+    const uint64_t m = bcount[c];
+    if (m == 0) return;  // whole block
+    float *dst = centers + uint64_t(c) * d;
+    for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) dst[j] = 0.f;
+    if (m != 1) return;  // whole block
+    __syncthreads();
+    const uint32_t r = perm[bstart[c]];
+    for (uint64_t p = indptr[r] + threadIdx.x; p < indptr[r + 1]; p += blockDim.x) dst[idx[p]] = vals[p];
+}
+
+// the sparse median of one (cluster, column) run: v = the run's nel value keys, ascending;
+// m = the cluster's rows.  Follows util/csc.h:856-890, including its choices: with more
+// than m/2 nonzeros and m even it averages the sorted positions m/2 and m/2 + 1 (counting
+// the zeros), the all-negative case reads one position past the middle, and an odd m with
+// exactly m/2 nonzeros of one sign gives half the smallest (largest) of them.  Where the
+// reference's position runs past the end of its vector (m = 2, or the all-negative case with
+// nel = m/2 + 1) the last element stands in.
+__device__ float l1csr_median(const uint32_t *__restrict__ v, uint64_t nel, uint64_t m) {
+    const uint64_t h = m / 2;
+    const float front = ord2f(v[0]), back = ord2f(v[nel - 1]);
+    auto nz = [&](uint64_t q) { return ord2f(v[q < nel ? q : nel - 1]); };
+    if (nel > h) {
+        if (front > 0.f || back < 0.f) {
+            const uint64_t t = front > 0.f ? nel + h - m : m - h;
+            return (m & 1) ? nz(t) : 0.5f * (nz(t) + nz(t + 1));
+        }
+        // mixed signs (or stored zeros): the negatives, then m - nel zeros, then the rest
+        uint64_t lo = 0, hi = nel;  // first key >= f2ord(-0.0)
+        while (lo < hi) {
+            const uint64_t mid = (lo + hi) >> 1;
+            if (v[mid] < 0x7fffffffu) lo = mid + 1;
+            else hi = mid;
+        }
+        const uint64_t nneg = lo, z = m - nel;
+        auto full = [&](uint64_t q) {
+            if (q >= m) q = m - 1;
+            return q < nneg ? ord2f(v[q]) : (q < nneg + z ? 0.f : ord2f(v[q - z]));
+        };
+        return (m & 1) ? full(h) : 0.5f * (full(h) + full(h + 1));
+    }
+    if ((m & 1) && nel == h) {
+        if (front > 0.f) return 0.5f * front;
+        if (back < 0.f) return 0.5f * back;
+    }
+    return 0.f;
+}
+
+__global__ void k_l1csr_runs(const uint64_t *__restrict__ key, const uint32_t *__restrict__ val, uint64_t nnz,
+                             uint64_t d, const uint64_t *__restrict__ bcount, float *centers) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < nnz;
+         i += gridDim.x * uint64_t(blockDim.x)) {
+        const uint64_t kk = key[i];
+        if (i > 0 && key[i - 1] == kk) continue;
+        const uint32_t c = uint32_t(kk >> 32);
+        const uint64_t m = bcount[c];
+        if (m < 2) continue;
+        // end of the run: galloping, then bisection (key[lo] == kk, key[hi] != kk or hi == nnz)
+        uint64_t lo = i, hi = i + 1, step = 1;
+        while (hi < nnz && key[hi] == kk) {
+            lo = hi;
+            step <<= 1;
+            hi = lo + step;
+        }
+        if (hi > nnz) hi = nnz;
+        while (hi - lo > 1) {
+            const uint64_t mid = lo + (hi - lo) / 2;
+            if (key[mid] == kk) lo = mid;
+            else hi = mid;
+        }
+        centers[uint64_t(c) * d + uint32_t(kk)] = l1csr_median(val + i, hi - i, m);
+    }
+}
+
+namespace {
+int bit_width(uint64_t x) {  // bits needed for values 0..x
+    int b = 0;
+    while (x >> b) ++b;
+    return b;
+}
+}  // namespace
+
+int launch_l1_medians_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n, uint64_t d,
+                          uint64_t nnz, uint32_t k, const uint32_t *asn, const SortWork &rows, L1CsrWork &w,
+                          float *centers, cudaStream_t st) {
+    if (k == 0 || d == 0) return MC_OK;
+    if (nnz >= (1ull << 32)) return fail(MC_EUNSUPPORTED, "CSR L1 medians take at most 2^32-1 nonzeros");
+    k_l1csr_init<<<k, 256, 0, st>>>(vals, idx, indptr, d, rows.perm.p, rows.bucket_start.p, rows.bucket_count.p,
+                                    centers), note_launch();
+    if (nnz == 0) {
+        MC_CUDA_TRY(cudaGetLastError());
+        return MC_OK;
+    }
+    MC_TRY(w.key.alloc(nnz, st));
+    MC_TRY(w.key2.alloc(nnz, st));
+    MC_TRY(w.val.alloc(nnz, st));
+    MC_TRY(w.val2.alloc(nnz, st));
+    MC_TRY(w.digit.alloc(nnz, st));
+    const unsigned g = unsigned(umin64((nnz + 255) / 256, 152 * 16));
+    k_l1csr_fill<<<unsigned(umin64((n + 7) / 8, 152 * 16)), 256, 0, st>>>(vals, idx, indptr, n, asn, w.key.p,
+                                                                         w.val.p), note_launch();
+    // LSD passes: (from_key, shift, bits), least significant field first
+    struct Pass { int from_key, shift, bits; };
+    std::vector<Pass> passes;
+    auto field = [&](int from_key, int base, int bits) {
+        const int np = (bits + 10) / 11;
+        for (int q = 0, done = 0; q < np; ++q) {
+            const int b = (bits - done + (np - q) - 1) / (np - q);
+            passes.push_back({from_key, base + done, b});
+            done += b;
+        }
+    };
+    field(0, 0, 32);
+    field(1, 0, std::max(1, bit_width(d - 1)));
+    field(1, 32, std::max(1, bit_width(uint64_t(k) - 1)));
+    for (const Pass &p : passes) {
+        k_l1csr_digit<<<g, 256, 0, st>>>(w.key.p, w.val.p, nnz, p.from_key, p.shift, (1u << p.bits) - 1u,
+                                         w.digit.p), note_launch();
+        MC_TRY(launch_sort_by_key(w.digit.p, nullptr, nnz, 1u << p.bits, w.sort, st));
+        k_l1csr_gather<<<g, 256, 0, st>>>(w.sort.perm.p, nnz, w.key.p, w.val.p, w.key2.p, w.val2.p), note_launch();
+        std::swap(w.key.p, w.key2.p), std::swap(w.key.n, w.key2.n);
+        std::swap(w.val.p, w.val2.p), std::swap(w.val.n, w.val2.n);
+    }
+    k_l1csr_runs<<<g, 256, 0, st>>>(w.key.p, w.val.p, nnz, d, rows.bucket_count.p, centers), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }

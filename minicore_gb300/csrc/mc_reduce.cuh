@@ -43,12 +43,33 @@ int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool p
 // (unweighted: odd -> middle, even -> 0.5f * (the two middles)); with weights, per column
 // the value of the row with the largest weight (smallest such value on ties), which is what
 // the reference's weighted_median returns.  Clusters without rows keep their center.
+// nw_local > 0: the r-th row of a cluster (ascending) weighs weights[r], as the minibatch
+// update's weighted_median(rows(data, asp, nasn), ret, *weights) reads them (kmedian.h:335);
+// positions past nw_local take no part.
 int launch_l1_medians(const float *X, uint64_t d, uint32_t k, const SortWork &w, const double *weights,
-                      float *centers, cudaStream_t st);
+                      float *centers, cudaStream_t st, uint64_t nw_local = 0);
 // the L1 restart's pass after reseeding center `id` at `center`: rows whose plain L1
 // distance (sequential float sum of |c - x|) is below their cost move to it
 int launch_l1_reseed_update(const float *X, uint64_t n, uint64_t d, const float *center, uint32_t id,
                             uint32_t *asn, double *costs, cudaStream_t st);
+// L1 centers over CSR rows, unweighted (set_centroids_l1 -> util/csc.h:829-893): every
+// nonzero as ((cluster << 32) | column, value key), sorted by an LSD radix sort (digits of at
+// most 11 bits: the value, then the column, then the cluster); each (cluster, column) run of
+// m_c rows with nel nonzeros then takes the reference's sparse median rule.  Clusters with one
+// row take that row; clusters without rows keep their center.
+struct L1CsrWork {
+    DBuf<uint64_t> key, key2;
+    DBuf<uint32_t> val, val2, digit;
+    SortWork sort;
+};
+int launch_l1_medians_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n, uint64_t d,
+                          uint64_t nnz, uint32_t k, const uint32_t *asn, const SortWork &rows, L1CsrWork &w,
+                          float *centers, cudaStream_t st);
+// launch_l1_reseed_update over CSR rows (the row's zeros take part: sequential float sum of
+// |c_j - x_j| over every column)
+int launch_l1_reseed_update_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n,
+                                uint64_t d, const float *center, uint32_t id, uint32_t *asn, double *costs,
+                                cudaStream_t st);
 int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st);
 int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, float *cnorm, cudaStream_t st);
 

@@ -174,7 +174,8 @@ def kmeanspp(X, k, msr, prior, uniforms_, weights=None):
 
 
 def l1_centers(X, asn, k, weights=None):
-    """The L1 center rule (set_centroids_l1's medians) for a given assignment, dense rows."""
+    """The L1 center rule (set_centroids_l1's medians) for a given assignment, dense or CSR
+    rows (no empty cluster)."""
     M = Matrix(X)
     a = np.ascontiguousarray(asn, dtype=np.uint32)
     w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
@@ -224,6 +225,8 @@ def hcluster(X, centers, msr, prior, weights=None, eps=1e-10, maxiter=100, seed=
                             _p(costs), ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it))
     if rc == 2:
         raise RuntimeError("Unexpected nan in ctr")
+    if rc == 3:
+        raise NotImplementedError("Not implemented: weighted L1 median for CSparseMatrix")
     return dict(initcost=ic.value, finalcost=fc.value, numiter=it.value, centers=cout, asn=asn,
                 costs=costs)
 
@@ -243,6 +246,8 @@ def minibatch(X, centers, msr, prior, weights=None, mbsize=100, maxiter=20, freq
                              ctypes.byref(fc), ctypes.byref(it))
     if rc == 2:
         raise RuntimeError("Unexpected nan in ctr")
+    if rc == 3:
+        raise NotImplementedError("Not implemented: weighted L1 median for CSparseMatrix")
     return dict(initcost=ic.value, finalcost=fc.value, numiter=it.value, centers=cout, asn=asn, costs=costs)
 
 

@@ -747,8 +747,9 @@ int orc_kmeanspp(const orc_matrix *mm, uint32_t k, int msr, double prior, const 
 }
 
 // perform_hard_clustering (solve.h:98-175) from explicit dense centers.
-// Returns 0 on success, 2 if a NaN center appeared.
-// L1 centers: set_centroids_l1 (clustering/centroid.h:435-504), dense rows.  Empty clusters
+// Returns 0 on success, 2 if a NaN center appeared, 3 for weighted L1 over CSR rows.
+// L1 centers: set_centroids_l1 (clustering/centroid.h:435-504), dense rows (CSR rows: the
+// sparse rule of l1_sparse_median below, a one-row cluster takes its row).  Empty clusters
 // are reseeded one at a time (D^2 draw over the current costs, U(seed, r) with the restart
 // counter), each followed by a pass that moves every row whose plain L1 distance to the new
 // center (sequential float sum of |c - x|) is below its cost; repeated while clusters are
@@ -763,7 +764,49 @@ inline float l1_plain(const float *c, const float *x, uint64_t d) {
     return a;
 }
 
-int set_centroids_l1_dense(const Mat &m, std::vector<uint32_t> &asn, std::vector<double> &costs, CenterSet &C,
+// l1_median over CSR rows, unweighted (util/csc.h:829-893), for the rows `rows` (nrows of
+// them): per column the sorted nonzeros v (nel of them), h = nrows / 2, and
+//   nel > h, all positive:  t = h - (nrows - nel); odd -> v[t], even -> 0.5f (v[t] + v[t+1])
+//   nel > h, all negative:  t = nrows - h;          odd -> v[t], even -> 0.5f (v[t] + v[t+1])
+//   nel > h, otherwise:     f = v and nrows - nel zeros, sorted; odd -> f[h], even ->
+//                           0.5f (f[h] + f[h+1])
+//   nrows odd, nel == h:    0.5f * v.front() if positive, 0.5f * v.back() if negative
+//   else 0.
+// A position past the end of its vector (where the reference reads out of bounds: nrows =
+// 2, or all negative with nel = h + 1) takes the last element.
+void l1_sparse_median(const Mat &m, const std::vector<uint64_t> &rows, std::vector<float> &out) {
+    const uint64_t nrows = rows.size(), h = nrows / 2;
+    std::map<uint32_t, std::vector<float>> feats;
+    for (uint64_t r : rows)
+        for (uint64_t p = m.indptr[r]; p < m.indptr[r + 1]; ++p) feats[m.idx[p]].push_back(m.vals[p]);
+    out.assign(m.d, 0.f);
+    auto at = [](const std::vector<float> &a, uint64_t q) { return a[std::min<uint64_t>(q, a.size() - 1)]; };
+    for (auto &kv : feats) {
+        std::vector<float> &v = kv.second;
+        std::sort(v.begin(), v.end());
+        const uint64_t nel = v.size();
+        float r = 0.f;
+        if (nel > h) {
+            if (v.front() > 0.f || v.back() < 0.f) {
+                const uint64_t t = v.front() > 0.f ? h - (nrows - nel) : nrows - h;
+                r = (nrows & 1) ? at(v, t) : 0.5f * (at(v, t) + at(v, t + 1));
+            } else {
+                std::vector<float> f = v;
+                f.resize(nrows, 0.f);
+                std::sort(f.begin(), f.end());
+                r = (nrows & 1) ? f[h] : 0.5f * (at(f, h) + at(f, h + 1));
+            }
+        } else if ((nrows & 1) && nel == h) {
+            if (v.front() > 0.f) r = 0.5f * v.front();
+            else if (v.back() < 0.f) r = 0.5f * v.back();
+        }
+        out[kv.first] = r;
+    }
+}
+
+// set_centroids_l1 over dense or CSR rows; CSR rows with weights raise in the reference
+// (util/csc.h:835): returns -3 then
+int set_centroids_l1(const Mat &m, std::vector<uint32_t> &asn, std::vector<double> &costs, CenterSet &C,
                            const double *w, uint64_t seed, uint64_t &restart_counter) {
     const uint64_t n = m.n, k = C.k, d = m.d;
     std::vector<std::vector<uint64_t>> assigned(k);
@@ -780,16 +823,28 @@ int set_centroids_l1_dense(const Mat &m, std::vector<uint32_t> &asn, std::vector
             const double u = uniform_at(seed, restart_counter++);
             uint64_t r = det_draw([&](uint64_t i) { return costs[i]; }, n, u);
             if (r >= n) r = 0;
-            C.set_row(id, dense_row(m, r), false);
+            const bool sparse = m.kind == 1;
+            C.set_row(id, dense_row(m, r), sparse);
             const float *cr = &C.dense[uint64_t(id) * d];
             for (uint64_t i = 0; i < n; ++i) {
-                const double c = l1_plain(cr, m.vals + i * d, d);
+                const double c = sparse ? l1_plain(cr, dense_row(m, i).data(), d) : l1_plain(cr, m.vals + i * d, d);
                 if (c < costs[i]) { asn[i] = id; costs[i] = c; }
             }
         }
         rebuild(empty);
     }
     std::vector<float> col, out(d);
+    if (m.kind == 1) {
+        if (w) return -3;
+        for (uint32_t c = 0; c < k; ++c) {
+            if (assigned[c].size() == 1) C.set_row(c, dense_row(m, assigned[c][0]), true);
+            else {
+                l1_sparse_median(m, assigned[c], out);
+                C.set_row(c, out, true);
+            }
+        }
+        return 0;
+    }
     for (uint32_t c = 0; c < k; ++c) {
         const auto &rows = assigned[c];  // ascending
         const uint64_t mc = rows.size();
@@ -819,18 +874,17 @@ int set_centroids_l1_dense(const Mat &m, std::vector<uint32_t> &asn, std::vector
 // the L1 center rule alone (no empty cluster allowed): centers_out[k][d]
 int orc_l1_centers(const orc_matrix *mm, const uint32_t *asn_in, uint32_t k, const double *w, float *centers_out) {
     const Mat m = to_mat(mm);
-    if (m.kind != 0) return 1;
     std::vector<uint32_t> asn(asn_in, asn_in + m.n);
     std::vector<double> costs(m.n, 0.0);
     CenterSet C;
     std::vector<float> zero(uint64_t(k) * m.d, 0.f);
-    C.set_from_dense(zero.data(), k, m.d, false);
+    C.set_from_dense(zero.data(), k, m.d, m.kind == 1);
     uint64_t rc = 0;
     for (uint64_t i = 0; i < m.n; ++i) if (asn[i] >= k) return 2;
     std::vector<uint64_t> cnt(k, 0);
     for (uint64_t i = 0; i < m.n; ++i) ++cnt[asn[i]];
     for (uint32_t c = 0; c < k; ++c) if (!cnt[c]) return 3;
-    set_centroids_l1_dense(m, asn, costs, C, w, 0, rc);
+    if (set_centroids_l1(m, asn, costs, C, w, 0, rc) == -3) return 4;
     std::copy(C.dense.begin(), C.dense.end(), centers_out);
     return 0;
 }
@@ -859,11 +913,10 @@ int orc_hcluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
     } else {
         cpy = centers;
         for (;;) {
-            // L1 over dense rows takes coordinate-wise medians (centroid.h:203, 487-504); the
-            // CSR L1 median (util/csc.h:829-893) is not restated: CSR L1 keeps the weighted mean
-            int res = (msr == L1 && !sparse)
-                          ? set_centroids_l1_dense(m, asn, costs, cpy, w, seed, restart_counter)
-                          : set_centroids_full_mean(m, msr, prior, asn, costs, cpy, w, rs, seed, restart_counter);
+            // L1 takes coordinate-wise medians (centroid.h:203, 487-504; util/csc.h:829-893)
+            int res = msr == L1 ? set_centroids_l1(m, asn, costs, cpy, w, seed, restart_counter)
+                                : set_centroids_full_mean(m, msr, prior, asn, costs, cpy, w, rs, seed, restart_counter);
+            if (res == -3) { rc = 3; break; }
             if (res < 0) { rc = 2; break; }
             assign_all(m, cpy, msr, prior, psum, rs, asn.data(), costs.data());
             const float newcost = compute_cost(costs.data(), w, n);
@@ -979,7 +1032,37 @@ int orc_minibatch(const orc_matrix *mm, const float *centers_in, uint32_t k, int
             groups[bc].push_back(r);
         }
         std::vector<float> out(d);
-        for (uint32_t c = 0; c < k; ++c) {
+        for (uint32_t c = 0; msr == L1 && c < k; ++c) {
+            // l1_median of the group (solve.h:559-561): CSR rows by the sparse rule (weights
+            // raise); dense rows by the sorted median, or with weights by weighted_median over
+            // rows(data, asp, nasn) reading the FULL weight vector at the group position q
+            // (kmedian.h:329-344): largest w[q], smallest value among its ties
+            const auto &g = groups[c];
+            if (g.empty()) continue;
+            if (sparse) {
+                if (w) return 3;
+                l1_sparse_median(m, g, out);
+            } else if (w) {
+                double mx = -std::numeric_limits<double>::max();
+                for (uint64_t q = 0; q < g.size() && q < n; ++q) mx = std::max(mx, w[q]);
+                for (uint64_t j = 0; j < d; ++j) {
+                    float b = std::numeric_limits<float>::infinity();
+                    for (uint64_t q = 0; q < g.size() && q < n; ++q)
+                        if (w[q] == mx) b = std::min(b, m.vals[g[q] * d + j]);
+                    out[j] = b;
+                }
+            } else {
+                std::vector<float> col(g.size());
+                for (uint64_t j = 0; j < d; ++j) {
+                    for (uint64_t q = 0; q < g.size(); ++q) col[q] = m.vals[g[q] * d + j];
+                    std::sort(col.begin(), col.end());
+                    const uint64_t hh = g.size() / 2;
+                    out[j] = (g.size() & 1) ? col[hh] : 0.5f * (col[hh - 1] + col[hh]);
+                }
+            }
+            C.set_row(c, out, sparse);
+        }
+        for (uint32_t c = 0; msr != L1 && c < k; ++c) {
             const auto &g = groups[c];
             if (g.empty()) continue;
             if (g.size() == 1) { C.set_row(c, dense_row(m, g[0]), sparse); continue; }
@@ -1009,6 +1092,8 @@ int orc_scluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
     const Mat m = to_mat(mm);
     const uint64_t n = m.n, d = m.d;
     const bool sparse = m.kind == 1;
+    // a weighted L1 median over CSR rows raises in the reference (util/csc.h:835)
+    if (sparse && msr == L1) return -2;
     // CSR rows: the soft means read a dense copy (a zero adds exactly nothing to the
     // compensated sums, so this is the per-nonzero accumulation of the device path)
     std::vector<float> dense_all;
@@ -1061,7 +1146,19 @@ int orc_scluster(const orc_matrix *mm, const float *centers_in, uint32_t k, int 
         cost = w ? det_sum([&](uint64_t i) { return rowval[i] * w[i]; }, n)
                  : det_sum([&](uint64_t i) { return rowval[i]; }, n);
         std::vector<float> nc(uint64_t(k) * d);
-        for (uint32_t c = 0; c < k; ++c) {
+        // L1 (dense): weighted_median with the soft assignments as weights returns, per
+        // column, the smallest value among the rows of largest weight (centroid.h:815-838)
+        for (uint32_t c = 0; msr == L1 && c < k; ++c) {
+            double mx = -std::numeric_limits<double>::max();
+            for (uint64_t r = 0; r < n; ++r) mx = std::max(mx, (w ? w[r] : 1.0) * double(asn[r * k + c]));
+            for (uint64_t j = 0; j < d; ++j) {
+                float b = std::numeric_limits<float>::infinity();
+                for (uint64_t r = 0; r < n; ++r)
+                    if ((w ? w[r] : 1.0) * double(asn[r * k + c]) == mx) b = std::min(b, xv[r * d + j]);
+                nc[uint64_t(c) * d + j] = b;
+            }
+        }
+        for (uint32_t c = 0; msr != L1 && c < k; ++c) {
             for (uint64_t j = 0; j < d; ++j) {
                 double num = 0.0, den = 0.0;
                 for (uint64_t r0 = 0; r0 < n; r0 += 256) {

@@ -99,3 +99,33 @@ def test_coreset_minibatch_matches_oracle(mc, orc, msr, weighted, precision):
     assert np.array_equal(res["asn"], asn)
     assert np.array_equal(res["costs"], costs.astype(np.float32))
     assert np.array_equal(res["centers"], best)
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_minibatch_dense_l1_medians(mc, orc, weighted):
+    """L1 minibatch: each hit center becomes the l1_median of its sampled rows (solve.h:559-561);
+    with weights, weighted_median over rows(data, asp, nasn) reads the full weight vector at
+    the group position (kmedian.h:329-344)."""
+    X = _mixture(3000, 10, 6, seed=8)
+    C0 = X[:6].copy()
+    w = np.random.default_rng(4).integers(1, 5, 3000).astype(np.float64) if weighted else None
+    g = mc.hcluster(X, C0, msr=0, weights=w, mbsize=301, maxiter=12, ncheckins=3, reseed_count=1, seed=6)
+    o = orc.minibatch(X, C0, 0, 0.0, weights=w, mbsize=301, maxiter=12, freq=4, reseed_after=1, seed=6)
+    _same(g, o)
+
+
+def test_minibatch_csr_l1_medians(mc, orc):
+    rng = np.random.default_rng(12)
+    M = sp.random(2000, 90, density=0.1, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.integers(1, 6, s).astype(np.float32)).astype(np.float32)
+    M.sort_indices()
+    ids = np.arange(0, 2000, 250)
+    C0 = np.asarray(M[ids].toarray(), np.float32)
+    g = mc.hcluster(M, ids, msr=0, mbsize=400, maxiter=10, ncheckins=2, reseed_count=1, seed=3)
+    o = orc.minibatch(M, C0, 0, 0.0, mbsize=400, maxiter=10, freq=5, reseed_after=1, seed=3)
+    assert g["numiter"] == o["numiter"]
+    assert g["finalcost"] == o["finalcost"]
+    assert np.array_equal(g["asn"], o["asn"])
+    (data, idx, indptr), shape = g["centers"]
+    Cg = sp.csr_matrix((data, idx.astype(np.int64), indptr.astype(np.int64)), shape=tuple(shape)).toarray()
+    assert np.array_equal(Cg, o["centers"])

@@ -400,3 +400,74 @@ def test_det_sums_match(mc, orc):
     c = j.cost()
     _, ocosts = orc.assign(X, C, 2, 0.0)
     assert c == float(np.float32(orc.det_sum(ocosts)))
+
+
+def _signed_sparse(n, d, density, seed, lo=-3, hi=4):
+    rng = np.random.default_rng(seed)
+    M = sp.random(n, d, density=density, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.integers(lo, hi, s).astype(np.float32))
+    M.sort_indices()
+    return M.astype(np.float32)
+
+
+def _dense_centers(res):
+    (data, idx, indptr), shape = res["centers"]
+    return sp.csr_matrix((data, idx.astype(np.int64), indptr.astype(np.int64)), shape=tuple(shape)).toarray()
+
+
+@pytest.mark.parametrize("signed", [False, True])
+def test_hcluster_csr_l1_medians(mc, orc, signed):
+    """L1 over CSR rows: the sparse median rule (util/csc.h:829-893) on the device (radix
+    sort of the nonzeros by cluster, column and value), bit-exact against the oracle: positive
+    counts, and signed values with stored zeros (every branch of the rule)."""
+    X = _signed_sparse(1200, 60, 0.25, seed=11) if signed else _counts(1500, 80, 0.1, seed=12)
+    ids = np.random.default_rng(4).choice(X.shape[0], 9, replace=False)
+    C0 = np.asarray(X[ids].toarray(), np.float32)
+    res = mc.hcluster(X, ids, msr=0, prior=0.0, eps=0.0, maxiter=5, seed=2)
+    ores = orc.hcluster(X, C0, 0, 0.0, eps=0.0, maxiter=5, seed=2)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(_dense_centers(res), ores["centers"])
+    assert res["finalcost"] == ores["finalcost"]
+
+
+def test_csr_l1_median_one_update_small_clusters(mc, orc):
+    """One L1 update over CSR rows from a known assignment, with clusters of 1, 2, 3, 4 and
+    more rows (the one-row copy, the m = 2 end-of-vector position, odd/even rules)."""
+    X = _signed_sparse(400, 50, 0.3, seed=21, lo=-2, hi=5)
+    rng = np.random.default_rng(6)
+    ids = rng.choice(400, 40, replace=False)  # many centers -> small clusters
+    C0 = np.asarray(X[ids].toarray(), np.float32)
+    a0, _ = orc.assign(X, C0, 0, 0.0)
+    sizes = np.bincount(a0, minlength=40)
+    assert (sizes == 1).any() and (sizes == 2).any()
+    one = mc.hcluster(X, ids, msr=0, prior=0.0, eps=0.0, maxiter=0, seed=9)
+    ref = orc.l1_centers(X, a0, 40) if (sizes > 0).all() else None
+    if one["numiter"] == 1 and ref is not None:
+        assert np.array_equal(_dense_centers(one), ref)
+    ores = orc.hcluster(X, C0, 0, 0.0, eps=0.0, maxiter=0, seed=9)
+    assert one["numiter"] == ores["numiter"]
+    assert np.array_equal(_dense_centers(one), ores["centers"])
+
+
+def test_hcluster_csr_l1_weighted_raises(mc):
+    X = _counts(300, 40, 0.2, seed=3)
+    with pytest.raises(Exception, match="weighted L1 median"):
+        mc.hcluster(X, np.arange(4), msr=0, weights=np.ones(300), maxiter=3)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_csr_l1_loop_modes_agree(mc, orc, mode):
+    """The CSR median inside the fused loop and the CUDA-graph loop gives the host loop's
+    result."""
+    X = _counts(2000, 120, 0.08, seed=31)
+    ids = np.arange(0, 2000, 200)
+    mc.loop_mode(mode)
+    try:
+        res = mc.hcluster(X, ids, msr=0, prior=0.0, eps=0.0, maxiter=20, seed=5)
+    finally:
+        mc.loop_mode(mc.LOOP_AUTO)
+    ores = orc.hcluster(X, np.asarray(X[ids].toarray(), np.float32), 0, 0.0, eps=0.0, maxiter=20, seed=5)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(_dense_centers(res), ores["centers"])

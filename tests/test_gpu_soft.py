@@ -68,3 +68,31 @@ def test_scluster_csr_matches_oracle(mc, orc, msr, prior, temp, weighted):
     Cg = sp.csr_matrix((data, idx.astype(np.int64), indptr.astype(np.int64)), shape=tuple(shape)).toarray()
     np.testing.assert_allclose(Cg, o["centers"], rtol=1e-4, atol=1e-5)
     np.testing.assert_allclose(g["asn"], o["asn"], atol=1e-4)
+
+
+@pytest.mark.parametrize("temp", [0.3, 4.0])
+@pytest.mark.parametrize("weighted", [False, True])
+def test_scluster_l1_matches_oracle(mc, orc, temp, weighted):
+    """L1 soft centers: weighted_median with the soft assignments (times the row weights) as
+    weights keeps, per column, the smallest value among the rows of largest weight
+    (centroid.h:815-838, kmedian.h:266-297).  Centers are copied values, so they match
+    exactly whenever the soft assignments pick the same rows."""
+    X = _mixture(2000, 12, 5, seed=40 + int(temp), nonneg=False)
+    C0 = X[:5].copy()
+    w = np.random.default_rng(9).uniform(0.5, 2.0, len(X)) if weighted else None
+    g = mc.scluster(X, C0, msr=0, temp=temp, maxiter=5, weights=w)
+    o = orc.scluster(X, C0, 0, 0.0, weights=w, temp=temp, maxiter=5)
+    assert g["numiter"] == o["numiter"]
+    np.testing.assert_allclose(g["finalcost"], o["finalcost"], rtol=1e-5)
+    np.testing.assert_array_equal(g["centers"], o["centers"])
+    np.testing.assert_allclose(g["asn"], o["asn"], atol=1e-5)
+    # every center coordinate is a value of the matrix's column
+    for c in g["centers"]:
+        assert all(np.any(X[:, j] == c[j]) for j in range(X.shape[1]))
+
+
+def test_scluster_l1_csr_raises(mc):
+    import scipy.sparse as sp
+    X = sp.random(200, 30, density=0.2, format="csr", random_state=1, dtype=np.float32)
+    with pytest.raises(Exception, match="weighted L1 median"):
+        mc.scluster(X, X[:3].toarray(), msr=0, temp=1.0, maxiter=2)

@@ -259,3 +259,61 @@ def test_oracle_l1_centers_are_medians(orc):
         top = sel & (w == w[sel].max())
         assert np.array_equal(cw[c], X[top].min(axis=0))
         assert np.array_equal(cu[c], r["centers"][c])
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_oracle_soft_l1_centers_rule(orc, weighted):
+    """One soft L1 iteration: each center coordinate is the smallest column value among the
+    rows whose soft weight (asn column times the row weight) is largest, the result of
+    kmedian.h:266-297 (weighted_median with wsum never accumulated)."""
+    rng = np.random.default_rng(5)
+    X = rng.normal(size=(300, 6)).astype(np.float32)
+    C0 = X[:3].copy()
+    w = rng.uniform(0.5, 2.0, 300) if weighted else None
+    r = orc.scluster(X, C0, 0, 0.0, weights=w, temp=0.7, maxiter=1)
+    asn = r["asn"].astype(np.float64)
+    for c in range(3):
+        cw = asn[:, c] * (w if weighted else 1.0)
+        rows = cw == cw.max()
+        np.testing.assert_array_equal(r["centers"][c], X[rows].min(axis=0))
+    with pytest.raises(ValueError):
+        orc.scluster(sp.random(50, 6, density=0.3, format="csr", random_state=1, dtype=np.float32),
+                     C0, 0, 0.0, temp=1.0, maxiter=1)
+
+
+# (rows in the cluster, nonzeros of column 0, expected center value) read off the sparse
+# median of util/csc.h:856-890: h = rows // 2; with more than h nonzeros of one sign the
+# positive case counts the zeros first (t = h - (rows - nel)) and the negative case reads
+# position rows - h; an even count averages positions t and t + 1; mixed signs sort the zeros
+# in; an odd count with exactly h nonzeros of one sign gives half the extreme one.
+SPARSE_MEDIAN_CASES = [
+    (5, [3, 1, 2], 1.0),          # zeros, zeros, 1, 2, 3 -> 1
+    (4, [1, 2, 3, 4], 3.5),       # positions 2 and 3
+    (4, [5, 7, 9], 8.0),          # t = 1 -> (7 + 9) / 2
+    (5, [4, 6], 2.0),             # nel == h, odd: half the smallest
+    (5, [-4, -6], -2.0),          # nel == h, odd: half the largest
+    (5, [-1, 2], 0.0),            # nel == h, mixed signs
+    (3, [-3, -1, -2], -1.0),      # all negative, odd: position rows - h = 2
+    (4, [-1, 3, 2], 2.5),         # mixed: -1 0 2 3 -> positions 2, 3
+    (5, [1], 0.0),                # too few nonzeros
+    (2, [1, 3], 3.0),             # position 2 runs past the end: the last element
+    (6, [2, 2, 2, 2, 9], 2.0),    # t = 3 - 1 = 2 -> (2 + 2) / 2
+    (7, [-5, -4, -3, -2, -1], -1.0),  # all negative, odd: position 7 - 3 = 4 (not -2)
+]
+
+
+@pytest.mark.parametrize("nrows,vals,expected", SPARSE_MEDIAN_CASES)
+def test_oracle_sparse_l1_median_rule(orc, nrows, vals, expected):
+    X = np.zeros((nrows, 3), np.float32)
+    X[:len(vals), 0] = vals
+    X[:, 2] = 1.0  # a column with every row equal
+    S = sp.csr_matrix(X)
+    c = orc.l1_centers(S, np.zeros(nrows, np.uint32), 1)
+    assert c[0, 0] == np.float32(expected)
+    assert c[0, 1] == 0.0 and c[0, 2] == 1.0
+
+
+def test_oracle_sparse_l1_weighted_raises(orc):
+    S = sp.csr_matrix(np.eye(4, dtype=np.float32))
+    with pytest.raises(ValueError):
+        orc.l1_centers(S, np.zeros(4, np.uint32), 1, weights=np.ones(4))
