@@ -43,8 +43,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "serving", "coreset", "pcmp", "minibatch",
-                                                         "soft", "small", "coreset_mb"],
+    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "csr_l1", "serving", "coreset", "pcmp",
+                                                         "minibatch", "soft", "small", "coreset_mb"],
                     help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
                          "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass; serving: "
                          "the Poisson job stream through the continuous-batching server; coreset: the "
@@ -114,7 +114,8 @@ def make_csr_counts(n, d=20_000, nnz_row=1500, seed=0, chunk=4096):
 
 def csr_bench(args):
     """Sparse count workload: D^2 seeding (k=50) then the timed assignment pass (MKL or JSD,
-    prior 1) with rows resident in HBM."""
+    prior 1) with rows resident in HBM; csr_l1: the timed step is one L1 Lloyd iteration
+    (sparse coordinate-wise medians of the clusters, then the L1 assignment pass)."""
     import torch
     import minicore_gb300 as mc
     from minicore_gb300 import _lib
@@ -124,7 +125,8 @@ def csr_bench(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     n, d, k = args.csr_rows, 20_000, 50
-    msr = 5 if args.workload == "csr_mkl" else 4
+    msr = {"csr_mkl": 5, "csr_jsd": 4, "csr_l1": 0}[args.workload]
+    prior = 0.0 if msr == 0 else 1.0
     vals, idx, indptr = make_csr_counts(n, d, seed=0)
     torch.cuda.synchronize()
     A = mc.CSparseMatrix(data=vals, indices=idx, indptr=indptr, shape=(n, d))
@@ -136,7 +138,7 @@ def csr_bench(args):
     costs = torch.empty(n, dtype=torch.float64, device="cuda")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    _lib.check(lib.mc_kmeanspp(ctx.handle, M.ref, k, msr, 1.0, None, mc._p(u), mc._p(ids), mc._p(asn),
+    _lib.check(lib.mc_kmeanspp(ctx.handle, M.ref, k, msr, prior, None, mc._p(u), mc._p(ids), mc._p(asn),
                                mc._p(costs)))
     e1.record(stream)
     torch.cuda.synchronize()
@@ -146,39 +148,78 @@ def csr_bench(args):
     for c, r in enumerate(ids.cpu().tolist()):
         b, e = int(ipc[r]), int(ipc[r + 1])
         C[c, idx[b:e].long()] = vals[b:e]
-    job = mc.Job(A, C, msr=msr, prior=1.0, ctx=ctx)
+    job = mc.Job(A, C, msr=msr, prior=prior, ctx=ctx)
+    step = job.lloyd_step if msr == 0 else job.assign
+    job.assign()
     for _ in range(args.warmup):
-        job.assign()
+        step()
     torch.cuda.synchronize()
     lib.mc_profile_reset()
     lib.mc_profile_enable(1)
+    l0 = lib.mc_kernel_launches()
     e0.record(stream)
     for _ in range(args.steps):
-        job.assign()
+        step()
     e1.record(stream)
     torch.cuda.synchronize()
     lib.mc_profile_enable(0)
     buf = ctypes.create_string_buffer(1 << 16)
     _lib.check(lib.mc_profile_report(buf, len(buf)))
     phases = json.loads(buf.value.decode())
+    launches = int(lib.mc_kernel_launches() - l0)
     ms = e0.elapsed_time(e1) / args.steps
     nnz = n * 1500
     algo_bytes = nnz * 8 + (n + 1) * 8 + n * 8 + n * 12 + k * d * 4
     pk, pk_kind = peaks()
     kern = phases.get("assign_csr_sparse") or phases.get("assign_csr_tiled") or {}
     kms = kern.get("ms", float("nan")) / max(kern.get("count", 1), 1)
-    out = {"metric": f"CSR {'MKL' if msr == 5 else 'JSD'} assignment passes/s 1Mx20000 k=50",
-           "value": 1000.0 / ms, "unit": "passes/s", "ms_per_pass": ms, "steps": args.steps,
-           "warmup": args.warmup, "dtype": "f32", "data": "synthetic",
+    name = {5: "MKL", 4: "JSD", 0: "L1"}[msr]
+    rows_tag = f"{n // 1_000_000}M" if n % 1_000_000 == 0 else f"{n // 1000}k"
+    metric = (f"CSR L1 Lloyd iterations/s {rows_tag}x20000 k=50" if msr == 0
+              else f"CSR {name} assignment passes/s {rows_tag}x20000 k=50")
+    unit = "iters/s" if msr == 0 else "passes/s"
+    out = {"metric": metric, "value": 1000.0 / ms, "unit": unit, "ms_per_pass": ms, "steps": args.steps,
+           "warmup": args.warmup, "dtype": "f32", "data": "synthetic", "gpu_launches": launches,
            "config": {"workload": f"CSR {n}x{d}, 1500 nnz/row Zipf(1.1) columns, NB(3,0.5) counts, "
-                                  f"msr={msr}, prior=1, k={k}, kmeans++ centers"},
+                                  f"msr={msr}, prior={prior:g}, k={k}, kmeans++ centers"},
            "kmeanspp_ms": kmpp_ms,
            "roofline": {"bound": "hbm" if msr == 5 else "compute", "achieved": algo_bytes / (kms * 1e-3) / 1e9,
                         "peak": pk.get("hbm_gbs", 6767.7), "unit": "GB/s",
                         "frac": algo_bytes / (kms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6767.7),
                         "algorithmic_bytes": algo_bytes, "kernel_ms": kms, "peak_source": pk_kind},
            "phases_ms": phases}
-    if not args.no_cpu:
+    if msr == 0:
+        # the median phase: algorithmic bytes = the nonzeros (values + indices), the row
+        # pointers and assignments, and the k x d centers written
+        # centroid_update: the counting sort of the rows by cluster and the medians, per step
+        med = phases.get("centroid_update", {})
+        med_ms = med.get("ms", float("nan")) / args.steps
+        med_bytes = nnz * 8 + (n + 1) * 8 + n * 4 + k * d * 4
+        out["l1_median_roofline"] = {"bound": "hbm", "achieved": med_bytes / (med_ms * 1e-3) / 1e9,
+                                     "peak": pk.get("hbm_gbs", 6767.7), "unit": "GB/s",
+                                     "frac": med_bytes / (med_ms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6767.7),
+                                     "algorithmic_bytes": med_bytes, "phase_ms": med_ms, "peak_source": pk_kind}
+    if not args.no_cpu and msr == 0:
+        # the oracle's assignment and sparse medians of the first S rows, scaled to n rows
+        import scipy.sparse as sp
+        import oracle
+        S = 20000
+        ipc_s = ipc[:S + 1].numpy().astype(np.int64)
+        sub = sp.csr_matrix((vals[:int(ipc_s[-1])].cpu().numpy(), idx[:int(ipc_s[-1])].cpu().numpy().astype(np.int64),
+                             ipc_s), shape=(S, d))
+        Ch = C.cpu().numpy()
+        t0 = time.perf_counter()
+        a_s, _ = oracle.assign(sub, Ch, 0, 0.0)
+        present = np.unique(a_s)
+        remap = np.zeros(k, np.uint32)
+        remap[present] = np.arange(present.size, dtype=np.uint32)
+        oracle.l1_centers(sub, remap[a_s], int(present.size))
+        cpu_s = (time.perf_counter() - t0) * (n / S)
+        out["cpu_baseline"] = {"value": 1.0 / cpu_s, "unit": "iters/s", "cores": os.cpu_count() or 1,
+                               "kind": "port",
+                               "sample": f"oracle L1 assignment + sparse medians of the first {S} rows "
+                                         f"(clusters present in the sample), scaled by {n}/{S}"}
+    elif not args.no_cpu:
         # the oracle (CPU restatement, 16-thread OpenMP union walk of the reference's sparse
         # measures) on the first rows of the same matrix and centers, scaled to all n rows
         import scipy.sparse as sp

@@ -10,6 +10,7 @@
 #include "mc_reduce.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 namespace mc {
@@ -458,20 +459,21 @@ __global__ void __launch_bounds__(256) k_scan_tile_write(const uint64_t *__restr
     }
 }
 
-int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st) {
+int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st, DBuf<uint64_t> *scratch) {
     if (m <= 16 * 1024) {  // one CTA
         k_exclusive_scan_u64<<<1, 1024, 0, st>>>(in, out, m), note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         return MC_OK;
     }
     const uint64_t nt = (m + kScanTile - 1) / kScanTile;
-    DBuf<uint64_t> tsum, toff;  // freed in stream order
-    MC_TRY(tsum.alloc(nt, st));
-    MC_TRY(toff.alloc(nt + 1, st));
-    k_scan_tile_sums<<<unsigned(nt), 256, 0, st>>>(in, m, tsum.p), note_launch();
-    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(tsum.p, toff.p, nt), note_launch();
-    k_scan_tile_write<<<unsigned(nt), 256, 0, st>>>(in, m, toff.p, out), note_launch();
-    MC_CUDA_TRY(cudaMemcpyAsync(out + m, toff.p + nt, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+    DBuf<uint64_t> own;  // freed in stream order
+    DBuf<uint64_t> &buf = scratch ? *scratch : own;
+    MC_TRY(buf.alloc(2 * nt + 1, st));
+    uint64_t *tsum = buf.p, *toff = buf.p + nt;
+    k_scan_tile_sums<<<unsigned(nt), 256, 0, st>>>(in, m, tsum), note_launch();
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(tsum, toff, nt), note_launch();
+    k_scan_tile_write<<<unsigned(nt), 256, 0, st>>>(in, m, toff, out), note_launch();
+    MC_CUDA_TRY(cudaMemcpyAsync(out + m, toff + nt, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }
@@ -1085,6 +1087,153 @@ __global__ void k_l1csr_runs(const uint64_t *__restrict__ key, const uint32_t *_
     }
 }
 
+// Bucket path (k * d <= kL1BucketMax): the nonzeros of clusters with two or more rows are
+// counted per (cluster, column) bucket, the counts scanned to offsets, and the value keys
+// scattered into their bucket with atomic cursors (order within a bucket is irrelevant: only
+// order statistics are read).  Buckets that need one (more than m/2 nonzeros, or an odd m
+// with exactly m/2) are listed, and one CTA per listed bucket takes the minimum, maximum and
+// negative count, then a 4-pass radix select of the (at most two) ranks the rule reads.
+constexpr uint64_t kL1BucketMax = 1ull << 28;
+
+__global__ void k_l1b_count(const uint32_t *__restrict__ idx, const uint64_t *__restrict__ indptr, uint64_t n,
+                            uint64_t d, const uint32_t *__restrict__ asn, const uint64_t *__restrict__ bcount,
+                            unsigned long long *cnt) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    for (uint64_t r = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; r < n; r += nw) {
+        const uint32_t c = asn[r];
+        if (bcount[c] < 2) continue;
+        const uint64_t base = uint64_t(c) * d, e = indptr[r + 1];
+        for (uint64_t p = indptr[r] + lane; p < e; p += 32) atomicAdd(&cnt[base + idx[p]], 1ull);
+    }
+}
+
+__global__ void k_l1b_scatter(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                              const uint64_t *__restrict__ indptr, uint64_t n, uint64_t d,
+                              const uint32_t *__restrict__ asn, const uint64_t *__restrict__ bcount,
+                              unsigned long long *cur, uint32_t *keys) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    for (uint64_t r = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; r < n; r += nw) {
+        const uint32_t c = asn[r];
+        if (bcount[c] < 2) continue;
+        const uint64_t base = uint64_t(c) * d, e = indptr[r + 1];
+        for (uint64_t p = indptr[r] + lane; p < e; p += 32) keys[atomicAdd(&cur[base + idx[p]], 1ull)] = f2ord(vals[p]);
+    }
+}
+
+__global__ void k_l1b_list(const unsigned long long *__restrict__ cnt, uint64_t nb, uint64_t d,
+                           const uint64_t *__restrict__ bcount, unsigned long long *nrun, uint64_t *runs) {
+    for (uint64_t b = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; b < nb; b += gridDim.x * uint64_t(blockDim.x)) {
+        const uint64_t nel = cnt[b];
+        if (!nel) continue;
+        const uint64_t m = bcount[b / d], h = m / 2;
+        if (m >= 2 && (nel > h || ((m & 1) && nel == h))) runs[atomicAdd(nrun, 1ull)] = b;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_l1b_select(const unsigned long long *__restrict__ nrun,
+                                                    const uint64_t *__restrict__ runs,
+                                                    const uint64_t *__restrict__ off,
+                                                    const unsigned long long *__restrict__ cnt,
+                                                    const uint32_t *__restrict__ keys, uint64_t d,
+                                                    const uint64_t *__restrict__ bcount, float *centers) {
+    __shared__ uint32_t hist[2][256];
+    __shared__ uint32_t wmin[8], wmax[8];
+    __shared__ uint64_t wneg[8];
+    __shared__ uint32_t prefix[2];
+    __shared__ uint64_t rank[2];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint64_t total = *nrun;
+    for (uint64_t ri = blockIdx.x; ri < total; ri += gridDim.x) {
+        const uint64_t b = runs[ri];
+        const uint64_t c = b / d, col = b - c * d;
+        const uint64_t m = bcount[c], h = m / 2, nel = cnt[b];
+        const uint32_t *v = keys + off[b];
+        uint32_t mn = 0xffffffffu, mx = 0u;
+        uint64_t ng = 0;
+        for (uint64_t i = t; i < nel; i += 256) {
+            const uint32_t kv = v[i];
+            mn = min(mn, kv);
+            mx = max(mx, kv);
+            ng += kv < 0x7fffffffu;  // strictly negative values
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) {
+            mn = min(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            ng += __shfl_xor_sync(0xffffffffu, ng, o);
+        }
+        if (lane == 0) wmin[warp] = mn, wmax[warp] = mx, wneg[warp] = ng;
+        __syncthreads();
+        mn = wmin[0], mx = wmax[0], ng = wneg[0];
+        for (int q = 1; q < 8; ++q) mn = min(mn, wmin[q]), mx = max(mx, wmax[q]), ng += wneg[q];
+        const float front = ord2f(mn), back = ord2f(mx);
+        // the ranks the rule reads, among the bucket's nonzeros (ascending); zero[s]: the
+        // position falls on one of the m - nel implicit zeros
+        uint64_t r[2] = {0, 0};
+        bool zero[2] = {false, false};
+        int nsel = 0;
+        float result = 0.f;
+        if (nel > h) {
+            nsel = (m & 1) ? 1 : 2;
+            if (front > 0.f || back < 0.f) {
+                const uint64_t tt = front > 0.f ? nel + h - m : m - h;
+                r[0] = tt < nel ? tt : nel - 1;
+                r[1] = tt + 1 < nel ? tt + 1 : nel - 1;
+            } else {
+                const uint64_t z = m - nel, qq[2] = {h, h + 1 < m ? h + 1 : m - 1};
+                for (int s2 = 0; s2 < 2; ++s2) {
+                    const uint64_t q = qq[s2];
+                    if (q < ng) r[s2] = q;
+                    else if (q < ng + z) zero[s2] = true;
+                    else r[s2] = q - z;
+                }
+            }
+        } else {
+            result = front > 0.f ? 0.5f * front : (back < 0.f ? 0.5f * back : 0.f);
+        }
+        if (nsel) {
+            if (t < 2) prefix[t] = 0, rank[t] = r[t];
+            for (int pass = 3; pass >= 0; --pass) {
+                for (int e = t; e < 512; e += 256) (&hist[0][0])[e] = 0;
+                __syncthreads();
+                const uint32_t p0 = prefix[0], p1 = prefix[1];
+                for (uint64_t i0 = 0; i0 < nel; i0 += 256) {
+                    const uint64_t i = i0 + t;
+                    const bool in = i < nel;
+                    const uint32_t kv = in ? v[i] : 0u;
+                    const uint32_t bin = (kv >> (8 * pass)) & 255u, hi = pass == 3 ? 0u : kv >> (8 * (pass + 1));
+#pragma unroll
+                    for (int s2 = 0; s2 < 2; ++s2) {
+                        const bool hit = in && (pass == 3 || hi == (s2 ? p1 : p0));
+                        // equal bins of a warp add once (count data repeats values)
+                        const unsigned grp = __match_any_sync(0xffffffffu, hit ? bin : 0xffffffffu);
+                        if (hit && (grp & ((1u << lane) - 1u)) == 0) atomicAdd(&hist[s2][bin], __popc(grp));
+                    }
+                }
+                __syncthreads();
+                if (t < 2) {
+                    const uint32_t *hh = hist[t];
+                    uint64_t rk = rank[t], cum = 0;
+                    uint32_t bin = 255;
+                    for (uint32_t q = 0; q < 256; ++q) {
+                        if (cum + hh[q] > rk) { bin = q; break; }
+                        cum += hh[q];
+                    }
+                    rank[t] = rk - cum;
+                    prefix[t] = (prefix[t] << 8) | bin;
+                }
+                __syncthreads();
+            }
+            const float x0 = zero[0] ? 0.f : ord2f(prefix[0]), x1 = zero[1] ? 0.f : ord2f(prefix[1]);
+            result = nsel == 1 ? x0 : 0.5f * (x0 + x1);
+        }
+        if (t == 0) centers[c * d + col] = result;
+        __syncthreads();  // shared memory is reused by the next bucket
+    }
+}
+
 namespace {
 int bit_width(uint64_t x) {  // bits needed for values 0..x
     int b = 0;
@@ -1101,6 +1250,32 @@ int launch_l1_medians_csr(const float *vals, const uint32_t *idx, const uint64_t
     k_l1csr_init<<<k, 256, 0, st>>>(vals, idx, indptr, d, rows.perm.p, rows.bucket_start.p, rows.bucket_count.p,
                                     centers), note_launch();
     if (nnz == 0) {
+        MC_CUDA_TRY(cudaGetLastError());
+        return MC_OK;
+    }
+    const uint64_t nb = uint64_t(k) * d;
+    const char *force = std::getenv("MC_L1CSR_SORT");
+    if (nb <= kL1BucketMax && !(force && force[0] == '1')) {
+        MC_TRY(w.cnt.alloc(nb, st));
+        MC_TRY(w.off.alloc(nb + 1, st));
+        MC_TRY(w.cur.alloc(nb, st));
+        MC_TRY(w.runs.alloc(nb + 1, st));
+        MC_TRY(w.val.alloc(nnz, st));
+        unsigned long long *cnt = reinterpret_cast<unsigned long long *>(w.cnt.p);
+        unsigned long long *cur = reinterpret_cast<unsigned long long *>(w.cur.p);
+        unsigned long long *nrun = reinterpret_cast<unsigned long long *>(w.runs.p + nb);
+        const unsigned gr = unsigned(umin64((n + 7) / 8, 152 * 16));
+        MC_CUDA_TRY(cudaMemsetAsync(w.cnt.p, 0, nb * sizeof(uint64_t), st));
+        k_l1b_count<<<gr, 256, 0, st>>>(idx, indptr, n, d, asn, rows.bucket_count.p, cnt), note_launch();
+        MC_TRY(launch_exclusive_scan_u64(w.cnt.p, w.off.p, nb, st, &w.scan));
+        MC_CUDA_TRY(cudaMemcpyAsync(w.cur.p, w.off.p, nb * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
+        k_l1b_scatter<<<gr, 256, 0, st>>>(vals, idx, indptr, n, d, asn, rows.bucket_count.p, cur, w.val.p),
+            note_launch();
+        MC_CUDA_TRY(cudaMemsetAsync(nrun, 0, sizeof(uint64_t), st));
+        k_l1b_list<<<unsigned(umin64((nb + 255) / 256, 152 * 16)), 256, 0, st>>>(cnt, nb, d, rows.bucket_count.p,
+                                                                                  nrun, w.runs.p), note_launch();
+        k_l1b_select<<<152 * 8, 256, 0, st>>>(nrun, w.runs.p, w.off.p, cnt, w.val.p, d, rows.bucket_count.p,
+                                              centers), note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         return MC_OK;
     }

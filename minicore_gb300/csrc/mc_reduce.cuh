@@ -52,15 +52,19 @@ int launch_l1_medians(const float *X, uint64_t d, uint32_t k, const SortWork &w,
 // distance (sequential float sum of |c - x|) is below their cost move to it
 int launch_l1_reseed_update(const float *X, uint64_t n, uint64_t d, const float *center, uint32_t id,
                             uint32_t *asn, double *costs, cudaStream_t st);
-// L1 centers over CSR rows, unweighted (set_centroids_l1 -> util/csc.h:829-893): every
-// nonzero as ((cluster << 32) | column, value key), sorted by an LSD radix sort (digits of at
-// most 11 bits: the value, then the column, then the cluster); each (cluster, column) run of
-// m_c rows with nel nonzeros then takes the reference's sparse median rule.  Clusters with one
-// row take that row; clusters without rows keep their center.
+// L1 centers over CSR rows, unweighted (set_centroids_l1 -> util/csc.h:829-893): each
+// (cluster, column) bucket of a cluster of m rows with nel nonzeros takes the reference's
+// sparse median rule.  Up to 2^28 buckets: per-bucket counts, an atomic scatter of the value
+// keys into their buckets and a radix select per bucket that needs an order statistic.  More
+// buckets (or MC_L1CSR_SORT=1): every nonzero as ((cluster << 32) | column, value key),
+// sorted by an LSD radix sort (digits of at most 11 bits: the value, then the column, then
+// the cluster), then one thread per run.  Clusters with one row take that row; clusters
+// without rows keep their center.
 struct L1CsrWork {
     DBuf<uint64_t> key, key2;
     DBuf<uint32_t> val, val2, digit;
     SortWork sort;
+    DBuf<uint64_t> cnt, off, cur, runs, scan;
 };
 int launch_l1_medians_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n, uint64_t d,
                           uint64_t nnz, uint32_t k, const uint32_t *asn, const SortWork &rows, L1CsrWork &w,
@@ -70,7 +74,9 @@ int launch_l1_medians_csr(const float *vals, const uint32_t *idx, const uint64_t
 int launch_l1_reseed_update_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n,
                                 uint64_t d, const float *center, uint32_t id, uint32_t *asn, double *costs,
                                 cudaStream_t st);
-int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st);
+// scratch: optional work space (kept by the caller, so that a captured graph allocates nothing)
+int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st,
+                              DBuf<uint64_t> *scratch = nullptr);
 int launch_center_sums(const float *C, uint32_t k, uint64_t d, double *csum, float *cnorm, cudaStream_t st);
 
 }  // namespace mc

@@ -415,11 +415,15 @@ def _dense_centers(res):
     return sp.csr_matrix((data, idx.astype(np.int64), indptr.astype(np.int64)), shape=tuple(shape)).toarray()
 
 
+@pytest.mark.parametrize("path", ["bucket", "sort"])
 @pytest.mark.parametrize("signed", [False, True])
-def test_hcluster_csr_l1_medians(mc, orc, signed):
-    """L1 over CSR rows: the sparse median rule (util/csc.h:829-893) on the device (radix
-    sort of the nonzeros by cluster, column and value), bit-exact against the oracle: positive
+def test_hcluster_csr_l1_medians(mc, orc, signed, path, monkeypatch):
+    """L1 over CSR rows: the sparse median rule (util/csc.h:829-893) on the device, by
+    (cluster, column) buckets with a radix select, or (MC_L1CSR_SORT=1, the path for more than
+    2^28 buckets) by a radix sort of all nonzeros; bit-exact against the oracle: positive
     counts, and signed values with stored zeros (every branch of the rule)."""
+    if path == "sort":
+        monkeypatch.setenv("MC_L1CSR_SORT", "1")
     X = _signed_sparse(1200, 60, 0.25, seed=11) if signed else _counts(1500, 80, 0.1, seed=12)
     ids = np.random.default_rng(4).choice(X.shape[0], 9, replace=False)
     C0 = np.asarray(X[ids].toarray(), np.float32)
