@@ -171,7 +171,8 @@ def csr_bench(args):
     nnz = n * 1500
     algo_bytes = nnz * 8 + (n + 1) * 8 + n * 8 + n * 12 + k * d * 4
     pk, pk_kind = peaks()
-    kern = phases.get("assign_csr_sparse") or phases.get("assign_csr_tiled") or {}
+    kern = (phases.get("assign_csr_sparse") or phases.get("assign_csr_l1_union") or phases.get("assign_csr_tiled")
+            or {})
     kms = kern.get("ms", float("nan")) / max(kern.get("count", 1), 1)
     name = {5: "MKL", 4: "JSD", 0: "L1"}[msr]
     rows_tag = f"{n // 1_000_000}M" if n % 1_000_000 == 0 else f"{n // 1000}k"

@@ -196,6 +196,7 @@ struct mc_job {
     uint32_t ngrp = 0;
     SortWork sort;
     L1CsrWork l1csr;  // L1 medians over CSR rows
+    DBuf<float> clist;  // L1 pair-mode CSR assignment: per 32-center group, columns and values
     TcState tc;
     uint64_t last_recheck = 0;
     // Lloyd loop as one CUDA graph (mc_job_run); captured per run, and again after a host
@@ -312,6 +313,11 @@ int job_assign_with(mc_job *j, const float *C, double prior_sum, bool force_exac
         a.dmat = dout->dmat;
         a.ldm = dout->ldm;
         a.dmode = dout->dmode;
+    }
+    if (csr && j->pair && j->msr == L1 && l1_union_work_entries(j->k, d) <= kL1UnionMaxEntries) {
+        Phase ph("assign_csr_l1_union", j->st);
+        MC_TRY(j->clist.alloc(l1_union_work_entries(j->k, d), j->st));
+        return launch_assign_l1_union(a, C, j->clist.p, j->ctx->sms, j->st);
     }
     const bool sparse = csr && j->sparse_path;
     a.kp = sparse ? sparse_center_pad(j->k) : tiled_center_pad(j->k, j->pair, j->msr);

@@ -792,6 +792,195 @@ int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, f
     return MC_OK;
 }
 
+// ------------------------------------------------------------------------------------
+// L1 over CSR rows with the pair-dependent prior (prior 0): the sequential float sum of
+// |(c + pv) - (x + pv)| over the columns in ascending order, skipping only columns where
+// both are zero (they add |pv - pv| = 0, so the sum equals the tiled kernel's walk over
+// every column bit for bit, and the reference's sparse merge walk).  One warp per row,
+// centers in groups of 32 (lane = center), two ways to walk a group:
+//   per lane:  each lane merges the row's columns with its own center's nonzero list
+//              ((column, value bits), ended by column 0xffffffff) -- divergent, about
+//              |row| + max_c |center c| steps;
+//   lockstep:  the row's columns merged with U_g, the ascending columns where any center of
+//              the group is nonzero, and V_g[i][lane] the values there -- warp-uniform,
+//              broadcast row and U_g loads, coalesced V_g rows; |row| + |U_g| steps.
+// The group's walk is chosen per row from those step counts.
+// ------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_l1_center_lists(const float *__restrict__ C, uint64_t d, uint2 *lists,
+                                                         uint32_t *cnz) {
+    __shared__ uint32_t wtot[8];
+    __shared__ uint64_t base;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t c = blockIdx.x;
+    const float *cr = C + uint64_t(c) * d;
+    uint2 *out = lists + uint64_t(c) * (d + 1);
+    if (t == 0) base = 0;
+    __syncthreads();
+    for (uint64_t j0 = 0; j0 < d; j0 += 256) {
+        const uint64_t j = j0 + t;
+        const float v = j < d ? cr[j] : 0.f;
+        const bool nz = v != 0.f;  // -0 is a zero; NaN is kept
+        const unsigned bal = __ballot_sync(0xffffffffu, nz);
+        if (lane == 0) wtot[warp] = __popc(bal);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int q = 0; q < 8; ++q) {
+            before += q < warp ? wtot[q] : 0u;
+            total += wtot[q];
+        }
+        if (nz) out[base + before + __popc(bal & ((1u << lane) - 1u))] = make_uint2(uint32_t(j), __float_as_uint(v));
+        __syncthreads();
+        if (t == 0) base += total;
+        __syncthreads();
+    }
+    if (t == 0) {
+        out[base] = make_uint2(0xffffffffu, 0u);
+        cnz[c] = uint32_t(base);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_l1_center_groups(const float *__restrict__ C, uint32_t k, uint64_t d,
+                                                          uint32_t *U, float *V, uint32_t *usize) {
+    __shared__ uint32_t wtot[8];
+    __shared__ uint64_t base;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t g = blockIdx.x, c0 = g * 32;
+    uint32_t *Ug = U + uint64_t(g) * (d + 1);
+    float *Vg = V + uint64_t(g) * d * 32;
+    if (t == 0) base = 0;
+    __syncthreads();
+    for (uint64_t j0 = 0; j0 < d; j0 += 256) {
+        const uint64_t j = j0 + t;
+        bool nz = false;
+        if (j < d)
+            for (uint32_t c = c0; c < c0 + 32 && c < k; ++c) nz |= C[uint64_t(c) * d + j] != 0.f;
+        const unsigned bal = __ballot_sync(0xffffffffu, nz);
+        if (lane == 0) wtot[warp] = __popc(bal);
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+        for (int q = 0; q < 8; ++q) {
+            before += q < warp ? wtot[q] : 0u;
+            total += wtot[q];
+        }
+        if (nz) {
+            const uint64_t pos = base + before + __popc(bal & ((1u << lane) - 1u));
+            Ug[pos] = uint32_t(j);
+            for (uint32_t l = 0; l < 32; ++l) {
+                const uint32_t c = c0 + l;
+                Vg[pos * 32 + l] = c < k ? C[uint64_t(c) * d + j] : 0.f;
+            }
+        }
+        __syncthreads();
+        if (t == 0) base += total;
+        __syncthreads();
+    }
+    if (t == 0) {
+        Ug[base] = 0xffffffffu;
+        usize[g] = uint32_t(base);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_assign_l1_union(AssignArgs a, const uint2 *__restrict__ lists,
+                                                         const uint32_t *__restrict__ cnz,
+                                                         const uint32_t *__restrict__ U,
+                                                         const float *__restrict__ V,
+                                                         const uint32_t *__restrict__ usize) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    const uint32_t ng = (a.k + 31) / 32;
+    for (uint64_t r = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; r < a.n; r += nw) {
+        const uint64_t rb = a.indptr[r], re = a.indptr[r + 1];
+        const uint32_t nr = uint32_t(re - rb);
+        const uint32_t *ri = a.idx + rb;
+        const float *rx = a.vals + rb;
+        const double rs = a.rowsum[r];
+        Best best;
+        best_init(best);
+        for (uint32_t g = 0; g < ng; ++g) {
+            const uint32_t c = g * 32 + lane;
+            const float pv = pair_scalars(a.prior, a.prior_sum, rs, c < a.k ? a.csum[c] : 0.0, a.d).pv;
+            uint32_t cmax = c < a.k ? cnz[c] : 0u;
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) cmax = max(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+            float acc = 0.f;
+            uint32_t p = 0, rc = nr ? ri[0] : 0xffffffffu;
+            float rv = nr ? rx[0] : 0.f;
+            if (uint64_t(nr + usize[g]) * 4 <= uint64_t(nr + cmax) * 5) {
+                const uint32_t *Ug = U + uint64_t(g) * (a.d + 1);
+                const float *Vg = V + uint64_t(g) * a.d * 32 + lane;
+                uint32_t q = 0, uc = Ug[0];
+                float uv = uc != 0xffffffffu ? Vg[0] : 0.f;
+                while ((rc & uc) != 0xffffffffu) {  // warp-uniform
+                    const bool tr = rc <= uc, tu = uc <= rc;
+                    const float av = (tu ? uv : 0.f) + pv;
+                    const float bv = (tr ? rv : 0.f) + pv;
+                    acc = acc + fabsf(av - bv);
+                    if (tr) {
+                        ++p;
+                        rc = p < nr ? ri[p] : 0xffffffffu;
+                        rv = p < nr ? rx[p] : 0.f;
+                    }
+                    if (tu) {
+                        uc = Ug[++q];
+                        uv = uc != 0xffffffffu ? Vg[uint64_t(q) * 32] : 0.f;
+                    }
+                }
+            } else if (c < a.k) {
+                const uint2 *cl = lists + uint64_t(c) * (a.d + 1);
+                uint2 ce = cl[0];
+                while ((rc & ce.x) != 0xffffffffu) {  // per lane
+                    const bool tr = rc <= ce.x, tc = ce.x <= rc;
+                    const float av = (tc ? __uint_as_float(ce.y) : 0.f) + pv;
+                    const float bv = (tr ? rv : 0.f) + pv;
+                    acc = acc + fabsf(av - bv);
+                    if (tr) {
+                        ++p;
+                        rc = p < nr ? ri[p] : 0xffffffffu;
+                        rv = p < nr ? rx[p] : 0.f;
+                    }
+                    if (tc) ce = *++cl;
+                }
+            }
+            if (c < a.k) {
+                const float key = finish_key<L1>(acc);
+                best_offer(best, key, c);
+                if (a.dmode) write_dist(a, r, c, float(key_to_cost<L1>(key)));
+            }
+        }
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) best_merge_shfl(best, m);
+        if (lane == 0) {
+            const bool nan0 = best.v == __int_as_float(0xff800000);
+            const double cost = nan0 ? __longlong_as_double(0x7ff8000000000000ll) : key_to_cost<L1>(best.v);
+            a.asn[r] = best.j;
+            a.costs[r] = double(float(cost));
+        }
+    }
+}
+
+uint64_t l1_union_work_entries(uint32_t k, uint64_t d) {
+    const uint64_t ng = (k + 31) / 32;
+    return uint64_t(k) * (d + 1) * 2 + ng * (d + 1) * 33 + k + ng + 8;
+}
+
+int launch_assign_l1_union(const AssignArgs &a, const float *C, float *work, int sms, cudaStream_t st) {
+    if (a.k == 0) return MC_OK;
+    const uint32_t ng = (a.k + 31) / 32;
+    // work: lists (8-byte aligned first), U, V, cnz, usize
+    uint2 *lists = reinterpret_cast<uint2 *>(work);
+    uint32_t *U = reinterpret_cast<uint32_t *>(work + uint64_t(a.k) * (a.d + 1) * 2);
+    float *V = reinterpret_cast<float *>(U + uint64_t(ng) * (a.d + 1));
+    uint32_t *cnz = reinterpret_cast<uint32_t *>(V + uint64_t(ng) * a.d * 32);
+    uint32_t *usize = cnz + a.k;
+    k_l1_center_lists<<<a.k, 256, 0, st>>>(C, a.d, lists, cnz), note_launch();
+    k_l1_center_groups<<<ng, 256, 0, st>>>(C, a.k, a.d, U, V, usize), note_launch();
+    if (a.n)
+        k_assign_l1_union<<<unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16)), 256, 0, st>>>(a, lists, cnz, U, V,
+                                                                                              usize), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 template <int MSR, bool CSR>
 static int tiled_t(const AssignArgs &a, bool pair, bool big, cudaStream_t st, bool tune) {
     if (pair) {

@@ -54,6 +54,12 @@ int launch_row_scalars(const double *rowsum, uint64_t n, uint64_t d, float pv, f
 // must not synchronise or allocate pass false)
 int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t st, bool tune = true);
 int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms, bool tune = true);
+// L1 over CSR rows in pair mode (prior 0): a walk over the union of nonzero columns,
+// bit-identical to the tiled kernel; work: l1_union_work_entries(k, d) floats
+int launch_assign_l1_union(const AssignArgs &a, const float *C, float *work, int sms, cudaStream_t st);
+uint64_t l1_union_work_entries(uint32_t k, uint64_t d);
+// the largest work space (in entries) for which the union kernel is used
+constexpr uint64_t kL1UnionMaxEntries = 1ull << 29;
 // JSD sparse-dot table: ztab[g * k + c] = sum over all columns j of f(a_cj, gval[g]) with
 // f(a, b) = a log a + b log b - (a + b) log((a + b) / 2) and a_cj the center transform
 int launch_jsd_ztable(const float *C, uint32_t k, uint64_t d, const double *csum, float pv, const float *gval,

@@ -475,3 +475,28 @@ def test_csr_l1_loop_modes_agree(mc, orc, mode):
     assert res["numiter"] == ores["numiter"]
     assert np.array_equal(res["asn"], ores["asn"])
     assert np.array_equal(_dense_centers(res), ores["centers"])
+
+
+@pytest.mark.parametrize("k", [5, 33, 70])
+def test_csr_l1_prior0_union_walk_exact(mc, orc, k):
+    """L1 over CSR rows with prior 0 (pair-dependent pv): the union merge walk gives the
+    oracle's distances and assignments bit for bit; signed values, stored zeros, an empty row,
+    values small enough for pv to matter, centers with zero columns, several lane rounds."""
+    X = _signed_sparse(1500, 120, 0.12, seed=k).tolil()
+    X[4, :] = 0.0
+    X[9, 7] = 3e-38
+    X[9, 8] = -2e-38
+    X = X.tocsr()
+    X.sort_indices()
+    rng = np.random.default_rng(k)
+    C = np.asarray(X[rng.choice(1500, k, replace=False)].toarray(), np.float32)
+    C[:, ::5] += 0.25
+    C[0, 7] = 1e-38
+    asn, costs = _assign_gpu(mc, X, C, 0, 0.0)
+    _check_assign(orc, X, C, 0, 0.0, asn, costs, exact=True)
+    # the distance output of the same kernel (cmp) against the oracle's per-pair values
+    D = mc.cmp(X, C, msr=0, prior=0.0)
+    Xd = X.toarray()
+    for i in (0, 4, 9, 777):
+        for c in (0, k - 1):
+            assert D[i, c] == np.float32(orc.msr_sparse(0, Xd[i], C[c], 0.0))
