@@ -443,8 +443,8 @@ int job_set_centroids_l1(mc_job *j) {
                 k_copy_row_csr<<<1, 256, 0, st>>>(j->M.vals, j->M.idx, j->M.indptr, j->idxbuf.p + k, dst),
                     note_launch();
                 MC_CUDA_TRY(cudaGetLastError());
-                MC_TRY(launch_l1_reseed_update_csr(j->M.vals, j->M.idx, j->M.indptr, n, d, dst, id, j->asn.p,
-                                                   j->costs.p, st));
+                MC_TRY(launch_l1_reseed_update_csr(j->M.vals, j->M.idx, j->M.indptr, n, j->idxbuf.p + k, id,
+                                                   j->asn.p, j->costs.p, st));
             }
         }
         MC_TRY(launch_sort_by_key(j->asn.p, nullptr, n, k, j->sort, st));

@@ -948,17 +948,23 @@ int launch_l1_reseed_update(const float *X, uint64_t n, uint64_t d, const float 
 // ------------------------------------------------------------------------------------
 // L1 medians over CSR rows
 // ------------------------------------------------------------------------------------
+// the new center is CSR row *rsel: the sequential sum over the union of the two rows' columns
+// (a column where both are zero adds exactly 0), one thread per row
 __global__ void k_l1_reseed_update_csr(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
-                                       const uint64_t *__restrict__ indptr, uint64_t n, uint64_t d,
-                                       const float *__restrict__ center, uint32_t id, uint32_t *asn, double *costs) {
+                                       const uint64_t *__restrict__ indptr, uint64_t n,
+                                       const uint64_t *__restrict__ rsel, uint32_t id, uint32_t *asn,
+                                       double *costs) {
+    const uint64_t cb = indptr[*rsel], ce = indptr[*rsel + 1];
     for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x)) {
-        uint64_t p = indptr[i];
+        uint64_t p = indptr[i], q = cb;
         const uint64_t pe = indptr[i + 1];
         float a = 0.f;
-        for (uint64_t j = 0; j < d; ++j) {
-            float x = 0.f;
-            if (p < pe && idx[p] == j) x = vals[p++];
-            a = a + fabsf(center[j] - x);
+        while (p < pe || q < ce) {
+            const uint32_t rc = p < pe ? idx[p] : 0xffffffffu, cc = q < ce ? idx[q] : 0xffffffffu;
+            const float x = rc <= cc ? vals[p] : 0.f, c = cc <= rc ? vals[q] : 0.f;
+            a = a + fabsf(c - x);
+            p += rc <= cc;
+            q += cc <= rc;
         }
         if (double(a) < costs[i]) {
             asn[i] = id;
@@ -968,11 +974,10 @@ __global__ void k_l1_reseed_update_csr(const float *__restrict__ vals, const uin
 }
 
 int launch_l1_reseed_update_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n,
-                                uint64_t d, const float *center, uint32_t id, uint32_t *asn, double *costs,
-                                cudaStream_t st) {
+                                const uint64_t *rsel, uint32_t id, uint32_t *asn, double *costs, cudaStream_t st) {
     if (n == 0) return MC_OK;
-    k_l1_reseed_update_csr<<<unsigned(umin64((n + 255) / 256, 4096)), 256, 0, st>>>(vals, idx, indptr, n, d, center,
-                                                                                   id, asn, costs), note_launch();
+    k_l1_reseed_update_csr<<<unsigned(umin64((n + 255) / 256, 4096)), 256, 0, st>>>(vals, idx, indptr, n, rsel, id,
+                                                                                   asn, costs), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }

@@ -69,11 +69,11 @@ struct L1CsrWork {
 int launch_l1_medians_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n, uint64_t d,
                           uint64_t nnz, uint32_t k, const uint32_t *asn, const SortWork &rows, L1CsrWork &w,
                           float *centers, cudaStream_t st);
-// launch_l1_reseed_update over CSR rows (the row's zeros take part: sequential float sum of
-// |c_j - x_j| over every column)
+// launch_l1_reseed_update over CSR rows, the new center being CSR row *rsel (device): the
+// sequential float sum of |c_j - x_j| over the union of the two rows' columns, which equals
+// the sum over every column
 int launch_l1_reseed_update_csr(const float *vals, const uint32_t *idx, const uint64_t *indptr, uint64_t n,
-                                uint64_t d, const float *center, uint32_t id, uint32_t *asn, double *costs,
-                                cudaStream_t st);
+                                const uint64_t *rsel, uint32_t id, uint32_t *asn, double *costs, cudaStream_t st);
 // scratch: optional work space (kept by the caller, so that a captured graph allocates nothing)
 int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st,
                               DBuf<uint64_t> *scratch = nullptr);

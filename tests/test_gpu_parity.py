@@ -500,3 +500,17 @@ def test_csr_l1_prior0_union_walk_exact(mc, orc, k):
     for i in (0, 4, 9, 777):
         for c in (0, k - 1):
             assert D[i, c] == np.float32(orc.msr_sparse(0, Xd[i], C[c], 0.0))
+
+
+def test_hcluster_csr_l1_empty_cluster_reseed(mc, orc):
+    """A CSR L1 center far from every row: the restart draws a row (D^2 over the costs), moves
+    the rows closer to it (union walk of the two rows), then takes the sparse medians; oracle
+    bit-exact."""
+    X = _counts(1500, 90, 0.1, seed=44)
+    C0 = np.concatenate([np.asarray(X[[3, 300, 600, 900]].toarray(), np.float32),
+                         np.full((1, 90), 1e4, np.float32)])
+    res = mc.hcluster(X, C0, msr=0, prior=0.0, eps=0.0, maxiter=4, seed=13)
+    ores = orc.hcluster(X, C0, 0, 0.0, eps=0.0, maxiter=4, seed=13)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(_dense_centers(res), ores["centers"])
