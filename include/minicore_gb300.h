@@ -140,7 +140,11 @@ int mc_assign(mc_context *ctx, const mc_matrix *X, const float *centers, uint32_
 
 /* Lloyd / Bregman EM from explicit centers (solve.h:98-175): eps, maxiter and the
  * revert-on-increase rule as in the reference; empty clusters restart by D^2 draws
- * U(seed, r).  weights: optional (double, n). */
+ * U(seed, r).  weights: optional (double, n).  L1 takes coordinate-wise medians
+ * (set_centroids_l1, centroid.h:435-504): dense rows by the sorted median (weighted: the
+ * largest-weight row's value, as weighted_median returns), CSR rows by the sparse rule of
+ * util/csc.h:829-893; weighted L1 over CSR rows returns MC_EUNSUPPORTED as the reference
+ * raises. */
 int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
                 double prior, const double *weights, double eps, uint64_t maxiter, uint64_t seed,
                 int precision, float *centers_out, uint32_t *asn, double *costs,
@@ -192,7 +196,9 @@ int mc_job_read(mc_job *job, float *centers, uint32_t *asn, double *costs);
  * exhaustive assignment, restarts of the centers holding <= reseed_after rows (D^2 draws
  * U(seed, r) over the costs), and the objective; between them, a sample of mbsize rows
  * (U(seed ^ 0x6A09E667F3BCC908, t), with or without replacement) is assigned and every hit
- * center is replaced by its group's mean.  Distances use the prior as the prior sum, as
+ * center is replaced by its group's mean (L1: its group's median; with weights over dense
+ * rows, weighted_median reading the full weight vector at the group position, as
+ * solve.h:559-561 does).  Distances use the prior as the prior sum, as
  * the reference's minibatch code does.  The centers of the best objective are kept; asn and
  * costs are those of the last exhaustive assignment. */
 int mc_job_minibatch(mc_job *job, uint64_t mbsize, uint64_t maxiter, uint64_t calc_cost_freq,
@@ -227,7 +233,9 @@ int mc_hcluster_coreset(mc_context *ctx, const mc_matrix *X, const float *center
  * dot(costs_i, asn_i) (FP64), centers = soft weighted means, costs = msr(rows, centers).
  * Stops when the objective improves by <= eps * max(old, new) or after maxiter iterations;
  * centers are taken only on improvement.  costs_out / asn_out: nrows x k float32 (the last
- * ones computed).  L1 (median centers) is not covered. */
+ * ones computed).  L1 over dense rows: per center the value, per column, of the row with
+ * the largest soft weight (weighted_median with the soft assignments, centroid.h:815-838);
+ * L1 over CSR rows returns MC_EUNSUPPORTED (the reference raises). */
 int mc_scluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
                 double prior, const double *weights, double temp, uint64_t maxiter, double eps,
                 float *centers_out, float *costs_out, float *asn_out, double *initcost,
