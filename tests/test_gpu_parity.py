@@ -514,3 +514,37 @@ def test_hcluster_csr_l1_empty_cluster_reseed(mc, orc):
     assert res["numiter"] == ores["numiter"]
     assert np.array_equal(res["asn"], ores["asn"])
     assert np.array_equal(_dense_centers(res), ores["centers"])
+
+
+@pytest.mark.parametrize("centers", ["dense", "disjoint"])
+def test_csr_l1_prior0_walk_forms(mc, orc, centers):
+    """Both walks of the CSR L1 prior-0 kernel: dense centers (every group's column union is
+    every column: the warp-uniform walk) and centers with disjoint supports (the per-lane
+    merge); 40 centers (two groups), empty rows, d = 97."""
+    X = _signed_sparse(900, 97, 0.15, seed=61).tolil()
+    X[10, :] = 0.0
+    X[11, :] = 0.0
+    X = X.tocsr()
+    X.sort_indices()
+    rng = np.random.default_rng(62)
+    if centers == "dense":
+        C = rng.uniform(-2, 3, (40, 97)).astype(np.float32)
+    else:
+        C = np.zeros((40, 97), np.float32)
+        for c in range(40):
+            cols = [(c * 2 + t) % 97 for t in range(2)]
+            C[c, cols] = rng.uniform(0.5, 3, 2)
+    asn, costs = _assign_gpu(mc, X, C, 0, 0.0)
+    _check_assign(orc, X, C, 0, 0.0, asn, costs, exact=True)
+
+
+def test_csr_l1_one_column_and_one_center(mc, orc):
+    X = sp.csr_matrix(np.array([[1.0], [0.0], [3.0], [-2.0], [0.0]], np.float32))
+    for C in (np.array([[0.5]], np.float32), np.array([[0.0], [2.0], [-1.0]], np.float32)):
+        asn, costs = _assign_gpu(mc, X, C, 0, 0.0)
+        _check_assign(orc, X, C, 0, 0.0, asn, costs, exact=True)
+    res = mc.hcluster(X, np.array([[0.0], [2.0]], np.float32), msr=0, eps=0.0, maxiter=3, seed=1)
+    ores = orc.hcluster(X, np.array([[0.0], [2.0]], np.float32), 0, 0.0, eps=0.0, maxiter=3, seed=1)
+    assert res["numiter"] == ores["numiter"]
+    assert np.array_equal(res["asn"], ores["asn"])
+    assert np.array_equal(_dense_centers(res), ores["centers"])
