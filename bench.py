@@ -189,6 +189,22 @@ def csr_bench(args):
                         "frac": algo_bytes / (kms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6767.7),
                         "algorithmic_bytes": algo_bytes, "kernel_ms": kms, "peak_source": pk_kind},
            "phases_ms": phases}
+    if msr != 0:
+        # a whole Lloyd update (weighted means of the CSR rows, then the assignment pass),
+        # the C2 loop's unit of work
+        lib.mc_profile_reset()
+        lib.mc_profile_enable(1)
+        e0.record(stream)
+        for _ in range(args.steps):
+            job.lloyd_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lib.mc_profile_enable(0)
+        buf2 = ctypes.create_string_buffer(1 << 16)
+        _lib.check(lib.mc_profile_report(buf2, len(buf2)))
+        out["lloyd_step"] = {"ms": e0.elapsed_time(e1) / args.steps,
+                             "iters_per_s": 1000.0 * args.steps / e0.elapsed_time(e1),
+                             "phases_ms": json.loads(buf2.value.decode())}
     if msr == 0:
         # the median phase: algorithmic bytes = the nonzeros (values + indices), the row
         # pointers and assignments, and the k x d centers written
