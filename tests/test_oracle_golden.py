@@ -317,3 +317,47 @@ def test_oracle_sparse_l1_weighted_raises(orc):
     S = sp.csr_matrix(np.eye(4, dtype=np.float32))
     with pytest.raises(ValueError):
         orc.l1_centers(S, np.zeros(4, np.uint32), 1, weights=np.ones(4))
+
+
+def _sparse_median_py(vals, nrows):
+    """util/csc.h:856-890 for one column of one cluster, in plain Python: vals = the
+    cluster's nonzeros in that column, nrows = the cluster's rows (positions past the end of
+    a vector, undefined in the reference, take its last element)."""
+    v = sorted(np.float32(x) for x in vals)
+    nel, h = len(v), nrows // 2
+    at = lambda a, q: a[min(q, len(a) - 1)]
+    half = lambda a, b: np.float32(np.float32(a + b) * np.float32(0.5))
+    if nel > h:
+        if v[0] > 0 or v[-1] < 0:
+            t = h - (nrows - nel) if v[0] > 0 else nrows - h
+            return at(v, t) if nrows & 1 else half(at(v, t), at(v, t + 1))
+        f = sorted(v + [np.float32(0)] * (nrows - nel))
+        return f[h] if nrows & 1 else half(at(f, h), at(f, h + 1))
+    if nrows & 1 and nel == h:
+        if v[0] > 0:
+            return np.float32(np.float32(0.5) * v[0])
+        if v[-1] < 0:
+            return np.float32(np.float32(0.5) * v[-1])
+    return np.float32(0)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_sparse_l1_medians_match_python_restatement(orc, seed):
+    rng = np.random.default_rng(seed)
+    n, d, k = int(rng.integers(5, 60)), int(rng.integers(1, 12)), int(rng.integers(1, 6))
+    dens = rng.uniform(0.1, 0.9)
+    X = (rng.integers(-3, 5, (n, d)) * (rng.random((n, d)) < dens)).astype(np.float32)
+    asn = rng.integers(0, k, n).astype(np.uint32)
+    asn[:k] = np.arange(k)  # no empty cluster
+    S = sp.csr_matrix(X)
+    got = orc.l1_centers(S, asn, k)
+    for c in range(k):
+        rows = np.nonzero(asn == c)[0]
+        for j in range(d):
+            if rows.size == 1:
+                want = X[rows[0], j]
+            else:
+                col = S[rows][:, j].toarray().ravel()
+                nz = [x for x, r in zip(col, rows) if S[r, j] != 0 or (S[r].indices == j).any()]
+                want = _sparse_median_py(nz, rows.size)
+            assert got[c, j] == want, (c, j)
