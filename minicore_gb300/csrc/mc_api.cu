@@ -386,6 +386,7 @@ int job_launch_centroids(mc_job *j, const uint32_t *keys2, uint64_t extra, bool 
     ca.vals = j->M.vals;
     ca.idx = j->M.idx;
     ca.indptr = j->M.indptr;
+    ca.nnz = j->M.nnz;
     ca.keys = j->asn.p;
     ca.keys2 = keys2;
     ca.extra_members = extra;
@@ -1555,6 +1556,7 @@ int mc_job_minibatch(mc_job *j, uint64_t mbsize, uint64_t maxiter, uint64_t calc
         ca.vals = sj->M.vals;
         ca.idx = sj->M.idx;
         ca.indptr = sj->M.indptr;
+        ca.nnz = sj->M.nnz;
         ca.keys = sj->asn.p;
         ca.w = sj->w.p;
         ca.centers = j->C.p;  // groups with no sampled row keep their center

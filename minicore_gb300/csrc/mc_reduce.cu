@@ -310,14 +310,15 @@ __global__ void __launch_bounds__(256) k_sort_key_scan(uint32_t *tile_counts, ui
 
 // exclusive scan of up to a few thousand counts (single CTA of 1024 threads): per-thread
 // sequential runs, then a parallel scan of the 1024 run totals (warp shuffles, 32 warp
-// totals); out[m] = total
-__global__ void __launch_bounds__(1024) k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m) {
+// totals); out[m] = total.  div > 0 scans ceil(in[i] / div) instead (chunks per bucket).
+__global__ void __launch_bounds__(1024) k_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m,
+                                                             uint64_t div) {
     __shared__ uint64_t wtot[32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const uint64_t per = (m + blockDim.x - 1) / blockDim.x;
     const uint64_t b = t * per, e = umin64(m, b + per);
     uint64_t s = 0;
-    for (uint64_t i = b; i < e; ++i) s += in[i];
+    for (uint64_t i = b; i < e; ++i) s += div ? (in[i] + div - 1) / div : in[i];
     uint64_t inc = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -339,7 +340,7 @@ __global__ void __launch_bounds__(1024) k_exclusive_scan_u64(const uint64_t *in,
     __syncthreads();
     uint64_t acc = wtot[w] + inc - s;
     for (uint64_t i = b; i < e; ++i) {
-        const uint64_t v = in[i];
+        const uint64_t v = div ? (in[i] + div - 1) / div : in[i];
         out[i] = acc;
         acc += v;
     }
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(256) k_scan_tile_write(const uint64_t *__restr
 
 int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cudaStream_t st, DBuf<uint64_t> *scratch) {
     if (m <= 16 * 1024) {  // one CTA
-        k_exclusive_scan_u64<<<1, 1024, 0, st>>>(in, out, m), note_launch();
+        k_exclusive_scan_u64<<<1, 1024, 0, st>>>(in, out, m, 0), note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         return MC_OK;
     }
@@ -471,7 +472,7 @@ int launch_exclusive_scan_u64(const uint64_t *in, uint64_t *out, uint64_t m, cud
     MC_TRY(buf.alloc(2 * nt + 1, st));
     uint64_t *tsum = buf.p, *toff = buf.p + nt;
     k_scan_tile_sums<<<unsigned(nt), 256, 0, st>>>(in, m, tsum), note_launch();
-    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(tsum, toff, nt), note_launch();
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(tsum, toff, nt, 0), note_launch();
     k_scan_tile_write<<<unsigned(nt), 256, 0, st>>>(in, m, toff, out), note_launch();
     MC_CUDA_TRY(cudaMemcpyAsync(out + m, toff + nt, sizeof(uint64_t), cudaMemcpyDeviceToDevice, st));
     MC_CUDA_TRY(cudaGetLastError());
@@ -491,7 +492,7 @@ int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, 
     else
         MC_CUDA_TRY(cudaMemsetAsync(w.bucket_count.p, 0, k * sizeof(uint64_t), st));
     if (ntiles) k_sort_key_scan<<<k, 256, 0, st>>>(w.tile_counts.p, ntiles, k, w.bucket_count.p), note_launch();
-    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.bucket_count.p, w.bucket_start.p, k), note_launch();
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.bucket_count.p, w.bucket_start.p, k, 0), note_launch();
     if (ntiles) {
         if (!keys2)
             k_sort_scatter<<<unsigned(ntiles), 32, k <= kSmemKeys ? k * sizeof(uint32_t) : 0, st>>>(
@@ -511,11 +512,6 @@ int launch_sort_by_key(const uint32_t *keys, const uint32_t *keys2, uint64_t n, 
 // chunk_start[c] = exclusive scan of the chunk counts (computed on device); a grid of
 // ceil(n/ch)+k CTAs maps its chunk id by binary search, extra CTAs exit.
 // ------------------------------------------------------------------------------------
-__global__ void k_chunk_counts(const uint64_t *bucket_count, uint32_t k, uint64_t ch, uint64_t *chunk_count) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < k) chunk_count[c] = (bucket_count[c] + ch - 1) / ch;
-}
-
 __device__ inline uint32_t find_bucket(const uint64_t *chunk_start, uint32_t k, uint64_t q) {
     // largest c with chunk_start[c] <= q (chunk_start has k+1 entries, nondecreasing)
     uint32_t lo = 0, hi = k;  // invariant: chunk_start[lo] <= q < chunk_start[hi]
@@ -717,16 +713,74 @@ __global__ void __launch_bounds__(256) k_centroid_chunks_csr(const float *__rest
     }
 }
 
+// The same for short rows (a few nonzeros each, where the register pipeline below costs
+// more instructions per row than it saves): rows one after the other.
+__global__ void k_centroid_chunks_csr_short(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
+                                      const uint64_t *__restrict__ indptr, uint64_t d, uint64_t band,
+                                      const uint32_t *__restrict__ perm, const uint64_t *__restrict__ bucket_start,
+                                      const uint64_t *__restrict__ bucket_count,
+                                      const uint64_t *__restrict__ chunk_start, uint32_t k, uint64_t ch,
+                                      const double *__restrict__ w, double *partial, double *partial_w) {
+    extern __shared__ unsigned char smraw[];
+    const uint64_t q = blockIdx.x;
+    if (q >= chunk_start[k]) return;
+    const uint32_t c = find_bucket(chunk_start, k, q);
+    const uint64_t local = q - chunk_start[c];
+    const uint64_t r0 = local * ch, r1 = umin64(bucket_count[c], r0 + ch);
+    const uint32_t *rows = perm + bucket_start[c];
+    const uint64_t j0 = blockIdx.y * band, j1 = umin64(d, j0 + band);
+    const uint64_t bw = j1 - j0;
+    if (w) {
+        double *acc = reinterpret_cast<double *>(smraw);
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x) acc[j] = 0.0;
+        __syncthreads();
+        for (uint64_t r = r0; r < r1; ++r) {
+            const uint32_t row = rows[r];
+            const double wr = w[row];
+            for (uint64_t p = indptr[row] + threadIdx.x; p < indptr[row + 1]; p += blockDim.x) {
+                const uint32_t col = idx[p];
+                if (col >= j0 && col < j1) acc[col - j0] = fma(wr, double(vals[p]), acc[col - j0]);
+            }
+            __syncthreads();
+        }
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x) partial[q * d + j0 + j] = acc[j];
+        if (blockIdx.y == 0 && threadIdx.x == 0) {
+            double wq = 0.0;
+            for (uint64_t r = r0; r < r1; ++r) wq = wq + w[rows[r]];
+            partial_w[q] = wq;
+        }
+    } else {
+        float *s = reinterpret_cast<float *>(smraw);
+        float *e = s + band;
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x) { s[j] = 0.f; e[j] = 0.f; }
+        __syncthreads();
+        for (uint64_t r = r0; r < r1; ++r) {
+            const uint32_t row = rows[r];
+            for (uint64_t p = indptr[row] + threadIdx.x; p < indptr[row + 1]; p += blockDim.x) {
+                const uint32_t col = idx[p];
+                if (col >= j0 && col < j1) two_sum_add(s[col - j0], e[col - j0], vals[p]);
+            }
+            __syncthreads();
+        }
+        for (uint64_t j = threadIdx.x; j < bw; j += blockDim.x)
+            partial[q * d + j0 + j] = double(s[j]) + double(e[j]);
+    }
+}
+
 // finalize: per (bucket, column): FP64 sum of chunk partials in order, divide, round.
-// Buckets with one row copy the row; empty buckets keep the old center.
+// Buckets with one row copy the row (here for dense rows X; CSR rows in
+// k_centroid_singletons_csr); empty buckets keep the old center.
 __global__ void k_centroid_finalize(const double *__restrict__ partial, const double *__restrict__ partial_w,
                                     const uint64_t *__restrict__ chunk_start, const uint64_t *__restrict__ bucket_count,
-                                    uint32_t k, uint64_t d, int weighted, float *centers, int *nan_flag) {
+                                    uint32_t k, uint64_t d, int weighted, float *centers, int *nan_flag,
+                                    const float *__restrict__ X, const uint32_t *__restrict__ perm,
+                                    const uint64_t *__restrict__ bucket_start) {
     const uint64_t j = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
     if (j >= d) return;
     for (uint32_t c = blockIdx.y; c < k; c += gridDim.y) {
         const uint64_t cnt = bucket_count[c];
-        if (cnt <= 1) continue;  // empty: keep; singleton: row copy (separate kernel)
+        if (cnt == 1 && X) centers[uint64_t(c) * d + j] = X[uint64_t(perm[bucket_start[c]]) * d + j];
+        if (cnt <= 1) continue;  // empty: keep
         const uint64_t q0 = chunk_start[c], q1 = chunk_start[c + 1];
         double S = partial[q0 * d + j];
         for (uint64_t q = q0 + 1; q < q1; ++q) S = S + partial[q * d + j];
@@ -743,17 +797,7 @@ __global__ void k_centroid_finalize(const double *__restrict__ partial, const do
     }
 }
 
-// singleton buckets copy the row verbatim (centroid.h:761-768)
-__global__ void k_centroid_singletons_dense(const float *__restrict__ X, uint64_t d, const uint32_t *perm,
-                                            const uint64_t *bucket_start, const uint64_t *bucket_count, uint32_t k,
-                                            float *centers) {
-    for (uint32_t c = blockIdx.x; c < k; c += gridDim.x) {
-        if (bucket_count[c] != 1) continue;
-        const uint32_t row = perm[bucket_start[c]];
-        for (uint64_t j = threadIdx.x; j < d; j += blockDim.x) centers[uint64_t(c) * d + j] = X[uint64_t(row) * d + j];
-    }
-}
-
+// singleton buckets of CSR rows copy the row verbatim (centroid.h:761-768)
 __global__ void k_centroid_singletons_csr(const float *__restrict__ vals, const uint32_t *__restrict__ idx,
                                           const uint64_t *__restrict__ indptr, uint64_t d, const uint32_t *perm,
                                           const uint64_t *bucket_start, const uint64_t *bucket_count, uint32_t k,
@@ -774,10 +818,9 @@ int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool p
     const uint32_t k = a.k;
     const uint64_t ch = a.csr ? 4096 : kDenseChunk;
     if (!presorted) MC_TRY(launch_sort_by_key(a.keys, a.keys2, n, k, w, st));
-    MC_TRY(w.chunk_count.alloc(k, st));
     MC_TRY(w.chunk_start.alloc(uint64_t(k) + 1, st));
-    k_chunk_counts<<<(k + 255) / 256, 256, 0, st>>>(w.bucket_count.p, k, ch, w.chunk_count.p), note_launch();
-    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.chunk_count.p, w.chunk_start.p, k), note_launch();
+    // chunk starts: exclusive scan of ceil(bucket count / ch)
+    k_exclusive_scan_u64<<<1, 1024, 0, st>>>(w.bucket_count.p, w.chunk_start.p, k, ch), note_launch();
     const uint64_t members = n + (a.keys2 ? a.extra_members : 0);
     const uint64_t max_chunks = (members + ch - 1) / ch + k;
     MC_TRY(w.partial.alloc(max_chunks * d, st));
@@ -793,18 +836,18 @@ int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool p
         const unsigned nb = unsigned((d + band - 1) / band);
         // always the largest band's size: a per-call value could be lowered by another host
         // thread between this call's set and its launch
-        MC_CUDA_TRY(cudaFuncSetAttribute(k_centroid_chunks_csr, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        // rows of 32 or more nonzeros on average: the register-pipelined kernel
+        auto kern = (a.nnz >= 32 * n) ? k_centroid_chunks_csr : k_centroid_chunks_csr_short;
+        MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(2 * 24576 * sizeof(float))));
-        k_centroid_chunks_csr<<<dim3(unsigned(max_chunks), nb), 256, smem, st>>>(
+        kern<<<dim3(unsigned(max_chunks), nb), 256, smem, st>>>(
             a.vals, a.idx, a.indptr, d, bw, w.perm.p, w.bucket_start.p, w.bucket_count.p, w.chunk_start.p, k, ch,
             a.w, w.partial.p, w.partial_w.p), note_launch();
     }
     k_centroid_finalize<<<dim3(unsigned((d + 127) / 128), k < 65535 ? k : 65535), 128, 0, st>>>(
-        w.partial.p, w.partial_w.p, w.chunk_start.p, w.bucket_count.p, k, d, a.w ? 1 : 0, a.centers, a.nan_flag), note_launch();
-    if (!a.csr)
-        k_centroid_singletons_dense<<<k < 65535 ? k : 65535, 128, 0, st>>>(a.X, d, w.perm.p, w.bucket_start.p, w.bucket_count.p, k,
-                                                       a.centers), note_launch();
-    else
+        w.partial.p, w.partial_w.p, w.chunk_start.p, w.bucket_count.p, k, d, a.w ? 1 : 0, a.centers, a.nan_flag,
+        a.csr ? nullptr : a.X, w.perm.p, w.bucket_start.p), note_launch();
+    if (a.csr)
         k_centroid_singletons_csr<<<k < 65535 ? k : 65535, 256, 0, st>>>(a.vals, a.idx, a.indptr, d, w.perm.p, w.bucket_start.p,
                                                      w.bucket_count.p, k, a.centers), note_launch();
     MC_CUDA_TRY(cudaGetLastError());

@@ -25,6 +25,7 @@ struct CentroidArgs {
     const float *vals = nullptr;              // CSR
     const uint32_t *idx = nullptr;
     const uint64_t *indptr = nullptr;
+    uint64_t nnz = 0;                         // CSR nonzeros (picks the row-pipelined kernel)
     const uint32_t *keys = nullptr;           // cluster of each row
     const uint32_t *keys2 = nullptr;          // optional second membership (0xffffffff none)
     uint64_t extra_members = 0;               // number of valid keys2 entries
