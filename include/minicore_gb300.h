@@ -91,6 +91,13 @@ const char *mc_version(void);
 const char *mc_last_error(void);
 /* Number of CUDA kernels this library has launched in this process (diagnostics). */
 uint64_t mc_kernel_launches(void);
+/* Test hook for the device-side failure path (no reference counterpart; the reference polls
+ * for interrupts on the host, clustering/solve.h:26-30): the next tensor-core assignment
+ * pass in this process makes its MMA issuer wait on a barrier that nothing completes.  The
+ * wait's bound (about one second) runs out, the kernel drains its copies in flight, frees
+ * its tensor memory and returns, and the call reports MC_ETIMEOUT; the context stays
+ * usable.  One shot: later passes run normally. */
+int mc_test_tc_stall_once(void);
 /* Phase profiler (diagnostics, off by default): CUDA events around the library's phases
  * (tensor-core passes, exact finalize, FP32/CSR assignment, centroid update, objective).
  * mc_profile_report writes {"phase": {"count": c, "ms": total}, ...} as JSON. */
@@ -334,7 +341,9 @@ int mc_autotune_report(char *json, uint64_t capacity);
  * call returns without waiting.  Its scratch (the centers transposed) lives in one fixed
  * device array of MC_NOALLOC_SCRATCH_FLOATS floats per GPU: kp * d must fit, kp being k
  * rounded up to a multiple of 64 (k < 128) or 128 (k >= 128), else MC_EINVAL.  The first
- * call on a device looks up that array's address, so make it before any stream capture.
+ * call on a device looks up that array's address (which may load the module holding it: a
+ * one-time 4 MiB), so make it before any stream capture; inside a capture it is refused.
+ * Pointers and stream must belong to the current device (another GPU's memory: MC_EINVAL).
  * All calls on a device share the array: calls that overlap on the GPU race. */
 int mc_assign_sqrl2_noalloc(const float *X, uint64_t n, uint64_t d, const float *centers, uint32_t k,
                             uint32_t *asn, double *costs, void *cuda_stream);

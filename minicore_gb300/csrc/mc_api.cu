@@ -55,6 +55,10 @@ int fail(int status, const std::string &msg) {
     return status;
 }
 
+// Memory the current device's kernels may read and write directly: managed memory, or
+// device memory of the current device.  Device memory of another GPU is not: a kernel
+// launched here would fault on it without peer access and silently cross the link with it,
+// so callers copy it like host memory (cudaMemcpyDefault moves it between GPUs).
 bool is_device_ptr(const void *p) {
     if (!p) return false;
     cudaPointerAttributes attr;
@@ -63,7 +67,29 @@ bool is_device_ptr(const void *p) {
         cudaGetLastError();
         return false;
     }
-    return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+    if (attr.type == cudaMemoryTypeManaged) return true;
+    if (attr.type != cudaMemoryTypeDevice) return false;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.device == dev;
+}
+
+bool is_foreign_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return attr.type == cudaMemoryTypeDevice && attr.device != dev;
 }
 
 // copy `bytes` from src (host or device) into a device buffer unless src already lives on
@@ -1089,6 +1115,10 @@ extern "C" {
 
 const char *mc_version(void) { return "minicore_gb300 0.1 (sm_103a)"; }
 uint64_t mc_kernel_launches(void) { return g_launches.load(); }
+int mc_test_tc_stall_once(void) {
+    tc_stall_next();
+    return MC_OK;
+}
 
 }  // extern "C"
 
@@ -1940,7 +1970,7 @@ static int distance_pass(mc_context *ctx, const mc_matrix *rows, const float *ce
     o.ldm = ldm;
     o.dmode = dmode;
     MC_TRY(job_assign_with(j, j->C.p, j->psum, true, &o));
-    if (D != out) MC_CUDA_TRY(cudaMemcpyAsync(out, D, out_count * sizeof(float), cudaMemcpyDeviceToHost, j->st));
+    if (D != out) MC_CUDA_TRY(cudaMemcpyAsync(out, D, out_count * sizeof(float), cudaMemcpyDefault, j->st));
     return sync(j->st);
 }
 

@@ -183,7 +183,10 @@ struct DBuf {
     }
 };
 
+// managed memory, or device memory of the current device
 bool is_device_ptr(const void *p);
+// device memory of a GPU other than the current one
+bool is_foreign_device_ptr(const void *p);
 
 // process-wide count of kernel launches issued by this library
 void note_launch();

@@ -34,6 +34,8 @@
 // flight, frees its TMEM and returns.
 #include <cuda.h>
 
+#include <atomic>
+
 #include <cmath>
 
 #include "mc_assign.cuh"
@@ -216,6 +218,7 @@ struct TcArgs {
     uint8_t *cnt;          // [rows][PARTS] pass 2: candidates per column part (255: too many)
     uint32_t *cand;        // [rows][PARTS][NCAND] pass 2: candidate centers
     int *err;
+    int stall_test;        // test hook: the MMA issuer first waits on a barrier nothing completes
 };
 
 enum TcMode { TC_TOP2 = 0, TC_CAND = 1 };
@@ -300,6 +303,10 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
             uint32_t s = 0, ph = 0;
             uint32_t acc_it = 0;
             bool ok = true;
+            // test hook (mc_test_tc_stall): `drain` completes only after this thread's own
+            // commit below, so this wait runs out its bound, sets the abort flag and error
+            // code 5, and every role then takes the bounded drain-and-return path
+            if (a.stall_test && !mbar_wait(&sm->drain, 0, sm, a.err, 5)) ok = false;
             for (uint32_t m = blockIdx.x; m < ntiles && ok; m += gridDim.x) {
                 for (uint32_t nc = 0; nc < a.nchunks && ok; ++nc, ++acc_it) {
                     const uint32_t buf = acc_it & 1, use = acc_it >> 1;
@@ -931,6 +938,10 @@ static int make_map(CUtensorMap *map, const void *ptr, bool tf32, uint64_t rows,
     return MC_OK;
 }
 
+// test hook: the next tensor-core pass 1 launched by this process stalls on purpose (one shot)
+static std::atomic<int> g_tc_stall_next{0};
+void tc_stall_next() { g_tc_stall_next.store(1); }
+
 int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
               int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
               uint64_t *recheck_count, bool graph_mode) {
@@ -1021,7 +1032,9 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     a.cnt = nullptr;
     a.cand = nullptr;
     a.err = s.err.p;
+    a.stall_test = 0;
     TcArgs a2 = a;  // pass 2: compact rows, count read on the device
+    a.stall_test = g_tc_stall_next.exchange(0);
     a2.n = cap;
     a2.count = s.count.p;
     a2.thrc = s.thrc.p;

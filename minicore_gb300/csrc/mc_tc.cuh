@@ -36,5 +36,7 @@ struct TcState {
 int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
               int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
               uint64_t *recheck_count, bool graph_mode = false);
+// test hook: the next tensor-core pass 1 waits on a barrier nothing completes (one shot)
+void tc_stall_next();
 
 }  // namespace mc

@@ -5,7 +5,7 @@ Reads (as text) the vectors that minicore's distance tests use:
   * src/tests/testmsr.cpp (large)    the `lhs` / `rhs` count vectors (d=26183) of the
     MKL / REVERSE_MKL positivity check; src/tests/testmsrcsr.cpp holds the same pair and is
     asserted to agree across sparse representations within 1e-5.
-Usage:  python tests/golden/make_golden.py [/path/to/minicore]
+Usage:  python tests/golden/make_golden.py /path/to/minicore   (or MINICORE_REFERENCE=/path/to/minicore)
 """
 import os
 import re
@@ -49,4 +49,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MINICORE_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <path to the minicore source tree> (or set MINICORE_REFERENCE)")
+    main(ref)

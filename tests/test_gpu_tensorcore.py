@@ -91,3 +91,30 @@ def test_tc_nan_rows(mc):
     assert np.array_equal(atc, a32)
     assert np.array_equal(ctc[np.isfinite(c32)], c32[np.isfinite(c32)])
     assert np.isnan(ctc[5]) == np.isnan(c32[5])
+
+
+def test_tc_bounded_wait_expires_and_context_survives(mc):
+    """The device failure path, without faulting anything: the test hook makes pass 1's MMA
+    issuer wait on a barrier that nothing completes.  Its bound (about one second) runs out,
+    the kernel drains its copies in flight, frees its tensor memory and returns; the call
+    reports MC_ETIMEOUT, and the next call on the same context gives the FP32 result."""
+    import time
+    from minicore_gb300 import _lib
+    lib = _lib.load()
+    X, C = _data(4096, 64, 256, seed=11)
+    a32, c32 = _assign(mc, X, C, "fp32")
+    M = mc._MatrixArg(X)
+    asn = np.empty(M.n, np.uint32)
+    costs = np.empty(M.n, np.float64)
+    assert lib.mc_test_tc_stall_once() == _lib.MC_OK
+    t0 = time.perf_counter()
+    rc = lib.mc_assign(mc.default_context().handle, M.ref, mc._p(C), C.shape[0], 2, 0.0, _lib.MC_BF16,
+                       mc._p(asn), mc._p(costs))
+    waited = time.perf_counter() - t0
+    assert rc == _lib.MC_ETIMEOUT, lib.mc_last_error()
+    assert b"bounded wait expired" in lib.mc_last_error()
+    assert waited < 30.0
+    for _ in range(2):  # the hook is one shot; the context is intact
+        atc, ctc = _assign(mc, X, C, "bf16")
+        assert np.array_equal(atc, a32)
+        assert np.array_equal(ctc, c32)
