@@ -1,17 +1,27 @@
 #!/usr/bin/env python3
-"""Benchmark: Lloyd iterations/s on the dense 4M x 128, k=1024 Gaussian-mixture workload.
+"""Benchmark: Lloyd iterations/s on the dense 4M x 128, k=1024 Gaussian-mixture workload,
+with one sub-line per other configuration of the clustering hot path.
 
-A step is one Lloyd iteration (centroid update + hard assignment) over all rows.
+A step of the headline is one Lloyd iteration (centroid update + hard assignment) over all
+4M rows in BF16 tensor-core form.
 
 * value: device-resident rows/centers (torch tensors handed to the C ABI), K steps timed
   with CUDA events on the library's stream, barrier + synchronize on both sides.  The rows
   (2 GiB f32 + 1 GiB bf16 copy) exceed the 129 MB L2, so no flush is needed between steps.
 * e2e: the reference-facing call (mc_hcluster through minicore_gb300.hcluster) with host
-  buffers in pinned memory: each step uploads the rows, runs kmeans++-seeded centers
-  through 10 Lloyd updates and reads back centers / assignments / costs.
-* roofline: the assignment kernel (the dominant launch), timed alone with CUDA events.
+  buffers in pinned memory: each call uploads the rows and runs 10 Lloyd updates from the
+  kmeans++ centers, then reads back centers / assignments / costs.  Copy bytes are given
+  per Lloyd iteration (one tenth of a call) and per call.
+* roofline: the assignment kernel (the dominant launch), from CUDA events around it.
 * cpu_baseline / --impl reference: the oracle (C++/OpenMP restatement of the reference's
-  CPU path) on a row sample, scaled to the full row count.
+  CPU path) on a 50,000-row sample, one assignment + one centroid update per iteration,
+  median of repeats, scaled to the full row count.  The in-line cpu_baseline runs the
+  reference arm itself in a child process (no GPU work, no torch threads beside it).
+* configs: the other workloads of the path, each measured in the same run with its own
+  roofline, CPU baseline, end-to-end call from host buffers, clocks and an FP64 accuracy
+  block: C1 (10,000 x 50, k = 25, whole hcluster calls), C2 (CSR 1M x 20,000, MKL and JSD,
+  k = 50), C3 in TF32, C4 (coreset pipeline on 2M x 64).  C5 (serving) runs a 1000-job
+  stream; `--workload serving` runs the full 20,000-job stream.
 """
 from __future__ import annotations
 
@@ -31,9 +41,11 @@ sys.path.insert(0, ROOT)
 
 N, D, K, COMPONENTS = 4_000_000, 128, 1024, 1024
 E2E_ITERS = 10
+CPU_SAMPLE = 50_000          # rows of the dense CPU-baseline sample
+CSR_D, CSR_NNZ_ROW, CSR_K = 20_000, 1500, 50
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -43,21 +55,25 @@ def parse():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "csr_l1", "serving", "coreset", "pcmp",
-                                                         "minibatch", "soft", "small", "coreset_mb"],
-                    help="dense: the 4M x 128 k=1024 Lloyd workload (the default line); csr_*: the sparse "
-                         "count-data workload (1M x 20000, 1500 nnz/row, k=50) assignment pass; serving: "
-                         "the Poisson job stream through the continuous-batching server; coreset: the "
-                         "2M x 64 kmeans++ -> sensitivity -> sampling -> weighted Lloyd pipeline")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the C1/C2/C3-TF32/C4 sub-lines of the default run")
+    ap.add_argument("--workload", default="dense", choices=["dense", "csr_mkl", "csr_jsd", "csr_l1", "serving", "coreset",
+                                                         "pcmp", "minibatch", "soft", "small", "coreset_mb", "tf32"],
+                    help="dense: the 4M x 128 k=1024 Lloyd workload with every config as a sub-line (the default "
+                         "line); csr_*: the sparse count-data workload (1M x 20000, 1500 nnz/row, k=50); serving: "
+                         "the Poisson job stream through the continuous-batching server; coreset: the 2M x 64 "
+                         "kmeans++ -> sensitivity -> sampling -> weighted Lloyd pipeline; small: 10000 x 50; "
+                         "tf32: the 4M x 128 workload in TF32")
     ap.add_argument("--coreset-rows", type=int, default=2_000_000)
-    ap.add_argument("--serving-jobs", type=int, default=4000,
+    ap.add_argument("--serving-jobs", type=int, default=20000,
                     help="jobs in the --workload serving stream (the full stream is 20000)")
     ap.add_argument("--serving-rate", type=float, default=200.0)
     ap.add_argument("--slots", type=int, default=8)
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the short serving run (p50/p99 job latency) in the default line")
     ap.add_argument("--csr-rows", type=int, default=1_000_000)
-    return ap.parse_args()
+    ap.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
+    return ap.parse_args(argv)
 
 
 def peaks():
@@ -67,6 +83,131 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+class Clocks:
+    """nvidia-smi sampling during a timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=2)
+        except Exception:
+            self.proc.kill()
+        s = [x for x in self.samples if len(x) >= 8]
+        if not s:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(x[0]) for x in s if x[0].replace(".", "").isdigit()]
+        mx = [float(x[1]) for x in s if x[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for x in s for i in range(4) if x[4 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(s)}
+
+
+def replica_throughput(ms_local, steps, world, device):
+    """Independent replicas (one per rank, no collective on the data path): the slowest
+    rank's time bounds the job, and every rank completed `steps` iterations.  Returns
+    (ms per step, whole-job iterations per second)."""
+    ms = float(ms_local)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / steps
+    return ms_per_step, world * 1000.0 / ms_per_step
+
+
+class Env:
+    """The library, a context and the non-default stream it launches on (CUDA events that
+    time a region are recorded on the same stream)."""
+
+    def __init__(self, device=0):
+        import torch
+        import minicore_gb300 as mc
+        from minicore_gb300 import _lib
+        torch.cuda.set_device(device)
+        self.torch, self.mc, self._lib = torch, mc, _lib
+        self.lib = _lib.load()
+        self.ctx = mc.Context(device)
+        self.stream = torch.cuda.Stream()
+        torch.cuda.set_stream(self.stream)
+        self.ctx.set_stream(self.stream.cuda_stream)
+
+    def event(self):
+        e = self.torch.cuda.Event(enable_timing=True)
+        e.record(self.stream)
+        return e
+
+    def timed(self, fn, steps, warmup=0, profile=False):
+        """warmup + steps calls of fn; returns (ms per call, kernel launches per call,
+        library phases {name: {count, ms}} over the timed calls, clocks)."""
+        torch, lib = self.torch, self.lib
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        clk = Clocks().start()
+        if profile:
+            lib.mc_profile_reset()
+            lib.mc_profile_enable(1)
+        l0 = lib.mc_kernel_launches()
+        e0 = self.event()
+        for _ in range(steps):
+            fn()
+        e1 = self.event()
+        torch.cuda.synchronize()
+        launches = int(lib.mc_kernel_launches() - l0)
+        clocks = clk.stop()
+        phases = {}
+        if profile:
+            lib.mc_profile_enable(0)
+            buf = ctypes.create_string_buffer(1 << 16)
+            self._lib.check(lib.mc_profile_report(buf, len(buf)))
+            phases = json.loads(buf.value.decode())
+        return e0.elapsed_time(e1) / steps, launches / max(steps, 1), phases, clocks
+
+    def free(self):
+        self.torch.cuda.synchronize()
+        self.torch.cuda.empty_cache()
+
+
+def kernel_ms(phases, *names):
+    """(ms per launch, launches) of the first phase present among `names`."""
+    for nm in names:
+        p = phases.get(nm)
+        if p and p.get("count"):
+            return p["ms"] / p["count"], p["count"]
+    return float("nan"), 0
+
+
+# ------------------------------------------------------------------------------------
+# synthetic inputs (seeded; the reference's benchmark datasets are not available)
+# ------------------------------------------------------------------------------------
 def make_data(n, seed=0):
     """1024 component means ~N(0, 4I), points ~N(mean, I) (seeded, generated on the GPU)."""
     import torch
@@ -78,7 +219,7 @@ def make_data(n, seed=0):
     return X.contiguous()
 
 
-def make_csr_counts(n, d=20_000, nnz_row=1500, seed=0, chunk=4096):
+def make_csr_counts(n, d=CSR_D, nnz_row=CSR_NNZ_ROW, seed=0, chunk=4096):
     """CSR count matrix: per row nnz_row distinct columns drawn by Zipf(1.1) rank weights
     without replacement (Gumbel top-k on the log weights, columns ranked by a seeded
     permutation); values negative binomial (mean 3, dispersion 0.5: r = 2) with zeros
@@ -112,10 +253,180 @@ def make_csr_counts(n, d=20_000, nnz_row=1500, seed=0, chunk=4096):
     return vals, idx, indptr
 
 
-def csr_bench(args):
-    """Sparse count workload: D^2 seeding (k=50) then the timed assignment pass (MKL or JSD,
-    prior 1) with rows resident in HBM; csr_l1: the timed step is one L1 Lloyd iteration
-    (sparse coordinate-wise medians of the clusters, then the L1 assignment pass)."""
+def make_coreset_data(n, d=64, comps=200, seed=0):
+    """200 means ~N(0, 4I); component weights ~Dirichlet(0.3); 2M points ~N(mean, I)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    wts = torch.from_numpy(rng.dirichlet(np.full(comps, 0.3))).cuda()
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    mu = torch.randn(comps, d, generator=g, device="cuda") * 2.0
+    lab = torch.multinomial(wts, n, replacement=True, generator=g)
+    return torch.randn(n, d, generator=g, device="cuda").add_(mu[lab]).contiguous()
+
+
+def make_small_data(seed=0):
+    """10,000 x 50: 25 centers ~U[-10, 10]^50, 400 points each ~N(center, I), shuffled."""
+    rng = np.random.default_rng(seed)
+    mu = rng.uniform(-10, 10, (25, 50))
+    return (mu[rng.integers(0, 25, 10000)] + rng.normal(size=(10000, 50))).astype(np.float32)
+
+
+def pinned_copy(t):
+    """A pinned host copy of a device tensor (the host buffers of the end-to-end calls)."""
+    import torch
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    return h
+
+
+# ------------------------------------------------------------------------------------
+# accuracy against FP64 (numpy / scipy in float64)
+# ------------------------------------------------------------------------------------
+def fp64_sqrl2_check(Xs, C, asn_s, costs_s):
+    """SQRL2 on a row sample: FP64 distances (||x||^2 - 2 x.c + ||c||^2 in float64) to the
+    same centers; the GPU's objective over the sample and its argmin agreement."""
+    Xs = np.asarray(Xs, np.float64)
+    C64 = np.asarray(C, np.float64)
+    cn = (C64 * C64).sum(1)
+    best = np.empty(len(Xs))
+    arg = np.empty(len(Xs), np.int64)
+    for i in range(0, len(Xs), 8192):
+        x = Xs[i:i + 8192]
+        dist = (x * x).sum(1)[:, None] - 2.0 * (x @ C64.T) + cn[None, :]
+        arg[i:i + 8192] = dist.argmin(1)
+        best[i:i + 8192] = np.maximum(dist.min(1), 0.0)
+    obj64 = float(best.sum())
+    obj_gpu = float(np.asarray(costs_s, np.float64).sum())
+    diff = np.nonzero(arg != asn_s)[0]
+    gap = 0.0
+    if len(diff):
+        xd = Xs[diff]
+        cd = C64[np.asarray(asn_s)[diff].astype(np.int64)]
+        gap = float((((xd - cd) ** 2).sum(1) - best[diff]).max())
+    return {"sample_rows": int(len(Xs)), "objective_gpu": obj_gpu, "objective_fp64": obj64,
+            "rel_err": abs(obj_gpu - obj64) / max(obj64, 1e-300),
+            "argmin_agreement": float(1.0 - len(diff) / max(len(Xs), 1)),
+            "max_fp64_gap_where_argmin_differs": gap}
+
+
+def fp64_objective_check(job, X, n, sample=100_000, seed=5):
+    """After the timed steps: the job's assignment and objective on a fixed row subsample
+    against FP64 distances with the same centers."""
+    import torch
+    k, d = job.k, X.shape[1]
+    C = np.empty((k, d), np.float32)
+    asn = np.empty(n, np.uint32)
+    costs = np.empty(n, np.float64)
+    job.read(C, asn, costs)
+    S = np.sort(np.random.default_rng(seed).choice(n, min(sample, n), replace=False))
+    Xs = X[torch.from_numpy(S).cuda()].cpu().numpy()
+    return fp64_sqrl2_check(Xs, C, asn[S], costs[S])
+
+
+def fp64_csr_distances(msr, sub, C):
+    """MKL or JSD (prior 1) between every sample row and every center in float64, through
+    identities that hold exactly in real arithmetic (prior 1: pv = 1, psum = d).  With
+    c~ = (c + 1) / (sum c + d) and p~ = (x + 1) / (sum x + d):
+      MKL:  KL(c~ || p~) = sum c~ log c~ - sum_{j in nz(x)} c~_j log(1 + x_j) + log(sum x + d)
+      JSD:  1/2 sum_j f(c~_j, p~_j), f(a, b) = a log a + b log b - (a + b) log((a + b) / 2), over
+            all columns: the zero columns take p~_j = r = 1 / (sum x + d), so the row's sum is
+            sum_j f(c~_j, r) + sum_{j in nz} [f(c~_j, p~_j) - f(c~_j, r)]."""
+    import scipy.sparse as sp
+    d = sub.shape[1]
+    C64 = np.asarray(C, np.float64)
+    ct = (C64 + 1.0) / (C64.sum(1, keepdims=True) + d)            # k x d
+    rs = np.asarray(sub.sum(1)).ravel().astype(np.float64)
+    if msr == 5:
+        H = (ct * np.log(ct)).sum(1)                                  # k
+        L = sp.csr_matrix((np.log1p(sub.data.astype(np.float64)), sub.indices, sub.indptr), shape=sub.shape) @ ct.T
+        out = H[None, :] - np.asarray(L) + np.log(rs + d)[:, None]
+        return np.maximum(out, 0.0)
+
+    def f(a, b):
+        return a * np.log(a) + b * np.log(b) - (a + b) * np.log((a + b) * 0.5)
+
+    out = np.empty((sub.shape[0], C64.shape[0]))
+    for i in range(sub.shape[0]):
+        b, e = sub.indptr[i], sub.indptr[i + 1]
+        cols = sub.indices[b:e]
+        r = 1.0 / (rs[i] + d)
+        p = (sub.data[b:e].astype(np.float64) + 1.0) * r
+        tot = f(ct, r).sum(1)
+        a = ct[:, cols]
+        tot += (f(a, p[None, :]) - f(a, r)).sum(1)
+        out[i] = 0.5 * tot
+    return np.maximum(out, 0.0)
+
+
+def csr_accuracy(msr, sub, C, asn_g, cost_g, oasn, ocost, fp64_rows):
+    """The GPU's assignment of a CSR row sample against the oracle (same FP32 arithmetic
+    as the reference, FT = float) and against FP64."""
+    oasn = np.asarray(oasn)
+    diff = np.nonzero(asn_g != oasn)[0]
+    rel = np.abs(cost_g - ocost) / np.maximum(np.abs(ocost), 1e-30)
+    out = {"oracle_sample_rows": int(sub.shape[0]),
+           "argmin_agreement_vs_oracle": float(1.0 - len(diff) / sub.shape[0]),
+           "max_rel_cost_diff_vs_oracle": float(rel.max()),
+           "disagreeing_rows": int(len(diff))}
+    if len(diff):
+        # the oracle's distance to the GPU's pick relative to its own best, at each disagreeing row
+        D64 = fp64_csr_distances(msr, sub[diff], C)
+        g = D64[np.arange(len(diff)), asn_g[diff].astype(np.int64)]
+        o = D64[np.arange(len(diff)), oasn[diff].astype(np.int64)]
+        out["fp64_margin_at_disagreements"] = [float((gi - oi) / max(abs(oi), 1e-30)) for gi, oi in zip(g, o)][:20]
+    S = min(fp64_rows, sub.shape[0])
+    D64 = fp64_csr_distances(msr, sub[:S], C)
+    best = D64.min(1)
+    arg = D64.argmin(1)
+    obj64 = float(best.sum())
+    objg = float(np.asarray(cost_g[:S], np.float64).sum())
+    dg = np.nonzero(arg != asn_g[:S])[0]
+    out.update({"fp64_sample_rows": int(S), "objective_gpu": objg, "objective_fp64": obj64,
+                "rel_err": abs(objg - obj64) / max(obj64, 1e-300),
+                "argmin_agreement": float(1.0 - len(dg) / S),
+                "max_fp64_rel_gap_where_argmin_differs":
+                    float(((D64[dg, asn_g[:S][dg].astype(np.int64)] - best[dg]) / np.maximum(best[dg], 1e-30)).max())
+                    if len(dg) else 0.0})
+    return out
+
+
+# ------------------------------------------------------------------------------------
+# CPU baseline (the oracle: the reference's CPU path restated, FT = float)
+# ------------------------------------------------------------------------------------
+def cpu_lloyd_iteration(X_sample, C, msr=2, prior=0.0, repeats=3):
+    """Seconds of one oracle Lloyd iteration (assignment + centroid update) on a sample:
+    the median over repeats of [assign, update, assign] minus the median of [assign]."""
+    import oracle
+    oracle.build()
+    ta, tc = [], []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        oracle.assign(X_sample, C, msr, prior)
+        ta.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.hcluster(X_sample, C, msr, prior, eps=0.0, maxiter=0, seed=1)
+        tc.append(time.perf_counter() - t0)
+    return float(np.median(tc) - np.median(ta)), float(np.median(ta))
+
+
+def cpu_reference_line(steps=5, warmup=1, sample=CPU_SAMPLE):
+    """The reference arm, run as a child process (no torch, no GPU in that process)."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", str(steps),
+           "--warmup", str(warmup), "--cpu-sample", str(sample)]
+    r = subprocess.run(cmd, capture_output=True, text=True, env={**os.environ, "RANK": "0", "WORLD_SIZE": "1"})
+    for line in r.stdout.splitlines()[::-1]:
+        if line.startswith("{"):
+            return json.loads(line)
+    return None
+
+
+# ------------------------------------------------------------------------------------
+# CSR L1 (prior 0)
+# ------------------------------------------------------------------------------------
+def csr_l1_bench(args):
+    """CSR L1 (prior 0) on the sparse count workload: D^2 seeding (k=50), then the timed
+    step is one L1 Lloyd iteration (sparse coordinate-wise medians of the clusters, then the
+    L1 assignment pass: the union walk over nonzero columns) with rows resident in HBM."""
     import torch
     import minicore_gb300 as mc
     from minicore_gb300 import _lib
@@ -254,127 +565,6 @@ def csr_bench(args):
                                "sample": f"oracle assignment of the first {S} rows against the same {k} centers, "
                                          f"scaled by {n}/{S}"}
     print(json.dumps(out))
-
-
-def coreset_bench(args):
-    """Coreset pipeline on 2M x 64 (200-component mixture, Dirichlet(0.3) component
-    weights): kmeans++ (k=100) -> LBK sensitivities + alias table -> 50,000 weighted draws
-    -> weighted Lloyd on the coreset -> full-data objective of the coreset centers, against
-    the objective of Lloyd on the full data from the same seeds.  Rows stay in HBM; every
-    stage is timed with CUDA events on the library's stream."""
-    import torch
-    import minicore_gb300 as mc
-    from minicore_gb300 import _lib
-    torch.cuda.set_device(0)
-    lib = _lib.load()
-    ctx = mc.Context(0)
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    ctx.set_stream(stream.cuda_stream)
-    n, d, k, m, comps = args.coreset_rows, 64, 100, 50_000, 200
-    rng = np.random.default_rng(0)
-    wts = torch.from_numpy(rng.dirichlet(np.full(comps, 0.3))).cuda()
-    g = torch.Generator(device="cuda").manual_seed(0)
-    mu = torch.randn(comps, d, generator=g, device="cuda") * 2.0
-    lab = torch.multinomial(wts, n, replacement=True, generator=g)
-    X = torch.randn(n, d, generator=g, device="cuda").add_(mu[lab]).contiguous()
-    del lab
-    M = mc._MatrixArg(X)
-    u = torch.from_numpy(mc.uniforms(77, k)).cuda()
-    ids = torch.empty(k, dtype=torch.int32, device="cuda")
-    asn = torch.empty(n, dtype=torch.int32, device="cuda")
-    costs = torch.empty(n, dtype=torch.float64, device="cuda")
-    cw = torch.empty(m, dtype=torch.float32, device="cuda")
-    cidx = torch.empty(m, dtype=torch.int64, device="cuda")
-    precision = args.precision
-
-    def ev():
-        e = torch.cuda.Event(enable_timing=True)
-        e.record(stream)
-        return e
-
-    def pipeline():
-        t = [ev()]
-        _lib.check(lib.mc_kmeanspp(ctx.handle, M.ref, k, 2, 0.0, None, mc._p(u), mc._p(ids), mc._p(asn),
-                                   mc._p(costs)))
-        t.append(ev())
-        h = ctypes.c_void_p()
-        _lib.check(lib.mc_sampler_create(ctx.handle, n, k, k, mc._p(costs), 1, mc._p(asn), None, 4, 0.0,
-                                         ctypes.byref(h)))
-        t.append(ev())
-        _lib.check(lib.mc_sampler_sample(h, m, 1234, 0, mc._p(cw), mc._p(cidx)))
-        t.append(ev())
-        lib.mc_sampler_destroy(h)
-        Xc = X[cidx].contiguous()
-        C0 = X[ids.long()].contiguous()
-        jc = mc.Job(Xc, C0, msr=2, weights=cw.double(), precision="fp32", seed=9, ctx=ctx)
-        jc.run(eps=1e-4, maxiter=20)
-        Cc = torch.empty((k, d), dtype=torch.float32, device="cuda")
-        jc.read(Cc, None, None)
-        t.append(ev())
-        # the coreset centers on the full data: one assignment pass + FP64 objective
-        jf = mc.Job(X, Cc, msr=2, precision=precision, seed=9, ctx=ctx)
-        jf.assign()
-        obj_core = jf.cost()
-        t.append(ev())
-        jc.close()
-        jf.close()
-        return t, obj_core, C0
-
-    for _ in range(max(args.warmup, 1)):
-        pipeline()
-    torch.cuda.synchronize()
-    clocks = Clocks()
-    clocks.start()
-    l0 = lib.mc_kernel_launches()
-    stage_ms = []
-    for _ in range(args.steps):
-        t, obj_core, C0 = pipeline()
-        torch.cuda.synchronize()
-        stage_ms.append([t[i].elapsed_time(t[i + 1]) for i in range(len(t) - 1)])
-    launches = int(lib.mc_kernel_launches() - l0)
-    clk = clocks.stop()
-    stage = np.mean(np.array(stage_ms), axis=0)
-    names = ["kmeanspp", "sensitivity_alias", "sample", "coreset_lloyd", "full_data_assign"]
-    total_ms = float(stage.sum())
-    # the full-data solution from the same seeds, for the objective ratio (untimed)
-    jfull = mc.Job(X, C0, msr=2, precision=precision, seed=9, ctx=ctx)
-    jfull.run(eps=1e-4, maxiter=20)
-    obj_full = jfull.cost()
-    jfull.close()
-    pk, pk_kind = peaks()
-    kmpp_bytes = k * n * d * 4 + k * n * 8 * 2
-    achieved = kmpp_bytes / (stage[0] * 1e-3) / 1e9
-    hbm = pk.get("hbm_gbs", 6800.0)
-    cpu = None
-    if not args.no_cpu:
-        import oracle
-        oracle.build()
-        S = 100_000
-        Xs = X[:S].cpu().numpy()
-        t0 = time.perf_counter()
-        oracle.kmeanspp(Xs, k, 2, 0.0, mc.uniforms(77, k))
-        per = (time.perf_counter() - t0) * (n / S)
-        cpu = {"value": 1.0 / per, "unit": "kmeans++ runs/s (k=100, 2M x 64)", "cores": os.cpu_count() or 1,
-               "kind": "port", "sample": f"oracle kmeans++ on {S} rows, k={k}, scaled by {n}/{S}"}
-    line = {"metric": "coreset pipelines/s 2M x 64 (kmeans++ k=100 -> LBK -> 50k draws -> weighted Lloyd)",
-            "value": 1000.0 / total_ms, "unit": "pipelines/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32" if precision == "fp32" else f"f32 ({precision} full-data assign)",
-            "data": "synthetic",
-            "config": {"workload": f"dense {n}x{d}, {comps} components N(0,4I) means, Dirichlet(0.3) weights; "
-                                   f"kmeans++ k={k}; LBK sensitivities; alias; m={m}; weighted Lloyd eps 1e-4 "
-                                   f"<= 20 updates", "l2": "rows 512 MB > L2"},
-            "stages_ms": dict(zip(names, map(float, stage))),
-            "objective": {"coreset_centers_on_full_data": obj_core, "full_data_lloyd": obj_full,
-                          "ratio": obj_core / obj_full},
-            "roofline": {"bound": "hbm", "kernel": "kmeans++ (k passes over the rows)", "achieved": achieved,
-                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-                         "peak_source": f"{pk_kind} hbm_gbs",
-                         "algorithmic": f"k*n*d*4 + 2*k*n*8 = {kmpp_bytes:.4g} bytes"},
-            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clk,
-            "e2e": None}
-    print(json.dumps(line))
 
 
 FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA x 2.07 GHz
@@ -693,132 +883,454 @@ def serving_main(args):
     print(json.dumps(line))
 
 
-class Clocks:
-    """nvidia-smi sampling during the timed region."""
-
-    def __init__(self):
-        self.samples = []
-        self.proc = None
-
-    def start(self):
+# ------------------------------------------------------------------------------------
+# C3: dense 4M x 128, k = 1024 (the headline in BF16; TF32 as a sub-line)
+# ------------------------------------------------------------------------------------
+def tc_roofline(phases, n, precision, pk, pk_kind):
+    """Pass 1 of the tensor-core assignment (every row x every center): 2 n k d FLOP per
+    launch against the measured BF16 burst peak (TF32: half of it, the tensor pipe's TF32
+    rate being half its BF16 rate)."""
+    flops = 2.0 * n * K * D
+    ms, launches = kernel_ms(phases, "tc_pass1_top2")
+    peak = pk.get("bf16_tflops", 1935.7) * (0.5 if precision == "tf32" else 1.0)
+    achieved = flops / (ms * 1e-3) / 1e12
+    traffic = None
+    if precision == "bf16" and n == N:
         try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
-        except Exception:
-            self.proc = None
-
-    def _read(self):
-        for line in self.proc.stdout:
-            self.samples.append([x.strip() for x in line.split(",")])
-
-    def stop(self):
-        if not self.proc:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        time.sleep(0.25)
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=2)
-        except Exception:
-            self.proc.kill()
-        s = [x for x in self.samples if len(x) >= 8]
-        if not s:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [float(x[0]) for x in s if x[0].replace(".", "").isdigit()]
-        mx = [float(x[1]) for x in s if x[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for x in s for i in range(4) if x[4 + i].lower().startswith("active")})
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(s)}
+            for line in open(os.path.join(ROOT, "profiles", "k_tc_assign_bf16_4Mx128_k1024.md")):
+                if line.startswith("traffic_bytes_per_launch_scaled_to_4M:"):
+                    traffic = float(line.split(":")[1].split()[0])
+        except OSError:
+            traffic = None
+    return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": traffic,
+            "peak_source": f"{pk_kind} bf16_tflops (burst)" + (" / 2 for TF32" if precision == "tf32" else ""),
+            "kernel": f"k_tc_assign<{precision}, TC_TOP2> (pass 1: every row x every center)",
+            "kernel_ms_per_launch": ms, "launches": launches,
+            "algorithmic": f"2*n*k*d = {flops:.4g} FLOP per launch (n={n}, k={K}, d={D})"}
 
 
-def replica_throughput(ms_local, steps, world, device):
-    """Independent replicas (one per rank, no collective on the data path): the slowest
-    rank's time bounds the job, and every rank completed `steps` iterations.  Returns
-    (ms per step, whole-job iterations per second)."""
-    ms = float(ms_local)
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64, device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_per_step = ms / steps
-    return ms_per_step, world * 1000.0 / ms_per_step
-
-
-def fp64_objective_check(job, X, n, sample=100_000, seed=5):
-    """After the timed steps: the job's assignment and objective on a fixed row subsample
-    against an FP64 computation (numpy, float64 GEMM form of the squared distances) with
-    the same centers."""
-    import torch
-    k, d = job.k, X.shape[1]
-    C = np.empty((k, d), np.float32)
-    asn = np.empty(n, np.uint32)
-    costs = np.empty(n, np.float64)
-    job.read(C, asn, costs)
-    S = np.sort(np.random.default_rng(seed).choice(n, min(sample, n), replace=False))
-    Xs = X[torch.from_numpy(S).cuda()].cpu().numpy().astype(np.float64)
-    C64 = C.astype(np.float64)
-    cn = (C64 * C64).sum(1)
-    best = np.empty(len(S))
-    arg = np.empty(len(S), np.int64)
-    for i in range(0, len(S), 8192):
-        x = Xs[i:i + 8192]
-        dist = (x * x).sum(1)[:, None] - 2.0 * (x @ C64.T) + cn[None, :]
-        arg[i:i + 8192] = dist.argmin(1)
-        best[i:i + 8192] = np.maximum(dist.min(1), 0.0)
-    obj64 = float(best.sum())
-    obj_gpu = float(costs[S].sum())
-    # the FP64 distance to the center the GPU picked, where the argmins differ
-    diff = np.nonzero(arg != asn[S])[0]
-    gap = 0.0
-    if len(diff):
-        xd = Xs[diff]
-        cd = C64[asn[S][diff].astype(np.int64)]
-        gap = float((((xd - cd) ** 2).sum(1) - best[diff]).max())
-    return {"sample_rows": int(len(S)), "objective_gpu": obj_gpu, "objective_fp64": obj64,
-            "rel_err": abs(obj_gpu - obj64) / obj64, "argmin_agreement": float(1.0 - len(diff) / len(S)),
-            "max_fp64_gap_where_argmin_differs": gap}
-
-
-def cpu_baseline(X_sample, C, threads):
-    """One Lloyd iteration (assignment + centroid update) of the oracle on a row sample."""
-    import oracle
-    oracle.build()
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+def dense_e2e(E, X, C0, precision, calls):
+    """hcluster from pinned host rows: each call uploads the rows, runs 10 Lloyd updates and
+    copies centers, assignments and costs back."""
+    mc, torch = E.mc, E.torch
+    n = X.shape[0]
+    Xh = pinned_copy(X)
+    Ch = C0.cpu().numpy()
+    mc.hcluster(Xh, Ch, msr=2, eps=0.0, maxiter=1, precision=precision, ctx=E.ctx)  # warm
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    oracle.hcluster(X_sample, C, 2, 0.0, eps=0.0, maxiter=0, seed=1)  # assign, update, assign
+    iters = 0
+    for _ in range(calls):
+        r = mc.hcluster(Xh, Ch, msr=2, eps=0.0, maxiter=E2E_ITERS - 1, precision=precision, ctx=E.ctx)
+        iters += int(r["numiter"])
     t = time.perf_counter() - t0
-    # two assignment passes + one centroid update; a Lloyd iteration is one of each
-    per_iter = t / 2.0
-    return per_iter
+    del Xh
+    h2d = int(n * D * 4 + K * D * 4)
+    d2h = int(K * D * 4 + n * 4 + n * 8)
+    per_iter = iters / calls
+    return {"value": iters / t, "unit": "iters/s", "h2d_bytes_per_step": int(h2d / per_iter),
+            "d2h_bytes_per_step": int(d2h / per_iter), "h2d_bytes_per_call": h2d, "d2h_bytes_per_call": d2h,
+            "iters_per_call": per_iter, "calls": calls,
+            "call": f"minicore_gb300.hcluster(pinned host rows, maxiter={E2E_ITERS - 1}, eps=0, precision={precision})",
+            "step": "one Lloyd iteration; copy bytes per step = per-call bytes / iterations per call"}
 
 
+def dense_job_line(E, X, C0, precision, steps, warmup):
+    """Device-resident Lloyd steps of one job (rows, centers, assignments stay in HBM)."""
+    mc = E.mc
+    job = mc.Job(X, C0, msr=2, precision=precision, seed=7, ctx=E.ctx)
+    job.assign()
+    ms, launches, phases, clk = E.timed(job.lloyd_step, steps, warmup, profile=True)
+    return job, ms, launches, phases, clk
+
+
+def c3_tf32(args, E, X, C0, fp32_iters):
+    """C3 in TF32: the same rows and kmeans++ centers as the BF16 headline."""
+    n = X.shape[0]
+    steps = max(3, min(args.steps, 10))
+    job, ms, launches, phases, clk = dense_job_line(E, X, C0, "tf32", steps, max(args.warmup, 3))
+    pk, pk_kind = peaks()
+    out = {"metric": "Lloyd iters/s 4M x128 k=1024 (TF32 tensor-core assignment)", "value": 1000.0 / ms,
+           "unit": "iters/s", "ms_per_step": ms, "steps": steps, "dtype": "tf32",
+           "config": {"workload": f"dense {n}x{D}, {COMPONENTS} components, SQRL2, k={K}, kmeans++ centers "
+                                  f"(the headline's), Lloyd iteration", "precision": "tf32"},
+           "speedup_vs_fp32_gpu": (1000.0 / ms / fp32_iters) if fp32_iters else None,
+           "recheck_rows_last_pass": job.recheck_count(),
+           "accuracy_vs_fp64": fp64_objective_check(job, X, n),
+           "roofline": tc_roofline(phases, n, "tf32", pk, pk_kind), "phases_ms_timed_region": phases,
+           "gpu_launches": int(launches * steps), "clocks": clk}
+    job.close()
+    E.free()
+    out["e2e"] = None if args.no_e2e else dense_e2e(E, X, C0, "tf32", 1)
+    return out
+
+
+# ------------------------------------------------------------------------------------
+# C1: dense 10,000 x 50, k = 25, kmeans++ then 20 Lloyd updates, whole calls from host
+# ------------------------------------------------------------------------------------
+def c1_small(args):
+    import torch
+    import minicore_gb300 as mc
+    X = make_small_data(0)
+    ids, _, _ = mc.kmeanspp(X, 25, msr=2, seed=42)
+    C0 = X[ids.astype(np.int64)]
+    out, res = {}, {}
+    steps = max(args.steps, 5)
+    modes = {"graph": mc.LOOP_GRAPH, "fused": mc.LOOP_FUSED, "host": mc.LOOP_HOST}
+    clk = Clocks().start()
+    for name, mode in modes.items():
+        mc.loop_mode(mode)
+        for _ in range(max(args.warmup, 3)):
+            mc.hcluster(X, C0, msr=2, eps=0.0, maxiter=19, seed=3)
+        torch.cuda.synchronize()
+        l0 = mc.kernel_launches()
+        t = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            r = mc.hcluster(X, C0, msr=2, eps=0.0, maxiter=19, seed=3)
+            t.append((time.perf_counter() - t0) * 1e3)
+        res[name] = r
+        t = np.sort(np.array(t))
+        out[name] = {"ms_per_call_p50": float(np.percentile(t, 50)), "ms_per_call_min": float(t[0]),
+                     "updates": int(r["numiter"]), "launches_per_call": (mc.kernel_launches() - l0) / steps}
+    clocks = clk.stop()
+    mc.loop_mode(mc.LOOP_AUTO)
+    same = all(np.array_equal(res[m][key], res["host"][key]) and res[m]["finalcost"] == res["host"]["finalcost"]
+               for m in ("graph", "fused") for key in ("asn", "costs", "centers"))
+    best = min(out, key=lambda m: out[m]["ms_per_call_p50"])
+    g = out[best]
+    r = res[best]
+    acc = fp64_sqrl2_check(X, r["centers"], r["asn"], r["costs"].astype(np.float64))
+    acc["finalcost_gpu"] = r["finalcost"]
+    acc["finalcost_rel_err_vs_fp64"] = abs(r["finalcost"] - acc["objective_fp64"]) / acc["objective_fp64"]
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        tt = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            oracle.hcluster(X, C0, 2, 0.0, eps=0.0, maxiter=19, seed=3)
+            tt.append(time.perf_counter() - t0)
+        cpu = {"value": 1.0 / float(np.median(tt)), "unit": "calls/s", "cores": os.cpu_count() or 1,
+               "kind": "port", "sample": "the whole oracle hcluster (20 updates) on the same 10000 x 50 rows and "
+                                         "seeds, median of 5"}
+    per_call = g["ms_per_call_p50"] * 1e-3
+    return {"metric": "hcluster calls/s 10000x50 k=25 (20 updates, host arrays in and out)",
+            "value": 1.0 / per_call, "unit": "calls/s", "loop_mode": best,
+            "lloyd_iters_per_s": g["updates"] / per_call, "modes": out, "identical_across_modes": bool(same),
+            "steps": steps, "dtype": "f32",
+            "config": {"workload": "10000x50, 25 components U[-10,10]^50 sigma 1, k=25, kmeans++ seeds, "
+                                   "maxiter=19 (20 updates), eps=0"},
+            "roofline": {"bound": "launch latency", "achieved": g["launches_per_call"] / per_call,
+                         "unit": "kernel launches/s", "peak": None, "frac": None, "traffic": None,
+                         "note": f"{g['launches_per_call']:.0f} launches of a few microseconds per call; "
+                                 "rows (2 MB) and centers sit in L2"},
+            "accuracy_vs_fp64": acc, "cpu_baseline": cpu, "gpu_launches": int(g["launches_per_call"] * steps),
+            "clocks": clocks,
+            "e2e": {"value": 1.0 / per_call, "unit": "calls/s", "h2d_bytes_per_step": int(X.nbytes + C0.nbytes),
+                    "d2h_bytes_per_step": int(C0.nbytes + X.shape[0] * (4 + 4)),
+                    "call": "minicore_gb300.hcluster(host numpy rows and centers, maxiter=19, eps=0)"}}
+
+
+# ------------------------------------------------------------------------------------
+# C2: CSR 1M x 20,000, ~1500 nonzeros per row, MKL and JSD (prior 1), k = 50
+# ------------------------------------------------------------------------------------
+class CsrData:
+    def __init__(self, n, seed=0):
+        import torch
+        self.n, self.d = n, CSR_D
+        self.vals, self.idx, self.indptr = make_csr_counts(n, CSR_D, seed=seed)
+        torch.cuda.synchronize()
+        self.nnz = int(self.vals.numel())
+        self.ipc = self.indptr.cpu()
+
+    def device_matrix(self, mc):
+        return mc.CSparseMatrix(data=self.vals, indices=self.idx, indptr=self.indptr, shape=(self.n, self.d))
+
+    def sample(self, S):
+        import scipy.sparse as sp
+        ip = self.ipc[:S + 1].numpy().astype(np.int64)
+        e = int(ip[-1])
+        return sp.csr_matrix((self.vals[:e].cpu().numpy(), self.idx[:e].cpu().numpy().astype(np.int64), ip),
+                             shape=(S, self.d))
+
+    def centers_from_ids(self, ids):
+        import torch
+        C = torch.zeros((len(ids), self.d), dtype=torch.float32, device="cuda")
+        for c, r in enumerate(ids):
+            b, e = int(self.ipc[r]), int(self.ipc[r + 1])
+            C[c, self.idx[b:e].long()] = self.vals[b:e]
+        return C
+
+
+def c2_csr(args, E, data, msr):
+    """Sparse count workload, MKL (5) or JSD (4), prior 1, k = 50: D^2 seeding, then Lloyd
+    iterations with rows resident in HBM.  The roofline is that of the assignment kernel:
+    MKL against HBM (bytes), JSD against the measured logf rate (two logf per nonzero and
+    center)."""
+    import torch
+    mc, _lib, lib = E.mc, E._lib, E.lib
+    n, d, k, prior = data.n, data.d, CSR_K, 1.0
+    name = {5: "MKL", 4: "JSD"}[msr]
+    A = data.device_matrix(mc)
+    M = mc._MatrixArg(A)
+    u = torch.from_numpy(mc.uniforms(99, k)).cuda()
+    ids = torch.empty(k, dtype=torch.int32, device="cuda")
+    asn = torch.empty(n, dtype=torch.int32, device="cuda")
+    costs = torch.empty(n, dtype=torch.float64, device="cuda")
+
+    def seed():
+        _lib.check(lib.mc_kmeanspp(E.ctx.handle, M.ref, k, msr, prior, None, mc._p(u), mc._p(ids), mc._p(asn),
+                                   mc._p(costs)))
+    kmpp_ms, _, _, _ = E.timed(seed, 1, 1)
+    id_list = ids.cpu().tolist()
+    C = data.centers_from_ids(id_list)
+    del asn, costs
+    job = mc.Job(A, C, msr=msr, prior=prior, ctx=E.ctx)
+    job.assign()
+    steps = max(3, min(args.steps, 10 if msr == 5 else 5))
+    ms, launches, phases, clk = E.timed(job.lloyd_step, steps, max(args.warmup, 2) if msr == 5 else 2, profile=True)
+    kms, kl = kernel_ms(phases, "assign_csr_sparse", "assign_csr_tiled")
+    pk, pk_kind = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    algo_bytes = data.nnz * 8 + (n + 1) * 8 + n * 8 + n * 12 + k * d * 4
+    if msr == 5:
+        ach = algo_bytes / (kms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": None, "peak_source": f"{pk_kind} hbm_gbs",
+                "kernel": "k_assign_sparse_pair<MKL> (sparse dot over each row's nonzeros, all centers)",
+                "kernel_ms_per_launch": kms, "launches": kl,
+                "algorithmic": f"nnz*8 + (n+1)*8 + n*20 + k*d*4 = {algo_bytes:.4g} bytes per launch"}
+    else:
+        rate = ctypes.c_double()
+        _lib.check(lib.mc_diag_logf_rate(0, ctypes.byref(rate)))
+        logs = 2.0 * data.nnz * k
+        ach = logs / (kms * 1e-3)
+        roof = {"bound": "logf (FP32 pipe)", "achieved": ach / 1e12, "peak": rate.value / 1e12, "unit": "Tlogf/s",
+                "frac": ach / rate.value, "traffic": None,
+                "peak_source": "measured: mc_diag_logf_rate (independent logf chains, full occupancy)",
+                "kernel": "k_assign_sparse<JSD> (row groups by zero-entry value + sparse dot)",
+                "kernel_ms_per_launch": kms, "launches": kl,
+                "algorithmic": f"2*nnz*k = {logs:.4g} logf per launch",
+                "hbm_frac_for_reference": algo_bytes / (kms * 1e-3) / 1e9 / hbm}
+    # accuracy: the GPU's final assignment of a row sample against the oracle (the
+    # reference's FP32 arithmetic) and against FP64
+    Ch = np.empty((k, d), np.float32)
+    asn_h = np.empty(n, np.uint32)
+    cost_h = np.empty(n, np.float64)
+    job.read(Ch, asn_h, cost_h)
+    job.close()
+    E.free()
+    S = 20_000 if msr == 5 else 8_000
+    sub = data.sample(S)
+    acc = cpu = None
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        t0 = time.perf_counter()
+        oasn, ocost = oracle.assign(sub, Ch, msr, prior)
+        t_assign = time.perf_counter() - t0
+        acc = csr_accuracy(msr, sub, Ch, asn_h[:S], cost_h[:S], oasn, ocost, 2000 if msr == 5 else 200)
+        t0 = time.perf_counter()
+        oracle.hcluster(sub, Ch, msr, prior, eps=0.0, maxiter=0, seed=1)   # assign, update, assign
+        t_iter = (time.perf_counter() - t0) - t_assign
+        cpu = {"value": 1.0 / (t_iter * n / S), "unit": "iters/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"oracle Lloyd iteration (union-walk assignment + CSR centroid update) of the first {S} "
+                         f"rows against the same {k} centers, scaled by {n}/{S}",
+               "assign_passes_per_s": 1.0 / (t_assign * n / S)}
+    e2e = None
+    if not args.no_e2e:
+        vh, ih, ph = pinned_copy(data.vals), pinned_copy(data.idx), pinned_copy(data.indptr)
+        Ah = mc.CSparseMatrix(data=vh, indices=ih, indptr=ph, shape=(n, d))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ids_e, _, _ = mc.kmeanspp(Ah, k, msr=msr, prior=prior, seed=99, ctx=E.ctx)
+        t_seed = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r = mc.hcluster(Ah, ids_e.astype(np.int64), msr=msr, prior=prior, eps=0.0, maxiter=E2E_ITERS - 1,
+                        ctx=E.ctx)
+        t_run = time.perf_counter() - t0
+        it = int(r["numiter"])
+        h2d = data.nnz * 8 + (n + 1) * 8
+        e2e = {"value": it / t_run, "unit": "iters/s", "h2d_bytes_per_step": int(h2d / max(it, 1)),
+               "d2h_bytes_per_step": int((k * d * 4 + n * 12) / max(it, 1)), "h2d_bytes_per_call": int(h2d),
+               "iters_per_call": it, "kmeanspp_s_from_host": t_seed,
+               "same_seeds_as_device_run": bool(np.array_equal(ids_e.astype(np.int64), np.array(id_list))),
+               "call": f"minicore_gb300.hcluster(pinned host CSR, kmeans++ row ids, msr={msr}, prior=1, "
+                       f"maxiter={E2E_ITERS - 1}, eps=0)",
+               "step": "one Lloyd iteration; copy bytes per step = per-call bytes / iterations per call"}
+        del vh, ih, ph, Ah
+    return {"metric": f"CSR {name} Lloyd iters/s 1Mx20000 k=50 (rows resident)", "value": 1000.0 / ms,
+            "unit": "iters/s", "ms_per_step": ms, "steps": steps, "dtype": "f32",
+            "assign_ms_per_pass": kms, "kmeanspp_ms": kmpp_ms,
+            "config": {"workload": f"CSR {n}x{d}, {CSR_NNZ_ROW} nnz/row Zipf(1.1) columns, NB(3,0.5) counts, "
+                                   f"msr={msr} ({name}), prior=1, k={k}, kmeans++ centers, Lloyd iteration",
+                       "l2": "rows 12 GB > L2"},
+            "roofline": roof, "phases_ms_timed_region": phases, "accuracy": acc, "cpu_baseline": cpu,
+            "gpu_launches": int(launches * steps), "clocks": clk, "e2e": e2e}
+
+
+# ------------------------------------------------------------------------------------
+# C4: coreset pipeline on 2M x 64
+# ------------------------------------------------------------------------------------
+def c4_coreset(args, E):
+    """kmeans++ (k=100) -> LBK sensitivities + alias table -> 50,000 weighted draws ->
+    weighted Lloyd on the coreset -> full-data objective of the coreset centers, against
+    the objective of Lloyd on the full data from the same seeds.  Rows stay in HBM; every
+    stage is timed with CUDA events on the library's stream."""
+    torch, mc, _lib, lib = E.torch, E.mc, E._lib, E.lib
+    n, d, k, m = args.coreset_rows, 64, 100, 50_000
+    X = make_coreset_data(n, d)
+    M = mc._MatrixArg(X)
+    u = torch.from_numpy(mc.uniforms(77, k)).cuda()
+    ids = torch.empty(k, dtype=torch.int32, device="cuda")
+    asn = torch.empty(n, dtype=torch.int32, device="cuda")
+    costs = torch.empty(n, dtype=torch.float64, device="cuda")
+    cw = torch.empty(m, dtype=torch.float32, device="cuda")
+    cidx = torch.empty(m, dtype=torch.int64, device="cuda")
+    precision = "bf16"
+    keep = {}
+
+    def pipeline():
+        t = [E.event()]
+        _lib.check(lib.mc_kmeanspp(E.ctx.handle, M.ref, k, 2, 0.0, None, mc._p(u), mc._p(ids), mc._p(asn),
+                                   mc._p(costs)))
+        t.append(E.event())
+        h = ctypes.c_void_p()
+        _lib.check(lib.mc_sampler_create(E.ctx.handle, n, k, k, mc._p(costs), 1, mc._p(asn), None, 4, 0.0,
+                                         ctypes.byref(h)))
+        t.append(E.event())
+        _lib.check(lib.mc_sampler_sample(h, m, 1234, 0, mc._p(cw), mc._p(cidx)))
+        t.append(E.event())
+        lib.mc_sampler_destroy(h)
+        Xc = X[cidx].contiguous()
+        C0 = X[ids.long()].contiguous()
+        jc = mc.Job(Xc, C0, msr=2, weights=cw.double(), precision="fp32", seed=9, ctx=E.ctx)
+        jc.run(eps=1e-4, maxiter=20)
+        Cc = torch.empty((k, d), dtype=torch.float32, device="cuda")
+        jc.read(Cc, None, None)
+        t.append(E.event())
+        jf = mc.Job(X, Cc, msr=2, precision=precision, seed=9, ctx=E.ctx)
+        jf.assign()
+        keep["obj"] = jf.cost()
+        t.append(E.event())
+        jc.close()
+        keep["jf"], keep["C0"], keep["Cc"] = jf, C0, Cc
+        return t
+
+    for _ in range(max(args.warmup, 1)):
+        pipeline()
+        keep["jf"].close()
+    torch.cuda.synchronize()
+    clk = Clocks().start()
+    l0 = lib.mc_kernel_launches()
+    stage_ms = []
+    steps = max(3, min(args.steps, 10))
+    for s in range(steps):
+        t = pipeline()
+        torch.cuda.synchronize()
+        stage_ms.append([t[i].elapsed_time(t[i + 1]) for i in range(len(t) - 1)])
+        if s + 1 < steps:
+            keep["jf"].close()
+    launches = int(lib.mc_kernel_launches() - l0)
+    clocks = clk.stop()
+    stage = np.mean(np.array(stage_ms), axis=0)
+    names = ["kmeanspp", "sensitivity_alias", "sample", "coreset_lloyd", "full_data_assign"]
+    total_ms = float(stage.sum())
+    acc = fp64_objective_check(keep["jf"], X, n)
+    keep["jf"].close()
+    jfull = mc.Job(X, keep["C0"], msr=2, precision=precision, seed=9, ctx=E.ctx)
+    jfull.run(eps=1e-4, maxiter=20)
+    obj_full = jfull.cost()
+    jfull.close()
+    pk, pk_kind = peaks()
+    kmpp_bytes = k * n * d * 4 + k * n * 8 * 2
+    achieved = kmpp_bytes / (stage[0] * 1e-3) / 1e9
+    hbm = pk.get("hbm_gbs", 6800.0)
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        S = 200_000
+        Xs = X[:S].cpu().numpy()
+        tt = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            oracle.kmeanspp(Xs, k, 2, 0.0, mc.uniforms(77, k))
+            tt.append(time.perf_counter() - t0)
+        per = float(np.median(tt)) * (n / S)
+        cpu = {"value": 1.0 / per, "unit": "kmeans++ runs/s (k=100, 2M x 64)", "cores": os.cpu_count() or 1,
+               "kind": "port", "sample": f"oracle kmeans++ on {S} rows, k={k}, median of 3, scaled by {n}/{S}",
+               "gpu_kmeanspp_runs_per_s": 1000.0 / float(stage[0])}
+    e2e = None
+    if not args.no_e2e:
+        Xh = pinned_copy(X)
+        t0 = time.perf_counter()
+        ids_e, asn_e, cost_e = mc.kmeanspp(Xh, k, msr=2, seed=77, ctx=E.ctx)
+        cs = mc.CoresetSampler(ctx=E.ctx)
+        cs.make_sampler(k, cost_e.astype(np.float64), asn_e.astype(np.uint32), seed=13, sens=4)
+        wts, idx = cs.sample(m, seed=1234)
+        Xc = Xh[torch.from_numpy(idx.astype(np.int64))]
+        r = mc.hcluster(Xc, Xh[torch.from_numpy(ids_e.astype(np.int64))], msr=2, weights=wts.astype(np.float64),
+                        eps=1e-4, maxiter=20, seed=9, ctx=E.ctx)
+        jf = mc.Job(Xh, r["centers"], msr=2, precision=precision, seed=9, ctx=E.ctx)
+        jf.assign()
+        obj_e = jf.cost()
+        jf.close()
+        t_e = time.perf_counter() - t0
+        e2e = {"value": 1.0 / t_e, "unit": "pipelines/s", "h2d_bytes_per_step": int(2 * n * d * 4 + m * d * 4),
+               "d2h_bytes_per_step": int(n * 12 + m * 12 + k * d * 4),
+               "call": "minicore_gb300.kmeanspp -> CoresetSampler.make_sampler(sens=LBK)/sample -> hcluster("
+                       "weighted coreset) -> Job(full rows).assign/cost, all from pinned host rows",
+               "objective_coreset_centers_on_full_data": obj_e}
+        del Xh
+    E.free()
+    return {"metric": "coreset pipelines/s 2M x 64 (kmeans++ k=100 -> LBK -> 50k draws -> weighted Lloyd)",
+            "value": 1000.0 / total_ms, "unit": "pipelines/s", "ms_per_step": total_ms, "steps": steps,
+            "dtype": "f32 (bf16 full-data assignment)",
+            "config": {"workload": f"dense {n}x{d}, 200 components N(0,4I) means, Dirichlet(0.3) weights; "
+                                   f"kmeans++ k={k}; LBK sensitivities; alias; m={m}; weighted Lloyd eps 1e-4 "
+                                   f"<= 20 updates", "l2": "rows 512 MB > L2"},
+            "stages_ms": dict(zip(names, map(float, stage))),
+            "objective": {"coreset_centers_on_full_data": keep["obj"], "full_data_lloyd": obj_full,
+                          "ratio": keep["obj"] / obj_full},
+            "accuracy_vs_fp64": acc,
+            "roofline": {"bound": "hbm", "kernel": "kmeans++ (k passes over the rows)", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_source": f"{pk_kind} hbm_gbs",
+                         "algorithmic": f"k*n*d*4 + 2*k*n*8 = {kmpp_bytes:.4g} bytes"},
+            "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks, "e2e": e2e}
+
+
+# ------------------------------------------------------------------------------------
+# the reference arm: the oracle's CPU Lloyd iteration on the headline workload
+# ------------------------------------------------------------------------------------
 def reference_arm(args):
-    """--impl reference: the oracle's CPU Lloyd iteration, all host threads, on a sample."""
+    """--impl reference: the oracle's CPU Lloyd iteration (one assignment + one centroid
+    update, FT = float), all host threads, on a sample of the 4M x 128 mixture, scaled to
+    the full row count; W warm-up iterations, then the median of K."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle
+    oracle.build()
     rng = np.random.default_rng(0)
-    S = 20_000
+    S = args.cpu_sample
     mu = rng.normal(size=(COMPONENTS, D)) * 2.0
     Xs = (mu[rng.integers(0, COMPONENTS, S)] + rng.normal(size=(S, D))).astype(np.float32)
     C = Xs[rng.choice(S, K, replace=False)]
     for _ in range(args.warmup):
-        pass
+        oracle.hcluster(Xs, C, 2, 0.0, eps=0.0, maxiter=0, seed=1)
     times = []
     for _ in range(max(args.steps, 1)):
-        times.append(cpu_baseline(Xs, C, threads))
-    per_iter_full = float(np.mean(times)) * (args.n / S)
+        t_iter, _ = cpu_lloyd_iteration(Xs, C, repeats=1)
+        times.append(t_iter)
+    per_iter_full = float(np.median(times)) * (args.n / S)
     v = 1.0 / per_iter_full
+    spread = (max(times) - min(times)) / float(np.median(times))
     line = {"metric": "Lloyd iters/s 4M x128 k=1024", "value": v, "unit": "iters/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter_full * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -826,62 +1338,16 @@ def reference_arm(args):
             "config": {"workload": f"dense {args.n}x{D} gaussian mixture, SQRL2, k={K}, Lloyd iteration",
                        "sample_rows": S},
             "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
-                             "sample": f"{S} rows x k={K} (one assignment + centroid update), scaled by {args.n}/{S}"},
+                             "sample": f"{S} rows x k={K}: one assignment + one centroid update of the oracle per "
+                                       f"iteration (median of {len(times)}, spread {spread:.2%}), scaled by "
+                                       f"{args.n}/{S}"},
             "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def small_bench(args):
-    """The small reference configuration (10,000 x 50, 25 Gaussian components ~U[-10, 10]^50,
-    unit variance): kmeans++ (k = 25) then hcluster(maxiter=19, eps=0), i.e. 20 updates, from
-    host NumPy arrays through the public API.  Timed per whole call, with the Lloyd loop as one
-    CUDA graph and as a host loop (identical results, checked)."""
-    import time
-    import torch
-    import minicore_gb300 as mc
-    rng = np.random.default_rng(0)
-    mu = rng.uniform(-10, 10, (25, 50))
-    X = (mu[rng.integers(0, 25, 10000)] + rng.normal(size=(10000, 50))).astype(np.float32)
-    ids, _, _ = mc.kmeanspp(X, 25, msr=2, seed=42)
-    C0 = X[ids.astype(np.int64)]
-    out = {}
-    res = {}
-    modes = {"graph": mc.LOOP_GRAPH, "fused": mc.LOOP_FUSED, "host": mc.LOOP_HOST}
-    for name, mode in modes.items():
-        mc.loop_mode(mode)
-        for _ in range(args.warmup):
-            mc.hcluster(X, C0, msr=2, eps=0.0, maxiter=19, seed=3)
-        torch.cuda.synchronize()
-        l0 = mc.kernel_launches()
-        t = []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            r = mc.hcluster(X, C0, msr=2, eps=0.0, maxiter=19, seed=3)
-            t.append((time.perf_counter() - t0) * 1e3)
-        res[name] = r
-        t = np.sort(np.array(t))
-        out[name] = {"ms_per_call_p50": float(np.percentile(t, 50)), "ms_per_call_min": float(t[0]),
-                     "updates": int(r["numiter"]), "launches_per_call": (mc.kernel_launches() - l0) / args.steps}
-    mc.loop_mode(mc.LOOP_AUTO)
-    same = all(np.array_equal(res[m][key], res["host"][key]) and res[m]["finalcost"] == res["host"]["finalcost"]
-               for m in ("graph", "fused") for key in ("asn", "costs", "centers"))
-    best = min(out, key=lambda m: out[m]["ms_per_call_p50"])
-    g = out[best]
-    cpu = None
-    if not args.no_cpu:
-        import oracle
-        t0 = time.perf_counter()
-        oracle.hcluster(X, C0, 2, 0.0, eps=0.0, maxiter=19, seed=3)
-        cpu = {"value": 1.0 / (time.perf_counter() - t0), "unit": "calls/s", "cores": os.cpu_count() or 1,
-               "kind": "port", "sample": "the whole oracle hcluster on the same 10000 x 50 rows and seeds"}
-    print(json.dumps({"metric": "hcluster calls/s 10000x50 k=25 (20 updates, host arrays in and out)",
-                      "value": 1000.0 / g["ms_per_call_p50"], "unit": "calls/s", "loop_mode": best,
-                      "lloyd_iters_per_s": g["updates"] * 1000.0 / g["ms_per_call_p50"],
-                      "modes": out, "identical": bool(same), "cpu_baseline": cpu,
-                      "steps": args.steps, "warmup": args.warmup, "dtype": "f32", "data": "synthetic",
-                      "config": {"workload": "10000x50, 25 components, k=25, kmeans++ seeds, maxiter=19, eps=0"}}))
-
-
+# ------------------------------------------------------------------------------------
+# the default line
+# ------------------------------------------------------------------------------------
 def main():
     args = parse()
     if args.impl == "reference":
@@ -889,13 +1355,24 @@ def main():
     if args.workload == "serving":
         return serving_main(args)
     if args.workload == "coreset":
-        return coreset_bench(args)
+        E = Env(0)
+        print(json.dumps(c4_coreset(args, E)))
+        return
     if args.workload in ("pcmp", "minibatch", "soft", "coreset_mb"):
         return next_rows_bench(args)
     if args.workload == "small":
-        return small_bench(args)
-    if args.workload != "dense":
-        return csr_bench(args)
+        Env(0)
+        print(json.dumps(c1_small(args)))
+        return
+    if args.workload in ("csr_mkl", "csr_jsd"):
+        E = Env(0)
+        data = CsrData(args.csr_rows)
+        print(json.dumps(c2_csr(args, E, data, 5 if args.workload == "csr_mkl" else 4)))
+        return
+    if args.workload == "csr_l1":
+        return csr_l1_bench(args)
+    if args.workload == "tf32":
+        args.precision = "tf32"
     import torch
     import torch.distributed as dist
     rank = int(os.environ.get("RANK", "0"))
@@ -904,54 +1381,44 @@ def main():
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
-    import minicore_gb300 as mc
-    ctx = mc.Context(local)
-    # a dedicated (non-default) stream: the library launches on it and the CUDA events
-    # that time the steps are recorded on it
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    ctx.set_stream(stream.cuda_stream)
+    E = Env(local)
+    mc, _lib, lib = E.mc, E._lib, E.lib
     n = args.n
     X = make_data(n, seed=rank)
-    # kmeans++ centers (untimed setup), ids on the host
-    seeds = mc.uniforms(1234, K)
-    ids = np.empty(K, np.uint32)
+    # kmeans++ centers (untimed setup)
+    M = mc._MatrixArg(X)
+    u = torch.from_numpy(mc.uniforms(1234, K)).cuda()
+    idst = torch.empty(K, dtype=torch.int32, device="cuda")
     asn0 = torch.empty(n, dtype=torch.int32, device="cuda")
     costs0 = torch.empty(n, dtype=torch.float64, device="cuda")
-    from minicore_gb300 import _lib
-    M = mc._MatrixArg(X)
-    u = torch.from_numpy(seeds).cuda()
-    idst = torch.empty(K, dtype=torch.int32, device="cuda")
-    _lib.check(_lib.load().mc_kmeanspp(ctx.handle, M.ref, K, 2, 0.0, None, mc._p(u), mc._p(idst), mc._p(asn0),
-                                       mc._p(costs0)))
+    _lib.check(lib.mc_kmeanspp(E.ctx.handle, M.ref, K, 2, 0.0, None, mc._p(u), mc._p(idst), mc._p(asn0),
+                               mc._p(costs0)))
     torch.cuda.synchronize()
-    ids = idst.cpu().numpy().astype(np.int64)
-    C0 = X[torch.from_numpy(ids).cuda()].contiguous()
+    C0 = X[idst.long()].contiguous()
     del asn0, costs0
 
-    job = mc.Job(X, C0, msr=2, precision=args.precision, seed=7, ctx=ctx)
+    job = mc.Job(X, C0, msr=2, precision=args.precision, seed=7, ctx=E.ctx)
     job.assign()
     for _ in range(args.warmup):
         job.lloyd_step()
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    clocks = Clocks()
-    clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks().start()
     torch.cuda.synchronize()
-    lib = _lib.load()
     lib.mc_profile_reset()
     lib.mc_profile_enable(1)  # CUDA events around the library's phases, on this stream
     l0 = lib.mc_kernel_launches()
     torch.cuda.nvtx.range_push("lloyd_timed")
-    ev0.record(stream)
+    ev0 = E.event()
     for _ in range(args.steps):
         job.lloyd_step()
-    ev1.record(stream)
+    ev1 = E.event()
     torch.cuda.nvtx.range_pop()
     launches = int(lib.mc_kernel_launches() - l0)
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     clk = clocks.stop()
     lib.mc_profile_enable(0)
     buf = ctypes.create_string_buffer(1 << 16)
@@ -960,89 +1427,57 @@ def main():
     ms_per_step, value = replica_throughput(ev0.elapsed_time(ev1), args.steps, world, "cuda")
     recheck = job.recheck_count()
     accuracy = fp64_objective_check(job, X, n) if rank == 0 else None
-
-    # dominant kernel: the tensor-core assignment kernel (two passes per assignment) or the
-    # FP32 tiled kernel, from the events recorded over the timed region
     pk, pk_kind = peaks()
-    flops = 2.0 * n * K * D
     if args.precision == "fp32":
-        kname, kinfo = "assign_dense_fp32 (k_assign_tiled)", phases.get("assign_dense_fp32", {})
-        launches_k = kinfo.get("count", 0)
-        avg_ms = kinfo.get("ms", float("nan")) / max(launches_k, 1)
-        peak, unit = None, "TFLOP/s"
+        kms, kl = kernel_ms(phases, "assign_dense_fp32")
+        flops = 2.0 * n * K * D
+        roofline = {"bound": "fp32", "achieved": flops / (kms * 1e-3) / 1e12, "peak": None, "unit": "TFLOP/s",
+                    "frac": None, "traffic": None, "kernel": "k_assign_tiled<SQRL2>", "kernel_ms_per_launch": kms,
+                    "launches": kl}
     else:
-        # pass 1 is the full GEMM (every row x every center); pass 2 runs over the rows
-        # whose top-2 margin is inside the rounding bound only
-        p1 = phases.get("tc_pass1_top2", {})
-        launches_k = p1.get("count", 0)
-        avg_ms = p1.get("ms", float("nan")) / max(launches_k, 1)
-        kname = f"k_tc_assign<{args.precision}, TC_TOP2> (pass 1: every row x every center)"
-        peak, unit = pk.get("bf16_tflops", 1935.7), "TFLOP/s"
-    achieved = flops / (avg_ms * 1e-3) / 1e12
-    traffic = None  # DRAM bytes per launch from the committed ncu summary (scaled to 4M rows)
-    if args.precision == "bf16" and n == N:
-        try:
-            for line in open(os.path.join(ROOT, "profiles", "k_tc_assign_bf16_4Mx128_k1024.md")):
-                if line.startswith("traffic_bytes_per_launch_scaled_to_4M:"):
-                    traffic = float(line.split(":")[1].split()[0])
-        except OSError:
-            traffic = None
-    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": unit,
-                "frac": (achieved / peak) if peak else None, "traffic": traffic,
-                "peak_source": f"{pk_kind} bf16_tflops (burst)", "kernel": kname,
-                "kernel_ms_per_launch": avg_ms, "launches": launches_k,
-                "algorithmic": f"2*n*k*d = {flops:.4g} FLOP per launch (n={n}, k={K}, d={D})"}
+        roofline = tc_roofline(phases, n, args.precision, pk, pk_kind)
+    job.close()
+    E.free()
 
-    # FP32 plain kernel for the same iteration (the comparison named by the metric)
+    # the plain FP32 GPU kernel on the same iteration (the comparison the metric names)
     fp32 = None
     if args.precision != "fp32":
-        j32 = mc.Job(X, C0, msr=2, precision="fp32", seed=7, ctx=ctx)
+        j32 = mc.Job(X, C0, msr=2, precision="fp32", seed=7, ctx=E.ctx)
         j32.assign()
-        j32.lloyd_step()
-        torch.cuda.synchronize()
-        b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        b0.record(stream)
-        for _ in range(2):
-            j32.lloyd_step()
-        b1.record(stream)
-        torch.cuda.synchronize()
-        fp32 = 1000.0 / (b0.elapsed_time(b1) / 2)
+        ms32, _, _, _ = E.timed(j32.lloyd_step, 2, 1)
+        fp32 = 1000.0 / ms32
         j32.close()
+        E.free()
 
-    # e2e: hcluster from pinned host buffers, 10 Lloyd updates per step
-    e2e = None
-    if not args.no_e2e:
-        Xh = torch.empty((n, D), dtype=torch.float32, pin_memory=True)
-        Xh.copy_(X)
-        Ch = C0.cpu().numpy()
-        Xn = Xh.numpy()
-        mc.hcluster(Xn, Ch, msr=2, eps=0.0, maxiter=1, precision=args.precision, ctx=ctx)  # warm
-        torch.cuda.synchronize()
-        e_steps = max(1, min(args.steps, 3))
-        t0 = time.perf_counter()
-        iters = 0
-        for _ in range(e_steps):
-            r = mc.hcluster(Xn, Ch, msr=2, eps=0.0, maxiter=E2E_ITERS - 1, precision=args.precision, ctx=ctx)
-            iters += int(r["numiter"])
-        t = time.perf_counter() - t0
-        e2e = {"value": iters / t, "unit": "iters/s", "h2d_bytes_per_step": int(n * D * 4 + K * D * 4),
-               "d2h_bytes_per_step": int(K * D * 4 + n * 4 + n * 8),
-               "call": "minicore_gb300.hcluster(host pinned rows, maxiter=9, eps=0)"}
+    e2e = None if args.no_e2e else dense_e2e(E, X, C0, args.precision, max(1, min(args.steps, 3)))
+    E.free()
+
+    configs = {}
+    if rank == 0 and not args.no_configs and args.workload == "dense" and n == N:
+        configs["C3_tf32"] = _guard(lambda: c3_tf32(args, E, X, C0, fp32))
+    del X
+    E.free()
 
     cpu = None
     if not args.no_cpu and rank == 0:
-        threads = os.cpu_count() or 1
-        S = 20_000
-        Xs = X[:S].cpu().numpy()
-        Cs = C0.cpu().numpy()
-        per = cpu_baseline(Xs, Cs, threads)
-        cpu = {"value": 1.0 / (per * n / S), "unit": "iters/s", "cores": threads, "kind": "port",
-               "sample": f"{S} rows x k={K}: one assignment + centroid update of the oracle, scaled by {n}/{S}"}
+        ref = cpu_reference_line(steps=5, warmup=1, sample=args.cpu_sample)
+        if ref:
+            cpu = dict(ref["cpu_baseline"])
+
+    if rank == 0 and not args.no_configs and args.workload == "dense":
+        configs["C1_small"] = _guard(lambda: c1_small(args))
+        E.free()
+        data = _guard(lambda: CsrData(args.csr_rows))
+        if isinstance(data, CsrData):
+            configs["C2_csr_mkl"] = _guard(lambda: c2_csr(args, E, data, 5))
+            configs["C2_csr_jsd"] = _guard(lambda: c2_csr(args, E, data, 4))
+        del data
+        E.free()
+        configs["C4_coreset"] = _guard(lambda: c4_coreset(args, E))
+        E.free()
 
     serving = None
     if not args.no_serving and rank == 0:
-        del job
-        torch.cuda.synchronize()
         serving = serving_bench(1000, rate=200.0, slots=args.slots, saturation_jobs=250)
 
     if rank == 0:
@@ -1062,10 +1497,21 @@ def main():
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk,
                 "job_latency_ms": (serving or {}).get("latency_ms"),
-                "serving": serving}
+                "serving": serving,
+                "configs": configs}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
+
+
+def _guard(fn):
+    """A sub-line that fails reports its error instead of ending the run."""
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001
+        import traceback
+        traceback.print_exc()
+        return {"error": f"{type(e).__name__}: {e}"}
 
 
 if __name__ == "__main__":

@@ -98,6 +98,10 @@ uint64_t mc_kernel_launches(void);
  * its tensor memory and returns, and the call reports MC_ETIMEOUT; the context stays
  * usable.  One shot: later passes run normally. */
 int mc_test_tc_stall_once(void);
+/* Measured logf throughput of `device` (logf results per second, full occupancy, 8
+ * independent chains per thread): the compute roof against which the CSR JSD sparse dot
+ * (two logf per nonzero and center) is reported.  Diagnostics; no reference counterpart. */
+int mc_diag_logf_rate(int device, double *logs_per_s);
 /* Phase profiler (diagnostics, off by default): CUDA events around the library's phases
  * (tensor-core passes, exact finalize, FP32/CSR assignment, centroid update, objective).
  * mc_profile_report writes {"phase": {"count": c, "ms": total}, ...} as JSON. */

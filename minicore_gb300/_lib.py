@@ -39,6 +39,7 @@ SIGNATURES = {
     "mc_last_error": (ctypes.c_char_p, []),
     "mc_kernel_launches": (U64, []),
     "mc_test_tc_stall_once": (I, []),
+    "mc_diag_logf_rate": (I, [I, ctypes.POINTER(D)]),
     "mc_profile_enable": (I, [I]),
     "mc_profile_reset": (I, []),
     "mc_profile_report": (I, [ctypes.c_char_p, U64]),

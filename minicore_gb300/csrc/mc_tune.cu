@@ -180,6 +180,66 @@ int tune_launch(const std::string &key0, int nvariants, int default_variant, cud
 
 using namespace mc;
 
+namespace mc {
+
+// Measured logf throughput of this GPU, the compute roof of the CSR JSD sparse dot (two
+// logf per nonzero and center): 8 independent chains per thread of x <- logf(x) + 4 (the
+// inputs stay positive normal floats near the fixed point 5.75), full occupancy, best of
+// three launches timed with CUDA events.
+__global__ void __launch_bounds__(256) k_logf_rate(float seed, int iters, float *sink) {
+    float x[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = seed + 0.125f * float(c) + 1e-6f * float(threadIdx.x);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = logf(x[c]) + 4.0f;
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s += x[c];
+    if (s == 123.456f) sink[0] = s;  // keeps the chains live
+}
+
+}  // namespace mc
+
+extern "C" int mc_diag_logf_rate(int device, double *logs_per_s) {
+    using namespace mc;
+    if (!logs_per_s) return fail(MC_EINVAL, "null output");
+    MC_CUDA_TRY(cudaSetDevice(device));
+    int sms = 0;
+    MC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    cudaStream_t st = nullptr;
+    MC_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float *sink = nullptr;
+    int rc = MC_OK;
+    const int iters = 4096, blocks = sms * 8, threads = 256;
+    float best = 0.f;
+    if (cudaMallocAsync(&sink, sizeof(float), st) != cudaSuccess) rc = fail(MC_ENOMEM, "probe buffer");
+    for (int rep = 0; rc == MC_OK && rep < 4; ++rep) {
+        cudaEventRecord(e0, st);
+        k_logf_rate<<<blocks, threads, 0, st>>>(1.5f, iters, sink), note_launch();
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+            rc = fail(MC_ECUDA, cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (best == 0.f || ms < best)) best = ms;  // launch 0 warms up
+    }
+    if (sink) cudaFreeAsync(sink, st);
+    cudaStreamSynchronize(st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    if (rc != MC_OK) return rc;
+    *logs_per_s = double(blocks) * threads * 8.0 * iters / (double(best) * 1e-3);
+    return MC_OK;
+}
+
 extern "C" {
 
 int mc_autotune_enable(int on) {

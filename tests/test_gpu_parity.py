@@ -327,7 +327,8 @@ def test_hcluster_other_measures(mc, orc, msr):
     ores = orc.hcluster(X, C0, msr, 1.0, eps=1e-10, maxiter=8, seed=5)
     np.testing.assert_allclose(res["finalcost"], ores["finalcost"], rtol=1e-5)
     np.testing.assert_allclose(res["centers"], ores["centers"], rtol=1e-5, atol=1e-6)
-    _check_assign(orc, X, res["centers"], msr, 1.0, res["asn"], res["costs"], exact=msr not in LOG_MEASURES)
+    # hcluster returns float32 costs (pycluster.h:160): compared within the tolerance
+    _check_assign(orc, X, res["centers"], msr, 1.0, res["asn"], res["costs"], exact=False)
     _check_loop_asn(orc, X, msr, 1.0, res["asn"], ores["centers"], ores["asn"])
 
 
