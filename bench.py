@@ -723,10 +723,12 @@ def _nb_counts(m, g):
     return x.clamp_(min=1.0).float()
 
 
-def make_serving_pool(seed=0):
-    """Device-resident row pools the serving jobs slice: per d in {32, 64, 128, 512}, a dense
-    200-component Gaussian mixture (means ~N(0, 4I), sigma 1) and a CSR count matrix at 1%
-    density (Bernoulli(0.01) columns, every row at least one entry, NB counts), 200k rows."""
+def make_serving_pool(seed=0, host=True):
+    """Row pools the serving jobs slice: per d in {32, 64, 128, 512}, a dense 200-component
+    Gaussian mixture (means ~N(0, 4I), sigma 1) and a CSR count matrix at 1% density
+    (Bernoulli(0.01) columns, every row at least one entry, NB counts), 200k rows each.
+    Generated on the GPU; host=True keeps pinned host copies only, so every job's rows are
+    uploaded by the server under load."""
     import torch
     g = torch.Generator(device="cuda").manual_seed(seed)
     dense, csr = {}, {}
@@ -743,6 +745,11 @@ def make_serving_pool(seed=0):
         indptr[1:] = torch.cumsum(torch.bincount(rows, minlength=SERVE_POOL_ROWS), 0)
         csr[d] = (_nb_counts(rows.numel(), g).contiguous(), cols.int().contiguous(), indptr)
         del mask
+    if host:
+        dense = {d: pinned_copy(v) for d, v in dense.items()}
+        csr = {d: tuple(pinned_copy(t) for t in v) for d, v in csr.items()}
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
     return dense, csr
 
 
@@ -764,6 +771,7 @@ def make_serving_jobs(pool, njobs, rate, seed):
             X = dense[d][off:off + n]
             spec = dict(matrix=X, k=k, msr=2, prior=0.0, precision="bf16")
             kind = "dense_sqrl2_bf16"
+            h2d = n * d * 4
         else:
             v, c, ip = csr[d]
             b, e = int(ip[off]), int(ip[off + n])
@@ -771,8 +779,10 @@ def make_serving_jobs(pool, njobs, rate, seed):
                                  shape=(n, d))
             spec = dict(matrix=X, k=k, msr=5, prior=1.0, precision="fp32")
             kind = "csr_mkl"
+            h2d = (e - b) * 8 + (n + 1) * 8
         spec.update(eps=1e-4, maxiter=10, seed=1000 + i)
-        jobs.append({"spec": spec, "t": float(arrivals[i]), "n": n, "d": d, "k": k, "kind": kind})
+        jobs.append({"spec": spec, "t": float(arrivals[i]), "n": n, "d": d, "k": k, "kind": kind,
+                     "h2d": int(h2d), "off": off})
     return jobs
 
 
@@ -807,9 +817,40 @@ def run_serving(srv, jobs, open_loop=True):
     return results, time.perf_counter() - t0
 
 
-def serving_bench(njobs, rate=200.0, slots=8, seed=0, saturation_jobs=None, serial=False):
+def serving_fp64_checks(pool, jobs, results, every):
+    """Every `every`-th job's returned centers and assignment against FP64: the objective
+    recomputed in float64 (dense: squared distances; CSR MKL: the FP64 identity of
+    fp64_csr_distances) against the job's final cost, and the argmin agreement."""
+    import scipy.sparse as sp
+    dense, csr = pool
+    errs, agree = [], []
+    for i in range(0, len(jobs), every):
+        j, r = jobs[i], results[i]
+        n, d, off = j["n"], j["d"], j["off"]
+        C = r["centers"]
+        if j["kind"] == "csr_mkl":
+            v, c, ip = csr[d]
+            b, e = int(ip[off]), int(ip[off + n])
+            sub = sp.csr_matrix((v[b:e].numpy(), c[b:e].numpy().astype(np.int64),
+                                 (ip[off:off + n + 1] - b).numpy().astype(np.int64)), shape=(n, d))
+            D64 = fp64_csr_distances(5, sub, C)
+            best = D64.min(1)
+            obj64 = float(best.sum())
+            ag = float((D64.argmin(1) == r["asn"]).mean())
+        else:
+            a = fp64_sqrl2_check(dense[d][off:off + n].numpy(), C, r["asn"], r["costs"])
+            obj64, ag = a["objective_fp64"], a["argmin_agreement"]
+        errs.append(abs(r["finalcost"] - obj64) / max(obj64, 1e-300))
+        agree.append(ag)
+    return {"jobs_checked": len(errs), "max_rel_err_finalcost_vs_fp64": float(max(errs)),
+            "median_rel_err": float(np.median(errs)), "min_argmin_agreement": float(min(agree)),
+            "mean_argmin_agreement": float(np.mean(agree))}
+
+
+def serving_bench(njobs, rate=200.0, slots=8, seed=0, saturation_jobs=None, serial=False, check_every=100):
     """The serving form: a seeded Poisson stream of uneven jobs through mc_server (continuous
-    batching over `slots` concurrent slots, admission by free device memory)."""
+    batching over `slots` concurrent slots, admission by free device memory), rows uploaded
+    from pinned host memory by the server for every job."""
     import torch
     import minicore_gb300 as mc
     from minicore_gb300 import _lib
@@ -824,8 +865,7 @@ def serving_bench(njobs, rate=200.0, slots=8, seed=0, saturation_jobs=None, seri
     with mc.Server(slots=slots) as srv:
         run_serving(srv, warm, open_loop=False)
         srv.reset_stats()
-        clocks = Clocks()
-        clocks.start()
+        clocks = Clocks().start()
         l0 = lib.mc_kernel_launches()
         res, wall = run_serving(srv, jobs, open_loop=True)
         launches = int(lib.mc_kernel_launches() - l0)
@@ -834,24 +874,39 @@ def serving_bench(njobs, rate=200.0, slots=8, seed=0, saturation_jobs=None, seri
         srv.reset_stats()
         res_s, wall_s = run_serving(srv, sat, open_loop=False)
         st_s = srv.stats()
-    tot = np.array([r["total_ms"] for r in res])
-    run = np.array([r["run_ms"] for r in res])
-    qms = np.array([r["queue_ms"] for r in res])
-    rows_iters = sum(j["n"] * (r["numiter"] + 1) for j, r in zip(jobs, res))
-    d2h = sum(j["k"] * j["d"] * 4 + j["n"] * 12 for j in jobs)
+
+    def col(name, sel=None):
+        a = np.array([r[name] for r in res])
+        return a if sel is None else a[sel]
 
     def pct(a):
         return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)), "mean": float(a.mean())}
 
+    rows_iters = sum(j["n"] * (r["numiter"] + 1) for j, r in zip(jobs, res))
+    d2h = sum(j["k"] * j["d"] * 4 + j["n"] * 12 for j in jobs)
+    h2d = sum(j["h2d"] for j in jobs)
     by_kind = {}
+    tot = col("total_ms")
     for kind in ("dense_sqrl2_bf16", "csr_mkl"):
         sel = np.array([j["kind"] == kind for j in jobs])
         if sel.any():
-            by_kind[kind] = {"jobs": int(sel.sum()), "total_ms": pct(tot[sel])}
+            by_kind[kind] = {"jobs": int(sel.sum()), **{nm: pct(col(nm, sel)) for nm in
+                                                        ("total_ms", "queue_ms", "setup_ms", "loop_ms", "read_ms")}}
+    # the slowest 1% of jobs: their shapes and where their time went
+    slow = np.argsort(tot)[-max(1, len(tot) // 100):]
+    tail = {"jobs": int(len(slow)), "kinds": {k: int(sum(jobs[i]["kind"] == k for i in slow))
+                                              for k in ("dense_sqrl2_bf16", "csr_mkl")},
+            "median_n": float(np.median([jobs[i]["n"] for i in slow])),
+            "median_k": float(np.median([jobs[i]["k"] for i in slow])),
+            "median_d": float(np.median([jobs[i]["d"] for i in slow])),
+            **{nm: float(np.mean(col(nm)[slow])) for nm in ("queue_ms", "setup_ms", "loop_ms", "read_ms")}}
     out = {"jobs": njobs, "rate_per_s": rate, "slots": slots, "wall_s": wall, "jobs_per_s": njobs / wall,
-           "latency_ms": {"total": pct(tot), "queue": pct(qms), "run": pct(run)},
-           "server_stats": st, "by_kind": by_kind, "row_iterations_per_s": rows_iters / wall,
-           "gpu_launches": launches, "clocks": clk, "d2h_bytes": int(d2h),
+           "latency_ms": {"total": pct(tot), "queue": pct(col("queue_ms")), "run": pct(col("run_ms")),
+                          "setup": pct(col("setup_ms")), "loop": pct(col("loop_ms")), "read": pct(col("read_ms"))},
+           "server_stats": st, "by_kind": by_kind, "slowest_1pct": tail,
+           "row_iterations_per_s": rows_iters / wall, "gpu_launches": launches, "clocks": clk,
+           "h2d_bytes": int(h2d), "d2h_bytes": int(d2h),
+           "accuracy_vs_fp64": serving_fp64_checks(pool, jobs, res, check_every),
            "saturated": {"jobs": len(sat), "jobs_per_s": len(sat) / wall_s, "wall_s": wall_s,
                          "max_running": st_s.get("max_running"),
                          "latency_ms": pct(np.array([r["total_ms"] for r in res_s]))}}
@@ -866,7 +921,8 @@ def serving_bench(njobs, rate=200.0, slots=8, seed=0, saturation_jobs=None, seri
 def serving_main(args):
     import torch
     torch.cuda.set_device(0)
-    s = serving_bench(args.serving_jobs, rate=args.serving_rate, slots=args.slots, serial=True)
+    s = serving_bench(args.serving_jobs, rate=args.serving_rate, slots=args.slots, serial=True,
+                      saturation_jobs=2000)
     line = {"metric": "serving jobs/s (Poisson 200/s mix of uneven clustering jobs); p50/p99 job latency",
             "value": s["jobs_per_s"], "unit": "jobs/s", "n_gpus": 1, "steps": s["jobs"], "warmup": 16,
             "ms_per_step": 1000.0 * s["wall_s"] / s["jobs"], "higher_is_better": True, "scaling": "weak",
@@ -874,12 +930,12 @@ def serving_main(args):
             "config": {"workload": f"{s['jobs']} jobs, Poisson {args.serving_rate}/s, n logU[1e3,2e5], "
                                    f"d in {{32,64,128,512}}, k logU[5,200], half dense SQRL2 BF16, half CSR "
                                    f"MKL 1% density; kmeans++ then Lloyd (eps 1e-4, 10 updates)",
-                       "slots": args.slots, "l2": "row pools 0.6 GB dense + CSR, jobs slice them"},
+                       "slots": args.slots, "rows": "pinned host pools; the server uploads every job's rows"},
             "latency_ms": s["latency_ms"], "serving": s, "gpu_launches": s["gpu_launches"],
-            "clocks": s["clocks"],
-            "e2e": {"value": s["jobs_per_s"], "unit": "jobs/s", "h2d_bytes_per_step": 0,
+            "clocks": s["clocks"], "accuracy_vs_fp64": s["accuracy_vs_fp64"],
+            "e2e": {"value": s["jobs_per_s"], "unit": "jobs/s", "h2d_bytes_per_step": int(s["h2d_bytes"] / s["jobs"]),
                     "d2h_bytes_per_step": int(s["d2h_bytes"] / s["jobs"]),
-                    "call": "minicore_gb300.Server.submit/wait (rows resident, outputs to host)"}}
+                    "call": "minicore_gb300.Server.submit/wait (rows from pinned host memory, outputs to host)"}}
     print(json.dumps(line))
 
 
@@ -1271,8 +1327,9 @@ def c4_coreset(args, E):
         cs = mc.CoresetSampler(ctx=E.ctx)
         cs.make_sampler(k, cost_e.astype(np.float64), asn_e.astype(np.uint32), seed=13, sens=4)
         wts, idx = cs.sample(m, seed=1234)
-        Xc = Xh[torch.from_numpy(idx.astype(np.int64))]
-        r = mc.hcluster(Xc, Xh[torch.from_numpy(ids_e.astype(np.int64))], msr=2, weights=wts.astype(np.float64),
+        Xn = Xh.numpy()
+        Xc = np.ascontiguousarray(Xn[idx.astype(np.int64)])
+        r = mc.hcluster(Xc, np.ascontiguousarray(Xn[ids_e.astype(np.int64)]), msr=2, weights=wts.astype(np.float64),
                         eps=1e-4, maxiter=20, seed=9, ctx=E.ctx)
         jf = mc.Job(Xh, r["centers"], msr=2, precision=precision, seed=9, ctx=E.ctx)
         jf.assign()
@@ -1463,6 +1520,8 @@ def main():
         ref = cpu_reference_line(steps=5, warmup=1, sample=args.cpu_sample)
         if ref:
             cpu = dict(ref["cpu_baseline"])
+        if isinstance(configs.get("C3_tf32"), dict) and "error" not in configs["C3_tf32"]:
+            configs["C3_tf32"]["cpu_baseline"] = cpu  # the same CPU Lloyd iteration (the oracle is FP32)
 
     if rank == 0 and not args.no_configs and args.workload == "dense":
         configs["C1_small"] = _guard(lambda: c1_small(args))

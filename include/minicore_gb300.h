@@ -289,6 +289,9 @@ typedef struct mc_job_result {
     double initcost, finalcost;
     double queue_ms, run_ms, total_ms;  /* submit->admit, admit->done, submit->done          */
     char error[256];           /* mc_last_error() text when status != MC_OK                  */
+    /* run_ms in parts: rows uploaded and validated, centers given or seeded (k-means++ on
+     * the device); the Lloyd loop; outputs copied back */
+    double setup_ms, loop_ms, read_ms;
 } mc_job_result;
 
 int mc_server_create(int device, uint32_t slots, uint64_t mem_budget_bytes, mc_server **out);

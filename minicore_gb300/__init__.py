@@ -779,7 +779,8 @@ class Server:
         if r.status != _lib.MC_OK:
             raise McError(r.status, r.error.decode(errors="replace"))
         res = {"initcost": r.initcost, "finalcost": r.finalcost, "numiter": r.numiter, "queue_ms": r.queue_ms,
-               "run_ms": r.run_ms, "total_ms": r.total_ms}
+               "run_ms": r.run_ms, "total_ms": r.total_ms, "setup_ms": r.setup_ms, "loop_ms": r.loop_ms,
+               "read_ms": r.read_ms}
         res.update(out)
         return res
 

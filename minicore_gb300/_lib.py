@@ -30,7 +30,8 @@ class McJobDesc(ctypes.Structure):
 
 class McJobResult(ctypes.Structure):
     _fields_ = [("status", I), ("numiter", U64), ("initcost", D), ("finalcost", D), ("queue_ms", D),
-                ("run_ms", D), ("total_ms", D), ("error", ctypes.c_char * 256)]
+                ("run_ms", D), ("total_ms", D), ("error", ctypes.c_char * 256), ("setup_ms", D), ("loop_ms", D),
+                ("read_ms", D)]
 
 
 # name -> (restype, argtypes); every symbol the header declares

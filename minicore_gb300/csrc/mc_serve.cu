@@ -101,14 +101,22 @@ namespace {
 int run_job(mc_context *ctx, Ticket &t) {
     const mc_job_desc &j = t.desc;
     mc_job *job = nullptr;
+    const Clock::time_point t0 = Clock::now();
     if (j.centers)
         MC_TRY(mc_job_create(ctx, &j.X, j.centers, j.k, j.msr, j.prior, j.weights, j.precision, j.seed, &job));
     else
         MC_TRY(mc_job_create_kmeanspp(ctx, &j.X, j.k, j.msr, j.prior, j.weights, j.precision, j.seed,
                                       j.center_ids_out, &job));
     std::unique_ptr<mc_job, int (*)(mc_job *)> guard(job, mc_job_destroy);
+    const Clock::time_point t1 = Clock::now();
     MC_TRY(mc_job_run(job, j.eps, j.maxiter, &t.res.initcost, &t.res.finalcost, &t.res.numiter));
-    return mc_job_read(job, j.centers_out, j.asn_out, j.costs_out);
+    const Clock::time_point t2 = Clock::now();
+    const int rc = mc_job_read(job, j.centers_out, j.asn_out, j.costs_out);
+    const Clock::time_point t3 = Clock::now();
+    t.res.setup_ms = ms_between(t0, t1);
+    t.res.loop_ms = ms_between(t1, t2);
+    t.res.read_ms = ms_between(t2, t3);
+    return rc;
 }
 
 // bytes the device can still hand out: free memory plus what the stream-ordered pool holds
