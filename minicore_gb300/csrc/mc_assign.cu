@@ -748,6 +748,192 @@ __global__ void __launch_bounds__(256) k_assign_sparse_pair(AssignArgs a) {
     }
 }
 
+// Column-band form for 64 padded centers (MKL, Hellinger, SQRL2, L1).  The center transform
+// CT0 ([d][64] floats, 5 MB at d = 20,000) does not fit in shared memory, and the gather
+// kernels above read one 256-byte center column per nonzero from L1/L2, so they wait on
+// cache misses.  Here a CTA streams CT0 through shared memory one band of kBandCols columns
+// at a time (two buffers, cp.async 16-byte copies: the next band loads while this one is
+// used), and each warp keeps kBandRows rows' accumulators in registers across all bands:
+// warp-per-row, lane l owns centers 2l and 2l + 1 (one 8-byte shared load per nonzero).
+// A row's nonzeros are visited once, in ascending column order: a window of the next 32
+// (column, g) pairs sits one per lane, and the part of the window inside the current band
+// is broadcast lane by lane.  Per (row, center) the sum is the same sequential fmaf chain
+// over the row's nonzeros as in k_assign_sparse_pair, and Hellinger's row term is summed in
+// that kernel's lane order, so the results are bit-identical to it (an autotuner variant).
+constexpr int kBandCols = 384;                 // columns per band: 384 x 256 B = 96 KB
+constexpr int kBandRows = 8;                   // rows per warp
+constexpr int kBandThreads = 512;              // 16 warps: 128 rows per CTA chunk
+constexpr size_t kBandSmem = 2ull * kBandCols * 64 * sizeof(float);
+
+template <int MSR>
+__global__ void __launch_bounds__(kBandThreads, 1) k_assign_sparse_band(AssignArgs a) {
+    static_assert(MSR != JSD, "JSD's zero-entry table path is not banded");
+    extern __shared__ __align__(16) float tband[];  // [2][kBandCols][64]
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    constexpr int R = kBandRows, WARPS = kBandThreads / 32, ROWS = WARPS * R;
+    const uint64_t nbands = (a.d + kBandCols - 1) / kBandCols;
+    const float pv = a.pv;
+    // band b of CT0 into buffer buf: contiguous floats [b0 * 64, b1 * 64)
+    auto stage = [&](uint64_t b, int buf) {
+        const uint64_t b0 = b * kBandCols, b1 = umin64(b0 + kBandCols, a.d);
+        const uint32_t items = uint32_t((b1 - b0) * 16);  // 16-byte items
+        const float4 *src = reinterpret_cast<const float4 *>(a.CT0 + b0 * 64);
+        float4 *dst = reinterpret_cast<float4 *>(tband + size_t(buf) * kBandCols * 64);
+        for (uint32_t e = threadIdx.x; e < items; e += kBandThreads) {
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(uint32_t(__cvta_generic_to_shared(dst + e))),
+                         "l"(src + e)
+                         : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    for (uint64_t chunk = blockIdx.x; chunk * ROWS < a.n; chunk += gridDim.x) {
+        uint64_t cur[R];   // next nonzero of row r not yet in its window
+        uint32_t left[R];  // nonzeros of row r after cur
+        uint32_t wst[R];   // window state: used prefix (bits 0-7), elements held (bits 8-15)
+        uint32_t wcol[R];
+        float wg[R];
+        float acc[R][2];
+        float rsi[R], rinc[R];
+        double sb[R];
+        // a window of the next 32 nonzeros of row r: lane l holds element cur + l
+        auto load_window = [&](int r) {
+            const uint64_t p = cur[r] + uint64_t(lane);
+            const uint32_t cnt = left[r] < 32u ? left[r] : 32u;
+            uint32_t col = 0;
+            float g = 0.f;
+            float hb = 0.f;  // Hellinger: this element's b
+            if (uint32_t(lane) < cnt) {
+                col = a.idx[p];
+                const float x = a.vals[p];
+                if (MSR == MKL) g = logf(rinc[r]) - logf(x * rsi[r] + rinc[r]);
+                else if (MSR == HELLINGER) {
+                    hb = x * rsi[r] + rinc[r];
+                    g = sqrtf(rinc[r]) - sqrtf(hb);
+                } else if (MSR == L1) g = x + pv;
+                else g = x;
+            }
+            if (MSR == HELLINGER) {
+                // k_assign_sparse_pair's lane order: half-warp lane h sums the elements at
+                // offsets = h (mod 16) in ascending order; here lanes h and h + 16 hold the
+                // window's two such elements, in that order
+                const float hb2 = __shfl_down_sync(0xffffffffu, hb, 16);
+                if (lane < 16) {
+                    if (uint32_t(lane) < cnt) sb[r] += double(hb);
+                    if (uint32_t(lane) + 16 < cnt) sb[r] += double(hb2);
+                }
+            }
+            wcol[r] = col;
+            wg[r] = g;
+            wst[r] = cnt << 8;
+            cur[r] += cnt;
+            left[r] -= cnt;
+        };
+        for (int r = 0; r < R; ++r) {
+            const uint64_t row = chunk * ROWS + uint64_t(wib) * R + r;
+            const bool live = row < a.n;
+            const uint64_t pb = live ? a.indptr[row] : 0, pe = live ? a.indptr[row + 1] : 0;
+            cur[r] = pb;
+            left[r] = uint32_t(pe - pb);
+            rsi[r] = (live && (MSR == MKL || MSR == HELLINGER)) ? a.rsi[row] : 0.f;
+            rinc[r] = (live && (MSR == MKL || MSR == HELLINGER)) ? a.rinc[row] : 0.f;
+            acc[r][0] = acc[r][1] = 0.f;
+            sb[r] = 0.0;
+            load_window(r);
+        }
+        stage(0, 0);
+        for (uint64_t b = 0; b < nbands; ++b) {
+            const int buf = int(b & 1);
+            if (b + 1 < nbands) {
+                stage(b + 1, buf ^ 1);
+                asm volatile("cp.async.wait_group 1;" ::: "memory");
+            } else {
+                asm volatile("cp.async.wait_group 0;" ::: "memory");
+            }
+            __syncthreads();
+            const uint32_t b0 = uint32_t(b * kBandCols), bend = uint32_t(umin64(b0 + kBandCols, a.d));
+            const float2 *tb = reinterpret_cast<const float2 *>(tband + size_t(buf) * kBandCols * 64) + lane;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                for (;;) {
+                    // the window's elements before bend form a prefix (columns ascend)
+                    const uint32_t held = wst[r] >> 8;
+                    const unsigned in = __ballot_sync(0xffffffffu, uint32_t(lane) < held && wcol[r] < bend);
+                    const uint32_t m = uint32_t(__popc(in));
+                    for (uint32_t q = wst[r] & 0xffu; q < m; ++q) {
+                        const uint32_t c = __shfl_sync(0xffffffffu, wcol[r], int(q));
+                        const float g = __shfl_sync(0xffffffffu, wg[r], int(q));
+                        const float2 cv = tb[(c - b0) * 32];
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            const float cc = h ? cv.y : cv.x;
+                            if (MSR == MKL || MSR == HELLINGER) acc[r][h] = fmaf(cc, g, acc[r][h]);
+                            else if (MSR == SQRL2) acc[r][h] = fmaf(g, g - 2.f * cc, acc[r][h]);
+                            else acc[r][h] = acc[r][h] + (fabsf(cc - g) - fabsf(cc - pv));
+                        }
+                    }
+                    if (m > (wst[r] & 0xffu)) wst[r] = (wst[r] & 0xff00u) | m;
+                    if (m == held && left[r] > 0) {
+                        load_window(r);  // all of this window used: the next 32 nonzeros
+                        continue;
+                    }
+                    break;
+                }
+            }
+            __syncthreads();  // every warp is done with buffer buf before it is refilled
+        }
+        // keys and argmin, as k_assign_sparse_pair
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint64_t row = chunk * ROWS + uint64_t(wib) * R + r;
+            const bool live = row < a.n;
+            const float rl = (MSR == MKL) ? logf(rinc[r]) : 0.f;
+            const float srinc = (MSR == HELLINGER) ? sqrtf(rinc[r]) : 0.f;
+            double bx = 0.0;
+            if (MSR == HELLINGER) {
+                double v = sb[r];
+#pragma unroll
+                for (int m = 8; m >= 1; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+                v = __shfl_sync(0xffffffffu, v, 0);  // lanes 0-15 hold the total; every lane needs it
+                const uint64_t nz = live ? a.indptr[row + 1] - a.indptr[row] : 0;
+                bx = v + double(a.d - nz) * double(rinc[r]);
+            }
+            Best best;
+            best_init(best);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t c = 2 * lane + h;
+                if (live && c < a.k) {
+                    float key;
+                    const double k0 = a.consts[uint64_t(c) * 4 + 0], k1 = a.consts[uint64_t(c) * 4 + 1];
+                    if (MSR == MKL) {
+                        key = post_divergence(float(k0 - double(rl) * k1 + double(acc[r][h])));
+                    } else if (MSR == HELLINGER) {
+                        double sv = k0 + bx - 2.0 * double(srinc) * k1 + 2.0 * double(acc[r][h]);
+                        if (sv < 0.0) sv = 0.0;
+                        key = float(sqrt(sv));
+                    } else if (MSR == SQRL2) {
+                        double sv = k0 + double(acc[r][h]);
+                        if (sv < 0.0) sv = 0.0;
+                        key = float(sv);
+                    } else {
+                        key = float(k0 + double(acc[r][h])) * 0.5f;
+                    }
+                    best_offer(best, key, c);
+                    if (a.dmode) write_dist(a, row, c, float(key_to_cost<MSR>(key)));
+                }
+            }
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) best_merge_shfl(best, m);
+            if (live && lane == 0) {
+                const bool nan0 = best.v == __int_as_float(0xff800000);
+                const double cost = nan0 ? __longlong_as_double(0x7ff8000000000000ll) : key_to_cost<MSR>(best.v);
+                a.asn[row] = best.j;
+                a.costs[row] = double(float(cost));
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------
@@ -1034,8 +1220,10 @@ static int sparse_kpl(const AssignArgs &a, cudaStream_t st, int sms, bool tune) 
     const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
     const unsigned pblocks = unsigned(umin64((a.n + 15) / 16, uint64_t(sms) * 16));
     const uint64_t avg = a.n ? (a.nnz + a.n - 1) / a.n : 0;
-    // 64 padded centers also admit the two-rows-per-warp kernel
-    const int nvar = (KPL == 2 && a.kp == 64) ? 5 : 3;
+    // 64 padded centers also admit the two-rows-per-warp kernel and (except JSD) the
+    // column-band kernel
+    const int nvar = (KPL == 2 && a.kp == 64) ? (MSR == JSD ? 5 : 6) : 3;
+    const unsigned bblocks = unsigned(umin64((a.n + 127) / 128, uint64_t(sms)));
     const std::string key = "csr_sparse|msr" + std::to_string(MSR) + "|kpl" + std::to_string(KPL) + "|g" +
                             std::to_string((a.k + 32 * KPL - 1) / (32 * KPL)) + "|nnz" + tune_bucket(avg) + "|v" +
                             std::to_string(nvar);
@@ -1044,7 +1232,12 @@ static int sparse_kpl(const AssignArgs &a, cudaStream_t st, int sms, bool tune) 
         else if (v == 1) k_assign_sparse<MSR, KPL, 4><<<blocks, 256, 0, st>>>(a), note_launch();
         else if (v == 2) k_assign_sparse<MSR, KPL, 16><<<blocks, 256, 0, st>>>(a), note_launch();
         else if (v == 3) k_assign_sparse_pair<MSR, 8><<<pblocks, 256, 0, st>>>(a), note_launch();
-        else k_assign_sparse_pair<MSR, 4><<<pblocks, 256, 0, st>>>(a), note_launch();
+        else if (v == 4) k_assign_sparse_pair<MSR, 4><<<pblocks, 256, 0, st>>>(a), note_launch();
+        else if constexpr (MSR != JSD) {
+            MC_CUDA_TRY(cudaFuncSetAttribute(k_assign_sparse_band<MSR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(kBandSmem)));
+            k_assign_sparse_band<MSR><<<bblocks, kBandThreads, kBandSmem, st>>>(a), note_launch();
+        }
         MC_CUDA_TRY(cudaGetLastError());
         return MC_OK;
     });

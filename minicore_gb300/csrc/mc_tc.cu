@@ -40,20 +40,27 @@
 
 #include "mc_assign.cuh"
 #include "mc_tc.cuh"
+#include "mc_tune.cuh"
 
 namespace mc {
 
 namespace tc {
 
 constexpr int BM = 128;           // rows per tile (MMA M)
-constexpr int BN = 256;           // centers per chunk (MMA N)
 constexpr int KBYTES = 128;       // bytes of K per k-block (one 128B swizzle row)
-constexpr int STAGES = 4;
 constexpr int A_STAGE = BM * KBYTES;   // 16 KB
-constexpr int B_STAGE = BN * KBYTES;   // 32 KB
-constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
 constexpr int PARTS = 4;          // column parts of a chunk: one epilogue warp per (lane quarter, part)
-constexpr int PCOLS = BN / PARTS;  // 64 columns per epilogue warp and chunk
+// Tile shapes (the autotuner picks one per shape bucket): BN centers per chunk (MMA N,
+// 128 or 256) and STAGES shared-memory stages of (A 16 KB + B BN x 128 B).  Centers are
+// padded to a multiple of 128; the BN = 256 shapes need a multiple of 256.
+template <int BN, int STAGES>
+struct Shape {
+    static constexpr int B_STAGE = BN * KBYTES;
+    static constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
+    static constexpr int PCOLS = BN / PARTS;  // columns per epilogue warp and chunk
+    static_assert(PCOLS % 32 == 0, "epilogue reads TMEM in 32-column groups");
+};
+constexpr int KP_ALIGN = 128;
 constexpr int NCAND = 3;          // pass 2 candidate slots per row and column part
 constexpr int EPI_WARPS = 4 * PARTS;
 constexpr int THREADS = 64 + 32 * EPI_WARPS;  // warp 0 TMA, warp 1 MMA (+TMEM alloc), warps 2-17 epilogue
@@ -61,6 +68,7 @@ constexpr int CN_SMEM = 4096;     // center norms staged in shared memory when k
 constexpr uint32_t TMEM_COLS = 512;
 constexpr long long WAIT_CYCLES = 2000000000ll;  // ~1 s at 2 GHz
 
+template <int STAGES>
 struct Smem {
     uint64_t full[STAGES], empty[STAGES], acc_full[2], acc_empty[2], drain;
     uint64_t nrows;      // rows of this launch (pass 2: the compact row count read on the device)
@@ -97,7 +105,8 @@ __device__ inline bool mbar_try(uint64_t *bar, uint32_t parity) {
 }
 
 // bounded wait; returns false on timeout or when another role aborted
-__device__ inline bool mbar_wait(uint64_t *bar, uint32_t parity, Smem *sm, int *err, int code) {
+template <class SM>
+__device__ inline bool mbar_wait(uint64_t *bar, uint32_t parity, SM *sm, int *err, int code) {
     if (mbar_try(bar, parity)) return true;
     const long long t0 = clock64();
     for (uint32_t it = 1;; ++it) {
@@ -140,7 +149,7 @@ __device__ inline uint64_t sdesc(const void *p) {
     return d;
 }
 
-template <bool TF32>
+template <bool TF32, int BN>
 __device__ inline uint32_t idesc() {
     // D = F32 (bits 4-5 = 1); A/B format BF16 = 1 or TF32 = 2 (bits 7-9, 10-12); both
     // K-major; N >> 3 at bits 17-22; M >> 4 at bits 24-28
@@ -148,9 +157,9 @@ __device__ inline uint32_t idesc() {
     return (1u << 4) | (fmt << 7) | (fmt << 10) | (uint32_t(BN >> 3) << 17) | (uint32_t(BM >> 4) << 24);
 }
 
-template <bool TF32>
+template <bool TF32, int BN>
 __device__ inline void mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
-    const uint32_t id = idesc<TF32>();
+    const uint32_t id = idesc<TF32, BN>();
     if (TF32) {
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
@@ -229,10 +238,13 @@ __device__ __forceinline__ void top2_merge(float &a1, float &a2, float b1, float
     a1 = fminf(a1, b1);
 }
 
-template <bool TF32, int MODE>
+template <bool TF32, int MODE, int BN, int STAGES>
 __global__ void __launch_bounds__(tc::THREADS, 1)
     k_tc_assign(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a) {
     using namespace tc;
+    using SH = Shape<BN, STAGES>;
+    constexpr int STAGE_BYTES = SH::STAGE_BYTES, PCOLS = SH::PCOLS;
+    using Smem = tc::Smem<STAGES>;
     extern __shared__ __align__(1024) unsigned char smraw[];
     unsigned char *base = reinterpret_cast<unsigned char *>((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
     unsigned char *stages = base;
@@ -322,7 +334,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
 #pragma unroll
                         for (int ks = 0; ks < 4; ++ks) {
                             // +32 bytes of K per MMA within the 128-byte swizzle row
-                            mma<TF32>(d_tmem, ad + uint64_t(ks * 2), bd + uint64_t(ks * 2), (kb | ks) ? 1u : 0u);
+                            mma<TF32, BN>(d_tmem, ad + uint64_t(ks * 2), bd + uint64_t(ks * 2), (kb | ks) ? 1u : 0u);
                         }
                         mma_commit(&sm->empty[s]);
                         if (++s == STAGES) { s = 0; ph ^= 1; }
@@ -942,6 +954,35 @@ static int make_map(CUtensorMap *map, const void *ptr, bool tf32, uint64_t rows,
 static std::atomic<int> g_tc_stall_next{0};
 void tc_stall_next() { g_tc_stall_next.store(1); }
 
+// Tile shapes of the tensor-core passes, as (BN, STAGES); the first kTcWideOnly need the
+// padded center count to be a multiple of 256.  Every shape issues, per output element, the
+// same chain of K-steps, and the exact FP32 finalize decides every assignment from the
+// rounding bound, so all shapes give identical assignments and costs.
+constexpr int kTcShapes = 4, kTcWideOnly = 2;
+
+template <bool TF32, int MODE, int BN, int STAGES>
+static int tc_launch_t(unsigned grid, const CUtensorMap &mA, const CUtensorMap &mB, TcArgs a, cudaStream_t st) {
+    a.nchunks = a.kp / BN;
+    const size_t smem = size_t(STAGES) * tc::Shape<BN, STAGES>::STAGE_BYTES + tc::CN_SMEM * sizeof(float) +
+                        sizeof(tc::Smem<STAGES>) + 1024;
+    auto kern = k_tc_assign<TF32, MODE, BN, STAGES>;
+    MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    kern<<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+template <bool TF32, int MODE>
+static int tc_shape_launch(int shape, unsigned grid, const CUtensorMap &mA, const CUtensorMap &mB128,
+                           const CUtensorMap &mB256, const TcArgs &a, cudaStream_t st) {
+    switch (shape) {
+        case 0: return tc_launch_t<TF32, MODE, 256, 4>(grid, mA, mB256, a, st);
+        case 1: return tc_launch_t<TF32, MODE, 256, 3>(grid, mA, mB256, a, st);
+        case 2: return tc_launch_t<TF32, MODE, 128, 4>(grid, mA, mB128, a, st);
+        default: return tc_launch_t<TF32, MODE, 128, 6>(grid, mA, mB128, a, st);
+    }
+}
+
 int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
               int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
               uint64_t *recheck_count, bool graph_mode) {
@@ -950,7 +991,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     const uint64_t kelems = tc::KBYTES / esz;            // K elements per k-block
     const uint64_t dp = (d + 7) / 8 * 8;                 // 16-byte row pitch for both types
     const uint32_t kb = uint32_t((d + kelems - 1) / kelems);
-    const uint32_t kp = (k + tc::BN - 1) / tc::BN * tc::BN;
+    const uint32_t kp = (k + tc::KP_ALIGN - 1) / tc::KP_ALIGN * tc::KP_ALIGN;
     const unsigned cg = unsigned(umin64((n * dp + 255) / 256, uint64_t(sms) * 64));
     // resident operand copy of the rows (once per matrix / precision)
     if (s.X_src != X || s.prec != precision || s.n != n || s.d != d) {
@@ -982,9 +1023,12 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     k_center_prep_tc<<<unsigned(umin64((uint64_t(kp) * dp + 255) / 256, 4096)), 256, 0, st>>>(
         C, k, kp, d, dp, tf32 ? 1 : 0, s.Cb.p, s.Ct.p, cnorm, s.cnorm_p.p), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
-    CUtensorMap mA, mB;
+    CUtensorMap mA, mB128, mB256;
+    const bool wide = kp % 256 == 0;  // the BN = 256 shapes need whole 256-center chunks
     MC_TRY(make_map(&mA, Aptr, tf32, n, d, apitch, tc::BM));
-    MC_TRY(make_map(&mB, tf32 ? (const void *)s.Ct.p : (const void *)s.Cb.p, tf32, kp, d, dp, tc::BN));
+    const void *Bptr = tf32 ? (const void *)s.Ct.p : (const void *)s.Cb.p;
+    MC_TRY(make_map(&mB128, Bptr, tf32, kp, d, dp, 128));
+    if (wide) MC_TRY(make_map(&mB256, Bptr, tf32, kp, d, dp, 256));
     using tc::PARTS;
     MC_TRY(s.b1.alloc(PARTS * n, st));
     MC_TRY(s.b2.alloc(PARTS * n, st));
@@ -1015,7 +1059,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     a.d = d;
     a.k = k;
     a.kb = kb;
-    a.nchunks = kp / tc::BN;
+    a.nchunks = 0;  // set per tile shape
     a.ntiles = uint32_t((n + tc::BM - 1) / tc::BM);
     a.rownorm = rownorm;
     a.cnp = s.cnorm_p.p;
@@ -1040,16 +1084,21 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     a2.thrc = s.thrc.p;
     a2.cnt = s.cnt.p;
     a2.cand = s.cand.p;
-    const size_t smem = size_t(tc::STAGES) * tc::STAGE_BYTES + tc::CN_SMEM * sizeof(float) + sizeof(tc::Smem) + 1024;
     const unsigned grid = unsigned(umin64(a.ntiles, uint64_t(sms)));
     const unsigned grid2 = unsigned(umin64((cap + tc::BM - 1) / tc::BM, uint64_t(sms)));
-    auto k1 = tf32 ? k_tc_assign<true, TC_TOP2> : k_tc_assign<false, TC_TOP2>;
-    auto k2 = tf32 ? k_tc_assign<true, TC_CAND> : k_tc_assign<false, TC_CAND>;
-    MC_CUDA_TRY(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    MC_CUDA_TRY(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    // tile shape per shape bucket (tc_shape_launch); the stall test hook and graph capture
+    // take the recorded decision or the default
+    const int nvar = wide ? kTcShapes : kTcShapes - kTcWideOnly;
+    auto shape_of = [&](int v) { return wide ? v : v + kTcWideOnly; };
+    const bool allow = !graph_mode && !a.stall_test;
+    const std::string bucket = std::string(tf32 ? "|tf32" : "|bf16") + "|kp" + std::to_string(kp) + "|d" +
+                               tune_bucket(d) + "|n" + tune_bucket(n);
     {
         Phase ph("tc_pass1_top2", st);
-        k1<<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
+        MC_TRY(tune_launch("tc1" + bucket, nvar, 0, st, allow, [&](int v) -> int {
+            return tf32 ? tc_shape_launch<true, TC_TOP2>(shape_of(v), grid, mA, mB128, mB256, a, st)
+                        : tc_shape_launch<false, TC_TOP2>(shape_of(v), grid, mA, mB128, mB256, a, st);
+        }));
     }
     MC_CUDA_TRY(cudaGetLastError());
     {
@@ -1065,7 +1114,10 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     MC_CUDA_TRY(cudaGetLastError());
     {
         Phase ph("tc_pass2_candidates", st);
-        k2<<<grid2, tc::THREADS, smem, st>>>(mC, mB, a2), note_launch();
+        MC_TRY(tune_launch("tc2" + bucket, nvar, 0, st, allow, [&](int v) -> int {
+            return tf32 ? tc_shape_launch<true, TC_CAND>(shape_of(v), grid2, mC, mB128, mB256, a2, st)
+                        : tc_shape_launch<false, TC_CAND>(shape_of(v), grid2, mC, mB128, mB256, a2, st);
+        }));
     }
     MC_CUDA_TRY(cudaGetLastError());
     {

@@ -55,7 +55,7 @@ def test_csr_sparse_tuned_equals_default(mc, k):
     assert np.array_equal(a0, a2) and np.array_equal(c0, c2)
     ent = mc.autotune_report()["entries"]
     assert any(key.startswith("csr_sparse|msr5|") for key in ent)
-    assert all(len(v["ms"]) in (3, 5) and 0 <= v["variant"] < len(v["ms"])
+    assert all(len(v["ms"]) in (3, 5, 6) and 0 <= v["variant"] < len(v["ms"])
                for key, v in ent.items() if key.startswith("csr"))
 
 
@@ -77,9 +77,10 @@ def test_csr_every_variant_equals_default(mc, msr, prior, tmp_path):
     mc.autotune(True)
     _assign(mc, X, C, msr, prior)
     keys = [k for k in mc.autotune_report()["entries"] if k.startswith("csr_sparse|")]
-    assert len(keys) == 1 and mc.autotune_report()["entries"][keys[0]]["ms"].__len__() == 5
+    nvar = 5 if msr == 4 else 6  # the column-band kernel covers every measure but JSD
+    assert len(keys) == 1 and mc.autotune_report()["entries"][keys[0]]["ms"].__len__() == nvar
     ref = None
-    for v in range(5):
+    for v in range(nvar):
         mc.autotune_reset()
         path = tmp_path / f"v{v}.tsv"
         path.write_text(f"{keys[0]}\t{v}\t\n")
@@ -110,3 +111,87 @@ def test_dense_sqrl2_and_kmeanspp_tuned_equal_default(mc):
     keys = list(mc.autotune_report()["entries"])
     assert any(k.startswith("dense_sqrl2|dense|k256|") for k in keys)
     assert any(k.startswith("kmpp_dense|msr2|") for k in keys)
+
+
+def _assign_prec(mc, X, C, precision):
+    from minicore_gb300 import _lib
+    M = mc._MatrixArg(X)
+    C = np.ascontiguousarray(C, np.float32)
+    asn = np.empty(M.n, np.uint32)
+    costs = np.empty(M.n, np.float64)
+    _lib.check(_lib.load().mc_assign(mc.default_context().handle, M.ref, mc._p(C), C.shape[0], 2, 0.0,
+                                     mc._PREC[precision], mc._p(asn), mc._p(costs)))
+    return asn, costs
+
+
+@pytest.mark.parametrize("precision", ["bf16", "tf32"])
+@pytest.mark.parametrize("n,d,k", [(9000, 128, 512), (5000, 96, 100), (3001, 40, 300)])
+def test_tc_every_tile_shape_equals_fp32(mc, precision, n, d, k, tmp_path):
+    """Each tensor-core tile shape (BN 256 with 4 or 3 stages when the padded center count
+    is a multiple of 256, BN 128 with 4 or 6 stages always), forced for both passes through a
+    loaded decision, gives the FP32 path's assignments and costs bit for bit; with tuning on,
+    the first call records a decision per pass."""
+    rng = np.random.default_rng(n + k)
+    mu = rng.normal(size=(max(2, k // 2), d)) * 2.0
+    X = (mu[rng.integers(0, mu.shape[0], n)] + rng.normal(size=(n, d))).astype(np.float32)
+    C = X[rng.choice(n, k, replace=False)].copy()
+    C[: k // 4] = C[k - k // 4:] + rng.normal(size=(k // 4, d)).astype(np.float32) * 0.05  # near ties
+    mc.autotune(False)
+    ref = _assign_prec(mc, X, C, "fp32")
+    mc.autotune_reset()
+    mc.autotune(True)
+    got = _assign_prec(mc, X, C, precision)   # tunes both passes
+    assert np.array_equal(ref[0], got[0]) and np.array_equal(ref[1], got[1])
+    ent = mc.autotune_report()["entries"]
+    keys = {p: [kk for kk in ent if kk.startswith(f"tc{p}|{precision}|")] for p in (1, 2)}
+    assert len(keys[1]) == 1 and len(keys[2]) == 1
+    nvar = len(ent[keys[1][0]]["ms"])
+    kp = (k + 127) // 128 * 128
+    assert nvar == (4 if kp % 256 == 0 else 2)
+    for v in range(nvar):
+        mc.autotune_reset()
+        path = tmp_path / f"tc{v}.tsv"
+        path.write_text(f"{keys[1][0]}\t{v}\t\n{keys[2][0]}\t{v}\t\n")
+        mc.autotune_load(str(path))
+        got = _assign_prec(mc, X, C, precision)
+        assert mc.autotune_report()["entries"][keys[1][0]]["variant"] == v
+        assert np.array_equal(ref[0], got[0]), v
+        assert np.array_equal(ref[1], got[1]), v
+    mc.autotune_reset()
+
+
+@pytest.mark.parametrize("msr,prior", [(5, 1.0), (6, 1.0), (2, 0.0), (0, 0.5)])
+def test_csr_band_kernel_many_bands_equals_default(mc, msr, prior, tmp_path):
+    """The column-band kernel (variant 5) over 2000 columns (six 384-column bands): rows of
+    100 nonzeros spread over every band, rows of 1000 (windows of 32 crossing band edges),
+    empty rows, a row with one nonzero in the last column, and a row count that leaves the
+    last CTA chunk partly empty; bit-identical to variant 0 and to the oracle's tolerance."""
+    rng = np.random.default_rng(100 + msr)
+    n, d = 2999, 2000
+    X = sp.random(n, d, density=0.05, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.integers(1, 6, s).astype(np.float32)).tolil()
+    for i in range(0, n, 101):
+        X.rows[i], X.data[i] = [], []
+    for i in range(7, n, 151):
+        cols = np.sort(rng.choice(d, 1000, replace=False))
+        X.rows[i], X.data[i] = list(cols), list(rng.integers(1, 6, 1000).astype(np.float32))
+    X.rows[3], X.data[3] = [d - 1], [2.0]
+    X = X.tocsr().astype(np.float32)
+    X.sort_indices()
+    C = np.asarray(X[np.arange(2, n, 60)[:50]].toarray(), np.float32) + 0.125
+    mc.autotune_reset()
+    mc.autotune(True)
+    _assign(mc, X, C, msr, prior)
+    keys = [k for k in mc.autotune_report()["entries"] if k.startswith("csr_sparse|")]
+    assert len(keys) == 1
+    got = {}
+    for v in (0, 5):
+        mc.autotune_reset()
+        path = tmp_path / f"b{v}.tsv"
+        path.write_text(f"{keys[0]}\t{v}\t\n")
+        mc.autotune_load(str(path))
+        got[v] = _assign(mc, X, C, msr, prior)
+        assert mc.autotune_report()["entries"][keys[0]]["variant"] == v
+    assert np.array_equal(got[0][0], got[5][0])
+    assert np.array_equal(got[0][1], got[5][1], equal_nan=True)
+    mc.autotune_reset()
