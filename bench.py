@@ -68,7 +68,7 @@ def parse(argv=None):
     ap.add_argument("--serving-jobs", type=int, default=20000,
                     help="jobs in the --workload serving stream (the full stream is 20000)")
     ap.add_argument("--serving-rate", type=float, default=200.0)
-    ap.add_argument("--slots", type=int, default=8)
+    ap.add_argument("--slots", type=int, default=16)
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the short serving run (p50/p99 job latency) in the default line")
     ap.add_argument("--csr-rows", type=int, default=1_000_000)
@@ -907,6 +907,7 @@ def serving_bench(njobs, rate=200.0, slots=8, seed=0, saturation_jobs=None, seri
                           "setup": pct(col("setup_ms")), "loop": pct(col("loop_ms")), "read": pct(col("read_ms"))},
            "server_stats": st, "by_kind": by_kind, "slowest_1pct": tail,
            "row_iterations_per_s": rows_iters / wall, "gpu_launches": launches, "clocks": clk,
+           "autotune_entries": len(mc.autotune_report().get("entries", {})),
            "h2d_bytes": int(h2d), "d2h_bytes": int(d2h),
            "accuracy_vs_fp64": serving_fp64_checks(pool, jobs, res, check_every),
            "saturated": {"jobs": len(sat), "jobs_per_s": len(sat) / wall_s, "wall_s": wall_s,
@@ -1219,7 +1220,10 @@ def c2_csr(args, E, data, msr):
                        f"maxiter={E2E_ITERS - 1}, eps=0)",
                "step": "one Lloyd iteration; copy bytes per step = per-call bytes / iterations per call"}
         del vh, ih, ph, Ah
+    tuned = {key: v for key, v in mc.autotune_report().get("entries", {}).items()
+             if key.startswith(f"csr_sparse|msr{msr}|")}
     return {"metric": f"CSR {name} Lloyd iters/s 1Mx20000 k=50 (rows resident)", "value": 1000.0 / ms,
+            "autotune_variants_ms": tuned,
             "unit": "iters/s", "ms_per_step": ms, "steps": steps, "dtype": "f32",
             "assign_ms_per_pass": kms, "kmeanspp_ms": kmpp_ms,
             "config": {"workload": f"CSR {n}x{d}, {CSR_NNZ_ROW} nnz/row Zipf(1.1) columns, NB(3,0.5) counts, "

@@ -1313,7 +1313,7 @@ static int job_create_impl(mc_context *ctx, const mc_matrix *X, const float *cen
         a.prior = prior;
         a.prior_sum = prior * double(d);
         a.cbuf = cbuf.p;
-        if (a.csr && kmpp_csr_nnz_path(d) && (msr != JSD || j->ngrp)) {
+        if (a.csr && kmpp_csr_nnz_path(n, d, j->M.nnz) && (msr != JSD || j->ngrp)) {
             MC_TRY(ct.alloc(d, st));
             MC_TRY(cconst.alloc(msr == JSD ? j->ngrp : 2, st));
             a.ct = ct.p;
@@ -2204,7 +2204,7 @@ static int kmeanspp_impl(mc_context *ctx, const mc_matrix *X, uint32_t k, int ms
     a.cbuf = cbuf.p;
     uint32_t ngrp = 0;
     if (a.csr && msr == JSD) MC_TRY(build_rinc_groups(rowsum.p, n, d, M.nnz, float(prior), st, grp, gval, ngrp));
-    if (a.csr && kmpp_csr_nnz_path(d) && (msr != JSD || ngrp)) {
+    if (a.csr && kmpp_csr_nnz_path(n, d, M.nnz) && (msr != JSD || ngrp)) {
         MC_TRY(ct.alloc(d, st));
         MC_TRY(cconst.alloc(msr == JSD ? ngrp : 2, st));
         a.ct = ct.p;

@@ -36,10 +36,15 @@ int kmpp_distances_to(const KmppArgs &a, const uint64_t *cand, double *out, int 
 int run_kmeanspp_greedy(const KmppArgs &a, uint32_t L, uint64_t seed, double *chunk_tmp, int sms, cudaStream_t st);
 
 // CSR seeding takes the O(nnz)-per-row update (per-center FP64 constants, a.ct / a.cconst)
-// only for wide rows: each round then pays a few microseconds of dependent FP64 sums (about
-// 75 ns per dependent add on this GPU), which the float column loop of k_kmpp_csr, O(d) per
-// row, undercuts up to a couple of thousand columns
-inline bool kmpp_csr_nnz_path(uint64_t d) { return d > 2048; }
+// for wide rows, and for large sparse matrices: each round then pays a few microseconds of
+// dependent FP64 sums for the constants (about 75 ns per dependent add on this GPU), which
+// the float column loop of k_kmpp_csr, O(d) per row (two logf per column for MKL), undercuts
+// only while the whole column loop is small (n d < 2^22) or the rows are not sparse
+// (more than one nonzero in eight columns)
+inline bool kmpp_csr_nnz_path(uint64_t n, uint64_t d, uint64_t nnz) {
+    if (d > 2048) return true;
+    return n * d >= (uint64_t(1) << 22) && nnz * 8 <= n * d;
+}
 
 // C[c] = row ids[c], c < k (CSR rows densified into d columns)
 int launch_gather_rows(bool csr, const float *X, const float *vals, const uint32_t *idx, const uint64_t *indptr,
