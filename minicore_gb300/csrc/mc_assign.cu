@@ -1144,12 +1144,101 @@ __global__ void __launch_bounds__(256) k_assign_l1_union(AssignArgs a, const uin
     }
 }
 
+// The same union walk, always in lock step and from registers: per 32-center group the
+// warp walks the merge of the row's columns with the group's column union U_g (all lanes
+// take the same step, lane = center), and nothing on the step's path waits for memory.  The
+// row's next 32 (column, value) pairs and U_g's next 32 columns sit one per lane and are
+// read by shuffle; the matching 32 x 32 slice of V_g (the group's center values at U_g's
+// columns) is staged in shared memory, one conflict-free load per step.  Each window is
+// refilled with coalesced loads when the walk has used it up.  Per (row, center) the sum is
+// the same sequential float chain over the union, ascending, as in k_assign_l1_union, so
+// the two kernels are bit-identical (autotuner variants).
+__global__ void __launch_bounds__(256) k_assign_l1_lockstep(AssignArgs a, const uint32_t *__restrict__ U,
+                                                            const float *__restrict__ V,
+                                                            const uint32_t *__restrict__ usize) {
+    __shared__ float vs[8][32][33];  // per warp: V_g rows q0 .. q0+31 (padded: no bank conflicts)
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint64_t nw = (gridDim.x * uint64_t(blockDim.x)) >> 5;
+    const uint32_t ng = (a.k + 31) / 32;
+    constexpr uint32_t END = 0xffffffffu;
+    for (uint64_t r = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5; r < a.n; r += nw) {
+        const uint64_t rb = a.indptr[r], re = a.indptr[r + 1];
+        const uint32_t nr = uint32_t(re - rb);
+        const uint32_t *ri = a.idx + rb;
+        const float *rx = a.vals + rb;
+        const double rs = a.rowsum[r];
+        Best best;
+        best_init(best);
+        for (uint32_t g = 0; g < ng; ++g) {
+            const uint32_t c = g * 32 + lane;
+            const float pv = pair_scalars(a.prior, a.prior_sum, rs, c < a.k ? a.csum[c] : 0.0, a.d).pv;
+            const uint32_t nu = usize[g];
+            const uint32_t *Ug = U + uint64_t(g) * (a.d + 1);
+            const float *Vg = V + uint64_t(g) * a.d * 32;
+            // windows: row elements p0 + lane, union columns q0 + lane, V_g rows q0 .. q0 + 31
+            uint32_t p = 0, q = 0;
+            uint32_t wrc = uint32_t(lane) < nr ? ri[lane] : END;
+            float wrv = uint32_t(lane) < nr ? rx[lane] : 0.f;
+            uint32_t wuc = uint32_t(lane) < nu ? Ug[lane] : END;
+            __syncwarp();
+            for (int i = 0; i < 32; ++i) vs[wib][i][lane] = uint32_t(i) < nu ? Vg[uint64_t(i) * 32 + lane] : 0.f;
+            __syncwarp();
+            uint32_t rc = __shfl_sync(0xffffffffu, wrc, 0), uc = __shfl_sync(0xffffffffu, wuc, 0);
+            float rv = __shfl_sync(0xffffffffu, wrv, 0);
+            float uv = vs[wib][0][lane];
+            float acc = 0.f;
+            while ((rc & uc) != END) {  // warp-uniform
+                const bool tr = rc <= uc, tu = uc <= rc;
+                const float av = (tu ? uv : 0.f) + pv;
+                const float bv = (tr ? rv : 0.f) + pv;
+                acc = acc + fabsf(av - bv);
+                if (tr) {
+                    ++p;
+                    if ((p & 31u) == 0) {
+                        const uint32_t e = p + uint32_t(lane);
+                        wrc = e < nr ? ri[e] : END;
+                        wrv = e < nr ? rx[e] : 0.f;
+                    }
+                    rc = __shfl_sync(0xffffffffu, wrc, int(p & 31u));
+                    rv = __shfl_sync(0xffffffffu, wrv, int(p & 31u));
+                }
+                if (tu) {
+                    ++q;
+                    if ((q & 31u) == 0) {
+                        const uint32_t e = q + uint32_t(lane);
+                        wuc = e < nu ? Ug[e] : END;
+                        __syncwarp();
+                        for (int i = 0; i < 32; ++i)
+                            vs[wib][i][lane] = q + uint32_t(i) < nu ? Vg[uint64_t(q + uint32_t(i)) * 32 + lane] : 0.f;
+                        __syncwarp();
+                    }
+                    uc = __shfl_sync(0xffffffffu, wuc, int(q & 31u));
+                    uv = uc != END ? vs[wib][q & 31u][lane] : 0.f;
+                }
+            }
+            if (c < a.k) {
+                const float key = finish_key<L1>(acc);
+                best_offer(best, key, c);
+                if (a.dmode) write_dist(a, r, c, float(key_to_cost<L1>(key)));
+            }
+        }
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) best_merge_shfl(best, m);
+        if (lane == 0) {
+            const bool nan0 = best.v == __int_as_float(0xff800000);
+            const double cost = nan0 ? __longlong_as_double(0x7ff8000000000000ll) : key_to_cost<L1>(best.v);
+            a.asn[r] = best.j;
+            a.costs[r] = double(float(cost));
+        }
+    }
+}
+
 uint64_t l1_union_work_entries(uint32_t k, uint64_t d) {
     const uint64_t ng = (k + 31) / 32;
     return uint64_t(k) * (d + 1) * 2 + ng * (d + 1) * 33 + k + ng + 8;
 }
 
-int launch_assign_l1_union(const AssignArgs &a, const float *C, float *work, int sms, cudaStream_t st) {
+int launch_assign_l1_union(const AssignArgs &a, const float *C, float *work, int sms, cudaStream_t st, bool tune) {
     if (a.k == 0) return MC_OK;
     const uint32_t ng = (a.k + 31) / 32;
     // work: lists (8-byte aligned first), U, V, cnz, usize
@@ -1160,9 +1249,20 @@ int launch_assign_l1_union(const AssignArgs &a, const float *C, float *work, int
     uint32_t *usize = cnz + a.k;
     k_l1_center_lists<<<a.k, 256, 0, st>>>(C, a.d, lists, cnz), note_launch();
     k_l1_center_groups<<<ng, 256, 0, st>>>(C, a.k, a.d, U, V, usize), note_launch();
-    if (a.n)
-        k_assign_l1_union<<<unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16)), 256, 0, st>>>(a, lists, cnz, U, V,
-                                                                                              usize), note_launch();
+    if (a.n) {
+        // the register-window lockstep walk, or the per-row choice of lockstep / per-lane
+        // merge from global memory: bit-identical, so the autotuner picks
+        const unsigned blocks = unsigned(umin64((a.n + 7) / 8, uint64_t(sms) * 16));
+        const uint64_t avg = (a.nnz + a.n - 1) / a.n;
+        const std::string key = "csr_l1_union|g" + std::to_string(ng) + "|d" + tune_bucket(a.d) + "|nnz" +
+                                tune_bucket(avg);
+        return tune_launch(key, 2, 0, st, tune, [&](int v) -> int {
+            if (v == 0) k_assign_l1_lockstep<<<blocks, 256, 0, st>>>(a, U, V, usize), note_launch();
+            else k_assign_l1_union<<<blocks, 256, 0, st>>>(a, lists, cnz, U, V, usize), note_launch();
+            MC_CUDA_TRY(cudaGetLastError());
+            return MC_OK;
+        });
+    }
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }

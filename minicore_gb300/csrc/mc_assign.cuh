@@ -56,7 +56,8 @@ int launch_assign_tiled(const AssignArgs &a, bool csr, bool pair, cudaStream_t s
 int launch_assign_sparse(const AssignArgs &a, cudaStream_t st, int sms, bool tune = true);
 // L1 over CSR rows in pair mode (prior 0): a walk over the union of nonzero columns,
 // bit-identical to the tiled kernel; work: l1_union_work_entries(k, d) floats
-int launch_assign_l1_union(const AssignArgs &a, const float *C, float *work, int sms, cudaStream_t st);
+int launch_assign_l1_union(const AssignArgs &a, const float *C, float *work, int sms, cudaStream_t st,
+                           bool tune = true);
 uint64_t l1_union_work_entries(uint32_t k, uint64_t d);
 // the largest work space (in entries) for which the union kernel is used
 constexpr uint64_t kL1UnionMaxEntries = 1ull << 29;

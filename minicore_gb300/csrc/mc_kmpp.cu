@@ -50,6 +50,44 @@ __device__ inline void kp_elem(float &acc, float c, float x, const PairScalars &
     }
 }
 
+// Dense SQRL2 pruning.  Row i's distance to its nearest center a = asn[i] so far is
+// D = dist[i], the FP32 sequential fmaf sum of d squared differences, so the exact squared
+// distance e_a lies in [D / (1 + g), D / (1 - g)] with g = (d + 2) 2^-24 / (1 - (d + 2) 2^-24).
+// By the triangle inequality the exact squared distance to the new center is at least
+// (delta - sqrt(e_a))^2 when delta = ||new center - center a|| exceeds sqrt(e_a), and the FP32
+// value the update would compute is at least (1 - g) times that.  When that lower bound is
+// at or above D, the update's test (new < D) is false, so the row can skip the distance:
+// the result is the same as computing it.  All bound arithmetic is FP64 with margins for its
+// own rounding; non-finite distances are always evaluated.
+__device__ __forceinline__ bool kp_prune(const KmppArgs &a, uint64_t i, double cur) {
+    if (!(cur < 1e300)) return false;
+    const double g = a.prune_g;
+    const double ea = sqrt(cur / (1.0 - g)) * (1.0 + 0x1p-50);
+    const double dl = a.cgap[a.asn[i]];
+    if (!(dl > ea)) return false;
+    const double t = dl - ea;
+    return t * t * (1.0 - g) * (1.0 - 0x1p-48) >= cur;
+}
+
+// per round: a lower bound of ||X[new center] - X[center a]|| for every earlier center
+// a < round (one warp each; FP64 sum of squared differences of the float rows, shrunk by its
+// rounding bound)
+__global__ void __launch_bounds__(256) k_kmpp_center_gap(const KmppArgs a, uint32_t round, double *gap) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t ca = uint32_t((blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5);
+    if (ca >= round) return;
+    const uint64_t c = *a.newc, o = a.center_ids[ca];
+    const float *x = a.X + c * a.d, *y = a.X + o * a.d;
+    double s = 0.0;
+    for (uint64_t j = lane; j < a.d; j += 32) {
+        const double df = double(x[j]) - double(y[j]);
+        s = fma(df, df, s);
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    if (lane == 0) gap[ca] = sqrt(s * (1.0 - double(a.d + 16) * 0x1p-50)) * (1.0 - 0x1p-50);
+}
+
 // first center from u[0]
 __global__ void k_kmpp_first(const double *u, uint64_t n, uint64_t *newc, uint32_t *center_ids) {
     uint64_t fc = uint64_t(u[0] * double(n));
@@ -104,6 +142,7 @@ __global__ void __launch_bounds__(256) k_kmpp_dense(const KmppArgs a, int first)
         }
         cur = a.dist[i];
         if (cur <= 0.0) return;
+        if (MSR == SQRL2 && a.cgap && kp_prune(a, i, cur)) return;
     }
     PairScalars s = {};
     if (MSR != SQRL2) s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], a.rowsum[c], a.d);
@@ -480,8 +519,13 @@ __global__ void __launch_bounds__(128) k_kmpp_dense_staged(const KmppArgs a, int
         } else {
             cur = a.dist[i];
             if (cur <= 0.0) active = false;
+            else if (MSR == SQRL2 && a.cgap && kp_prune(a, i, cur)) active = false;
         }
     }
+    // rows that need no distance are not staged; a CTA with none left stops here
+    __shared__ unsigned char act_s[128];
+    act_s[t] = active ? 1 : 0;
+    if (!__syncthreads_or(active ? 1 : 0)) return;
     PairScalars s = {};
     if (active && MSR != SQRL2) s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], a.rowsum[c], a.d);
     const uint64_t d = a.d;
@@ -491,7 +535,7 @@ __global__ void __launch_bounds__(128) k_kmpp_dense_staged(const KmppArgs a, int
         const int kmax = int(umin64(32, d - k0));
         for (int e = t; e < 128 * 8; e += 128) {
             const int r = e >> 3, q4 = e & 7;
-            const bool ok = row0 + r < a.n && 4 * q4 < kmax;
+            const bool ok = act_s[r] && 4 * q4 < kmax;
             kp_cp_async16(&xs[buf][r][4 * q4], ok ? a.X + (row0 + r) * d + k0 + 4 * q4 : a.X, ok ? 16 : 0);
         }
         if (t < 8) {
@@ -586,6 +630,7 @@ static int update(const KmppArgs &a, int first, uint32_t round, int sms, cudaStr
 
 int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st) {
     KmppArgs a = a0;
+    a.cgap = nullptr;
     const unsigned tb = 256, tg = unsigned(umin64((a.d + tb - 1) / tb, 1024));
     MC_CUDA_TRY(cudaMemsetAsync(a.asn, 0, a.n * sizeof(uint32_t), st));
     k_kmpp_first<<<1, 1, 0, st>>>(u_dev, a.n, a.newc, a.center_ids), note_launch();
@@ -595,9 +640,22 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
         k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
     }
     MC_TRY(update(a, 1, 0, sms, st));
+    // dense SQRL2 over a large matrix: rounds after the first prune by the triangle
+    // inequality (one more small launch per round; the results are unchanged)
+    const bool prune = !a.csr && a.msr == SQRL2 && a.k > 1 && a.n * a.d >= (uint64_t(1) << 20);
+    DBuf<double> gap;
+    if (prune) {
+        MC_TRY(gap.alloc(a.k, st));
+        const double g = double(a.d + 2) * 0x1p-24;
+        a.prune_g = g / (1.0 - g);
+    }
     DetInput in{a.w ? DET_F64_W : DET_F64, a.dist, nullptr, a.w, a.n};
     for (uint32_t ci = 1; ci < a.k; ++ci) {
         MC_TRY(launch_det_draw(in, chunk_tmp, u_dev + ci, 0.0, 1, a.dist, a.newc, st));
+        if (prune) {
+            k_kmpp_center_gap<<<unsigned((ci + 7) / 8), 256, 0, st>>>(a, ci, gap.p), note_launch();
+            a.cgap = gap.p;
+        }
         if (a.csr && !fused) {
             // CSR centers are densified into cbuf; the dense update reads the center row itself
             k_kmpp_take<<<tg, tb, 0, st>>>(a, ci), note_launch();

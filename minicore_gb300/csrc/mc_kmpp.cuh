@@ -27,6 +27,10 @@ struct KmppArgs {
     const uint32_t *grp = nullptr;  // CSR JSD: per-row group of equal rinc
     const float *gval = nullptr;    // CSR JSD: rinc of each group
     uint32_t ngrp = 0;
+    // dense SQRL2 pruning (rounds after the first): lower bounds of the distance from the new
+    // center to each earlier center, and the relative error bound of an FP32 row distance
+    const double *cgap = nullptr;
+    double prune_g = 0.0;
 };
 
 int run_kmeanspp(const KmppArgs &a, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st);

@@ -195,3 +195,36 @@ def test_csr_band_kernel_many_bands_equals_default(mc, msr, prior, tmp_path):
     assert np.array_equal(got[0][0], got[5][0])
     assert np.array_equal(got[0][1], got[5][1], equal_nan=True)
     mc.autotune_reset()
+
+
+def test_csr_l1_union_walk_variants_equal_oracle(mc, orc, tmp_path):
+    """L1 over CSR rows with prior 0 (pair-dependent pv): the register-window lockstep walk
+    (variant 0) and the per-row lockstep / per-lane merge kernel (variant 1), forced in turn,
+    both equal the oracle's all-column walk bit for bit; rows longer than a 32-element window,
+    empty rows and a union longer than 32 columns are included."""
+    rng = np.random.default_rng(77)
+    n, d = 1500, 700
+    X = sp.random(n, d, density=0.08, format="csr", random_state=rng,
+                  data_rvs=lambda s: rng.integers(1, 9, s).astype(np.float32)).tolil()
+    for i in range(0, n, 89):
+        X.rows[i], X.data[i] = [], []
+    X = X.tocsr().astype(np.float32)
+    X.sort_indices()
+    C = np.asarray(X[np.arange(3, n, 40)[:37]].toarray(), np.float32)
+    C[:, ::5] += 1.5
+    oasn, ocost = orc.assign(X, C, 0, 0.0)
+    mc.autotune_reset()
+    mc.autotune(True)
+    _assign(mc, X, C, 0, 0.0)
+    keys = [k for k in mc.autotune_report()["entries"] if k.startswith("csr_l1_union|")]
+    assert len(keys) == 1
+    for v in (0, 1):
+        mc.autotune_reset()
+        path = tmp_path / f"l1{v}.tsv"
+        path.write_text(f"{keys[0]}\t{v}\t\n")
+        mc.autotune_load(str(path))
+        asn, cost = _assign(mc, X, C, 0, 0.0)
+        assert mc.autotune_report()["entries"][keys[0]]["variant"] == v
+        assert np.array_equal(asn, oasn), v
+        assert np.array_equal(cost, ocost), v
+    mc.autotune_reset()

@@ -214,6 +214,25 @@ def test_kmeanspp_dense_matches_oracle(mc, orc, msr):
         assert np.array_equal(costs, ocosts.astype(np.float32))
 
 
+@pytest.mark.parametrize("weighted", [False, True])
+@pytest.mark.parametrize("d", [32, 61])
+def test_kmeanspp_dense_sqrl2_pruned_matches_oracle(mc, orc, weighted, d):
+    """Over n d >= 2^20 values the dense SQRL2 rounds skip rows whose distance to the new
+    center provably cannot beat their current one (triangle inequality with FP32 rounding
+    bounds); ids, assignments and costs stay bit-identical to the oracle, which evaluates
+    every row.  Well-separated components (most rows pruned in later rounds), duplicated
+    rows (zero distances), d not a multiple of 4 (the unstaged kernel)."""
+    n = 50_000 if d == 32 else 20_000
+    X = _mixture(n, d, 60, seed=d, spread=20.0)
+    X[1000:1200] = X[0]
+    w = np.random.default_rng(d).random(n) + 0.05 if weighted else None
+    ids, asn, costs = mc.kmeanspp(X, 48, msr=2, seed=77, weights=w)
+    oids, oasn, ocosts = orc.kmeanspp(X, 48, 2, 0.0, orc.uniforms(77, 48), weights=w)
+    assert np.array_equal(ids, oids)
+    assert np.array_equal(asn.astype(np.uint32), oasn)
+    assert np.array_equal(costs, ocosts.astype(np.float32))
+
+
 @pytest.mark.parametrize("msr,trials,weighted", [(2, 3, False), (2, 2, True), (0, 4, False)])
 def test_kmeanspp_greedy_matches_oracle(mc, orc, msr, trials, weighted):
     """n_local_trials > 1 (greedy seeding, kmeans.h:79-177): ids, assignments and distances
