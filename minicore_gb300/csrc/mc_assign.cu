@@ -859,16 +859,30 @@ __global__ void __launch_bounds__(kBandThreads, 1) k_assign_sparse_band(AssignAr
                     const uint32_t held = wst[r] >> 8;
                     const unsigned in = __ballot_sync(0xffffffffu, uint32_t(lane) < held && wcol[r] < bend);
                     const uint32_t m = uint32_t(__popc(in));
-                    for (uint32_t q = wst[r] & 0xffu; q < m; ++q) {
-                        const uint32_t c = __shfl_sync(0xffffffffu, wcol[r], int(q));
-                        const float g = __shfl_sync(0xffffffffu, wg[r], int(q));
-                        const float2 cv = tb[(c - b0) * 32];
+                    // batches of 8: the 8 shared loads issue before the chain of fmaf uses
+                    // them; slots past m load column b0 and are not added
+                    for (uint32_t q0 = wst[r] & 0xffu; q0 < m; q0 += 8) {
+                        float2 cv[8];
+                        float gq[8];
 #pragma unroll
-                        for (int h = 0; h < 2; ++h) {
-                            const float cc = h ? cv.y : cv.x;
-                            if (MSR == MKL || MSR == HELLINGER) acc[r][h] = fmaf(cc, g, acc[r][h]);
-                            else if (MSR == SQRL2) acc[r][h] = fmaf(g, g - 2.f * cc, acc[r][h]);
-                            else acc[r][h] = acc[r][h] + (fabsf(cc - g) - fabsf(cc - pv));
+                        for (int u = 0; u < 8; ++u) {
+                            const uint32_t q = q0 + uint32_t(u);
+                            const uint32_t c = __shfl_sync(0xffffffffu, wcol[r], int(q & 31u));
+                            gq[u] = __shfl_sync(0xffffffffu, wg[r], int(q & 31u));
+                            cv[u] = tb[(q < m ? c - b0 : 0u) * 32];
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            if (q0 + uint32_t(u) < m) {
+#pragma unroll
+                                for (int h = 0; h < 2; ++h) {
+                                    const float cc = h ? cv[u].y : cv[u].x;
+                                    const float g = gq[u];
+                                    if (MSR == MKL || MSR == HELLINGER) acc[r][h] = fmaf(cc, g, acc[r][h]);
+                                    else if (MSR == SQRL2) acc[r][h] = fmaf(g, g - 2.f * cc, acc[r][h]);
+                                    else acc[r][h] = acc[r][h] + (fabsf(cc - g) - fabsf(cc - pv));
+                                }
+                            }
                         }
                     }
                     if (m > (wst[r] & 0xffu)) wst[r] = (wst[r] & 0xff00u) | m;

@@ -43,11 +43,12 @@ int run_kmeanspp_greedy(const KmppArgs &a, uint32_t L, uint64_t seed, double *ch
 // for wide rows, and for large sparse matrices: each round then pays a few microseconds of
 // dependent FP64 sums for the constants (about 75 ns per dependent add on this GPU), which
 // the float column loop of k_kmpp_csr, O(d) per row (two logf per column for MKL), undercuts
-// only while the whole column loop is small (n d < 2^22) or the rows are not sparse
-// (more than one nonzero in eight columns)
+// only while the whole column loop is small (n d < 2^25: tens of microseconds of logf per
+// round, about the constants' latency) or the rows are not sparse (more than one nonzero in
+// eight columns)
 inline bool kmpp_csr_nnz_path(uint64_t n, uint64_t d, uint64_t nnz) {
     if (d > 2048) return true;
-    return n * d >= (uint64_t(1) << 22) && nnz * 8 <= n * d;
+    return n * d >= (uint64_t(1) << 25) && nnz * 8 <= n * d;
 }
 
 // C[c] = row ids[c], c < k (CSR rows densified into d columns)

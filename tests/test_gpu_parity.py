@@ -311,10 +311,10 @@ def test_kmeanspp_csr_nnz_path(mc, orc, msr, prior):
 
 @pytest.mark.parametrize("msr,prior", [(5, 1.0), (2, 0.0), (6, 1.0), (0, 1.0), (4, 1.0)])
 def test_kmeanspp_csr_large_sparse_nnz_path(mc, orc, msr, prior):
-    """A large sparse matrix with narrow rows (n d >= 2^22, d <= 2048, fewer than one
+    """A large sparse matrix with narrow rows (n d >= 2^25, d <= 2048, fewer than one
     nonzero in eight columns) takes the O(nnz) update: draws bit-exact given the GPU's own
     distances, distances within the CSR tolerance of the oracle's merge."""
-    S = _counts(20000, 256, 0.02, seed=60 + msr)
+    S = _counts(20000, 1700, 0.003, seed=60 + msr)
     ids = _replay_draws(mc, orc, S, 8, msr, prior, 21)
     _, asn, costs = mc.kmeanspp(S, 8, msr=msr, prior=prior, seed=21)
     _check_seed_costs(orc, S, ids, costs, msr, prior)
