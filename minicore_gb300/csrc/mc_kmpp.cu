@@ -229,8 +229,11 @@ __global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, u
 //   SQRL2  key = max(K0 + sum x (x - 2c), 0)                  K0 = sum c^2
 //   L1     key = (K0 + sum |c' - (x+pv)| - |c' - pv|) / 2     K0 = sum |c' - pv|, c' = c + pv
 //   MKL    key = K0 - log(rinc) K1 + sum a (log rinc - log b) K0 = sum a log a, K1 = sum a
-//   Hell.  key = sqrt(K0 + B - 2 sqrt(rinc) K1 + 2 sum sqrt(a) (sqrt(rinc) - sqrt(b)))
-//          K0 = sum a, K1 = sum sqrt a, B = sum over all columns of b
+//   Hell.  key = sqrt(K0 - 2 s K1 + d s^2 + sum ((t - sqrt b)^2 - (t - s)^2))
+//          t = sqrt a (float), s = sqrt(rinc), K0 = sum t^2, K1 = sum t; the zero columns'
+//          part sum (t - s)^2 is formed whole and the nonzero terms in FP64, so a row equal
+//          to the center gets a distance near 0 (a sum of a + b - 2 sqrt(ab) cancels to the
+//          float rounding of its terms, which the square root lifts to ~1e-4)
 //   JSD    key = (Z[g] + sum (b log b - r log r) + sum (m0 log(m0/2) - m1 log(m1/2))) / 2
 //          m0 = a + r, m1 = a + b, r = rinc of the row's group g, Z[g] = sum over all
 //          columns of f(a, r) (k_kmpp_jsd_zcol)
@@ -266,7 +269,7 @@ __global__ void __launch_bounds__(1024) k_kmpp_center_prep(const KmppArgs a) {
                 s1 = s1 + double(av);
             } else {
                 t = sqrtf(av);
-                s0 = s0 + double(av);
+                s0 = s0 + double(t) * double(t);
                 s1 = s1 + double(t);
             }
         }
@@ -352,9 +355,10 @@ __device__ __forceinline__ void kp_nnz_rows(const KmppArgs &a, int first, uint32
                     acc = acc + (m0 * logf(m0 * 0.5f) - m1 * logf(m1 * 0.5f));
                     bsum = bsum + double(b * logf(b) - rlr);
                 } else {
+                    // (sqrt a - sqrt b)^2 - (sqrt a - sqrt r)^2 in FP64 from the float roots
                     const float b = x * rsi + rinc;
-                    acc = fmaf(cj, srinc - sqrtf(b), acc);
-                    bsum = bsum + double(b);
+                    const double dd = double(cj) - double(sqrtf(b)), de = double(cj) - double(srinc);
+                    bsum = bsum + (dd * dd - de * de);
                 }
             }
 #pragma unroll
@@ -377,8 +381,8 @@ __device__ __forceinline__ void kp_nnz_rows(const KmppArgs &a, int first, uint32
                 key = post_divergence(float((a.cconst[a.grp[i]] + bsum + double(acc)) * 0.5));
                 v = double(key);
             } else {
-                const double bx = bsum + double(a.d - (pe - pb)) * double(rinc);
-                double t = K0 + bx - 2.0 * double(srinc) * K1 + 2.0 * double(acc);
+                const double sr = double(srinc);
+                double t = (K0 - 2.0 * sr * K1 + double(a.d) * sr * sr) + bsum;
                 key = float(sqrt(t < 0.0 ? 0.0 : t));
                 v = double(key) * kSqrt1_2;
             }
@@ -457,7 +461,7 @@ __global__ void __launch_bounds__(1024) k_kmpp_csr_fused(const KmppArgs a, int f
                 s1 = s1 + double(av);
             } else {
                 t = sqrtf(av);
-                s0 = s0 + double(av);
+                s0 = s0 + double(t) * double(t);
                 s1 = s1 + double(t);
             }
         }
