@@ -945,12 +945,31 @@ def serving_main(args):
 # ------------------------------------------------------------------------------------
 # C3: dense 4M x 128, k = 1024 (the headline in BF16; TF32 as a sub-line)
 # ------------------------------------------------------------------------------------
+TC_PASS1_VARIANTS = ["k_tc_assign<{p}, TC_TOP2, BN 256, 4 stages>", "k_tc_assign<{p}, TC_TOP2, BN 256, 3 stages>",
+                     "k_tc_assign<{p}, TC_TOP2, BN 128, 4 stages>", "k_tc_assign<{p}, TC_TOP2, BN 128, 6 stages>",
+                     "k_tc_top2_res<{p}> (centers resident in shared memory, 2 groups of 512)"]
+
+
+def tc_pass1_variant(precision, kp=1024):
+    """The pass 1 kernel the autotuner kept for the 4M x 128, k = 1024 bucket (kp % 256 == 0:
+    variants 0-3 are the streaming tile shapes, 4 the resident-centers kernel)."""
+    import minicore_gb300 as mc
+    for key, e in mc.autotune_report().get("entries", {}).items():
+        if key.startswith(f"tc1|{precision}|kp{kp}|d2^7|n2^22"):
+            v = int(e["variant"])
+            name = TC_PASS1_VARIANTS[v] if v < len(TC_PASS1_VARIANTS) else f"variant {v}"
+            return name.format(p=precision) + " (pass 1: every row x every center)", {
+                "variant": v, "ms": e.get("ms")}
+    return TC_PASS1_VARIANTS[0].format(p=precision) + " (pass 1: every row x every center; untuned default)", None
+
+
 def tc_roofline(phases, n, precision, pk, pk_kind):
     """Pass 1 of the tensor-core assignment (every row x every center): 2 n k d FLOP per
     launch against the measured BF16 burst peak (TF32: half of it, the tensor pipe's TF32
     rate being half its BF16 rate)."""
     flops = 2.0 * n * K * D
     ms, launches = kernel_ms(phases, "tc_pass1_top2")
+    kernel, variant = tc_pass1_variant(precision)
     peak = pk.get("bf16_tflops", 1935.7) * (0.5 if precision == "tf32" else 1.0)
     achieved = flops / (ms * 1e-3) / 1e12
     traffic = None
@@ -964,7 +983,7 @@ def tc_roofline(phases, n, precision, pk, pk_kind):
     return {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
             "traffic": traffic,
             "peak_source": f"{pk_kind} bf16_tflops (burst)" + (" / 2 for TF32" if precision == "tf32" else ""),
-            "kernel": f"k_tc_assign<{precision}, TC_TOP2> (pass 1: every row x every center)",
+            "kernel": kernel, "autotune_variant": variant,
             "kernel_ms_per_launch": ms, "launches": launches,
             "algorithmic": f"2*n*k*d = {flops:.4g} FLOP per launch (n={n}, k={K}, d={D})"}
 

@@ -210,6 +210,56 @@ __device__ inline void tmem_ld32(uint32_t taddr, float *v) {
 __device__ inline void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ inline void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+__device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(unsigned long long v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+// three-input minimum (sm_100 family)
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Pass 1 epilogue over 32 accumulator columns (centers j0 .. j0 + 31, norms cn32[0 .. 31]):
+// v_j = ||c_j||^2 - 2 acc_j
+// (packed f32x2 FMA, each half the IEEE fmaf(-2, acc, ||c||^2)), padding centers (j >= k) at
+// +inf, the minimum of each 8-center subgroup, merged into the row's (m1, m2, sg1): the two
+// smallest subgroup minima and the first subgroup holding m1.
+__device__ __forceinline__ void top2_group32(float (&v)[32], const float *cn32, uint32_t j0, uint32_t k, float &m1,
+                                             float &m2, uint32_t &sg1) {
+    const float INF = __int_as_float(0x7f800000);
+    const unsigned long long m2x = pk2(-2.f, -2.f);
+    const float4 *c4 = reinterpret_cast<const float4 *>(cn32);
+#pragma unroll
+    for (int q4 = 0; q4 < 8; ++q4) {
+        const float4 c = c4[q4];
+        unsigned long long r0, r1;
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r0) : "l"(pk2(v[4 * q4 + 0], v[4 * q4 + 1])), "l"(m2x), "l"(pk2(c.x, c.y)));
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r1) : "l"(pk2(v[4 * q4 + 2], v[4 * q4 + 3])), "l"(m2x), "l"(pk2(c.z, c.w)));
+        upk2(r0, v[4 * q4 + 0], v[4 * q4 + 1]);
+        upk2(r1, v[4 * q4 + 2], v[4 * q4 + 3]);
+    }
+    if (j0 + 32 > k) {  // padding centers take no part
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (j0 + uint32_t(i) >= k) v[i] = INF;
+    }
+#pragma unroll
+    for (int sg = 0; sg < 4; ++sg) {
+        const float *w = v + 8 * sg;
+        const float sv = fmin3(fmin3(w[0], w[1], w[2]), fmin3(w[3], w[4], w[5]), fminf(w[6], w[7]));
+        const bool lower = sv < m1;
+        m2 = fminf(m2, fmaxf(m1, sv));
+        sg1 = lower ? (j0 >> 3) + uint32_t(sg) : sg1;
+        m1 = fminf(m1, sv);
+    }
+}
+
 }  // namespace tc
 
 struct TcArgs {
@@ -382,38 +432,18 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
                     float v[32];
                     tmem_ld32(taddr + g * 32, v);
                     const uint32_t j0 = nc * BN + part * PCOLS + g * 32;
-                    const float4 *c4 = reinterpret_cast<const float4 *>(cnp + j0);
-#pragma unroll
-                    for (int q4 = 0; q4 < 8; ++q4) {
-                        const float4 c = c4[q4];
-                        v[4 * q4 + 0] = fmaf(-2.f, v[4 * q4 + 0], c.x);
-                        v[4 * q4 + 1] = fmaf(-2.f, v[4 * q4 + 1], c.y);
-                        v[4 * q4 + 2] = fmaf(-2.f, v[4 * q4 + 2], c.z);
-                        v[4 * q4 + 3] = fmaf(-2.f, v[4 * q4 + 3], c.w);
-                    }
                     if (MODE == TC_TOP2) {
-                        if (j0 + 32 > a.k) {  // the chunk's padding centers take no part
-#pragma unroll
-                            for (int i = 0; i < 32; ++i)
-                                if (j0 + uint32_t(i) >= a.k) v[i] = INF;
-                        }
-                        float smin[4];
-#pragma unroll
-                        for (int sg = 0; sg < 4; ++sg) {
-                            const float *w = v + 8 * sg;
-                            smin[sg] = fminf(fminf(fminf(w[0], w[1]), fminf(w[2], w[3])),
-                                             fminf(fminf(w[4], w[5]), fminf(w[6], w[7])));
-                        }
-                        // top-2 over the row's subgroup minima, with the subgroup of the minimum
-#pragma unroll
-                        for (int sg = 0; sg < 4; ++sg) {
-                            const float sv = smin[sg];
-                            const bool lower = sv < m1;
-                            m2 = fminf(m2, fmaxf(m1, sv));
-                            sg1 = lower ? (j0 >> 3) + uint32_t(sg) : sg1;
-                            m1 = fminf(m1, sv);
-                        }
+                        top2_group32(v, cnp + j0, j0, a.k, m1, m2, sg1);
                     } else {
+                        const float4 *c4 = reinterpret_cast<const float4 *>(cnp + j0);
+#pragma unroll
+                        for (int q4 = 0; q4 < 8; ++q4) {
+                            const float4 c = c4[q4];
+                            v[4 * q4 + 0] = fmaf(-2.f, v[4 * q4 + 0], c.x);
+                            v[4 * q4 + 1] = fmaf(-2.f, v[4 * q4 + 1], c.y);
+                            v[4 * q4 + 2] = fmaf(-2.f, v[4 * q4 + 2], c.z);
+                            v[4 * q4 + 3] = fmaf(-2.f, v[4 * q4 + 3], c.w);
+                        }
                         float smin[4];
 #pragma unroll
                         for (int sg = 0; sg < 4; ++sg) {
@@ -460,6 +490,190 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         // copies still in flight into this CTA's shared memory: wait for them (bounded)
         for (int s = 0; s < STAGES; ++s)
             if (sm->outstanding[s]) mbar_drain(&sm->full[s], sm->out_parity[s]);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// Pass 1 with the centers resident in shared memory.  Streaming the center operand for every
+// row tile (k_tc_assign) moves (128 + 256) x K operand elements through L2 per 128 x 256 x K
+// MMA block, about 16 TB/s at this kernel's pace; here the centers are split into groups of
+// `gch` 256-center chunks that fit shared memory next to two row-tile stages, each CTA loads
+// its group's centers once and then streams row tiles only, and the rows' tiles are read once
+// per group.  CTA b serves group b % G and row tiles b / G, b / G + T, ... (T = grid / G).
+// The epilogue is the TC_TOP2 one; each group writes its own column parts, so a row has
+// G x PARTS (m1, m2, subgroup) entries at [row][g][part] for k_tc_select to merge.
+namespace tc {
+template <int KB>
+struct ResShape {
+    static constexpr int A_TILE = KB * A_STAGE;                  // a row tile's k-blocks
+    static constexpr int ASTAGES = KB == 1 ? 4 : 2;
+    static constexpr int GCH = KB == 1 ? 4 : 2;                  // 256-center chunks per group
+    static constexpr int B_CHUNK = KB * 256 * KBYTES;            // 32 KB per k-block
+    static constexpr int SMEM = ASTAGES * A_TILE + GCH * B_CHUNK + GCH * 256 * 4;
+};
+struct ResSmem {
+    uint64_t afull[4], aempty[4], bfull, acc_full[2], acc_empty[2], drain;
+    uint32_t tmem_base;
+    int abort;
+    int a_out[4], b_out;
+    uint32_t a_par[4];
+};
+}  // namespace tc
+
+template <bool TF32, int KB>
+__global__ void __launch_bounds__(tc::THREADS, 1)
+    k_tc_top2_res(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a,
+                  uint32_t G, uint32_t nchunks) {
+    using namespace tc;
+    using RS = ResShape<KB>;
+    constexpr int BN = 256, PCOLS = BN / PARTS, ASTAGES = RS::ASTAGES;
+    extern __shared__ __align__(1024) unsigned char smraw[];
+    unsigned char *base = reinterpret_cast<unsigned char *>((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
+    unsigned char *astages = base;
+    unsigned char *bres = base + ASTAGES * RS::A_TILE;
+    float *cn_s = reinterpret_cast<float *>(bres + RS::GCH * RS::B_CHUNK);
+    ResSmem *sm = reinterpret_cast<ResSmem *>(reinterpret_cast<unsigned char *>(cn_s) + RS::GCH * 256 * 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t g = blockIdx.x % G, T = gridDim.x / G, t0 = blockIdx.x / G;
+    const uint32_t c0 = g * RS::GCH;                                   // first chunk of the group
+    const uint32_t gch = umin64(RS::GCH, nchunks - c0);                // chunks of this group
+    const uint32_t ntiles = a.ntiles;
+    for (uint32_t j = threadIdx.x; j < gch * 256; j += THREADS) cn_s[j] = a.cnp[c0 * 256 + j];
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ASTAGES; ++s) {
+            mbar_init(&sm->afull[s], 1);
+            mbar_init(&sm->aempty[s], 1);
+            sm->a_out[s] = 0;
+            sm->a_par[s] = 0;
+        }
+        mbar_init(&sm->bfull, 1);
+        sm->b_out = 0;
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&sm->acc_full[b], 1);
+            mbar_init(&sm->acc_empty[b], 32 * EPI_WARPS);
+        }
+        mbar_init(&sm->drain, 1);
+        sm->abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm->tmem_base)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = sm->tmem_base;
+
+    if (warp == 0) {
+        // ---------------- TMA producer: the group's centers once, then row tiles ----------------
+        if (lane == 0 && t0 < ntiles) {
+            mbar_expect_tx(&sm->bfull, gch * RS::B_CHUNK);
+            sm->b_out = 1;
+            for (uint32_t nc = 0; nc < gch; ++nc)
+                for (int kb = 0; kb < KB; ++kb)
+                    tma_load_2d(bres + (nc * KB + kb) * (256 * KBYTES), &tmB, &sm->bfull, kb * (TF32 ? 32 : 64),
+                                int((c0 + nc) * BN));
+            uint32_t s = 0, ph = 0;
+            for (uint32_t m = t0; m < ntiles; m += T) {
+                if (!mbar_wait(&sm->aempty[s], ph ^ 1, sm, a.err, 1)) break;
+                unsigned char *st = astages + s * RS::A_TILE;
+                mbar_expect_tx(&sm->afull[s], RS::A_TILE);
+                sm->a_out[s] = 1;
+                sm->a_par[s] = ph;
+                for (int kb = 0; kb < KB; ++kb)
+                    tma_load_2d(st + kb * A_STAGE, &tmA, &sm->afull[s], kb * (TF32 ? 32 : 64), int(m * BM));
+                if (++s == ASTAGES) { s = 0; ph ^= 1; }
+            }
+        }
+    } else if (warp == 1) {
+        // ---------------- MMA issuer ----------------
+        if (lane == 0 && t0 < ntiles) {
+            bool ok = true;
+            if (a.stall_test && !mbar_wait(&sm->drain, 0, sm, a.err, 5)) ok = false;
+            if (ok && !mbar_wait(&sm->bfull, 0, sm, a.err, 6)) ok = false;
+            if (ok) sm->b_out = 0;
+            uint32_t s = 0, ph = 0, acc_it = 0;
+            for (uint32_t m = t0; m < ntiles && ok; m += T) {
+                if (!mbar_wait(&sm->afull[s], ph, sm, a.err, 3)) { ok = false; break; }
+                sm->a_out[s] = 0;
+                fence_after();
+                const uint64_t ad0 = sdesc(astages + s * RS::A_TILE);
+                for (uint32_t nc = 0; nc < gch && ok; ++nc, ++acc_it) {
+                    const uint32_t buf = acc_it & 1, use = acc_it >> 1;
+                    if (!mbar_wait(&sm->acc_empty[buf], (use & 1) ^ 1, sm, a.err, 2)) { ok = false; break; }
+                    fence_after();
+                    const uint32_t d_tmem = tmem + buf * BN;
+#pragma unroll
+                    for (int kb = 0; kb < KB; ++kb) {
+                        const uint64_t ad = ad0 + uint64_t((kb * A_STAGE) >> 4);
+                        const uint64_t bd = sdesc(bres + (nc * KB + kb) * (256 * KBYTES));
+#pragma unroll
+                        for (int ks = 0; ks < 4; ++ks)
+                            mma<TF32, BN>(d_tmem, ad + uint64_t(ks * 2), bd + uint64_t(ks * 2), (kb | ks) ? 1u : 0u);
+                    }
+                    mma_commit(&sm->acc_full[buf]);
+                }
+                if (!ok) break;
+                mma_commit(&sm->aempty[s]);  // the row tile's stage is free once these MMAs finish
+                if (++s == ASTAGES) { s = 0; ph ^= 1; }
+            }
+            mma_commit(&sm->drain);
+            mbar_drain(&sm->drain, 0);
+        }
+    } else {
+        // ---------------- epilogue (warps 2-17) ----------------
+        const int quarter = warp & 3;
+        const int part = (warp - 2) >> 2;
+        const uint32_t lane_base = uint32_t(quarter * 32) << 16;
+        const int rloc = quarter * 32 + lane;
+        const float INF = __int_as_float(0x7f800000);
+        uint32_t acc_it = 0;
+        bool ok = true;
+        for (uint32_t m = t0; m < ntiles && ok; m += T) {
+            const uint64_t row = uint64_t(m) * BM + rloc;
+            float m1 = INF, m2 = INF;
+            uint32_t sg1 = 0xffffffffu;
+            for (uint32_t nc = 0; nc < gch; ++nc, ++acc_it) {
+                const uint32_t buf = acc_it & 1, use = acc_it >> 1;
+                int got = 0;
+                if (lane == 0) got = mbar_wait(&sm->acc_full[buf], use & 1, sm, a.err, 4) ? 1 : 0;
+                got = __shfl_sync(0xffffffffu, got, 0);
+                __syncwarp();
+                if (!got) { ok = false; break; }
+                fence_after();
+                const uint32_t taddr = tmem + lane_base + buf * BN + part * PCOLS;
+                float v0[32], v1[32];
+                tmem_ld32(taddr, v0);
+                tmem_ld32(taddr + 32, v1);
+                fence_before();
+                mbar_arrive(&sm->acc_empty[buf]);  // both column groups are in registers
+                const uint32_t jl = nc * BN + part * PCOLS, j0 = c0 * 256 + jl;
+                top2_group32(v0, cn_s + jl, j0, a.k, m1, m2, sg1);
+                top2_group32(v1, cn_s + jl + 32, j0 + 32, a.k, m1, m2, sg1);
+            }
+            if (!ok) break;
+            if (row < a.n) {
+                const uint64_t o = (row * G + g) * PARTS + part;
+                a.b1[o] = m1;
+                a.b2[o] = m2;
+                a.j1[o] = m1 < INF ? sg1 : 0xffffffffu;
+            }
+        }
+    }
+    // ---------------- teardown ----------------
+    __syncthreads();
+    if (threadIdx.x == 0 && sm->abort) {
+        if (sm->b_out) mbar_drain(&sm->bfull, 0);
+        for (int s = 0; s < ASTAGES; ++s)
+            if (sm->a_out[s]) mbar_drain(&sm->afull[s], sm->a_par[s]);
     }
     fence_before();
     __syncthreads();
@@ -522,8 +736,8 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
                                                     uint32_t *key, uint32_t *crow, float *thrc, unsigned *count,
                                                     uint32_t cap, const uint4 *__restrict__ A, uint64_t row_u4,
                                                     uint4 *Xc, uint32_t *over_rows, unsigned long long *nover,
-                                                    unsigned long long *nmulti) {
-    static_assert(tc::PARTS == 4, "one 16-byte load per row and array");
+                                                    unsigned long long *nmulti, uint32_t ngroups) {
+    static_assert(tc::PARTS == 4, "one 16-byte load per row, group and array");
     __shared__ uint32_t mrow[8][32], mslot[8][32];  // the warp's multi rows and their slots
     const uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -533,14 +747,18 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
     if (row < n) {
         float m1 = INF, m2 = INF;
         uint32_t gr = ST_OVER;
-        const float4 v1 = reinterpret_cast<const float4 *>(b1)[row], v2 = reinterpret_cast<const float4 *>(b2)[row];
-        const uint4 vj = reinterpret_cast<const uint4 *>(j1)[row];
-        const float c1s[4] = {v1.x, v1.y, v1.z, v1.w}, c2s[4] = {v2.x, v2.y, v2.z, v2.w};
-        const uint32_t js[4] = {vj.x, vj.y, vj.z, vj.w};
+        // the column parts of every center group
+        for (uint32_t g = 0; g < ngroups; ++g) {
+            const uint64_t o = row * ngroups + g;
+            const float4 v1 = reinterpret_cast<const float4 *>(b1)[o], v2 = reinterpret_cast<const float4 *>(b2)[o];
+            const uint4 vj = reinterpret_cast<const uint4 *>(j1)[o];
+            const float c1s[4] = {v1.x, v1.y, v1.z, v1.w}, c2s[4] = {v2.x, v2.y, v2.z, v2.w};
+            const uint32_t js[4] = {vj.x, vj.y, vj.z, vj.w};
 #pragma unroll
-        for (int p = 0; p < tc::PARTS; ++p) {
-            if (c1s[p] < m1) gr = js[p];
-            top2_merge(m1, m2, c1s[p], c2s[p]);
+            for (int p = 0; p < tc::PARTS; ++p) {
+                if (c1s[p] < m1) gr = js[p];
+                top2_merge(m1, m2, c1s[p], c2s[p]);
+            }
         }
         const float cmax = *cmaxp;
         const float xn = sqrtf(rownorm[row]);
@@ -983,6 +1201,39 @@ static int tc_shape_launch(int shape, unsigned grid, const CUtensorMap &mA, cons
     }
 }
 
+// Pass 1 with resident centers (k_tc_top2_res): usable when a row has at most two k-blocks
+// and the centers fill whole 256-center chunks; G groups of GCH chunks, T = sms / G CTAs each.
+struct ResPlan {
+    bool ok = false;
+    uint32_t G = 1, grid = 0, nchunks = 0;
+    size_t smem = 0;
+};
+
+static ResPlan res_plan(uint32_t kb, uint32_t kp, int sms) {
+    ResPlan p;
+    if (kb < 1 || kb > 2 || kp % 256 != 0) return p;
+    const uint32_t gch = kb == 1 ? tc::ResShape<1>::GCH : tc::ResShape<2>::GCH;
+    p.nchunks = kp / 256;
+    p.G = (p.nchunks + gch - 1) / gch;
+    const uint32_t T = uint32_t(sms) / p.G;
+    if (T < 2) return p;
+    p.grid = T * p.G;
+    p.smem = size_t(kb == 1 ? tc::ResShape<1>::SMEM : tc::ResShape<2>::SMEM) + sizeof(tc::ResSmem) + 1024;
+    p.ok = true;
+    return p;
+}
+
+template <bool TF32>
+static int tc_res_launch(const ResPlan &p, uint32_t kb, const CUtensorMap &mA, const CUtensorMap &mB256, TcArgs a,
+                         cudaStream_t st) {
+    a.nchunks = p.nchunks;
+    auto kern = kb == 1 ? k_tc_top2_res<TF32, 1> : k_tc_top2_res<TF32, 2>;
+    MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(p.smem)));
+    kern<<<p.grid, tc::THREADS, p.smem, st>>>(mA, mB256, a, p.G, p.nchunks), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C, const float *cnorm, uint32_t k,
               int precision, const float *rownorm, uint32_t *asn, double *costs, int sms, cudaStream_t st,
               uint64_t *recheck_count, bool graph_mode) {
@@ -1030,9 +1281,11 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     MC_TRY(make_map(&mB128, Bptr, tf32, kp, d, dp, 128));
     if (wide) MC_TRY(make_map(&mB256, Bptr, tf32, kp, d, dp, 256));
     using tc::PARTS;
-    MC_TRY(s.b1.alloc(PARTS * n, st));
-    MC_TRY(s.b2.alloc(PARTS * n, st));
-    MC_TRY(s.j1.alloc(PARTS * n, st));
+    const ResPlan rp = res_plan(kb, kp, sms);
+    const uint64_t ngmax = rp.ok ? rp.G : 1;  // pass 1 writes PARTS entries per row and center group
+    MC_TRY(s.b1.alloc(PARTS * n * ngmax, st));
+    MC_TRY(s.b2.alloc(PARTS * n * ngmax, st));
+    MC_TRY(s.j1.alloc(PARTS * n * ngmax, st));
     MC_TRY(s.status.alloc(n, st));
     MC_TRY(s.key.alloc(n, st));
     const uint32_t nsg = kp / 8;  // subgroups of 8 centers
@@ -1093,9 +1346,18 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     const bool allow = !graph_mode && !a.stall_test;
     const std::string bucket = std::string(tf32 ? "|tf32" : "|bf16") + "|kp" + std::to_string(kp) + "|d" +
                                tune_bucket(d) + "|n" + tune_bucket(n);
+    // pass 1 variants: the tile shapes, then (where it fits) the resident-centers kernel; the
+    // output layout is that of the variant launched last
+    uint32_t ngroups = 1;
     {
         Phase ph("tc_pass1_top2", st);
-        MC_TRY(tune_launch("tc1" + bucket, nvar, 0, st, allow, [&](int v) -> int {
+        const int nvar1 = nvar + (rp.ok ? 1 : 0);
+        MC_TRY(tune_launch("tc1" + bucket, nvar1, 0, st, allow, [&](int v) -> int {
+            if (v == nvar) {
+                ngroups = rp.G;
+                return tf32 ? tc_res_launch<true>(rp, kb, mA, mB256, a, st) : tc_res_launch<false>(rp, kb, mA, mB256, a, st);
+            }
+            ngroups = 1;
             return tf32 ? tc_shape_launch<true, TC_TOP2>(shape_of(v), grid, mA, mB128, mB256, a, st)
                         : tc_shape_launch<false, TC_TOP2>(shape_of(v), grid, mA, mB128, mB256, a, st);
         }));
@@ -1106,7 +1368,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
         k_tc_select<<<unsigned((n + 255) / 256), 256, 0, st>>>(
             n, s.b1.p, s.b2.p, s.j1.p, rownorm, s.cnorm_p.p + kp, a.eta, a.gamma, nsg, s.status.p, s.key.p,
             s.crow.p, s.thrc.p, s.count.p, uint32_t(cap), static_cast<const uint4 *>(Aptr), row_u4, s.Xc.p,
-            s.over_rows.p, s.nrecheck.p + 1, s.nrecheck.p), note_launch();
+            s.over_rows.p, s.nrecheck.p + 1, s.nrecheck.p, ngroups), note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         // finalize order: rows grouped by subgroup, then multi rows, then OVER rows
         MC_TRY(launch_sort_by_key(s.key.p, nullptr, n, nsg + 2, s.sort, st));

@@ -125,12 +125,16 @@ def _assign_prec(mc, X, C, precision):
 
 
 @pytest.mark.parametrize("precision", ["bf16", "tf32"])
-@pytest.mark.parametrize("n,d,k", [(9000, 128, 512), (5000, 96, 100), (3001, 40, 300)])
+@pytest.mark.parametrize("n,d,k", [(9000, 128, 512), (5000, 96, 100), (3001, 40, 300), (6000, 128, 1280),
+                                   (4000, 64, 1536), (2500, 20, 1024)])
 def test_tc_every_tile_shape_equals_fp32(mc, precision, n, d, k, tmp_path):
     """Each tensor-core tile shape (BN 256 with 4 or 3 stages when the padded center count
     is a multiple of 256, BN 128 with 4 or 6 stages always), forced for both passes through a
     loaded decision, gives the FP32 path's assignments and costs bit for bit; with tuning on,
-    the first call records a decision per pass."""
+    the first call records a decision per pass.  Pass 1 has one more variant where a row is
+    at most two 128-byte k-blocks and the centers fill 256-center chunks: the centers resident
+    in shared memory, split into groups of 4 (one k-block) or 2 chunks, one group per CTA (the
+    cases above cover one group, two and three groups, and a last group with fewer chunks)."""
     rng = np.random.default_rng(n + k)
     mu = rng.normal(size=(max(2, k // 2), d)) * 2.0
     X = (mu[rng.integers(0, mu.shape[0], n)] + rng.normal(size=(n, d))).astype(np.float32)
@@ -147,7 +151,10 @@ def test_tc_every_tile_shape_equals_fp32(mc, precision, n, d, k, tmp_path):
     assert len(keys[1]) == 1 and len(keys[2]) == 1
     nvar = len(ent[keys[1][0]]["ms"])
     kp = (k + 127) // 128 * 128
-    assert nvar == (4 if kp % 256 == 0 else 2)
+    kb = -(-d * (4 if precision == "tf32" else 2) // 128)
+    resident = kp % 256 == 0 and kb <= 2
+    assert nvar == (4 if kp % 256 == 0 else 2) + (1 if resident else 0)
+    assert len(ent[keys[2][0]]["ms"]) == (4 if kp % 256 == 0 else 2)
     for v in range(nvar):
         mc.autotune_reset()
         path = tmp_path / f"tc{v}.tsv"
