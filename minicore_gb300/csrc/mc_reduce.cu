@@ -767,6 +767,76 @@ __global__ void k_centroid_chunks_csr_short(const float *__restrict__ vals, cons
     }
 }
 
+// The same sums for short rows and narrow bands (d <= 2048): the chunk's rows are taken
+// kCsrTileRows at a time and scattered into a dense [rows][512 columns] tile in shared
+// memory (rows in parallel, one warp each); then each thread walks its column down the tile
+// in row order.  A column's additions are the same as in k_centroid_chunks_csr_short (every
+// stored value of the column, rows ascending; a zero added by TwoSum or by the weighted fma
+// leaves the sum unchanged, so empty tile cells are skipped), so the partials are
+// bit-identical, but the rows of a batch are loaded concurrently instead of one dependent
+// round trip per row.
+constexpr int kCsrTileRows = 32, kCsrTileBand = 512;
+
+__global__ void __launch_bounds__(kCsrTileBand) k_centroid_chunks_csr_tile(
+    const float *__restrict__ vals, const uint32_t *__restrict__ idx, const uint64_t *__restrict__ indptr, uint64_t d,
+    const uint32_t *__restrict__ perm, const uint64_t *__restrict__ bucket_start,
+    const uint64_t *__restrict__ bucket_count, const uint64_t *__restrict__ chunk_start, uint32_t k, uint64_t ch,
+    const double *__restrict__ w, double *partial, double *partial_w) {
+    extern __shared__ __align__(16) float tile[];  // [kCsrTileRows][kCsrTileBand]
+    __shared__ uint64_t rb[kCsrTileRows], re[kCsrTileRows];
+    __shared__ double rw[kCsrTileRows];
+    const uint64_t q = blockIdx.x;
+    if (q >= chunk_start[k]) return;
+    const uint32_t c = find_bucket(chunk_start, k, q);
+    const uint64_t local = q - chunk_start[c];
+    const uint64_t r0 = local * ch, r1 = umin64(bucket_count[c], r0 + ch);
+    const uint32_t *rows = perm + bucket_start[c];
+    const uint64_t j0 = uint64_t(blockIdx.y) * kCsrTileBand, j1 = umin64(d, j0 + kCsrTileBand);
+    const int t = threadIdx.x, lane = t & 31, wp = t >> 5;
+    constexpr int NW = kCsrTileBand / 32;
+    const bool weighted = w != nullptr;
+    for (int e = t; e < kCsrTileRows * kCsrTileBand; e += kCsrTileBand) tile[e] = 0.f;
+    const uint64_t j = j0 + uint64_t(t);
+    float s = 0.f, er = 0.f;
+    double acc = 0.0, wq = 0.0;
+    for (uint64_t b0 = r0; b0 < r1; b0 += kCsrTileRows) {
+        const int nb = int(umin64(kCsrTileRows, r1 - b0));
+        if (t < nb) {
+            const uint32_t row = rows[b0 + t];
+            rb[t] = indptr[row];
+            re[t] = indptr[row + 1];
+            if (weighted) rw[t] = w[row];
+        }
+        __syncthreads();
+        for (int rr = wp; rr < nb; rr += NW)
+            for (uint64_t p = rb[rr] + lane; p < re[rr]; p += 32) {
+                const uint32_t col = idx[p];
+                if (col >= j0 && col < j1) tile[rr * kCsrTileBand + int(col - j0)] = vals[p];
+            }
+        __syncthreads();
+        if (j < j1) {
+            for (int rr = 0; rr < nb; ++rr) {
+                const float v = tile[rr * kCsrTileBand + t];
+                if (v != 0.f) {
+                    if (weighted) acc = fma(rw[rr], double(v), acc);
+                    else two_sum_add(s, er, v);
+                }
+            }
+        }
+        if (weighted && t == 0 && blockIdx.y == 0)
+            for (int rr = 0; rr < nb; ++rr) wq = wq + rw[rr];
+        __syncthreads();
+        for (int rr = wp; rr < nb; rr += NW)
+            for (uint64_t p = rb[rr] + lane; p < re[rr]; p += 32) {
+                const uint32_t col = idx[p];
+                if (col >= j0 && col < j1) tile[rr * kCsrTileBand + int(col - j0)] = 0.f;
+            }
+        __syncthreads();
+    }
+    if (j < j1) partial[q * d + j] = weighted ? acc : double(s) + double(er);
+    if (weighted && t == 0 && blockIdx.y == 0) partial_w[q] = wq;
+}
+
 // finalize: per (bucket, column): FP64 sum of chunk partials in order, divide, round.
 // Buckets with one row copy the row (here for dense rows X; CSR rows in
 // k_centroid_singletons_csr); empty buckets keep the old center.
@@ -837,12 +907,25 @@ int launch_centroids(const CentroidArgs &a, SortWork &w, cudaStream_t st, bool p
         // always the largest band's size: a per-call value could be lowered by another host
         // thread between this call's set and its launch
         // rows of 32 or more nonzeros on average: the register-pipelined kernel
-        auto kern = (a.nnz >= 32 * n) ? k_centroid_chunks_csr : k_centroid_chunks_csr_short;
-        MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(2 * 24576 * sizeof(float))));
-        kern<<<dim3(unsigned(max_chunks), nb), 256, smem, st>>>(
-            a.vals, a.idx, a.indptr, d, bw, w.perm.p, w.bucket_start.p, w.bucket_count.p, w.chunk_start.p, k, ch,
-            a.w, w.partial.p, w.partial_w.p), note_launch();
+        if (a.nnz < 32 * n && d <= 4 * uint64_t(kCsrTileBand)) {
+            // short rows over at most four 512-column bands: rows of a batch scattered into a
+            // dense shared-memory tile, columns walked in row order
+            const size_t tsm = size_t(kCsrTileRows) * kCsrTileBand * sizeof(float);
+            MC_CUDA_TRY(cudaFuncSetAttribute(k_centroid_chunks_csr_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(tsm)));
+            k_centroid_chunks_csr_tile<<<dim3(unsigned(max_chunks), unsigned((d + kCsrTileBand - 1) / kCsrTileBand)),
+                                         kCsrTileBand, tsm, st>>>(a.vals, a.idx, a.indptr, d, w.perm.p,
+                                                                  w.bucket_start.p, w.bucket_count.p,
+                                                                  w.chunk_start.p, k, ch, a.w, w.partial.p,
+                                                                  w.partial_w.p), note_launch();
+        } else {
+            auto kern = (a.nnz >= 32 * n) ? k_centroid_chunks_csr : k_centroid_chunks_csr_short;
+            MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             int(2 * 24576 * sizeof(float))));
+            kern<<<dim3(unsigned(max_chunks), nb), 256, smem, st>>>(
+                a.vals, a.idx, a.indptr, d, bw, w.perm.p, w.bucket_start.p, w.bucket_count.p, w.chunk_start.p, k,
+                ch, a.w, w.partial.p, w.partial_w.p), note_launch();
+        }
     }
     k_centroid_finalize<<<dim3(unsigned((d + 127) / 128), k < 65535 ? k : 65535), 128, 0, st>>>(
         w.partial.p, w.partial_w.p, w.chunk_start.p, w.bucket_count.p, k, d, a.w ? 1 : 0, a.centers, a.nan_flag,
