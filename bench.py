@@ -963,6 +963,19 @@ def tc_pass1_variant(precision, kp=1024):
     return TC_PASS1_VARIANTS[0].format(p=precision) + " (pass 1: every row x every center; untuned default)", None
 
 
+def tc_autotune_entries(precision, kp=1024):
+    """The autotuner's decisions for the tensor-core passes of this workload's shape bucket
+    (tc1: pass 1 kernel / tile shape, tc2: pass 2 tile shape), with each variant's measured
+    milliseconds."""
+    import minicore_gb300 as mc
+    out = {}
+    for key, e in mc.autotune_report().get("entries", {}).items():
+        for fam in ("tc1", "tc2"):
+            if key.startswith(f"{fam}|{precision}|kp{kp}|d2^7|n2^22"):
+                out[fam] = {"variant": int(e["variant"]), "ms": e.get("ms")}
+    return out
+
+
 def tc_roofline(phases, n, precision, pk, pk_kind):
     """Pass 1 of the tensor-core assignment (every row x every center): 2 n k d FLOP per
     launch against the measured BF16 burst peak (TF32: half of it, the tensor pipe's TF32
@@ -1578,6 +1591,7 @@ def main():
                 "recheck_rows_last_pass": recheck,
                 "accuracy_vs_fp64": accuracy,
                 "roofline": roofline, "phases_ms_timed_region": phases,
+                "autotune_tc": tc_autotune_entries(args.precision),
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk,
                 "job_latency_ms": (serving or {}).get("latency_ms"),

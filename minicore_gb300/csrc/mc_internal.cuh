@@ -107,6 +107,22 @@ constexpr int kDetThreads = 256;
 constexpr int kDetPer = 32;
 
 __host__ __device__ inline uint64_t det_chunks(uint64_t n) { return (n + kDetChunk - 1) / kDetChunk; }
+
+// from the root of a heap with P leaves (node j has children 2j, 2j + 1; leaves at [P, 2P)):
+// left when r < L or R is not positive, else r -= L; returns the leaf
+__device__ inline uint64_t det_heap_descend(const double *T, uint64_t P, double &r) {
+    uint64_t j = 1;
+    while (j < P) {
+        const double L = T[2 * j], R = T[2 * j + 1];
+        if (r < L || !(R > 0.0)) {
+            j = 2 * j;
+        } else {
+            r = r - L;
+            j = 2 * j + 1;
+        }
+    }
+    return j - P;
+}
 // leaves of the tree over the chunk totals (a power of two, at least 1)
 __host__ __device__ inline uint64_t det_leaves(uint64_t n) {
     uint64_t p = 1;

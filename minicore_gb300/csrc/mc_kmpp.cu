@@ -8,6 +8,9 @@
 #include "mc_kmpp.cuh"
 #include "mc_tune.cuh"
 
+#include <mutex>
+#include <unordered_map>
+
 namespace mc {
 
 template <int MSR>
@@ -632,7 +635,337 @@ static int update(const KmppArgs &a, int first, uint32_t round, int sms, cudaStr
     }
 }
 
+// ------------------------------------------------------------------------------------
+// Persistent seeding for small dense matrices: one thread-block cluster runs every round.
+// The rounds above cost four to five dependent launches each (about 40 us per round at
+// serving sizes, where the distance pass itself takes one or two); here the cluster's CTAs
+// update their own 32-row blocks of the distances, leave each block's pairwise FP64 sum in
+// `blk`, and meet at a cluster barrier; CTA 0 then builds every chunk's tree of 256 block
+// sums and the tree over the chunk totals, descends them with u[r] S to one row (the
+// arithmetic and descent of k_det_chunks / k_det_draw), and the CTAs meet again.  The
+// barriers are the hardware's cluster barriers (the cluster's CTAs are co-scheduled), taken
+// by every thread of every CTA the same number of times.  Distances, assignments, center ids
+// and draws are bit-identical to the launch-per-round path.
+// ------------------------------------------------------------------------------------
+constexpr int kKcThreads = 512;
+constexpr uint64_t kKcMaxRows = 32 * uint64_t(kDetChunk);  // 32 chunks: CTA 0's trees fit shared memory
+
+__device__ __forceinline__ uint32_t kc_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t kc_size() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+// every thread of every CTA of the cluster; writes before it are visible to reads after it
+__device__ __forceinline__ void kc_sync() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// one row's update in round `round` (k_kmpp_dense's arithmetic); returns its distance after it
+template <int MSR, bool VEC4>
+__device__ __forceinline__ double kc_row(const KmppArgs &a, uint64_t i, uint64_t c, bool first, uint32_t round) {
+    double cur = 0.0;
+    if (!first) {
+        if (i == c) {
+            a.dist[i] = 0.0;
+            return 0.0;
+        }
+        cur = a.dist[i];
+        if (cur <= 0.0) return cur;
+    }
+    PairScalars s = {};
+    if (MSR != SQRL2) s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], a.rowsum[c], a.d);
+    const float *xr = a.X + i * a.d, *cr = a.X + c * a.d;
+    float acc = 0.f;
+    if (VEC4) {
+        const float4 *x4 = reinterpret_cast<const float4 *>(xr), *c4 = reinterpret_cast<const float4 *>(cr);
+        const uint64_t d4 = a.d / 4;
+        uint64_t q = 0;
+        for (; q + 8 <= d4; q += 8) {
+            float4 xv[8], cv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                xv[u] = __ldg(x4 + q + u);
+                cv[u] = __ldg(c4 + q + u);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                kp_elem<MSR>(acc, cv[u].x, xv[u].x, s);
+                kp_elem<MSR>(acc, cv[u].y, xv[u].y, s);
+                kp_elem<MSR>(acc, cv[u].z, xv[u].z, s);
+                kp_elem<MSR>(acc, cv[u].w, xv[u].w, s);
+            }
+        }
+        for (; q < d4; ++q) {
+            const float4 xv = __ldg(x4 + q), cv = __ldg(c4 + q);
+            kp_elem<MSR>(acc, cv.x, xv.x, s);
+            kp_elem<MSR>(acc, cv.y, xv.y, s);
+            kp_elem<MSR>(acc, cv.z, xv.z, s);
+            kp_elem<MSR>(acc, cv.w, xv.w, s);
+        }
+    } else {
+        for (uint64_t j = 0; j < a.d; ++j) kp_elem<MSR>(acc, __ldg(cr + j), __ldg(xr + j), s);
+    }
+    const double v = kp_cost<MSR>(acc);
+    if (first) {
+        const double nv = (i == c) ? 0.0 : v;
+        a.dist[i] = nv;
+        return nv;
+    }
+    if (v < cur) {
+        a.dist[i] = v;
+        a.asn[i] = round;
+        return v;
+    }
+    return cur;
+}
+
+// pairwise sum of 32 consecutive values (det_block32's tree)
+__device__ __forceinline__ double kc_block32(const double *v0) {
+    double v[32];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) v[e] = v0[e];
+#pragma unroll
+    for (int sft = 1; sft < 32; sft <<= 1)
+#pragma unroll
+        for (int e = 0; e < 32; e += 2 * sft) v[e] = v[e] + v[e + sft];
+    return v[0];
+}
+
+template <int MSR, bool VEC4>
+__global__ void __launch_bounds__(kKcThreads, 1) k_kmpp_cluster(const KmppArgs a, const double *u, double *blk) {
+    extern __shared__ double H[];  // CTA 0: [chunks][512] heaps of the block sums (leaves at 256..511)
+    __shared__ double sval[kKcThreads + 32];
+    __shared__ double T[2 * 32], E[64];
+    __shared__ uint64_t sm_g, sm_b;
+    __shared__ double sm_r;
+    __shared__ int sm_pos;
+    const int t = threadIdx.x;
+    const uint32_t rank = kc_rank(), CS = kc_size();
+    const uint64_t n = a.n, nblk = (n + 31) / 32;
+    const uint64_t G = det_chunks(n), P = det_leaves(n);
+    const uint64_t b_lo = nblk * rank / CS, b_hi = nblk * (rank + 1) / CS;  // this CTA's 32-row blocks
+    const bool weighted = a.w != nullptr;
+    uint64_t c = uint64_t(u[0] * double(n));
+    if (c >= n) c = n - 1;
+    for (uint32_t round = 0; round < a.k; ++round) {
+        const bool first = round == 0;
+        if (!first) c = __ldcg(a.newc);
+        if (rank == 0 && t == 0) {
+            a.center_ids[round] = uint32_t(c);
+            if (!first) a.asn[c] = round;
+        }
+        // ---- distances of this CTA's rows, 512 at a time, and their 32-row block sums ----
+        for (uint64_t r0 = b_lo * 32; r0 < b_hi * 32; r0 += kKcThreads) {
+            const uint64_t i = r0 + uint64_t(t);
+            double v = 0.0;
+            if (i < b_hi * 32 && i < n) {
+                v = kc_row<MSR, VEC4>(a, i, c, first, round);
+                if (weighted) v = v * a.w[i];
+            }
+            sval[t] = v;
+            __syncthreads();
+            if (t < kKcThreads / 32) {
+                const uint64_t b = r0 / 32 + uint64_t(t);
+                if (b < b_hi) blk[b] = kc_block32(sval + 32 * t);
+            }
+            __syncthreads();
+        }
+        if (round + 1 == a.k) break;
+        kc_sync();
+        // ---- CTA 0: the draw of the next round ----
+        if (rank == 0) {
+            for (uint64_t e = t; e < G * 256; e += kKcThreads) {
+                const uint64_t g = e >> 8, l = e & 255, b = g * 256 + l;
+                H[g * 512 + 256 + l] = b < nblk ? __ldcg(blk + b) : 0.0;
+            }
+            __syncthreads();
+            for (uint64_t lv = 128; lv >= 1; lv >>= 1) {
+                for (uint64_t e = t; e < G * lv; e += kKcThreads) {
+                    const uint64_t g = e / lv, j = lv + e % lv;
+                    H[g * 512 + j] = H[g * 512 + 2 * j] + H[g * 512 + 2 * j + 1];
+                }
+                __syncthreads();
+            }
+            for (uint64_t g = t; g < P; g += kKcThreads) T[P + g] = g < G ? H[g * 512 + 1] : 0.0;
+            __syncthreads();
+            for (uint64_t lv = P >> 1; lv >= 1; lv >>= 1) {
+                for (uint64_t j = lv + t; j < 2 * lv; j += kKcThreads) T[j] = T[2 * j] + T[2 * j + 1];
+                __syncthreads();
+            }
+            if (t == 0) {
+                const double S = T[1];
+                sm_pos = S > 0.0;
+                if (S > 0.0) {
+                    double r = u[round + 1] * S;
+                    const uint64_t g = det_heap_descend(T, P, r);
+                    const uint64_t b = det_heap_descend(H + g * 512, 256, r);
+                    sm_g = g;
+                    sm_b = b;
+                    sm_r = r;
+                }
+            }
+            __syncthreads();
+            if (!sm_pos) {
+                // total not positive: the first maximum of the distances (k_det_draw's fallback)
+                if (t == 0) {
+                    uint64_t am = 0;
+                    double best = __ldcg(a.dist);
+                    for (uint64_t i = 1; i < n; ++i) {
+                        const double v = __ldcg(a.dist + i);
+                        if (v > best) {
+                            best = v;
+                            am = i;
+                        }
+                    }
+                    *a.newc = am;
+                }
+            } else if (t < 32) {
+                const uint64_t base = sm_g * kDetChunk + sm_b * 32, i = base + uint64_t(t);
+                double v = 0.0;
+                if (i < n) {
+                    v = __ldcg(a.dist + i);
+                    if (weighted) v = v * a.w[i];
+                }
+                E[32 + t] = v;
+                __syncwarp();
+                for (int lv = 16; lv >= 1; lv >>= 1) {
+                    if (t < lv) E[lv + t] = E[2 * (lv + t)] + E[2 * (lv + t) + 1];
+                    __syncwarp();
+                }
+                if (t == 0) {
+                    double r = sm_r;
+                    uint64_t res = base + det_heap_descend(E, 32, r);
+                    if (res >= n) res = 0;
+                    *a.newc = res;
+                }
+            }
+        }
+        kc_sync();
+    }
+}
+
+// cluster size for this device (16 where a 16-CTA cluster of this kernel fits one GPC, else
+// 8), 0 when none can be launched
+static int kmpp_cluster_size(const void *kern, size_t smem) {
+    static std::mutex mu;
+    static std::unordered_map<const void *, int> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    const void *key = reinterpret_cast<const char *>(kern) + dev;
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int best = 0;
+    for (int cs : {16, 8}) {
+        if (cs > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(unsigned(cs));
+        cfg.blockDim = dim3(kKcThreads);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = unsigned(cs);
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, kern, &cfg) == cudaSuccess && nc >= 1) {
+            best = cs;
+            break;
+        }
+        cudaGetLastError();
+    }
+    cache[key] = best;
+    return best;
+}
+
+template <int MSR, bool VEC4>
+static int kmpp_cluster_t(const KmppArgs &a, const double *u_dev, double *blk, cudaStream_t st) {
+    auto kern = k_kmpp_cluster<MSR, VEC4>;
+    const size_t smem = size_t(det_chunks(a.n)) * 512 * sizeof(double);
+    MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int cs = kmpp_cluster_size(reinterpret_cast<const void *>(kern), smem);
+    if (cs == 0) return fail(MC_ECUDA, "k-means++: no thread-block cluster fits this device");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(cs));
+    cfg.blockDim = dim3(kKcThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = unsigned(cs);
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    MC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, a, u_dev, blk));
+    note_launch();
+    return MC_OK;
+}
+
+template <int MSR>
+static int kmpp_cluster_m(const KmppArgs &a, const double *u_dev, double *blk, cudaStream_t st) {
+    const bool vec4 = a.d % 4 == 0 && (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
+    return vec4 ? kmpp_cluster_t<MSR, true>(a, u_dev, blk, st) : kmpp_cluster_t<MSR, false>(a, u_dev, blk, st);
+}
+
+static int run_kmeanspp_cluster(const KmppArgs &a, const double *u_dev, cudaStream_t st) {
+    DBuf<double> blk;
+    MC_TRY(blk.alloc((a.n + 31) / 32, st));
+    MC_CUDA_TRY(cudaMemsetAsync(a.asn, 0, a.n * sizeof(uint32_t), st));
+    switch (a.msr) {
+        case SQRL2: MC_TRY(kmpp_cluster_m<SQRL2>(a, u_dev, blk.p, st)); break;
+        case L1: MC_TRY(kmpp_cluster_m<L1>(a, u_dev, blk.p, st)); break;
+        case HELLINGER: MC_TRY(kmpp_cluster_m<HELLINGER>(a, u_dev, blk.p, st)); break;
+        case MKL: MC_TRY(kmpp_cluster_m<MKL>(a, u_dev, blk.p, st)); break;
+        case JSD: MC_TRY(kmpp_cluster_m<JSD>(a, u_dev, blk.p, st)); break;
+        default: return fail(MC_EUNSUPPORTED, "measure not supported");
+    }
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
+static int run_kmeanspp_launches(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms,
+                                 cudaStream_t st, bool prune_ok);
+
 int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st) {
+    // dense rows up to 32 chunks and 2^23 values (a cluster of 8-16 SMs reads them in well
+    // under the four to five launches of a round): the persistent cluster or a launch
+    // sequence per round, whichever the autotuner measured faster for this shape (identical
+    // results)
+    if (!a0.csr && a0.n <= kKcMaxRows && a0.n * a0.d <= (uint64_t(1) << 23) && a0.k > 1) {
+        const std::string key = "kmpp_run|msr" + std::to_string(a0.msr) + "|w" + std::to_string(a0.w ? 1 : 0) +
+                                "|d" + tune_bucket(a0.d) + "|n" + tune_bucket(a0.n) + "|k" + tune_bucket(a0.k);
+        return tune_launch(key, 2, 0, st, true, [&](int v) -> int {
+            return v == 1 ? run_kmeanspp_cluster(a0, u_dev, st)
+                          : run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, false);
+        });
+    }
+    // dense SQRL2 over a large matrix: with or without the triangle-inequality pruning below
+    // (it skips rows only where the result is provably unchanged, but costs dependent loads
+    // before each row's distance: on the 2M x 64 Gaussian mixture it measured 19.2 ms per
+    // 100-center run against 14.4 ms without), whichever the autotuner measures faster
+    if (!a0.csr && a0.msr == SQRL2 && a0.k > 1 && a0.n * a0.d >= (uint64_t(1) << 20)) {
+        const std::string key = "kmpp_prune|d" + tune_bucket(a0.d) + "|n" + tune_bucket(a0.n) + "|k" +
+                                tune_bucket(a0.k);
+        return tune_launch(key, 2, 0, st, true, [&](int v) -> int {
+            return run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, v == 1);
+        });
+    }
+    return run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, false);
+}
+
+static int run_kmeanspp_launches(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms,
+                                 cudaStream_t st, bool prune_ok) {
     KmppArgs a = a0;
     a.cgap = nullptr;
     const unsigned tb = 256, tg = unsigned(umin64((a.d + tb - 1) / tb, 1024));
@@ -644,9 +977,9 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
         k_kmpp_scatter<<<64, 256, 0, st>>>(a), note_launch();
     }
     MC_TRY(update(a, 1, 0, sms, st));
-    // dense SQRL2 over a large matrix: rounds after the first prune by the triangle
-    // inequality (one more small launch per round; the results are unchanged)
-    const bool prune = !a.csr && a.msr == SQRL2 && a.k > 1 && a.n * a.d >= (uint64_t(1) << 20);
+    // rounds after the first may prune by the triangle inequality (one more small launch per
+    // round; the results are unchanged)
+    const bool prune = prune_ok && !a.csr && a.msr == SQRL2 && a.k > 1;
     DBuf<double> gap;
     if (prune) {
         MC_TRY(gap.alloc(a.k, st));

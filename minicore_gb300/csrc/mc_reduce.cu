@@ -69,21 +69,6 @@ __device__ void det_heap_build(double *T, uint64_t P, uint64_t G) {
     }
 }
 
-// from the root of a heap with P leaves: left when r < L or R is not positive, else r -= L
-__device__ inline uint64_t det_heap_descend(const double *T, uint64_t P, double &r) {
-    uint64_t j = 1;
-    while (j < P) {
-        const double L = T[2 * j], R = T[2 * j + 1];
-        if (r < L || !(R > 0.0)) {
-            j = 2 * j;
-        } else {
-            r = r - L;
-            j = 2 * j + 1;
-        }
-    }
-    return j - P;
-}
-
 constexpr uint64_t kDetSmemLeaves = 2048;  // tree in shared memory up to this many leaves
 
 __global__ void __launch_bounds__(kDetThreads) k_det_final(double *tree, uint64_t P, uint64_t G, double *out) {

@@ -210,6 +210,19 @@ __device__ inline void tmem_ld32(uint32_t taddr, float *v) {
 __device__ inline void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ inline void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+// UMMA shared-memory descriptor for the 32-byte-swizzled K = 16 (BF16) / 8 (TF32) operand
+// tiles (one 32-byte row per M/N row, 8-row atoms 256 B apart)
+__device__ inline uint64_t sdesc32(const void *p) {
+    const uint64_t addr = smem_u32(p);
+    uint64_t d = 0;
+    d |= (addr >> 4) & 0x3FFFull;          // start address
+    d |= uint64_t(1) << 16;                // leading byte offset (unused for K-major swizzle)
+    d |= uint64_t(256 >> 4) << 32;         // stride byte offset: 8 rows x 32 B
+    d |= uint64_t(1) << 46;                // descriptor version
+    d |= uint64_t(6) << 61;                // 32-byte swizzle
+    return d;
+}
+
 __device__ __forceinline__ unsigned long long pk2(float lo, float hi) {
     unsigned long long r;
     asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
@@ -223,6 +236,36 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
     float r;
     asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
+}
+
+// three-input maximum (sm_100 family)
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// The same over accumulators that already hold D_j = x.c_j - ||c_j||^2 / 2 (the norm enters
+// the accumulator through one more MMA, k_tc_top2_res): v_j = -2 D_j exactly, so the smallest
+// v are the largest D.  Keeps the two largest subgroup maxima (M1 >= M2) and the first
+// subgroup holding M1; padding centers (j >= k) at -inf.
+__device__ __forceinline__ void top2max_group32(float (&v)[32], uint32_t j0, uint32_t k, float &M1, float &M2,
+                                                uint32_t &sg1) {
+    const float NINF = __int_as_float(0xff800000);
+    if (j0 + 32 > k) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (j0 + uint32_t(i) >= k) v[i] = NINF;
+    }
+#pragma unroll
+    for (int sg = 0; sg < 4; ++sg) {
+        const float *w = v + 8 * sg;
+        const float sv = fmax3(fmax3(w[0], w[1], w[2]), fmax3(w[3], w[4], w[5]), fmaxf(w[6], w[7]));
+        const bool higher = sv > M1;
+        M2 = fmaxf(M2, fminf(M1, sv));
+        sg1 = higher ? (j0 >> 3) + uint32_t(sg) : sg1;
+        M1 = fmaxf(M1, sv);
+    }
 }
 
 // Pass 1 epilogue over 32 accumulator columns (centers j0 .. j0 + 31, norms cn32[0 .. 31]):
@@ -260,6 +303,45 @@ __device__ __forceinline__ void top2_group32(float (&v)[32], const float *cn32, 
     }
 }
 
+// Column-part exchange of a row tile: each epilogue warp leaves its rows' (m1, m2, subgroup)
+// for its column part; the part-0 warp of each lane quarter merges the four parts in part order
+// (the first part holding the minimum gives the subgroup) after a named barrier of the quarter's
+// four warps (ids 1-4).  Two tile slots alternate, so one barrier per tile suffices: a warp
+// rewrites a slot only after the next tile's barrier, which the merging warp reaches after its
+// reads.
+struct PartX {
+    float m1[2][PARTS][BM], m2[2][PARTS][BM];
+    uint32_t sg[2][PARTS][BM];
+};
+
+__device__ __forceinline__ void quarter_sync(int quarter) {
+    asm volatile("bar.sync %0, 128;" ::"r"(1 + quarter) : "memory");
+}
+
+// leaves this part's entry, merges on the part-0 warp; returns true there (m1, m2, sg1 merged)
+__device__ __forceinline__ bool part_merge(PartX *px, uint32_t tile, int quarter, int part, int rloc, float &m1,
+                                           float &m2, uint32_t &sg1) {
+    const int sl = int(tile & 1u);
+    px->m1[sl][part][rloc] = m1;
+    px->m2[sl][part][rloc] = m2;
+    px->sg[sl][part][rloc] = m1 < __int_as_float(0x7f800000) ? sg1 : 0xffffffffu;
+    quarter_sync(quarter);
+    if (part != 0) return false;
+    float a1 = __int_as_float(0x7f800000), a2 = a1;
+    uint32_t gr = 0xffffffffu;
+#pragma unroll
+    for (int p = 0; p < PARTS; ++p) {
+        const float c1 = px->m1[sl][p][rloc], c2 = px->m2[sl][p][rloc];
+        if (c1 < a1) gr = px->sg[sl][p][rloc];
+        a2 = fminf(fminf(a2, c2), fmaxf(a1, c1));
+        a1 = fminf(a1, c1);
+    }
+    m1 = a1;
+    m2 = a2;
+    sg1 = gr;
+    return true;
+}
+
 }  // namespace tc
 
 struct TcArgs {
@@ -269,9 +351,9 @@ struct TcArgs {
     float eta, gamma;
     const float *cnp;      // [kp] center norms, +inf past k; [kp] holds Cmax
     uint32_t kp;
-    float *b1;             // [n][PARTS] pass 1: smallest subgroup minimum per row and column part
-    float *b2;             // [n][PARTS] pass 1: second smallest subgroup minimum
-    uint32_t *j1;          // [n][PARTS] pass 1: subgroup (8 centers) of b1 (0xffffffff: none)
+    float *b1;             // [n][entries] pass 1: smallest subgroup minimum per row (per group and part)
+    float *b2;             // [n][entries] pass 1: second smallest subgroup minimum
+    uint32_t *j1;          // [n][entries] pass 1: first subgroup (8 centers) holding b1 (0xffffffff: none)
     const unsigned *count; // pass 2: device count of compact rows (rows = min(*count, n))
     const float *thrc;     // [rows] pass 2: candidate threshold per compact row
     uint8_t *cnt;          // [rows][PARTS] pass 2: candidates per column part (255: too many)
@@ -299,7 +381,8 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     unsigned char *base = reinterpret_cast<unsigned char *>((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
     unsigned char *stages = base;
     float *cn_s = reinterpret_cast<float *>(base + STAGES * STAGE_BYTES);
-    Smem *sm = reinterpret_cast<Smem *>(base + STAGES * STAGE_BYTES + CN_SMEM * sizeof(float));
+    PartX *px = reinterpret_cast<PartX *>(base + STAGES * STAGE_BYTES + CN_SMEM * sizeof(float));
+    Smem *sm = reinterpret_cast<Smem *>(reinterpret_cast<unsigned char *>(px) + (MODE == TC_TOP2 ? sizeof(PartX) : 0));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool cn_in_smem = a.kp <= CN_SMEM;
     if (cn_in_smem)
@@ -406,7 +489,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         const uint32_t lane_base = uint32_t(quarter * 32) << 16;
         const int rloc = quarter * 32 + lane;
         const float INF = __int_as_float(0x7f800000);
-        uint32_t acc_it = 0;
+        uint32_t acc_it = 0, tcount = 0;
         bool ok = true;
         for (uint32_t m = blockIdx.x; m < ntiles && ok; m += gridDim.x) {
             const uint64_t row = uint64_t(m) * BM + rloc;  // pass 2: compact row
@@ -472,15 +555,15 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
                 mbar_arrive(&sm->acc_empty[buf]);
             }
             if (!ok) break;
-            if (valid) {
-                const uint64_t o = row * PARTS + part;
-                if (MODE == TC_TOP2) {
-                    a.b1[o] = m1;
-                    a.b2[o] = m2;
-                    a.j1[o] = m1 < INF ? sg1 : 0xffffffffu;
-                } else {
-                    a.cnt[o] = ncand > NCAND ? uint8_t(255) : uint8_t(ncand);
+            if (MODE == TC_TOP2) {
+                // one merged entry per row (all four part warps of the quarter take part)
+                if (part_merge(px, tcount++, quarter, part, rloc, m1, m2, sg1) && valid) {
+                    a.b1[row] = m1;
+                    a.b2[row] = m2;
+                    a.j1[row] = sg1;
                 }
+            } else if (valid) {
+                a.cnt[row * PARTS + part] = ncand > NCAND ? uint8_t(255) : uint8_t(ncand);
             }
         }
     }
@@ -504,16 +587,28 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
 // `gch` 256-center chunks that fit shared memory next to two row-tile stages, each CTA loads
 // its group's centers once and then streams row tiles only, and the rows' tiles are read once
 // per group.  CTA b serves group b % G and row tiles b / G, b / G + T, ... (T = grid / G).
-// The epilogue is the TC_TOP2 one; each group writes its own column parts, so a row has
-// G x PARTS (m1, m2, subgroup) entries at [row][g][part] for k_tc_select to merge.
+// The norms enter the accumulators instead of the epilogue: every chunk starts with one more
+// MMA (K = 16 BF16 / 8 TF32, 32-byte swizzled operands) of A = (1, 1, 1, 0, ...) against
+// B_j = -||c_j||^2 / 2 split into three parts, so D_j = x.c_j - ||c_j||^2 / 2 and
+// v_j = -2 D_j exactly.  Adding the norm in the epilogue took one 4-byte broadcast per
+// (warp, center) from shared memory, which kept the load/store pipe about 80 % busy.  The
+// norm now shares the accumulator's FP32 rounding: with T = d / 16 + 1 accumulation steps of
+// relative error <= 2^-22 each over partial sums of magnitude <= ||x|| ||c|| + Cmax^2 / 2, and
+// the three-part split exact to 2^-24, v_j moves by at most (d + 1) 2^-22 Cmax^2 beyond the
+// dot-product bound, which k_tc_select adds twice to Delta.  The epilogue keeps the two
+// largest subgroup maxima of D.  Each group writes its own column parts unmerged (a merge
+// across the part warps, as k_tc_assign does, measured slower here), so a row has G x PARTS
+// (m1, m2, subgroup) entries at [row][g][part] for k_tc_select to merge in that order.
 namespace tc {
 template <int KB>
 struct ResShape {
     static constexpr int A_TILE = KB * A_STAGE;                  // a row tile's k-blocks
-    static constexpr int ASTAGES = KB == 1 ? 4 : 2;
+    static constexpr int ASTAGES = KB == 1 ? 3 : 2;
     static constexpr int GCH = KB == 1 ? 4 : 2;                  // 256-center chunks per group
     static constexpr int B_CHUNK = KB * 256 * KBYTES;            // 32 KB per k-block
-    static constexpr int SMEM = ASTAGES * A_TILE + GCH * B_CHUNK + GCH * 256 * 4;
+    static constexpr int AUXA = BM * 32;                         // norm MMA: ones, 32 B per row
+    static constexpr int AUXB = 256 * 32;                        // norm MMA: -||c||^2 / 2 split, per chunk
+    static constexpr int SMEM = ASTAGES * A_TILE + GCH * B_CHUNK + AUXA + GCH * AUXB;
 };
 struct ResSmem {
     uint64_t afull[4], aempty[4], bfull, acc_full[2], acc_empty[2], drain;
@@ -526,7 +621,8 @@ struct ResSmem {
 
 template <bool TF32, int KB>
 __global__ void __launch_bounds__(tc::THREADS, 1)
-    k_tc_top2_res(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs a,
+    k_tc_top2_res(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  const __grid_constant__ CUtensorMap tmAuxA, const __grid_constant__ CUtensorMap tmAuxB, TcArgs a,
                   uint32_t G, uint32_t nchunks) {
     using namespace tc;
     using RS = ResShape<KB>;
@@ -535,14 +631,14 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     unsigned char *base = reinterpret_cast<unsigned char *>((uintptr_t(smraw) + 1023) & ~uintptr_t(1023));
     unsigned char *astages = base;
     unsigned char *bres = base + ASTAGES * RS::A_TILE;
-    float *cn_s = reinterpret_cast<float *>(bres + RS::GCH * RS::B_CHUNK);
-    ResSmem *sm = reinterpret_cast<ResSmem *>(reinterpret_cast<unsigned char *>(cn_s) + RS::GCH * 256 * 4);
+    unsigned char *auxa = bres + RS::GCH * RS::B_CHUNK;
+    unsigned char *auxb = auxa + RS::AUXA;
+    ResSmem *sm = reinterpret_cast<ResSmem *>(auxb + RS::GCH * RS::AUXB);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t g = blockIdx.x % G, T = gridDim.x / G, t0 = blockIdx.x / G;
     const uint32_t c0 = g * RS::GCH;                                   // first chunk of the group
     const uint32_t gch = umin64(RS::GCH, nchunks - c0);                // chunks of this group
     const uint32_t ntiles = a.ntiles;
-    for (uint32_t j = threadIdx.x; j < gch * 256; j += THREADS) cn_s[j] = a.cnp[c0 * 256 + j];
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < ASTAGES; ++s) {
@@ -575,12 +671,15 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
     if (warp == 0) {
         // ---------------- TMA producer: the group's centers once, then row tiles ----------------
         if (lane == 0 && t0 < ntiles) {
-            mbar_expect_tx(&sm->bfull, gch * RS::B_CHUNK);
+            mbar_expect_tx(&sm->bfull, gch * RS::B_CHUNK + RS::AUXA + gch * RS::AUXB);
             sm->b_out = 1;
             for (uint32_t nc = 0; nc < gch; ++nc)
                 for (int kb = 0; kb < KB; ++kb)
                     tma_load_2d(bres + (nc * KB + kb) * (256 * KBYTES), &tmB, &sm->bfull, kb * (TF32 ? 32 : 64),
                                 int((c0 + nc) * BN));
+            tma_load_2d(auxa, &tmAuxA, &sm->bfull, 0, 0);
+            for (uint32_t nc = 0; nc < gch; ++nc)
+                tma_load_2d(auxb + nc * RS::AUXB, &tmAuxB, &sm->bfull, 0, int((c0 + nc) * BN));
             uint32_t s = 0, ph = 0;
             for (uint32_t m = t0; m < ntiles; m += T) {
                 if (!mbar_wait(&sm->aempty[s], ph ^ 1, sm, a.err, 1)) break;
@@ -611,13 +710,15 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
                     if (!mbar_wait(&sm->acc_empty[buf], (use & 1) ^ 1, sm, a.err, 2)) { ok = false; break; }
                     fence_after();
                     const uint32_t d_tmem = tmem + buf * BN;
+                    // D = 1 . (-||c||^2 / 2, split in three) ... then += x . c
+                    mma<TF32, BN>(d_tmem, sdesc32(auxa), sdesc32(auxb + nc * RS::AUXB), 0u);
 #pragma unroll
                     for (int kb = 0; kb < KB; ++kb) {
                         const uint64_t ad = ad0 + uint64_t((kb * A_STAGE) >> 4);
                         const uint64_t bd = sdesc(bres + (nc * KB + kb) * (256 * KBYTES));
 #pragma unroll
                         for (int ks = 0; ks < 4; ++ks)
-                            mma<TF32, BN>(d_tmem, ad + uint64_t(ks * 2), bd + uint64_t(ks * 2), (kb | ks) ? 1u : 0u);
+                            mma<TF32, BN>(d_tmem, ad + uint64_t(ks * 2), bd + uint64_t(ks * 2), 1u);
                     }
                     mma_commit(&sm->acc_full[buf]);
                 }
@@ -639,7 +740,7 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
         bool ok = true;
         for (uint32_t m = t0; m < ntiles && ok; m += T) {
             const uint64_t row = uint64_t(m) * BM + rloc;
-            float m1 = INF, m2 = INF;
+            float M1 = -INF, M2 = -INF;  // the two largest subgroup maxima of D
             uint32_t sg1 = 0xffffffffu;
             for (uint32_t nc = 0; nc < gch; ++nc, ++acc_it) {
                 const uint32_t buf = acc_it & 1, use = acc_it >> 1;
@@ -655,16 +756,17 @@ __global__ void __launch_bounds__(tc::THREADS, 1)
                 tmem_ld32(taddr + 32, v1);
                 fence_before();
                 mbar_arrive(&sm->acc_empty[buf]);  // both column groups are in registers
-                const uint32_t jl = nc * BN + part * PCOLS, j0 = c0 * 256 + jl;
-                top2_group32(v0, cn_s + jl, j0, a.k, m1, m2, sg1);
-                top2_group32(v1, cn_s + jl + 32, j0 + 32, a.k, m1, m2, sg1);
+                const uint32_t j0 = (c0 + nc) * BN + part * PCOLS;
+                top2max_group32(v0, j0, a.k, M1, M2, sg1);
+                top2max_group32(v1, j0 + 32, a.k, M1, M2, sg1);
             }
             if (!ok) break;
             if (row < a.n) {
+                // v = -2 D exactly: the smallest and second smallest subgroup minima of v
                 const uint64_t o = (row * G + g) * PARTS + part;
-                a.b1[o] = m1;
-                a.b2[o] = m2;
-                a.j1[o] = m1 < INF ? sg1 : 0xffffffffu;
+                a.b1[o] = -2.f * M1;
+                a.b2[o] = -2.f * M2;
+                a.j1[o] = M1 > -INF ? sg1 : 0xffffffffu;
             }
         }
     }
@@ -736,8 +838,7 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
                                                     uint32_t *key, uint32_t *crow, float *thrc, unsigned *count,
                                                     uint32_t cap, const uint4 *__restrict__ A, uint64_t row_u4,
                                                     uint4 *Xc, uint32_t *over_rows, unsigned long long *nover,
-                                                    unsigned long long *nmulti, uint32_t ngroups) {
-    static_assert(tc::PARTS == 4, "one 16-byte load per row, group and array");
+                                                    unsigned long long *nmulti, uint32_t ngroups, float nerr) {
     __shared__ uint32_t mrow[8][32], mslot[8][32];  // the warp's multi rows and their slots
     const uint64_t row = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -747,22 +848,17 @@ __global__ void __launch_bounds__(256) k_tc_select(uint64_t n, const float *__re
     if (row < n) {
         float m1 = INF, m2 = INF;
         uint32_t gr = ST_OVER;
-        // the column parts of every center group
+        // the row's pass 1 entries (one, or one per center group and column part), in order
         for (uint32_t g = 0; g < ngroups; ++g) {
             const uint64_t o = row * ngroups + g;
-            const float4 v1 = reinterpret_cast<const float4 *>(b1)[o], v2 = reinterpret_cast<const float4 *>(b2)[o];
-            const uint4 vj = reinterpret_cast<const uint4 *>(j1)[o];
-            const float c1s[4] = {v1.x, v1.y, v1.z, v1.w}, c2s[4] = {v2.x, v2.y, v2.z, v2.w};
-            const uint32_t js[4] = {vj.x, vj.y, vj.z, vj.w};
-#pragma unroll
-            for (int p = 0; p < tc::PARTS; ++p) {
-                if (c1s[p] < m1) gr = js[p];
-                top2_merge(m1, m2, c1s[p], c2s[p]);
-            }
+            const float c1 = b1[o], c2 = b2[o];
+            if (c1 < m1) gr = j1[o];
+            top2_merge(m1, m2, c1, c2);
         }
         const float cmax = *cmaxp;
         const float xn = sqrtf(rownorm[row]);
-        const float delta = 4.f * eta * xn * cmax * 1.0001f + 4.f * gamma * (xn + cmax) * (xn + cmax);
+        const float delta =
+            4.f * eta * xn * cmax * 1.0001f + 4.f * gamma * (xn + cmax) * (xn + cmax) + nerr * cmax * cmax;
         // no finite minimum or a non-finite bound proves nothing: exact rescan
         if (!(m1 < INF) || !(delta <= 3.402823466e+38f) || gr >= nsg) {
             over = true;
@@ -1168,6 +1264,63 @@ static int make_map(CUtensorMap *map, const void *ptr, bool tf32, uint64_t rows,
     return MC_OK;
 }
 
+// Operands of the norm MMA of k_tc_top2_res, 32 bytes per row: A = (1, 1, 1, 0, ...) for every
+// row; B row j = (h, m, l, 0, ...) with h + m + l = -||c_j||^2 / 2 in three BF16 (round to
+// nearest) or TF32 (truncated) parts, each the remainder of the one before (exact in FP32);
+// padding centers (j >= k) are zero rows (the epilogue sets their values to -inf).
+__device__ inline float tf32_trunc(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+__global__ void k_tc_aux_prep(const float *__restrict__ cnorm, uint32_t k, uint32_t kp, int tf32, uint32_t *auxa,
+                              uint32_t *auxb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < tc::BM) {
+        uint32_t *r = auxa + i * 8;
+        for (int q = 0; q < 8; ++q) r[q] = 0u;
+        if (tf32) {
+            r[0] = r[1] = r[2] = __float_as_uint(1.f);
+        } else {
+            r[0] = 0x3F803F80u;  // bf16 1.0, 1.0
+            r[1] = 0x00003F80u;  // bf16 1.0, 0
+        }
+    }
+    if (i < kp) {
+        uint32_t *r = auxb + uint64_t(i) * 8;
+        for (int q = 0; q < 8; ++q) r[q] = 0u;
+        if (i < k) {
+            const float t = -0.5f * cnorm[i];
+            if (tf32) {
+                const float h = tf32_trunc(t), r1 = t - h, m = tf32_trunc(r1), l = tf32_trunc(r1 - m);
+                r[0] = __float_as_uint(h);
+                r[1] = __float_as_uint(m);
+                r[2] = __float_as_uint(l);
+            } else {
+                const __nv_bfloat16 h = __float2bfloat16_rn(t);
+                const float r1 = t - __bfloat162float(h);
+                const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+                const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+                r[0] = uint32_t(__bfloat16_as_ushort(h)) | (uint32_t(__bfloat16_as_ushort(m)) << 16);
+                r[1] = uint32_t(__bfloat16_as_ushort(l));
+            }
+        }
+    }
+}
+
+// tensor map of a [rows][32 bytes] operand tile with the 32-byte swizzle (box: 32 bytes x box_rows)
+static int make_map_aux(CUtensorMap *map, const void *ptr, bool tf32, uint64_t rows, uint32_t box_rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return fail(MC_ECUDA, "cuTensorMapEncodeTiled unavailable");
+    const uint64_t esz = tf32 ? 4 : 2;
+    cuuint64_t dims[2] = {cuuint64_t(32 / esz), cuuint64_t(rows)};
+    cuuint64_t strides[1] = {32};
+    cuuint32_t box[2] = {cuuint32_t(32 / esz), box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                    const_cast<void *>(ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(MC_ECUDA, "cuTensorMapEncodeTiled (norm operands) failed: " + std::to_string(int(r)));
+    return MC_OK;
+}
+
 // test hook: the next tensor-core pass 1 launched by this process stalls on purpose (one shot)
 static std::atomic<int> g_tc_stall_next{0};
 void tc_stall_next() { g_tc_stall_next.store(1); }
@@ -1182,7 +1335,7 @@ template <bool TF32, int MODE, int BN, int STAGES>
 static int tc_launch_t(unsigned grid, const CUtensorMap &mA, const CUtensorMap &mB, TcArgs a, cudaStream_t st) {
     a.nchunks = a.kp / BN;
     const size_t smem = size_t(STAGES) * tc::Shape<BN, STAGES>::STAGE_BYTES + tc::CN_SMEM * sizeof(float) +
-                        sizeof(tc::Smem<STAGES>) + 1024;
+                        (MODE == TC_TOP2 ? sizeof(tc::PartX) : 0) + sizeof(tc::Smem<STAGES>) + 1024;
     auto kern = k_tc_assign<TF32, MODE, BN, STAGES>;
     MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     kern<<<grid, tc::THREADS, smem, st>>>(mA, mB, a), note_launch();
@@ -1224,12 +1377,12 @@ static ResPlan res_plan(uint32_t kb, uint32_t kp, int sms) {
 }
 
 template <bool TF32>
-static int tc_res_launch(const ResPlan &p, uint32_t kb, const CUtensorMap &mA, const CUtensorMap &mB256, TcArgs a,
-                         cudaStream_t st) {
+static int tc_res_launch(const ResPlan &p, uint32_t kb, const CUtensorMap &mA, const CUtensorMap &mB256,
+                         const CUtensorMap &mAuxA, const CUtensorMap &mAuxB, TcArgs a, cudaStream_t st) {
     a.nchunks = p.nchunks;
     auto kern = kb == 1 ? k_tc_top2_res<TF32, 1> : k_tc_top2_res<TF32, 2>;
     MC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(p.smem)));
-    kern<<<p.grid, tc::THREADS, p.smem, st>>>(mA, mB256, a, p.G, p.nchunks), note_launch();
+    kern<<<p.grid, tc::THREADS, p.smem, st>>>(mA, mB256, mAuxA, mAuxB, a, p.G, p.nchunks), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;
 }
@@ -1282,10 +1435,22 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     if (wide) MC_TRY(make_map(&mB256, Bptr, tf32, kp, d, dp, 256));
     using tc::PARTS;
     const ResPlan rp = res_plan(kb, kp, sms);
-    const uint64_t ngmax = rp.ok ? rp.G : 1;  // pass 1 writes PARTS entries per row and center group
-    MC_TRY(s.b1.alloc(PARTS * n * ngmax, st));
-    MC_TRY(s.b2.alloc(PARTS * n * ngmax, st));
-    MC_TRY(s.j1.alloc(PARTS * n * ngmax, st));
+    // pass 1 writes one merged entry per row (k_tc_assign) or one per center group and column
+    // part (k_tc_top2_res)
+    const uint64_t ngmax = rp.ok ? uint64_t(rp.G) * PARTS : 1;
+    MC_TRY(s.b1.alloc(n * ngmax, st));
+    MC_TRY(s.b2.alloc(n * ngmax, st));
+    MC_TRY(s.j1.alloc(n * ngmax, st));
+    CUtensorMap mAuxA, mAuxB;
+    if (rp.ok) {
+        MC_TRY(s.auxa.alloc(uint64_t(tc::BM) * 8, st));
+        MC_TRY(s.auxb.alloc(uint64_t(kp) * 8, st));
+        k_tc_aux_prep<<<(kp > tc::BM ? kp : tc::BM) / 128 + 1, 128, 0, st>>>(cnorm, k, kp, tf32 ? 1 : 0, s.auxa.p,
+                                                                          s.auxb.p), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        MC_TRY(make_map_aux(&mAuxA, s.auxa.p, tf32, tc::BM, tc::BM));
+        MC_TRY(make_map_aux(&mAuxB, s.auxb.p, tf32, kp, 256));
+    }
     MC_TRY(s.status.alloc(n, st));
     MC_TRY(s.key.alloc(n, st));
     const uint32_t nsg = kp / 8;  // subgroups of 8 centers
@@ -1349,15 +1514,19 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     // pass 1 variants: the tile shapes, then (where it fits) the resident-centers kernel; the
     // output layout is that of the variant launched last
     uint32_t ngroups = 1;
+    float nerr = 0.f;  // extra bound term (times Cmax^2) of pass 1 values that carry the norms
     {
         Phase ph("tc_pass1_top2", st);
         const int nvar1 = nvar + (rp.ok ? 1 : 0);
         MC_TRY(tune_launch("tc1" + bucket, nvar1, 0, st, allow, [&](int v) -> int {
             if (v == nvar) {
-                ngroups = rp.G;
-                return tf32 ? tc_res_launch<true>(rp, kb, mA, mB256, a, st) : tc_res_launch<false>(rp, kb, mA, mB256, a, st);
+                ngroups = rp.G * PARTS;
+                nerr = float(double(d + 1) * std::ldexp(1.0, -21) * 1.0001);
+                return tf32 ? tc_res_launch<true>(rp, kb, mA, mB256, mAuxA, mAuxB, a, st)
+                            : tc_res_launch<false>(rp, kb, mA, mB256, mAuxA, mAuxB, a, st);
             }
             ngroups = 1;
+            nerr = 0.f;
             return tf32 ? tc_shape_launch<true, TC_TOP2>(shape_of(v), grid, mA, mB128, mB256, a, st)
                         : tc_shape_launch<false, TC_TOP2>(shape_of(v), grid, mA, mB128, mB256, a, st);
         }));
@@ -1368,7 +1537,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
         k_tc_select<<<unsigned((n + 255) / 256), 256, 0, st>>>(
             n, s.b1.p, s.b2.p, s.j1.p, rownorm, s.cnorm_p.p + kp, a.eta, a.gamma, nsg, s.status.p, s.key.p,
             s.crow.p, s.thrc.p, s.count.p, uint32_t(cap), static_cast<const uint4 *>(Aptr), row_u4, s.Xc.p,
-            s.over_rows.p, s.nrecheck.p + 1, s.nrecheck.p, ngroups), note_launch();
+            s.over_rows.p, s.nrecheck.p + 1, s.nrecheck.p, ngroups, nerr), note_launch();
         MC_CUDA_TRY(cudaGetLastError());
         // finalize order: rows grouped by subgroup, then multi rows, then OVER rows
         MC_TRY(launch_sort_by_key(s.key.p, nullptr, n, nsg + 2, s.sort, st));

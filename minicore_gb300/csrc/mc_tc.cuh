@@ -13,8 +13,8 @@ struct TcState {
     DBuf<__nv_bfloat16> Cb;      // [kp][dp]
     DBuf<float> Ct;              // [kp][dp]
     DBuf<float> cnorm_p;         // device scalar: max center norm
-    DBuf<float> b1, b2;          // [n][4] pass 1 top-2 subgroup minima per row and column part
-    DBuf<uint32_t> j1;           // [n][4] subgroup of b1
+    DBuf<float> b1, b2;          // [n][entries] pass 1 top-2 subgroup minima per row (per group and part)
+    DBuf<uint32_t> j1;           // [n][entries] subgroup of b1
     DBuf<uint32_t> status;       // [n] candidate subgroup / multi slot / rescan
     DBuf<uint32_t> key;          // [n] finalize order key (subgroup, multi, rescan)
     SortWork sort;               // rows sorted by key
@@ -28,6 +28,7 @@ struct TcState {
     DBuf<unsigned long long> nrecheck;   // [0] multi rows (pass 2), [1] rows rescanned
     DBuf<uint32_t> over_rows;    // rows rescanned over all centers
     DBuf<float> CT0;             // transposed centers for that rescan
+    DBuf<uint32_t> auxa, auxb;   // norm MMA operands of the resident pass 1 (32 bytes per row)
     const float *X_src = nullptr;
     uint64_t n = 0, d = 0, dp = 0;
     int prec = -1;

@@ -104,11 +104,15 @@ void append_locked(const std::string &key, const Decision &d) {
     if (f) f << line_of(key, d) << '\n';
 }
 
+// attribute queries (cudaGetDeviceProperties fills the whole structure, far slower per call)
 std::string device_tag() {
-    int dev = 0;
-    cudaDeviceProp prop;
-    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return "dev?";
-    return "sm" + std::to_string(prop.major * 10 + prop.minor) + "x" + std::to_string(prop.multiProcessorCount);
+    int dev = 0, major = 0, minor = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return "dev?";
+    return "sm" + std::to_string(major * 10 + minor) + "x" + std::to_string(sms);
 }
 
 }  // namespace
@@ -123,14 +127,19 @@ int tune_launch(const std::string &key0, int nvariants, int default_variant, cud
                 const std::function<int(int)> &launch) {
     if (nvariants <= 1 || !allow) return launch(default_variant);
     std::string key;
+    int known = -1;  // decided under the lock, launched outside it (a launch may tune a nested key)
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
-        if (!tune_enabled_locked()) return launch(default_variant);
-        ensure_loaded_locked();
-        key = key0 + "|" + device_tag();
-        auto it = g_tune.find(key);
-        if (it != g_tune.end() && it->second.variant < nvariants) return launch(it->second.variant);
+        if (!tune_enabled_locked()) {
+            known = default_variant;
+        } else {
+            ensure_loaded_locked();
+            key = key0 + "|" + device_tag();
+            auto it = g_tune.find(key);
+            if (it != g_tune.end() && it->second.variant < nvariants) known = it->second.variant;
+        }
     }
+    if (known >= 0) return launch(known);
     // a stream being captured into a graph cannot time anything: the default (the variants
     // give identical results)
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;

@@ -235,3 +235,51 @@ def test_csr_l1_union_walk_variants_equal_oracle(mc, orc, tmp_path):
         assert np.array_equal(asn, oasn), v
         assert np.array_equal(cost, ocost), v
     mc.autotune_reset()
+
+
+@pytest.mark.parametrize("msr,prior,weighted,n,d,k,dup", [
+    (2, 0.0, False, 20011, 96, 40, False),   # three chunks, a ragged last 32-row block
+    (2, 0.0, True, 9000, 64, 25, False),     # weighted draws
+    (0, 0.5, False, 5003, 33, 17, False),    # L1, d not a multiple of 4 (scalar loads)
+    (6, 1.0, False, 3001, 40, 10, False),    # Hellinger
+    (5, 1.0, False, 4001, 52, 12, False),    # MKL
+    (4, 1.0, False, 3001, 40, 10, False),    # JSD
+    (2, 0.0, False, 3000, 16, 12, True),     # five distinct rows: zero total, first-maximum fallback
+    (2, 0.0, False, 262144, 32, 8, False),   # 32 chunks, 2^23 values: the largest cluster case
+])
+def test_kmeanspp_cluster_equals_launches(mc, orc, msr, prior, weighted, n, d, k, dup, tmp_path):
+    """Dense k-means++ as one persistent thread-block cluster (variant 1 of "kmpp_run") and as
+    a launch sequence per round (variant 0), each forced through a loaded decision: identical
+    center ids, assignments and costs, and for the exact measures identical to the oracle."""
+    rng = np.random.default_rng(n + d + k)
+    if msr in (4, 5, 6):
+        X = rng.integers(0, 6, size=(n, d)).astype(np.float32)
+    else:
+        X = (rng.normal(size=(n, d)) * 3.0).astype(np.float32)
+    if dup:
+        X = X[rng.integers(0, 5, n)]
+    w = rng.uniform(0.5, 2.0, n) if weighted else None
+    mc.autotune_reset()
+    mc.autotune(True)
+    mc.kmeanspp(X, k, msr=msr, prior=prior, seed=5, weights=w)   # records the decision
+    keys = [kk for kk in mc.autotune_report()["entries"] if kk.startswith("kmpp_run|")]
+    assert len(keys) == 1
+    got = []
+    for v in (0, 1):
+        mc.autotune_reset()
+        path = tmp_path / f"kc{v}.tsv"
+        path.write_text(f"{keys[0]}\t{v}\t\n")
+        mc.autotune_load(str(path))
+        got.append(mc.kmeanspp(X, k, msr=msr, prior=prior, seed=5, weights=w))
+        assert mc.autotune_report()["entries"][keys[0]]["variant"] == v
+    for a, b in zip(got[0], got[1]):
+        assert np.array_equal(a, b, equal_nan=True)
+    if msr in (0, 2, 6) and n <= 20011:
+        oids, oasn, ocosts = orc.kmeanspp(X, k, msr, prior, orc.uniforms(5, k), weights=w)
+        assert np.array_equal(got[1][0], oids)
+        assert np.array_equal(got[1][1], oasn)
+        assert np.array_equal(got[1][2], ocosts.astype(got[1][2].dtype))
+    if dup:
+        assert len(set(X[got[1][0].astype(np.int64)].tobytes()[i * d * 4:(i + 1) * d * 4] for i in range(k))) == 5
+    mc.autotune_reset()
+

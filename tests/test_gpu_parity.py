@@ -216,21 +216,35 @@ def test_kmeanspp_dense_matches_oracle(mc, orc, msr):
 
 @pytest.mark.parametrize("weighted", [False, True])
 @pytest.mark.parametrize("d", [32, 61])
-def test_kmeanspp_dense_sqrl2_pruned_matches_oracle(mc, orc, weighted, d):
-    """Over n d >= 2^20 values the dense SQRL2 rounds skip rows whose distance to the new
-    center provably cannot beat their current one (triangle inequality with FP32 rounding
-    bounds); ids, assignments and costs stay bit-identical to the oracle, which evaluates
-    every row.  Well-separated components (most rows pruned in later rounds), duplicated
-    rows (zero distances), d not a multiple of 4 (the unstaged kernel)."""
-    n = 50_000 if d == 32 else 20_000
+def test_kmeanspp_dense_sqrl2_pruned_matches_oracle(mc, orc, weighted, d, tmp_path):
+    """Over large dense SQRL2 matrices (beyond the persistent-cluster sizes) the rounds may
+    skip rows whose distance to the new center provably cannot beat their current one
+    (triangle inequality with FP32 rounding bounds), an autotuner choice ("kmpp_prune"
+    variant 1, forced here through a loaded decision, and variant 0 without it); ids,
+    assignments and costs stay bit-identical to the oracle, which evaluates every row.
+    Well-separated components (most rows pruned in later rounds), duplicated rows (zero
+    distances), d not a multiple of 4 (the unstaged kernel)."""
+    n = 300_000 if d == 32 else 140_000
     X = _mixture(n, d, 60, seed=d, spread=20.0)
     X[1000:1200] = X[0]
     w = np.random.default_rng(d).random(n) + 0.05 if weighted else None
-    ids, asn, costs = mc.kmeanspp(X, 48, msr=2, seed=77, weights=w)
     oids, oasn, ocosts = orc.kmeanspp(X, 48, 2, 0.0, orc.uniforms(77, 48), weights=w)
-    assert np.array_equal(ids, oids)
-    assert np.array_equal(asn.astype(np.uint32), oasn)
-    assert np.array_equal(costs, ocosts.astype(np.float32))
+    mc.autotune(True)
+    mc.autotune_reset()
+    mc.kmeanspp(X, 48, msr=2, seed=77, weights=w)   # records the decision
+    keys = [k for k in mc.autotune_report()["entries"] if k.startswith("kmpp_prune|")]
+    assert len(keys) == 1
+    for v in (1, 0):
+        mc.autotune_reset()
+        path = tmp_path / f"prune{v}.tsv"
+        path.write_text(f"{keys[0]}\t{v}\t\n")
+        mc.autotune_load(str(path))
+        ids, asn, costs = mc.kmeanspp(X, 48, msr=2, seed=77, weights=w)
+        assert mc.autotune_report()["entries"][keys[0]]["variant"] == v
+        assert np.array_equal(ids, oids)
+        assert np.array_equal(asn.astype(np.uint32), oasn)
+        assert np.array_equal(costs, ocosts.astype(np.float32))
+    mc.autotune_reset()
 
 
 @pytest.mark.parametrize("msr,trials,weighted", [(2, 3, False), (2, 2, True), (0, 4, False)])
