@@ -943,8 +943,9 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     // sequence per round, whichever the autotuner measured faster for this shape (identical
     // results)
     if (!a0.csr && a0.n <= kKcMaxRows && a0.n * a0.d <= (uint64_t(1) << 23) && a0.k > 1) {
+        // (time per round hardly depends on k: no k in the key, so a server tunes few buckets)
         const std::string key = "kmpp_run|msr" + std::to_string(a0.msr) + "|w" + std::to_string(a0.w ? 1 : 0) +
-                                "|d" + tune_bucket(a0.d) + "|n" + tune_bucket(a0.n) + "|k" + tune_bucket(a0.k);
+                                "|d" + tune_bucket(a0.d) + "|n" + tune_bucket(a0.n);
         return tune_launch(key, 2, 0, st, true, [&](int v) -> int {
             return v == 1 ? run_kmeanspp_cluster(a0, u_dev, st)
                           : run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, false);
@@ -955,8 +956,8 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     // before each row's distance: on the 2M x 64 Gaussian mixture it measured 19.2 ms per
     // 100-center run against 14.4 ms without), whichever the autotuner measures faster
     if (!a0.csr && a0.msr == SQRL2 && a0.k > 1 && a0.n * a0.d >= (uint64_t(1) << 20)) {
-        const std::string key = "kmpp_prune|d" + tune_bucket(a0.d) + "|n" + tune_bucket(a0.n) + "|k" +
-                                tune_bucket(a0.k);
+        const std::string key = "kmpp_prune|w" + std::to_string(a0.w ? 1 : 0) + "|d" + tune_bucket(a0.d) + "|n" +
+                                tune_bucket(a0.n);
         return tune_launch(key, 2, 0, st, true, [&](int v) -> int {
             return run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, v == 1);
         });
