@@ -189,9 +189,12 @@ __global__ void __launch_bounds__(256) k_kmpp_dense(const KmppArgs a, int first)
     }
 }
 
-// CSR rows (any measure, any prior): one warp per row.  sum over all columns of
-// f(a_j, b0) (b0: transform of a zero entry) plus, over the row's nonzeros,
-// f(a_j, b_j) - f(a_j, b0).
+// CSR rows (any measure, any prior): sum over all columns of f(a_j, b0) (b0: transform of a
+// zero entry) plus, over the row's nonzeros, f(a_j, b_j) - f(a_j, b0).  A warp takes 32 rows
+// at a time: lane l evaluates row g0 + l's skip test, prior scalars and FP64 cost (a warp-wide
+// FP64 instruction costs the SM's FP64 pipe the same whatever its active lanes, so these run
+// once per 32 rows), and the warp walks each row's columns together (lanes strided, a butterfly
+// for the float sum), as one warp per row did: the arithmetic and its order are unchanged.
 template <int MSR>
 __global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, uint32_t round) {
     const int lane = threadIdx.x & 31;
@@ -199,31 +202,91 @@ __global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, u
     const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
     const uint64_t c = *a.newc;
     const double csum = a.rowsum[c];
-    for (uint64_t i = warp; i < a.n; i += nwarps) {
-        if (!first && (i == c || a.dist[i] <= 0.0)) continue;
-        const PairScalars s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], csum, a.d);
-        float acc = 0.f;
-        for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, a.cbuf[j], 0.f, s);
-        for (uint64_t p = a.indptr[i] + lane; p < a.indptr[i + 1]; p += 32) {
-            const float cj = a.cbuf[a.idx[p]];
-            float t1 = 0.f, t0 = 0.f;
-            kp_elem<MSR>(t1, cj, a.vals[p], s);
-            kp_elem<MSR>(t0, cj, 0.f, s);
-            acc = acc + (t1 - t0);
+    for (uint64_t g0 = warp * 32; g0 < a.n; g0 += nwarps * 32) {
+        const uint64_t my = g0 + uint64_t(lane);
+        const bool go = my < a.n && (first || (my != c && !(a.dist[my] <= 0.0)));
+        PairScalars sm = {0.f, 0.f, 0.f, 0.f, 0.f};
+        uint64_t pbm = 0, pem = 0;
+        if (go) {
+            sm = pair_scalars(a.prior, a.prior_sum, a.rowsum[my], csum, a.d);
+            pbm = a.indptr[my];
+            pem = a.indptr[my + 1];
         }
-#pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
-        if (lane == 0) {
-            double v = kp_cost<MSR>(acc);
-            if (MSR == SQRL2 && v < 0.0) v = 0.0;
-            if (first) {
-                a.dist[i] = (i == c) ? 0.0 : v;
-            } else if (v < a.dist[i]) {
-                a.dist[i] = v;
-                a.asn[i] = round;
+        float accm = 0.f;
+        unsigned todo = __ballot_sync(0xffffffffu, go);
+        while (todo) {
+            const int r = __ffs(todo) - 1;
+            todo &= todo - 1;
+            PairScalars s;
+            s.pv = __shfl_sync(0xffffffffu, sm.pv, r);
+            s.lhrsi = __shfl_sync(0xffffffffu, sm.lhrsi, r);
+            s.rhrsi = __shfl_sync(0xffffffffu, sm.rhrsi, r);
+            s.lhinc = __shfl_sync(0xffffffffu, sm.lhinc, r);
+            s.rhinc = __shfl_sync(0xffffffffu, sm.rhinc, r);
+            const uint64_t pb = __shfl_sync(0xffffffffu, pbm, r), pe = __shfl_sync(0xffffffffu, pem, r);
+            float acc = 0.f;
+            for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, a.cbuf[j], 0.f, s);
+            for (uint64_t p = pb + lane; p < pe; p += 32) {
+                const float cj = a.cbuf[a.idx[p]];
+                float t1 = 0.f, t0 = 0.f;
+                kp_elem<MSR>(t1, cj, a.vals[p], s);
+                kp_elem<MSR>(t0, cj, 0.f, s);
+                acc = acc + (t1 - t0);
             }
+#pragma unroll
+            for (int m = 16; m >= 1; m >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
+            if (lane == r) accm = acc;
+        }
+        if (!go) continue;
+        double v = kp_cost<MSR>(accm);
+        if (MSR == SQRL2 && v < 0.0) v = 0.0;
+        if (first) {
+            a.dist[my] = (my == c) ? 0.0 : v;
+        } else if (v < a.dist[my]) {
+            a.dist[my] = v;
+            a.asn[my] = round;
         }
     }
+}
+
+// Block sums of the per-thread FP64 partials (s0, s1) of a 1024-thread CTA: a pairwise tree
+// over the 32 lanes of each warp (shfl_xor), then over the 32 warp totals; warps that held no
+// column add nothing (their totals are 0).  Every thread gets the sums.  A dependent FP64 add
+// costs about 75 ns here and a warp-wide FP64 instruction occupies the SM's FP64 pipe for the
+// whole warp whatever its active lanes, so the trees replace sequential walks in every warp.
+__device__ __forceinline__ void kp_block_sum2(double s0, double s1, uint64_t d, double *w0, double *w1, double &u0,
+                                              double &u1) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (uint64_t(wid) * 32 < d) {
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) {
+            s0 = s0 + __shfl_xor_sync(0xffffffffu, s0, m);
+            s1 = s1 + __shfl_xor_sync(0xffffffffu, s1, m);
+        }
+    } else {
+        s0 = 0.0;
+        s1 = 0.0;
+    }
+    if (lane == 0) {
+        w0[wid] = s0;
+        w1[wid] = s1;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        double t0 = w0[lane], t1 = w1[lane];
+#pragma unroll
+        for (int m = 16; m >= 1; m >>= 1) {
+            t0 = t0 + __shfl_xor_sync(0xffffffffu, t0, m);
+            t1 = t1 + __shfl_xor_sync(0xffffffffu, t1, m);
+        }
+        if (lane == 0) {
+            w0[32] = t0;
+            w1[32] = t1;
+        }
+    }
+    __syncthreads();
+    u0 = w0[32];
+    u1 = w1[32];
 }
 
 // CSR rows against the new center in O(nnz) per row (SQRL2, L1, MKL, Hellinger; rows whose
@@ -243,11 +306,11 @@ __global__ void __launch_bounds__(256) k_kmpp_csr(const KmppArgs a, int first, u
 // with a = c * lhrsi + lhinc (center side), b = x * rhrsi + rhinc (row side).  Rows whose pair
 // moves the prior to the smallest-pv floor take the column loop of k_kmpp_csr.
 // k_kmpp_center_prep (one CTA) writes ct (c, c', a or sqrt a per column) and K0, K1: thread t
-// adds columns t, t+1024, ... in FP64; the 32 lanes of a warp, then the 32 warps, are added in
-// order.
+// adds columns t, t+1024, ... in FP64; the 32 lanes of a warp, then the 32 warps, are added by
+// pairwise trees (kp_block_sum2).
 template <int MSR>
 __global__ void __launch_bounds__(1024) k_kmpp_center_prep(const KmppArgs a) {
-    __shared__ double w0[32], w1[32];
+    __shared__ double w0[33], w1[33];
     const uint64_t c = *a.newc;
     const float pv = float(a.prior);
     float rsi = 0.f, inc = 0.f;
@@ -278,24 +341,9 @@ __global__ void __launch_bounds__(1024) k_kmpp_center_prep(const KmppArgs a) {
         }
         a.ct[j] = t;
     }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double t0 = 0.0, t1 = 0.0;
-#pragma unroll
-    for (int l = 0; l < 32; ++l) {
-        t0 = t0 + __shfl_sync(0xffffffffu, s0, l);
-        t1 = t1 + __shfl_sync(0xffffffffu, s1, l);
-    }
-    if (lane == 0) {
-        w0[wid] = t0;
-        w1[wid] = t1;
-    }
-    __syncthreads();
+    double u0, u1;
+    kp_block_sum2(s0, s1, a.d, w0, w1, u0, u1);
     if (threadIdx.x == 0 && MSR != JSD) {
-        double u0 = 0.0, u1 = 0.0;
-        for (int q = 0; q < 32; ++q) {
-            u0 = u0 + w0[q];
-            u1 = u1 + w1[q];
-        }
         a.cconst[0] = u0;
         a.cconst[1] = u1;
     }
@@ -321,7 +369,11 @@ __global__ void __launch_bounds__(256) k_kmpp_jsd_zcol(const KmppArgs a) {
     if (lane == 0) a.cconst[g] = t;
 }
 
-// the rows of one round (warp per row): ct = transformed center, raw = densified center
+// the rows of one round: ct = transformed center, raw = densified center.  A warp takes 32
+// rows at a time: lane l evaluates row g0 + l's skip test, prior scalars and FP64 key (one
+// FP64 warp instruction per 32 rows), and the warp walks each row's nonzeros together (lanes
+// strided over the nonzeros, a butterfly for the float sum), as one warp per row did: the
+// arithmetic and its order are unchanged.
 template <int MSR>
 __device__ __forceinline__ void kp_nnz_rows(const KmppArgs &a, int first, uint32_t round, uint64_t c,
                                             const float *ct, const float *raw, double K0, double K1) {
@@ -330,87 +382,123 @@ __device__ __forceinline__ void kp_nnz_rows(const KmppArgs &a, int first, uint32
     const uint64_t nwarps = (gridDim.x * uint64_t(blockDim.x)) >> 5;
     const double csum = a.rowsum[c];
     const float fp = float(a.prior);
-    for (uint64_t i = warp; i < a.n; i += nwarps) {
-        if (!first && (i == c || a.dist[i] <= 0.0)) continue;
-        const PairScalars s = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], csum, a.d);
-        const uint64_t pb = a.indptr[i], pe = a.indptr[i + 1];
-        double v;
-        if (MSR == SQRL2 || s.pv == fp) {
-            const float rsi = s.rhrsi, rinc = (MSR == JSD) ? a.gval[a.grp[i]] : s.rhinc;
-            const float rlr = (MSR == JSD) ? rinc * logf(rinc) : 0.f;
-            const float rl = (MSR == MKL) ? logf(rinc) : 0.f;
-            const float srinc = (MSR == HELLINGER) ? sqrtf(rinc) : 0.f;
-            float acc = 0.f;
-            double bsum = 0.0;
+    for (uint64_t g0 = warp * 32; g0 < a.n; g0 += nwarps * 32) {
+        const uint64_t my = g0 + uint64_t(lane);
+        const bool go = my < a.n && (first || (my != c && !(a.dist[my] <= 0.0)));
+        PairScalars sm = {0.f, 0.f, 0.f, 0.f, 0.f};
+        uint64_t pbm = 0, pem = 0;
+        float rincm = 0.f, rlm = 0.f, rlrm = 0.f, srincm = 0.f;
+        bool fastm = true;
+        if (go) {
+            sm = pair_scalars(a.prior, a.prior_sum, a.rowsum[my], csum, a.d);
+            pbm = a.indptr[my];
+            pem = a.indptr[my + 1];
+            fastm = MSR == SQRL2 || sm.pv == fp;
+            rincm = (MSR == JSD) ? a.gval[a.grp[my]] : sm.rhinc;
+            rlrm = (MSR == JSD) ? rincm * logf(rincm) : 0.f;
+            rlm = (MSR == MKL) ? logf(rincm) : 0.f;
+            srincm = (MSR == HELLINGER) ? sqrtf(rincm) : 0.f;
+        }
+        float accm = 0.f;     // lane l: row g0 + l's float sum
+        double bsumm = 0.0;   // lane l: row g0 + l's FP64 sum (Hellinger, JSD)
+        unsigned todo = __ballot_sync(0xffffffffu, go);
+        while (todo) {
+            const int r = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint64_t pb = __shfl_sync(0xffffffffu, pbm, r), pe = __shfl_sync(0xffffffffu, pem, r);
+            const bool fast = __shfl_sync(0xffffffffu, fastm ? 1 : 0, r) != 0;
+            if (fast) {
+                const float rsi = __shfl_sync(0xffffffffu, sm.rhrsi, r);
+                const float rinc = __shfl_sync(0xffffffffu, rincm, r);
+                const float rlr = __shfl_sync(0xffffffffu, rlrm, r);
+                const float rl = __shfl_sync(0xffffffffu, rlm, r);
+                const float srinc = __shfl_sync(0xffffffffu, srincm, r);
+                float acc = 0.f;
+                double bsum = 0.0;
 #pragma unroll 4
-            for (uint64_t p = pb + lane; p < pe; p += 32) {
-                const float x = a.vals[p];
-                const float cj = ct[a.idx[p]];
-                if (MSR == SQRL2) {
-                    acc = fmaf(x, x - 2.f * cj, acc);
-                } else if (MSR == L1) {
-                    acc = acc + (fabsf(cj - (x + fp)) - fabsf(cj - fp));
-                } else if (MSR == MKL) {
-                    acc = fmaf(cj, rl - logf(x * rsi + rinc), acc);
-                } else if (MSR == JSD) {
-                    const float b = x * rsi + rinc;
-                    const float m0 = cj + rinc, m1 = cj + b;
-                    acc = acc + (m0 * logf(m0 * 0.5f) - m1 * logf(m1 * 0.5f));
-                    bsum = bsum + double(b * logf(b) - rlr);
-                } else {
-                    // (sqrt a - sqrt b)^2 - (sqrt a - sqrt r)^2 in FP64 from the float roots
-                    const float b = x * rsi + rinc;
-                    const double dd = double(cj) - double(sqrtf(b)), de = double(cj) - double(srinc);
-                    bsum = bsum + (dd * dd - de * de);
+                for (uint64_t p = pb + lane; p < pe; p += 32) {
+                    const float x = a.vals[p];
+                    const float cj = ct[a.idx[p]];
+                    if (MSR == SQRL2) {
+                        acc = fmaf(x, x - 2.f * cj, acc);
+                    } else if (MSR == L1) {
+                        acc = acc + (fabsf(cj - (x + fp)) - fabsf(cj - fp));
+                    } else if (MSR == MKL) {
+                        acc = fmaf(cj, rl - logf(x * rsi + rinc), acc);
+                    } else if (MSR == JSD) {
+                        const float b = x * rsi + rinc;
+                        const float m0 = cj + rinc, m1 = cj + b;
+                        acc = acc + (m0 * logf(m0 * 0.5f) - m1 * logf(m1 * 0.5f));
+                        bsum = bsum + double(b * logf(b) - rlr);
+                    } else {
+                        // (sqrt a - sqrt b)^2 - (sqrt a - sqrt r)^2 in FP64 from the float roots
+                        const float b = x * rsi + rinc;
+                        const double dd = double(cj) - double(sqrtf(b)), de = double(cj) - double(srinc);
+                        bsum = bsum + (dd * dd - de * de);
+                    }
                 }
-            }
 #pragma unroll
-            for (int m = 16; m >= 1; m >>= 1) {
-                acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
-                if (MSR == HELLINGER || MSR == JSD) bsum = bsum + __shfl_xor_sync(0xffffffffu, bsum, m);
+                for (int m = 16; m >= 1; m >>= 1) {
+                    acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
+                    if (MSR == HELLINGER || MSR == JSD) bsum = bsum + __shfl_xor_sync(0xffffffffu, bsum, m);
+                }
+                if (lane == r) {
+                    accm = acc;
+                    bsumm = bsum;
+                }
+            } else {
+                PairScalars s;
+                s.pv = __shfl_sync(0xffffffffu, sm.pv, r);
+                s.lhrsi = __shfl_sync(0xffffffffu, sm.lhrsi, r);
+                s.rhrsi = __shfl_sync(0xffffffffu, sm.rhrsi, r);
+                s.lhinc = __shfl_sync(0xffffffffu, sm.lhinc, r);
+                s.rhinc = __shfl_sync(0xffffffffu, sm.rhinc, r);
+                float acc = 0.f;
+                for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, raw[j], 0.f, s);
+                for (uint64_t p = pb + lane; p < pe; p += 32) {
+                    const float cj = raw[a.idx[p]];
+                    float t1 = 0.f, t0 = 0.f;
+                    kp_elem<MSR>(t1, cj, a.vals[p], s);
+                    kp_elem<MSR>(t0, cj, 0.f, s);
+                    acc = acc + (t1 - t0);
+                }
+#pragma unroll
+                for (int m = 16; m >= 1; m >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
+                if (lane == r) accm = acc;
             }
+        }
+        if (!go) continue;
+        double v;
+        if (fastm) {
             float key;
             if (MSR == SQRL2) {
-                double t = K0 + double(acc);
+                double t = K0 + double(accm);
                 key = float(t < 0.0 ? 0.0 : t);
                 v = double(key);
             } else if (MSR == L1) {
-                key = float(K0 + double(acc)) * 0.5f;
+                key = float(K0 + double(accm)) * 0.5f;
                 v = double(key) * 2.0;
             } else if (MSR == MKL) {
-                key = post_divergence(float(K0 - double(rl) * K1 + double(acc)));
+                key = post_divergence(float(K0 - double(rlm) * K1 + double(accm)));
                 v = double(key);
             } else if (MSR == JSD) {
-                key = post_divergence(float((a.cconst[a.grp[i]] + bsum + double(acc)) * 0.5));
+                key = post_divergence(float((a.cconst[a.grp[my]] + bsumm + double(accm)) * 0.5));
                 v = double(key);
             } else {
-                const double sr = double(srinc);
-                double t = (K0 - 2.0 * sr * K1 + double(a.d) * sr * sr) + bsum;
+                const double sr = double(srincm);
+                double t = (K0 - 2.0 * sr * K1 + double(a.d) * sr * sr) + bsumm;
                 key = float(sqrt(t < 0.0 ? 0.0 : t));
                 v = double(key) * kSqrt1_2;
             }
         } else {
-            float acc = 0.f;
-            for (uint64_t j = lane; j < a.d; j += 32) kp_elem<MSR>(acc, raw[j], 0.f, s);
-            for (uint64_t p = pb + lane; p < pe; p += 32) {
-                const float cj = raw[a.idx[p]];
-                float t1 = 0.f, t0 = 0.f;
-                kp_elem<MSR>(t1, cj, a.vals[p], s);
-                kp_elem<MSR>(t0, cj, 0.f, s);
-                acc = acc + (t1 - t0);
-            }
-#pragma unroll
-            for (int m = 16; m >= 1; m >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
-            v = kp_cost<MSR>(acc);
+            v = kp_cost<MSR>(accm);
             if (MSR == SQRL2 && v < 0.0) v = 0.0;
         }
-        if (lane == 0) {
-            if (first) {
-                a.dist[i] = (i == c) ? 0.0 : v;
-            } else if (v < a.dist[i]) {
-                a.dist[i] = v;
-                a.asn[i] = round;
-            }
+        if (first) {
+            a.dist[my] = (my == c) ? 0.0 : v;
+        } else if (v < a.dist[my]) {
+            a.dist[my] = v;
+            a.asn[my] = round;
         }
     }
 }
@@ -431,7 +519,7 @@ template <int MSR>
 __global__ void __launch_bounds__(1024) k_kmpp_csr_fused(const KmppArgs a, int first, uint32_t round) {
     extern __shared__ float sm_kp[];
     float *raw = sm_kp, *ct = sm_kp + a.d;
-    __shared__ double w0[32], w1[32], kk[2];
+    __shared__ double w0[33], w1[33];
     const uint64_t c = *a.newc;
     const int tid = threadIdx.x;
     for (uint64_t j = tid; j < a.d; j += 1024) raw[j] = 0.f;
@@ -470,29 +558,9 @@ __global__ void __launch_bounds__(1024) k_kmpp_csr_fused(const KmppArgs a, int f
         }
         ct[j] = t;
     }
-    const int lane = tid & 31, wid = tid >> 5;
-    double t0 = 0.0, t1 = 0.0;
-#pragma unroll
-    for (int l = 0; l < 32; ++l) {
-        t0 = t0 + __shfl_sync(0xffffffffu, s0, l);
-        t1 = t1 + __shfl_sync(0xffffffffu, s1, l);
-    }
-    if (lane == 0) {
-        w0[wid] = t0;
-        w1[wid] = t1;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        double u0 = 0.0, u1 = 0.0;
-        for (int q = 0; q < 32; ++q) {
-            u0 = u0 + w0[q];
-            u1 = u1 + w1[q];
-        }
-        kk[0] = u0;
-        kk[1] = u1;
-    }
-    __syncthreads();
-    kp_nnz_rows<MSR>(a, first, round, c, ct, raw, kk[0], kk[1]);
+    double u0, u1;
+    kp_block_sum2(s0, s1, a.d, w0, w1, u0, u1);
+    kp_nnz_rows<MSR>(a, first, round, c, ct, raw, u0, u1);
 }
 
 __device__ __forceinline__ void kp_cp_async16(void *dst, const void *src, int src_bytes) {
