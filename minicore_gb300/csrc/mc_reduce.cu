@@ -208,8 +208,58 @@ __global__ void k_row_sums_csr(const float *__restrict__ vals, const uint64_t *_
     rowsum[i] = s;
 }
 
+// norms only, rows of d % 4 == 0 floats at 16-byte alignment: the CTA's 128 rows are staged
+// 32 columns at a time through shared memory with coalesced cp.async (double buffered), and
+// each thread keeps its row's sequential fmaf chain (k_row_sums_dense reads a row per thread
+// straight from global memory: 32 rows per load instruction, about 1.2 TB/s)
+__global__ void __launch_bounds__(128) k_row_norms_staged(const float *__restrict__ X, uint64_t n, uint64_t d,
+                                                          float *rownorm) {
+    __shared__ __align__(16) float xs[2][128][36];
+    const int t = threadIdx.x;
+    const uint64_t row0 = uint64_t(blockIdx.x) * 128;
+    const uint64_t nchunk = (d + 31) / 32;
+    auto stage = [&](uint64_t ci, int buf) {
+        const uint64_t k0 = ci * 32;
+        const int kmax = int(umin64(32, d - k0));
+        for (int e = t; e < 128 * 8; e += 128) {
+            const int r = e >> 3, q4 = e & 7;
+            const bool ok = row0 + r < n && 4 * q4 < kmax;
+            const float *src = ok ? X + (row0 + r) * d + k0 + 4 * q4 : X;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(uint32_t(__cvta_generic_to_shared(
+                             &xs[buf][r][4 * q4]))),
+                         "l"(src), "r"(ok ? 16 : 0)
+                         : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    float q = 0.f;
+    stage(0, 0);
+    for (uint64_t ci = 0; ci < nchunk; ++ci) {
+        const int buf = int(ci & 1);
+        if (ci + 1 < nchunk) {
+            stage(ci + 1, buf ^ 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        const int kmax = int(umin64(32, d - ci * 32));
+        for (int kk = 0; kk < kmax; ++kk) {
+            const float v = xs[buf][t][kk];
+            q = fmaf(v, v, q);
+        }
+        __syncthreads();
+    }
+    if (row0 + t < n) rownorm[row0 + t] = q;
+}
+
 int launch_row_sums_dense(const float *X, uint64_t n, uint64_t d, double *rowsum, float *rownorm, cudaStream_t st) {
     if (n == 0) return MC_OK;
+    if (!rowsum && rownorm && d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0) {
+        k_row_norms_staged<<<unsigned((n + 127) / 128), 128, 0, st>>>(X, n, d, rownorm), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        return MC_OK;
+    }
     k_row_sums_dense<<<unsigned((n + 127) / 128), 128, 0, st>>>(X, n, d, rowsum, rownorm), note_launch();
     MC_CUDA_TRY(cudaGetLastError());
     return MC_OK;

@@ -796,6 +796,22 @@ __global__ void k_to_bf16_pad(const float *__restrict__ X, uint64_t n, uint64_t 
     }
 }
 
+// rows without padding (d % 8 == 0, 16-byte aligned): eight floats per thread, two float4
+// loads and one 16-byte store of four bf16 pairs (the same round-to-nearest conversion)
+__global__ void k_to_bf16_flat8(const float4 *__restrict__ X, uint64_t n8, uint4 *__restrict__ Y) {
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < n8; e += gridDim.x * uint64_t(blockDim.x)) {
+        const float4 a = X[2 * e], b = X[2 * e + 1];
+        const __nv_bfloat162 p0 = __floats2bfloat162_rn(a.x, a.y), p1 = __floats2bfloat162_rn(a.z, a.w);
+        const __nv_bfloat162 p2 = __floats2bfloat162_rn(b.x, b.y), p3 = __floats2bfloat162_rn(b.z, b.w);
+        uint4 o;
+        o.x = *reinterpret_cast<const uint32_t *>(&p0);
+        o.y = *reinterpret_cast<const uint32_t *>(&p1);
+        o.z = *reinterpret_cast<const uint32_t *>(&p2);
+        o.w = *reinterpret_cast<const uint32_t *>(&p3);
+        Y[e] = o;
+    }
+}
+
 __global__ void k_pad_f32(const float *__restrict__ X, uint64_t n, uint64_t d, uint64_t dp, float *__restrict__ Y) {
     const uint64_t total = n * dp;
     for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x)) {
@@ -1408,7 +1424,11 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
             }
         } else {
             MC_TRY(s.Xb.alloc(n * dp, st));
-            k_to_bf16_pad<<<cg, 256, 0, st>>>(X, n, d, dp, s.Xb.p), note_launch();
+            if (dp == d && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
+                k_to_bf16_flat8<<<unsigned(umin64((n * d / 8 + 255) / 256, uint64_t(sms) * 16)), 256, 0, st>>>(
+                    reinterpret_cast<const float4 *>(X), n * d / 8, reinterpret_cast<uint4 *>(s.Xb.p)), note_launch();
+            else
+                k_to_bf16_pad<<<cg, 256, 0, st>>>(X, n, d, dp, s.Xb.p), note_launch();
         }
         MC_CUDA_TRY(cudaGetLastError());
         s.X_src = X;

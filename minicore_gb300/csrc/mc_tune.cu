@@ -125,7 +125,7 @@ std::string tune_bucket(uint64_t v) {
 
 int tune_launch(const std::string &key0, int nvariants, int default_variant, cudaStream_t st, bool allow,
                 const std::function<int(int)> &launch) {
-    if (nvariants <= 1 || !allow) return launch(default_variant);
+    if (nvariants <= 1) return launch(default_variant);
     std::string key;
     int known = -1;  // decided under the lock, launched outside it (a launch may tune a nested key)
     {
@@ -140,6 +140,9 @@ int tune_launch(const std::string &key0, int nvariants, int default_variant, cud
         }
     }
     if (known >= 0) return launch(known);
+    // a caller that may not time (a loop that must not synchronise, a stream being captured)
+    // takes a recorded decision above, else the default
+    if (!allow) return launch(default_variant);
     // a stream being captured into a graph cannot time anything: the default (the variants
     // give identical results)
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;

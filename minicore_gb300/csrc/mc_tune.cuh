@@ -11,8 +11,9 @@ namespace mc {
 // variant must write the same results (same per-element arithmetic and summation order)
 // and be idempotent, so timing them changes nothing but speed.  On the first call for a
 // key, unless the cache holds it, each variant runs twice on `st` (CUDA events) and the
-// fastest is kept; later calls launch the kept variant only.  With tuning off, or when
-// `allow` is false (callers that must not synchronise or allocate), the default runs.
+// fastest is kept; later calls launch the kept variant only.  With tuning off, the default
+// runs; when `allow` is false (callers that must not synchronise: the loops that run without
+// host round trips, stream capture), a recorded decision runs, else the default.
 int tune_launch(const std::string &key, int nvariants, int default_variant, cudaStream_t st, bool allow,
                 const std::function<int(int)> &launch);
 
