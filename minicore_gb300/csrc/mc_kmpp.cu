@@ -651,6 +651,119 @@ __global__ void __launch_bounds__(128) k_kmpp_dense_staged(const KmppArgs a, int
     }
 }
 
+// The same with persistent CTAs: each of sms x 4 CTAs walks its row tiles (stride gridDim)
+// as one stream of (tile, 32-column chunk) items, staging the next item while it evaluates
+// the current one, across tile boundaries too (the next tile's skip flags are read first).
+// With one tile per CTA, every CTA waits for its first chunk from DRAM before any work; here
+// the copies of the next tile overlap the last chunk of the current one.  Same per-row
+// arithmetic and bookkeeping as k_kmpp_dense_staged.
+template <int MSR>
+__global__ void __launch_bounds__(128) k_kmpp_dense_persist(const KmppArgs a, int first) {
+    __shared__ __align__(16) float xs[2][128][36];
+    __shared__ __align__(16) float cs[2][32];
+    __shared__ unsigned char act_s[2][128];
+    const uint64_t c = *a.newc;
+    if (!first && blockIdx.x == 0 && threadIdx.x == 0) {
+        a.center_ids[a.round] = uint32_t(c);
+        a.asn[c] = a.round;
+    }
+    const int t = threadIdx.x;
+    const uint64_t d = a.d, nchunk = (d + 31) / 32, ntiles = (a.n + 127) / 128;
+    auto row_state = [&](uint64_t m, bool &act, double &cur, PairScalars &ps) {
+        const uint64_t i = m * 128 + uint64_t(t);
+        act = i < a.n;
+        cur = 0.0;
+        ps = PairScalars{0.f, 0.f, 0.f, 0.f, 0.f};
+        if (act && !first) {
+            if (i == c) {
+                a.dist[i] = 0.0;
+                act = false;
+            } else {
+                cur = a.dist[i];
+                if (cur <= 0.0) act = false;
+                else if (MSR == SQRL2 && a.cgap && kp_prune(a, i, cur)) act = false;
+            }
+        }
+        if (act && MSR != SQRL2) ps = pair_scalars(a.prior, a.prior_sum, a.rowsum[i], a.rowsum[c], a.d);
+    };
+    auto stage = [&](uint64_t m, uint64_t ci, int buf, int ab) {
+        const uint64_t k0 = ci * 32, row0 = m * 128;
+        const int kmax = int(umin64(32, d - k0));
+        for (int e = t; e < 128 * 8; e += 128) {
+            const int r = e >> 3, q4 = e & 7;
+            const bool ok = act_s[ab][r] && 4 * q4 < kmax;
+            kp_cp_async16(&xs[buf][r][4 * q4], ok ? a.X + (row0 + r) * d + k0 + 4 * q4 : a.X, ok ? 16 : 0);
+        }
+        if (t < 8) {
+            const bool ok = 4 * t < kmax;
+            kp_cp_async16(&cs[buf][4 * t], ok ? a.X + c * d + k0 + 4 * t : a.X, ok ? 16 : 0);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    uint64_t m = blockIdx.x;
+    if (m >= ntiles) return;
+    bool active;
+    double cur;
+    PairScalars ps;
+    row_state(m, active, cur, ps);
+    int ab = 0, buf = 0;
+    act_s[ab][t] = active ? 1 : 0;
+    __syncthreads();
+    stage(m, 0, buf, ab);
+    float acc = 0.f;
+    for (;;) {
+        for (uint64_t ci = 0; ci < nchunk; ++ci) {
+            const bool last = ci + 1 == nchunk;
+            const uint64_t mn = m + gridDim.x;
+            const bool have_next = !last || mn < ntiles;
+            bool act2 = false;
+            double cur2 = 0.0;
+            PairScalars ps2 = PairScalars{0.f, 0.f, 0.f, 0.f, 0.f};
+            if (!last) {
+                stage(m, ci + 1, buf ^ 1, ab);
+            } else if (have_next) {
+                row_state(mn, act2, cur2, ps2);
+                act_s[ab ^ 1][t] = act2 ? 1 : 0;
+                __syncthreads();
+                stage(mn, 0, buf ^ 1, ab ^ 1);
+            }
+            if (have_next) asm volatile("cp.async.wait_group 1;" ::: "memory");
+            else asm volatile("cp.async.wait_group 0;" ::: "memory");
+            __syncthreads();
+            const int kmax = int(umin64(32, d - ci * 32));
+            if (active) {
+                if (kmax == 32) {
+#pragma unroll
+                    for (int kk = 0; kk < 32; ++kk) kp_elem<MSR>(acc, cs[buf][kk], xs[buf][t][kk], ps);
+                } else {
+                    for (int kk = 0; kk < kmax; ++kk) kp_elem<MSR>(acc, cs[buf][kk], xs[buf][t][kk], ps);
+                }
+            }
+            __syncthreads();  // buffer buf is restaged in the next iteration
+            buf ^= 1;
+            if (last) {
+                if (active) {
+                    const uint64_t i = m * 128 + uint64_t(t);
+                    const double v = kp_cost<MSR>(acc);
+                    if (first) {
+                        a.dist[i] = (i == c) ? 0.0 : v;
+                    } else if (v < cur) {
+                        a.dist[i] = v;
+                        a.asn[i] = a.round;
+                    }
+                }
+                if (!have_next) return;
+                m = mn;
+                active = act2;
+                cur = cur2;
+                ps = ps2;
+                ab ^= 1;
+                acc = 0.f;
+            }
+        }
+    }
+}
+
 // CSR update in one launch per round: the center row and its transform fit in 32 KB
 static bool kmpp_csr_fused_ok(const KmppArgs &a) { return a.csr && a.msr != JSD && a.ct && a.d <= 4096; }
 
@@ -665,11 +778,14 @@ static int update_t(const KmppArgs &a, int first, uint32_t round, int sms, cudaS
             // per-row arithmetic): the autotuner keeps the faster for this measure and width
             const std::string key = "kmpp_dense|msr" + std::to_string(MSR) + "|d" + tune_bucket(a.d) + "|n" +
                                     tune_bucket(a.n);
-            return tune_launch(key, 2, 0, st, true, [&](int v) -> int {
+            return tune_launch(key, 3, 0, st, true, [&](int v) -> int {
                 if (v == 0)
                     k_kmpp_dense_staged<MSR><<<unsigned((a.n + 127) / 128), 128, 0, st>>>(b, first), note_launch();
-                else
+                else if (v == 1)
                     k_kmpp_dense<MSR, true><<<unsigned((a.n + 255) / 256), 256, 0, st>>>(b, first), note_launch();
+                else
+                    k_kmpp_dense_persist<MSR><<<unsigned(umin64((a.n + 127) / 128, uint64_t(sms) * 4)), 128, 0, st>>>(
+                        b, first), note_launch();
                 MC_CUDA_TRY(cudaGetLastError());
                 return MC_OK;
             });

@@ -283,3 +283,43 @@ def test_kmeanspp_cluster_equals_launches(mc, orc, msr, prior, weighted, n, d, k
         assert len(set(X[got[1][0].astype(np.int64)].tobytes()[i * d * 4:(i + 1) * d * 4] for i in range(k))) == 5
     mc.autotune_reset()
 
+
+
+@pytest.mark.parametrize("msr,prior,d", [(2, 0.0, 64), (5, 1.0, 36), (0, 0.5, 100)])
+def test_kmeanspp_dense_update_variants_equal_oracle(mc, orc, msr, prior, d, tmp_path):
+    """The dense k-means++ distance update in each form, forced through a loaded decision: rows
+    staged per CTA (variant 0), read directly (1), or persistent CTAs streaming (tile, chunk)
+    items across tile boundaries (2).  A matrix beyond the persistent-cluster sizes (n d >
+    2^23), d with a partial last 32-column chunk; ids, assignments and costs equal the oracle's
+    (SQRL2, L1) or each other (MKL)."""
+    n = 150_000 if d <= 64 else 90_000
+    rng = np.random.default_rng(d + msr)
+    if msr == 5:
+        X = rng.integers(0, 6, size=(n, d)).astype(np.float32)
+    else:
+        X = (rng.normal(size=(n, d)) * 2.0 + rng.integers(0, 8, size=(n, 1))).astype(np.float32)
+    k = 12
+    mc.autotune(True)
+    mc.autotune_reset()
+    mc.kmeanspp(X, k, msr=msr, prior=prior, seed=9)
+    keys = [kk for kk in mc.autotune_report()["entries"] if kk.startswith(f"kmpp_dense|msr{msr}|")]
+    assert len(keys) == 1 and len(mc.autotune_report()["entries"][keys[0]]["ms"]) == 3
+    prune = [kk for kk in mc.autotune_report()["entries"] if kk.startswith("kmpp_prune|")]
+    got = []
+    for v in (0, 1, 2):
+        mc.autotune_reset()
+        path = tmp_path / f"upd{v}.tsv"
+        lines = f"{keys[0]}\t{v}\t\n" + "".join(f"{p}\t0\t\n" for p in prune)
+        path.write_text(lines)
+        mc.autotune_load(str(path))
+        got.append(mc.kmeanspp(X, k, msr=msr, prior=prior, seed=9))
+        assert mc.autotune_report()["entries"][keys[0]]["variant"] == v
+    for r in got[1:]:
+        for a, b in zip(got[0], r):
+            assert np.array_equal(a, b)
+    if msr in (0, 2):
+        oids, oasn, ocosts = orc.kmeanspp(X, k, msr, prior, orc.uniforms(9, k))
+        assert np.array_equal(got[2][0], oids)
+        assert np.array_equal(got[2][1].astype(np.uint32), oasn)
+        assert np.array_equal(got[2][2], ocosts.astype(np.float32))
+    mc.autotune_reset()
