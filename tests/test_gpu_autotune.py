@@ -323,4 +323,3 @@ def test_kmeanspp_dense_update_variants_equal_oracle(mc, orc, msr, prior, d, tmp
         assert np.array_equal(got[2][1].astype(np.uint32), oasn)
         assert np.array_equal(got[2][2], ocosts.astype(np.float32))
     mc.autotune_reset()
-
