@@ -1073,6 +1073,21 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
         for (int q = 0; q < NSLOT; ++q) cj[q] = 0xffffffffu;
     }
     __syncthreads();
+    const uint64_t nchunk = (d + FIN_COLS - 1) / FIN_COLS;
+    auto stage = [&](uint64_t ci, int buf) {
+        const uint64_t k0 = ci * FIN_COLS;
+        const int kmax = int(umin64(FIN_COLS, d - k0));
+        for (int e = t; e < R * (FIN_COLS / 4); e += R) {
+            const int r = e / (FIN_COLS / 4), q4 = e % (FIN_COLS / 4);
+            const uint32_t rr = rows_s[r];
+            const bool ok = rr != 0xffffffffu && 4 * q4 < kmax;
+            const float *src = ok ? X + uint64_t(rr) * d + k0 + 4 * q4 : X;
+            cp_async16(&xs4[buf][r][4 * q4], src, ok ? 16 : 0);
+        }
+        cp_async_commit();
+    };
+    // the rows' first column chunk is in flight while the centers are staged
+    if (VEC4) stage(0, 0);
     // staged centers: subgroups sg_first .. sg_first + FIN_SG - 1
     const uint32_t sgf = sg_first;
     if (sgf != 0xffffffffu) {
@@ -1121,22 +1136,9 @@ __global__ void __launch_bounds__(FIN_ROWS) k_tc_finalize(const float *__restric
 #pragma unroll
     for (int q = 0; q < NSLOT; ++q) acc[q] = 0.f;
     if (VEC4) {
-        // d % 4 == 0: 32-column chunks (the last one may be narrower) double-buffered with
-        // cp.async, so the next chunk's rows load while this one is evaluated
-        const uint64_t nchunk = (d + FIN_COLS - 1) / FIN_COLS;
-        auto stage = [&](uint64_t ci, int buf) {
-            const uint64_t k0 = ci * FIN_COLS;
-            const int kmax = int(umin64(FIN_COLS, d - k0));
-            for (int e = t; e < R * (FIN_COLS / 4); e += R) {
-                const int r = e / (FIN_COLS / 4), q4 = e % (FIN_COLS / 4);
-                const uint32_t rr = rows_s[r];
-                const bool ok = rr != 0xffffffffu && 4 * q4 < kmax;
-                const float *src = ok ? X + uint64_t(rr) * d + k0 + 4 * q4 : X;
-                cp_async16(&xs4[buf][r][4 * q4], src, ok ? 16 : 0);
-            }
-            cp_async_commit();
-        };
-        stage(0, 0);
+        // d % 4 == 0: FIN_COLS-column chunks (the last one may be narrower) double-buffered
+        // with cp.async, so the next chunk's rows load while this one is evaluated (chunk 0 was
+        // issued before the centers were staged)
         for (uint64_t ci = 0; ci < nchunk; ++ci) {
             const int buf = int(ci & 1);
             if (ci + 1 < nchunk) {
