@@ -1028,7 +1028,7 @@ def dense_e2e(E, X, C0, precision, calls):
     t = time.perf_counter() - t0
     del Xh
     h2d = int(n * D * 4 + K * D * 4)
-    d2h = int(K * D * 4 + n * 4 + n * 8)
+    d2h = int(K * D * 4 + n * 4 + n * 4)  # centers, assignments, float32 costs
     per_iter = iters / calls
     return {"value": iters / t, "unit": "iters/s", "h2d_bytes_per_step": int(h2d / per_iter),
             "d2h_bytes_per_step": int(d2h / per_iter), "h2d_bytes_per_call": h2d, "d2h_bytes_per_call": d2h,

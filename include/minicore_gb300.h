@@ -12,6 +12,7 @@
  *                        + set_center                  centroid.h:81-112 (CSR), 137-178 (dense)
  *   mc_hcluster          perform_hard_clustering       include/minicore/clustering/solve.h:98-175
  *                        driven by cpp_pycluster_from_centers python/pycluster.h:10-63
+ *                        (mc_hcluster_f32: the costs as that binding returns them, float32)
  *   mc_sampler_*         CoresetSampler::make_sampler  include/minicore/coreset/coreset.h:386-422
  *                        make_probs_{bfl,fl,vx,lbk}, make_gmm_sampler coreset.h:340-578,
  *                        sample                        coreset.h:625-699
@@ -160,6 +161,13 @@ int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
                 double prior, const double *weights, double eps, uint64_t maxiter, uint64_t seed,
                 int precision, float *centers_out, uint32_t *asn, double *costs,
                 double *initcost, double *finalcost, uint64_t *numiter);
+/* mc_hcluster with the costs rounded to float32 on the device, as the reference's Python
+ * binding returns them (python/pycluster.h:59, vec2fnp<..., float>): half the bytes to copy
+ * back and no host-side conversion. */
+int mc_hcluster_f32(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
+                    double prior, const double *weights, double eps, uint64_t maxiter, uint64_t seed,
+                    int precision, float *centers_out, uint32_t *asn, float *costs,
+                    double *initcost, double *finalcost, uint64_t *numiter);
 
 /* Pairwise distances (python/pycmp.cpp:15-300, python/pyarrcmp.cpp:52-144), exact FP32,
  * written as float32.  Y: dense m x ncols float32.  reverse == 0: out[i][j] =
@@ -202,6 +210,7 @@ int mc_job_cost(mc_job *job, double *cost);           /* FP64 objective of curre
 int mc_job_run(mc_job *job, double eps, uint64_t maxiter, double *initcost, double *finalcost,
                uint64_t *numiter);                    /* the perform_hard_clustering loop */
 int mc_job_read(mc_job *job, float *centers, uint32_t *asn, double *costs);
+int mc_job_read_f32(mc_job *job, float *centers, uint32_t *asn, float *costs);  /* costs as float32 */
 /* Minibatch hard clustering on a job (perform_hard_minibatch_clustering,
  * clustering/solve.h:386-582): every calc_cost_freq iterations (and at the last) an
  * exhaustive assignment, restarts of the centers holding <= reseed_after rows (D^2 draws

@@ -326,9 +326,9 @@ def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxit
     w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float64)
     cout = np.empty_like(C)
     asn = np.empty(M.n, dtype=np.uint32)
-    costs = np.empty(M.n, dtype=np.float64)
     ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
     if mbsize is not None and int(mbsize) >= 0:
+        costs = np.empty(M.n, dtype=np.float64)
         # perform_hard_minibatch_clustering (python/pycluster.h:31-40): ncheckins < 0 -> 10
         nchk = int(ncheckins) if ncheckins is not None and int(ncheckins) > 0 else 10
         if cs:  # pycluster.h:36-38
@@ -343,12 +343,14 @@ def hcluster(matrix, centers, *, prior=0., msr=2, weights=None, eps=1e-10, maxit
                                                     _p(asn), _p(costs), ctypes.byref(ic), ctypes.byref(fc),
                                                     ctypes.byref(it)))
     else:
-        check(_lib.load().mc_hcluster(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(eps),
-                                      int(maxiter), _seed(seed), _PREC[precision], _p(cout), _p(asn), _p(costs),
-                                      ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
+        # the costs come back as float32, rounded on the device (python/pycluster.h:59)
+        costs = np.empty(M.n, dtype=np.float32)
+        check(_lib.load().mc_hcluster_f32(ctx.handle, M.ref, _p(C), k, _msr(msr), float(prior), _p(w), float(eps),
+                                          int(maxiter), _seed(seed), _PREC[precision], _p(cout), _p(asn), _p(costs),
+                                          ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
     centers_out = cout if M.kind == _lib.MC_DENSE_F32 else _centers_to_csr(cout)
     return {"initcost": ic.value, "finalcost": fc.value, "numiter": it.value, "centers": centers_out,
-            "costs": costs.astype(np.float32), "asn": asn}
+            "costs": costs if costs.dtype == np.float32 else costs.astype(np.float32), "asn": asn}
 
 
 def scluster(matrix, centers, msr=2, prior=0., temp=1., maxiter=1000, mbsize=-1, mbn=-1, savepref="",

@@ -56,6 +56,7 @@ SIGNATURES = {
     "mc_cmp": (I, [P, P, P, U64, I, D, I, P]),
     "mc_pcmp": (I, [P, P, I, D, P]),
     "mc_hcluster": (I, [P, P, P, U32, I, D, P, D, U64, U64, I, P, P, P, P, P, P]),
+    "mc_hcluster_f32": (I, [P, P, P, U32, I, D, P, D, U64, U64, I, P, P, P, P, P, P]),
     "mc_sampler_create": (I, [P, U64, U64, U64, P, I, P, P, I, D, ctypes.POINTER(P)]),
     "mc_sampler_from_probs": (I, [P, U64, P, P, ctypes.POINTER(P)]),
     "mc_sampler_info": (I, [P, ctypes.POINTER(U64), ctypes.POINTER(I), ctypes.POINTER(I)]),
@@ -71,6 +72,7 @@ SIGNATURES = {
     "mc_job_cost": (I, [P, ctypes.POINTER(D)]),
     "mc_job_run": (I, [P, D, U64, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(U64)]),
     "mc_job_read": (I, [P, P, P, P]),
+    "mc_job_read_f32": (I, [P, P, P, P]),
     "mc_job_minibatch": (I, [P, U64, U64, U64, U64, I, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(U64)]),
     "mc_hcluster_minibatch": (I, [P, P, P, U32, I, D, P, U64, U64, U64, U64, I, U64, I, P, P, P, ctypes.POINTER(D),
                                   ctypes.POINTER(D), ctypes.POINTER(U64)]),

@@ -212,6 +212,7 @@ struct mc_job {
     double psum = 0.0;
     DBuf<double> rowsum, w, costs, csum, consts, det_tmp, scal;
     DBuf<float> rownorm, rsi, rinc, C, Cw, CT0, CT1, cnorm;
+    DBuf<float> costs32;  // mc_job_read_f32: the costs rounded to float on the device
     DBuf<uint32_t> asn, asn2;
     DBuf<int> flag;
     DBuf<uint64_t> idxbuf;
@@ -1904,6 +1905,32 @@ int mc_job_read(mc_job *j, float *centers, uint32_t *asn, double *costs) {
     return MC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+__global__ void k_costs_to_f32(const double *__restrict__ c, uint64_t n, float *out) {
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n; i += gridDim.x * uint64_t(blockDim.x))
+        out[i] = float(c[i]);  // round to nearest, as a float32 cast of the FP64 costs
+}
+}  // namespace
+
+extern "C" {
+
+int mc_job_read_f32(mc_job *j, float *centers, uint32_t *asn, float *costs) {
+    if (!j) return fail(MC_EINVAL, "job is null");
+    MC_TRY(copy_out(centers, j->C.p, uint64_t(j->k) * j->M.d, j->st));
+    MC_TRY(copy_out(asn, j->asn.p, j->M.n, j->st));
+    if (costs && j->M.n) {
+        MC_TRY(j->costs32.alloc(j->M.n, j->st));
+        k_costs_to_f32<<<unsigned(umin64((j->M.n + 255) / 256, uint64_t(j->ctx->sms) * 8)), 256, 0, j->st>>>(
+            j->costs.p, j->M.n, j->costs32.p), note_launch();
+        MC_CUDA_TRY(cudaGetLastError());
+        MC_TRY(copy_out(costs, j->costs32.p, j->M.n, j->st));
+    }
+    MC_TRY(sync(j->st));
+    return MC_OK;
+}
+
 int mc_job_recheck_count(mc_job *j, uint64_t *count) {
     if (!j || !count) return fail(MC_EINVAL, "null argument");
     *count = j->last_recheck;
@@ -2017,6 +2044,17 @@ int mc_hcluster(mc_context *ctx, const mc_matrix *X, const float *centers_in, ui
     std::unique_ptr<mc_job> guard(j);
     MC_TRY(mc_job_run(j, eps, maxiter, initcost, finalcost, numiter));
     return mc_job_read(j, centers_out, asn, costs);
+}
+
+int mc_hcluster_f32(mc_context *ctx, const mc_matrix *X, const float *centers_in, uint32_t k, int msr,
+                    double prior, const double *weights, double eps, uint64_t maxiter, uint64_t seed, int precision,
+                    float *centers_out, uint32_t *asn, float *costs, double *initcost, double *finalcost,
+                    uint64_t *numiter) {
+    mc_job *j = nullptr;
+    MC_TRY(mc_job_create(ctx, X, centers_in, k, msr, prior, weights, precision, seed, &j));
+    std::unique_ptr<mc_job> guard(j);
+    MC_TRY(mc_job_run(j, eps, maxiter, initcost, finalcost, numiter));
+    return mc_job_read_f32(j, centers_out, asn, costs);
 }
 
 }  // extern "C"

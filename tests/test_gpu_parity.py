@@ -363,6 +363,32 @@ def test_hcluster_dense_sqrl2_bit_exact(mc, orc):
     assert res["initcost"] == ores["initcost"] and res["finalcost"] == ores["finalcost"]
 
 
+@pytest.mark.parametrize("precision,msr", [("fp32", 2), ("bf16", 2), ("fp32", 5)])
+def test_hcluster_f32_costs_equal_rounded_fp64_costs(mc, precision, msr):
+    """mc_hcluster_f32 (the entry behind the Python hcluster) returns the same centers,
+    assignments and objectives as mc_hcluster, and its costs are mc_hcluster's FP64 costs
+    rounded to float32 (numpy's cast), for dense SQRL2 in both precisions and MKL."""
+    import ctypes
+    from minicore_gb300 import _lib
+    X = _mixture(3001, 24, 7, seed=31, nonneg=msr != 2)
+    C0 = X[:7].copy()
+    M = mc._MatrixArg(X)
+    out = {}
+    for name, ctype in (("mc_hcluster", np.float64), ("mc_hcluster_f32", np.float32)):
+        cout = np.empty_like(C0)
+        asn = np.empty(M.n, np.uint32)
+        costs = np.empty(M.n, ctype)
+        ic, fc, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        _lib.check(getattr(_lib.load(), name)(mc.default_context().handle, M.ref, mc._p(C0), 7, msr, 1.0, None,
+                                              0.0, 6, 5, mc._PREC[precision], mc._p(cout), mc._p(asn),
+                                              mc._p(costs), ctypes.byref(ic), ctypes.byref(fc), ctypes.byref(it)))
+        out[name] = (cout, asn, costs, ic.value, fc.value, it.value)
+    a, b = out["mc_hcluster"], out["mc_hcluster_f32"]
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert a[3:] == b[3:]
+    assert np.array_equal(a[2].astype(np.float32), b[2])
+
+
 @pytest.mark.parametrize("msr", [0, 4, 5, 6])
 def test_hcluster_other_measures(mc, orc, msr):
     X = _mixture(2000, 20, 6, seed=20 + msr, nonneg=True)
