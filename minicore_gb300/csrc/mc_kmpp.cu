@@ -6,8 +6,10 @@
 // dist[newc] = 0.  Nothing returns to the host between rounds, so the k rounds are queued
 // back to back on one stream.
 #include "mc_kmpp.cuh"
+#include "mc_tc.cuh"
 #include "mc_tune.cuh"
 
+#include <cmath>
 #include <mutex>
 #include <unordered_map>
 
@@ -1118,8 +1120,171 @@ static int run_kmeanspp_cluster(const KmppArgs &a, const double *u_dev, cudaStre
     return MC_OK;
 }
 
+// ------------------------------------------------------------------------------------
+// Dense SQRL2 rounds screened through a BF16 copy of the rows.  A round can change row i only
+// when the new center's FP32 distance v (the sequential fmaf sum the update computes) is
+// below dist[i].  With xb = bf16(x) (round to nearest: |xb_j - x_j| <= 2^-9 |x_j|, so
+// ||xb - x|| <= 2^-9 ||x||) and A the FP32 sum of (xb_j - c_j)^2 in any order, the exact
+// squared distance S = ||x - c||^2 satisfies
+//   |Sb - S| <= 2 ||xb - x|| sqrt(S) + ||xb - x||^2,  sqrt(S) <= sqrt(Sb) + ||xb - x||,
+//   S >= Sb - 2^-8 ||x|| sqrt(Sb) - 3 2^-18 ||x||^2,
+// where Sb = ||xb - c||^2 lies in [A / (1 + g), A / (1 - g)], and v >= S (1 - g), with
+// g = (d + 2) 2^-24 / (1 - (d + 2) 2^-24) (the bound of an FP32 sum of d squared
+// differences).  k_kmpp_screen evaluates that lower bound of v in FP32 with every rounding
+// directed down (the subtracted terms up) and lists the rows where it does not exceed
+// dist[i]; k_kmpp_exact_list then runs the update's own arithmetic on those rows only.
+// Every other row keeps its distance and assignment, as the update would leave them, so the
+// results are bit-identical to the unscreened rounds, and a round reads the 2-byte copy plus
+// the listed rows' FP32 values instead of every FP32 value.
+// ------------------------------------------------------------------------------------
+struct ScreenArgs {
+    const uint4 *Xb;       // [n][d / 8] BF16 rows
+    const float *rn2;      // [n] FP32 squared row norms (sequential fmaf)
+    float norm_up;         // (1 + (d + 4) 2^-24) rounded up: covers the error of sqrt(rn2)
+    float one_m_g, one_p_2g;  // 1 - g rounded down, 1 + 2 g rounded up
+    uint32_t *list;        // rows for the exact update
+    unsigned *count;
+};
+
+// One row per thread, 128 rows per CTA: the rows' BF16 values staged in shared memory by
+// cp.async (coalesced: 16 bytes per thread and copy), each thread then sums its own row.
+template <int G>  // 16-byte groups per row: d / 8
+__global__ void __launch_bounds__(128) k_kmpp_screen(const KmppArgs a, const ScreenArgs sa) {
+    constexpr int P = G + 1;  // row pitch in 16-byte groups (4 banks apart)
+    __shared__ __align__(16) uint4 xs[128 * P];
+    __shared__ __align__(16) float cs[8 * G];
+    const uint64_t c = *a.newc;
+    const int t = threadIdx.x, lane = t & 31;
+    if (blockIdx.x == 0 && t == 0) {
+        a.center_ids[a.round] = uint32_t(c);
+        a.asn[c] = a.round;
+    }
+    const uint64_t row0 = uint64_t(blockIdx.x) * 128;
+    for (int e = t; e < 128 * G; e += 128) {
+        const int r = e / G, q = e % G;
+        const bool ok = row0 + uint64_t(r) < a.n;
+        kp_cp_async16(&xs[r * P + q], ok ? sa.Xb + (row0 + uint64_t(r)) * G + q : sa.Xb, ok ? 16 : 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    for (int j = t; j < 8 * G; j += 128) cs[j] = a.X[c * a.d + uint64_t(j)];
+    const uint64_t i = row0 + uint64_t(t);
+    // the current distance's bits (no FP64 instruction here) and the squared norm
+    const unsigned long long cb = i < a.n ? reinterpret_cast<const unsigned long long *>(a.dist)[i] : 0ull;
+    const float r2 = i < a.n ? sa.rn2[i] : 0.f;
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    __syncthreads();
+    bool need = false;
+    // the update skips rows at distance 0 or below (and NaN never compares below): in bits,
+    // zero, the sign bit, or above +inf
+    if (i < a.n) {
+        if (i == c) {
+            a.dist[i] = 0.0;
+        } else if (cb != 0ull && !(cb >> 63) && cb <= 0x7ff0000000000000ull) {
+            float A = 0.f;
+#pragma unroll
+            for (int q = 0; q < G; ++q) {
+                const uint4 w = xs[t * P + q];
+                const uint32_t u[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const float lo = __uint_as_float(u[h] << 16), hi = __uint_as_float(u[h] & 0xffff0000u);
+                    const float d0 = lo - cs[8 * q + 2 * h], d1 = hi - cs[8 * q + 2 * h + 1];
+                    A = fmaf(d0, d0, A);
+                    A = fmaf(d1, d1, A);
+                }
+            }
+            const float xn = __fmul_ru(__fsqrt_ru(r2), sa.norm_up);
+            const float t1 = __fmul_rd(A, sa.one_m_g);
+            const float t2 = __fmul_ru(__fmul_ru(xn, 0.00390625f), __fsqrt_ru(__fmul_ru(A, sa.one_p_2g)));
+            const float t3 = __fmul_ru(__fmul_ru(xn, xn), 1.1444091796875e-05f);  // 3 2^-18
+            const float slo = __fsub_rd(__fsub_rd(t1, t2), t3);
+            const float vlo = slo > 0.f ? __fmul_rd(slo, sa.one_m_g) : 0.f;
+            // vlo as a double's bits (exact for a normal float; a subnormal or zero bound
+            // counts as 0, which only lowers it), compared with the positive distance as
+            // integers
+            const uint32_t fb = __float_as_uint(vlo), fe = (fb >> 23) & 0xffu;
+            const unsigned long long vb =
+                fe == 0u ? 0ull : ((unsigned long long)(fe + 896u) << 52) | ((unsigned long long)(fb & 0x7fffffu) << 29);
+            // a non-finite bound proves nothing: the exact update decides
+            need = !(vb > cb) || !(A <= 3.402823466e+38f) || !(xn <= 3.402823466e+38f) || !(vlo <= 3.402823466e+38f);
+        }
+    }
+    const unsigned nb = __ballot_sync(0xffffffffu, need);
+    if (nb) {
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(sa.count, unsigned(__popc(nb)));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (need) sa.list[base + __popc(nb & ((1u << lane) - 1u))] = uint32_t(i);
+    }
+}
+
+// The update's arithmetic (k_kmpp_dense) on the listed rows: the sequential fmaf sum over the
+// columns, replaced only when below the current distance.
+__global__ void __launch_bounds__(256) k_kmpp_exact_list(const KmppArgs a, const uint32_t *__restrict__ list,
+                                                         const unsigned *__restrict__ count) {
+    extern __shared__ __align__(16) float csm[];  // the new center's row
+    const uint64_t c = *a.newc;
+    for (uint64_t j = threadIdx.x; j < a.d; j += blockDim.x) csm[j] = a.X[c * a.d + j];
+    __syncthreads();
+    const unsigned cnt = *count;
+    const PairScalars ps = {};
+    for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < cnt; e += gridDim.x * uint64_t(blockDim.x)) {
+        const uint64_t i = list[e];
+        const float4 *xr = reinterpret_cast<const float4 *>(a.X + i * a.d);
+        float acc = 0.f;
+        // 32 columns at a time: their eight loads in flight together (d is a multiple of 16)
+        for (uint64_t j0 = 0; j0 < a.d / 4; j0 += 8) {
+            float4 x[8];
+            const uint64_t m = a.d / 4 - j0 < 8 ? a.d / 4 - j0 : 8;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) x[u] = uint64_t(u) < m ? xr[j0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (uint64_t(u) < m) {
+                    const float *cc = csm + 4 * (j0 + u);
+                    kp_elem<SQRL2>(acc, cc[0], x[u].x, ps);
+                    kp_elem<SQRL2>(acc, cc[1], x[u].y, ps);
+                    kp_elem<SQRL2>(acc, cc[2], x[u].z, ps);
+                    kp_elem<SQRL2>(acc, cc[3], x[u].w, ps);
+                }
+            }
+        }
+        const double v = kp_cost<SQRL2>(acc);
+        if (v < a.dist[i]) {
+            a.dist[i] = v;
+            a.asn[i] = a.round;
+        }
+    }
+}
+
+// the screened rounds apply: dense SQRL2, d = 8 G with G in {2, 4, 8, 16} (a CTA's staged
+// rows within 48 KB of static shared memory), 16-byte aligned rows
+static bool kmpp_screen_ok(const KmppArgs &a) {
+    const uint64_t g = a.d / 8;
+    return !a.csr && a.msr == SQRL2 && a.d % 8 == 0 && (g == 2 || g == 4 || g == 8 || g == 16) &&
+           (reinterpret_cast<uintptr_t>(a.X) & 15) == 0;
+}
+
+static int screened_round(const KmppArgs &a, uint32_t round, const ScreenArgs &sa, int sms, cudaStream_t st) {
+    KmppArgs b = a;
+    b.round = round;
+    MC_CUDA_TRY(cudaMemsetAsync(sa.count, 0, sizeof(unsigned), st));
+    const unsigned grid = unsigned((a.n + 127) / 128);
+    switch (a.d / 8) {
+        case 2: k_kmpp_screen<2><<<grid, 128, 0, st>>>(b, sa), note_launch(); break;
+        case 4: k_kmpp_screen<4><<<grid, 128, 0, st>>>(b, sa), note_launch(); break;
+        case 8: k_kmpp_screen<8><<<grid, 128, 0, st>>>(b, sa), note_launch(); break;
+        default: k_kmpp_screen<16><<<grid, 128, 0, st>>>(b, sa), note_launch(); break;
+    }
+    // few rows are listed after the first rounds: a small grid (each CTA stages the center)
+    k_kmpp_exact_list<<<unsigned(umin64((a.n + 255) / 256, uint64_t(sms) * 2)), 256, a.d * sizeof(float), st>>>(
+        b, sa.list, sa.count), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 static int run_kmeanspp_launches(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms,
-                                 cudaStream_t st, bool prune_ok);
+                                 cudaStream_t st, bool prune_ok, bool screen_ok = false);
 
 int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms, cudaStream_t st) {
     // dense rows up to 32 chunks and 2^23 values (a cluster of 8-16 SMs reads them in well
@@ -1142,15 +1307,16 @@ int run_kmeanspp(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int
     if (!a0.csr && a0.msr == SQRL2 && a0.k > 1 && a0.n * a0.d >= (uint64_t(1) << 20)) {
         const std::string key = "kmpp_prune|w" + std::to_string(a0.w ? 1 : 0) + "|d" + tune_bucket(a0.d) + "|n" +
                                 tune_bucket(a0.n);
-        return tune_launch(key, 2, 0, st, true, [&](int v) -> int {
-            return run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, v == 1);
+        // variant 2: rounds screened through a BF16 copy of the rows (also identical results)
+        return tune_launch(key, kmpp_screen_ok(a0) ? 3 : 2, 0, st, true, [&](int v) -> int {
+            return run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, v == 1, v == 2);
         });
     }
     return run_kmeanspp_launches(a0, u_dev, chunk_tmp, sms, st, false);
 }
 
 static int run_kmeanspp_launches(const KmppArgs &a0, const double *u_dev, double *chunk_tmp, int sms,
-                                 cudaStream_t st, bool prune_ok) {
+                                 cudaStream_t st, bool prune_ok, bool screen_ok) {
     KmppArgs a = a0;
     a.cgap = nullptr;
     const unsigned tb = 256, tg = unsigned(umin64((a.d + tb - 1) / tb, 1024));
@@ -1171,9 +1337,35 @@ static int run_kmeanspp_launches(const KmppArgs &a0, const double *u_dev, double
         const double g = double(a.d + 2) * 0x1p-24;
         a.prune_g = g / (1.0 - g);
     }
+    const bool screen = screen_ok && !prune && kmpp_screen_ok(a) && a.k > 1;
+    DBuf<uint4> xb;
+    DBuf<float> rn2;
+    DBuf<uint32_t> slist;
+    DBuf<unsigned> scount;
+    ScreenArgs sa{};
+    if (screen) {
+        MC_TRY(xb.alloc(a.n * a.d / 8, st));
+        MC_TRY(rn2.alloc(a.n, st));
+        MC_TRY(slist.alloc(a.n, st));
+        MC_TRY(scount.alloc(1, st));
+        MC_TRY(launch_to_bf16_flat8(a.X, a.n * a.d / 8, xb.p, sms, st));
+        MC_TRY(launch_row_sums_dense(a.X, a.n, a.d, nullptr, rn2.p, st));
+        const double g = double(a.d + 2) * 0x1p-24 / (1.0 - double(a.d + 2) * 0x1p-24);
+        sa.Xb = xb.p;
+        sa.rn2 = rn2.p;
+        sa.norm_up = std::nextafter(float(1.0 + double(a.d + 4) * 0x1p-24), 2.0f);
+        sa.one_m_g = std::nextafter(float(1.0 - g), 0.0f);
+        sa.one_p_2g = std::nextafter(float(1.0 + 2.0 * g), 2.0f);
+        sa.list = slist.p;
+        sa.count = scount.p;
+    }
     DetInput in{a.w ? DET_F64_W : DET_F64, a.dist, nullptr, a.w, a.n};
     for (uint32_t ci = 1; ci < a.k; ++ci) {
         MC_TRY(launch_det_draw(in, chunk_tmp, u_dev + ci, 0.0, 1, a.dist, a.newc, st));
+        if (screen) {
+            MC_TRY(screened_round(a, ci, sa, sms, st));
+            continue;
+        }
         if (prune) {
             k_kmpp_center_gap<<<unsigned((ci + 7) / 8), 256, 0, st>>>(a, ci, gap.p), note_launch();
             a.cgap = gap.p;

@@ -812,6 +812,14 @@ __global__ void k_to_bf16_flat8(const float4 *__restrict__ X, uint64_t n8, uint4
     }
 }
 
+int launch_to_bf16_flat8(const float *X, uint64_t n8, void *Y, int sms, cudaStream_t st) {
+    if (n8 == 0) return MC_OK;
+    k_to_bf16_flat8<<<unsigned(umin64((n8 + 255) / 256, uint64_t(sms) * 16)), 256, 0, st>>>(
+        reinterpret_cast<const float4 *>(X), n8, reinterpret_cast<uint4 *>(Y)), note_launch();
+    MC_CUDA_TRY(cudaGetLastError());
+    return MC_OK;
+}
+
 __global__ void k_pad_f32(const float *__restrict__ X, uint64_t n, uint64_t d, uint64_t dp, float *__restrict__ Y) {
     const uint64_t total = n * dp;
     for (uint64_t e = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; e < total; e += gridDim.x * uint64_t(blockDim.x)) {

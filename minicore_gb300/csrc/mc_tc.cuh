@@ -39,5 +39,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
               uint64_t *recheck_count, bool graph_mode = false);
 // test hook: the next tensor-core pass 1 waits on a barrier nothing completes (one shot)
 void tc_stall_next();
+// BF16 copy (round to nearest) of n8 groups of eight floats: X and Y 16-byte aligned
+int launch_to_bf16_flat8(const float *X, uint64_t n8, void *Y, int sms, cudaStream_t st);
 
 }  // namespace mc

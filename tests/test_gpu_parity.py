@@ -215,15 +215,17 @@ def test_kmeanspp_dense_matches_oracle(mc, orc, msr):
 
 
 @pytest.mark.parametrize("weighted", [False, True])
-@pytest.mark.parametrize("d", [32, 61])
+@pytest.mark.parametrize("d", [32, 61, 64])
 def test_kmeanspp_dense_sqrl2_pruned_matches_oracle(mc, orc, weighted, d, tmp_path):
     """Over large dense SQRL2 matrices (beyond the persistent-cluster sizes) the rounds may
-    skip rows whose distance to the new center provably cannot beat their current one
-    (triangle inequality with FP32 rounding bounds), an autotuner choice ("kmpp_prune"
-    variant 1, forced here through a loaded decision, and variant 0 without it); ids,
-    assignments and costs stay bit-identical to the oracle, which evaluates every row.
-    Well-separated components (most rows pruned in later rounds), duplicated rows (zero
-    distances), d not a multiple of 4 (the unstaged kernel)."""
+    skip rows whose distance to the new center provably cannot beat their current one, an
+    autotuner choice ("kmpp_prune"): variant 1 by the triangle inequality with FP32 rounding
+    bounds, variant 2 (d = 8 G, G a power of two up to 32) by a lower bound from a BF16 copy
+    of the rows (the rows it cannot settle get the exact update), variant 0 neither; each is
+    forced here through a loaded decision, and ids, assignments and costs stay bit-identical
+    to the oracle, which evaluates every row.  Well-separated components (most rows settled
+    in later rounds), duplicated rows (zero distances), d not a multiple of 4 (the unstaged
+    kernel, no BF16 screen)."""
     n = 300_000 if d == 32 else 140_000
     X = _mixture(n, d, 60, seed=d, spread=20.0)
     X[1000:1200] = X[0]
@@ -234,7 +236,9 @@ def test_kmeanspp_dense_sqrl2_pruned_matches_oracle(mc, orc, weighted, d, tmp_pa
     mc.kmeanspp(X, 48, msr=2, seed=77, weights=w)   # records the decision
     keys = [k for k in mc.autotune_report()["entries"] if k.startswith("kmpp_prune|")]
     assert len(keys) == 1
-    for v in (1, 0):
+    nvar = len(mc.autotune_report()["entries"][keys[0]]["ms"])
+    assert nvar == (3 if d in (32, 64) else 2)
+    for v in range(nvar):
         mc.autotune_reset()
         path = tmp_path / f"prune{v}.tsv"
         path.write_text(f"{keys[0]}\t{v}\t\n")
