@@ -279,6 +279,24 @@ def pinned_copy(t):
     return h
 
 
+def pinned_h2d_rate(h, nbytes=1 << 29):
+    """This box's pinned host -> device copy rate (GB/s, best of two 512 MB copies, CUDA
+    events): the end-to-end calls' upload runs at it, and it varies from box to box."""
+    import torch
+    flat = h.reshape(-1).view(torch.uint8)[:nbytes]
+    dev = torch.empty(flat.shape, dtype=torch.uint8, device="cuda")
+    best = 0.0
+    for _ in range(2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        dev.copy_(flat, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, flat.numel() / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+    del dev
+    return best
+
+
 # ------------------------------------------------------------------------------------
 # accuracy against FP64 (numpy / scipy in float64)
 # ------------------------------------------------------------------------------------
@@ -1018,6 +1036,7 @@ def dense_e2e(E, X, C0, precision, calls):
     n = X.shape[0]
     Xh = pinned_copy(X)
     Ch = C0.cpu().numpy()
+    h2d_gbps = pinned_h2d_rate(Xh)
     mc.hcluster(Xh, Ch, msr=2, eps=0.0, maxiter=1, precision=precision, ctx=E.ctx)  # warm
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -1033,6 +1052,7 @@ def dense_e2e(E, X, C0, precision, calls):
     return {"value": iters / t, "unit": "iters/s", "h2d_bytes_per_step": int(h2d / per_iter),
             "d2h_bytes_per_step": int(d2h / per_iter), "h2d_bytes_per_call": h2d, "d2h_bytes_per_call": d2h,
             "iters_per_call": per_iter, "calls": calls,
+            "pinned_h2d_gbps_this_box": h2d_gbps,
             "call": f"minicore_gb300.hcluster(pinned host rows, maxiter={E2E_ITERS - 1}, eps=0, precision={precision})",
             "step": "one Lloyd iteration; copy bytes per step = per-call bytes / iterations per call"}
 
