@@ -1123,11 +1123,11 @@ static int run_kmeanspp_cluster(const KmppArgs &a, const double *u_dev, cudaStre
 // ------------------------------------------------------------------------------------
 // Dense SQRL2 rounds screened through a BF16 copy of the rows.  A round can change row i only
 // when the new center's FP32 distance v (the sequential fmaf sum the update computes) is
-// below dist[i].  With xb = bf16(x) (round to nearest: |xb_j - x_j| <= 2^-9 |x_j|, so
-// ||xb - x|| <= 2^-9 ||x||, plus 2^-130 for subnormal entries) and A the FP32 sum of
+// below dist[i].  With xb = bf16(x) (round to nearest, 8-bit significand: |xb_j - x_j| <=
+// 2^-8 |x_j|, so ||xb - x|| <= 2^-8 ||x||, plus 2^-130 for subnormal entries) and A the FP32 sum of
 // (xb_j - c_j)^2 in any order, the exact squared distance S = ||x - c||^2 satisfies
 //   |Sb - S| <= 2 ||xb - x|| sqrt(S) + ||xb - x||^2,  sqrt(S) <= sqrt(Sb) + ||xb - x||,
-//   S >= Sb - 2^-8 ||x|| sqrt(Sb) - 3 2^-18 ||x||^2 (minus the subnormal slack's terms),
+//   S >= Sb - 2^-7 ||x|| sqrt(Sb) - 3 2^-16 ||x||^2 (minus the subnormal slack's terms),
 // where Sb = ||xb - c||^2 lies in [A / (1 + g), A / (1 - g)], and v >= S (1 - g), with
 // g = (d + 2) 2^-24 / (1 - (d + 2) 2^-24) (the bound of an FP32 sum of d squared
 // differences).  k_kmpp_screen evaluates that lower bound of v in FP32 with every rounding
@@ -1195,12 +1195,12 @@ __global__ void __launch_bounds__(128) k_kmpp_screen(const KmppArgs a, const Scr
             }
             const float xn = __fmul_ru(__fsqrt_ru(r2), sa.norm_up);
             const float t1 = __fmul_rd(A, sa.one_m_g);
-            const float t2 = __fmul_ru(__fmul_ru(xn, 0.00390625f), __fsqrt_ru(__fmul_ru(A, sa.one_p_2g)));
-            const float t3 = __fmul_ru(__fmul_ru(xn, xn), 1.1444091796875e-05f);  // 3 2^-18
+            const float t2 = __fmul_ru(__fmul_ru(xn, 0x1p-7f), __fsqrt_ru(__fmul_ru(A, sa.one_p_2g)));
+            const float t3 = __fmul_ru(__fmul_ru(xn, xn), 4.57763671875e-05f);  // 3 2^-16
             // subnormal x_j round to BF16 with an absolute error up to 2^-134, so ||xb - x|| <=
-            // 2^-9 ||x|| + 2^-130 (d <= 128): the cross terms of that slack
+            // 2^-8 ||x|| + 2^-130 (d <= 128): the cross terms of that slack
             const float t4 = __fadd_ru(__fadd_ru(__fmul_ru(__fsqrt_ru(__fmul_ru(A, sa.one_p_2g)), 0x1p-129f),
-                                                 __fmul_ru(xn, 0x1p-136f)),
+                                                 __fmul_ru(xn, 0x1p-135f)),
                                        0x1p-140f);
             const float slo = __fsub_rd(__fsub_rd(__fsub_rd(t1, t2), t3), t4);
             const float vlo = slo > 0.f ? __fmul_rd(slo, sa.one_m_g) : 0.f;

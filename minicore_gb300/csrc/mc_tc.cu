@@ -6,8 +6,9 @@
 // K-major), both staged in shared memory by TMA (128-byte swizzle), accumulators in TMEM
 // (two 256-column buffers so the epilogue drains one while the MMA fills the other).
 //
-// Rounding bound.  With per-operand relative rounding u (BF16 round-to-nearest: 2^-9;
-// TF32 operands taken by truncation: 2^-10) and FP32 accumulation over d products,
+// Rounding bound.  With per-operand relative rounding u (BF16 round-to-nearest, 8-bit
+// significand: 2^-8; TF32 operands taken by truncation, 11-bit significand: 2^-10) and FP32
+// accumulation over d products,
 //   |v_j - v*_j| <= 2 eta ||x|| ||c_j||,   eta = 2u + u^2 + d 2^-22.
 // Every center whose exact distance can be the row's minimum satisfies v_j <= b1 + Delta,
 //   Delta = 4 eta ||x|| Cmax + 4 gamma_d (||x|| + Cmax)^2,
@@ -1484,9 +1485,9 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     MC_TRY(s.status.alloc(n, st));
     MC_TRY(s.key.alloc(n, st));
     const uint32_t nsg = kp / 8;  // subgroups of 8 centers
-    // compact buffer for the multi rows: all rows up to 2^20, else a quarter of them (rows
+    // compact buffer for the multi rows: all rows up to 2^20, else half of them (rows
     // beyond the capacity are rescanned exactly)
-    const uint64_t cap = n <= (1u << 20) ? n : (n / 4 > (1u << 20) ? n / 4 : (1u << 20));
+    const uint64_t cap = n <= (1u << 20) ? n : (n / 2 > (1u << 20) ? n / 2 : (1u << 20));
     const uint64_t row_u4 = apitch * esz / 16;
     MC_TRY(s.crow.alloc(cap, st));
     MC_TRY(s.thrc.alloc(cap, st));
@@ -1512,7 +1513,7 @@ int tc_assign(TcState &s, const float *X, uint64_t n, uint64_t d, const float *C
     a.rownorm = rownorm;
     a.cnp = s.cnorm_p.p;
     a.kp = kp;
-    const double u = tf32 ? 1.0 / 1024.0 : 1.0 / 512.0;
+    const double u = tf32 ? 1.0 / 1024.0 : 1.0 / 256.0;  // unit roundoff of the operands (see above)
     a.eta = float(2 * u + u * u + double(d) * std::ldexp(1.0, -22));
     const double g = double(d) * std::ldexp(1.0, -24);
     a.gamma = float(g / (1.0 - g) * 2.0);
