@@ -74,10 +74,11 @@ def test_screen_bound_never_exceeds_fp32_distance(d):
             s = 10.0 ** rng.integers(-20, 20, size=d)
             x = (rng.normal(size=d) * s).astype(np.float32)
             c = (rng.normal(size=d) * s).astype(np.float32)
-        v = _fp32_seq_dist(x, c)
-        if not np.isfinite(v):
-            continue
-        lo = _screen_bound(x, c)
+        with np.errstate(over="ignore", under="ignore"):  # FP32 overflow: such rows are skipped
+            v = _fp32_seq_dist(x, c)
+            if not np.isfinite(v):
+                continue
+            lo = _screen_bound(x, c)
         assert lo <= v, (d, trial, lo, v)
         if v > 0:
             worst = max(worst, lo / v)
